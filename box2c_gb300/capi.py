@@ -1,0 +1,221 @@
+"""ctypes mirror of the box2d C API (include/box2d/*.h) and of the scene generators.
+
+The same bindings drive any shared object that exports the box2d C API: this
+package's GPU library, and (in tests only) the plain-C oracle and the reference
+build.  Struct layouts follow include/box2d/{math_functions,id,types,inspect}.h, which
+in turn keep the layouts of the reference include/box2d headers.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+import os
+
+import numpy as np
+
+
+class Vec2(C.Structure):
+    _fields_ = [("x", C.c_float), ("y", C.c_float)]
+
+
+class Rot(C.Structure):
+    _fields_ = [("c", C.c_float), ("s", C.c_float)]
+
+
+class Transform(C.Structure):
+    _fields_ = [("p", Vec2), ("q", Rot)]
+
+
+class WorldId(C.Structure):
+    _fields_ = [("index1", C.c_uint16), ("revision", C.c_uint16)]
+
+
+class BodyId(C.Structure):
+    _fields_ = [("index1", C.c_int32), ("world0", C.c_uint16), ("revision", C.c_uint16)]
+
+
+ShapeId = BodyId
+JointId = BodyId
+
+
+class Counters(C.Structure):
+    _fields_ = [(n, C.c_int32) for n in (
+        "staticBodyCount", "bodyCount", "shapeCount", "contactCount", "jointCount",
+        "islandCount", "stackUsed", "staticTreeHeight", "treeHeight", "byteCount",
+        "taskCount")] + [("colorCounts", C.c_int32 * 12)]
+
+
+class Profile(C.Structure):
+    _fields_ = [(n, C.c_float) for n in (
+        "step", "pairs", "collide", "solve", "buildIslands", "solveConstraints",
+        "prepareTasks", "solverTasks", "prepareConstraints", "integrateVelocities",
+        "warmStart", "solveVelocities", "integratePositions", "relaxVelocities",
+        "applyRestitution", "storeImpulses", "finalizeBodies", "splitIslands",
+        "sleepIslands", "hitEvents", "broadphase", "continuous")]
+
+
+class InspectPoint(C.Structure):
+    _fields_ = [("anchorA", C.c_float * 2), ("anchorB", C.c_float * 2), ("point", C.c_float * 2),
+                ("separation", C.c_float), ("normalImpulse", C.c_float),
+                ("tangentImpulse", C.c_float), ("maxNormalImpulse", C.c_float),
+                ("normalVelocity", C.c_float), ("id", C.c_int32), ("persisted", C.c_int32)]
+
+
+class InspectContact(C.Structure):
+    _fields_ = [("contactId", C.c_int32), ("shapeIdA", C.c_int32), ("shapeIdB", C.c_int32),
+                ("colorIndex", C.c_int32), ("localIndex", C.c_int32), ("touching", C.c_int32),
+                ("pointCount", C.c_int32), ("normal", C.c_float * 2), ("friction", C.c_float),
+                ("restitution", C.c_float), ("points", InspectPoint * 2)]
+
+
+class InspectShape(C.Structure):
+    _fields_ = [("aabb", C.c_float * 4), ("fatAABB", C.c_float * 4), ("proxyKey", C.c_int32),
+                ("bodyId", C.c_int32)]
+
+
+BODY_FLOATS = 8
+
+
+def _load(path: str) -> C.CDLL:
+    # RTLD_LOCAL keeps each backend's b2* symbols private, so several backends can
+    # live in one process without interposing on one another.
+    return C.CDLL(path, mode=os.RTLD_LOCAL | os.RTLD_NOW)
+
+
+class Backend:
+    """One implementation of the box2d C API plus its scene generator library."""
+
+    def __init__(self, lib_path: str, scenes_path: str, name: str):
+        self.name = name
+        self.lib = _load(lib_path)
+        self.scenes = _load(scenes_path)
+        L, S = self.lib, self.scenes
+        L.b2World_Step.argtypes = [WorldId, C.c_float, C.c_int]
+        L.b2World_Step.restype = None
+        L.b2DestroyWorld.argtypes = [WorldId]
+        L.b2DestroyWorld.restype = None
+        L.b2World_GetCounters.argtypes = [WorldId]
+        L.b2World_GetCounters.restype = Counters
+        L.b2World_GetProfile.argtypes = [WorldId]
+        L.b2World_GetProfile.restype = Profile
+        L.b2World_InspectBodies.argtypes = [WorldId, C.c_void_p, C.c_int]
+        L.b2World_InspectBodies.restype = C.c_int
+        L.b2World_InspectShapes.argtypes = [WorldId, C.c_void_p, C.c_int]
+        L.b2World_InspectShapes.restype = C.c_int
+        L.b2World_InspectContacts.argtypes = [WorldId, C.c_void_p, C.c_int]
+        L.b2World_InspectContacts.restype = C.c_int
+        L.b2Body_GetPosition.argtypes = [BodyId]
+        L.b2Body_GetPosition.restype = Vec2
+        L.b2Body_GetRotation.argtypes = [BodyId]
+        L.b2Body_GetRotation.restype = Rot
+        L.b2Body_GetLinearVelocity.argtypes = [BodyId]
+        L.b2Body_GetLinearVelocity.restype = Vec2
+        L.b2Body_GetAngularVelocity.argtypes = [BodyId]
+        L.b2Body_GetAngularVelocity.restype = C.c_float
+        L.b2Body_SetLinearVelocity.argtypes = [BodyId, Vec2]
+        L.b2Body_SetLinearVelocity.restype = None
+        S.b2s_pyramid.argtypes = [C.c_int, C.c_float, C.c_uint64]
+        S.b2s_pyramid.restype = WorldId
+        S.b2s_tumbler.argtypes = [C.c_int, C.c_uint64, C.c_int]
+        S.b2s_tumbler.restype = WorldId
+        S.b2s_drop_boxes.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_float]
+        S.b2s_drop_boxes.restype = WorldId
+        S.b2s_hello_world.argtypes = [C.POINTER(BodyId)]
+        S.b2s_hello_world.restype = WorldId
+        S.b2s_tilted_stacks.argtypes = []
+        S.b2s_tilted_stacks.restype = WorldId
+        S.b2s_draw_ints.argtypes = [C.c_int, C.c_uint64, C.c_int, C.c_int, C.c_void_p]
+        S.b2s_draw_ints.restype = None
+        S.b2s_draw_uniform.argtypes = [C.c_int, C.c_uint64, C.c_float, C.c_float, C.c_void_p]
+        S.b2s_draw_uniform.restype = None
+        S.b2s_draw_normal.argtypes = [C.c_int, C.c_uint64, C.c_void_p]
+        S.b2s_draw_normal.restype = None
+
+    # -- scenes --------------------------------------------------------------------
+    def pyramid(self, base: int, jitter: float = 0.0, seed: int = 0) -> WorldId:
+        w = self.scenes.b2s_pyramid(base, jitter, seed)
+        if w.index1 == 0:
+            raise RuntimeError(f"{self.name}: world creation failed")
+        return w
+
+    def tumbler(self, count: int = 2000, seed: int = 1236, variant: int = 0) -> WorldId:
+        return self.scenes.b2s_tumbler(count, seed, variant)
+
+    def drop_boxes(self, heights, vx, vy, friction: float) -> WorldId:
+        h = np.ascontiguousarray(heights, np.float32)
+        a = np.ascontiguousarray(vx, np.float32)
+        b = np.ascontiguousarray(vy, np.float32)
+        return self.scenes.b2s_drop_boxes(len(h), h.ctypes.data, a.ctypes.data, b.ctypes.data, friction)
+
+    def hello_world(self):
+        body = BodyId()
+        w = self.scenes.b2s_hello_world(C.byref(body))
+        return w, body
+
+    def tilted_stacks(self) -> WorldId:
+        return self.scenes.b2s_tilted_stacks()
+
+    def draw_ints(self, n, seed, lo, hi):
+        out = np.zeros(n, np.int32)
+        self.scenes.b2s_draw_ints(n, seed, lo, hi, out.ctypes.data)
+        return out
+
+    def draw_uniform(self, n, seed, lo, hi):
+        out = np.zeros(n, np.float32)
+        self.scenes.b2s_draw_uniform(n, seed, lo, hi, out.ctypes.data)
+        return out
+
+    def draw_normal(self, n, seed):
+        out = np.zeros(n, np.float32)
+        self.scenes.b2s_draw_normal(n, seed, out.ctypes.data)
+        return out
+
+    # -- stepping and state ----------------------------------------------------------
+    def step(self, world: WorldId, dt: float = 1.0 / 60.0, substeps: int = 4, count: int = 1):
+        for _ in range(count):
+            self.lib.b2World_Step(world, dt, substeps)
+
+    def destroy(self, world: WorldId):
+        self.lib.b2DestroyWorld(world)
+
+    def counters(self, world: WorldId) -> Counters:
+        return self.lib.b2World_GetCounters(world)
+
+    def bodies(self, world: WorldId) -> np.ndarray:
+        n = self.lib.b2World_InspectBodies(world, None, 0)
+        out = np.zeros((n, BODY_FLOATS), np.float32)
+        self.lib.b2World_InspectBodies(world, out.ctypes.data, n)
+        return out
+
+    def shapes(self, world: WorldId) -> np.ndarray:
+        n = self.lib.b2World_InspectShapes(world, None, 0)
+        arr = (InspectShape * max(n, 1))()
+        self.lib.b2World_InspectShapes(world, C.addressof(arr), n)
+        return np.ctypeslib.as_array(arr)[:n].copy() if n else np.zeros(0, dtype=np.dtype(InspectShape))
+
+    def contacts(self, world: WorldId) -> np.ndarray:
+        n = self.lib.b2World_InspectContacts(world, None, 0)
+        arr = (InspectContact * max(n, 1))()
+        self.lib.b2World_InspectContacts(world, C.addressof(arr), n)
+        return np.ctypeslib.as_array(arr)[:n].copy() if n else np.zeros(0, dtype=np.dtype(InspectContact))
+
+
+def contact_table(contacts: np.ndarray) -> np.ndarray:
+    """(contactId, shapeIdA, shapeIdB, colorIndex, touching, pointCount) rows."""
+    if len(contacts) == 0:
+        return np.zeros((0, 6), np.int64)
+    return np.stack([contacts["contactId"], contacts["shapeIdA"], contacts["shapeIdB"],
+                     contacts["colorIndex"], contacts["touching"], contacts["pointCount"]], 1).astype(np.int64)
+
+
+def finite_max_rel(a: np.ndarray, b: np.ndarray, floor: float = 1.0) -> float:
+    """max |a-b| / max(|b|, floor) over finite entries."""
+    m = np.isfinite(a) & np.isfinite(b)
+    if not m.any():
+        return 0.0
+    return float(np.max(np.abs(a[m] - b[m]) / np.maximum(np.abs(b[m]), floor)))
+
+
+__all__ = ["Vec2", "Rot", "Transform", "WorldId", "BodyId", "Counters", "Profile",
+           "InspectContact", "InspectShape", "InspectPoint", "Backend", "contact_table",
+           "finite_max_rel", "BODY_FLOATS", "math"]

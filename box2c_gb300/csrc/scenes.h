@@ -1,0 +1,71 @@
+/*
+ * scenes.h -- seeded synthetic scene generators for the benchmark workloads.
+ *
+ * The generators use only the public box2d C API, so the same source is compiled
+ * against this library, against the plain-C oracle and against the reference build;
+ * each copy lives in its own shared object next to the backend it drives.  Random
+ * numbers come from PCG32 (O'Neill 2014) and float arithmetic without transcendental
+ * functions, so a seed produces bit-identical scenes on x86-64 and aarch64.
+ */
+#pragma once
+
+#include "box2d/box2d.h"
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* PCG32 stream state. */
+typedef struct b2sRandom
+{
+	uint64_t state;
+	uint64_t inc;
+} b2sRandom;
+
+void b2s_seed( b2sRandom* rng, uint64_t seed );
+uint32_t b2s_next( b2sRandom* rng );
+/* Uniform in [lo, hi). */
+float b2s_uniform( b2sRandom* rng, float lo, float hi );
+/* Zero-mean unit-variance normal approximated by the Irwin-Hall sum of 12 uniforms. */
+float b2s_normal( b2sRandom* rng );
+
+/* Default world definition of every benchmark scene: sleep off, continuous on
+ * (reference benchmark/main.c:185-186). */
+b2WorldDef b2s_world_def( void );
+
+/* Pyramid of unit boxes on a 200 m x 1 m static ground whose top face is y = 0.
+ * Row i (0-based) holds baseCount - i boxes; each box centre gets x jitter uniform in
+ * [-jitter, jitter] from `seed` (no jitter when jitter == 0).  Layout follows the
+ * reference benchmark/large_pyramid.c:34-50.  Returns the world. */
+b2WorldId b2s_pyramid( int baseCount, float jitter, uint64_t seed );
+
+/* Adds the pyramid bodies to an existing world (used to pack several into one). */
+void b2s_add_pyramid( b2WorldId worldId, int baseCount, float jitter, uint64_t seed, float xOffset );
+
+/* Motor-driven hollow box (20 x 20 m, 1 m thick walls, density 50) on a revolute joint
+ * to a shapeless static ground.  variant 0: `count` bodies alternating boxes of
+ * half-extent 0.125 and circles of radius 0.125 at seeded jittered-grid positions
+ * inside, motor 0.05*pi rad/s.  variant 1: the reference benchmark scene
+ * (benchmark/tumbler.c:8-80): a 45 x 45 grid of 0.125 boxes, motor 25 deg/s. */
+b2WorldId b2s_tumbler( int count, uint64_t seed, int variant );
+
+/* `count` boxes of half-extent 0.5 at x = 1.5 k, y = heights[k], initial velocity
+ * (vx[k], vy[k]), on the pyramid ground; every shape uses `friction`. */
+b2WorldId b2s_drop_boxes( int count, const float* heights, const float* vx, const float* vy, float friction );
+
+/* Draws `n` integers uniform in [lo, hi] from `seed` into out. */
+void b2s_draw_ints( int n, uint64_t seed, int lo, int hi, int* out );
+/* Draws `n` floats uniform in [lo, hi) / standard normal from `seed` into out. */
+void b2s_draw_uniform( int n, uint64_t seed, float lo, float hi, float* out );
+void b2s_draw_normal( int n, uint64_t seed, float* out );
+
+/* Reference unit-test scenes: test/test_world.c:17-97 (HelloWorld) and
+ * test/test_determinism.c:87-177 (10 x 10 rounded-box tilted stacks). */
+b2WorldId b2s_hello_world( b2BodyId* bodyOut );
+b2WorldId b2s_tilted_stacks( void );
+
+#ifdef __cplusplus
+}
+#endif

@@ -1,0 +1,99 @@
+/*
+ * box2d/box2d.h -- the world / body / shape / joint C API served by the GB300 backend.
+ *
+ * Each declaration has the signature of the same-named function in the reference
+ * `include/box2d/box2d.h` (line numbers cited per group).  A C program written against
+ * the reference links this library instead and keeps its source unchanged for the
+ * functions below.  b2World_Step runs the per-step contact pipeline (broadphase pairs,
+ * narrowphase manifolds, graph colouring, soft-step solver) on the GPU.
+ *
+ * Error convention (reference core.h:80-91): invalid input trips B2_ASSERT through the
+ * b2SetAssertFcn hook; create functions return a null id on failure.  Device failures
+ * never abort the process: they are reported by b2World_GetStatus (box2d/gpu.h).
+ */
+#pragma once
+
+#include "base.h"
+#include "collision.h"
+#include "id.h"
+#include "types.h"
+
+/* World (reference box2d.h:27-160) */
+B2_API b2WorldId b2CreateWorld( const b2WorldDef* def );
+B2_API void b2DestroyWorld( b2WorldId worldId );
+B2_API bool b2World_IsValid( b2WorldId id );
+B2_API void b2World_Step( b2WorldId worldId, float timeStep, int subStepCount );
+B2_API b2ContactEvents b2World_GetContactEvents( b2WorldId worldId );
+B2_API void b2World_EnableSleeping( b2WorldId worldId, bool flag );
+B2_API void b2World_EnableContinuous( b2WorldId worldId, bool flag );
+B2_API void b2World_SetRestitutionThreshold( b2WorldId worldId, float value );
+B2_API void b2World_SetHitEventThreshold( b2WorldId worldId, float value );
+B2_API void b2World_SetGravity( b2WorldId worldId, b2Vec2 gravity );
+B2_API b2Vec2 b2World_GetGravity( b2WorldId worldId );
+B2_API void b2World_SetContactTuning( b2WorldId worldId, float hertz, float dampingRatio, float pushVelocity );
+B2_API void b2World_EnableWarmStarting( b2WorldId worldId, bool flag );
+B2_API b2Profile b2World_GetProfile( b2WorldId worldId );
+B2_API b2Counters b2World_GetCounters( b2WorldId worldId );
+
+/* Body (reference box2d.h:175-405) */
+B2_API b2BodyId b2CreateBody( b2WorldId worldId, const b2BodyDef* def );
+B2_API bool b2Body_IsValid( b2BodyId id );
+B2_API b2BodyType b2Body_GetType( b2BodyId bodyId );
+B2_API void b2Body_SetUserData( b2BodyId bodyId, void* userData );
+B2_API void* b2Body_GetUserData( b2BodyId bodyId );
+B2_API b2Vec2 b2Body_GetPosition( b2BodyId bodyId );
+B2_API b2Rot b2Body_GetRotation( b2BodyId bodyId );
+B2_API b2Transform b2Body_GetTransform( b2BodyId bodyId );
+B2_API b2Vec2 b2Body_GetLocalPoint( b2BodyId bodyId, b2Vec2 worldPoint );
+B2_API b2Vec2 b2Body_GetWorldPoint( b2BodyId bodyId, b2Vec2 localPoint );
+B2_API b2Vec2 b2Body_GetLinearVelocity( b2BodyId bodyId );
+B2_API float b2Body_GetAngularVelocity( b2BodyId bodyId );
+B2_API void b2Body_SetLinearVelocity( b2BodyId bodyId, b2Vec2 linearVelocity );
+B2_API void b2Body_SetAngularVelocity( b2BodyId bodyId, float angularVelocity );
+B2_API float b2Body_GetMass( b2BodyId bodyId );
+B2_API float b2Body_GetInertiaTensor( b2BodyId bodyId );
+B2_API b2Vec2 b2Body_GetLocalCenterOfMass( b2BodyId bodyId );
+B2_API b2Vec2 b2Body_GetWorldCenterOfMass( b2BodyId bodyId );
+B2_API float b2Body_GetLinearDamping( b2BodyId bodyId );
+B2_API float b2Body_GetAngularDamping( b2BodyId bodyId );
+B2_API float b2Body_GetGravityScale( b2BodyId bodyId );
+B2_API int b2Body_GetShapeCount( b2BodyId bodyId );
+B2_API int b2Body_GetShapes( b2BodyId bodyId, b2ShapeId* shapeArray, int capacity );
+B2_API int b2Body_GetJointCount( b2BodyId bodyId );
+B2_API int b2Body_GetContactCapacity( b2BodyId bodyId );
+B2_API int b2Body_GetContactData( b2BodyId bodyId, b2ContactData* contactData, int capacity );
+
+/* Shape (reference box2d.h:423-571) */
+B2_API b2ShapeId b2CreateCircleShape( b2BodyId bodyId, const b2ShapeDef* def, const b2Circle* circle );
+B2_API b2ShapeId b2CreateSegmentShape( b2BodyId bodyId, const b2ShapeDef* def, const b2Segment* segment );
+B2_API b2ShapeId b2CreateCapsuleShape( b2BodyId bodyId, const b2ShapeDef* def, const b2Capsule* capsule );
+B2_API b2ShapeId b2CreatePolygonShape( b2BodyId bodyId, const b2ShapeDef* def, const b2Polygon* polygon );
+B2_API bool b2Shape_IsValid( b2ShapeId id );
+B2_API b2ShapeType b2Shape_GetType( b2ShapeId shapeId );
+B2_API b2BodyId b2Shape_GetBody( b2ShapeId shapeId );
+B2_API float b2Shape_GetDensity( b2ShapeId shapeId );
+B2_API void b2Shape_SetFriction( b2ShapeId shapeId, float friction );
+B2_API float b2Shape_GetFriction( b2ShapeId shapeId );
+B2_API void b2Shape_SetRestitution( b2ShapeId shapeId, float restitution );
+B2_API float b2Shape_GetRestitution( b2ShapeId shapeId );
+B2_API b2Filter b2Shape_GetFilter( b2ShapeId shapeId );
+B2_API b2Polygon b2Shape_GetPolygon( b2ShapeId shapeId );
+B2_API b2Circle b2Shape_GetCircle( b2ShapeId shapeId );
+B2_API b2AABB b2Shape_GetAABB( b2ShapeId shapeId );
+
+/* Joint (reference box2d.h:605-946); the revolute joint is the one on the step path. */
+B2_API b2JointId b2CreateRevoluteJoint( b2WorldId worldId, const b2RevoluteJointDef* def );
+B2_API bool b2Joint_IsValid( b2JointId id );
+B2_API b2JointType b2Joint_GetType( b2JointId jointId );
+B2_API b2BodyId b2Joint_GetBodyA( b2JointId jointId );
+B2_API b2BodyId b2Joint_GetBodyB( b2JointId jointId );
+B2_API void b2RevoluteJoint_EnableMotor( b2JointId jointId, bool enableMotor );
+B2_API bool b2RevoluteJoint_IsMotorEnabled( b2JointId jointId );
+B2_API void b2RevoluteJoint_SetMotorSpeed( b2JointId jointId, float motorSpeed );
+B2_API float b2RevoluteJoint_GetMotorSpeed( b2JointId jointId );
+B2_API void b2RevoluteJoint_SetMaxMotorTorque( b2JointId jointId, float torque );
+B2_API float b2RevoluteJoint_GetMaxMotorTorque( b2JointId jointId );
+B2_API float b2RevoluteJoint_GetMotorTorque( b2JointId jointId );
+B2_API void b2RevoluteJoint_EnableLimit( b2JointId jointId, bool enableLimit );
+B2_API void b2RevoluteJoint_SetLimits( b2JointId jointId, float lower, float upper );
+B2_API void b2RevoluteJoint_EnableSpring( b2JointId jointId, bool enableSpring );

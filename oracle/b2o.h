@@ -1,0 +1,364 @@
+/*
+ * b2o.h -- internal types of the plain-C oracle (a scalar CPU restatement of the
+ * reference's per-step contact pipeline).
+ *
+ * TEST INFRASTRUCTURE ONLY: tests/, the smoke check and the benchmark's CPU-baseline leg
+ * load this code as the checker; the GPU library never links it.  It restates the
+ * reference algorithms (cited per function in the .c files) with its own data layout:
+ * body, shape, contact and joint records are indexed by their stable ids, and the
+ * reference's moving arrays (constraint-graph colours, the non-touching contact array,
+ * the awake body set) are kept as arrays of ids with the same swap-remove order, because
+ * that order fixes contact ids, colours and the overflow solve order.
+ */
+#pragma once
+
+#include "b2o_math.h"
+
+#include "box2d/box2d.h"
+
+#include <stdlib.h>
+
+/* ---------------------------------------------------------------- small containers */
+typedef struct oIntArray
+{
+	int* data;
+	int count;
+	int capacity;
+} oIntArray;
+
+void oia_push( oIntArray* a, int v );
+int oia_remove_swap( oIntArray* a, int index ); /* returns the moved index or -1 */
+void oia_free( oIntArray* a );
+
+/* Open-addressing set of non-zero 64-bit keys (membership only; its iteration order is
+ * never observed, as in the reference src/table.c). */
+typedef struct oSet
+{
+	uint64_t* keys;
+	int capacity;
+	int count;
+} oSet;
+
+bool oset_add( oSet* s, uint64_t key ); /* returns true if it was already present */
+bool oset_remove( oSet* s, uint64_t key );
+bool oset_contains( const oSet* s, uint64_t key );
+void oset_clear( oSet* s );
+void oset_free( oSet* s );
+
+/* LIFO id pool (reference src/id_pool.c:21-45; a freed id is always pushed). */
+typedef struct oIdPool
+{
+	oIntArray freeIds;
+	int next;
+} oIdPool;
+
+int oid_alloc( oIdPool* p );
+void oid_free( oIdPool* p, int id );
+int oid_count( const oIdPool* p );
+
+typedef struct oBits
+{
+	uint64_t* words;
+	int wordCount;
+} oBits;
+
+bool obits_get( const oBits* b, int i );
+void obits_set( oBits* b, int i ); /* grows */
+void obits_clear( oBits* b, int i );
+void obits_free( oBits* b );
+
+/* ---------------------------------------------------------------- dynamic tree */
+typedef struct oNode
+{
+	oBox box;
+	uint32_t category;
+	int parent; /* also the free-list link */
+	int child1, child2;
+	int userData;
+	int16_t height; /* 0 leaf, -1 free */
+	bool enlarged;
+} oNode;
+
+typedef struct oTree
+{
+	oNode* nodes;
+	int root;
+	int nodeCount;
+	int capacity;
+	int freeList;
+	int proxyCount;
+	int* leafIndices;
+	oVec* leafCenters;
+	int rebuildCapacity;
+} oTree;
+
+void otree_init( oTree* t );
+void otree_free( oTree* t );
+int otree_create_proxy( oTree* t, oBox box, uint32_t category, int userData );
+void otree_destroy_proxy( oTree* t, int proxyId );
+void otree_move_proxy( oTree* t, int proxyId, oBox box );
+void otree_enlarge_proxy( oTree* t, int proxyId, oBox box );
+void otree_rebuild( oTree* t );
+int otree_height( const oTree* t );
+typedef bool oQueryFcn( int proxyId, int userData, void* ctx );
+void otree_query( const oTree* t, oBox box, uint32_t mask, oQueryFcn* fcn, void* ctx );
+
+/* ---------------------------------------------------------------- geometry */
+typedef struct oPolygon
+{
+	oVec v[8];
+	oVec n[8];
+	oVec centroid;
+	b2r radius;
+	int count;
+} oPolygon;
+
+typedef struct oCircle
+{
+	oVec center;
+	b2r radius;
+} oCircle;
+
+typedef struct oCapsule
+{
+	oVec c1, c2;
+	b2r radius;
+} oCapsule;
+
+typedef struct oSegment
+{
+	oVec p1, p2;
+} oSegment;
+
+typedef struct oMPoint
+{
+	oVec point, anchorA, anchorB;
+	b2r separation, normalImpulse, tangentImpulse, maxNormalImpulse, normalVelocity;
+	uint16_t id;
+	bool persisted;
+} oMPoint;
+
+typedef struct oManifold
+{
+	oMPoint pts[2];
+	oVec normal;
+	int count;
+} oManifold;
+
+oManifold o_collide_circles( const oCircle* a, oXf xfA, const oCircle* b, oXf xfB );
+oManifold o_collide_capsule_circle( const oCapsule* a, oXf xfA, const oCircle* b, oXf xfB );
+oManifold o_collide_polygon_circle( const oPolygon* a, oXf xfA, const oCircle* b, oXf xfB );
+oManifold o_collide_polygons( const oPolygon* a, oXf xfA, const oPolygon* b, oXf xfB );
+oPolygon o_make_capsule( oVec p1, oVec p2, b2r radius );
+
+typedef struct oSegDist
+{
+	oVec c1, c2;
+	b2r f1, f2, dist2;
+} oSegDist;
+oSegDist o_segment_distance( oVec p1, oVec q1, oVec p2, oVec q2 );
+
+/* ---------------------------------------------------------------- world records */
+typedef struct oShape
+{
+	int id; /* -1 when free */
+	int bodyId;
+	int prev, next;
+	b2ShapeType type;
+	b2r density, friction, restitution;
+	oBox aabb, fatAABB;
+	oVec localCentroid;
+	int proxyKey;
+	b2Filter filter;
+	void* userData;
+	union
+	{
+		oPolygon polygon;
+		oCircle circle;
+		oCapsule capsule;
+		oSegment segment;
+	};
+	uint16_t revision;
+	bool isSensor, enableContactEvents, enableSensorEvents, enableHitEvents, enablePreSolveEvents;
+	bool enlargedAABB, isFast;
+} oShape;
+
+typedef struct oBody
+{
+	int id; /* -1 when free */
+	b2BodyType type;
+	int awakeIndex; /* position in the awake list, -1 for static */
+	int headShape, shapeCount;
+	int headContactKey, contactCount;
+	int headJointKey, jointCount;
+	void* userData;
+	uint16_t revision;
+	bool fixedRotation, isBullet, enableSleep, isSpeedCapped, automaticMass;
+	b2r sleepThreshold, sleepTime;
+
+	/* simulation record (reference src/body.h:95-133) */
+	oXf xf;
+	oVec center, center0, localCenter, force;
+	oRot rot0;
+	b2r torque, mass, invMass, inertia, invI, minExtent, maxExtent;
+	b2r linearDamping, angularDamping, gravityScale;
+	bool isFast, simSpeedCapped, enlargeAABB;
+
+	/* solver record (reference src/body.h:76-91) */
+	oVec v, dp;
+	b2r w;
+	oRot dq;
+} oBody;
+
+enum
+{
+	OC_TOUCHING = 1,
+	OC_SENSOR = 4,
+	OC_ENABLE_SENSOR_EVENTS = 0x10,
+	OC_ENABLE_CONTACT_EVENTS = 0x20,
+
+	OS_TOUCHING = 0x10000,
+	OS_DISJOINT = 0x20000,
+	OS_STARTED = 0x40000,
+	OS_STOPPED = 0x80000,
+	OS_HIT = 0x100000,
+};
+
+typedef struct oEdge
+{
+	int bodyId, prevKey, nextKey;
+} oEdge;
+
+typedef struct oContact
+{
+	int id; /* -1 when free */
+	int colorIndex, localIndex;
+	oEdge edges[2];
+	int shapeIdA, shapeIdB;
+	uint32_t flags;
+
+	/* simulation record (reference src/contact.h:107-141) */
+	int simIndexA, simIndexB; /* body ids of awake bodies, -1 for static */
+	b2r invMassA, invIA, invMassB, invIB;
+	oManifold manifold;
+	b2r friction, restitution;
+	uint32_t simFlags;
+} oContact;
+
+typedef struct oRevolute
+{
+	oVec linearImpulse;
+	b2r springImpulse, motorImpulse, lowerImpulse, upperImpulse;
+	b2r hertz, dampingRatio, maxMotorTorque, motorSpeed, referenceAngle, lowerAngle, upperAngle;
+	int indexA, indexB;
+	oVec anchorA, anchorB, deltaCenter;
+	b2r deltaAngle, axialMass;
+	b2r springBias, springMass, springImpulseScale;
+	bool enableSpring, enableMotor, enableLimit;
+} oRevolute;
+
+typedef struct oJoint
+{
+	int id;
+	b2JointType type;
+	int bodyIdA, bodyIdB;
+	oEdge edges[2];
+	int colorIndex, localIndex;
+	oVec localAnchorA, localAnchorB;
+	b2r invMassA, invMassB, invIA, invIB;
+	oRevolute rev;
+	bool collideConnected;
+	uint16_t revision;
+	void* userData;
+} oJoint;
+
+typedef struct oSoft
+{
+	b2r biasRate, massScale, impulseScale;
+} oSoft;
+
+typedef struct oColor
+{
+	oBits bodySet;
+	oIntArray contacts; /* contact ids in colour array order */
+	oIntArray joints;
+} oColor;
+
+/* Per-constraint solver data (overflow path: reference src/contact_solver.h:11-35; the
+ * coloured path keeps the same fields per lane of the 8-wide record). */
+typedef struct oCPoint
+{
+	oVec anchorA, anchorB;
+	b2r baseSeparation, relativeVelocity, normalImpulse, tangentImpulse, maxNormalImpulse, normalMass, tangentMass;
+} oCPoint;
+
+typedef struct oConstraint
+{
+	int contactId;
+	int indexA, indexB;
+	oCPoint pts[2];
+	oVec normal;
+	b2r invMassA, invMassB, invIA, invIB, friction, restitution;
+	oSoft soft;
+	int pointCount;
+} oConstraint;
+
+typedef struct oWorld
+{
+	bool inUse;
+	uint16_t revision;
+	int slot;
+
+	oIdPool bodyIds, shapeIds, contactIds, jointIds;
+	oBody* bodies;
+	int bodyCap;
+	oShape* shapes;
+	int shapeCap;
+	oContact* contacts;
+	int contactCap;
+	oJoint* joints;
+	int jointCap;
+
+	oIntArray awake;		 /* awake body ids in solver order */
+	oIntArray staticBodies;	 /* static body ids */
+	oIntArray nonTouching;	 /* awake non-touching contact ids */
+	oColor colors[O_COLORS];
+
+	oTree trees[3];
+	oIntArray moveArray;
+	oSet moveSet;
+	oSet pairSet;
+
+	oVec gravity;
+	b2r restitutionThreshold, pushout, hitThreshold, contactHertz, contactDamping, jointHertz, jointDamping;
+	bool enableSleep, enableWarmStarting, enableContinuous, locked;
+
+	b2ContactBeginTouchEvent* beginEvents;
+	int beginCount, beginCap;
+	b2ContactEndTouchEvent* endEvents;
+	int endCount, endCap;
+
+	b2Profile profile;
+	uint64_t stepIndex;
+	b2r inv_h;
+	int unsupportedToi;
+} oWorld;
+
+oWorld* o_world( b2WorldId id );
+oWorld* o_world_index( int index );
+void o_step( oWorld* w, b2r dt, int subSteps );
+void o_update_pairs( oWorld* w );
+void o_collide( oWorld* w );
+void o_solve( oWorld* w, b2r dt, int subSteps );
+void o_create_contact( oWorld* w, oShape* a, oShape* b );
+void o_destroy_contact( oWorld* w, oContact* c );
+void o_add_contact_to_graph( oWorld* w, oContact* c );
+void o_remove_contact_from_graph( oWorld* w, int bodyIdA, int bodyIdB, int colorIndex, int localIndex );
+int o_assign_joint_color( oWorld* w, int bodyIdA, int bodyIdB, bool staticA, bool staticB );
+
+oBox o_shape_aabb( const oShape* s, oXf xf );
+void o_update_body_mass( oWorld* w, oBody* b );
+oSoft o_make_soft( b2r hertz, b2r zeta, b2r h );
+
+oVec ovf( b2Vec2 v );
+b2Vec2 vfo( oVec v );

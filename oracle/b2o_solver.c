@@ -1,0 +1,918 @@
+/*
+ * b2o_solver.c -- soft-step solver, revolute joint, body finalisation, proxy enlargement
+ * and the fast-body path of the plain-C oracle (TEST INFRASTRUCTURE).
+ *
+ * Restates the reference: step context and softness (src/world.c:717-745,
+ * src/solver.h:144-156); b2Solve stage order (src/solver.c:559-731, :1108-1668);
+ * velocity / position integration (:34-93, :146-163); finalisation (:165-351); proxy
+ * enlargement (:1741-1797); the fast-body part of continuous collision (:787-1105,
+ * :1807-1954).  Contact constraints follow src/contact_solver.c: the overflow colour
+ * uses the scalar path (:21-471) and graph colours the 8-lane path (:597-1293), whose
+ * arithmetic differs; both are restated lane by lane, including the dummy second point
+ * the 8-lane path evaluates for one-point manifolds.  The revolute joint follows
+ * src/revolute_joint.c:201-470.
+ */
+#include "b2o.h"
+
+#include <string.h>
+
+typedef struct oStep
+{
+	b2r dt, inv_dt, h, inv_h;
+	int subSteps;
+	oSoft contactSoft, staticSoft, jointSoft;
+	b2r restitutionThreshold, pushout;
+	bool enableWarmStarting;
+} oStep;
+
+oSoft o_make_soft( b2r hertz, b2r zeta, b2r h )
+{
+	oSoft s;
+	if ( hertz == R( 0 ) )
+	{
+		s.biasRate = 0;
+		s.massScale = 1;
+		s.impulseScale = 0;
+		return s;
+	}
+	b2r omega = R( 2 ) * O_PI * hertz;
+	b2r a1 = R( 2 ) * zeta + h * omega;
+	b2r a2 = h * omega * a1;
+	b2r a3 = R( 1 ) / ( R( 1 ) + a2 );
+	s.biasRate = omega / a1;
+	s.massScale = a2 * a3;
+	s.impulseScale = a3;
+	return s;
+}
+
+/* Body solver state with a detached dummy for static bodies. */
+typedef struct oState
+{
+	oVec v;
+	b2r w;
+	oVec dp;
+	oRot dq;
+} oState;
+
+static oState load_state( oWorld* w, int index )
+{
+	oState s;
+	if ( index == O_NULL )
+	{
+		s.v = ov( 0, 0 );
+		s.w = 0;
+		s.dp = ov( 0, 0 );
+		s.dq = orot( 1, 0 );
+		return s;
+	}
+	oBody* b = w->bodies + index;
+	s.v = b->v;
+	s.w = b->w;
+	s.dp = b->dp;
+	s.dq = b->dq;
+	return s;
+}
+
+static void store_velocity( oWorld* w, int index, oVec v, b2r a )
+{
+	if ( index == O_NULL )
+		return;
+	w->bodies[index].v = v;
+	w->bodies[index].w = a;
+}
+
+/* ------------------------------------------------------------ contact prepare (shared) */
+static void prepare_contact( oWorld* w, const oStep* st, oConstraint* k, oContact* c )
+{
+	const oManifold* m = &c->manifold;
+	b2r warm = st->enableWarmStarting ? R( 1 ) : R( 0 );
+	k->contactId = c->id;
+	k->indexA = c->simIndexA;
+	k->indexB = c->simIndexB;
+	k->normal = m->normal;
+	k->friction = c->friction;
+	k->restitution = c->restitution;
+	k->pointCount = m->count;
+	oState sA = load_state( w, k->indexA );
+	oState sB = load_state( w, k->indexB );
+	b2r mA = c->invMassA, iA = c->invIA, mB = c->invMassB, iB = c->invIB;
+	k->soft = ( k->indexA == O_NULL || k->indexB == O_NULL ) ? st->staticSoft : st->contactSoft;
+	k->invMassA = mA;
+	k->invIA = iA;
+	k->invMassB = mB;
+	k->invIB = iB;
+	oVec n = k->normal;
+	oVec t = oright( n );
+	memset( k->pts, 0, sizeof( k->pts ) );
+	for ( int j = 0; j < m->count; ++j )
+	{
+		const oMPoint* mp = m->pts + j;
+		oCPoint* cp = k->pts + j;
+		cp->normalImpulse = warm * mp->normalImpulse;
+		cp->tangentImpulse = warm * mp->tangentImpulse;
+		cp->maxNormalImpulse = 0;
+		oVec rA = mp->anchorA, rB = mp->anchorB;
+		cp->anchorA = rA;
+		cp->anchorB = rB;
+		cp->baseSeparation = mp->separation - odot( osub( rB, rA ), n );
+		b2r rnA = ocross( rA, n ), rnB = ocross( rB, n );
+		b2r kN = mA + mB + iA * rnA * rnA + iB * rnB * rnB;
+		cp->normalMass = kN > R( 0 ) ? R( 1 ) / kN : R( 0 );
+		b2r rtA = ocross( rA, t ), rtB = ocross( rB, t );
+		b2r kT = mA + mB + iA * rtA * rtA + iB * rtB * rtB;
+		cp->tangentMass = kT > R( 0 ) ? R( 1 ) / kT : R( 0 );
+		oVec vrA = oadd( sA.v, ocross_sv( sA.w, rA ) );
+		oVec vrB = oadd( sB.v, ocross_sv( sB.w, rB ) );
+		cp->relativeVelocity = odot( n, osub( vrB, vrA ) );
+	}
+}
+
+/* ------------------------------------------------------------ overflow (scalar) path */
+static void warm_start_overflow( oWorld* w, oConstraint* k )
+{
+	oState sA = load_state( w, k->indexA );
+	oState sB = load_state( w, k->indexB );
+	oVec vA = sA.v, vB = sB.v;
+	b2r wA = sA.w, wB = sB.w;
+	b2r mA = k->invMassA, iA = k->invIA, mB = k->invMassB, iB = k->invIB;
+	oVec n = k->normal, t = oright( n );
+	for ( int j = 0; j < k->pointCount; ++j )
+	{
+		oCPoint* cp = k->pts + j;
+		oVec P = oadd( omulsv( cp->normalImpulse, n ), omulsv( cp->tangentImpulse, t ) );
+		wA -= iA * ocross( cp->anchorA, P );
+		vA = omuladd( vA, -mA, P );
+		wB += iB * ocross( cp->anchorB, P );
+		vB = omuladd( vB, mB, P );
+	}
+	store_velocity( w, k->indexA, vA, wA );
+	store_velocity( w, k->indexB, vB, wB );
+}
+
+static void solve_overflow( oWorld* w, const oStep* st, oConstraint* k, bool useBias )
+{
+	oState sA = load_state( w, k->indexA );
+	oState sB = load_state( w, k->indexB );
+	b2r mA = k->invMassA, iA = k->invIA, mB = k->invMassB, iB = k->invIB;
+	oVec vA = sA.v, vB = sB.v;
+	b2r wA = sA.w, wB = sB.w;
+	oRot dqA = sA.dq, dqB = sB.dq;
+	oVec dp = osub( sB.dp, sA.dp );
+	oVec n = k->normal, t = oright( n );
+	b2r friction = k->friction;
+	oSoft soft = k->soft;
+	for ( int j = 0; j < k->pointCount; ++j )
+	{
+		oCPoint* cp = k->pts + j;
+		oVec ds = oadd( dp, osub( orotate( dqB, cp->anchorB ), orotate( dqA, cp->anchorA ) ) );
+		b2r s = odot( ds, n ) + cp->baseSeparation;
+		b2r velocityBias = 0, massScale = 1, impulseScale = 0;
+		if ( s > R( 0 ) )
+			velocityBias = s * st->inv_h;
+		else if ( useBias )
+		{
+			velocityBias = omax( soft.biasRate * s, -st->pushout );
+			massScale = soft.massScale;
+			impulseScale = soft.impulseScale;
+		}
+		oVec rA = cp->anchorA, rB = cp->anchorB;
+		oVec vrA = oadd( vA, ocross_sv( wA, rA ) );
+		oVec vrB = oadd( vB, ocross_sv( wB, rB ) );
+		b2r vn = odot( osub( vrB, vrA ), n );
+		b2r impulse = -cp->normalMass * massScale * ( vn + velocityBias ) - impulseScale * cp->normalImpulse;
+		b2r newImpulse = omax( cp->normalImpulse + impulse, R( 0 ) );
+		impulse = newImpulse - cp->normalImpulse;
+		cp->normalImpulse = newImpulse;
+		cp->maxNormalImpulse = omax( cp->maxNormalImpulse, impulse );
+		oVec P = omulsv( impulse, n );
+		vA = omulsub( vA, mA, P );
+		wA -= iA * ocross( rA, P );
+		vB = omuladd( vB, mB, P );
+		wB += iB * ocross( rB, P );
+	}
+	for ( int j = 0; j < k->pointCount; ++j )
+	{
+		oCPoint* cp = k->pts + j;
+		oVec rA = cp->anchorA, rB = cp->anchorB;
+		oVec vrB = oadd( vB, ocross_sv( wB, rB ) );
+		oVec vrA = oadd( vA, ocross_sv( wA, rA ) );
+		b2r vt = odot( osub( vrB, vrA ), t );
+		b2r impulse = cp->tangentMass * ( -vt );
+		b2r maxFriction = friction * cp->normalImpulse;
+		b2r newImpulse = oclamp( cp->tangentImpulse + impulse, -maxFriction, maxFriction );
+		impulse = newImpulse - cp->tangentImpulse;
+		cp->tangentImpulse = newImpulse;
+		oVec P = omulsv( impulse, t );
+		vA = omulsub( vA, mA, P );
+		wA -= iA * ocross( rA, P );
+		vB = omuladd( vB, mB, P );
+		wB += iB * ocross( rB, P );
+	}
+	store_velocity( w, k->indexA, vA, wA );
+	store_velocity( w, k->indexB, vB, wB );
+}
+
+static void restitution_overflow( oWorld* w, const oStep* st, oConstraint* k )
+{
+	if ( k->restitution == R( 0 ) )
+		return;
+	oState sA = load_state( w, k->indexA );
+	oState sB = load_state( w, k->indexB );
+	b2r mA = k->invMassA, iA = k->invIA, mB = k->invMassB, iB = k->invIB;
+	oVec vA = sA.v, vB = sB.v;
+	b2r wA = sA.w, wB = sB.w;
+	oVec n = k->normal;
+	for ( int j = 0; j < k->pointCount; ++j )
+	{
+		oCPoint* cp = k->pts + j;
+		if ( cp->relativeVelocity > -st->restitutionThreshold || cp->maxNormalImpulse == R( 0 ) )
+			continue;
+		oVec rA = cp->anchorA, rB = cp->anchorB;
+		oVec vrB = oadd( vB, ocross_sv( wB, rB ) );
+		oVec vrA = oadd( vA, ocross_sv( wA, rA ) );
+		b2r vn = odot( osub( vrB, vrA ), n );
+		b2r impulse = -cp->normalMass * ( vn + k->restitution * cp->relativeVelocity );
+		b2r newImpulse = omax( cp->normalImpulse + impulse, R( 0 ) );
+		impulse = newImpulse - cp->normalImpulse;
+		cp->normalImpulse = newImpulse;
+		cp->maxNormalImpulse = omax( cp->maxNormalImpulse, impulse );
+		oVec P = omulsv( impulse, n );
+		vA = omulsub( vA, mA, P );
+		wA -= iA * ocross( rA, P );
+		vB = omuladd( vB, mB, P );
+		wB += iB * ocross( rB, P );
+	}
+	store_velocity( w, k->indexA, vA, wA );
+	store_velocity( w, k->indexB, vB, wB );
+}
+
+/* ------------------------------------------------------------ graph-colour (8-lane) path */
+/* One lane of the 8-wide record: both point slots are always evaluated; a one-point
+ * manifold carries zeros in slot 1 exactly like the reference remainder data. */
+static void apply_impulse_lane( oVec* vA, b2r* wA, oVec* vB, b2r* wB, const oConstraint* k, oVec rA, oVec rB, b2r Px, b2r Py )
+{
+	vA->x = vA->x - k->invMassA * Px;
+	vA->y = vA->y - k->invMassA * Py;
+	*wA = *wA - k->invIA * ( rA.x * Py - rA.y * Px );
+	vB->x = vB->x + k->invMassB * Px;
+	vB->y = vB->y + k->invMassB * Py;
+	*wB = *wB + k->invIB * ( rB.x * Py - rB.y * Px );
+}
+
+static void warm_start_lane( oWorld* w, oConstraint* k )
+{
+	oState sA = load_state( w, k->indexA );
+	oState sB = load_state( w, k->indexB );
+	b2r tX = k->normal.y;
+	b2r tY = R( 0 ) - k->normal.x;
+	for ( int j = 0; j < 2; ++j )
+	{
+		oCPoint* cp = k->pts + j;
+		oVec rA = cp->anchorA, rB = cp->anchorB;
+		b2r Px = cp->normalImpulse * k->normal.x + cp->tangentImpulse * tX;
+		b2r Py = cp->normalImpulse * k->normal.y + cp->tangentImpulse * tY;
+		sA.w = sA.w - k->invIA * ( rA.x * Py - rA.y * Px );
+		sA.v.x = sA.v.x - k->invMassA * Px;
+		sA.v.y = sA.v.y - k->invMassA * Py;
+		sB.w = sB.w + k->invIB * ( rB.x * Py - rB.y * Px );
+		sB.v.x = sB.v.x + k->invMassB * Px;
+		sB.v.y = sB.v.y + k->invMassB * Py;
+	}
+	store_velocity( w, k->indexA, sA.v, sA.w );
+	store_velocity( w, k->indexB, sB.v, sB.w );
+}
+
+static void solve_lane( oWorld* w, const oStep* st, oConstraint* k, bool useBias )
+{
+	oState sA = load_state( w, k->indexA );
+	oState sB = load_state( w, k->indexB );
+	b2r biasRate = useBias ? k->soft.biasRate : R( 0 );
+	b2r massScale = useBias ? k->soft.massScale : R( 1 );
+	b2r impulseScale = useBias ? k->soft.impulseScale : R( 0 );
+	b2r minBias = -st->pushout;
+	oVec dp = ov( sB.dp.x - sA.dp.x, sB.dp.y - sA.dp.y );
+	oVec n = k->normal;
+	for ( int j = 0; j < 2; ++j )
+	{
+		oCPoint* cp = k->pts + j;
+		oVec rsA = ov( sA.dq.c * cp->anchorA.x - sA.dq.s * cp->anchorA.y, sA.dq.s * cp->anchorA.x + sA.dq.c * cp->anchorA.y );
+		oVec rsB = ov( sB.dq.c * cp->anchorB.x - sB.dq.s * cp->anchorB.y, sB.dq.s * cp->anchorB.x + sB.dq.c * cp->anchorB.y );
+		oVec ds = ov( dp.x + ( rsB.x - rsA.x ), dp.y + ( rsB.y - rsA.y ) );
+		b2r s = ( n.x * ds.x + n.y * ds.y ) + cp->baseSeparation;
+		b2r specBias = s * st->inv_h;
+		b2r softBias = omax( biasRate * s, minBias );
+		b2r bias = s > R( 0 ) ? specBias : softBias;
+		oVec rA = cp->anchorA, rB = cp->anchorB;
+		b2r dvx = ( sB.v.x - sB.w * rB.y ) - ( sA.v.x - sA.w * rA.y );
+		b2r dvy = ( sB.v.y + sB.w * rB.x ) - ( sA.v.y + sA.w * rA.x );
+		b2r vn = dvx * n.x + dvy * n.y;
+		b2r negImpulse = cp->normalMass * ( massScale * ( vn + bias ) ) + impulseScale * cp->normalImpulse;
+		b2r newImpulse = omax( cp->normalImpulse - negImpulse, R( 0 ) );
+		b2r impulse = newImpulse - cp->normalImpulse;
+		cp->normalImpulse = newImpulse;
+		cp->maxNormalImpulse = omax( cp->maxNormalImpulse, newImpulse );
+		apply_impulse_lane( &sA.v, &sA.w, &sB.v, &sB.w, k, rA, rB, impulse * n.x, impulse * n.y );
+	}
+	b2r tX = n.y;
+	b2r tY = R( 0 ) - n.x;
+	for ( int j = 0; j < 2; ++j )
+	{
+		oCPoint* cp = k->pts + j;
+		oVec rA = cp->anchorA, rB = cp->anchorB;
+		b2r dvx = ( sB.v.x - sB.w * rB.y ) - ( sA.v.x - sA.w * rA.y );
+		b2r dvy = ( sB.v.y + sB.w * rB.x ) - ( sA.v.y + sA.w * rA.x );
+		b2r vt = dvx * tX + dvy * tY;
+		b2r negImpulse = cp->tangentMass * vt;
+		b2r maxFriction = k->friction * cp->normalImpulse;
+		b2r newImpulse = cp->tangentImpulse - negImpulse;
+		b2r lo = R( 0 ) - maxFriction;
+		b2r mn = newImpulse < maxFriction ? newImpulse : maxFriction;
+		newImpulse = lo > mn ? lo : mn;
+		b2r impulse = newImpulse - cp->tangentImpulse;
+		cp->tangentImpulse = newImpulse;
+		apply_impulse_lane( &sA.v, &sA.w, &sB.v, &sB.w, k, rA, rB, impulse * tX, impulse * tY );
+	}
+	store_velocity( w, k->indexA, sA.v, sA.w );
+	store_velocity( w, k->indexB, sB.v, sB.w );
+}
+
+static void restitution_lane( oWorld* w, const oStep* st, oConstraint* k )
+{
+	oState sA = load_state( w, k->indexA );
+	oState sB = load_state( w, k->indexB );
+	oVec n = k->normal;
+	for ( int j = 0; j < 2; ++j )
+	{
+		oCPoint* cp = k->pts + j;
+		bool skip = ( cp->relativeVelocity + st->restitutionThreshold > R( 0 ) ) || ( cp->maxNormalImpulse == R( 0 ) );
+		b2r mass = skip ? R( 0 ) : cp->normalMass;
+		oVec rA = cp->anchorA, rB = cp->anchorB;
+		b2r dvx = ( sB.v.x - sB.w * rB.y ) - ( sA.v.x - sA.w * rA.y );
+		b2r dvy = ( sB.v.y + sB.w * rB.x ) - ( sA.v.y + sA.w * rA.x );
+		b2r vn = dvx * n.x + dvy * n.y;
+		b2r negImpulse = mass * ( vn + k->restitution * cp->relativeVelocity );
+		b2r newImpulse = omax( cp->normalImpulse - negImpulse, R( 0 ) );
+		b2r impulse = newImpulse - cp->normalImpulse;
+		cp->normalImpulse = newImpulse;
+		apply_impulse_lane( &sA.v, &sA.w, &sB.v, &sB.w, k, rA, rB, impulse * n.x, impulse * n.y );
+	}
+	store_velocity( w, k->indexA, sA.v, sA.w );
+	store_velocity( w, k->indexB, sB.v, sB.w );
+}
+
+/* ------------------------------------------------------------ revolute joint */
+static void prepare_revolute( oWorld* w, const oStep* st, oJoint* j )
+{
+	oBody* a = w->bodies + j->bodyIdA;
+	oBody* b = w->bodies + j->bodyIdB;
+	j->invMassA = a->invMass;
+	j->invMassB = b->invMass;
+	j->invIA = a->invI;
+	j->invIB = b->invI;
+	oRevolute* r = &j->rev;
+	r->indexA = a->awakeIndex != O_NULL ? a->id : O_NULL;
+	r->indexB = b->awakeIndex != O_NULL ? b->id : O_NULL;
+	r->anchorA = orotate( a->xf.q, osub( j->localAnchorA, a->localCenter ) );
+	r->anchorB = orotate( b->xf.q, osub( j->localAnchorB, b->localCenter ) );
+	r->deltaCenter = osub( b->center, a->center );
+	r->deltaAngle = orelangle( b->xf.q, a->xf.q ) - r->referenceAngle;
+	r->deltaAngle = ounwind( r->deltaAngle );
+	b2r k = j->invIA + j->invIB;
+	r->axialMass = k > R( 0 ) ? R( 1 ) / k : R( 0 );
+	oSoft s = o_make_soft( r->hertz, r->dampingRatio, st->h );
+	r->springBias = s.biasRate;
+	r->springMass = s.massScale;
+	r->springImpulseScale = s.impulseScale;
+	if ( st->enableWarmStarting == false )
+	{
+		r->linearImpulse = ov( 0, 0 );
+		r->springImpulse = 0;
+		r->motorImpulse = 0;
+		r->lowerImpulse = 0;
+		r->upperImpulse = 0;
+	}
+}
+
+static void warm_start_revolute( oWorld* w, oJoint* j )
+{
+	oRevolute* r = &j->rev;
+	oState sA = load_state( w, r->indexA );
+	oState sB = load_state( w, r->indexB );
+	oVec rA = orotate( sA.dq, r->anchorA );
+	oVec rB = orotate( sB.dq, r->anchorB );
+	b2r axial = r->springImpulse + r->motorImpulse + r->lowerImpulse - r->upperImpulse;
+	sA.v = omulsub( sA.v, j->invMassA, r->linearImpulse );
+	sA.w -= j->invIA * ( ocross( rA, r->linearImpulse ) + axial );
+	sB.v = omuladd( sB.v, j->invMassB, r->linearImpulse );
+	sB.w += j->invIB * ( ocross( rB, r->linearImpulse ) + axial );
+	store_velocity( w, r->indexA, sA.v, sA.w );
+	store_velocity( w, r->indexB, sB.v, sB.w );
+}
+
+static void solve_revolute( oWorld* w, const oStep* st, oJoint* j, bool useBias )
+{
+	oRevolute* r = &j->rev;
+	b2r mA = j->invMassA, mB = j->invMassB, iA = j->invIA, iB = j->invIB;
+	oState sA = load_state( w, r->indexA );
+	oState sB = load_state( w, r->indexB );
+	oVec vA = sA.v, vB = sB.v;
+	b2r wA = sA.w, wB = sB.w;
+	bool fixedRotation = ( iA + iB == R( 0 ) );
+
+	if ( r->enableSpring && fixedRotation == false )
+	{
+		b2r C = orelangle( sB.dq, sA.dq ) + r->deltaAngle;
+		b2r bias = r->springBias * C;
+		b2r Cdot = wB - wA;
+		b2r impulse = -r->springMass * r->axialMass * ( Cdot + bias ) - r->springImpulseScale * r->springImpulse;
+		r->springImpulse += impulse;
+		wA -= iA * impulse;
+		wB += iB * impulse;
+	}
+	if ( r->enableMotor && fixedRotation == false )
+	{
+		b2r Cdot = wB - wA - r->motorSpeed;
+		b2r impulse = -r->axialMass * Cdot;
+		b2r old = r->motorImpulse;
+		b2r maxImpulse = st->h * r->maxMotorTorque;
+		r->motorImpulse = oclamp( r->motorImpulse + impulse, -maxImpulse, maxImpulse );
+		impulse = r->motorImpulse - old;
+		wA -= iA * impulse;
+		wB += iB * impulse;
+	}
+	if ( r->enableLimit && fixedRotation == false )
+	{
+		b2r angle = orelangle( sB.dq, sA.dq ) + r->deltaAngle;
+		angle = ounwind( angle );
+		{
+			b2r C = angle - r->lowerAngle;
+			b2r bias = 0, massScale = 1, impulseScale = 0;
+			if ( C > R( 0 ) )
+				bias = C * st->inv_h;
+			else if ( useBias )
+			{
+				bias = st->jointSoft.biasRate * C;
+				massScale = st->jointSoft.massScale;
+				impulseScale = st->jointSoft.impulseScale;
+			}
+			b2r Cdot = wB - wA;
+			b2r impulse = -massScale * r->axialMass * ( Cdot + bias ) - impulseScale * r->lowerImpulse;
+			b2r old = r->lowerImpulse;
+			r->lowerImpulse = omax( r->lowerImpulse + impulse, R( 0 ) );
+			impulse = r->lowerImpulse - old;
+			wA -= iA * impulse;
+			wB += iB * impulse;
+		}
+		{
+			b2r C = r->upperAngle - angle;
+			b2r bias = 0, massScale = 1, impulseScale = 0;
+			if ( C > R( 0 ) )
+				bias = C * st->inv_h;
+			else if ( useBias )
+			{
+				bias = st->jointSoft.biasRate * C;
+				massScale = st->jointSoft.massScale;
+				impulseScale = st->jointSoft.impulseScale;
+			}
+			b2r Cdot = wA - wB;
+			/* the reference scales the upper-limit term by lowerImpulse (revolute_joint.c:409) */
+			b2r impulse = -massScale * r->axialMass * ( Cdot + bias ) - impulseScale * r->lowerImpulse;
+			b2r old = r->upperImpulse;
+			r->upperImpulse = omax( r->upperImpulse + impulse, R( 0 ) );
+			impulse = r->upperImpulse - old;
+			wA += iA * impulse;
+			wB -= iB * impulse;
+		}
+	}
+	{
+		oVec rA = orotate( sA.dq, r->anchorA );
+		oVec rB = orotate( sB.dq, r->anchorB );
+		oVec Cdot = osub( oadd( vB, ocross_sv( wB, rB ) ), oadd( vA, ocross_sv( wA, rA ) ) );
+		oVec bias = ov( 0, 0 );
+		b2r massScale = 1, impulseScale = 0;
+		if ( useBias )
+		{
+			oVec sep = oadd( oadd( osub( sB.dp, sA.dp ), osub( rB, rA ) ), r->deltaCenter );
+			bias = omulsv( st->jointSoft.biasRate, sep );
+			massScale = st->jointSoft.massScale;
+			impulseScale = st->jointSoft.impulseScale;
+		}
+		b2r k11 = mA + mB + rA.y * rA.y * iA + rB.y * rB.y * iB;
+		b2r k12 = -rA.y * rA.x * iA - rB.y * rB.x * iB;
+		b2r k22 = mA + mB + rA.x * rA.x * iA + rB.x * rB.x * iB;
+		oVec rhs = oadd( Cdot, bias );
+		b2r det = k11 * k22 - k12 * k12;
+		if ( det != R( 0 ) )
+			det = R( 1 ) / det;
+		oVec bb = ov( det * ( k22 * rhs.x - k12 * rhs.y ), det * ( k11 * rhs.y - k12 * rhs.x ) );
+		oVec impulse;
+		impulse.x = -massScale * bb.x - impulseScale * r->linearImpulse.x;
+		impulse.y = -massScale * bb.y - impulseScale * r->linearImpulse.y;
+		r->linearImpulse.x += impulse.x;
+		r->linearImpulse.y += impulse.y;
+		vA = omulsub( vA, mA, impulse );
+		wA -= iA * ocross( rA, impulse );
+		vB = omuladd( vB, mB, impulse );
+		wB += iB * ocross( rB, impulse );
+	}
+	store_velocity( w, r->indexA, vA, wA );
+	store_velocity( w, r->indexB, vB, wB );
+}
+
+/* ------------------------------------------------------------ bodies */
+static void integrate_velocities( oWorld* w, const oStep* st )
+{
+	oVec g = w->gravity;
+	b2r h = st->h;
+	b2r maxLin = O_MAX_TRANSLATION * st->inv_dt;
+	b2r maxAng = O_MAX_ROTATION * st->inv_dt;
+	b2r maxLin2 = maxLin * maxLin, maxAng2 = maxAng * maxAng;
+	for ( int i = 0; i < w->awake.count; ++i )
+	{
+		oBody* b = w->bodies + w->awake.data[i];
+		oVec v = b->v;
+		b2r a = b->w;
+		b2r ld = R( 1 ) / ( R( 1 ) + h * b->linearDamping );
+		b2r ad = R( 1 ) / ( R( 1 ) + h * b->angularDamping );
+		oVec lvd = omulsv( h * b->invMass, omuladd( b->force, b->mass * b->gravityScale, g ) );
+		b2r avd = h * b->invI * b->torque;
+		v = omuladd( lvd, ld, v );
+		a = avd + ad * a;
+		if ( odot( v, v ) > maxLin2 )
+		{
+			b2r ratio = maxLin / olen( v );
+			v = omulsv( ratio, v );
+			b->simSpeedCapped = true;
+		}
+		if ( a * a > maxAng2 )
+		{
+			b2r ratio = maxAng / oabs( a );
+			a *= ratio;
+			b->simSpeedCapped = true;
+		}
+		b->v = v;
+		b->w = a;
+	}
+}
+
+static void integrate_positions( oWorld* w, const oStep* st )
+{
+	for ( int i = 0; i < w->awake.count; ++i )
+	{
+		oBody* b = w->bodies + w->awake.data[i];
+		b->dq = ointrot( b->dq, st->h * b->w );
+		b->dp = omuladd( b->dp, st->h, b->v );
+	}
+}
+
+typedef struct oFinalize
+{
+	uint8_t* enlarged; /* by awake index */
+	int* fast;
+	int fastCount;
+} oFinalize;
+
+static void finalize_bodies( oWorld* w, const oStep* st, oFinalize* f )
+{
+	for ( int i = 0; i < w->awake.count; ++i )
+	{
+		oBody* b = w->bodies + w->awake.data[i];
+		oVec v = b->v;
+		b2r a = b->w;
+		b->center = oadd( b->center, b->dp );
+		b->xf.q = onormrot( omulrot( b->dq, b->xf.q ) );
+		b2r maxVelocity = olen( v ) + oabs( a ) * b->maxExtent;
+		b2r maxDeltaPosition = olen( b->dp ) + oabs( b->dq.s ) * b->maxExtent;
+		b2r sleepVelocity = omax( maxVelocity, R( 0.5f ) * st->inv_dt * maxDeltaPosition );
+		b->dp = ov( 0, 0 );
+		b->dq = orot( 1, 0 );
+		b->xf.p = osub( b->center, orotate( b->xf.q, b->localCenter ) );
+		b->force = ov( 0, 0 );
+		b->torque = 0;
+		b->isSpeedCapped = b->simSpeedCapped;
+		b->simSpeedCapped = false;
+		b->isFast = false;
+		if ( w->enableSleep == false || b->enableSleep == false || sleepVelocity > b->sleepThreshold )
+		{
+			b->sleepTime = 0;
+			if ( b->type == b2_dynamicBody && w->enableContinuous && maxVelocity * st->dt > R( 0.5f ) * b->minExtent )
+			{
+				f->fast[f->fastCount++] = b->id;
+				b->isFast = true;
+			}
+			else
+			{
+				b->center0 = b->center;
+				b->rot0 = b->xf.q;
+			}
+		}
+		else
+		{
+			b->center0 = b->center;
+			b->rot0 = b->xf.q;
+			b->sleepTime += st->dt;
+		}
+		for ( int sid = b->headShape; sid != O_NULL; sid = w->shapes[sid].next )
+		{
+			oShape* s = w->shapes + sid;
+			if ( b->isFast )
+			{
+				s->isFast = true;
+				f->enlarged[i] = 1;
+			}
+			else
+			{
+				oBox aabb = o_shape_aabb( s, b->xf );
+				aabb.lo.x -= O_SPECULATIVE;
+				aabb.lo.y -= O_SPECULATIVE;
+				aabb.hi.x += O_SPECULATIVE;
+				aabb.hi.y += O_SPECULATIVE;
+				s->aabb = aabb;
+				if ( obox_contains( s->fatAABB, aabb ) == false )
+				{
+					s->fatAABB.lo.x = aabb.lo.x - O_AABB_MARGIN;
+					s->fatAABB.lo.y = aabb.lo.y - O_AABB_MARGIN;
+					s->fatAABB.hi.x = aabb.hi.x + O_AABB_MARGIN;
+					s->fatAABB.hi.y = aabb.hi.y + O_AABB_MARGIN;
+					s->enlargedAABB = true;
+					f->enlarged[i] = 1;
+				}
+			}
+		}
+	}
+}
+
+static void buffer_move( oWorld* w, int proxyKey )
+{
+	if ( oset_add( &w->moveSet, (uint64_t)( proxyKey + 1 ) ) == false )
+		oia_push( &w->moveArray, proxyKey );
+}
+
+/* Candidate filter of the static-tree sweep (reference src/solver.c:800-858).  Time of
+ * impact itself is not restated: a sweep that reaches it is counted and treated as no
+ * hit, and the tests assert that the count stays zero on the scenes they compare. */
+typedef struct oSweepCtx
+{
+	oWorld* w;
+	oShape* fast;
+	oBody* fastBody;
+	int hits;
+} oSweepCtx;
+
+static bool sweep_query( int proxyId, int shapeId, void* context )
+{
+	(void)proxyId;
+	oSweepCtx* q = (oSweepCtx*)context;
+	oWorld* w = q->w;
+	if ( shapeId == q->fast->id )
+		return true;
+	oShape* s = w->shapes + shapeId;
+	if ( s->bodyId == q->fast->bodyId )
+		return true;
+	b2Filter fa = q->fast->filter, fb = s->filter;
+	if ( fa.groupIndex == fb.groupIndex && fa.groupIndex != 0 )
+	{
+		if ( fa.groupIndex <= 0 )
+			return true;
+	}
+	else if ( ( fa.maskBits & fb.categoryBits ) == 0 || ( fa.categoryBits & fb.maskBits ) == 0 )
+		return true;
+	if ( s->isSensor )
+		return true;
+	oBody* body = w->bodies + s->bodyId;
+	if ( body->isBullet )
+		return true;
+	q->hits += 1;
+	return true;
+}
+
+static void solve_continuous( oWorld* w, oBody* b )
+{
+	oXf xf2 = b->xf;
+	oSweepCtx q = { w, NULL, b, 0 };
+	for ( int sid = b->headShape; sid != O_NULL; sid = w->shapes[sid].next )
+	{
+		oShape* s = w->shapes + sid;
+		s->isFast = false;
+		oBox box1 = s->aabb;
+		oBox box2 = o_shape_aabb( s, xf2 );
+		oBox box = obox_union( box1, box2 );
+		s->aabb = box2;
+		if ( s->isSensor )
+			continue;
+		q.fast = s;
+		otree_query( w->trees + b2_staticBody, box, 0xFFFFFFFFu, sweep_query, &q );
+		if ( b->isBullet )
+		{
+			otree_query( w->trees + b2_kinematicBody, box, 0xFFFFFFFFu, sweep_query, &q );
+			otree_query( w->trees + b2_dynamicBody, box, 0xFFFFFFFFu, sweep_query, &q );
+		}
+	}
+	w->unsupportedToi += q.hits;
+	b->rot0 = b->xf.q;
+	b->center0 = b->center;
+	for ( int sid = b->headShape; sid != O_NULL; sid = w->shapes[sid].next )
+	{
+		oShape* s = w->shapes + sid;
+		if ( obox_contains( s->fatAABB, s->aabb ) == false )
+		{
+			s->fatAABB.lo.x = s->aabb.lo.x - O_AABB_MARGIN;
+			s->fatAABB.lo.y = s->aabb.lo.y - O_AABB_MARGIN;
+			s->fatAABB.hi.x = s->aabb.hi.x + O_AABB_MARGIN;
+			s->fatAABB.hi.y = s->aabb.hi.y + O_AABB_MARGIN;
+			s->enlargedAABB = true;
+			b->enlargeAABB = true;
+		}
+	}
+}
+
+/* ------------------------------------------------------------ solve */
+void o_solve( oWorld* w, b2r dt, int subSteps )
+{
+	(void)dt;
+	oStep st;
+	st.subSteps = subSteps < 1 ? 1 : subSteps;
+	st.dt = dt;
+	st.inv_dt = R( 1 ) / dt;
+	st.h = dt / (b2r)st.subSteps;
+	st.inv_h = (b2r)st.subSteps * st.inv_dt;
+	b2r contactHertz = omin( w->contactHertz, R( 0.25f ) * st.inv_h );
+	b2r jointHertz = omin( w->jointHertz, R( 0.125f ) * st.inv_h );
+	st.contactSoft = o_make_soft( contactHertz, w->contactDamping, st.h );
+	st.staticSoft = o_make_soft( R( 2 ) * contactHertz, w->contactDamping, st.h );
+	st.jointSoft = o_make_soft( jointHertz, w->jointDamping, st.h );
+	st.restitutionThreshold = w->restitutionThreshold;
+	st.pushout = w->pushout;
+	st.enableWarmStarting = w->enableWarmStarting;
+
+	w->stepIndex += 1;
+	w->inv_h = st.inv_h;
+	int awakeCount = w->awake.count;
+	if ( awakeCount == 0 )
+		return;
+
+	/* active colours 0..10 in order, then the overflow colour */
+	int active[O_COLORS];
+	int activeCount = 0;
+	for ( int i = 0; i < O_OVERFLOW; ++i )
+		if ( w->colors[i].contacts.count + w->colors[i].joints.count > 0 )
+			active[activeCount++] = i;
+
+	int totalContacts = 0;
+	for ( int i = 0; i < O_COLORS; ++i )
+		totalContacts += w->colors[i].contacts.count;
+	oConstraint* cons = (oConstraint*)malloc( sizeof( oConstraint ) * (size_t)( totalContacts + 1 ) );
+	int colorStart[O_COLORS + 1];
+	{
+		int n = 0;
+		for ( int i = 0; i < O_COLORS; ++i )
+		{
+			colorStart[i] = n;
+			oIntArray* a = &w->colors[i].contacts;
+			for ( int k = 0; k < a->count; ++k )
+				prepare_contact( w, &st, cons + n++, w->contacts + a->data[k] );
+		}
+		colorStart[O_COLORS] = n;
+	}
+	for ( int c = 0; c < O_COLORS; ++c )
+	{
+		oIntArray* j = &w->colors[c].joints;
+		for ( int k = 0; k < j->count; ++k )
+			prepare_revolute( w, &st, w->joints + j->data[k] );
+	}
+
+	oColor* overflow = w->colors + O_OVERFLOW;
+	oConstraint* ocons = cons + colorStart[O_OVERFLOW];
+	int ocount = overflow->contacts.count;
+
+	for ( int sub = 0; sub < st.subSteps; ++sub )
+	{
+		integrate_velocities( w, &st );
+
+		for ( int k = 0; k < overflow->joints.count; ++k )
+			warm_start_revolute( w, w->joints + overflow->joints.data[k] );
+		for ( int k = 0; k < ocount; ++k )
+			warm_start_overflow( w, ocons + k );
+		if ( st.enableWarmStarting )
+		{
+			for ( int a = 0; a < activeCount; ++a )
+			{
+				int c = active[a];
+				for ( int k = 0; k < w->colors[c].joints.count; ++k )
+					warm_start_revolute( w, w->joints + w->colors[c].joints.data[k] );
+				for ( int k = colorStart[c]; k < colorStart[c + 1]; ++k )
+					warm_start_lane( w, cons + k );
+			}
+		}
+
+		for ( int k = 0; k < overflow->joints.count; ++k )
+			solve_revolute( w, &st, w->joints + overflow->joints.data[k], true );
+		for ( int k = 0; k < ocount; ++k )
+			solve_overflow( w, &st, ocons + k, true );
+		for ( int a = 0; a < activeCount; ++a )
+		{
+			int c = active[a];
+			for ( int k = 0; k < w->colors[c].joints.count; ++k )
+				solve_revolute( w, &st, w->joints + w->colors[c].joints.data[k], true );
+			for ( int k = colorStart[c]; k < colorStart[c + 1]; ++k )
+				solve_lane( w, &st, cons + k, true );
+		}
+
+		integrate_positions( w, &st );
+
+		for ( int k = 0; k < overflow->joints.count; ++k )
+			solve_revolute( w, &st, w->joints + overflow->joints.data[k], false );
+		for ( int k = 0; k < ocount; ++k )
+			solve_overflow( w, &st, ocons + k, false );
+		for ( int a = 0; a < activeCount; ++a )
+		{
+			int c = active[a];
+			for ( int k = 0; k < w->colors[c].joints.count; ++k )
+				solve_revolute( w, &st, w->joints + w->colors[c].joints.data[k], false );
+			for ( int k = colorStart[c]; k < colorStart[c + 1]; ++k )
+				solve_lane( w, &st, cons + k, false );
+		}
+	}
+
+	for ( int k = 0; k < ocount; ++k )
+		restitution_overflow( w, &st, ocons + k );
+	for ( int a = 0; a < activeCount; ++a )
+	{
+		int c = active[a];
+		for ( int k = colorStart[c]; k < colorStart[c + 1]; ++k )
+			restitution_lane( w, &st, cons + k );
+	}
+
+	/* store impulses: the overflow path writes existing points, the 8-lane path both */
+	for ( int k = 0; k < colorStart[O_COLORS]; ++k )
+	{
+		oConstraint* c = cons + k;
+		oManifold* m = &w->contacts[c->contactId].manifold;
+		bool lane = k < colorStart[O_OVERFLOW];
+		int n = lane ? 2 : m->count;
+		for ( int j = 0; j < n; ++j )
+		{
+			m->pts[j].normalImpulse = c->pts[j].normalImpulse;
+			m->pts[j].tangentImpulse = c->pts[j].tangentImpulse;
+			m->pts[j].maxNormalImpulse = c->pts[j].maxNormalImpulse;
+			m->pts[j].normalVelocity = c->pts[j].relativeVelocity;
+		}
+	}
+	free( cons );
+
+	oFinalize f;
+	f.enlarged = (uint8_t*)calloc( (size_t)awakeCount, 1 );
+	f.fast = (int*)malloc( sizeof( int ) * (size_t)awakeCount );
+	f.fastCount = 0;
+	finalize_bodies( w, &st, &f );
+
+	/* enlarge proxies in awake order (reference src/solver.c:1741-1797) */
+	for ( int i = 0; i < awakeCount; ++i )
+	{
+		if ( f.enlarged[i] == 0 )
+			continue;
+		oBody* b = w->bodies + w->awake.data[i];
+		for ( int sid = b->headShape; sid != O_NULL; sid = w->shapes[sid].next )
+		{
+			oShape* s = w->shapes + sid;
+			if ( s->enlargedAABB )
+			{
+				otree_enlarge_proxy( w->trees + ( s->proxyKey & 3 ), s->proxyKey >> 2, s->fatAABB );
+				buffer_move( w, s->proxyKey );
+				s->enlargedAABB = false;
+			}
+			else if ( s->isFast )
+			{
+				buffer_move( w, s->proxyKey );
+			}
+		}
+	}
+
+	for ( int i = 0; i < f.fastCount; ++i )
+		solve_continuous( w, w->bodies + f.fast[i] );
+	for ( int i = 0; i < f.fastCount; ++i )
+	{
+		oBody* b = w->bodies + f.fast[i];
+		if ( b->enlargeAABB == false )
+			continue;
+		b->enlargeAABB = false;
+		for ( int sid = b->headShape; sid != O_NULL; sid = w->shapes[sid].next )
+		{
+			oShape* s = w->shapes + sid;
+			if ( s->enlargedAABB == false )
+				continue;
+			s->enlargedAABB = false;
+			otree_enlarge_proxy( w->trees + b2_dynamicBody, s->proxyKey >> 2, s->fatAABB );
+		}
+	}
+	free( f.enlarged );
+	free( f.fast );
+}
+
+void o_step( oWorld* w, b2r dt, int subSteps )
+{
+	o_update_pairs( w );
+	o_collide( w );
+	if ( dt > R( 0 ) )
+		o_solve( w, dt, subSteps );
+}
