@@ -1,0 +1,297 @@
+"""Benchmark of the per-step contact pipeline on one GB300.
+
+Workload (default): the large pyramid -- 100 rows, 5050 unit boxes with U(-0.01, 0.01) m
+x jitter (seed 1235) on a 200 m static ground, dt 1/60, 4 substeps -- stepped with
+b2World_Step.  One "step" is one b2World_Step of that world.
+
+Printed JSON line (rank 0):
+  value       device-timed ms/step (CUDA events on the world's stream around each step;
+              L2 flushed between timed steps, outside the events)
+  e2e         ms/step through the C API with host buffers: b2World_Step followed by
+              b2World_GetBodyStates (device -> host copy of every body's state)
+  roofline    algorithmic bytes of the colour-phase solver stage (per-unit byte model of
+              the step path, counted from the live contact and body counts) over its
+              device time, against the measured HBM copy bandwidth
+  cpu_baseline  the plain-C CPU restatement of the same step (single thread) on a
+              bounded sample of the same workload
+
+--impl reference times the CPU implementation of the step (the plain-C restatement
+built from oracle/, single thread) on the same workload and prints the same metric.
+--gpus N: the path does not shard (colour phases are global Gauss-Seidel sweeps), so N
+ranks step N independent replicas; value is the slowest rank's ms/step.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+import numpy as np  # noqa: E402
+
+METRIC = "ms/step large pyramid; batched world-steps/s; fwd+bwd vs fwd ms, 1 GB300"
+BASE = 100
+JITTER = 0.01
+SEED = 1235
+DT = 1.0 / 60.0
+SUBSTEPS = 4
+
+
+class DeviceTimes(C.Structure):
+    _fields_ = [("step", C.c_float), ("collide", C.c_float), ("solve", C.c_float), ("finalize", C.c_float),
+                ("eventCount", C.c_int), ("recordCount", C.c_int), ("launches", C.c_int)]
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """Samples SM clocks and throttle reasons with nvidia-smi during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
+                if out.returncode == 0 and out.stdout.strip():
+                    self.samples.append([x.strip() for x in out.stdout.strip().split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        if self._t:
+            self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for s in self.samples:
+            for k, n in enumerate(names):
+                if len(s) > 4 + k and s[4 + k].lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.samples)}
+
+
+def measured_peak():
+    p = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def algorithmic_bytes(contacts, awake_bodies, shape_vertex_counts, substeps):
+    """Per-step byte model of the step path (reads + writes each stage must move once).
+
+    contacts: list of point counts of coloured (touching) contacts; the narrowphase also
+    visits non-touching contacts (0 points).  Returns (total, solver_stage) in bytes.
+    """
+    P = np.asarray(contacts["points"], np.int64)
+    Pall = np.asarray(contacts["all_points"], np.int64)
+    S = substeps
+    N = awake_bodies
+    collide = int(np.sum(244 + 56 * Pall))
+    prepare = int(np.sum(120 + 72 * P))
+    intvel = S * N * 60
+    warm = S * int(np.sum(80 + 24 * P))
+    solve = S * int(np.sum(128 + 52 * P))
+    intpos = S * N * 44
+    relax = S * int(np.sum(116 + 52 * P))
+    restitution = int(np.sum(84 + 36 * P))
+    store = int(np.sum(32 * P))
+    finalize = N * 128 + int(np.sum(8 * np.asarray(shape_vertex_counts) + 32))
+    solver = prepare + intvel + warm + solve + intpos + relax + restitution + store
+    total = collide + solver + finalize
+    return total, solver
+
+
+def cpu_baseline(steps_sample=20):
+    """Times the plain-C CPU restatement of the step on the same workload (1 thread)."""
+    subprocess.run(["make", "-s", "-j8", "-f", "oracle/Makefile"], cwd=REPO, check=True, capture_output=True)
+    from box2c_gb300.capi import Backend
+    ob = os.path.join(REPO, "oracle", "_build")
+    o = Backend(os.path.join(ob, "liboracle.so"), os.path.join(ob, "liboracle_scenes.so"), "oracle")
+    w = o.pyramid(BASE, JITTER, SEED)
+    o.step(w, DT, SUBSTEPS, count=2)
+    t0 = time.perf_counter()
+    o.step(w, DT, SUBSTEPS, count=steps_sample)
+    ms = (time.perf_counter() - t0) * 1e3 / steps_sample
+    o.destroy(w)
+    return ms, steps_sample
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    ms, n = cpu_baseline(steps_sample=max(5, min(args.steps, 40)))
+    line = {"metric": METRIC, "value": round(ms, 4), "unit": "ms/step", "n_gpus": args.gpus, "steps": n,
+            "warmup": 2, "ms_per_step": round(ms, 4), "higher_is_better": False, "impl": "reference",
+            "dtype": "f32", "data": "synthetic", "scaling": "weak", "vs_baseline": None,
+            "config": {"workload": "large_pyramid_100_rows_5050_boxes", "dt": DT, "substeps": SUBSTEPS},
+            "cpu_baseline": {"value": round(ms, 4), "unit": "ms/step", "cores": 1, "kind": "port",
+                             "sample": f"{n} steps of the 100-row pyramid after 2 warm-up steps"},
+            "e2e": {"value": round(ms, 4), "unit": "ms/step", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def run_gpu(args):
+    import box2c_gb300
+    from box2c_gb300.capi import WorldId
+
+    rank, world_size, local = dist_env()
+    if world_size > 1:
+        os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local))
+    dist = None
+    if world_size > 1:
+        import torch.distributed as dist  # noqa: F811
+        dist.init_process_group("gloo")
+
+    import torch
+    box2c_gb300.build()
+    g = box2c_gb300.load()
+    L = g.lib
+    L.b2World_EnableDeviceTiming.argtypes = [WorldId, C.c_bool]
+    L.b2World_GetDeviceTimes.argtypes = [WorldId]
+    L.b2World_GetDeviceTimes.restype = DeviceTimes
+    L.b2World_GetBodyStates.argtypes = [WorldId, C.c_void_p, C.c_int]
+    L.b2World_GetBodyStates.restype = C.c_int
+    L.b2World_GetStatus.argtypes = [WorldId]
+    L.b2World_GetUnsupportedToiCount.argtypes = [WorldId]
+
+    w = g.pyramid(BASE, JITTER, SEED)
+    L.b2World_EnableDeviceTiming(w, True)
+    for _ in range(max(3, args.warmup)):
+        g.step(w, DT, SUBSTEPS)
+
+    # L2 is flushed between timed steps by writing a buffer larger than the 129 MB L2
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    step_ms, solve_ms, collide_ms, finalize_ms, launches = [], [], [], [], []
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    sampler = ClockSampler(0)
+    with sampler:
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            g.step(w, DT, SUBSTEPS)
+            t1 = time.perf_counter()
+            t = L.b2World_GetDeviceTimes(w)
+            step_ms.append(t.step)
+            solve_ms.append(t.solve)
+            collide_ms.append(t.collide)
+            finalize_ms.append(t.finalize)
+            launches.append(t.launches)
+    torch.cuda.synchronize()
+    ms = float(np.mean(step_ms))
+    if dist:
+        tt = torch.tensor([ms])
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms = float(tt.item())
+
+    # end to end through the C API with host buffers
+    n_bodies = L.b2World_GetBodyStates(w, None, 0)
+    host = np.zeros(7 * n_bodies, np.float32)
+    e2e_steps = max(10, args.steps // 2)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        L.b2World_Step(w, DT, SUBSTEPS)
+        L.b2World_GetBodyStates(w, host.ctypes.data, n_bodies)
+    e2e_ms = (time.perf_counter() - t0) * 1e3 / e2e_steps
+
+    contacts = g.contacts(w)
+    touching = contacts[contacts["colorIndex"] >= 0]
+    cinfo = {"points": touching["pointCount"], "all_points": contacts["pointCount"]}
+    counters = g.counters(w)
+    shapes = g.shapes(w)
+    total_bytes, solver_bytes = algorithmic_bytes(cinfo, n_bodies - 1, [4] * (len(shapes) - 1), SUBSTEPS)
+    solve_dev = float(np.mean(solve_ms))
+    peak, peak_kind = measured_peak()
+    achieved = solver_bytes / (solve_dev * 1e-3) / 1e9 if solve_dev > 0 else 0.0
+    status = L.b2World_GetStatus(w)
+    toi = L.b2World_GetUnsupportedToiCount(w)
+    g.destroy(w)
+
+    if rank != 0:
+        return
+    cpu_ms, cpu_n = cpu_baseline() if not args.no_cpu else (None, 0)
+    clocks = sampler.summary()
+    line = {
+        "metric": METRIC, "value": round(ms, 4), "unit": "ms/step", "n_gpus": world_size, "steps": args.steps,
+        "warmup": max(3, args.warmup), "ms_per_step": round(ms, 4), "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "large_pyramid_100_rows_5050_boxes", "rows": BASE, "bodies": n_bodies - 1,
+                   "contacts": int(len(contacts)), "touching": int(len(touching)), "colors": list(counters.colorCounts),
+                   "dt": DT, "substeps": SUBSTEPS, "l2": "flushed between timed steps (256 MB write)",
+                   "parallelism": f"replicas{world_size}"},
+        "stages_ms": {"collide": round(float(np.mean(collide_ms)), 4), "solve": round(solve_dev, 4),
+                      "finalize": round(float(np.mean(finalize_ms)), 4)},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "traffic": None, "kernel": "solver stage (prepare..store)",
+                     "algorithmic_bytes_per_step": solver_bytes, "peak_kind": peak_kind},
+        "step_roofline": {"algorithmic_bytes_per_step": total_bytes,
+                          "achieved_gbs": round(total_bytes / (ms * 1e-3) / 1e9, 2)},
+        "e2e": {"value": round(e2e_ms, 4), "unit": "ms/step", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": int(n_bodies * 7 * 4 + n_bodies * 64)},
+        "gpu_launches": int(sum(launches)),
+        "cpu_baseline": ({"value": round(cpu_ms, 4), "unit": "ms/step", "cores": 1, "kind": "port",
+                          "sample": f"{cpu_n} steps of the same 100-row pyramid after 2 warm-up steps"}
+                         if cpu_ms is not None else None),
+        "clocks": clocks, "status": status, "unsupported_toi": toi,
+    }
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=500)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,404 @@
+/*
+ * arena.cu -- device memory of one world: allocation, growth, host<->device copies and
+ * the mapped pinned buffers through which the narrowphase and the finalisation kernel
+ * hand their (rare) events to the host without an extra copy.
+ *
+ * Every array grows geometrically and keeps its contents; growth only happens while
+ * the host adds bodies, shapes or contacts, never inside a kernel sequence.
+ */
+#include "b2g_device.h"
+
+#include <cuda_runtime.h>
+
+#include <stdlib.h>
+#include <string.h>
+
+static cudaError_t s_err = cudaSuccess;
+
+static int ok( cudaError_t e )
+{
+	if ( e != cudaSuccess )
+	{
+		s_err = e;
+		return (int)e;
+	}
+	return 0;
+}
+
+extern "C" int b2gd_device_ok( void )
+{
+	int n = 0;
+	if ( cudaGetDeviceCount( &n ) != cudaSuccess )
+		return 0;
+	return n > 0;
+}
+
+/* Reallocates a device array from oldBytes to newBytes keeping the prefix. */
+static int grow( void** ptr, size_t oldBytes, size_t newBytes, cudaStream_t s )
+{
+	if ( newBytes <= oldBytes && *ptr != nullptr )
+		return 0;
+	void* p = nullptr;
+	int e = ok( cudaMalloc( &p, newBytes ) );
+	if ( e )
+		return e;
+	cudaMemsetAsync( p, 0, newBytes, s );
+	if ( *ptr != nullptr )
+	{
+		if ( oldBytes > 0 )
+			cudaMemcpyAsync( p, *ptr, oldBytes, cudaMemcpyDeviceToDevice, s );
+		cudaStreamSynchronize( s );
+		cudaFree( *ptr );
+	}
+	*ptr = p;
+	return 0;
+}
+
+static int grow_host_mapped( void** hptr, void** dptr, size_t bytes )
+{
+	if ( *hptr )
+		cudaFreeHost( *hptr );
+	*hptr = nullptr;
+	*dptr = nullptr;
+	int e = ok( cudaHostAlloc( hptr, bytes, cudaHostAllocMapped ) );
+	if ( e )
+		return e;
+	memset( *hptr, 0, bytes );
+	return ok( cudaHostGetDevicePointer( dptr, *hptr, 0 ) );
+}
+
+extern "C" int b2gd_init( b2gDevWorld* w, b2gHostIO* io )
+{
+	memset( w, 0, sizeof( *w ) );
+	memset( io, 0, sizeof( *io ) );
+	cudaStream_t s;
+	int e = ok( cudaStreamCreateWithFlags( &s, cudaStreamNonBlocking ) );
+	if ( e )
+		return e;
+	w->stream = (void*)s;
+	e = ok( cudaMalloc( (void**)&w->counters, 4 * sizeof( int ) ) );
+	if ( e )
+		return e;
+	e = ok( cudaHostAlloc( (void**)&io->counters, 4 * sizeof( int ), cudaHostAllocDefault ) );
+	if ( e )
+		return e;
+	memset( io->counters, 0, 4 * sizeof( int ) );
+	return ok( cudaMemsetAsync( w->counters, 0, 4 * sizeof( int ), s ) );
+}
+
+#define FREE_DEV( p )                                                                                                            \
+	do                                                                                                                           \
+	{                                                                                                                            \
+		if ( p )                                                                                                                 \
+			cudaFree( (void*)( p ) );                                                                                            \
+		p = nullptr;                                                                                                             \
+	}                                                                                                                            \
+	while ( 0 )
+
+extern "C" void b2gd_free( b2gDevWorld* w, b2gHostIO* io )
+{
+	if ( w->stream )
+		cudaStreamSynchronize( (cudaStream_t)w->stream );
+	FREE_DEV( w->state );
+	FREE_DEV( w->xf );
+	FREE_DEV( w->centers );
+	FREE_DEV( w->prev );
+	FREE_DEV( w->mass );
+	FREE_DEV( w->force );
+	FREE_DEV( w->extent );
+	FREE_DEV( w->bodyInfo );
+	FREE_DEV( w->awake );
+	FREE_DEV( w->shapeRange );
+	FREE_DEV( w->shapeList );
+	FREE_DEV( w->geo );
+	FREE_DEV( w->aabb );
+	FREE_DEV( w->fat );
+	FREE_DEV( w->cShapes );
+	FREE_DEV( w->cMix );
+	FREE_DEV( w->cFlags );
+	FREE_DEV( w->cBodies );
+	FREE_DEV( w->cMass );
+	FREE_DEV( w->manifold );
+	FREE_DEV( w->solveList );
+	FREE_DEV( w->jointList );
+	FREE_DEV( w->kIdx );
+	FREE_DEV( w->kNF );
+	FREE_DEV( w->kSoft );
+	FREE_DEV( w->kMass );
+	for ( int j = 0; j < 2; ++j )
+	{
+		FREE_DEV( w->kAnchor[j] );
+		FREE_DEV( w->kCoef[j] );
+		FREE_DEV( w->kImp[j] );
+	}
+	FREE_DEV( w->joints );
+	FREE_DEV( w->newContacts );
+	FREE_DEV( w->counters );
+	for ( int i = 0; i < 8; ++i )
+		if ( w->timers[i] )
+			cudaEventDestroy( (cudaEvent_t)w->timers[i] );
+	if ( io->events )
+		cudaFreeHost( io->events );
+	if ( io->records )
+		cudaFreeHost( io->records );
+	if ( io->counters )
+		cudaFreeHost( io->counters );
+	if ( io->newContacts )
+		cudaFreeHost( io->newContacts );
+	if ( w->stream )
+		cudaStreamDestroy( (cudaStream_t)w->stream );
+	memset( w, 0, sizeof( *w ) );
+	memset( io, 0, sizeof( *io ) );
+}
+
+static int next_cap( int have, int need )
+{
+	if ( need <= have )
+		return have;
+	int c = have < 64 ? 64 : have;
+	while ( c < need )
+		c *= 2;
+	return c;
+}
+
+extern "C" int b2gd_reserve( b2gDevWorld* w, b2gHostIO* io, int bodyCap, int shapeCap, int contactCap, int jointCap, int solveCap,
+							 int listCap )
+{
+	cudaStream_t s = (cudaStream_t)w->stream;
+	int e = 0;
+	if ( bodyCap > w->bodyCap )
+	{
+		int nc = next_cap( w->bodyCap, bodyCap );
+		size_t o4 = 16u * (size_t)w->bodyCap, n4 = 16u * (size_t)nc;
+		e |= grow( &w->state, 2 * o4, 2 * n4, s );
+		e |= grow( &w->xf, o4, n4, s );
+		e |= grow( &w->centers, o4, n4, s );
+		e |= grow( &w->prev, o4, n4, s );
+		e |= grow( &w->mass, o4, n4, s );
+		e |= grow( &w->force, o4, n4, s );
+		e |= grow( &w->extent, o4, n4, s );
+		e |= grow( (void**)&w->bodyInfo, 4u * (size_t)w->bodyCap, 4u * (size_t)nc, s );
+		e |= grow( (void**)&w->awake, 4u * (size_t)w->bodyCap, 4u * (size_t)nc, s );
+		e |= grow( (void**)&w->shapeRange, 8u * (size_t)w->bodyCap, 8u * (size_t)nc, s );
+		w->bodyCap = nc;
+	}
+	if ( shapeCap > w->shapeCap )
+	{
+		int nc = next_cap( w->shapeCap, shapeCap );
+		e |= grow( (void**)&w->geo, sizeof( b2gShapeGeo ) * (size_t)w->shapeCap, sizeof( b2gShapeGeo ) * (size_t)nc, s );
+		e |= grow( &w->aabb, 16u * (size_t)w->shapeCap, 16u * (size_t)nc, s );
+		e |= grow( &w->fat, 16u * (size_t)w->shapeCap, 16u * (size_t)nc, s );
+		e |= grow( (void**)&w->shapeList, 4u * (size_t)w->shapeCap, 4u * (size_t)nc, s );
+		/* two records at most per shape and step */
+		e |= grow_host_mapped( (void**)&io->records, (void**)&w->records, sizeof( b2gRecord ) * 2u * (size_t)nc );
+		w->recordCap = 2 * nc;
+		w->shapeCap = nc;
+	}
+	if ( contactCap > w->contactCap )
+	{
+		int nc = next_cap( w->contactCap, contactCap );
+		size_t o = (size_t)w->contactCap, n = (size_t)nc;
+		e |= grow( (void**)&w->cShapes, 8u * o, 8u * n, s );
+		e |= grow( (void**)&w->cMix, 8u * o, 8u * n, s );
+		e |= grow( (void**)&w->cFlags, 4u * o, 4u * n, s );
+		e |= grow( (void**)&w->cBodies, 8u * o, 8u * n, s );
+		e |= grow( &w->cMass, 16u * o, 16u * n, s );
+		e |= grow( (void**)&w->manifold, sizeof( b2gManifold ) * o, sizeof( b2gManifold ) * n, s );
+		e |= grow_host_mapped( (void**)&io->events, (void**)&w->events, 4u * n );
+		w->eventCap = nc;
+		/* new contacts per step are bounded by the contact capacity */
+		if ( io->newContacts )
+			cudaFreeHost( io->newContacts );
+		e |= ok( cudaHostAlloc( (void**)&io->newContacts, sizeof( b2gContactInit ) * n, cudaHostAllocDefault ) );
+		e |= grow( (void**)&w->newContacts, sizeof( b2gContactInit ) * o, sizeof( b2gContactInit ) * n, s );
+		w->newCap = nc;
+		w->contactCap = nc;
+	}
+	if ( solveCap > w->solveCap )
+	{
+		int nc = next_cap( w->solveCap, solveCap );
+		size_t o = (size_t)w->solveCap, n = (size_t)nc;
+		e |= grow( (void**)&w->solveList, 4u * o, 4u * n, s );
+		e |= grow( &w->kIdx, 16u * o, 16u * n, s );
+		e |= grow( &w->kNF, 16u * o, 16u * n, s );
+		e |= grow( &w->kSoft, 16u * o, 16u * n, s );
+		e |= grow( &w->kMass, 16u * o, 16u * n, s );
+		for ( int j = 0; j < 2; ++j )
+		{
+			e |= grow( &w->kAnchor[j], 16u * o, 16u * n, s );
+			e |= grow( &w->kCoef[j], 16u * o, 16u * n, s );
+			e |= grow( &w->kImp[j], 16u * o, 16u * n, s );
+		}
+		w->solveCap = nc;
+	}
+	if ( jointCap > w->jointCap )
+	{
+		int nc = next_cap( w->jointCap, jointCap );
+		e |= grow( (void**)&w->joints, sizeof( b2gJointDev ) * (size_t)w->jointCap, sizeof( b2gJointDev ) * (size_t)nc, s );
+		e |= grow( (void**)&w->jointList, 4u * (size_t)w->jointCap, 4u * (size_t)nc, s );
+		w->jointCap = nc;
+	}
+	(void)listCap;
+	if ( e == 0 )
+		e = ok( cudaStreamSynchronize( s ) );
+	return e;
+}
+
+static int h2d( void* dst, const void* src, size_t bytes, cudaStream_t s )
+{
+	if ( bytes == 0 )
+		return 0;
+	return ok( cudaMemcpyAsync( dst, src, bytes, cudaMemcpyHostToDevice, s ) );
+}
+
+static int d2h( void* dst, const void* src, size_t bytes, cudaStream_t s )
+{
+	if ( bytes == 0 )
+		return 0;
+	return ok( cudaMemcpyAsync( dst, src, bytes, cudaMemcpyDeviceToHost, s ) );
+}
+
+extern "C" int b2gd_upload_bodies( b2gDevWorld* w, const float* state, const float* xf, const float* centers, const float* prev,
+								   const float* mass, const float* force, const float* extent, const int* info, int count )
+{
+	cudaStream_t s = (cudaStream_t)w->stream;
+	size_t n4 = 16u * (size_t)count;
+	int e = 0;
+	e |= h2d( w->state, state, 2 * n4, s );
+	e |= h2d( w->xf, xf, n4, s );
+	e |= h2d( w->centers, centers, n4, s );
+	e |= h2d( w->prev, prev, n4, s );
+	e |= h2d( w->mass, mass, n4, s );
+	e |= h2d( w->force, force, n4, s );
+	e |= h2d( w->extent, extent, n4, s );
+	e |= h2d( w->bodyInfo, info, 4u * (size_t)count, s );
+	return e;
+}
+
+extern "C" int b2gd_upload_awake( b2gDevWorld* w, const int* awake, int count )
+{
+	return h2d( w->awake, awake, 4u * (size_t)count, (cudaStream_t)w->stream );
+}
+
+extern "C" int b2gd_upload_shapes( b2gDevWorld* w, const b2gShapeGeo* geo, const float* aabb, const float* fat, int count )
+{
+	cudaStream_t s = (cudaStream_t)w->stream;
+	int e = h2d( w->geo, geo, sizeof( b2gShapeGeo ) * (size_t)count, s );
+	e |= h2d( w->aabb, aabb, 16u * (size_t)count, s );
+	e |= h2d( w->fat, fat, 16u * (size_t)count, s );
+	return e;
+}
+
+extern "C" int b2gd_upload_shape_lists( b2gDevWorld* w, const int* range, int bodyCount, const int* list, int listCount )
+{
+	cudaStream_t s = (cudaStream_t)w->stream;
+	int e = h2d( w->shapeRange, range, 8u * (size_t)bodyCount, s );
+	e |= h2d( w->shapeList, list, 4u * (size_t)listCount, s );
+	return e;
+}
+
+extern "C" int b2gd_upload_joints( b2gDevWorld* w, const b2gJointDev* joints, int count )
+{
+	return h2d( w->joints, joints, sizeof( b2gJointDev ) * (size_t)count, (cudaStream_t)w->stream );
+}
+
+extern "C" int b2gd_upload_solve_lists( b2gDevWorld* w, const int* solveList, int solveCount, const int* jointList, int jointCount )
+{
+	cudaStream_t s = (cudaStream_t)w->stream;
+	int e = h2d( w->solveList, solveList, 4u * (size_t)solveCount, s );
+	e |= h2d( w->jointList, jointList, 4u * (size_t)jointCount, s );
+	return e;
+}
+
+extern "C" int b2gd_upload_fat( b2gDevWorld* w, int shapeId, const float* fat4 )
+{
+	return h2d( (char*)w->fat + 16u * (size_t)shapeId, fat4, 16u, (cudaStream_t)w->stream );
+}
+
+extern "C" int b2gd_upload_body_velocity( b2gDevWorld* w, int bodyId, const float* v3 )
+{
+	return h2d( (char*)w->state + 32u * (size_t)bodyId, v3, 12u, (cudaStream_t)w->stream );
+}
+
+extern "C" int b2gd_download_bodies( b2gDevWorld* w, float* state, float* xf, float* centers, int count )
+{
+	cudaStream_t s = (cudaStream_t)w->stream;
+	size_t n4 = 16u * (size_t)count;
+	int e = d2h( state, w->state, 2 * n4, s );
+	e |= d2h( xf, w->xf, n4, s );
+	e |= d2h( centers, w->centers, n4, s );
+	e |= ok( cudaStreamSynchronize( s ) );
+	return e;
+}
+
+extern "C" int b2gd_download_manifolds( b2gDevWorld* w, b2gManifold* out, uint32_t* flags, int count )
+{
+	cudaStream_t s = (cudaStream_t)w->stream;
+	int e = d2h( out, w->manifold, sizeof( b2gManifold ) * (size_t)count, s );
+	if ( flags )
+		e |= d2h( flags, w->cFlags, 4u * (size_t)count, s );
+	e |= ok( cudaStreamSynchronize( s ) );
+	return e;
+}
+
+extern "C" int b2gd_download_shapes( b2gDevWorld* w, float* aabb, float* fat, int count )
+{
+	cudaStream_t s = (cudaStream_t)w->stream;
+	int e = d2h( aabb, w->aabb, 16u * (size_t)count, s );
+	e |= d2h( fat, w->fat, 16u * (size_t)count, s );
+	e |= ok( cudaStreamSynchronize( s ) );
+	return e;
+}
+
+extern "C" int b2gd_download_joints( b2gDevWorld* w, b2gJointDev* joints, int count )
+{
+	cudaStream_t s = (cudaStream_t)w->stream;
+	int e = d2h( joints, w->joints, sizeof( b2gJointDev ) * (size_t)count, s );
+	e |= ok( cudaStreamSynchronize( s ) );
+	return e;
+}
+
+extern "C" int b2gd_sync( b2gDevWorld* w )
+{
+	return ok( cudaStreamSynchronize( (cudaStream_t)w->stream ) );
+}
+
+extern "C" void b2gd_enable_timing( b2gDevWorld* w, int flag )
+{
+	if ( flag && w->timers[0] == nullptr )
+	{
+		for ( int i = 0; i < 8; ++i )
+		{
+			cudaEvent_t e;
+			cudaEventCreate( &e );
+			w->timers[i] = (void*)e;
+		}
+	}
+	w->timing = flag && w->timers[0] != nullptr;
+}
+
+static float elapsed( void* a, void* b )
+{
+	float ms = 0.0f;
+	if ( cudaEventElapsedTime( &ms, (cudaEvent_t)a, (cudaEvent_t)b ) != cudaSuccess )
+		return 0.0f;
+	return ms;
+}
+
+extern "C" void b2gd_mark( b2gDevWorld* w, int slot )
+{
+	if ( w->timing )
+		cudaEventRecord( (cudaEvent_t)w->timers[slot], (cudaStream_t)w->stream );
+}
+
+extern "C" void b2gd_stage_times( b2gDevWorld* w, float* stepMs, float* collideMs, float* solveMs, float* finalizeMs )
+{
+	*stepMs = *collideMs = *solveMs = *finalizeMs = 0.0f;
+	if ( w->timing == 0 )
+		return;
+	cudaEventSynchronize( (cudaEvent_t)w->timers[6] );
+	*stepMs = elapsed( w->timers[0], w->timers[6] );
+	*collideMs = elapsed( w->timers[1], w->timers[2] );
+	*solveMs = elapsed( w->timers[3], w->timers[4] );
+	*finalizeMs = elapsed( w->timers[4], w->timers[5] );
+}

@@ -1,0 +1,77 @@
+/*
+ * b2g_device.h -- C interface between the host step driver (C) and the CUDA side
+ * (device arena management, transfers and kernel launch sequences).
+ */
+#pragma once
+
+#include "b2g_types.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Colour-major layout of one step's constraint rows and joint list.  Colour c (0..10)
+ * owns rows [colorStart[c], colorStart[c+1]) and joints [jointStart[c], jointStart[c+1]);
+ * colour 11 is the overflow set, solved serially in list order. */
+typedef struct b2gSolvePlan
+{
+	int colorStart[B2G_COLORS + 1];
+	int jointStart[B2G_COLORS + 1];
+	int active[B2G_COLORS];
+	int activeCount;
+	int awakeCount;
+} b2gSolvePlan;
+
+/* Pinned host staging owned by the device module (mapped into the device). */
+typedef struct b2gHostIO
+{
+	int* counters;		/* [0] events [1] records [2] status, copied back each sync */
+	int* events;		/* mapped: narrowphase events */
+	b2gRecord* records; /* mapped: finalisation records */
+	b2gContactInit* newContacts;
+} b2gHostIO;
+
+int b2gd_device_ok( void );
+const char* b2gd_last_error( void );
+
+int b2gd_init( b2gDevWorld* w, b2gHostIO* io );
+void b2gd_free( b2gDevWorld* w, b2gHostIO* io );
+
+/* Grow device arrays (contents preserved). Returns 0 on success. */
+int b2gd_reserve( b2gDevWorld* w, b2gHostIO* io, int bodyCap, int shapeCap, int contactCap, int jointCap, int solveCap,
+				  int listCap );
+
+/* Host -> device copies of body / shape / list data (host arrays use the device layout). */
+int b2gd_upload_bodies( b2gDevWorld* w, const float* state, const float* xf, const float* centers, const float* prev,
+						const float* mass, const float* force, const float* extent, const int* info, int count );
+int b2gd_upload_awake( b2gDevWorld* w, const int* awake, int count );
+int b2gd_upload_shapes( b2gDevWorld* w, const b2gShapeGeo* geo, const float* aabb, const float* fat, int count );
+int b2gd_upload_shape_lists( b2gDevWorld* w, const int* range, int bodyCount, const int* list, int listCount );
+int b2gd_upload_joints( b2gDevWorld* w, const b2gJointDev* joints, int count );
+int b2gd_upload_solve_lists( b2gDevWorld* w, const int* solveList, int solveCount, const int* jointList, int jointCount );
+int b2gd_upload_fat( b2gDevWorld* w, int shapeId, const float* fat4 );
+int b2gd_upload_body_velocity( b2gDevWorld* w, int bodyId, const float* v3 );
+
+/* Device -> host copies. */
+int b2gd_download_bodies( b2gDevWorld* w, float* state, float* xf, float* centers, int count );
+int b2gd_download_manifolds( b2gDevWorld* w, b2gManifold* out, uint32_t* flags, int count );
+int b2gd_download_shapes( b2gDevWorld* w, float* aabb, float* fat, int count );
+int b2gd_download_joints( b2gDevWorld* w, b2gJointDev* joints, int count );
+
+/* Step stages.  b2gd_collide launches contact creation and the narrowphase and copies
+ * the event count back; b2gd_solve launches the solver and finalisation and copies the
+ * record count back.  b2gd_sync waits for the stream; returns 0 or a CUDA error. */
+int b2gd_collide( b2gDevWorld* w, b2gHostIO* io, int newContactCount, int contactIdCount );
+int b2gd_solve( b2gDevWorld* w, b2gHostIO* io, const b2gSolvePlan* plan, const b2gStepConst* sc );
+int b2gd_sync( b2gDevWorld* w );
+
+/* Device time of the last step's stages in milliseconds (CUDA events recorded when
+ * w->timing is set). */
+void b2gd_enable_timing( b2gDevWorld* w, int flag );
+void b2gd_stage_times( b2gDevWorld* w, float* stepMs, float* collideMs, float* solveMs, float* finalizeMs );
+/* Records timer slot 0 (step start) or 6 (step end) on the world's stream. */
+void b2gd_mark( b2gDevWorld* w, int slot );
+
+#ifdef __cplusplus
+}
+#endif

@@ -1,0 +1,209 @@
+/*
+ * b2g_types.h -- data layout shared by the host C code and the sm_103a kernels.
+ *
+ * Device memory of one world ("arena") holds structure-of-arrays records indexed by the
+ * stable ids of the C API:
+ *   bodies   : solver state (2 x float4: v.x v.y w flags | dp.x dp.y dq.c dq.s, the
+ *              32-byte b2BodyState of reference src/body.h:76-91), transform, centre,
+ *              previous pose, mass, force, damping/extent (float4 each)
+ *   shapes   : geometry (160 B), tight and fat AABB (float4 each)
+ *   contacts : shape pair, mixed friction/restitution, flags, manifold (112 B)
+ *   solver   : per-step constraint rows in colour-major order (see kernels.cu)
+ * The host keeps pinned mirrors of the body arrays with the same layout, so setup data
+ * and read-back move with single contiguous copies.
+ */
+#pragma once
+
+#include "b2g_math.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Shape geometry record (160 bytes).  Polygons use v/n/centroid/count/radius; circles
+ * v[0] and radius; capsules v[0], v[1] and radius; segments v[0], v[1]. */
+typedef struct b2gShapeGeo
+{
+	int32_t type;
+	int32_t count;
+	float radius;
+	int32_t bodyId;
+	b2gVec v[8];
+	b2gVec n[8];
+	b2gVec centroid;
+	int32_t enableHitEvents;
+	int32_t isSensor;
+} b2gShapeGeo;
+
+typedef struct b2gPoint
+{
+	b2gVec anchorA, anchorB, point;
+	float separation, normalImpulse, tangentImpulse, maxNormalImpulse, normalVelocity;
+	uint16_t id;
+	uint8_t persisted;
+	uint8_t pad;
+} b2gPoint;
+
+/* Contact manifold (112 bytes), same fields as reference b2Manifold
+ * (include/box2d/collision.h:474-520). */
+typedef struct b2gManifold
+{
+	b2gPoint pts[2];
+	b2gVec normal;
+	int32_t count;
+	int32_t pad;
+} b2gManifold;
+
+/* Contact flags kept on the device (reference src/contact.h:85-104). */
+enum
+{
+	B2G_C_LIVE = 0x1,
+	B2G_C_TOUCHING = 0x10000,
+	B2G_C_HIT = 0x100000,
+};
+
+/* Narrowphase event codes, packed as (contactId << 2) | code. */
+enum
+{
+	B2G_EV_DISJOINT = 1,
+	B2G_EV_STARTED = 2,
+	B2G_EV_STOPPED = 3,
+};
+
+/* Body info bits (bodyInfo array). */
+enum
+{
+	B2G_B_TYPE_MASK = 0x3,
+	B2G_B_AWAKE = 0x4,
+	B2G_B_BULLET = 0x8,
+	B2G_B_SLEEP_OK = 0x10,
+};
+
+/* Staged contact record: a contact created by the host broadphase (flags 0), or the
+ * retirement of a destroyed contact id (flags B2G_INIT_KILL). */
+#define B2G_INIT_KILL 0x80000000u
+
+typedef struct b2gContactInit
+{
+	int32_t id;
+	int32_t shapeA;
+	int32_t shapeB;
+	float friction;
+	float restitution;
+	uint32_t flags;
+} b2gContactInit;
+
+/* Finalisation record for a shape whose broadphase proxy needs host attention. */
+enum
+{
+	B2G_R_ENLARGED = 0x1,	   /* non-fast shape with a grown fat box */
+	B2G_R_FAST = 0x2,		   /* shape of a fast body: moved to the move buffer */
+	B2G_R_FAST_ENLARGED = 0x4, /* fast shape whose fat box grew after the sweep */
+	B2G_R_BULLET = 0x8,
+};
+
+typedef struct b2gRecord
+{
+	int32_t awakeIndex;
+	int32_t slot; /* position of the shape in its body's shape list */
+	int32_t shapeId;
+	int32_t flags;
+	float fat[4];
+	float sweep[4]; /* swept box of a fast shape (union of old and new boxes) */
+} b2gRecord;
+
+/* Revolute joint configuration (host-owned) and solver state (device-owned),
+ * reference src/joint.h:161-190 and src/revolute_joint.c:201-470. */
+typedef struct b2gJointDev
+{
+	int32_t bodyIdA, bodyIdB;
+	int32_t indexA, indexB;
+	b2gVec localAnchorA, localAnchorB;
+	float hertz, dampingRatio, maxMotorTorque, motorSpeed, referenceAngle, lowerAngle, upperAngle;
+	int32_t enableSpring, enableMotor, enableLimit;
+
+	/* solver state */
+	float invMassA, invMassB, invIA, invIB;
+	b2gVec linearImpulse;
+	float springImpulse, motorImpulse, lowerImpulse, upperImpulse;
+	b2gVec anchorA, anchorB, deltaCenter;
+	float deltaAngle, axialMass;
+	float springBias, springMass, springImpulseScale;
+	int32_t pad;
+} b2gJointDev;
+
+/* Step constants (reference b2StepContext, src/solver.h:76-140). */
+typedef struct b2gStepConst
+{
+	float dt, inv_dt, h, inv_h;
+	int32_t subSteps;
+	float contactSoft[3]; /* biasRate, massScale, impulseScale */
+	float staticSoft[3];
+	float jointSoft[3];
+	float restitutionThreshold, pushout;
+	b2gVec gravity;
+	int32_t enableWarmStarting, enableContinuous, enableSleep;
+} b2gStepConst;
+
+/* Device arena of one world: raw device pointers and capacities. */
+typedef struct b2gDevWorld
+{
+	int bodyCap, shapeCap, contactCap, jointCap, solveCap, listCap;
+
+	/* bodies, indexed by body id */
+	void* state;   /* float4[2*bodyCap] */
+	void* xf;	   /* float4: p.x p.y q.c q.s */
+	void* centers; /* float4: center.x center.y localCenter.x localCenter.y */
+	void* prev;	   /* float4: center0.x center0.y rot0.c rot0.s */
+	void* mass;	   /* float4: mass invMass inertia invI */
+	void* force;   /* float4: force.x force.y torque gravityScale */
+	void* extent;  /* float4: linearDamping angularDamping minExtent maxExtent */
+	int* bodyInfo;
+	int* awake;		 /* awake body ids in solver order */
+	int* shapeRange; /* 2 per body: start, count into shapeList */
+	int* shapeList;
+
+	/* shapes, indexed by shape id */
+	b2gShapeGeo* geo;
+	void* aabb; /* float4 */
+	void* fat;	/* float4 */
+
+	/* contacts, indexed by contact id */
+	int* cShapes;	/* 2 per contact */
+	float* cMix;	/* friction, restitution */
+	uint32_t* cFlags;
+	int* cBodies; /* 2 per contact: awake body id or -1 */
+	void* cMass;  /* float4: invMassA invIA invMassB invIB */
+	b2gManifold* manifold;
+
+	/* colour-major solve lists */
+	int* solveList; /* contact ids */
+	int* jointList; /* joint ids */
+
+	/* constraint rows */
+	void* kIdx;	 /* int4: indexA indexB contactId pointCount */
+	void* kNF;	 /* float4: normal.x normal.y friction restitution */
+	void* kSoft; /* float4: biasRate massScale impulseScale 0 */
+	void* kMass; /* float4: mA iA mB iB */
+	void* kAnchor[2];
+	void* kCoef[2]; /* baseSeparation normalMass tangentMass relativeVelocity */
+	void* kImp[2];	/* normalImpulse tangentImpulse maxNormalImpulse 0 */
+
+	b2gJointDev* joints;
+
+	/* staging and outputs */
+	b2gContactInit* newContacts;
+	int newCap;
+	int* counters;	   /* device: [0] events, [1] records, [2] status */
+	int* events;	   /* device view of the mapped event buffer */
+	b2gRecord* records; /* device view of the mapped record buffer */
+	int eventCap, recordCap;
+	void* stream; /* cudaStream_t */
+	void* timers[8]; /* cudaEvent_t: step start, collide start/end, solve start/end, finalize end, step end */
+	int timing;
+	int launches;
+} b2gDevWorld;
+
+#ifdef __cplusplus
+}
+#endif

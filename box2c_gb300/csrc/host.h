@@ -1,0 +1,300 @@
+/*
+ * host.h -- host-side records of the GB300 step driver.
+ *
+ * The host keeps what is serial and order-sensitive in the reference step: id pools
+ * (src/id_pool.c), body/shape/contact/joint bookkeeping and linked lists
+ * (src/body.c, src/shape.c, src/contact.c, src/joint.c), the three broadphase trees and
+ * move buffer (src/dynamic_tree.c, src/broad_phase.c) and the constraint-graph colour
+ * arrays (src/constraint_graph.c).  Numeric state (body motion, shape boxes, manifolds,
+ * impulses) lives in the device arena (b2g_types.h) and is mirrored into pinned host
+ * arrays only for setup and read-back.
+ */
+#pragma once
+
+#include "b2g_device.h"
+#include "b2g_math.h"
+#include "b2g_types.h"
+
+#include "box2d/box2d.h"
+
+#include <stdlib.h>
+
+/* ---------------------------------------------------------------- containers */
+typedef struct gIntArray
+{
+	int* data;
+	int count;
+	int capacity;
+} gIntArray;
+
+void gia_push( gIntArray* a, int v );
+int gia_remove_swap( gIntArray* a, int index ); /* returns the moved index or -1 */
+void gia_free( gIntArray* a );
+
+typedef struct gSet
+{
+	uint64_t* keys;
+	int capacity;
+	int count;
+} gSet;
+
+bool gset_add( gSet* s, uint64_t key ); /* true if already present */
+bool gset_remove( gSet* s, uint64_t key );
+bool gset_contains( const gSet* s, uint64_t key );
+void gset_clear( gSet* s );
+void gset_free( gSet* s );
+
+typedef struct gIdPool
+{
+	gIntArray freeIds;
+	int next;
+} gIdPool;
+
+int gid_alloc( gIdPool* p );
+void gid_free( gIdPool* p, int id );
+int gid_count( const gIdPool* p );
+
+typedef struct gBits
+{
+	uint64_t* words;
+	int wordCount;
+} gBits;
+
+bool gbits_get( const gBits* b, int i );
+void gbits_set( gBits* b, int i );
+void gbits_clear( gBits* b, int i );
+void gbits_free( gBits* b );
+
+/* ---------------------------------------------------------------- tree */
+typedef struct gNode
+{
+	b2gBox box;
+	uint32_t category;
+	int parent;
+	int child1, child2;
+	int userData;
+	int16_t height;
+	bool enlarged;
+} gNode;
+
+typedef struct gTree
+{
+	gNode* nodes;
+	int root;
+	int nodeCount;
+	int capacity;
+	int freeList;
+	int proxyCount;
+	int* leafIndices;
+	b2gVec* leafCenters;
+	int rebuildCapacity;
+} gTree;
+
+static inline float gbox_perimeter( b2gBox a )
+{
+	float wx = a.hi.x - a.lo.x;
+	float wy = a.hi.y - a.lo.y;
+	return 2.0f * ( wx + wy );
+}
+
+static inline b2gVec gbox_center( b2gBox a ) { return gv( 0.5f * ( a.lo.x + a.hi.x ), 0.5f * ( a.lo.y + a.hi.y ) ); }
+
+static inline bool gbox_enlarge( b2gBox* a, b2gBox b )
+{
+	bool changed = false;
+	if ( b.lo.x < a->lo.x )
+	{
+		a->lo.x = b.lo.x;
+		changed = true;
+	}
+	if ( b.lo.y < a->lo.y )
+	{
+		a->lo.y = b.lo.y;
+		changed = true;
+	}
+	if ( a->hi.x < b.hi.x )
+	{
+		a->hi.x = b.hi.x;
+		changed = true;
+	}
+	if ( a->hi.y < b.hi.y )
+	{
+		a->hi.y = b.hi.y;
+		changed = true;
+	}
+	return changed;
+}
+
+void gtree_init( gTree* t );
+void gtree_free( gTree* t );
+int gtree_create_proxy( gTree* t, b2gBox box, uint32_t category, int userData );
+void gtree_destroy_proxy( gTree* t, int proxyId );
+void gtree_move_proxy( gTree* t, int proxyId, b2gBox box );
+void gtree_enlarge_proxy( gTree* t, int proxyId, b2gBox box );
+void gtree_rebuild( gTree* t );
+int gtree_height( const gTree* t );
+typedef bool gQueryFcn( int proxyId, int userData, void* ctx );
+void gtree_query( const gTree* t, b2gBox box, uint32_t mask, gQueryFcn* fcn, void* ctx );
+
+/* ---------------------------------------------------------------- records */
+typedef struct gBody
+{
+	int id; /* -1 when free */
+	b2BodyType type;
+	int awakeIndex;
+	int headShape, shapeCount;
+	int headContactKey, contactCount;
+	int headJointKey, jointCount;
+	void* userData;
+	uint16_t revision;
+	bool fixedRotation, isBullet, enableSleep, automaticMass;
+	float sleepThreshold;
+} gBody;
+
+typedef struct gShape
+{
+	int id;
+	int bodyId;
+	int prev, next;
+	b2ShapeType type;
+	float density, friction, restitution;
+	b2Filter filter;
+	void* userData;
+	int proxyKey;
+	uint16_t revision;
+	bool isSensor, enableContactEvents, enableSensorEvents, enableHitEvents, enablePreSolveEvents;
+} gShape;
+
+typedef struct gEdge
+{
+	int bodyId, prevKey, nextKey;
+} gEdge;
+
+enum
+{
+	G_TOUCHING = 1,
+	G_SENSOR = 4,
+	G_ENABLE_SENSOR_EVENTS = 0x10,
+	G_ENABLE_CONTACT_EVENTS = 0x20,
+};
+
+typedef struct gContact
+{
+	int id;
+	int colorIndex, localIndex;
+	gEdge edges[2];
+	int shapeIdA, shapeIdB;
+	uint32_t flags;
+	float friction, restitution;
+} gContact;
+
+typedef struct gJoint
+{
+	int id;
+	b2JointType type;
+	int bodyIdA, bodyIdB;
+	gEdge edges[2];
+	int colorIndex, localIndex;
+	bool collideConnected;
+	uint16_t revision;
+	void* userData;
+} gJoint;
+
+typedef struct gColor
+{
+	gBits bodySet;
+	gIntArray contacts;
+	gIntArray joints;
+} gColor;
+
+typedef struct gWorld
+{
+	bool inUse;
+	uint16_t revision;
+	int slot;
+
+	gIdPool bodyIds, shapeIds, contactIds, jointIds;
+	gBody* bodies;
+	int bodyCap;
+	gShape* shapes;
+	int shapeCap;
+	gContact* contacts;
+	int contactCap;
+	gJoint* joints;
+	int jointCap;
+
+	/* pinned host mirrors in device layout, indexed by id */
+	float* hState; /* 8 per body */
+	float* hXf;
+	float* hCenters;
+	float* hPrev;
+	float* hMass;
+	float* hForce;
+	float* hExtent;
+	int* hInfo;
+	int mirrorCap;
+	b2gShapeGeo* hGeo;
+	float* hAabb;
+	float* hFat;
+	int shapeMirrorCap;
+	b2gJointDev* hJoints;
+	int jointMirrorCap;
+
+	gIntArray awake;
+	gIntArray nonTouching;
+	gColor colors[B2G_COLORS];
+
+	gTree trees[3];
+	gIntArray moveArray;
+	gSet moveSet;
+	gSet pairSet;
+
+	/* step staging */
+	b2gContactInit* pending;
+	int pendingCount, pendingCap;
+	int* scratch;
+	int scratchCap;
+	gIntArray solveList;
+	gIntArray jointList;
+
+	b2gVec gravity;
+	float restitutionThreshold, pushout, hitThreshold, contactHertz, contactDamping, jointHertz, jointDamping;
+	float inv_h;
+	bool enableSleep, enableWarmStarting, enableContinuous, locked;
+
+	/* dirty / stale tracking */
+	bool bodiesDirty, awakeDirty, shapesDirty, shapeListsDirty, jointsDirty, solveDirty;
+	bool mirrorStale, shapeMirrorStale, jointMirrorStale;
+
+	b2ContactBeginTouchEvent* beginEvents;
+	int beginCount, beginCap;
+	b2ContactEndTouchEvent* endEvents;
+	int endCount, endCap;
+
+	b2Profile profile;
+	int status; /* last CUDA error or 0 */
+	int unsupportedToi;
+	int lastEventCount, lastRecordCount;
+
+	b2gDevWorld dev;
+	b2gHostIO io;
+} gWorld;
+
+gWorld* gworld_get( b2WorldId id );
+gWorld* gworld_slot( int slot );
+void gworld_fail( const char* what );
+
+void gworld_ensure_mirror( gWorld* w );
+void gworld_ensure_shape_mirror( gWorld* w );
+void gworld_reserve_mirrors( gWorld* w );
+void gworld_flush( gWorld* w );
+
+void gstep_run( gWorld* w, float dt, int subSteps );
+void gcontact_create( gWorld* w, gShape* a, gShape* b );
+void gcontact_destroy( gWorld* w, gContact* c );
+int gassign_joint_color( gWorld* w, int bodyIdA, int bodyIdB, bool staticA, bool staticB );
+void gbuffer_move( gWorld* w, int proxyKey );
+
+b2gBox gshape_geo_aabb( const b2gShapeGeo* g, b2gXf xf );
+void gbody_update_mass( gWorld* w, gBody* b );
+double b2g_now_ms( void );

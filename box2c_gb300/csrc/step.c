@@ -1,0 +1,709 @@
+/*
+ * step.c -- b2World_Step on the GB300: host bookkeeping around two device stages.
+ *
+ *   1. broadphase pairs (host trees, reference src/broad_phase.c:162-436) create contacts
+ *      in the reference order; their sim records are staged for the device;
+ *   2. device: contact creation + narrowphase over every live contact (kernels.cu);
+ *      meanwhile the host rebuilds the trees (src/dynamic_tree.c:1811-1925);
+ *   3. host: begin/end/disjoint events in ascending contact id, contact destruction and
+ *      graph colouring (src/world.c:489-667, src/constraint_graph.c:64-214);
+ *   4. device: the soft-step solver, colour by colour, and body finalisation;
+ *   5. host: proxy enlargement in awake order and the fast-body pass
+ *      (src/solver.c:1741-1954).
+ * Steps 3 and 5 only touch the few contacts and proxies whose state changed.
+ */
+#include "host.h"
+
+#include <string.h>
+
+#define PAIR_KEY( K1, K2 ) ( ( K1 ) < ( K2 ) ? (uint64_t)( K1 ) << 32 | (uint64_t)( K2 ) : (uint64_t)( K2 ) << 32 | (uint64_t)( K1 ) )
+
+/* ------------------------------------------------------------ event lists */
+static void push_begin( gWorld* w, int a, int b )
+{
+	if ( w->beginCount == w->beginCap )
+	{
+		w->beginCap = w->beginCap ? 2 * w->beginCap : 16;
+		w->beginEvents = realloc( w->beginEvents, sizeof( b2ContactBeginTouchEvent ) * (size_t)w->beginCap );
+	}
+	b2ContactBeginTouchEvent* e = w->beginEvents + w->beginCount++;
+	e->shapeIdA = ( b2ShapeId ){ a + 1, (uint16_t)w->slot, w->shapes[a].revision };
+	e->shapeIdB = ( b2ShapeId ){ b + 1, (uint16_t)w->slot, w->shapes[b].revision };
+}
+
+static void push_end( gWorld* w, int a, int b )
+{
+	if ( w->endCount == w->endCap )
+	{
+		w->endCap = w->endCap ? 2 * w->endCap : 16;
+		w->endEvents = realloc( w->endEvents, sizeof( b2ContactEndTouchEvent ) * (size_t)w->endCap );
+	}
+	b2ContactEndTouchEvent* e = w->endEvents + w->endCount++;
+	e->shapeIdA = ( b2ShapeId ){ a + 1, (uint16_t)w->slot, w->shapes[a].revision };
+	e->shapeIdB = ( b2ShapeId ){ b + 1, (uint16_t)w->slot, w->shapes[b].revision };
+}
+
+/* ------------------------------------------------------------ contacts */
+/* Contact records staged for the device, applied in order before the next narrowphase
+ * (creation, or retirement of a contact destroyed outside the narrowphase). */
+static b2gContactInit* push_pending( gWorld* w )
+{
+	if ( w->pendingCount == w->pendingCap )
+	{
+		w->pendingCap = w->pendingCap ? 2 * w->pendingCap : 256;
+		w->pending = (b2gContactInit*)realloc( w->pending, sizeof( b2gContactInit ) * (size_t)w->pendingCap );
+	}
+	return w->pending + w->pendingCount++;
+}
+
+/* Keeps only the last staged record of each contact id (ids can be freed and reused
+ * between two steps), so the device can apply them in parallel. */
+static int compact_pending( gWorld* w )
+{
+	int n = w->pendingCount;
+	int ids = w->contactIds.next > 0 ? w->contactIds.next : 1;
+	for ( int i = 0; i < n; ++i )
+		if ( w->pending[i].id + 1 > ids )
+			ids = w->pending[i].id + 1;
+	if ( ids > w->scratchCap )
+	{
+		w->scratch = (int*)realloc( w->scratch, sizeof( int ) * (size_t)ids );
+		w->scratchCap = ids;
+	}
+	for ( int i = 0; i < n; ++i )
+		w->scratch[w->pending[i].id] = i;
+	int m = 0;
+	for ( int i = 0; i < n; ++i )
+		if ( w->scratch[w->pending[i].id] == i )
+			w->pending[m++] = w->pending[i];
+	return m;
+}
+
+/* Registered shape pairs and primary order (reference src/contact.c:150-183). */
+static int registered( b2ShapeType a, b2ShapeType b, bool* primary )
+{
+	static const int table[5][5] = {
+		{ 1, -1, -1, -1, -1 }, { 1, 1, -1, -1, -1 }, { 1, 1, 0, 1, 0 }, { 1, 1, -1, 1, -1 }, { 1, 1, 0, 1, 0 },
+	};
+	int v = table[a][b];
+	if ( v == 0 )
+		return 0;
+	*primary = v > 0;
+	return 1;
+}
+
+void gcontact_create( gWorld* w, gShape* shapeA, gShape* shapeB )
+{
+	bool primary;
+	if ( registered( shapeA->type, shapeB->type, &primary ) == 0 )
+		return;
+	if ( primary == false )
+	{
+		gcontact_create( w, shapeB, shapeA );
+		return;
+	}
+	gBody* bodyA = w->bodies + shapeA->bodyId;
+	gBody* bodyB = w->bodies + shapeB->bodyId;
+	int id = gid_alloc( &w->contactIds );
+	if ( id + 1 > w->contactCap )
+	{
+		int nc = w->contactCap < 64 ? 64 : w->contactCap;
+		while ( nc < id + 1 )
+			nc *= 2;
+		w->contacts = (gContact*)realloc( w->contacts, sizeof( gContact ) * (size_t)nc );
+		for ( int i = w->contactCap; i < nc; ++i )
+			w->contacts[i].id = B2G_NULL;
+		w->contactCap = nc;
+	}
+	gContact* c = w->contacts + id;
+	memset( c, 0, sizeof( *c ) );
+	c->id = id;
+	c->colorIndex = B2G_NULL;
+	c->localIndex = w->nonTouching.count;
+	c->shapeIdA = shapeA->id;
+	c->shapeIdB = shapeB->id;
+	if ( shapeA->isSensor || shapeB->isSensor )
+		c->flags |= G_SENSOR;
+	if ( shapeA->enableSensorEvents || shapeB->enableSensorEvents )
+		c->flags |= G_ENABLE_SENSOR_EVENTS;
+	if ( shapeA->enableContactEvents || shapeB->enableContactEvents )
+		c->flags |= G_ENABLE_CONTACT_EVENTS;
+	c->friction = sqrtf( shapeA->friction * shapeB->friction );
+	c->restitution = shapeA->restitution > shapeB->restitution ? shapeA->restitution : shapeB->restitution;
+
+	c->edges[0].bodyId = shapeA->bodyId;
+	c->edges[0].prevKey = B2G_NULL;
+	c->edges[0].nextKey = bodyA->headContactKey;
+	int keyA = ( id << 1 ) | 0;
+	if ( bodyA->headContactKey != B2G_NULL )
+		w->contacts[bodyA->headContactKey >> 1].edges[bodyA->headContactKey & 1].prevKey = keyA;
+	bodyA->headContactKey = keyA;
+	bodyA->contactCount += 1;
+
+	c->edges[1].bodyId = shapeB->bodyId;
+	c->edges[1].prevKey = B2G_NULL;
+	c->edges[1].nextKey = bodyB->headContactKey;
+	int keyB = ( id << 1 ) | 1;
+	if ( bodyB->headContactKey != B2G_NULL )
+		w->contacts[bodyB->headContactKey >> 1].edges[bodyB->headContactKey & 1].prevKey = keyB;
+	bodyB->headContactKey = keyB;
+	bodyB->contactCount += 1;
+
+	gset_add( &w->pairSet, PAIR_KEY( (uint64_t)shapeA->id, (uint64_t)shapeB->id ) );
+	gia_push( &w->nonTouching, id );
+
+	b2gContactInit* init = push_pending( w );
+	init->id = id;
+	init->shapeA = shapeA->id;
+	init->shapeB = shapeB->id;
+	init->friction = c->friction;
+	init->restitution = c->restitution;
+	init->flags = 0;
+}
+
+static void remove_non_touching( gWorld* w, int localIndex )
+{
+	int moved = gia_remove_swap( &w->nonTouching, localIndex );
+	if ( moved != B2G_NULL )
+		w->contacts[w->nonTouching.data[localIndex]].localIndex = localIndex;
+}
+
+static void remove_from_graph( gWorld* w, int bodyIdA, int bodyIdB, int colorIndex, int localIndex )
+{
+	gColor* color = w->colors + colorIndex;
+	if ( colorIndex != B2G_OVERFLOW )
+	{
+		gbits_clear( &color->bodySet, bodyIdA );
+		gbits_clear( &color->bodySet, bodyIdB );
+	}
+	int moved = gia_remove_swap( &color->contacts, localIndex );
+	if ( moved != B2G_NULL )
+		w->contacts[color->contacts.data[localIndex]].localIndex = localIndex;
+	w->solveDirty = true;
+}
+
+static void unlink_edge( gWorld* w, gContact* c, int e )
+{
+	gEdge* edge = c->edges + e;
+	gBody* body = w->bodies + edge->bodyId;
+	if ( edge->prevKey != B2G_NULL )
+		w->contacts[edge->prevKey >> 1].edges[edge->prevKey & 1].nextKey = edge->nextKey;
+	if ( edge->nextKey != B2G_NULL )
+		w->contacts[edge->nextKey >> 1].edges[edge->nextKey & 1].prevKey = edge->prevKey;
+	int key = ( c->id << 1 ) | e;
+	if ( body->headContactKey == key )
+		body->headContactKey = edge->nextKey;
+	body->contactCount -= 1;
+}
+
+/* Reference src/contact.c:342-447.  The device record is retired by the narrowphase
+ * (disjoint) or ignored once its id is free. */
+void gcontact_destroy( gWorld* w, gContact* c )
+{
+	gset_remove( &w->pairSet, PAIR_KEY( (uint64_t)c->shapeIdA, (uint64_t)c->shapeIdB ) );
+	unlink_edge( w, c, 0 );
+	unlink_edge( w, c, 1 );
+	if ( c->colorIndex != B2G_NULL )
+		remove_from_graph( w, c->edges[0].bodyId, c->edges[1].bodyId, c->colorIndex, c->localIndex );
+	else
+		remove_non_touching( w, c->localIndex );
+	int id = c->id;
+	c->id = B2G_NULL;
+	c->colorIndex = B2G_NULL;
+	c->localIndex = B2G_NULL;
+	gid_free( &w->contactIds, id );
+	/* retire the device record before the next narrowphase */
+	b2gContactInit* kill = push_pending( w );
+	memset( kill, 0, sizeof( *kill ) );
+	kill->id = id;
+	kill->flags = B2G_INIT_KILL;
+}
+
+/* Greedy first-fit colouring keyed by body id (reference src/constraint_graph.c:64-183). */
+static void add_to_graph( gWorld* w, gContact* c )
+{
+	int colorIndex = B2G_OVERFLOW;
+	int a = c->edges[0].bodyId;
+	int b = c->edges[1].bodyId;
+	bool staticA = w->bodies[a].type == b2_staticBody;
+	bool staticB = w->bodies[b].type == b2_staticBody;
+	if ( staticA == false && staticB == false )
+	{
+		for ( int i = 0; i < B2G_OVERFLOW; ++i )
+		{
+			gBits* set = &w->colors[i].bodySet;
+			if ( gbits_get( set, a ) || gbits_get( set, b ) )
+				continue;
+			gbits_set( set, a );
+			gbits_set( set, b );
+			colorIndex = i;
+			break;
+		}
+	}
+	else if ( staticA == false )
+	{
+		for ( int i = 1; i < B2G_OVERFLOW; ++i )
+		{
+			gBits* set = &w->colors[i].bodySet;
+			if ( gbits_get( set, a ) )
+				continue;
+			gbits_set( set, a );
+			colorIndex = i;
+			break;
+		}
+	}
+	else if ( staticB == false )
+	{
+		for ( int i = 1; i < B2G_OVERFLOW; ++i )
+		{
+			gBits* set = &w->colors[i].bodySet;
+			if ( gbits_get( set, b ) )
+				continue;
+			gbits_set( set, b );
+			colorIndex = i;
+			break;
+		}
+	}
+	gColor* color = w->colors + colorIndex;
+	c->colorIndex = colorIndex;
+	c->localIndex = color->contacts.count;
+	gia_push( &color->contacts, c->id );
+	w->solveDirty = true;
+}
+
+/* ------------------------------------------------------------ broadphase pairs */
+typedef struct gPairList
+{
+	int* a;
+	int* b;
+	int count, capacity;
+} gPairList;
+
+typedef struct gQueryCtx
+{
+	gWorld* w;
+	gPairList* list;
+	int queryTreeType, queryProxyKey, queryShapeIndex;
+} gQueryCtx;
+
+static bool should_shapes_collide( b2Filter a, b2Filter b )
+{
+	if ( a.groupIndex == b.groupIndex && a.groupIndex != 0 )
+		return a.groupIndex > 0;
+	return ( a.maskBits & b.categoryBits ) != 0 && ( a.categoryBits & b.maskBits ) != 0;
+}
+
+static bool should_bodies_collide( gWorld* w, gBody* a, gBody* b )
+{
+	if ( a->type != b2_dynamicBody && b->type != b2_dynamicBody )
+		return false;
+	int key, other;
+	if ( a->jointCount < b->jointCount )
+	{
+		key = a->headJointKey;
+		other = b->id;
+	}
+	else
+	{
+		key = b->headJointKey;
+		other = a->id;
+	}
+	while ( key != B2G_NULL )
+	{
+		gJoint* j = w->joints + ( key >> 1 );
+		int e = key & 1;
+		if ( j->collideConnected == false && j->edges[e ^ 1].bodyId == other )
+			return false;
+		key = j->edges[e].nextKey;
+	}
+	return true;
+}
+
+static bool pair_query( int proxyId, int shapeId, void* context )
+{
+	gQueryCtx* q = (gQueryCtx*)context;
+	gWorld* w = q->w;
+	int proxyKey = ( proxyId << 2 ) | q->queryTreeType;
+	if ( proxyKey == q->queryProxyKey )
+		return true;
+	if ( q->queryTreeType != b2_staticBody )
+	{
+		bool moved = gset_contains( &w->moveSet, (uint64_t)( proxyKey + 1 ) );
+		if ( moved && proxyKey < q->queryProxyKey )
+			return true;
+	}
+	if ( gset_contains( &w->pairSet, PAIR_KEY( (uint64_t)shapeId, (uint64_t)q->queryShapeIndex ) ) )
+		return true;
+	int idA, idB;
+	if ( proxyKey < q->queryProxyKey )
+	{
+		idA = shapeId;
+		idB = q->queryShapeIndex;
+	}
+	else
+	{
+		idA = q->queryShapeIndex;
+		idB = shapeId;
+	}
+	gShape* sA = w->shapes + idA;
+	gShape* sB = w->shapes + idB;
+	if ( sA->bodyId == sB->bodyId )
+		return true;
+	if ( should_shapes_collide( sA->filter, sB->filter ) == false )
+		return true;
+	if ( sA->isSensor && sB->isSensor )
+		return true;
+	if ( should_bodies_collide( w, w->bodies + sA->bodyId, w->bodies + sB->bodyId ) == false )
+		return true;
+	gPairList* l = q->list;
+	if ( l->count == l->capacity )
+	{
+		l->capacity = l->capacity ? 2 * l->capacity : 16;
+		l->a = (int*)realloc( l->a, sizeof( int ) * (size_t)l->capacity );
+		l->b = (int*)realloc( l->b, sizeof( int ) * (size_t)l->capacity );
+	}
+	l->a[l->count] = idA;
+	l->b[l->count] = idB;
+	l->count += 1;
+	return true;
+}
+
+/* All moved proxies are queried before any contact is created; each proxy's pairs are
+ * then created in reverse discovery order (the reference prepends to a list). */
+static void update_pairs( gWorld* w )
+{
+	int moveCount = w->moveArray.count;
+	if ( moveCount == 0 )
+		return;
+	gPairList* lists = (gPairList*)calloc( (size_t)moveCount, sizeof( gPairList ) );
+	for ( int i = 0; i < moveCount; ++i )
+	{
+		int proxyKey = w->moveArray.data[i];
+		if ( proxyKey == B2G_NULL )
+			continue;
+		int proxyType = proxyKey & 3;
+		int proxyId = proxyKey >> 2;
+		const gTree* base = w->trees + proxyType;
+		b2gBox fat = base->nodes[proxyId].box;
+		gQueryCtx q;
+		q.w = w;
+		q.list = lists + i;
+		q.queryProxyKey = proxyKey;
+		q.queryShapeIndex = base->nodes[proxyId].userData;
+		if ( proxyType == b2_dynamicBody )
+		{
+			q.queryTreeType = b2_kinematicBody;
+			gtree_query( w->trees + b2_kinematicBody, fat, 0xFFFFFFFFu, pair_query, &q );
+			q.queryTreeType = b2_staticBody;
+			gtree_query( w->trees + b2_staticBody, fat, 0xFFFFFFFFu, pair_query, &q );
+		}
+		q.queryTreeType = b2_dynamicBody;
+		gtree_query( w->trees + b2_dynamicBody, fat, 0xFFFFFFFFu, pair_query, &q );
+	}
+	for ( int i = 0; i < moveCount; ++i )
+	{
+		gPairList* l = lists + i;
+		for ( int k = l->count - 1; k >= 0; --k )
+			gcontact_create( w, w->shapes + l->a[k], w->shapes + l->b[k] );
+		free( l->a );
+		free( l->b );
+	}
+	free( lists );
+	w->moveArray.count = 0;
+	gset_clear( &w->moveSet );
+}
+
+/* ------------------------------------------------------------ narrowphase events */
+static int cmp_int( const void* a, const void* b )
+{
+	int x = *(const int*)a, y = *(const int*)b;
+	return ( x > y ) - ( x < y );
+}
+
+static void process_events( gWorld* w, int count )
+{
+	int* ev = w->io.events;
+	qsort( ev, (size_t)count, sizeof( int ), cmp_int );
+	for ( int i = 0; i < count; ++i )
+	{
+		int id = ev[i] >> 2;
+		int code = ev[i] & 3;
+		gContact* c = w->contacts + id;
+		uint32_t flags = c->flags;
+		if ( code == B2G_EV_DISJOINT )
+		{
+			if ( ( flags & G_TOUCHING ) && ( flags & G_ENABLE_CONTACT_EVENTS ) )
+				push_end( w, c->shapeIdA, c->shapeIdB );
+			c->flags &= ~G_TOUCHING;
+			gcontact_destroy( w, c );
+		}
+		else if ( code == B2G_EV_STARTED )
+		{
+			if ( flags & G_SENSOR )
+				continue;
+			if ( flags & G_ENABLE_CONTACT_EVENTS )
+				push_begin( w, c->shapeIdA, c->shapeIdB );
+			c->flags |= G_TOUCHING;
+			int localIndex = c->localIndex;
+			add_to_graph( w, c );
+			remove_non_touching( w, localIndex );
+		}
+		else if ( code == B2G_EV_STOPPED )
+		{
+			if ( flags & G_SENSOR )
+				continue;
+			c->flags &= ~G_TOUCHING;
+			if ( c->flags & G_ENABLE_CONTACT_EVENTS )
+				push_end( w, c->shapeIdA, c->shapeIdB );
+			int a = c->edges[0].bodyId, b = c->edges[1].bodyId;
+			int colorIndex = c->colorIndex, localIndex = c->localIndex;
+			c->colorIndex = B2G_NULL;
+			c->localIndex = w->nonTouching.count;
+			gia_push( &w->nonTouching, id );
+			remove_from_graph( w, a, b, colorIndex, localIndex );
+		}
+	}
+}
+
+/* ------------------------------------------------------------ finalisation records */
+typedef struct gSweepCtx
+{
+	gWorld* w;
+	gShape* fast;
+	int hits;
+} gSweepCtx;
+
+/* Candidate filter of the fast-body sweep (reference src/solver.c:800-858).  Time of
+ * impact is not computed: a sweep that reaches it is counted in the world status. */
+static bool sweep_query( int proxyId, int shapeId, void* context )
+{
+	(void)proxyId;
+	gSweepCtx* q = (gSweepCtx*)context;
+	gWorld* w = q->w;
+	if ( shapeId == q->fast->id )
+		return true;
+	gShape* s = w->shapes + shapeId;
+	if ( s->bodyId == q->fast->bodyId )
+		return true;
+	if ( should_shapes_collide( q->fast->filter, s->filter ) == false )
+		return true;
+	if ( s->isSensor )
+		return true;
+	if ( w->bodies[s->bodyId].isBullet )
+		return true;
+	q->hits += 1;
+	return true;
+}
+
+static int cmp_record( const void* a, const void* b )
+{
+	const b2gRecord* x = (const b2gRecord*)a;
+	const b2gRecord* y = (const b2gRecord*)b;
+	if ( x->awakeIndex != y->awakeIndex )
+		return ( x->awakeIndex > y->awakeIndex ) - ( x->awakeIndex < y->awakeIndex );
+	return ( x->slot > y->slot ) - ( x->slot < y->slot );
+}
+
+static b2gBox box4( const float* f )
+{
+	b2gBox b;
+	b.lo = gv( f[0], f[1] );
+	b.hi = gv( f[2], f[3] );
+	return b;
+}
+
+static void process_records( gWorld* w, int count )
+{
+	b2gRecord* rec = w->io.records;
+	qsort( rec, (size_t)count, sizeof( b2gRecord ), cmp_record );
+	/* proxy enlargement and move buffer in awake order (reference src/solver.c:1741-1797) */
+	for ( int i = 0; i < count; ++i )
+	{
+		b2gRecord* r = rec + i;
+		gShape* s = w->shapes + r->shapeId;
+		if ( r->flags & B2G_R_ENLARGED )
+		{
+			memcpy( w->hFat + 4 * r->shapeId, r->fat, 16 );
+			gtree_enlarge_proxy( w->trees + ( s->proxyKey & 3 ), s->proxyKey >> 2, box4( r->fat ) );
+			gbuffer_move( w, s->proxyKey );
+		}
+		else if ( r->flags & B2G_R_FAST )
+		{
+			gbuffer_move( w, s->proxyKey );
+		}
+	}
+	/* fast shapes: sweep candidates, then enlarge in the dynamic tree (src/solver.c:1807-1954) */
+	for ( int i = 0; i < count; ++i )
+	{
+		b2gRecord* r = rec + i;
+		if ( ( r->flags & B2G_R_FAST ) == 0 )
+			continue;
+		gShape* s = w->shapes + r->shapeId;
+		if ( s->isSensor == false )
+		{
+			gSweepCtx q = { w, s, 0 };
+			b2gBox sweep = box4( r->sweep );
+			gtree_query( w->trees + b2_staticBody, sweep, 0xFFFFFFFFu, sweep_query, &q );
+			if ( r->flags & B2G_R_BULLET )
+			{
+				gtree_query( w->trees + b2_kinematicBody, sweep, 0xFFFFFFFFu, sweep_query, &q );
+				gtree_query( w->trees + b2_dynamicBody, sweep, 0xFFFFFFFFu, sweep_query, &q );
+			}
+			w->unsupportedToi += q.hits;
+		}
+		if ( r->flags & B2G_R_FAST_ENLARGED )
+		{
+			memcpy( w->hFat + 4 * r->shapeId, r->fat, 16 );
+			gtree_enlarge_proxy( w->trees + b2_dynamicBody, s->proxyKey >> 2, box4( r->fat ) );
+		}
+	}
+}
+
+/* ------------------------------------------------------------ step */
+static void make_soft( float hertz, float zeta, float h, float* out )
+{
+	if ( hertz == 0.0f )
+	{
+		out[0] = 0.0f;
+		out[1] = 1.0f;
+		out[2] = 0.0f;
+		return;
+	}
+	float omega = 2.0f * B2G_PI * hertz;
+	float a1 = 2.0f * zeta + h * omega;
+	float a2 = h * omega * a1;
+	float a3 = 1.0f / ( 1.0f + a2 );
+	out[0] = omega / a1;
+	out[1] = a2 * a3;
+	out[2] = a3;
+}
+
+static void build_solve_lists( gWorld* w, b2gSolvePlan* plan )
+{
+	w->solveList.count = 0;
+	w->jointList.count = 0;
+	plan->activeCount = 0;
+	for ( int c = 0; c < B2G_COLORS; ++c )
+	{
+		plan->colorStart[c] = w->solveList.count;
+		plan->jointStart[c] = w->jointList.count;
+		gIntArray* ca = &w->colors[c].contacts;
+		gIntArray* ja = &w->colors[c].joints;
+		for ( int k = 0; k < ca->count; ++k )
+			gia_push( &w->solveList, ca->data[k] );
+		for ( int k = 0; k < ja->count; ++k )
+			gia_push( &w->jointList, ja->data[k] );
+		if ( c < B2G_OVERFLOW && ca->count + ja->count > 0 )
+			plan->active[plan->activeCount++] = c;
+	}
+	plan->colorStart[B2G_COLORS] = w->solveList.count;
+	plan->jointStart[B2G_COLORS] = w->jointList.count;
+}
+
+void gstep_run( gWorld* w, float dt, int subSteps )
+{
+	double t0 = b2g_now_ms();
+	update_pairs( w );
+	double t1 = b2g_now_ms();
+	w->profile.pairs = (float)( t1 - t0 );
+
+	int idCount = w->contactIds.next;
+	int e = b2gd_reserve( &w->dev, &w->io, w->bodyIds.next, w->shapeIds.next, idCount, w->jointIds.next, idCount, w->shapeIds.next );
+	if ( e )
+	{
+		w->status = e;
+		return;
+	}
+	int staged = compact_pending( w );
+	if ( staged > 0 )
+		memcpy( w->io.newContacts, w->pending, sizeof( b2gContactInit ) * (size_t)staged );
+	w->pendingCount = 0;
+	e = b2gd_collide( &w->dev, &w->io, staged, idCount );
+	/* the tree rebuild overlaps the device narrowphase (reference src/world.c:420) */
+	gtree_rebuild( w->trees + b2_dynamicBody );
+	gtree_rebuild( w->trees + b2_kinematicBody );
+	e |= b2gd_sync( &w->dev );
+	if ( e )
+	{
+		w->status = e;
+		return;
+	}
+	int eventCount = w->io.counters[0];
+	w->lastEventCount = eventCount;
+	process_events( w, eventCount < w->dev.eventCap ? eventCount : w->dev.eventCap );
+	double t2 = b2g_now_ms();
+	w->profile.collide = (float)( t2 - t1 );
+
+	if ( dt <= 0.0f )
+		return;
+
+	b2gStepConst sc;
+	memset( &sc, 0, sizeof( sc ) );
+	sc.subSteps = subSteps < 1 ? 1 : subSteps;
+	sc.dt = dt;
+	sc.inv_dt = 1.0f / dt;
+	sc.h = dt / (float)sc.subSteps;
+	sc.inv_h = (float)sc.subSteps * sc.inv_dt;
+	w->inv_h = sc.inv_h;
+	float contactHertz = gmin( w->contactHertz, 0.25f * sc.inv_h );
+	float jointHertz = gmin( w->jointHertz, 0.125f * sc.inv_h );
+	make_soft( contactHertz, w->contactDamping, sc.h, sc.contactSoft );
+	make_soft( 2.0f * contactHertz, w->contactDamping, sc.h, sc.staticSoft );
+	make_soft( jointHertz, w->jointDamping, sc.h, sc.jointSoft );
+	sc.restitutionThreshold = w->restitutionThreshold;
+	sc.pushout = w->pushout;
+	sc.gravity = w->gravity;
+	sc.enableWarmStarting = w->enableWarmStarting;
+	sc.enableContinuous = w->enableContinuous;
+	sc.enableSleep = w->enableSleep;
+
+	if ( w->awake.count == 0 )
+		return;
+
+	b2gSolvePlan plan;
+	build_solve_lists( w, &plan );
+	plan.awakeCount = w->awake.count;
+	if ( w->solveDirty )
+	{
+		e = b2gd_upload_solve_lists( &w->dev, w->solveList.data, w->solveList.count, w->jointList.data, w->jointList.count );
+		w->solveDirty = false;
+	}
+	e |= b2gd_solve( &w->dev, &w->io, &plan, &sc );
+	e |= b2gd_sync( &w->dev );
+	if ( e )
+	{
+		w->status = e;
+		return;
+	}
+	double t3 = b2g_now_ms();
+	w->profile.solve = (float)( t3 - t2 );
+	int recordCount = w->io.counters[1];
+	w->lastRecordCount = recordCount;
+	process_records( w, recordCount < w->dev.recordCap ? recordCount : w->dev.recordCap );
+	w->profile.broadphase = (float)( b2g_now_ms() - t3 );
+}
+
+void b2World_Step( b2WorldId worldId, float timeStep, int subStepCount )
+{
+	gWorld* w = gworld_get( worldId );
+	if ( w->locked )
+		return;
+	w->beginCount = 0;
+	w->endCount = 0;
+	memset( &w->profile, 0, sizeof( w->profile ) );
+	if ( timeStep == 0.0f )
+		return;
+	double t0 = b2g_now_ms();
+	w->locked = true;
+	b2gd_mark( &w->dev, 0 );
+	gworld_flush( w );
+	gstep_run( w, timeStep, subStepCount );
+	b2gd_mark( &w->dev, 6 );
+	w->mirrorStale = true;
+	w->shapeMirrorStale = true;
+	w->jointMirrorStale = true;
+	w->locked = false;
+	w->profile.step = (float)( b2g_now_ms() - t0 );
+	if ( w->status )
+		gworld_fail( b2gd_last_error() );
+}

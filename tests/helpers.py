@@ -1,0 +1,43 @@
+"""Step-by-step comparison of two box2d backends on the same seeded scene."""
+import numpy as np
+
+from box2c_gb300.capi import contact_table
+
+
+def state_bits(backend, world):
+    b = backend.bodies(world)
+    return b, b.view(np.uint32)
+
+
+def lockstep(a, b, make, steps, dt=1.0 / 60.0, substeps=4, check_manifolds=False):
+    """Steps both backends; returns (first mismatching step or None, detail, worst rel err)."""
+    wa, wb = make(a), make(b)
+    worst = 0.0
+    try:
+        for s in range(steps + 1):
+            ba, ua = state_bits(a, wa)
+            bb, ub = state_bits(b, wb)
+            ta, tb = contact_table(a.contacts(wa)), contact_table(b.contacts(wb))
+            if ta.shape != tb.shape or not np.array_equal(ta, tb):
+                return s, "contact set / colours differ", worst
+            if not np.array_equal(ua, ub):
+                m = np.isfinite(ba) & np.isfinite(bb)
+                rel = np.abs(ba[m] - bb[m]) / np.maximum(np.abs(bb[m]), 1.0)
+                worst = max(worst, float(rel.max()))
+                return s, f"body state differs (max rel {rel.max():.3e})", worst
+            if check_manifolds:
+                ca, cb = a.contacts(wa), b.contacts(wb)
+                for f in ("normal",):
+                    if not np.array_equal(ca[f].view(np.uint32), cb[f].view(np.uint32)):
+                        return s, "manifold normals differ", worst
+                pa, pb = ca["points"], cb["points"]
+                for f in ("anchorA", "anchorB", "separation", "normalImpulse", "tangentImpulse"):
+                    if not np.array_equal(pa[f].view(np.uint32), pb[f].view(np.uint32)):
+                        return s, f"manifold {f} differs", worst
+            if s < steps:
+                a.step(wa, dt, substeps)
+                b.step(wb, dt, substeps)
+        return None, "bit-exact", worst
+    finally:
+        a.destroy(wa)
+        b.destroy(wb)

@@ -1,0 +1,61 @@
+"""The C-ABI library builds, loads without a GPU, and exports every function declared in
+include/box2d/*.h (no compute call is made here)."""
+import ctypes as C
+import os
+import re
+
+import pytest
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+INC = os.path.join(REPO, "include", "box2d")
+
+
+def declared_functions():
+    names = set()
+    for f in sorted(os.listdir(INC)):
+        text = open(os.path.join(INC, f)).read()
+        # B2_API declarations and the plain prototypes of inspect.h / gpu.h
+        for m in re.finditer(r"B2_API\s+[\w\s\*]+?\b(b2\w+)\s*\(", text):
+            names.add(m.group(1))
+        if f in ("inspect.h", "gpu.h"):
+            for m in re.finditer(r"^\s*(?:int|void|float|bool|b2\w+)\s*\*?\s*(b2\w+)\s*\(", text, re.M):
+                names.add(m.group(1))
+    return sorted(names)
+
+
+@pytest.fixture(scope="module")
+def lib():
+    import box2c_gb300
+    path = box2c_gb300.build()
+    return C.CDLL(path, mode=os.RTLD_LOCAL | os.RTLD_NOW)
+
+
+def test_headers_declare_the_step_path():
+    names = declared_functions()
+    for required in ("b2CreateWorld", "b2World_Step", "b2CreateBody", "b2CreatePolygonShape",
+                     "b2CreateRevoluteJoint", "b2Body_GetPosition", "b2World_InspectContacts"):
+        assert required in names
+
+
+def test_every_declared_symbol_is_exported(lib):
+    missing = [n for n in declared_functions() if not hasattr(lib, n)]
+    assert missing == [], f"not exported: {missing}"
+
+
+def test_no_device_means_no_world(lib):
+    """Without a GPU the library refuses to create a world instead of falling back."""
+    lib.b2gd_device_ok.restype = C.c_int
+    if lib.b2gd_device_ok():
+        pytest.skip("a GPU is visible")
+    from box2c_gb300.capi import WorldId
+
+    class WorldDef(C.Structure):
+        _fields_ = [("gx", C.c_float), ("gy", C.c_float)] + [(f"f{i}", C.c_float) for i in range(7)] + \
+                   [("s", C.c_bool), ("c", C.c_bool), ("wc", C.c_int32), ("e", C.c_void_p), ("fi", C.c_void_p),
+                    ("u", C.c_void_p), ("iv", C.c_int32)]
+    lib.b2DefaultWorldDef.restype = WorldDef
+    lib.b2CreateWorld.restype = WorldId
+    lib.b2CreateWorld.argtypes = [C.c_void_p]
+    d = lib.b2DefaultWorldDef()
+    w = lib.b2CreateWorld(C.byref(d))
+    assert w.index1 == 0

@@ -1,0 +1,139 @@
+"""The plain-C oracle against the reference: known answers from the reference's own
+unit tests, golden vectors produced by the reference build, and (where the reference
+sources are present) step-by-step lockstep with the reference itself."""
+import ctypes as C
+import hashlib
+import math
+import os
+
+import numpy as np
+import pytest
+
+from box2c_gb300.capi import Vec2, Transform, Rot, contact_table
+from tests.golden.make_golden import SCENES, make_scene, digest
+from tests.golden.shapes import Manifold, random_pairs, manifold_array
+from tests.helpers import lockstep
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+FLT_EPS = float(np.finfo(np.float32).eps)
+
+
+class SegDist(C.Structure):
+    _fields_ = [("closest1", Vec2), ("closest2", Vec2), ("fraction1", C.c_float), ("fraction2", C.c_float),
+                ("distanceSquared", C.c_float)]
+
+
+def test_segment_distance_kat(oracle):
+    # reference test/test_distance.c:11-29
+    f = oracle.lib.b2SegmentDistance
+    f.restype = SegDist
+    f.argtypes = [Vec2, Vec2, Vec2, Vec2]
+    r = f(Vec2(-1, -1), Vec2(-1, 1), Vec2(2, 0), Vec2(1, 0))
+    assert abs(r.fraction1 - 0.5) <= FLT_EPS and abs(r.fraction2 - 1.0) <= FLT_EPS
+    assert abs(r.closest1.x + 1) <= FLT_EPS and abs(r.closest1.y) <= FLT_EPS
+    assert abs(r.closest2.x - 1) <= FLT_EPS and abs(r.closest2.y) <= FLT_EPS
+    assert abs(r.distanceSquared - 4) <= FLT_EPS
+
+
+class MassData(C.Structure):
+    _fields_ = [("mass", C.c_float), ("center", Vec2), ("rotationalInertia", C.c_float)]
+
+
+def test_mass_kat(oracle):
+    # reference test/test_shape.c:18-70: circle at (1,0) r=1, box 1x1 half extents
+    from tests.golden.shapes import Circle, _box
+    L = oracle.lib
+    L.b2ComputeCircleMass.restype = MassData
+    L.b2ComputeCircleMass.argtypes = [C.c_void_p, C.c_float]
+    c = Circle(Vec2(1.0, 0.0), 1.0)
+    md = L.b2ComputeCircleMass(C.addressof(c), 1.0)
+    assert abs(np.float32(md.mass) - np.float32(math.pi)) <= FLT_EPS
+    assert md.center.x == 1.0 and md.center.y == 0.0
+    assert abs(np.float32(md.rotationalInertia) - np.float32(1.5) * np.float32(math.pi)) <= FLT_EPS
+    L.b2ComputePolygonMass.restype = MassData
+    L.b2ComputePolygonMass.argtypes = [C.c_void_p, C.c_float]
+    box = _box(1.0, 1.0)
+    md = L.b2ComputePolygonMass(C.addressof(box), 1.0)
+    assert abs(md.mass - 4.0) <= FLT_EPS
+    assert abs(md.center.x) <= FLT_EPS and abs(md.center.y) <= FLT_EPS
+    assert abs(np.float32(md.rotationalInertia) - np.float32(8.0) / np.float32(3.0)) <= 2 * FLT_EPS
+
+
+def test_manifold_golden(oracle):
+    golden = np.load(os.path.join(GOLDEN, "manifolds.npz"))["outputs"]
+    pairs = random_pairs(seed=7, count=len(golden))
+    for k, (kind, a, xa, b, xb) in enumerate(pairs):
+        fn = getattr(oracle.lib, kind)
+        fn.restype = Manifold
+        fn.argtypes = [C.c_void_p, Transform, C.c_void_p, Transform]
+        got = manifold_array(fn(C.addressof(a), xa, C.addressof(b), xb))
+        assert np.array_equal(got.view(np.uint32), golden[k].view(np.uint32)), (k, kind, got, golden[k])
+
+
+@pytest.mark.parametrize("name", list(SCENES))
+def test_scene_golden(oracle, name):
+    """Per-step bit-exact body state and contact table against the reference's hashes."""
+    g = np.load(os.path.join(GOLDEN, "scenes.npz"))
+    steps, snaps = SCENES[name]
+    bh, ch = g[f"{name}/body_hash"], g[f"{name}/contact_hash"]
+    w = make_scene(oracle, name)
+    try:
+        for s in range(steps + 1):
+            bodies = oracle.bodies(w)
+            assert digest(contact_table(oracle.contacts(w))) == ch[s], f"{name}: contact table differs at step {s}"
+            if digest(bodies.view(np.uint32)) != bh[s]:
+                snap = [k for k in snaps if k >= s]
+                msg = f"{name}: body state differs at step {s}"
+                pytest.fail(msg)
+            if s in snaps:
+                assert np.array_equal(bodies.view(np.uint32), g[f"{name}/bodies_{s}"].view(np.uint32))
+            if s < steps:
+                oracle.step(w)
+    finally:
+        oracle.destroy(w)
+
+
+def test_hello_world(oracle):
+    # reference test/test_world.c:17-97
+    w, body = oracle.hello_world()
+    oracle.step(w, count=90)
+    p = oracle.lib.b2Body_GetPosition(body)
+    q = oracle.lib.b2Body_GetRotation(body)
+    oracle.destroy(w)
+    assert abs(p.x) < 0.01 and abs(p.y - 1.0) < 0.01 and abs(math.atan2(q.s, q.c)) < 0.01
+
+
+def test_determinism_repeat(oracle):
+    # reference test/test_determinism.c:179-202: the same scene twice is bit-identical
+    finals = []
+    for _ in range(2):
+        w = oracle.tilted_stacks()
+        oracle.step(w, dt=1 / 60, substeps=3, count=100)
+        finals.append(oracle.bodies(w).copy())
+        oracle.destroy(w)
+    assert np.array_equal(finals[0].view(np.uint32), finals[1].view(np.uint32))
+
+
+@pytest.mark.parametrize("scene,steps", [("pyramid20", 120), ("tumbler", 120), ("tumbler_ref", 60), ("tilted", 100)])
+def test_lockstep_reference(oracle, reference, scene, steps):
+    make = {
+        "pyramid20": lambda b: b.pyramid(20),
+        "tumbler": lambda b: b.tumbler(1200, 99, 0),
+        "tumbler_ref": lambda b: b.tumbler(0, 0, 1),
+        "tilted": lambda b: b.tilted_stacks(),
+    }[scene]
+    step, detail, _ = lockstep(reference, oracle, make, steps, check_manifolds=True)
+    assert step is None, f"{scene}: {detail} at step {step}"
+
+
+def test_fp64_oracle_tracks_fp32(oracle, oracle64):
+    """The FP64 build runs the same step; on a short drop it stays within 1e-4 of FP32."""
+    h = [1.2, 2.0, 3.1, 4.5]
+    w32 = oracle.drop_boxes(h, [0.3, -0.2, 0.1, 0.0], [0.0, 0.5, -1.0, 0.2], 0.6)
+    w64 = oracle64.drop_boxes(h, [0.3, -0.2, 0.1, 0.0], [0.0, 0.5, -1.0, 0.2], 0.6)
+    oracle.step(w32, count=30)
+    oracle64.step(w64, count=30)
+    a, b = oracle.bodies(w32), oracle64.bodies(w64)
+    oracle.destroy(w32)
+    oracle64.destroy(w64)
+    assert np.nanmax(np.abs(a[:, :2] - b[:, :2])) < 1e-3
