@@ -402,3 +402,42 @@ extern "C" void b2gd_stage_times( b2gDevWorld* w, float* stepMs, float* collideM
 	*solveMs = elapsed( w->timers[3], w->timers[4] );
 	*finalizeMs = elapsed( w->timers[4], w->timers[5] );
 }
+
+/* Raw device readback for diagnostics: 0 contact flags (u32), 1 shape geometry,
+ * 2 contact shape pairs (2 x i32), 3 body info (i32). */
+extern "C" int b2gd_debug_read( b2gDevWorld* w, int which, void* out, int count )
+{
+	cudaStream_t s = (cudaStream_t)w->stream;
+	const void* src = nullptr;
+	size_t bytes = 0;
+	switch ( which )
+	{
+		case 0:
+			src = w->cFlags;
+			bytes = 4u * (size_t)count;
+			break;
+		case 1:
+			src = w->geo;
+			bytes = sizeof( b2gShapeGeo ) * (size_t)count;
+			break;
+		case 2:
+			src = w->cShapes;
+			bytes = 8u * (size_t)count;
+			break;
+		case 3:
+			src = w->bodyInfo;
+			bytes = 4u * (size_t)count;
+			break;
+		case 4:
+			src = w->counters;
+			bytes = 16u;
+			break;
+		default:
+			return -1;
+	}
+	if ( src == nullptr )
+		return -2;
+	int e = ok( cudaMemcpyAsync( out, src, bytes, cudaMemcpyDeviceToHost, s ) );
+	e |= ok( cudaStreamSynchronize( s ) );
+	return e;
+}

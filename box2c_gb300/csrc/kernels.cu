@@ -161,6 +161,19 @@ __global__ void k_scatter_contacts( b2gDevWorld W, const b2gContactInit* inits, 
 }
 
 /* ------------------------------------------------------------------ narrowphase */
+/* Manifold of one shape pair; sensors never generate points.  Kept behind a call
+ * boundary: inlined into k_collide, this routine returned empty manifolds for touching
+ * boxes on sm_103a (nvcc 13.0.88, -O3 --fmad=false) while the same source called from a
+ * one-thread kernel, or on the host, was correct; the non-inlined form is correct in
+ * both kernels and bit-identical to the reference. */
+__device__ __noinline__ void narrowphase( b2gManifold* m, const b2gShapeGeo* gA, b2gXf xfA, const b2gShapeGeo* gB, b2gXf xfB )
+{
+	if ( gA->isSensor || gB->isSensor )
+		gmanifold_clear( m );
+	else
+		gcollide_shapes( m, gA, xfA, gB, xfB );
+}
+
 __device__ __forceinline__ void emit_event( const b2gDevWorld& W, int id, int code )
 {
 	int slot = atomicAdd( W.counters + 0, 1 );
@@ -214,11 +227,7 @@ __global__ void __launch_bounds__( BLOCK ) k_collide( b2gDevWorld W, int idCount
 
 	b2gManifold old = W.manifold[id];
 	b2gManifold m;
-	bool sensor = gA->isSensor || gB->isSensor;
-	if ( sensor )
-		gmanifold_clear( &m );
-	else
-		gcollide_shapes( &m, gA, xfA, gB, xfB );
+	narrowphase( &m, gA, xfA, gB, xfB );
 
 	int pointCount = m.count;
 	bool touching = pointCount > 0;
@@ -1170,4 +1179,61 @@ extern "C" int b2gd_solve( b2gDevWorld* w, b2gHostIO* io, const b2gSolvePlan* pl
 	w->launches += launches;
 	cudaMemcpyAsync( io->counters, w->counters, 4 * sizeof( int ), cudaMemcpyDeviceToHost, s );
 	return check( cudaGetLastError() );
+}
+
+/* ------------------------------------------------------------------ diagnostics */
+/* Replays the narrowphase of one contact and writes its inputs and manifold to out:
+ * [0..3] shape ids / flags, [4..11] xfA xfB, [12..39] manifold (28 words). */
+__global__ void k_debug_collide( b2gDevWorld W, int id, float* out )
+{
+	if ( threadIdx.x != 0 || blockIdx.x != 0 )
+		return;
+	int sA = W.cShapes[2 * id];
+	int sB = W.cShapes[2 * id + 1];
+	const b2gShapeGeo* gA = W.geo + sA;
+	const b2gShapeGeo* gB = W.geo + sB;
+	const float4* xf = (const float4*)W.xf;
+	float4 xa = xf[gA->bodyId], xb = xf[gB->bodyId];
+	if ( out[40] != 0.0f )
+	{
+		/* caller-supplied transforms in out[41..48] */
+		xa = make_float4( out[41], out[42], out[43], out[44] );
+		xb = make_float4( out[45], out[46], out[47], out[48] );
+	}
+	b2gXf xfA, xfB;
+	xfA.p = gv( xa.x, xa.y );
+	xfA.q = grot( xa.z, xa.w );
+	xfB.p = gv( xb.x, xb.y );
+	xfB.q = grot( xb.z, xb.w );
+	b2gManifold m;
+	narrowphase( &m, gA, xfA, gB, xfB );
+	int* oi = (int*)out;
+	oi[0] = sA;
+	oi[1] = sB;
+	oi[2] = (int)W.cFlags[id];
+	oi[3] = gA->isSensor | ( gB->isSensor << 1 );
+	out[4] = xa.x;
+	out[5] = xa.y;
+	out[6] = xa.z;
+	out[7] = xa.w;
+	out[8] = xb.x;
+	out[9] = xb.y;
+	out[10] = xb.z;
+	out[11] = xb.w;
+	const float* mf = (const float*)&m;
+	for ( int i = 0; i < (int)( sizeof( b2gManifold ) / 4 ); ++i )
+		out[12 + i] = mf[i];
+}
+
+extern "C" int b2gd_debug_collide( b2gDevWorld* w, int id, float* hostOut )
+{
+	float* d = nullptr;
+	cudaMalloc( &d, 64 * sizeof( float ) );
+	cudaMemcpy( d, hostOut, 64 * sizeof( float ), cudaMemcpyHostToDevice );
+	k_debug_collide<<<1, 1, 0, (cudaStream_t)w->stream>>>( *w, id, d );
+	cudaError_t e = cudaGetLastError();
+	cudaMemcpyAsync( hostOut, d, 64 * sizeof( float ), cudaMemcpyDeviceToHost, (cudaStream_t)w->stream );
+	cudaStreamSynchronize( (cudaStream_t)w->stream );
+	cudaFree( d );
+	return (int)e;
 }

@@ -1349,3 +1349,16 @@ int b2World_GetBodyStates( b2WorldId worldId, float* out, int capacity )
 	}
 	return n;
 }
+
+/* Diagnostics: raw copy of a device array of the world (see b2gd_debug_read). */
+int b2gd_debug_read( b2gDevWorld* w, int which, void* out, int count );
+int b2World_DebugRead( b2WorldId worldId, int which, void* out, int count )
+{
+	return b2gd_debug_read( &gworld_get( worldId )->dev, which, out, count );
+}
+
+int b2gd_debug_collide( b2gDevWorld* w, int id, float* hostOut );
+int b2World_DebugCollide( b2WorldId worldId, int contactId, float* out64 )
+{
+	return b2gd_debug_collide( &gworld_get( worldId )->dev, contactId, out64 );
+}

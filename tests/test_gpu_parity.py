@@ -64,16 +64,18 @@ def test_gpu_hello_world(gpu):
     assert abs(p.x) < 0.01 and abs(p.y - 1.0) < 0.01 and abs(math.atan2(q.s, q.c)) < 0.01
 
 
-def test_gpu_large_pyramid_properties(gpu):
-    """Full-size workload (100 rows, 5050 boxes): counts, no NaN, the pyramid stands."""
-    w = gpu.pyramid(100, 0.01, 1235)
-    gpu.step(w, count=200)
-    c = gpu.counters(w)
-    b = gpu.bodies(w)
-    gpu.destroy(w)
-    assert c.bodyCount == 5051
-    assert np.isfinite(b).all()
-    assert sum(c.colorCounts) > 14000
-    top = b[1:, 1].max()
-    assert top > 99.0, top
-    assert gpu.lib.b2World_GetStatus if hasattr(gpu.lib, "b2World_GetStatus") else True
+def test_gpu_large_pyramid_full_size(gpu, oracle):
+    """Full-size workload (100 rows, 5050 boxes, 500 steps): the GPU state equals the
+    oracle's bit for bit at the end; counts and colours match; nothing is NaN."""
+    wg, wo = gpu.pyramid(100, 0.01, 1235), oracle.pyramid(100, 0.01, 1235)
+    gpu.step(wg, count=500)
+    oracle.step(wo, count=500)
+    cg, co = gpu.counters(wg), oracle.counters(wo)
+    bg, bo = gpu.bodies(wg), oracle.bodies(wo)
+    tg, to = contact_table(gpu.contacts(wg)), contact_table(oracle.contacts(wo))
+    gpu.destroy(wg)
+    oracle.destroy(wo)
+    assert cg.bodyCount == 5051 and list(cg.colorCounts) == list(co.colorCounts)
+    assert np.isfinite(bg).all()
+    assert np.array_equal(tg, to)
+    assert np.array_equal(bg.view(np.uint32), bo.view(np.uint32))
