@@ -219,3 +219,34 @@ def finite_max_rel(a: np.ndarray, b: np.ndarray, floor: float = 1.0) -> float:
 __all__ = ["Vec2", "Rot", "Transform", "WorldId", "BodyId", "Counters", "Profile",
            "InspectContact", "InspectShape", "InspectPoint", "Backend", "contact_table",
            "finite_max_rel", "BODY_FLOATS", "math"]
+
+
+class ManifoldPoint(C.Structure):
+    _fields_ = [("point", Vec2), ("anchorA", Vec2), ("anchorB", Vec2), ("separation", C.c_float),
+                ("normalImpulse", C.c_float), ("tangentImpulse", C.c_float),
+                ("maxNormalImpulse", C.c_float), ("normalVelocity", C.c_float),
+                ("id", C.c_uint16), ("persisted", C.c_bool)]
+
+
+class Manifold(C.Structure):
+    _fields_ = [("points", ManifoldPoint * 2), ("normal", Vec2), ("pointCount", C.c_int32)]
+
+
+MANIFOLD_BYTES = C.sizeof(Manifold)
+
+
+class ContactSolveDesc(C.Structure):
+    """include/box2d/gpu.h b2ContactSolveDesc."""
+    _fields_ = [("states", C.c_void_p), ("massData", C.c_void_p), ("forces", C.c_void_p),
+                ("damping", C.c_void_p), ("bodies", C.c_void_p), ("bodyCount", C.c_int32),
+                ("contactBodies", C.c_void_p), ("contactMix", C.c_void_p), ("manifolds", C.c_void_p),
+                ("contactCount", C.c_int32), ("colorStart", C.c_int32 * 13),
+                ("timeStep", C.c_float), ("subStepCount", C.c_int32), ("gravity", Vec2),
+                ("contactHertz", C.c_float), ("contactDampingRatio", C.c_float),
+                ("contactPushout", C.c_float), ("restitutionThreshold", C.c_float),
+                ("enableWarmStarting", C.c_bool), ("stream", C.c_void_p)]
+
+
+def bind_solve_api(lib: C.CDLL) -> None:
+    lib.b2SolveContacts.argtypes = [C.POINTER(ContactSolveDesc)]
+    lib.b2SolveContacts.restype = C.c_int

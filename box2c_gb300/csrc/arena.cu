@@ -117,7 +117,6 @@ extern "C" void b2gd_free( b2gDevWorld* w, b2gHostIO* io )
 	FREE_DEV( w->cMix );
 	FREE_DEV( w->cFlags );
 	FREE_DEV( w->cBodies );
-	FREE_DEV( w->cMass );
 	FREE_DEV( w->manifold );
 	FREE_DEV( w->solveList );
 	FREE_DEV( w->jointList );
@@ -202,7 +201,6 @@ extern "C" int b2gd_reserve( b2gDevWorld* w, b2gHostIO* io, int bodyCap, int sha
 		e |= grow( (void**)&w->cMix, 8u * o, 8u * n, s );
 		e |= grow( (void**)&w->cFlags, 4u * o, 4u * n, s );
 		e |= grow( (void**)&w->cBodies, 8u * o, 8u * n, s );
-		e |= grow( &w->cMass, 16u * o, 16u * n, s );
 		e |= grow( (void**)&w->manifold, sizeof( b2gManifold ) * o, sizeof( b2gManifold ) * n, s );
 		e |= grow_host_mapped( (void**)&io->events, (void**)&w->events, 4u * n );
 		w->eventCap = nc;

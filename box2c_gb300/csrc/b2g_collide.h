@@ -48,7 +48,6 @@ B2G_HD void gmanifold_clear( b2gManifold* m )
 	}
 	m->normal = gv( 0.0f, 0.0f );
 	m->count = 0;
-	m->pad = 0;
 }
 
 B2G_HD b2gSegDist gsegment_distance( b2gVec p1, b2gVec q1, b2gVec p2, b2gVec q2 )

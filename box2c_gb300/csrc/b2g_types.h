@@ -37,21 +37,21 @@ typedef struct b2gShapeGeo
 
 typedef struct b2gPoint
 {
-	b2gVec anchorA, anchorB, point;
+	b2gVec point, anchorA, anchorB;
 	float separation, normalImpulse, tangentImpulse, maxNormalImpulse, normalVelocity;
 	uint16_t id;
 	uint8_t persisted;
 	uint8_t pad;
 } b2gPoint;
 
-/* Contact manifold (112 bytes), same fields as reference b2Manifold
- * (include/box2d/collision.h:474-520). */
+/* Contact manifold (108 bytes): the layout of the public b2Manifold
+ * (include/box2d/collision.h, reference include/box2d/collision.h:474-520), so device
+ * manifolds can be handed to callers as b2Manifold arrays. */
 typedef struct b2gManifold
 {
 	b2gPoint pts[2];
 	b2gVec normal;
 	int32_t count;
-	int32_t pad;
 } b2gManifold;
 
 /* Contact flags kept on the device (reference src/contact.h:85-104). */
@@ -173,7 +173,6 @@ typedef struct b2gDevWorld
 	float* cMix;	/* friction, restitution */
 	uint32_t* cFlags;
 	int* cBodies; /* 2 per contact: awake body id or -1 */
-	void* cMass;  /* float4: invMassA invIA invMassB invIB */
 	b2gManifold* manifold;
 
 	/* colour-major solve lists */

@@ -154,7 +154,6 @@ __global__ void k_scatter_contacts( b2gDevWorld W, const b2gContactInit* inits, 
 	W.cFlags[id] = B2G_C_LIVE;
 	W.cBodies[2 * id] = -1;
 	W.cBodies[2 * id + 1] = -1;
-	( (float4*)W.cMass )[id] = make_float4( 0.0f, 0.0f, 0.0f, 0.0f );
 	b2gManifold m;
 	gmanifold_clear( &m );
 	W.manifold[id] = m;
@@ -208,11 +207,6 @@ __global__ void __launch_bounds__( BLOCK ) k_collide( b2gDevWorld W, int idCount
 	int infoB = W.bodyInfo[bB];
 	W.cBodies[2 * id] = ( infoA & B2G_B_AWAKE ) ? bA : -1;
 	W.cBodies[2 * id + 1] = ( infoB & B2G_B_AWAKE ) ? bB : -1;
-	const float4* mass = (const float4*)W.mass;
-	float4 mA = mass[bA];
-	float4 mB = mass[bB];
-	( (float4*)W.cMass )[id] = make_float4( mA.y, mA.w, mB.y, mB.w );
-
 	const float4* xf = (const float4*)W.xf;
 	const float4* centers = (const float4*)W.centers;
 	float4 xa = xf[bA], xb = xf[bB];
@@ -269,12 +263,16 @@ __global__ void __launch_bounds__( BLOCK ) k_prepare( b2gDevWorld W, int total, 
 	int k = blockIdx.x * blockDim.x + threadIdx.x;
 	if ( k >= total )
 		return;
-	int cid = W.solveList[k];
+	/* a null solve list means rows are the contacts in order */
+	int cid = W.solveList ? W.solveList[k] : k;
 	const b2gManifold* m = W.manifold + cid;
 	int ia = W.cBodies[2 * cid];
 	int ib = W.cBodies[2 * cid + 1];
-	float4 cm = ( (const float4*)W.cMass )[cid];
-	float mA = cm.x, iA = cm.y, mB = cm.z, iB = cm.w;
+	/* inverse masses of the reference's contact sim: the body's, zero for static bodies */
+	const float4* mass = (const float4*)W.mass;
+	float4 ma = ia >= 0 ? mass[ia] : make_float4( 0.0f, 0.0f, 0.0f, 0.0f );
+	float4 mb = ib >= 0 ? mass[ib] : make_float4( 0.0f, 0.0f, 0.0f, 0.0f );
+	float mA = ma.y, iA = ma.w, mB = mb.y, iB = mb.w;
 	float friction = W.cMix[2 * cid];
 	float restitution = W.cMix[2 * cid + 1];
 	DevState sA = load_state( W, ia );
@@ -1101,7 +1099,9 @@ extern "C" int b2gd_collide( b2gDevWorld* w, b2gHostIO* io, int newCount, int id
 	return check( cudaGetLastError() );
 }
 
-extern "C" int b2gd_solve( b2gDevWorld* w, b2gHostIO* io, const b2gSolvePlan* plan, const b2gStepConst* scp )
+/* Prepare .. store impulses on the world's stream (no body finalisation).  Returns the
+ * number of kernels launched. */
+extern "C" int b2gd_contact_solver( b2gDevWorld* w, const b2gSolvePlan* plan, const b2gStepConst* scp )
 {
 	cudaStream_t s = (cudaStream_t)w->stream;
 	b2gStepConst sc = *scp;
@@ -1113,23 +1113,32 @@ extern "C" int b2gd_solve( b2gDevWorld* w, b2gHostIO* io, const b2gSolvePlan* pl
 	int ovRow = cs[B2G_OVERFLOW], ovRows = cs[B2G_COLORS] - cs[B2G_OVERFLOW];
 	int ovJoint = js[B2G_OVERFLOW], ovJoints = js[B2G_COLORS] - js[B2G_OVERFLOW];
 	bool overflow = ovRows + ovJoints > 0;
-
-	if ( w->timing )
-		cudaEventRecord( (cudaEvent_t)w->timers[3], s );
-	cudaMemsetAsync( w->counters + 1, 0, sizeof( int ), s );
 	int launches = 0;
-	if ( rows > 0 )
-		k_prepare<<<blocks_for( rows ), BLOCK, 0, s>>>( *w, rows, sc );
-	if ( joints > 0 )
-		k_prepare_joints<<<blocks_for( joints ), BLOCK, 0, s>>>( *w, joints, sc );
 
+	if ( rows > 0 )
+	{
+		k_prepare<<<blocks_for( rows ), BLOCK, 0, s>>>( *w, rows, sc );
+		launches += 1;
+	}
+	if ( joints > 0 )
+	{
+		k_prepare_joints<<<blocks_for( joints ), BLOCK, 0, s>>>( *w, joints, sc );
+		launches += 1;
+	}
 	for ( int sub = 0; sub < sc.subSteps; ++sub )
 	{
-		k_integrate_velocities<<<blocks_for( awake ), BLOCK, 0, s>>>( *w, awake, sc );
+		if ( awake > 0 )
+		{
+			k_integrate_velocities<<<blocks_for( awake ), BLOCK, 0, s>>>( *w, awake, sc );
+			launches += 1;
+		}
 		for ( int phase = PH_WARM; phase <= PH_SOLVE; ++phase )
 		{
 			if ( overflow )
+			{
 				k_overflow<<<1, 32, 0, s>>>( *w, phase, ovJoint, ovJoints, ovRow, ovRows, sc );
+				launches += 1;
+			}
 			if ( phase == PH_WARM && sc.enableWarmStarting == 0 )
 				continue;
 			for ( int a = 0; a < plan->activeCount; ++a )
@@ -1137,46 +1146,67 @@ extern "C" int b2gd_solve( b2gDevWorld* w, b2gHostIO* io, const b2gSolvePlan* pl
 				int c = plan->active[a];
 				int nj = js[c + 1] - js[c], nr = cs[c + 1] - cs[c];
 				k_color<<<blocks_for( nj + nr ), BLOCK, 0, s>>>( *w, phase, js[c], nj, cs[c], nr, sc );
+				launches += 1;
 			}
 		}
-		k_integrate_positions<<<blocks_for( awake ), BLOCK, 0, s>>>( *w, awake, sc );
+		if ( awake > 0 )
+		{
+			k_integrate_positions<<<blocks_for( awake ), BLOCK, 0, s>>>( *w, awake, sc );
+			launches += 1;
+		}
 		if ( overflow )
+		{
 			k_overflow<<<1, 32, 0, s>>>( *w, PH_RELAX, ovJoint, ovJoints, ovRow, ovRows, sc );
+			launches += 1;
+		}
 		for ( int a = 0; a < plan->activeCount; ++a )
 		{
 			int c = plan->active[a];
 			int nj = js[c + 1] - js[c], nr = cs[c + 1] - cs[c];
 			k_color<<<blocks_for( nj + nr ), BLOCK, 0, s>>>( *w, PH_RELAX, js[c], nj, cs[c], nr, sc );
+			launches += 1;
 		}
 	}
 	if ( ovRows > 0 )
+	{
 		k_overflow<<<1, 32, 0, s>>>( *w, PH_RESTITUTION, ovJoint, 0, ovRow, ovRows, sc );
+		launches += 1;
+	}
 	for ( int a = 0; a < plan->activeCount; ++a )
 	{
 		int c = plan->active[a];
 		int nr = cs[c + 1] - cs[c];
 		if ( nr > 0 )
+		{
 			k_color<<<blocks_for( nr ), BLOCK, 0, s>>>( *w, PH_RESTITUTION, 0, 0, cs[c], nr, sc );
+			launches += 1;
+		}
 	}
 	if ( rows > 0 )
+	{
 		k_store<<<blocks_for( rows ), BLOCK, 0, s>>>( *w, rows, ovRow );
+		launches += 1;
+	}
+	return launches;
+}
+
+extern "C" int b2gd_solve( b2gDevWorld* w, b2gHostIO* io, const b2gSolvePlan* plan, const b2gStepConst* scp )
+{
+	cudaStream_t s = (cudaStream_t)w->stream;
+	int awake = plan->awakeCount;
+	if ( w->timing )
+		cudaEventRecord( (cudaEvent_t)w->timers[3], s );
+	cudaMemsetAsync( w->counters + 1, 0, sizeof( int ), s );
+	w->launches += b2gd_contact_solver( w, plan, scp );
 	if ( w->timing )
 		cudaEventRecord( (cudaEvent_t)w->timers[4], s );
 	if ( awake > 0 )
-		k_finalize<<<blocks_for( awake ), BLOCK, 0, s>>>( *w, awake, sc );
+	{
+		k_finalize<<<blocks_for( awake ), BLOCK, 0, s>>>( *w, awake, *scp );
+		w->launches += 1;
+	}
 	if ( w->timing )
 		cudaEventRecord( (cudaEvent_t)w->timers[5], s );
-	/* launch count of this sequence, for the benchmark's kernel accounting */
-	launches = ( rows > 0 ) + ( joints > 0 ) + ( rows > 0 ) + ( awake > 0 );
-	{
-		int perSub = 2 + ( overflow ? 3 : 0 );
-		int colorLaunches = 0;
-		for ( int a = 0; a < plan->activeCount; ++a )
-			colorLaunches += 1;
-		perSub += colorLaunches * ( sc.enableWarmStarting ? 3 : 2 );
-		launches += sc.subSteps * perSub + ( ovRows > 0 ) + colorLaunches;
-	}
-	w->launches += launches;
 	cudaMemcpyAsync( io->counters, w->counters, 4 * sizeof( int ), cudaMemcpyDeviceToHost, s );
 	return check( cudaGetLastError() );
 }

@@ -43,6 +43,45 @@ B2_API b2DeviceTimes b2World_GetDeviceTimes( b2WorldId worldId );
  * floats).  One device-to-host copy per call.  Returns the number of body ids. */
 B2_API int b2World_GetBodyStates( b2WorldId worldId, float* out, int capacity );
 
+/* One soft-step contact solve on caller-owned device buffers: the solver stage of
+ * b2World_Step (reference src/solver.c:559-731 and src/contact_solver.c) without the
+ * broadphase, narrowphase, colouring or body finalisation.  The caller supplies
+ * coloured contacts (no two contacts of one colour share a non-static body; colour 11
+ * is the overflow set, solved serially in array order) and receives updated body
+ * velocities, position/rotation deltas and accumulated impulses.  All pointers are
+ * device pointers except colorStart; the call is asynchronous on `stream`. */
+typedef struct b2ContactSolveDesc
+{
+	/* bodies, indexed by body index */
+	float* states;			/* in/out, 8 per body: v.x v.y w (unused) dp.x dp.y dq.c dq.s */
+	const float* massData;	/* 4 per body: mass invMass inertia invInertia */
+	const float* forces;	/* 4 per body: force.x force.y torque gravityScale */
+	const float* damping;	/* 4 per body: linearDamping angularDamping (2 unused) */
+	const int* bodies;		/* bodyCount body indices integrated every substep */
+	int bodyCount;
+
+	/* contacts, colour-major */
+	const int* contactBodies; /* 2 per contact: body index, -1 for a static body */
+	const float* contactMix;  /* 2 per contact: friction, restitution */
+	b2Manifold* manifolds;	  /* in: points, centre-relative anchors, separations and
+							   * warm-start impulses; out: impulses, max impulse and
+							   * relative normal velocity per point */
+	int contactCount;
+	int colorStart[13]; /* host ints; colorStart[12] == contactCount */
+
+	/* step */
+	float timeStep;
+	int subStepCount;
+	b2Vec2 gravity;
+	float contactHertz, contactDampingRatio, contactPushout, restitutionThreshold;
+	bool enableWarmStarting;
+	void* stream; /* cudaStream_t; null for the default stream */
+} b2ContactSolveDesc;
+
+/* Returns 0, or a CUDA error code / -1 for invalid arguments.  Allocates its per-call
+ * constraint rows (160 bytes per contact) with stream-ordered device allocation. */
+B2_API int b2SolveContacts( const b2ContactSolveDesc* desc );
+
 #ifdef __cplusplus
 }
 #endif

@@ -16,6 +16,9 @@
 
 #include <string.h>
 
+void o_capture_inputs( oWorld* w );
+void o_capture_outputs( oWorld* w );
+
 typedef struct oStep
 {
 	b2r dt, inv_dt, h, inv_h;
@@ -758,6 +761,7 @@ void o_solve( oWorld* w, b2r dt, int subSteps )
 		if ( w->colors[i].contacts.count + w->colors[i].joints.count > 0 )
 			active[activeCount++] = i;
 
+	o_capture_inputs( w );
 	int totalContacts = 0;
 	for ( int i = 0; i < O_COLORS; ++i )
 		totalContacts += w->colors[i].contacts.count;
@@ -859,6 +863,7 @@ void o_solve( oWorld* w, b2r dt, int subSteps )
 		}
 	}
 	free( cons );
+	o_capture_outputs( w );
 
 	oFinalize f;
 	f.enlarged = (uint8_t*)calloc( (size_t)awakeCount, 1 );
@@ -915,4 +920,149 @@ void o_step( oWorld* w, b2r dt, int subSteps )
 	o_collide( w );
 	if ( dt > R( 0 ) )
 		o_solve( w, dt, subSteps );
+}
+
+/* ------------------------------------------------------------ solver-stage capture */
+/* Test hook: records the inputs of the solver stage (after the narrowphase and the
+ * colouring) and its outputs (after impulses are stored, before bodies are finalised),
+ * in the layouts of b2ContactSolveDesc (include/box2d/gpu.h). */
+typedef struct b2oCapture
+{
+	int bodyCap, contactCap;
+	int bodyCount, awakeCount, contactCount, overflow;
+	float *statesIn, *statesOut, *mass, *force, *damping;
+	int* awake;
+	int* contactBodies;
+	float* mix;
+	b2Manifold *manifoldsIn, *manifoldsOut;
+	int colorStart[13];
+} b2oCapture;
+
+static b2oCapture* s_capture;
+
+static void capture_states( oWorld* w, float* out )
+{
+	for ( int i = 0; i < w->bodyIds.next; ++i )
+	{
+		oBody* b = w->bodies + i;
+		float* o = out + 8 * i;
+		bool moving = b->id == i && b->type != b2_staticBody;
+		o[0] = moving ? (float)b->v.x : 0.0f;
+		o[1] = moving ? (float)b->v.y : 0.0f;
+		o[2] = moving ? (float)b->w : 0.0f;
+		o[3] = 0.0f;
+		o[4] = moving ? (float)b->dp.x : 0.0f;
+		o[5] = moving ? (float)b->dp.y : 0.0f;
+		o[6] = moving ? (float)b->dq.c : 1.0f;
+		o[7] = moving ? (float)b->dq.s : 0.0f;
+	}
+}
+
+static void capture_manifolds( oWorld* w, b2Manifold* out )
+{
+	int n = 0;
+	for ( int c = 0; c < O_COLORS; ++c )
+	{
+		oIntArray* a = &w->colors[c].contacts;
+		for ( int k = 0; k < a->count; ++k )
+		{
+			const oManifold* m = &w->contacts[a->data[k]].manifold;
+			b2Manifold* o = out + n++;
+			memset( o, 0, sizeof( *o ) );
+			o->normal.x = (float)m->normal.x;
+			o->normal.y = (float)m->normal.y;
+			o->pointCount = m->count;
+			for ( int j = 0; j < 2; ++j )
+			{
+				const oMPoint* p = m->pts + j;
+				b2ManifoldPoint* q = o->points + j;
+				q->point = vfo( p->point );
+				q->anchorA = vfo( p->anchorA );
+				q->anchorB = vfo( p->anchorB );
+				q->separation = (float)p->separation;
+				q->normalImpulse = (float)p->normalImpulse;
+				q->tangentImpulse = (float)p->tangentImpulse;
+				q->maxNormalImpulse = (float)p->maxNormalImpulse;
+				q->normalVelocity = (float)p->normalVelocity;
+				q->id = p->id;
+				q->persisted = p->persisted;
+			}
+		}
+	}
+}
+
+void o_capture_inputs( oWorld* w )
+{
+	b2oCapture* cap = s_capture;
+	if ( cap == NULL )
+		return;
+	int nb = w->bodyIds.next;
+	int nc = 0;
+	for ( int c = 0; c < O_COLORS; ++c )
+		nc += w->colors[c].contacts.count;
+	cap->bodyCount = nb;
+	cap->awakeCount = w->awake.count;
+	cap->contactCount = nc;
+	if ( nb > cap->bodyCap || nc > cap->contactCap || w->awake.count > cap->bodyCap )
+	{
+		cap->overflow = 1;
+		return;
+	}
+	capture_states( w, cap->statesIn );
+	for ( int i = 0; i < nb; ++i )
+	{
+		oBody* b = w->bodies + i;
+		float* m = cap->mass + 4 * i;
+		float* f = cap->force + 4 * i;
+		float* d = cap->damping + 4 * i;
+		m[0] = (float)b->mass;
+		m[1] = (float)b->invMass;
+		m[2] = (float)b->inertia;
+		m[3] = (float)b->invI;
+		f[0] = (float)b->force.x;
+		f[1] = (float)b->force.y;
+		f[2] = (float)b->torque;
+		f[3] = (float)b->gravityScale;
+		d[0] = (float)b->linearDamping;
+		d[1] = (float)b->angularDamping;
+		d[2] = (float)b->minExtent;
+		d[3] = (float)b->maxExtent;
+	}
+	memcpy( cap->awake, w->awake.data, sizeof( int ) * (size_t)w->awake.count );
+	int n = 0;
+	for ( int c = 0; c < O_COLORS; ++c )
+	{
+		cap->colorStart[c] = n;
+		oIntArray* a = &w->colors[c].contacts;
+		for ( int k = 0; k < a->count; ++k )
+		{
+			oContact* ct = w->contacts + a->data[k];
+			cap->contactBodies[2 * n] = ct->simIndexA;
+			cap->contactBodies[2 * n + 1] = ct->simIndexB;
+			cap->mix[2 * n] = (float)ct->friction;
+			cap->mix[2 * n + 1] = (float)ct->restitution;
+			n += 1;
+		}
+	}
+	cap->colorStart[O_COLORS] = n;
+	capture_manifolds( w, cap->manifoldsIn );
+}
+
+void o_capture_outputs( oWorld* w )
+{
+	b2oCapture* cap = s_capture;
+	if ( cap == NULL || cap->overflow )
+		return;
+	capture_states( w, cap->statesOut );
+	capture_manifolds( w, cap->manifoldsOut );
+}
+
+/* Steps the world once, capturing the solver stage's inputs and outputs. */
+int b2o_StepCapture( b2WorldId worldId, float timeStep, int subStepCount, b2oCapture* cap )
+{
+	cap->overflow = 0;
+	s_capture = cap;
+	b2World_Step( worldId, timeStep, subStepCount );
+	s_capture = NULL;
+	return cap->overflow ? -1 : 0;
 }
