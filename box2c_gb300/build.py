@@ -26,7 +26,7 @@ CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU_SOURCES = ["kernels.cu", "arena.cu", "solve_api.cu"]
+CU_SOURCES = ["kernels.cu", "arena.cu", "solve_api.cu", "solve_noalloc.cu"]
 C_SOURCES = ["world.c", "step.c", "tree.c", "util.c", "geometry.c"]
 HEADERS = ["b2g_math.h", "b2g_types.h", "b2g_collide.h", "b2g_device.h", "host.h"]
 

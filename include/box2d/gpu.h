@@ -82,6 +82,21 @@ typedef struct b2ContactSolveDesc
  * constraint rows (160 bytes per contact) with stream-ordered device allocation. */
 B2_API int b2SolveContacts( const b2ContactSolveDesc* desc );
 
+/* b2SolveContacts that allocates nothing; no counterpart in the reference API.  Its
+ * constraint rows live in one fixed device array per device, compiled into the library:
+ * B2_SOLVE_NOALLOC_MAX_CONTACTS rows of 160 bytes (2.5 MiB).  Same descriptor, same
+ * results and return codes as b2SolveContacts, plus B2_SOLVE_NOALLOC_TOO_LARGE (nothing
+ * launched) when contactCount exceeds the maximum.
+ * - The first call on each device (with that device current) looks up the array's
+ *   address; make it before any stream capture starts.
+ * - Nothing in the array has to start at zero: every row is written before it is read.
+ * - Calls that overlap on one device share the array and race: order them (one stream,
+ *   or events between streams, and one host thread at a time). */
+#define B2_SOLVE_NOALLOC_MAX_CONTACTS 16384
+#define B2_SOLVE_NOALLOC_TOO_LARGE ( -2 )
+
+B2_API int b2SolveContactsNoAlloc( const b2ContactSolveDesc* desc );
+
 #ifdef __cplusplus
 }
 #endif
