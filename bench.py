@@ -45,11 +45,6 @@ DT = 1.0 / 60.0
 SUBSTEPS = 4
 
 
-class DeviceTimes(C.Structure):
-    _fields_ = [("step", C.c_float), ("collide", C.c_float), ("solve", C.c_float), ("finalize", C.c_float),
-                ("eventCount", C.c_int), ("recordCount", C.c_int), ("launches", C.c_int)]
-
-
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -171,7 +166,7 @@ def run_reference(args):
 
 def run_gpu(args):
     import box2c_gb300
-    from box2c_gb300.capi import WorldId
+    from box2c_gb300.capi import bind_gpu_api
 
     rank, world_size, local = dist_env()
     if world_size > 1:
@@ -185,13 +180,7 @@ def run_gpu(args):
     box2c_gb300.build()
     g = box2c_gb300.load()
     L = g.lib
-    L.b2World_EnableDeviceTiming.argtypes = [WorldId, C.c_bool]
-    L.b2World_GetDeviceTimes.argtypes = [WorldId]
-    L.b2World_GetDeviceTimes.restype = DeviceTimes
-    L.b2World_GetBodyStates.argtypes = [WorldId, C.c_void_p, C.c_int]
-    L.b2World_GetBodyStates.restype = C.c_int
-    L.b2World_GetStatus.argtypes = [WorldId]
-    L.b2World_GetUnsupportedToiCount.argtypes = [WorldId]
+    bind_gpu_api(L)
 
     w = g.pyramid(BASE, JITTER, SEED)
     L.b2World_EnableDeviceTiming(w, True)
@@ -202,6 +191,7 @@ def run_gpu(args):
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
     step_ms, solve_ms, collide_ms, finalize_ms, launches = [], [], [], [], []
+    fused_steps = 0
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
@@ -219,6 +209,7 @@ def run_gpu(args):
             collide_ms.append(t.collide)
             finalize_ms.append(t.finalize)
             launches.append(t.launches)
+            fused_steps += t.fusedSolver
     torch.cuda.synchronize()
     ms = float(np.mean(step_ms))
     if dist:
@@ -260,7 +251,8 @@ def run_gpu(args):
         "config": {"workload": "large_pyramid_100_rows_5050_boxes", "rows": BASE, "bodies": n_bodies - 1,
                    "contacts": int(len(contacts)), "touching": int(len(touching)), "colors": list(counters.colorCounts),
                    "dt": DT, "substeps": SUBSTEPS, "l2": "flushed between timed steps (256 MB write)",
-                   "parallelism": f"replicas{world_size}"},
+                   "parallelism": f"replicas{world_size}",
+                   "solver": "fused cluster kernel" if fused_steps == args.steps else "per-phase kernels"},
         "stages_ms": {"collide": round(float(np.mean(collide_ms)), 4), "solve": round(solve_dev, 4),
                       "finalize": round(float(np.mean(finalize_ms)), 4)},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",

@@ -250,3 +250,25 @@ class ContactSolveDesc(C.Structure):
 def bind_solve_api(lib: C.CDLL) -> None:
     lib.b2SolveContacts.argtypes = [C.POINTER(ContactSolveDesc)]
     lib.b2SolveContacts.restype = C.c_int
+
+
+class DeviceTimes(C.Structure):
+    """include/box2d/gpu.h b2DeviceTimes."""
+    _fields_ = [("step", C.c_float), ("collide", C.c_float), ("solve", C.c_float), ("finalize", C.c_float),
+                ("eventCount", C.c_int), ("recordCount", C.c_int), ("launches", C.c_int), ("fusedSolver", C.c_int)]
+
+
+def bind_gpu_api(lib: C.CDLL) -> None:
+    """Binds the additive device entry points of include/box2d/gpu.h."""
+    lib.b2World_GetStatus.argtypes = [WorldId]
+    lib.b2World_GetStatus.restype = C.c_int
+    lib.b2World_GetUnsupportedToiCount.argtypes = [WorldId]
+    lib.b2World_GetUnsupportedToiCount.restype = C.c_int
+    lib.b2World_EnableDeviceTiming.argtypes = [WorldId, C.c_bool]
+    lib.b2World_EnableDeviceTiming.restype = None
+    lib.b2World_GetDeviceTimes.argtypes = [WorldId]
+    lib.b2World_GetDeviceTimes.restype = DeviceTimes
+    lib.b2World_EnableFusedSolver.argtypes = [WorldId, C.c_bool]
+    lib.b2World_EnableFusedSolver.restype = None
+    lib.b2World_GetBodyStates.argtypes = [WorldId, C.c_void_p, C.c_int]
+    lib.b2World_GetBodyStates.restype = C.c_int

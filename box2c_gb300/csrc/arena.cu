@@ -76,6 +76,7 @@ extern "C" int b2gd_init( b2gDevWorld* w, b2gHostIO* io )
 	if ( e )
 		return e;
 	w->stream = (void*)s;
+	w->fused = 1;
 	e = ok( cudaMalloc( (void**)&w->counters, 4 * sizeof( int ) ) );
 	if ( e )
 		return e;

@@ -20,6 +20,7 @@ typedef struct b2gSolvePlan
 	int active[B2G_COLORS];
 	int activeCount;
 	int awakeCount;
+	int bodyIdCount; /* body ids in use (0: caller buffers, per-phase kernels only) */
 } b2gSolvePlan;
 
 /* Pinned host staging owned by the device module (mapped into the device). */

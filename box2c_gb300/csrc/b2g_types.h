@@ -201,6 +201,8 @@ typedef struct b2gDevWorld
 	void* timers[8]; /* cudaEvent_t: step start, collide start/end, solve start/end, finalize end, step end */
 	int timing;
 	int launches;
+	int fused;	   /* use the fused cluster solver when the world fits on chip */
+	int fusedUsed; /* the last step's solver stage ran fused */
 } b2gDevWorld;
 
 #ifdef __cplusplus

@@ -26,6 +26,7 @@
  */
 #include "b2g_collide.h"
 #include "b2g_device.h"
+#include "b2g_solve.h"
 
 #include <cuda_runtime.h>
 
@@ -34,45 +35,19 @@
 #define BLOCK 256
 
 /* ------------------------------------------------------------------ state access */
-struct DevState
-{
-	b2gVec v;
-	float w;
-	b2gVec dp;
-	b2gRot dq;
-};
-
 __device__ __forceinline__ DevState load_state( const b2gDevWorld& W, int b )
 {
-	DevState s;
 	if ( b < 0 )
-	{
-		s.v = gv( 0.0f, 0.0f );
-		s.w = 0.0f;
-		s.dp = gv( 0.0f, 0.0f );
-		s.dq = grot( 1.0f, 0.0f );
-		return s;
-	}
+		return identity_state();
 	const float4* st = (const float4*)W.state;
-	float4 a = st[2 * b];
-	float4 c = st[2 * b + 1];
-	s.v = gv( a.x, a.y );
-	s.w = a.z;
-	s.dp = gv( c.x, c.y );
-	s.dq = grot( c.z, c.w );
-	return s;
+	return state_of( st[2 * b], st[2 * b + 1] );
 }
 
-__device__ __forceinline__ void store_velocity( const b2gDevWorld& W, int b, b2gVec v, float w )
+__device__ __forceinline__ void store_velocity( const b2gDevWorld& W, int b, const DevState& s )
 {
 	if ( b < 0 )
 		return;
-	float4* st = (float4*)W.state;
-	float4 a = st[2 * b];
-	a.x = v.x;
-	a.y = v.y;
-	a.z = w;
-	st[2 * b] = a;
+	( (float4*)W.state )[2 * b] = velocity_word( s );
 }
 
 __device__ __forceinline__ b2gBox box_of( float4 f )
@@ -265,67 +240,26 @@ __global__ void __launch_bounds__( BLOCK ) k_prepare( b2gDevWorld W, int total, 
 		return;
 	/* a null solve list means rows are the contacts in order */
 	int cid = W.solveList ? W.solveList[k] : k;
-	const b2gManifold* m = W.manifold + cid;
 	int ia = W.cBodies[2 * cid];
 	int ib = W.cBodies[2 * cid + 1];
 	/* inverse masses of the reference's contact sim: the body's, zero for static bodies */
 	const float4* mass = (const float4*)W.mass;
-	float4 ma = ia >= 0 ? mass[ia] : make_float4( 0.0f, 0.0f, 0.0f, 0.0f );
-	float4 mb = ib >= 0 ? mass[ib] : make_float4( 0.0f, 0.0f, 0.0f, 0.0f );
-	float mA = ma.y, iA = ma.w, mB = mb.y, iB = mb.w;
-	float friction = W.cMix[2 * cid];
-	float restitution = W.cMix[2 * cid + 1];
-	DevState sA = load_state( W, ia );
-	DevState sB = load_state( W, ib );
-	const float* soft = ( ia < 0 || ib < 0 ) ? sc.staticSoft : sc.contactSoft;
-	b2gVec n = m->normal;
-	int count = m->count;
-	float warm = sc.enableWarmStarting ? 1.0f : 0.0f;
-
-	( (int4*)W.kIdx )[k] = make_int4( ia, ib, cid, count );
-	( (float4*)W.kNF )[k] = make_float4( n.x, n.y, friction, restitution );
-	( (float4*)W.kSoft )[k] = make_float4( soft[0], soft[1], soft[2], 0.0f );
-	( (float4*)W.kMass )[k] = make_float4( mA, iA, mB, iB );
-	b2gVec t = gright( n );
+	float4 zero = make_float4( 0.0f, 0.0f, 0.0f, 0.0f );
+	Row r;
+	prepare_row( r, W.manifold + cid, ia, ib, ia >= 0 ? mass[ia] : zero, ib >= 0 ? mass[ib] : zero, load_state( W, ia ),
+				 load_state( W, ib ), W.cMix[2 * cid], W.cMix[2 * cid + 1], ( ia < 0 || ib < 0 ) ? sc.staticSoft : sc.contactSoft,
+				 sc.enableWarmStarting ? 1.0f : 0.0f );
+	( (int4*)W.kIdx )[k] = make_int4( ia, ib, cid, r.count );
+	( (float4*)W.kNF )[k] = make_float4( r.n.x, r.n.y, r.friction, r.restitution );
+	( (float4*)W.kSoft )[k] = make_float4( r.biasRate, r.massScale, r.impulseScale, 0.0f );
+	( (float4*)W.kMass )[k] = make_float4( r.mA, r.iA, r.mB, r.iB );
 	for ( int j = 0; j < 2; ++j )
 	{
-		float4 anchor = make_float4( 0.0f, 0.0f, 0.0f, 0.0f );
-		float4 coef = make_float4( 0.0f, 0.0f, 0.0f, 0.0f );
-		float4 imp = make_float4( 0.0f, 0.0f, 0.0f, 0.0f );
-		if ( j < count )
-		{
-			const b2gPoint* mp = m->pts + j;
-			b2gVec rA = mp->anchorA, rB = mp->anchorB;
-			float base = mp->separation - gdot( gsub( rB, rA ), n );
-			float rnA = gcross( rA, n ), rnB = gcross( rB, n );
-			float kN = mA + mB + iA * rnA * rnA + iB * rnB * rnB;
-			float rtA = gcross( rA, t ), rtB = gcross( rB, t );
-			float kT = mA + mB + iA * rtA * rtA + iB * rtB * rtB;
-			b2gVec vrA = gadd( sA.v, gcross_sv( sA.w, rA ) );
-			b2gVec vrB = gadd( sB.v, gcross_sv( sB.w, rB ) );
-			float relVel = gdot( n, gsub( vrB, vrA ) );
-			anchor = make_float4( rA.x, rA.y, rB.x, rB.y );
-			coef = make_float4( base, kN > 0.0f ? 1.0f / kN : 0.0f, kT > 0.0f ? 1.0f / kT : 0.0f, relVel );
-			imp = make_float4( warm * mp->normalImpulse, warm * mp->tangentImpulse, 0.0f, 0.0f );
-		}
-		( (float4*)W.kAnchor[j] )[k] = anchor;
-		( (float4*)W.kCoef[j] )[k] = coef;
-		( (float4*)W.kImp[j] )[k] = imp;
+		( (float4*)W.kAnchor[j] )[k] = make_float4( r.rA[j].x, r.rA[j].y, r.rB[j].x, r.rB[j].y );
+		( (float4*)W.kCoef[j] )[k] = make_float4( r.base[j], r.nMass[j], r.tMass[j], r.relVel[j] );
+		( (float4*)W.kImp[j] )[k] = make_float4( r.ni[j], r.ti[j], r.maxNi[j], 0.0f );
 	}
 }
-
-/* One constraint row held in registers. */
-struct Row
-{
-	int ia, ib, count;
-	b2gVec n;
-	float friction, restitution;
-	float biasRate, massScale, impulseScale;
-	float mA, iA, mB, iB;
-	b2gVec rA[2], rB[2];
-	float base[2], nMass[2], tMass[2], relVel[2];
-	float ni[2], ti[2], maxNi[2];
-};
 
 __device__ __forceinline__ void load_row( const b2gDevWorld& W, int k, Row& r )
 {
@@ -369,251 +303,31 @@ __device__ __forceinline__ void store_impulses( const b2gDevWorld& W, int k, con
 		( (float4*)W.kImp[j] )[k] = make_float4( r.ni[j], r.ti[j], r.maxNi[j], 0.0f );
 }
 
-/* 8-lane path: both point slots are evaluated (slot 1 of a one-point manifold carries
- * zeros, like the reference's SIMD remainder data). */
-__device__ __forceinline__ void lane_apply( DevState& a, DevState& b, const Row& r, b2gVec rA, b2gVec rB, float Px, float Py )
-{
-	a.v.x = a.v.x - r.mA * Px;
-	a.v.y = a.v.y - r.mA * Py;
-	a.w = a.w - r.iA * ( rA.x * Py - rA.y * Px );
-	b.v.x = b.v.x + r.mB * Px;
-	b.v.y = b.v.y + r.mB * Py;
-	b.w = b.w + r.iB * ( rB.x * Py - rB.y * Px );
-}
-
-__device__ void lane_warm( const b2gDevWorld& W, int k )
+/* Row phases over global body state: load, solve in registers, store. */
+__device__ void row_phase( const b2gDevWorld& W, int k, int phase, bool scalar, const b2gStepConst& sc )
 {
 	Row r;
 	load_row( W, k, r );
 	DevState a = load_state( W, r.ia );
 	DevState b = load_state( W, r.ib );
-	float tX = r.n.y;
-	float tY = 0.0f - r.n.x;
-	for ( int j = 0; j < 2; ++j )
-	{
-		b2gVec rA = r.rA[j], rB = r.rB[j];
-		float Px = r.ni[j] * r.n.x + r.ti[j] * tX;
-		float Py = r.ni[j] * r.n.y + r.ti[j] * tY;
-		a.w = a.w - r.iA * ( rA.x * Py - rA.y * Px );
-		a.v.x = a.v.x - r.mA * Px;
-		a.v.y = a.v.y - r.mA * Py;
-		b.w = b.w + r.iB * ( rB.x * Py - rB.y * Px );
-		b.v.x = b.v.x + r.mB * Px;
-		b.v.y = b.v.y + r.mB * Py;
-	}
-	store_velocity( W, r.ia, a.v, a.w );
-	store_velocity( W, r.ib, b.v, b.w );
-}
-
-__device__ void lane_solve( const b2gDevWorld& W, int k, bool useBias, float inv_h, float pushout )
-{
-	Row r;
-	load_row( W, k, r );
-	DevState a = load_state( W, r.ia );
-	DevState b = load_state( W, r.ib );
-	float biasRate = useBias ? r.biasRate : 0.0f;
-	float massScale = useBias ? r.massScale : 1.0f;
-	float impulseScale = useBias ? r.impulseScale : 0.0f;
-	float minBias = -pushout;
-	b2gVec dp = gv( b.dp.x - a.dp.x, b.dp.y - a.dp.y );
-	b2gVec n = r.n;
-	for ( int j = 0; j < 2; ++j )
-	{
-		b2gVec aA = r.rA[j], aB = r.rB[j];
-		b2gVec rsA = gv( a.dq.c * aA.x - a.dq.s * aA.y, a.dq.s * aA.x + a.dq.c * aA.y );
-		b2gVec rsB = gv( b.dq.c * aB.x - b.dq.s * aB.y, b.dq.s * aB.x + b.dq.c * aB.y );
-		b2gVec ds = gv( dp.x + ( rsB.x - rsA.x ), dp.y + ( rsB.y - rsA.y ) );
-		float s = ( n.x * ds.x + n.y * ds.y ) + r.base[j];
-		float specBias = s * inv_h;
-		float softBias = gmax( biasRate * s, minBias );
-		float bias = s > 0.0f ? specBias : softBias;
-		float dvx = ( b.v.x - b.w * aB.y ) - ( a.v.x - a.w * aA.y );
-		float dvy = ( b.v.y + b.w * aB.x ) - ( a.v.y + a.w * aA.x );
-		float vn = dvx * n.x + dvy * n.y;
-		float negImpulse = r.nMass[j] * ( massScale * ( vn + bias ) ) + impulseScale * r.ni[j];
-		float newImpulse = gmax( r.ni[j] - negImpulse, 0.0f );
-		float impulse = newImpulse - r.ni[j];
-		r.ni[j] = newImpulse;
-		r.maxNi[j] = gmax( r.maxNi[j], newImpulse );
-		lane_apply( a, b, r, aA, aB, impulse * n.x, impulse * n.y );
-	}
-	float tX = n.y;
-	float tY = 0.0f - n.x;
-	for ( int j = 0; j < 2; ++j )
-	{
-		b2gVec aA = r.rA[j], aB = r.rB[j];
-		float dvx = ( b.v.x - b.w * aB.y ) - ( a.v.x - a.w * aA.y );
-		float dvy = ( b.v.y + b.w * aB.x ) - ( a.v.y + a.w * aA.x );
-		float vt = dvx * tX + dvy * tY;
-		float negImpulse = r.tMass[j] * vt;
-		float maxFriction = r.friction * r.ni[j];
-		float newImpulse = r.ti[j] - negImpulse;
-		float lo = 0.0f - maxFriction;
-		float mn = newImpulse < maxFriction ? newImpulse : maxFriction;
-		newImpulse = lo > mn ? lo : mn;
-		float impulse = newImpulse - r.ti[j];
-		r.ti[j] = newImpulse;
-		lane_apply( a, b, r, aA, aB, impulse * tX, impulse * tY );
-	}
-	store_velocity( W, r.ia, a.v, a.w );
-	store_velocity( W, r.ib, b.v, b.w );
-	store_impulses( W, k, r );
-}
-
-__device__ void lane_restitution( const b2gDevWorld& W, int k, float threshold )
-{
-	Row r;
-	load_row( W, k, r );
-	DevState a = load_state( W, r.ia );
-	DevState b = load_state( W, r.ib );
-	b2gVec n = r.n;
-	for ( int j = 0; j < 2; ++j )
-	{
-		bool skip = ( r.relVel[j] + threshold > 0.0f ) || ( r.maxNi[j] == 0.0f );
-		float mass = skip ? 0.0f : r.nMass[j];
-		b2gVec aA = r.rA[j], aB = r.rB[j];
-		float dvx = ( b.v.x - b.w * aB.y ) - ( a.v.x - a.w * aA.y );
-		float dvy = ( b.v.y + b.w * aB.x ) - ( a.v.y + a.w * aA.x );
-		float vn = dvx * n.x + dvy * n.y;
-		float negImpulse = mass * ( vn + r.restitution * r.relVel[j] );
-		float newImpulse = gmax( r.ni[j] - negImpulse, 0.0f );
-		float impulse = newImpulse - r.ni[j];
-		r.ni[j] = newImpulse;
-		lane_apply( a, b, r, aA, aB, impulse * n.x, impulse * n.y );
-	}
-	store_velocity( W, r.ia, a.v, a.w );
-	store_velocity( W, r.ib, b.v, b.w );
-	store_impulses( W, k, r );
-}
-
-/* Overflow (scalar) path: only the manifold's points, different operand grouping. */
-__device__ void ovf_warm( const b2gDevWorld& W, int k )
-{
-	Row r;
-	load_row( W, k, r );
-	DevState a = load_state( W, r.ia );
-	DevState b = load_state( W, r.ib );
-	b2gVec t = gright( r.n );
-	for ( int j = 0; j < r.count; ++j )
-	{
-		b2gVec P = gadd( gmulsv( r.ni[j], r.n ), gmulsv( r.ti[j], t ) );
-		a.w -= r.iA * gcross( r.rA[j], P );
-		a.v = gmuladd( a.v, -r.mA, P );
-		b.w += r.iB * gcross( r.rB[j], P );
-		b.v = gmuladd( b.v, r.mB, P );
-	}
-	store_velocity( W, r.ia, a.v, a.w );
-	store_velocity( W, r.ib, b.v, b.w );
-}
-
-__device__ void ovf_solve( const b2gDevWorld& W, int k, bool useBias, float inv_h, float pushout )
-{
-	Row r;
-	load_row( W, k, r );
-	DevState a = load_state( W, r.ia );
-	DevState b = load_state( W, r.ib );
-	b2gVec dp = gsub( b.dp, a.dp );
-	b2gVec n = r.n, t = gright( n );
-	for ( int j = 0; j < r.count; ++j )
-	{
-		b2gVec rA = r.rA[j], rB = r.rB[j];
-		b2gVec ds = gadd( dp, gsub( grotate( b.dq, rB ), grotate( a.dq, rA ) ) );
-		float s = gdot( ds, n ) + r.base[j];
-		float velocityBias = 0.0f, massScale = 1.0f, impulseScale = 0.0f;
-		if ( s > 0.0f )
-			velocityBias = s * inv_h;
-		else if ( useBias )
-		{
-			velocityBias = gmax( r.biasRate * s, -pushout );
-			massScale = r.massScale;
-			impulseScale = r.impulseScale;
-		}
-		b2gVec vrA = gadd( a.v, gcross_sv( a.w, rA ) );
-		b2gVec vrB = gadd( b.v, gcross_sv( b.w, rB ) );
-		float vn = gdot( gsub( vrB, vrA ), n );
-		float impulse = -r.nMass[j] * massScale * ( vn + velocityBias ) - impulseScale * r.ni[j];
-		float newImpulse = gmax( r.ni[j] + impulse, 0.0f );
-		impulse = newImpulse - r.ni[j];
-		r.ni[j] = newImpulse;
-		r.maxNi[j] = gmax( r.maxNi[j], impulse );
-		b2gVec P = gmulsv( impulse, n );
-		a.v = gmulsub( a.v, r.mA, P );
-		a.w -= r.iA * gcross( rA, P );
-		b.v = gmuladd( b.v, r.mB, P );
-		b.w += r.iB * gcross( rB, P );
-	}
-	for ( int j = 0; j < r.count; ++j )
-	{
-		b2gVec rA = r.rA[j], rB = r.rB[j];
-		b2gVec vrB = gadd( b.v, gcross_sv( b.w, rB ) );
-		b2gVec vrA = gadd( a.v, gcross_sv( a.w, rA ) );
-		float vt = gdot( gsub( vrB, vrA ), t );
-		float impulse = r.tMass[j] * ( -vt );
-		float maxFriction = r.friction * r.ni[j];
-		float newImpulse = gclamp( r.ti[j] + impulse, -maxFriction, maxFriction );
-		impulse = newImpulse - r.ti[j];
-		r.ti[j] = newImpulse;
-		b2gVec P = gmulsv( impulse, t );
-		a.v = gmulsub( a.v, r.mA, P );
-		a.w -= r.iA * gcross( rA, P );
-		b.v = gmuladd( b.v, r.mB, P );
-		b.w += r.iB * gcross( rB, P );
-	}
-	store_velocity( W, r.ia, a.v, a.w );
-	store_velocity( W, r.ib, b.v, b.w );
-	store_impulses( W, k, r );
-}
-
-__device__ void ovf_restitution( const b2gDevWorld& W, int k, float threshold )
-{
-	Row r;
-	load_row( W, k, r );
-	if ( r.restitution == 0.0f )
+	bool changed = true;
+	if ( phase == 0 )
+		scalar ? warm_scalar( r, a, b ) : warm_lane( r, a, b );
+	else if ( phase == 1 || phase == 2 )
+		scalar ? solve_scalar( r, a, b, phase == 1, sc.inv_h, sc.pushout ) : solve_lane( r, a, b, phase == 1, sc.inv_h, sc.pushout );
+	else if ( scalar )
+		changed = restitution_scalar( r, a, b, sc.restitutionThreshold );
+	else
+		restitution_lane( r, a, b, sc.restitutionThreshold );
+	if ( changed == false )
 		return;
-	DevState a = load_state( W, r.ia );
-	DevState b = load_state( W, r.ib );
-	b2gVec n = r.n;
-	for ( int j = 0; j < r.count; ++j )
-	{
-		if ( r.relVel[j] > -threshold || r.maxNi[j] == 0.0f )
-			continue;
-		b2gVec rA = r.rA[j], rB = r.rB[j];
-		b2gVec vrB = gadd( b.v, gcross_sv( b.w, rB ) );
-		b2gVec vrA = gadd( a.v, gcross_sv( a.w, rA ) );
-		float vn = gdot( gsub( vrB, vrA ), n );
-		float impulse = -r.nMass[j] * ( vn + r.restitution * r.relVel[j] );
-		float newImpulse = gmax( r.ni[j] + impulse, 0.0f );
-		impulse = newImpulse - r.ni[j];
-		r.ni[j] = newImpulse;
-		r.maxNi[j] = gmax( r.maxNi[j], impulse );
-		b2gVec P = gmulsv( impulse, n );
-		a.v = gmulsub( a.v, r.mA, P );
-		a.w -= r.iA * gcross( rA, P );
-		b.v = gmuladd( b.v, r.mB, P );
-		b.w += r.iB * gcross( rB, P );
-	}
-	store_velocity( W, r.ia, a.v, a.w );
-	store_velocity( W, r.ib, b.v, b.w );
-	store_impulses( W, k, r );
+	store_velocity( W, r.ia, a );
+	store_velocity( W, r.ib, b );
+	if ( phase != 0 )
+		store_impulses( W, k, r );
 }
 
 /* ------------------------------------------------------------------ revolute joint */
-__device__ float rel_angle( b2gRot b, b2gRot a )
-{
-	float s = b.s * a.c - b.c * a.s;
-	float c = b.c * a.c + b.s * a.s;
-	return atan2f( s, c );
-}
-
-__device__ float unwind( float a )
-{
-	if ( a < -B2G_PI )
-		return a + 2.0f * B2G_PI;
-	if ( a > B2G_PI )
-		return a - 2.0f * B2G_PI;
-	return a;
-}
-
 __device__ void make_soft( float hertz, float zeta, float h, float* out )
 {
 	if ( hertz == 0.0f )
@@ -674,128 +388,17 @@ __global__ void k_prepare_joints( b2gDevWorld W, int count, b2gStepConst sc )
 	}
 }
 
-__device__ void joint_warm( const b2gDevWorld& W, int jid )
+__device__ void joint_phase( const b2gDevWorld& W, int jid, int phase, const b2gStepConst& sc )
 {
 	b2gJointDev* j = W.joints + jid;
 	DevState a = load_state( W, j->indexA );
 	DevState b = load_state( W, j->indexB );
-	b2gVec rA = grotate( a.dq, j->anchorA );
-	b2gVec rB = grotate( b.dq, j->anchorB );
-	float axial = j->springImpulse + j->motorImpulse + j->lowerImpulse - j->upperImpulse;
-	a.v = gmulsub( a.v, j->invMassA, j->linearImpulse );
-	a.w -= j->invIA * ( gcross( rA, j->linearImpulse ) + axial );
-	b.v = gmuladd( b.v, j->invMassB, j->linearImpulse );
-	b.w += j->invIB * ( gcross( rB, j->linearImpulse ) + axial );
-	store_velocity( W, j->indexA, a.v, a.w );
-	store_velocity( W, j->indexB, b.v, b.w );
-}
-
-__device__ void joint_solve( const b2gDevWorld& W, int jid, bool useBias, const b2gStepConst& sc )
-{
-	b2gJointDev* j = W.joints + jid;
-	float mA = j->invMassA, mB = j->invMassB, iA = j->invIA, iB = j->invIB;
-	DevState a = load_state( W, j->indexA );
-	DevState b = load_state( W, j->indexB );
-	b2gVec vA = a.v, vB = b.v;
-	float wA = a.w, wB = b.w;
-	bool fixedRotation = ( iA + iB == 0.0f );
-	if ( j->enableSpring && fixedRotation == false )
-	{
-		float C = rel_angle( b.dq, a.dq ) + j->deltaAngle;
-		float bias = j->springBias * C;
-		float Cdot = wB - wA;
-		float impulse = -j->springMass * j->axialMass * ( Cdot + bias ) - j->springImpulseScale * j->springImpulse;
-		j->springImpulse += impulse;
-		wA -= iA * impulse;
-		wB += iB * impulse;
-	}
-	if ( j->enableMotor && fixedRotation == false )
-	{
-		float Cdot = wB - wA - j->motorSpeed;
-		float impulse = -j->axialMass * Cdot;
-		float old = j->motorImpulse;
-		float maxImpulse = sc.h * j->maxMotorTorque;
-		j->motorImpulse = gclamp( j->motorImpulse + impulse, -maxImpulse, maxImpulse );
-		impulse = j->motorImpulse - old;
-		wA -= iA * impulse;
-		wB += iB * impulse;
-	}
-	if ( j->enableLimit && fixedRotation == false )
-	{
-		float angle = unwind( rel_angle( b.dq, a.dq ) + j->deltaAngle );
-		{
-			float C = angle - j->lowerAngle;
-			float bias = 0.0f, massScale = 1.0f, impulseScale = 0.0f;
-			if ( C > 0.0f )
-				bias = C * sc.inv_h;
-			else if ( useBias )
-			{
-				bias = sc.jointSoft[0] * C;
-				massScale = sc.jointSoft[1];
-				impulseScale = sc.jointSoft[2];
-			}
-			float Cdot = wB - wA;
-			float impulse = -massScale * j->axialMass * ( Cdot + bias ) - impulseScale * j->lowerImpulse;
-			float old = j->lowerImpulse;
-			j->lowerImpulse = gmax( j->lowerImpulse + impulse, 0.0f );
-			impulse = j->lowerImpulse - old;
-			wA -= iA * impulse;
-			wB += iB * impulse;
-		}
-		{
-			float C = j->upperAngle - angle;
-			float bias = 0.0f, massScale = 1.0f, impulseScale = 0.0f;
-			if ( C > 0.0f )
-				bias = C * sc.inv_h;
-			else if ( useBias )
-			{
-				bias = sc.jointSoft[0] * C;
-				massScale = sc.jointSoft[1];
-				impulseScale = sc.jointSoft[2];
-			}
-			float Cdot = wA - wB;
-			/* upper limit scaled by lowerImpulse, as in the reference (revolute_joint.c:409) */
-			float impulse = -massScale * j->axialMass * ( Cdot + bias ) - impulseScale * j->lowerImpulse;
-			float old = j->upperImpulse;
-			j->upperImpulse = gmax( j->upperImpulse + impulse, 0.0f );
-			impulse = j->upperImpulse - old;
-			wA += iA * impulse;
-			wB -= iB * impulse;
-		}
-	}
-	{
-		b2gVec rA = grotate( a.dq, j->anchorA );
-		b2gVec rB = grotate( b.dq, j->anchorB );
-		b2gVec Cdot = gsub( gadd( vB, gcross_sv( wB, rB ) ), gadd( vA, gcross_sv( wA, rA ) ) );
-		b2gVec bias = gv( 0.0f, 0.0f );
-		float massScale = 1.0f, impulseScale = 0.0f;
-		if ( useBias )
-		{
-			b2gVec sep = gadd( gadd( gsub( b.dp, a.dp ), gsub( rB, rA ) ), j->deltaCenter );
-			bias = gmulsv( sc.jointSoft[0], sep );
-			massScale = sc.jointSoft[1];
-			impulseScale = sc.jointSoft[2];
-		}
-		float k11 = mA + mB + rA.y * rA.y * iA + rB.y * rB.y * iB;
-		float k12 = -rA.y * rA.x * iA - rB.y * rB.x * iB;
-		float k22 = mA + mB + rA.x * rA.x * iA + rB.x * rB.x * iB;
-		b2gVec rhs = gadd( Cdot, bias );
-		float det = k11 * k22 - k12 * k12;
-		if ( det != 0.0f )
-			det = 1.0f / det;
-		b2gVec x = gv( det * ( k22 * rhs.x - k12 * rhs.y ), det * ( k11 * rhs.y - k12 * rhs.x ) );
-		b2gVec impulse;
-		impulse.x = -massScale * x.x - impulseScale * j->linearImpulse.x;
-		impulse.y = -massScale * x.y - impulseScale * j->linearImpulse.y;
-		j->linearImpulse.x += impulse.x;
-		j->linearImpulse.y += impulse.y;
-		vA = gmulsub( vA, mA, impulse );
-		wA -= iA * gcross( rA, impulse );
-		vB = gmuladd( vB, mB, impulse );
-		wB += iB * gcross( rB, impulse );
-	}
-	store_velocity( W, j->indexA, vA, wA );
-	store_velocity( W, j->indexB, vB, wB );
+	if ( phase == 0 )
+		joint_warm_state( j, a, b );
+	else
+		joint_solve_state( j, a, b, phase == 1, sc );
+	store_velocity( W, j->indexA, a );
+	store_velocity( W, j->indexB, b );
 }
 
 /* ------------------------------------------------------------------ phases */
@@ -814,27 +417,13 @@ __global__ void __launch_bounds__( BLOCK )
 	int t = blockIdx.x * blockDim.x + threadIdx.x;
 	if ( t < jointCount )
 	{
-		int jid = W.jointList[jointStart + t];
-		if ( phase == PH_WARM )
-			joint_warm( W, jid );
-		else if ( phase == PH_SOLVE )
-			joint_solve( W, jid, true, sc );
-		else if ( phase == PH_RELAX )
-			joint_solve( W, jid, false, sc );
+		joint_phase( W, W.jointList[jointStart + t], phase, sc );
 		return;
 	}
 	t -= jointCount;
 	if ( t >= rowCount )
 		return;
-	int k = rowStart + t;
-	if ( phase == PH_WARM )
-		lane_warm( W, k );
-	else if ( phase == PH_SOLVE )
-		lane_solve( W, k, true, sc.inv_h, sc.pushout );
-	else if ( phase == PH_RELAX )
-		lane_solve( W, k, false, sc.inv_h, sc.pushout );
-	else
-		lane_restitution( W, k, sc.restitutionThreshold );
+	row_phase( W, rowStart + t, phase, false, sc );
 }
 
 /* Overflow constraints share bodies, so they run serially in list order (joints first). */
@@ -845,26 +434,10 @@ __global__ void k_overflow( b2gDevWorld W, int phase, int jointStart, int jointC
 	if ( phase != PH_RESTITUTION )
 	{
 		for ( int i = 0; i < jointCount; ++i )
-		{
-			int jid = W.jointList[jointStart + i];
-			if ( phase == PH_WARM )
-				joint_warm( W, jid );
-			else
-				joint_solve( W, jid, phase == PH_SOLVE, sc );
-		}
+			joint_phase( W, W.jointList[jointStart + i], phase, sc );
 	}
 	for ( int i = 0; i < rowCount; ++i )
-	{
-		int k = rowStart + i;
-		if ( phase == PH_WARM )
-			ovf_warm( W, k );
-		else if ( phase == PH_SOLVE )
-			ovf_solve( W, k, true, sc.inv_h, sc.pushout );
-		else if ( phase == PH_RELAX )
-			ovf_solve( W, k, false, sc.inv_h, sc.pushout );
-		else
-			ovf_restitution( W, k, sc.restitutionThreshold );
-	}
+		row_phase( W, rowStart + i, phase, true, sc );
 }
 
 /* ------------------------------------------------------------------ bodies */
@@ -874,37 +447,10 @@ __global__ void __launch_bounds__( BLOCK ) k_integrate_velocities( b2gDevWorld W
 	if ( i >= awakeCount )
 		return;
 	int b = W.awake[i];
-	float4* st = (float4*)W.state;
-	float4 s0 = st[2 * b];
-	float4 ms = ( (const float4*)W.mass )[b];
-	float4 fo = ( (const float4*)W.force )[b];
-	float4 ex = ( (const float4*)W.extent )[b];
-	float h = sc.h;
-	float maxLin = B2G_MAX_TRANSLATION * sc.inv_dt;
-	float maxAng = B2G_MAX_ROTATION * sc.inv_dt;
-	float maxLin2 = maxLin * maxLin, maxAng2 = maxAng * maxAng;
-	b2gVec v = gv( s0.x, s0.y );
-	float w = s0.z;
-	float ld = 1.0f / ( 1.0f + h * ex.x );
-	float ad = 1.0f / ( 1.0f + h * ex.y );
-	b2gVec lvd = gmulsv( h * ms.y, gmuladd( gv( fo.x, fo.y ), ms.x * fo.w, sc.gravity ) );
-	float avd = h * ms.w * fo.z;
-	v = gmuladd( lvd, ld, v );
-	w = avd + ad * w;
-	if ( gdot( v, v ) > maxLin2 )
-	{
-		float ratio = maxLin / glen( v );
-		v = gmulsv( ratio, v );
-	}
-	if ( w * w > maxAng2 )
-	{
-		float ratio = maxAng / gabs( w );
-		w *= ratio;
-	}
-	s0.x = v.x;
-	s0.y = v.y;
-	s0.z = w;
-	st[2 * b] = s0;
+	DevState s = load_state( W, b );
+	VelocityTerms t = velocity_terms( ( (const float4*)W.mass )[b], ( (const float4*)W.force )[b], ( (const float4*)W.extent )[b], sc );
+	integrate_velocity( s, t, sc );
+	store_velocity( W, b, s );
 }
 
 __global__ void __launch_bounds__( BLOCK ) k_integrate_positions( b2gDevWorld W, int awakeCount, b2gStepConst sc )
@@ -913,12 +459,9 @@ __global__ void __launch_bounds__( BLOCK ) k_integrate_positions( b2gDevWorld W,
 	if ( i >= awakeCount )
 		return;
 	int b = W.awake[i];
-	float4* st = (float4*)W.state;
-	float4 s0 = st[2 * b];
-	float4 s1 = st[2 * b + 1];
-	b2gRot dq = gintrot( grot( s1.z, s1.w ), sc.h * s0.z );
-	b2gVec dp = gmuladd( gv( s1.x, s1.y ), sc.h, gv( s0.x, s0.y ) );
-	st[2 * b + 1] = make_float4( dp.x, dp.y, dq.c, dq.s );
+	DevState s = load_state( W, b );
+	integrate_position( s, sc.h );
+	( (float4*)W.state )[2 * b + 1] = make_float4( s.dp.x, s.dp.y, s.dq.c, s.dq.s );
 }
 
 __global__ void __launch_bounds__( BLOCK ) k_store( b2gDevWorld W, int total, int overflowStart )
@@ -1190,6 +733,18 @@ extern "C" int b2gd_contact_solver( b2gDevWorld* w, const b2gSolvePlan* plan, co
 	return launches;
 }
 
+/* Prepares the step's joints (all colours); used by the fused solver, which runs
+ * everything else of the solver stage. */
+extern "C" int b2gd_prepare_joints( b2gDevWorld* w, int joints, const b2gStepConst* sc )
+{
+	if ( joints <= 0 )
+		return 0;
+	k_prepare_joints<<<blocks_for( joints ), BLOCK, 0, (cudaStream_t)w->stream>>>( *w, joints, *sc );
+	return 1;
+}
+
+extern "C" int b2gd_solver_fused( b2gDevWorld* w, const b2gSolvePlan* plan, const b2gStepConst* sc );
+
 extern "C" int b2gd_solve( b2gDevWorld* w, b2gHostIO* io, const b2gSolvePlan* plan, const b2gStepConst* scp )
 {
 	cudaStream_t s = (cudaStream_t)w->stream;
@@ -1197,7 +752,11 @@ extern "C" int b2gd_solve( b2gDevWorld* w, b2gHostIO* io, const b2gSolvePlan* pl
 	if ( w->timing )
 		cudaEventRecord( (cudaEvent_t)w->timers[3], s );
 	cudaMemsetAsync( w->counters + 1, 0, sizeof( int ), s );
-	w->launches += b2gd_contact_solver( w, plan, scp );
+	int fused = w->fused ? b2gd_solver_fused( w, plan, scp ) : 0;
+	if ( fused < 0 )
+		return check( cudaGetLastError() );
+	w->fusedUsed = fused > 0;
+	w->launches += fused > 0 ? fused : b2gd_contact_solver( w, plan, scp );
 	if ( w->timing )
 		cudaEventRecord( (cudaEvent_t)w->timers[4], s );
 	if ( awake > 0 )

@@ -663,6 +663,7 @@ void gstep_run( gWorld* w, float dt, int subSteps )
 	b2gSolvePlan plan;
 	build_solve_lists( w, &plan );
 	plan.awakeCount = w->awake.count;
+	plan.bodyIdCount = w->bodyIds.next;
 	if ( w->solveDirty )
 	{
 		e = b2gd_upload_solve_lists( &w->dev, w->solveList.data, w->solveList.count, w->jointList.data, w->jointList.count );

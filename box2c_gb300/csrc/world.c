@@ -1325,7 +1325,14 @@ b2DeviceTimes b2World_GetDeviceTimes( b2WorldId worldId )
 	t.eventCount = w->lastEventCount;
 	t.recordCount = w->lastRecordCount;
 	t.launches = w->dev.launches;
+	t.fusedSolver = w->dev.fusedUsed;
 	return t;
+}
+
+void b2World_EnableFusedSolver( b2WorldId worldId, bool flag )
+{
+	gWorld* w = gworld_get( worldId );
+	w->dev.fused = flag ? 1 : 0;
 }
 
 int b2World_GetBodyStates( b2WorldId worldId, float* out, int capacity )

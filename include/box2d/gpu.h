@@ -34,10 +34,17 @@ typedef struct b2DeviceTimes
 	int eventCount;	 /* narrowphase begin/end/disjoint events */
 	int recordCount; /* finalisation records (grown proxies, fast shapes) */
 	int launches;	 /* kernel launches of the last step */
+	int fusedSolver; /* 1 when the last step's solver stage ran as one fused launch */
 } b2DeviceTimes;
 
 B2_API void b2World_EnableDeviceTiming( b2WorldId worldId, bool flag );
 B2_API b2DeviceTimes b2World_GetDeviceTimes( b2WorldId worldId );
+
+/* Solver-stage implementation: one fused launch of a 16-CTA cluster that keeps the
+ * world's bodies and constraint rows in shared memory (the default; used whenever the
+ * world fits, roughly 20k contacts), or one kernel launch per phase.  Both give
+ * bit-identical results. */
+B2_API void b2World_EnableFusedSolver( b2WorldId worldId, bool flag );
 
 /* Copies p.x p.y q.c q.s v.x v.y w (7 floats) of every body id into out (7 * capacity
  * floats).  One device-to-host copy per call.  Returns the number of body ids. */

@@ -6,7 +6,7 @@ import os
 import numpy as np
 import pytest
 
-from box2c_gb300.capi import contact_table
+from box2c_gb300.capi import bind_gpu_api, contact_table
 from tests.golden.make_golden import SCENES, make_scene, digest
 from tests.helpers import lockstep
 
@@ -79,3 +79,40 @@ def test_gpu_large_pyramid_full_size(gpu, oracle):
     assert np.isfinite(bg).all()
     assert np.array_equal(tg, to)
     assert np.array_equal(bg.view(np.uint32), bo.view(np.uint32))
+
+
+def _per_phase(gpu, world):
+    bind_gpu_api(gpu.lib)
+    gpu.lib.b2World_EnableFusedSolver(world, False)
+    return world
+
+
+@pytest.mark.parametrize("scene,steps,sub", [("pyramid20", 150, 4), ("tumbler", 100, 4), ("tilted", 60, 3)])
+def test_gpu_per_phase_solver_lockstep_oracle(gpu, oracle, scene, steps, sub):
+    """The one-launch-per-phase solver path (used when a world does not fit on chip)."""
+    scenes = {
+        "pyramid20": lambda b: b.pyramid(20),
+        "tumbler": lambda b: b.tumbler(900, 5, 0),
+        "tilted": lambda b: b.tilted_stacks(),
+    }
+
+    def make(b):
+        w = scenes[scene](b)
+        return _per_phase(b, w) if b is gpu else w
+
+    step, detail, _ = lockstep(gpu, oracle, make, steps, substeps=sub, check_manifolds=True)
+    assert step is None, f"{scene}: {detail} at step {step}"
+
+
+@pytest.mark.parametrize("fused", [True, False])
+def test_gpu_solver_path_selection(gpu, fused):
+    """The large pyramid runs its solver stage fused by default; both paths agree."""
+    bind_gpu_api(gpu.lib)
+    w = gpu.pyramid(100, 0.01, 1235)
+    gpu.lib.b2World_EnableFusedSolver(w, fused)
+    gpu.step(w, count=3)
+    t = gpu.lib.b2World_GetDeviceTimes(w)
+    status = gpu.lib.b2World_GetStatus(w)
+    gpu.destroy(w)
+    assert status == 0
+    assert t.fusedSolver == (1 if fused else 0)
