@@ -192,6 +192,7 @@ def run_gpu(args):
 
     step_ms, solve_ms, collide_ms, finalize_ms, launches = [], [], [], [], []
     fused_steps = 0
+    host_prof = []
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
@@ -209,6 +210,8 @@ def run_gpu(args):
             collide_ms.append(t.collide)
             finalize_ms.append(t.finalize)
             launches.append(t.launches)
+            p = L.b2World_GetProfile(w)
+            host_prof.append((p.step, p.pairs, p.collide, p.solve, p.broadphase))
             fused_steps += t.fusedSolver
     torch.cuda.synchronize()
     ms = float(np.mean(step_ms))
@@ -255,6 +258,8 @@ def run_gpu(args):
                    "solver": "fused cluster kernel" if fused_steps == args.steps else "per-phase kernels"},
         "stages_ms": {"collide": round(float(np.mean(collide_ms)), 4), "solve": round(solve_dev, 4),
                       "finalize": round(float(np.mean(finalize_ms)), 4)},
+        "host_ms": dict(zip(("step", "pairs", "collide_and_events", "solve_and_sync", "records"),
+                            [round(float(x), 4) for x in np.mean(np.array(host_prof), 0)])),
         "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": None, "kernel": "solver stage (prepare..store)",
                      "algorithmic_bytes_per_step": solver_bytes, "peak_kind": peak_kind},

@@ -145,6 +145,8 @@ extern "C" void b2gd_free( b2gDevWorld* w, b2gHostIO* io )
 		cudaFreeHost( io->counters );
 	if ( io->newContacts )
 		cudaFreeHost( io->newContacts );
+	if ( w->stage )
+		cudaFree( w->stage );
 	if ( w->stream )
 		cudaStreamDestroy( (cudaStream_t)w->stream );
 	memset( w, 0, sizeof( *w ) );

@@ -13,6 +13,10 @@ extern "C" {
 /* Colour-major layout of one step's constraint rows and joint list.  Colour c (0..10)
  * owns rows [colorStart[c], colorStart[c+1]) and joints [jointStart[c], jointStart[c+1]);
  * colour 11 is the overflow set, solved serially in list order. */
+/* CTAs of the fused solver's thread-block cluster; body id b belongs to CTA
+ * b / bodyBlock. */
+#define B2G_FUSED_CTAS 16
+
 typedef struct b2gSolvePlan
 {
 	int colorStart[B2G_COLORS + 1];
@@ -21,6 +25,11 @@ typedef struct b2gSolvePlan
 	int activeCount;
 	int awakeCount;
 	int bodyIdCount; /* body ids in use (0: caller buffers, per-phase kernels only) */
+	/* Within colour c (< 11) the rows are grouped by the CTA owning their first
+	 * non-static body: rowSplit[c][o] rows for CTA o, in CTA order.  bodyBlock = 0 means
+	 * no grouping (the fused solver is not used). */
+	int bodyBlock;
+	int rowSplit[B2G_OVERFLOW][B2G_FUSED_CTAS];
 } b2gSolvePlan;
 
 /* Pinned host staging owned by the device module (mapped into the device). */

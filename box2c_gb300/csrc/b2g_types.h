@@ -16,6 +16,8 @@
 
 #include "b2g_math.h"
 
+#include <stddef.h>
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -203,6 +205,8 @@ typedef struct b2gDevWorld
 	int launches;
 	int fused;	   /* use the fused cluster solver when the world fits on chip */
 	int fusedUsed; /* the last step's solver stage ran fused */
+	void* stage;   /* fused solver: per-CTA shared-memory images */
+	size_t stageBytes;
 } b2gDevWorld;
 
 #ifdef __cplusplus

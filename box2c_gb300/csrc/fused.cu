@@ -31,10 +31,12 @@
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
+#include <string.h>
+
 namespace cg = cooperative_groups;
 
 #define FUSED_THREADS 256
-#define FUSED_CLUSTER 16
+#define FUSED_CLUSTER B2G_FUSED_CTAS
 /* dynamic shared memory per CTA, leaving 1 KB of the 227 KB opt-in limit for statics */
 #define FUSED_SMEM_MAX ( 226 * 1024 )
 
@@ -52,20 +54,28 @@ struct FusedPlan
 	int jointStart[B2G_COLORS + 1];
 	int active[B2G_COLORS];
 	int activeCount;
-	int awakeCount;
 	int bodyIdCount;
-	int bodySlots; /* body slots per CTA */
+	int bodySlots; /* body slots per CTA: body b lives in CTA b / bodySlots */
 	int rowCap;	   /* row slots per CTA */
+	int imageFloat4;
+	/* rows of colour c owned by CTA o: offsets [split[c][o], split[c][o+1]) within the
+	 * colour, stored from local index ctaBase[c][o]; the overflow rows live in CTA 0 from
+	 * ctaBase[B2G_OVERFLOW][0] */
+	int split[B2G_OVERFLOW][B2G_FUSED_CTAS + 1];
+	int ctaBase[B2G_COLORS][B2G_FUSED_CTAS];
 };
 
 /* Shared-memory carve-up; every CTA uses the same offsets, so a local address maps to
- * the same object in another CTA. */
+ * the same object in another CTA.  The first imageFloat4 float4 are the image the
+ * staging kernel writes to global memory (rows, bodies, awake flags); the local awake
+ * list follows it. */
 struct FusedSmem
 {
 	float4* st0;   /* v.x v.y w tag */
 	float4* st1;   /* dp.x dp.y dq.c dq.s */
 	float4* term;  /* lvd.x lvd.y avd ld */
 	float* ad;	   /* angular damping factor */
+	int* flags;	   /* 1 for an awake body */
 	int* awake;	   /* local awake slots */
 	int4* idx;	   /* ia ib contactId count */
 	float4* nf;	   /* n.x n.y friction restitution */
@@ -78,9 +88,15 @@ struct FusedSmem
 	float4* imp1;
 };
 
-static __host__ __device__ size_t fused_smem_bytes( int bodySlots, int rowCap )
+static __host__ __device__ int image_float4( int bodySlots, int rowCap )
 {
-	return (size_t)bodySlots * ( 3 * 16 + 4 + 4 ) + (size_t)rowCap * ( 9 * 16 ) + 64;
+	/* 9 row arrays, 3 body float4 arrays, two body 4-byte arrays */
+	return 9 * rowCap + 3 * bodySlots + ( 2 * bodySlots + 3 ) / 4;
+}
+
+static size_t fused_smem_bytes( int bodySlots, int rowCap )
+{
+	return 16 * (size_t)image_float4( bodySlots, rowCap ) + 4 * (size_t)bodySlots + 16;
 }
 
 __device__ __forceinline__ FusedSmem carve( float4* base, int BS, int RC )
@@ -99,34 +115,50 @@ __device__ __forceinline__ FusedSmem carve( float4* base, int BS, int RC )
 	m.st1 = m.st0 + BS;
 	m.term = m.st1 + BS;
 	m.ad = (float*)( m.term + BS );
-	m.awake = (int*)( m.ad + BS );
+	m.flags = (int*)( m.ad + BS );
+	m.awake = (int*)( base + image_float4( BS, RC ) );
 	return m;
 }
 
-template <int CL>
+/* Body states of the cluster: body b lives in CTA b / slots at slot b % slots.  A body
+ * of this CTA is read and written in local shared memory, any other through
+ * distributed shared memory. */
 struct ClusterBodies
 {
 	cg::cluster_group cl;
 	float4* st0;
 	float4* st1;
+	int slots;
+	int rank;
 
+	__device__ __forceinline__ float4* word( float4* base, int b ) const
+	{
+		int r = b / slots;
+		int s = b - r * slots;
+		return r == rank ? base + s : cl.map_shared_rank( base + s, (unsigned)r );
+	}
+
+	/* full state (solve, relax, joints) */
 	__device__ __forceinline__ DevState load( int b ) const
 	{
 		if ( b < 0 )
 			return identity_state();
-		unsigned r = (unsigned)b % CL;
-		int s = b / CL;
-		const float4* p0 = cl.map_shared_rank( st0 + s, r );
-		const float4* p1 = cl.map_shared_rank( st1 + s, r );
-		return state_of( *p0, *p1 );
+		return state_of( *word( st0, b ), *word( st1, b ) );
+	}
+
+	/* velocity only (warm start, restitution): dp and dq are not read */
+	__device__ __forceinline__ DevState load_velocity( int b ) const
+	{
+		if ( b < 0 )
+			return identity_state();
+		return state_of( *word( st0, b ), make_float4( 0.0f, 0.0f, 1.0f, 0.0f ) );
 	}
 
 	__device__ __forceinline__ void store( int b, const DevState& x ) const
 	{
 		if ( b < 0 )
 			return;
-		float4* p0 = cl.map_shared_rank( st0 + b / CL, (unsigned)b % CL );
-		*p0 = velocity_word( x );
+		*word( st0, b ) = velocity_word( x );
 	}
 };
 
@@ -183,14 +215,14 @@ __device__ __forceinline__ void store_row_smem( const FusedSmem& m, int k, int c
 	m.imp1[k] = make_float4( r.ni[1], r.ti[1], r.maxNi[1], 0.0f );
 }
 
-template <int CL>
-__device__ __forceinline__ void row_step( const FusedSmem& m, const ClusterBodies<CL>& B, int k, int phase, bool scalar,
+__device__ __forceinline__ void row_step( const FusedSmem& m, const ClusterBodies& B, int k, int phase, bool scalar,
 										  const b2gStepConst& sc )
 {
 	Row r;
 	load_row_smem( m, k, sc, r );
-	DevState a = B.load( r.ia );
-	DevState b = B.load( r.ib );
+	bool delta = phase == F_SOLVE || phase == F_RELAX;
+	DevState a = delta ? B.load( r.ia ) : B.load_velocity( r.ia );
+	DevState b = delta ? B.load( r.ib ) : B.load_velocity( r.ib );
 	bool changed = true;
 	if ( phase == F_WARM )
 		scalar ? warm_scalar( r, a, b ) : warm_lane( r, a, b );
@@ -212,8 +244,7 @@ __device__ __forceinline__ void row_step( const FusedSmem& m, const ClusterBodie
 	}
 }
 
-template <int CL>
-__device__ __forceinline__ void joint_step( const b2gDevWorld& W, const ClusterBodies<CL>& B, int jid, int phase,
+__device__ __forceinline__ void joint_step( const b2gDevWorld& W, const ClusterBodies& B, int jid, int phase,
 											const b2gStepConst& sc )
 {
 	b2gJointDev* j = W.joints + jid;
@@ -232,8 +263,8 @@ __device__ __forceinline__ int local_count( int n, int rank, int CL ) { return n
 /* One stage over all colours: the overflow set first (serially, CTA 0 thread 0), then
  * each active colour with a cluster barrier after it. */
 template <int CL>
-__device__ void run_stage( const b2gDevWorld& W, const FusedPlan& P, const FusedSmem& m, const ClusterBodies<CL>& B,
-						   const int* base, int rank, int phase, const b2gStepConst& sc )
+__device__ void run_stage( const b2gDevWorld& W, const FusedPlan& P, const FusedSmem& m, const ClusterBodies& B, int rank,
+						   int phase, const b2gStepConst& sc )
 {
 	const int* cs = P.colorStart;
 	const int* js = P.jointStart;
@@ -248,9 +279,10 @@ __device__ void run_stage( const b2gDevWorld& W, const FusedPlan& P, const Fused
 		if ( rank == 0 && threadIdx.x == 0 )
 		{
 			for ( int i = 0; i < ovJoints; ++i )
-				joint_step<CL>( W, B, W.jointList[js[B2G_OVERFLOW] + i], phase, sc );
+				joint_step( W, B, W.jointList[js[B2G_OVERFLOW] + i], phase, sc );
+			int base = P.ctaBase[B2G_OVERFLOW][0];
 			for ( int i = 0; i < ovRows; ++i )
-				row_step<CL>( m, B, base[B2G_OVERFLOW] + i, phase, true, sc );
+				row_step( m, B, base + i, phase, true, sc );
 		}
 		B.cl.sync();
 	}
@@ -259,23 +291,79 @@ __device__ void run_stage( const b2gDevWorld& W, const FusedPlan& P, const Fused
 	for ( int a = 0; a < P.activeCount; ++a )
 	{
 		int c = P.active[a];
-		int nr = local_count( cs[c + 1] - cs[c], rank, CL );
-		int nj = phase == F_RESTITUTION ? 0 : local_count( js[c + 1] - js[c], rank, CL );
 		if ( phase == F_RESTITUTION && cs[c + 1] == cs[c] )
 			continue;
+		int base = P.ctaBase[c][rank];
+		int nr = P.split[c][rank + 1] - P.split[c][rank];
+		int nj = phase == F_RESTITUTION ? 0 : local_count( js[c + 1] - js[c], rank, CL );
 		for ( int j = threadIdx.x; j < nr; j += FUSED_THREADS )
-			row_step<CL>( m, B, base[c] + j, phase, false, sc );
+			row_step( m, B, base + j, phase, false, sc );
 		for ( int j = threadIdx.x; j < nj; j += FUSED_THREADS )
-			joint_step<CL>( W, B, W.jointList[js[c] + rank + j * CL], phase, sc );
+			joint_step( W, B, W.jointList[js[c] + rank + j * CL], phase, sc );
 		B.cl.sync();
 	}
 }
 
+/* Staging: writes every CTA's shared-memory image (constraint rows, reference
+ * src/contact_solver.c:597-808 and :21-147; body states; per-step velocity terms,
+ * src/solver.c:34-93) to global memory, one thread per row and per body id. */
+__global__ void __launch_bounds__( 256 ) k_fused_stage( b2gDevWorld W, FusedPlan P, b2gStepConst sc, float4* image )
+{
+	int t = blockIdx.x * blockDim.x + threadIdx.x;
+	const int* cs = P.colorStart;
+	const int BS = P.bodySlots, RC = P.rowCap;
+	const float4* gst = (const float4*)W.state;
+	const float4* mass = (const float4*)W.mass;
+	if ( t < cs[B2G_COLORS] )
+	{
+		int c = 0;
+		while ( cs[c + 1] <= t )
+			++c;
+		int o = 0, local;
+		if ( c == B2G_OVERFLOW )
+			local = P.ctaBase[B2G_OVERFLOW][0] + ( t - cs[B2G_OVERFLOW] );
+		else
+		{
+			int i = t - cs[c];
+			while ( P.split[c][o + 1] <= i )
+				++o;
+			local = P.ctaBase[c][o] + ( i - P.split[c][o] );
+		}
+		FusedSmem m = carve( image + (size_t)o * P.imageFloat4, BS, RC );
+		int cid = W.solveList[t];
+		int ia = W.cBodies[2 * cid];
+		int ib = W.cBodies[2 * cid + 1];
+		float4 zero = make_float4( 0.0f, 0.0f, 0.0f, 0.0f );
+		DevState sA = ia >= 0 ? state_of( gst[2 * ia], gst[2 * ia + 1] ) : identity_state();
+		DevState sB = ib >= 0 ? state_of( gst[2 * ib], gst[2 * ib + 1] ) : identity_state();
+		Row r;
+		prepare_row( r, W.manifold + cid, ia, ib, ia >= 0 ? mass[ia] : zero, ib >= 0 ? mass[ib] : zero, sA, sB,
+					 W.cMix[2 * cid], W.cMix[2 * cid + 1], ( ia < 0 || ib < 0 ) ? sc.staticSoft : sc.contactSoft,
+					 sc.enableWarmStarting ? 1.0f : 0.0f );
+		store_row_smem( m, local, cid, r );
+	}
+	if ( t < P.bodyIdCount )
+	{
+		int o = t / BS;
+		int s = t - o * BS;
+		FusedSmem m = carve( image + (size_t)o * P.imageFloat4, BS, RC );
+		m.st0[s] = gst[2 * t];
+		m.st1[s] = gst[2 * t + 1];
+		bool awake = ( W.bodyInfo[t] & B2G_B_AWAKE ) != 0;
+		m.flags[s] = awake ? 1 : 0;
+		if ( awake )
+		{
+			VelocityTerms v = velocity_terms( mass[t], ( (const float4*)W.force )[t], ( (const float4*)W.extent )[t], sc );
+			m.term[s] = make_float4( v.lvd.x, v.lvd.y, v.avd, v.ld );
+			m.ad[s] = v.ad;
+		}
+	}
+}
+
 template <int CL>
-__global__ void __launch_bounds__( FUSED_THREADS ) k_solve_fused( b2gDevWorld W, FusedPlan P, b2gStepConst sc )
+__global__ void __launch_bounds__( FUSED_THREADS ) k_solve_fused( b2gDevWorld W, FusedPlan P, b2gStepConst sc, const float4* image )
 {
 	extern __shared__ float4 smem[];
-	__shared__ int base[B2G_COLORS + 1];
 	__shared__ int awakeLocal;
 	cg::cluster_group cl = cg::this_cluster();
 	const int rank = (int)cl.block_rank();
@@ -284,74 +372,23 @@ __global__ void __launch_bounds__( FUSED_THREADS ) k_solve_fused( b2gDevWorld W,
 	FusedSmem m = carve( smem, BS, P.rowCap );
 	const int* cs = P.colorStart;
 
+	/* this CTA's image: rows, owned bodies, velocity terms, awake flags */
+	const float4* src = image + (size_t)rank * P.imageFloat4;
+	const int n4 = P.imageFloat4;
+#pragma unroll 4
+	for ( int i = tid; i < n4; i += FUSED_THREADS )
+		smem[i] = src[i];
 	if ( tid == 0 )
-	{
-		/* local row bases: active colours in order, then the overflow set (CTA 0 only) */
-		int n = 0;
-		for ( int c = 0; c <= B2G_COLORS; ++c )
-			base[c] = 0;
-		for ( int a = 0; a < P.activeCount; ++a )
-		{
-			int c = P.active[a];
-			base[c] = n;
-			n += local_count( cs[c + 1] - cs[c], rank, CL );
-		}
-		base[B2G_OVERFLOW] = n;
 		awakeLocal = 0;
-	}
-
-	/* owned body states */
-	const float4* gst = (const float4*)W.state;
-	for ( int s = tid; s < BS; s += FUSED_THREADS )
-	{
-		int b = s * CL + rank;
-		if ( b < P.bodyIdCount )
-		{
-			m.st0[s] = gst[2 * b];
-			m.st1[s] = gst[2 * b + 1];
-		}
-	}
 	__syncthreads();
-
-	/* owned awake bodies and their per-step velocity terms */
-	for ( int i = tid; i < P.awakeCount; i += FUSED_THREADS )
+	int bodies = P.bodyIdCount - rank * BS;
+	bodies = bodies < 0 ? 0 : ( bodies > BS ? BS : bodies );
+	for ( int s = tid; s < bodies; s += FUSED_THREADS )
 	{
-		int b = W.awake[i];
-		if ( b % CL != rank )
-			continue;
-		int s = b / CL;
-		int slot = atomicAdd( &awakeLocal, 1 );
-		m.awake[slot] = s;
-		VelocityTerms t = velocity_terms( ( (const float4*)W.mass )[b], ( (const float4*)W.force )[b],
-										  ( (const float4*)W.extent )[b], sc );
-		m.term[s] = make_float4( t.lvd.x, t.lvd.y, t.avd, t.ld );
-		m.ad[s] = t.ad;
+		if ( m.flags[s] )
+			m.awake[atomicAdd( &awakeLocal, 1 )] = s;
 	}
-
-	/* constraint rows (reference src/contact_solver.c:597-808), from the global state */
-	const float4* mass = (const float4*)W.mass;
-	const float4 zero = make_float4( 0.0f, 0.0f, 0.0f, 0.0f );
-	const float warm = sc.enableWarmStarting ? 1.0f : 0.0f;
-	for ( int a = -1; a < P.activeCount; ++a )
-	{
-		int c = a < 0 ? B2G_OVERFLOW : P.active[a];
-		int n = cs[c + 1] - cs[c];
-		int local = c == B2G_OVERFLOW ? ( rank == 0 ? n : 0 ) : local_count( n, rank, CL );
-		for ( int j = tid; j < local; j += FUSED_THREADS )
-		{
-			int i = c == B2G_OVERFLOW ? j : rank + j * CL;
-			int cid = W.solveList[cs[c] + i];
-			int ia = W.cBodies[2 * cid];
-			int ib = W.cBodies[2 * cid + 1];
-			DevState sA = ia >= 0 ? state_of( gst[2 * ia], gst[2 * ia + 1] ) : identity_state();
-			DevState sB = ib >= 0 ? state_of( gst[2 * ib], gst[2 * ib + 1] ) : identity_state();
-			Row r;
-			prepare_row( r, W.manifold + cid, ia, ib, ia >= 0 ? mass[ia] : zero, ib >= 0 ? mass[ib] : zero, sA, sB,
-						 W.cMix[2 * cid], W.cMix[2 * cid + 1], ( ia < 0 || ib < 0 ) ? sc.staticSoft : sc.contactSoft, warm );
-			store_row_smem( m, base[c] + j, cid, r );
-		}
-	}
-	ClusterBodies<CL> B{ cl, m.st0, m.st1 };
+	ClusterBodies B{ cl, m.st0, m.st1, BS, rank };
 	cl.sync();
 
 	for ( int sub = 0; sub < sc.subSteps; ++sub )
@@ -370,8 +407,8 @@ __global__ void __launch_bounds__( FUSED_THREADS ) k_solve_fused( b2gDevWorld W,
 			m.st0[s] = velocity_word( x );
 		}
 		cl.sync();
-		run_stage<CL>( W, P, m, B, base, rank, F_WARM, sc );
-		run_stage<CL>( W, P, m, B, base, rank, F_SOLVE, sc );
+		run_stage<CL>( W, P, m, B, rank, F_WARM, sc );
+		run_stage<CL>( W, P, m, B, rank, F_SOLVE, sc );
 		for ( int j = tid; j < awakeLocal; j += FUSED_THREADS )
 		{
 			int s = m.awake[j];
@@ -380,18 +417,24 @@ __global__ void __launch_bounds__( FUSED_THREADS ) k_solve_fused( b2gDevWorld W,
 			m.st1[s] = make_float4( x.dp.x, x.dp.y, x.dq.c, x.dq.s );
 		}
 		cl.sync();
-		run_stage<CL>( W, P, m, B, base, rank, F_RELAX, sc );
+		run_stage<CL>( W, P, m, B, rank, F_RELAX, sc );
 	}
-	run_stage<CL>( W, P, m, B, base, rank, F_RESTITUTION, sc );
+	run_stage<CL>( W, P, m, B, rank, F_RESTITUTION, sc );
 
 	/* store impulses (reference src/contact_solver.c:442-471, :1180-1293): colour rows
 	 * write both point slots, overflow rows their points */
-	int localRows = base[B2G_OVERFLOW] + ( rank == 0 ? cs[B2G_COLORS] - cs[B2G_OVERFLOW] : 0 );
+	int colourRows = 0;
+	for ( int a = 0; a < P.activeCount; ++a )
+	{
+		int c = P.active[a];
+		colourRows += P.split[c][rank + 1] - P.split[c][rank];
+	}
+	int localRows = colourRows + ( rank == 0 ? cs[B2G_COLORS] - cs[B2G_OVERFLOW] : 0 );
 	for ( int k = tid; k < localRows; k += FUSED_THREADS )
 	{
 		int4 idx = m.idx[k];
 		b2gManifold* mf = W.manifold + idx.z;
-		int n = k < base[B2G_OVERFLOW] ? 2 : idx.w;
+		int n = k < colourRows ? 2 : idx.w;
 		float4 imp[2] = { m.imp0[k], m.imp1[k] };
 		float4 coef[2] = { m.coef0[k], m.coef1[k] };
 		for ( int j = 0; j < n; ++j )
@@ -407,29 +450,47 @@ __global__ void __launch_bounds__( FUSED_THREADS ) k_solve_fused( b2gDevWorld W,
 	for ( int j = tid; j < awakeLocal; j += FUSED_THREADS )
 	{
 		int s = m.awake[j];
-		int b = s * CL + rank;
+		int b = rank * BS + s;
 		gout[2 * b] = m.st0[s];
 		gout[2 * b + 1] = m.st1[s];
 	}
 }
 
-/* Launches the fused solver when the world fits on chip; returns the number of launches,
- * or 0 when the world does not fit (or clusters of FUSED_CLUSTER are unavailable) and the
- * caller must use the per-phase kernels. */
 extern "C" int b2gd_prepare_joints( b2gDevWorld* w, int joints, const b2gStepConst* sc );
 
+static cudaLaunchConfig_t cluster_config( cudaLaunchAttribute* attr, size_t smem, cudaStream_t stream )
+{
+	cudaLaunchConfig_t cfg = {};
+	attr[0].id = cudaLaunchAttributeClusterDimension;
+	attr[0].val.clusterDim.x = FUSED_CLUSTER;
+	attr[0].val.clusterDim.y = 1;
+	attr[0].val.clusterDim.z = 1;
+	cfg.gridDim = dim3( FUSED_CLUSTER, 1, 1 );
+	cfg.blockDim = dim3( FUSED_THREADS, 1, 1 );
+	cfg.dynamicSmemBytes = smem;
+	cfg.stream = stream;
+	cfg.attrs = attr;
+	cfg.numAttrs = 1;
+	return cfg;
+}
+
+/* Launches the fused solver when the world fits on chip; returns the number of launches,
+ * 0 when it does not fit (or clusters of FUSED_CLUSTER CTAs are unavailable) and the
+ * caller must use the per-phase kernels, or -1 on a launch error. */
 extern "C" int b2gd_solver_fused( b2gDevWorld* w, const b2gSolvePlan* plan, const b2gStepConst* sc )
 {
 	/* per device: 0 unknown, 1 available, -1 unavailable */
 	static int s_readyByDevice[64];
 	const int CL = FUSED_CLUSTER;
+	if ( plan->bodyIdCount <= 0 || plan->bodyBlock <= 0 )
+		return 0;
 	int dev = 0;
 	if ( cudaGetDevice( &dev ) != cudaSuccess || dev < 0 || dev >= 64 )
 		return 0;
-	int& s_ready = s_readyByDevice[dev];
-	if ( plan->bodyIdCount <= 0 )
-		return 0;
+	int& ready = s_readyByDevice[dev];
+
 	FusedPlan P;
+	memset( &P, 0, sizeof( P ) );
 	for ( int c = 0; c <= B2G_COLORS; ++c )
 	{
 		P.colorStart[c] = plan->colorStart[c];
@@ -438,62 +499,78 @@ extern "C" int b2gd_solver_fused( b2gDevWorld* w, const b2gSolvePlan* plan, cons
 	for ( int c = 0; c < B2G_COLORS; ++c )
 		P.active[c] = plan->active[c];
 	P.activeCount = plan->activeCount;
-	P.awakeCount = plan->awakeCount;
 	P.bodyIdCount = plan->bodyIdCount;
-	P.bodySlots = ( plan->bodyIdCount + CL - 1 ) / CL;
-	int rows = 0;
+	P.bodySlots = plan->bodyBlock;
+	int perCta[B2G_FUSED_CTAS] = { 0 };
+	for ( int c = 0; c < B2G_OVERFLOW; ++c )
+	{
+		int n = 0;
+		for ( int o = 0; o < CL; ++o )
+		{
+			P.split[c][o] = n;
+			n += plan->rowSplit[c][o];
+		}
+		P.split[c][CL] = n;
+		if ( n != plan->colorStart[c + 1] - plan->colorStart[c] )
+			return 0; /* rows not grouped by owner */
+	}
 	for ( int a = 0; a < plan->activeCount; ++a )
 	{
 		int c = plan->active[a];
-		rows += ( plan->colorStart[c + 1] - plan->colorStart[c] + CL - 1 ) / CL;
+		for ( int o = 0; o < CL; ++o )
+		{
+			P.ctaBase[c][o] = perCta[o];
+			perCta[o] += plan->rowSplit[c][o];
+		}
 	}
-	rows += plan->colorStart[B2G_COLORS] - plan->colorStart[B2G_OVERFLOW];
-	P.rowCap = rows > 0 ? rows : 1;
+	P.ctaBase[B2G_OVERFLOW][0] = perCta[0];
+	perCta[0] += plan->colorStart[B2G_COLORS] - plan->colorStart[B2G_OVERFLOW];
+	int rowCap = 1;
+	for ( int o = 0; o < CL; ++o )
+		rowCap = perCta[o] > rowCap ? perCta[o] : rowCap;
+	P.rowCap = rowCap;
+	P.imageFloat4 = image_float4( P.bodySlots, P.rowCap );
 	size_t bytes = fused_smem_bytes( P.bodySlots, P.rowCap );
 	if ( bytes > FUSED_SMEM_MAX )
 		return 0;
 
 	auto kernel = k_solve_fused<FUSED_CLUSTER>;
-	if ( s_ready == 0 )
+	if ( ready == 0 )
 	{
-		s_ready = -1;
+		ready = -1;
 		if ( cudaFuncSetAttribute( kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1 ) == cudaSuccess &&
 			 cudaFuncSetAttribute( kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, FUSED_SMEM_MAX ) == cudaSuccess )
 		{
-			cudaLaunchConfig_t cfg = {};
 			cudaLaunchAttribute attr[1];
-			attr[0].id = cudaLaunchAttributeClusterDimension;
-			attr[0].val.clusterDim.x = CL;
-			attr[0].val.clusterDim.y = 1;
-			attr[0].val.clusterDim.z = 1;
-			cfg.gridDim = dim3( CL, 1, 1 );
-			cfg.blockDim = dim3( FUSED_THREADS, 1, 1 );
-			cfg.dynamicSmemBytes = FUSED_SMEM_MAX;
-			cfg.attrs = attr;
-			cfg.numAttrs = 1;
+			cudaLaunchConfig_t cfg = cluster_config( attr, FUSED_SMEM_MAX, nullptr );
 			int clusters = 0;
 			if ( cudaOccupancyMaxActiveClusters( &clusters, kernel, &cfg ) == cudaSuccess && clusters >= 1 )
-				s_ready = 1;
+				ready = 1;
 		}
 		cudaGetLastError();
 	}
-	if ( s_ready != 1 )
+	if ( ready != 1 )
 		return 0;
 
-	cudaLaunchConfig_t cfg = {};
-	cudaLaunchAttribute attr[1];
-	attr[0].id = cudaLaunchAttributeClusterDimension;
-	attr[0].val.clusterDim.x = CL;
-	attr[0].val.clusterDim.y = 1;
-	attr[0].val.clusterDim.z = 1;
-	cfg.gridDim = dim3( CL, 1, 1 );
-	cfg.blockDim = dim3( FUSED_THREADS, 1, 1 );
-	cfg.dynamicSmemBytes = bytes;
-	cfg.stream = (cudaStream_t)w->stream;
-	cfg.attrs = attr;
-	cfg.numAttrs = 1;
+	size_t stage = 16 * (size_t)P.imageFloat4 * CL;
+	if ( w->stageBytes < stage )
+	{
+		if ( w->stage )
+			cudaFree( w->stage );
+		w->stage = nullptr;
+		w->stageBytes = 0;
+		if ( cudaMalloc( &w->stage, stage ) != cudaSuccess )
+			return -1;
+		w->stageBytes = stage;
+	}
+	cudaStream_t s = (cudaStream_t)w->stream;
 	int launches = b2gd_prepare_joints( w, plan->jointStart[B2G_COLORS], sc );
-	if ( cudaLaunchKernelEx( &cfg, kernel, *w, P, *sc ) != cudaSuccess )
+	int rows = plan->colorStart[B2G_COLORS];
+	int threads = rows > plan->bodyIdCount ? rows : plan->bodyIdCount;
+	k_fused_stage<<<( threads + 255 ) / 256, 256, 0, s>>>( *w, P, *sc, (float4*)w->stage );
+	cudaLaunchAttribute attr[1];
+	cudaLaunchConfig_t cfg = cluster_config( attr, bytes, s );
+	if ( cudaLaunchKernelEx( &cfg, kernel, *w, P, *sc, (const float4*)w->stage ) != cudaSuccess )
 		return -1;
-	return launches + 1;
+	return launches + 2;
 }

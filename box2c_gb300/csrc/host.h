@@ -256,6 +256,8 @@ typedef struct gWorld
 	int scratchCap;
 	gIntArray solveList;
 	gIntArray jointList;
+	b2gSolvePlan solvePlan; /* plan of the current solve lists */
+	bool solveUploaded;		/* solve lists on the device match the host's */
 
 	b2gVec gravity;
 	float restitutionThreshold, pushout, hitThreshold, contactHertz, contactDamping, jointHertz, jointDamping;

@@ -578,19 +578,66 @@ static void make_soft( float hertz, float zeta, float h, float* out )
 	out[2] = a3;
 }
 
+/* Owner CTA of a contact row in the fused solver: the block of its first non-static
+ * body. */
+static int row_owner( gWorld* w, const gContact* c, int block )
+{
+	int a = c->edges[0].bodyId, b = c->edges[1].bodyId;
+	int key = w->bodies[a].type != b2_staticBody ? a : b;
+	int o = key / block;
+	return o < B2G_FUSED_CTAS ? o : B2G_FUSED_CTAS - 1;
+}
+
+/* Colour-major solve lists.  Within a graph colour the order of rows does not change any
+ * result (no two rows of a colour share a non-static body), so rows are grouped by owner
+ * CTA (a stable counting sort); the overflow colour keeps its order, which is the order
+ * it is solved in.  Rebuilt only when the colouring or the body count changed. */
 static void build_solve_lists( gWorld* w, b2gSolvePlan* plan )
 {
+	int bodyIdCount = w->bodyIds.next;
+	int block = ( bodyIdCount + B2G_FUSED_CTAS - 1 ) / B2G_FUSED_CTAS;
+	if ( block < 1 )
+		block = 1;
+	if ( w->solveDirty == false && w->solvePlan.bodyBlock == block )
+	{
+		*plan = w->solvePlan;
+		return;
+	}
+	memset( plan, 0, sizeof( *plan ) );
+	plan->bodyBlock = block;
 	w->solveList.count = 0;
 	w->jointList.count = 0;
-	plan->activeCount = 0;
 	for ( int c = 0; c < B2G_COLORS; ++c )
 	{
 		plan->colorStart[c] = w->solveList.count;
 		plan->jointStart[c] = w->jointList.count;
 		gIntArray* ca = &w->colors[c].contacts;
 		gIntArray* ja = &w->colors[c].joints;
-		for ( int k = 0; k < ca->count; ++k )
-			gia_push( &w->solveList, ca->data[k] );
+		if ( c < B2G_OVERFLOW && ca->count > 0 )
+		{
+			int* split = plan->rowSplit[c];
+			for ( int k = 0; k < ca->count; ++k )
+				split[row_owner( w, w->contacts + ca->data[k], block )] += 1;
+			int offset[B2G_FUSED_CTAS];
+			int start = w->solveList.count;
+			for ( int o = 0, n = 0; o < B2G_FUSED_CTAS; ++o )
+			{
+				offset[o] = start + n;
+				n += split[o];
+			}
+			for ( int k = 0; k < ca->count; ++k )
+				gia_push( &w->solveList, 0 );
+			for ( int k = 0; k < ca->count; ++k )
+			{
+				int id = ca->data[k];
+				w->solveList.data[offset[row_owner( w, w->contacts + id, block )]++] = id;
+			}
+		}
+		else
+		{
+			for ( int k = 0; k < ca->count; ++k )
+				gia_push( &w->solveList, ca->data[k] );
+		}
 		for ( int k = 0; k < ja->count; ++k )
 			gia_push( &w->jointList, ja->data[k] );
 		if ( c < B2G_OVERFLOW && ca->count + ja->count > 0 )
@@ -598,6 +645,9 @@ static void build_solve_lists( gWorld* w, b2gSolvePlan* plan )
 	}
 	plan->colorStart[B2G_COLORS] = w->solveList.count;
 	plan->jointStart[B2G_COLORS] = w->jointList.count;
+	w->solvePlan = *plan;
+	w->solveDirty = false;
+	w->solveUploaded = false;
 }
 
 void gstep_run( gWorld* w, float dt, int subSteps )
@@ -664,10 +714,10 @@ void gstep_run( gWorld* w, float dt, int subSteps )
 	build_solve_lists( w, &plan );
 	plan.awakeCount = w->awake.count;
 	plan.bodyIdCount = w->bodyIds.next;
-	if ( w->solveDirty )
+	if ( w->solveUploaded == false )
 	{
 		e = b2gd_upload_solve_lists( &w->dev, w->solveList.data, w->solveList.count, w->jointList.data, w->jointList.count );
-		w->solveDirty = false;
+		w->solveUploaded = true;
 	}
 	e |= b2gd_solve( &w->dev, &w->io, &plan, &sc );
 	e |= b2gd_sync( &w->dev );
