@@ -272,3 +272,23 @@ def bind_gpu_api(lib: C.CDLL) -> None:
     lib.b2World_EnableFusedSolver.restype = None
     lib.b2World_GetBodyStates.argtypes = [WorldId, C.c_void_p, C.c_int]
     lib.b2World_GetBodyStates.restype = C.c_int
+
+
+class BatchStats(C.Structure):
+    """include/box2d/gpu.h b2BatchStats."""
+    _fields_ = [("collide", C.c_float), ("solve", C.c_float), ("solveThreads", C.c_int), ("launches", C.c_int)]
+
+
+def bind_batch_api(lib: C.CDLL) -> None:
+    lib.b2World_StepBatch.argtypes = [C.c_void_p, C.c_int, C.c_float, C.c_int]
+    lib.b2World_StepBatch.restype = None
+    lib.b2World_GetBatchStats.argtypes = []
+    lib.b2World_GetBatchStats.restype = BatchStats
+
+
+def world_array(worlds) -> C.Array:
+    """A C array of b2WorldId for b2World_StepBatch."""
+    arr = (WorldId * len(worlds))()
+    for i, w in enumerate(worlds):
+        arr[i] = w
+    return arr

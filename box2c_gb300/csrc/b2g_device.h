@@ -75,6 +75,46 @@ int b2gd_collide( b2gDevWorld* w, b2gHostIO* io, int newContactCount, int contac
 int b2gd_solve( b2gDevWorld* w, b2gHostIO* io, const b2gSolvePlan* plan, const b2gStepConst* sc );
 int b2gd_sync( b2gDevWorld* w );
 
+/* ---------------------------------------------------------------- batched worlds */
+/* One world of a batched step (device copy of its descriptor plus the step's counts).
+ * W.counters points into the batch's counter array, 4 ints per world. */
+typedef struct b2gBatchItem
+{
+	b2gDevWorld W;
+	b2gStepConst sc;
+	int colorStart[B2G_COLORS + 1];
+	int jointStart[B2G_COLORS + 1];
+	int active[B2G_COLORS];
+	int activeCount;
+	int awakeCount;
+	int bodyIdCount;
+	int idCount; /* contact ids run through the narrowphase */
+	int staged;	 /* staged contact records */
+	int solve;	 /* 1 when the solver stage runs */
+} b2gBatchItem;
+
+/* Device context of batched steps: pinned staging of items and counters, device copies,
+ * captured CUDA graphs and the solver autotuner's state. */
+typedef struct b2gBatch b2gBatch;
+
+b2gBatch* b2gd_batch_create( void );
+void b2gd_batch_destroy( b2gBatch* b );
+/* Grows the item and counter buffers; returns the pinned item array or null. */
+b2gBatchItem* b2gd_batch_items( b2gBatch* b, int count );
+void* b2gd_batch_stream( b2gBatch* b );
+/* Host copy of world i's 4 counters after the last sync. */
+const int* b2gd_batch_counters( b2gBatch* b, int i );
+/* Narrowphase of all items (contact records staged by b2gd_stage_contacts). */
+int b2gd_batch_collide( b2gBatch* b, int count );
+/* Solver stage and finalisation of all items with solve != 0, one world per CTA. */
+int b2gd_batch_solve( b2gBatch* b, int count );
+int b2gd_batch_sync( b2gBatch* b );
+/* Device milliseconds of the last batched narrowphase and solve, the solver's CTA size
+ * and the number of graph launches. */
+void b2gd_batch_stats( b2gBatch* b, float* collideMs, float* solveMs, int* threads, int* launches );
+/* Copies a world's staged contact records to the device on the world's stream. */
+int b2gd_stage_contacts( b2gDevWorld* w, b2gHostIO* io, int count );
+
 /* Device time of the last step's stages in milliseconds (CUDA events recorded when
  * w->timing is set). */
 void b2gd_enable_timing( b2gDevWorld* w, int flag );

@@ -1,0 +1,575 @@
+/*
+ * b2g_stages.h -- the per-item work of each device stage, as device functions over one
+ * world descriptor: contact creation, narrowphase, row and joint preparation, body
+ * integration, impulse storage and body finalisation.
+ *
+ * kernels.cu wraps them in one-launch-per-stage kernels for a single world; batch.cu
+ * calls the same functions from the batched kernels that step many worlds per launch,
+ * so both give the same bits.
+ *
+ * Stage                reference
+ * contact creation     src/contact.c:185-332 (sim part)
+ * narrowphase          src/world.c:290-365, src/contact.c:493-582
+ * prepare contacts     src/contact_solver.c:21-147, :597-808
+ * prepare joints       src/revolute_joint.c:201-270
+ * integrate velocities src/solver.c:34-93
+ * integrate positions  src/solver.c:146-163
+ * store impulses       src/contact_solver.c:442-471, :1180-1293
+ * finalize bodies      src/solver.c:165-351 (+ fast-body sweep boxes, :787-1105)
+ */
+#pragma once
+
+#include "b2g_collide.h"
+#include "b2g_device.h"
+#include "b2g_solve.h"
+
+#include <cuda_runtime.h>
+
+/* ------------------------------------------------------------------ state access */
+static __device__ __forceinline__ DevState load_state( const b2gDevWorld& W, int b )
+{
+	if ( b < 0 )
+		return identity_state();
+	const float4* st = (const float4*)W.state;
+	return state_of( st[2 * b], st[2 * b + 1] );
+}
+
+static __device__ __forceinline__ void store_velocity( const b2gDevWorld& W, int b, const DevState& s )
+{
+	if ( b < 0 )
+		return;
+	( (float4*)W.state )[2 * b] = velocity_word( s );
+}
+
+static __device__ __forceinline__ b2gBox box_of( float4 f )
+{
+	b2gBox b;
+	b.lo = gv( f.x, f.y );
+	b.hi = gv( f.z, f.w );
+	return b;
+}
+
+static __device__ __forceinline__ float4 f4_of( b2gBox b ) { return make_float4( b.lo.x, b.lo.y, b.hi.x, b.hi.y ); }
+
+/* Shape AABB (reference src/geometry.c:385-430, src/shape.c:457-478). */
+static __device__ b2gBox shape_aabb( const b2gShapeGeo& g, b2gXf xf )
+{
+	b2gBox b;
+	switch ( g.type )
+	{
+		case 0:
+		{
+			b2gVec p = gxfpoint( xf, g.v[0] );
+			float r = g.radius;
+			b.lo = gv( p.x - r, p.y - r );
+			b.hi = gv( p.x + r, p.y + r );
+			return b;
+		}
+		case 1:
+		{
+			b2gVec v1 = gxfpoint( xf, g.v[0] );
+			b2gVec v2 = gxfpoint( xf, g.v[1] );
+			b2gVec r = gv( g.radius, g.radius );
+			b.lo = gsub( gminv( v1, v2 ), r );
+			b.hi = gadd( gmaxv( v1, v2 ), r );
+			return b;
+		}
+		case 2:
+		{
+			b2gVec v1 = gxfpoint( xf, g.v[0] );
+			b2gVec v2 = gxfpoint( xf, g.v[1] );
+			b.lo = gminv( v1, v2 );
+			b.hi = gmaxv( v1, v2 );
+			return b;
+		}
+		default:
+		{
+			b2gVec lo = gxfpoint( xf, g.v[0] );
+			b2gVec hi = lo;
+			for ( int i = 1; i < g.count; ++i )
+			{
+				b2gVec v = gxfpoint( xf, g.v[i] );
+				lo = gminv( lo, v );
+				hi = gmaxv( hi, v );
+			}
+			b2gVec r = gv( g.radius, g.radius );
+			b.lo = gsub( lo, r );
+			b.hi = gadd( hi, r );
+			return b;
+		}
+	}
+}
+
+/* ------------------------------------------------------------------ contact creation */
+static __device__ __forceinline__ void scatter_contact( const b2gDevWorld& W, const b2gContactInit* inits, int t )
+{
+	b2gContactInit c = inits[t];
+	int id = c.id;
+	if ( c.flags & B2G_INIT_KILL )
+	{
+		W.cFlags[id] = 0;
+		return;
+	}
+	W.cShapes[2 * id] = c.shapeA;
+	W.cShapes[2 * id + 1] = c.shapeB;
+	W.cMix[2 * id] = c.friction;
+	W.cMix[2 * id + 1] = c.restitution;
+	W.cFlags[id] = B2G_C_LIVE;
+	W.cBodies[2 * id] = -1;
+	W.cBodies[2 * id + 1] = -1;
+	b2gManifold m;
+	gmanifold_clear( &m );
+	W.manifold[id] = m;
+}
+
+/* ------------------------------------------------------------------ narrowphase */
+/* Manifold of one shape pair; sensors never generate points.  Kept behind a call
+ * boundary: inlined into k_collide, this routine returned empty manifolds for touching
+ * boxes on sm_103a (nvcc 13.0.88, -O3 --fmad=false) while the same source called from a
+ * one-thread kernel, or on the host, was correct; the non-inlined form is correct in
+ * both kernels and bit-identical to the reference. */
+static __device__ __noinline__ void narrowphase( b2gManifold* m, const b2gShapeGeo* gA, b2gXf xfA, const b2gShapeGeo* gB, b2gXf xfB )
+{
+	if ( gA->isSensor || gB->isSensor )
+		gmanifold_clear( m );
+	else
+		gcollide_shapes( m, gA, xfA, gB, xfB );
+}
+
+static __device__ __forceinline__ void emit_event( const b2gDevWorld& W, int id, int code )
+{
+	int slot = atomicAdd( W.counters + 0, 1 );
+	if ( slot < W.eventCap )
+		W.events[slot] = ( id << 2 ) | code;
+}
+
+static __device__ void collide_contact( const b2gDevWorld& W, int id )
+{
+	uint32_t flags = W.cFlags[id];
+	if ( ( flags & B2G_C_LIVE ) == 0 )
+		return;
+	int sA = W.cShapes[2 * id];
+	int sB = W.cShapes[2 * id + 1];
+	const float4* fat = (const float4*)W.fat;
+	if ( gbox_overlaps( box_of( fat[sA] ), box_of( fat[sB] ) ) == false )
+	{
+		/* the host destroys the contact while processing this event */
+		W.cFlags[id] = 0;
+		emit_event( W, id, B2G_EV_DISJOINT );
+		return;
+	}
+	bool wasTouching = ( flags & B2G_C_TOUCHING ) != 0;
+	const b2gShapeGeo* gA = W.geo + sA;
+	const b2gShapeGeo* gB = W.geo + sB;
+	int bA = gA->bodyId;
+	int bB = gB->bodyId;
+	int infoA = W.bodyInfo[bA];
+	int infoB = W.bodyInfo[bB];
+	W.cBodies[2 * id] = ( infoA & B2G_B_AWAKE ) ? bA : -1;
+	W.cBodies[2 * id + 1] = ( infoB & B2G_B_AWAKE ) ? bB : -1;
+	const float4* xf = (const float4*)W.xf;
+	const float4* centers = (const float4*)W.centers;
+	float4 xa = xf[bA], xb = xf[bB];
+	b2gXf xfA, xfB;
+	xfA.p = gv( xa.x, xa.y );
+	xfA.q = grot( xa.z, xa.w );
+	xfB.p = gv( xb.x, xb.y );
+	xfB.q = grot( xb.z, xb.w );
+	float4 ca = centers[bA], cb = centers[bB];
+	b2gVec offA = grotate( xfA.q, gv( ca.z, ca.w ) );
+	b2gVec offB = grotate( xfB.q, gv( cb.z, cb.w ) );
+
+	b2gManifold old = W.manifold[id];
+	b2gManifold m;
+	narrowphase( &m, gA, xfA, gB, xfB );
+
+	int pointCount = m.count;
+	bool touching = pointCount > 0;
+	for ( int i = 0; i < pointCount; ++i )
+	{
+		b2gPoint* mp2 = m.pts + i;
+		mp2->anchorA = gsub( mp2->anchorA, offA );
+		mp2->anchorB = gsub( mp2->anchorB, offB );
+		mp2->normalImpulse = 0.0f;
+		mp2->tangentImpulse = 0.0f;
+		mp2->maxNormalImpulse = 0.0f;
+		mp2->normalVelocity = 0.0f;
+		mp2->persisted = 0;
+		for ( int j = 0; j < old.count; ++j )
+		{
+			if ( old.pts[j].id == mp2->id )
+			{
+				mp2->normalImpulse = old.pts[j].normalImpulse;
+				mp2->tangentImpulse = old.pts[j].tangentImpulse;
+				mp2->persisted = 1;
+				break;
+			}
+		}
+	}
+	W.manifold[id] = m;
+	uint32_t nf = B2G_C_LIVE | ( touching ? B2G_C_TOUCHING : 0u );
+	if ( touching && ( gA->enableHitEvents || gB->enableHitEvents ) )
+		nf |= B2G_C_HIT;
+	W.cFlags[id] = nf;
+	if ( touching && !wasTouching )
+		emit_event( W, id, B2G_EV_STARTED );
+	else if ( !touching && wasTouching )
+		emit_event( W, id, B2G_EV_STOPPED );
+}
+
+/* ------------------------------------------------------------------ constraint rows */
+static __device__ void prepare_contact_row( const b2gDevWorld& W, int k, const b2gStepConst& sc )
+{
+	/* a null solve list means rows are the contacts in order */
+	int cid = W.solveList ? W.solveList[k] : k;
+	int ia = W.cBodies[2 * cid];
+	int ib = W.cBodies[2 * cid + 1];
+	/* inverse masses of the reference's contact sim: the body's, zero for static bodies */
+	const float4* mass = (const float4*)W.mass;
+	float4 zero = make_float4( 0.0f, 0.0f, 0.0f, 0.0f );
+	Row r;
+	prepare_row( r, W.manifold + cid, ia, ib, ia >= 0 ? mass[ia] : zero, ib >= 0 ? mass[ib] : zero, load_state( W, ia ),
+				 load_state( W, ib ), W.cMix[2 * cid], W.cMix[2 * cid + 1], ( ia < 0 || ib < 0 ) ? sc.staticSoft : sc.contactSoft,
+				 sc.enableWarmStarting ? 1.0f : 0.0f );
+	( (int4*)W.kIdx )[k] = make_int4( ia, ib, cid, r.count );
+	( (float4*)W.kNF )[k] = make_float4( r.n.x, r.n.y, r.friction, r.restitution );
+	( (float4*)W.kSoft )[k] = make_float4( r.biasRate, r.massScale, r.impulseScale, 0.0f );
+	( (float4*)W.kMass )[k] = make_float4( r.mA, r.iA, r.mB, r.iB );
+	for ( int j = 0; j < 2; ++j )
+	{
+		( (float4*)W.kAnchor[j] )[k] = make_float4( r.rA[j].x, r.rA[j].y, r.rB[j].x, r.rB[j].y );
+		( (float4*)W.kCoef[j] )[k] = make_float4( r.base[j], r.nMass[j], r.tMass[j], r.relVel[j] );
+		( (float4*)W.kImp[j] )[k] = make_float4( r.ni[j], r.ti[j], r.maxNi[j], 0.0f );
+	}
+}
+
+static __device__ __forceinline__ void load_row( const b2gDevWorld& W, int k, Row& r )
+{
+	int4 idx = ( (const int4*)W.kIdx )[k];
+	float4 nf = ( (const float4*)W.kNF )[k];
+	float4 so = ( (const float4*)W.kSoft )[k];
+	float4 ms = ( (const float4*)W.kMass )[k];
+	r.ia = idx.x;
+	r.ib = idx.y;
+	r.count = idx.w;
+	r.n = gv( nf.x, nf.y );
+	r.friction = nf.z;
+	r.restitution = nf.w;
+	r.biasRate = so.x;
+	r.massScale = so.y;
+	r.impulseScale = so.z;
+	r.mA = ms.x;
+	r.iA = ms.y;
+	r.mB = ms.z;
+	r.iB = ms.w;
+	for ( int j = 0; j < 2; ++j )
+	{
+		float4 a = ( (const float4*)W.kAnchor[j] )[k];
+		float4 c = ( (const float4*)W.kCoef[j] )[k];
+		float4 i = ( (const float4*)W.kImp[j] )[k];
+		r.rA[j] = gv( a.x, a.y );
+		r.rB[j] = gv( a.z, a.w );
+		r.base[j] = c.x;
+		r.nMass[j] = c.y;
+		r.tMass[j] = c.z;
+		r.relVel[j] = c.w;
+		r.ni[j] = i.x;
+		r.ti[j] = i.y;
+		r.maxNi[j] = i.z;
+	}
+}
+
+static __device__ __forceinline__ void store_impulses( const b2gDevWorld& W, int k, const Row& r )
+{
+	for ( int j = 0; j < 2; ++j )
+		( (float4*)W.kImp[j] )[k] = make_float4( r.ni[j], r.ti[j], r.maxNi[j], 0.0f );
+}
+
+/* Row phases over global body state: load, solve in registers, store. */
+/* Body-state views for the row and joint work below. */
+struct GlobalBodies
+{
+	const b2gDevWorld* W;
+	__device__ __forceinline__ DevState load( int b ) const { return load_state( *W, b ); }
+	__device__ __forceinline__ DevState load_velocity( int b ) const { return load_state( *W, b ); }
+	__device__ __forceinline__ void store( int b, const DevState& x ) const { store_velocity( *W, b, x ); }
+};
+
+struct SharedBodies
+{
+	float4* st0;
+	float4* st1;
+	__device__ __forceinline__ DevState load( int b ) const
+	{
+		return b < 0 ? identity_state() : state_of( st0[b], st1[b] );
+	}
+	__device__ __forceinline__ DevState load_velocity( int b ) const
+	{
+		return b < 0 ? identity_state() : state_of( st0[b], make_float4( 0.0f, 0.0f, 1.0f, 0.0f ) );
+	}
+	__device__ __forceinline__ void store( int b, const DevState& x ) const
+	{
+		if ( b >= 0 )
+			st0[b] = velocity_word( x );
+	}
+};
+
+/* One row phase (0 warm start, 1 solve, 2 relax, 3 restitution): row from the world's
+ * row arrays, bodies through B. */
+template <class Bodies>
+static __device__ __forceinline__ void row_work( const b2gDevWorld& W, const Bodies& B, int k, int phase, bool scalar,
+												 const b2gStepConst& sc )
+{
+	Row r;
+	load_row( W, k, r );
+	bool delta = phase == 1 || phase == 2;
+	DevState a = delta ? B.load( r.ia ) : B.load_velocity( r.ia );
+	DevState b = delta ? B.load( r.ib ) : B.load_velocity( r.ib );
+	bool changed = true;
+	if ( phase == 0 )
+		scalar ? warm_scalar( r, a, b ) : warm_lane( r, a, b );
+	else if ( phase == 1 || phase == 2 )
+		scalar ? solve_scalar( r, a, b, phase == 1, sc.inv_h, sc.pushout ) : solve_lane( r, a, b, phase == 1, sc.inv_h, sc.pushout );
+	else if ( scalar )
+		changed = restitution_scalar( r, a, b, sc.restitutionThreshold );
+	else
+		restitution_lane( r, a, b, sc.restitutionThreshold );
+	if ( changed == false )
+		return;
+	B.store( r.ia, a );
+	B.store( r.ib, b );
+	if ( phase != 0 )
+		store_impulses( W, k, r );
+}
+
+static __device__ void row_phase( const b2gDevWorld& W, int k, int phase, bool scalar, const b2gStepConst& sc )
+{
+	row_work( W, GlobalBodies{ &W }, k, phase, scalar, sc );
+}
+
+/* ------------------------------------------------------------------ revolute joint */
+static __device__ void make_soft( float hertz, float zeta, float h, float* out )
+{
+	if ( hertz == 0.0f )
+	{
+		out[0] = 0.0f;
+		out[1] = 1.0f;
+		out[2] = 0.0f;
+		return;
+	}
+	float omega = 2.0f * B2G_PI * hertz;
+	float a1 = 2.0f * zeta + h * omega;
+	float a2 = h * omega * a1;
+	float a3 = 1.0f / ( 1.0f + a2 );
+	out[0] = omega / a1;
+	out[1] = a2 * a3;
+	out[2] = a3;
+}
+
+static __device__ void prepare_joint( const b2gDevWorld& W, int t, const b2gStepConst& sc )
+{
+	b2gJointDev* j = W.joints + W.jointList[t];
+	const float4* mass = (const float4*)W.mass;
+	const float4* xf = (const float4*)W.xf;
+	const float4* centers = (const float4*)W.centers;
+	int a = j->bodyIdA, b = j->bodyIdB;
+	float4 ma = mass[a], mb = mass[b];
+	j->invMassA = ma.y;
+	j->invMassB = mb.y;
+	j->invIA = ma.w;
+	j->invIB = mb.w;
+	j->indexA = ( W.bodyInfo[a] & B2G_B_AWAKE ) ? a : -1;
+	j->indexB = ( W.bodyInfo[b] & B2G_B_AWAKE ) ? b : -1;
+	float4 xa = xf[a], xb = xf[b];
+	float4 ca = centers[a], cb = centers[b];
+	b2gRot qA = grot( xa.z, xa.w ), qB = grot( xb.z, xb.w );
+	j->anchorA = grotate( qA, gsub( j->localAnchorA, gv( ca.z, ca.w ) ) );
+	j->anchorB = grotate( qB, gsub( j->localAnchorB, gv( cb.z, cb.w ) ) );
+	j->deltaCenter = gsub( gv( cb.x, cb.y ), gv( ca.x, ca.y ) );
+	j->deltaAngle = rel_angle( qB, qA ) - j->referenceAngle;
+	j->deltaAngle = unwind( j->deltaAngle );
+	float k = j->invIA + j->invIB;
+	j->axialMass = k > 0.0f ? 1.0f / k : 0.0f;
+	float s[3];
+	make_soft( j->hertz, j->dampingRatio, sc.h, s );
+	j->springBias = s[0];
+	j->springMass = s[1];
+	j->springImpulseScale = s[2];
+	if ( sc.enableWarmStarting == 0 )
+	{
+		j->linearImpulse = gv( 0.0f, 0.0f );
+		j->springImpulse = 0.0f;
+		j->motorImpulse = 0.0f;
+		j->lowerImpulse = 0.0f;
+		j->upperImpulse = 0.0f;
+	}
+}
+
+template <class Bodies>
+static __device__ __forceinline__ void joint_work( const b2gDevWorld& W, const Bodies& B, int jid, int phase, const b2gStepConst& sc )
+{
+	b2gJointDev* j = W.joints + jid;
+	DevState a = B.load( j->indexA );
+	DevState b = B.load( j->indexB );
+	if ( phase == 0 )
+		joint_warm_state( j, a, b );
+	else
+		joint_solve_state( j, a, b, phase == 1, sc );
+	B.store( j->indexA, a );
+	B.store( j->indexB, b );
+}
+
+static __device__ void joint_phase( const b2gDevWorld& W, int jid, int phase, const b2gStepConst& sc )
+{
+	joint_work( W, GlobalBodies{ &W }, jid, phase, sc );
+}
+
+/* ------------------------------------------------------------------ bodies */
+static __device__ __forceinline__ void integrate_body_velocity( const b2gDevWorld& W, int i, const b2gStepConst& sc )
+{
+	int b = W.awake[i];
+	DevState s = load_state( W, b );
+	VelocityTerms t = velocity_terms( ( (const float4*)W.mass )[b], ( (const float4*)W.force )[b], ( (const float4*)W.extent )[b], sc );
+	integrate_velocity( s, t, sc );
+	store_velocity( W, b, s );
+}
+
+static __device__ __forceinline__ void integrate_body_position( const b2gDevWorld& W, int i, const b2gStepConst& sc )
+{
+	int b = W.awake[i];
+	DevState s = load_state( W, b );
+	integrate_position( s, sc.h );
+	( (float4*)W.state )[2 * b + 1] = make_float4( s.dp.x, s.dp.y, s.dq.c, s.dq.s );
+}
+
+static __device__ __forceinline__ void store_row( const b2gDevWorld& W, int k, int overflowStart )
+{
+	int4 idx = ( (const int4*)W.kIdx )[k];
+	b2gManifold* m = W.manifold + idx.z;
+	int n = k < overflowStart ? 2 : idx.w;
+	for ( int j = 0; j < n; ++j )
+	{
+		float4 imp = ( (const float4*)W.kImp[j] )[k];
+		float4 coef = ( (const float4*)W.kCoef[j] )[k];
+		m->pts[j].normalImpulse = imp.x;
+		m->pts[j].tangentImpulse = imp.y;
+		m->pts[j].maxNormalImpulse = imp.z;
+		m->pts[j].normalVelocity = coef.w;
+	}
+}
+
+static __device__ __forceinline__ void emit_record( const b2gDevWorld& W, int awakeIndex, int slot, int shapeId, int flags, b2gBox fat,
+											 b2gBox sweep )
+{
+	int r = atomicAdd( W.counters + 1, 1 );
+	if ( r >= W.recordCap )
+		return;
+	b2gRecord rec;
+	rec.awakeIndex = awakeIndex;
+	rec.slot = slot;
+	rec.shapeId = shapeId;
+	rec.flags = flags;
+	rec.fat[0] = fat.lo.x;
+	rec.fat[1] = fat.lo.y;
+	rec.fat[2] = fat.hi.x;
+	rec.fat[3] = fat.hi.y;
+	rec.sweep[0] = sweep.lo.x;
+	rec.sweep[1] = sweep.lo.y;
+	rec.sweep[2] = sweep.hi.x;
+	rec.sweep[3] = sweep.hi.y;
+	W.records[r] = rec;
+}
+
+static __device__ void finalize_body( const b2gDevWorld& W, int i, const b2gStepConst& sc )
+{
+	int b = W.awake[i];
+	float4* st = (float4*)W.state;
+	float4 s0 = st[2 * b];
+	float4 s1 = st[2 * b + 1];
+	float4* xfs = (float4*)W.xf;
+	float4* cen = (float4*)W.centers;
+	float4* prev = (float4*)W.prev;
+	float4 x = xfs[b];
+	float4 c = cen[b];
+	float4 ex = ( (const float4*)W.extent )[b];
+	int info = W.bodyInfo[b];
+
+	b2gVec v = gv( s0.x, s0.y );
+	float w = s0.z;
+	b2gVec dp = gv( s1.x, s1.y );
+	b2gRot dq = grot( s1.z, s1.w );
+	b2gVec center = gadd( gv( c.x, c.y ), dp );
+	b2gRot q = gnormrot( gmulrot( dq, grot( x.z, x.w ) ) );
+	float maxExtent = ex.w, minExtent = ex.z;
+	float maxVelocity = glen( v ) + gabs( w ) * maxExtent;
+	float maxDeltaPosition = glen( dp ) + gabs( dq.s ) * maxExtent;
+	float sleepVelocity = gmax( maxVelocity, 0.5f * sc.inv_dt * maxDeltaPosition );
+	st[2 * b + 1] = make_float4( 0.0f, 0.0f, 1.0f, 0.0f );
+	b2gVec p = gsub( center, grotate( q, gv( c.z, c.w ) ) );
+	b2gXf xf;
+	xf.p = p;
+	xf.q = q;
+	xfs[b] = make_float4( p.x, p.y, q.c, q.s );
+	cen[b] = make_float4( center.x, center.y, c.z, c.w );
+	float4* fo = (float4*)W.force;
+	float4 f = fo[b];
+	fo[b] = make_float4( 0.0f, 0.0f, 0.0f, f.w );
+
+	bool isFast = false;
+	float sleepThreshold = s0.w;
+	if ( sc.enableSleep == 0 || ( info & B2G_B_SLEEP_OK ) == 0 || sleepVelocity > sleepThreshold )
+	{
+		if ( ( info & B2G_B_TYPE_MASK ) == 2 && sc.enableContinuous && maxVelocity * sc.dt > 0.5f * minExtent )
+			isFast = true;
+	}
+	/* with no time-of-impact event the fast body also advances its sweep start */
+	prev[b] = make_float4( center.x, center.y, q.c, q.s );
+
+	int start = W.shapeRange[2 * b];
+	int count = W.shapeRange[2 * b + 1];
+	float4* aabbs = (float4*)W.aabb;
+	float4* fats = (float4*)W.fat;
+	int bullet = ( info & B2G_B_BULLET ) ? B2G_R_BULLET : 0;
+	for ( int slot = 0; slot < count; ++slot )
+	{
+		int sid = W.shapeList[start + slot];
+		b2gShapeGeo g = W.geo[sid];
+		b2gBox fat = box_of( fats[sid] );
+		if ( isFast )
+		{
+			b2gBox box1 = box_of( aabbs[sid] );
+			b2gBox box2 = shape_aabb( g, xf );
+			aabbs[sid] = f4_of( box2 );
+			int flags = B2G_R_FAST | bullet;
+			if ( gbox_contains( fat, box2 ) == false )
+			{
+				fat.lo.x = box2.lo.x - B2G_AABB_MARGIN;
+				fat.lo.y = box2.lo.y - B2G_AABB_MARGIN;
+				fat.hi.x = box2.hi.x + B2G_AABB_MARGIN;
+				fat.hi.y = box2.hi.y + B2G_AABB_MARGIN;
+				fats[sid] = f4_of( fat );
+				flags |= B2G_R_FAST_ENLARGED;
+			}
+			emit_record( W, i, slot, sid, flags, fat, gbox_union( box1, box2 ) );
+		}
+		else
+		{
+			b2gBox aabb = shape_aabb( g, xf );
+			aabb.lo.x -= B2G_SPECULATIVE;
+			aabb.lo.y -= B2G_SPECULATIVE;
+			aabb.hi.x += B2G_SPECULATIVE;
+			aabb.hi.y += B2G_SPECULATIVE;
+			aabbs[sid] = f4_of( aabb );
+			if ( gbox_contains( fat, aabb ) == false )
+			{
+				fat.lo.x = aabb.lo.x - B2G_AABB_MARGIN;
+				fat.lo.y = aabb.lo.y - B2G_AABB_MARGIN;
+				fat.hi.x = aabb.hi.x + B2G_AABB_MARGIN;
+				fat.hi.y = aabb.hi.y + B2G_AABB_MARGIN;
+				fats[sid] = f4_of( fat );
+				emit_record( W, i, slot, sid, B2G_R_ENLARGED, fat, aabb );
+			}
+		}
+	}
+}
+

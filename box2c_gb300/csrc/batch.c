@@ -1,0 +1,176 @@
+/*
+ * batch.c -- b2World_StepBatch: one step of many independent worlds with the device
+ * work of all of them in two replayed CUDA graphs (narrowphase, then solver and
+ * finalisation).
+ *
+ * The host work of each world is the single-world step's, phase by phase (step.c:
+ * gstep_begin, gstep_rebuild_trees, gstep_after_collide, gstep_finish); only the device
+ * launches are shared.  While the batch runs, every world's uploads go to the batch's
+ * stream, so they are ordered before the graphs that read them.
+ */
+#include "host.h"
+
+#include "box2d/gpu.h"
+
+#include <stdlib.h>
+#include <string.h>
+
+static b2gBatch* s_batch;
+static gWorld** s_worlds;
+static void** s_streams;
+static int s_cap;
+
+static bool reserve_worlds( int count )
+{
+	if ( count <= s_cap )
+		return true;
+	int cap = count < 64 ? 64 : count;
+	gWorld** w = (gWorld**)realloc( s_worlds, sizeof( gWorld* ) * (size_t)cap );
+	if ( w == NULL )
+		return false;
+	s_worlds = w;
+	void** s = (void**)realloc( s_streams, sizeof( void* ) * (size_t)cap );
+	if ( s == NULL )
+		return false;
+	s_streams = s;
+	s_cap = cap;
+	return true;
+}
+
+static void fill_item( b2gBatchItem* it, gWorld* w )
+{
+	it->W = w->dev;
+	it->bodyIdCount = w->bodyIds.next;
+}
+
+void b2World_StepBatch( const b2WorldId* worldIds, int count, float timeStep, int subStepCount )
+{
+	if ( worldIds == NULL || count <= 0 || timeStep == 0.0f )
+		return;
+	if ( s_batch == NULL )
+	{
+		s_batch = b2gd_batch_create();
+		if ( s_batch == NULL )
+			return;
+	}
+	if ( reserve_worlds( count ) == false )
+		return;
+
+	/* valid, healthy, distinct worlds */
+	int n = 0;
+	for ( int i = 0; i < count; ++i )
+	{
+		if ( b2World_IsValid( worldIds[i] ) == false )
+			continue;
+		gWorld* w = gworld_get( worldIds[i] );
+		if ( w->locked || w->status != 0 )
+			continue;
+		w->locked = true;
+		s_worlds[n++] = w;
+	}
+	if ( n == 0 )
+		return;
+	b2gBatchItem* items = b2gd_batch_items( s_batch, n );
+	void* stream = b2gd_batch_stream( s_batch );
+	if ( items == NULL )
+	{
+		for ( int k = 0; k < n; ++k )
+			s_worlds[k]->locked = false;
+		return;
+	}
+
+	double t0 = b2g_now_ms();
+	for ( int k = 0; k < n; ++k )
+	{
+		gWorld* w = s_worlds[k];
+		b2gBatchItem* it = items + k;
+		memset( it, 0, sizeof( *it ) );
+		w->beginCount = 0;
+		w->endCount = 0;
+		memset( &w->profile, 0, sizeof( w->profile ) );
+		s_streams[k] = w->dev.stream;
+		w->dev.stream = stream;
+		gworld_flush( w );
+		int staged = gstep_begin( w );
+		if ( staged < 0 )
+			continue;
+		if ( b2gd_stage_contacts( &w->dev, &w->io, staged ) != 0 )
+		{
+			w->status = -1;
+			continue;
+		}
+		fill_item( it, w );
+		it->idCount = w->stepIdCount;
+		it->staged = staged;
+	}
+
+	int e = b2gd_batch_collide( s_batch, n );
+	for ( int k = 0; k < n; ++k )
+		if ( s_worlds[k]->status == 0 )
+			gstep_rebuild_trees( s_worlds[k] );
+	e |= b2gd_batch_sync( s_batch );
+
+	for ( int k = 0; k < n; ++k )
+	{
+		gWorld* w = s_worlds[k];
+		b2gBatchItem* it = items + k;
+		if ( e != 0 )
+			w->status = e;
+		if ( w->status != 0 )
+		{
+			it->solve = 0;
+			continue;
+		}
+		w->io.counters[0] = b2gd_batch_counters( s_batch, k )[0];
+		b2gStepConst sc;
+		b2gSolvePlan plan;
+		int run = gstep_after_collide( w, timeStep, subStepCount, &sc, &plan );
+		/* uploads above may have grown the arena: copy the descriptor again */
+		fill_item( it, w );
+		it->solve = run && w->status == 0;
+		if ( it->solve == 0 )
+			continue;
+		it->sc = sc;
+		memcpy( it->colorStart, plan.colorStart, sizeof( it->colorStart ) );
+		memcpy( it->jointStart, plan.jointStart, sizeof( it->jointStart ) );
+		memcpy( it->active, plan.active, sizeof( it->active ) );
+		it->activeCount = plan.activeCount;
+		it->awakeCount = plan.awakeCount;
+		it->bodyIdCount = plan.bodyIdCount;
+	}
+
+	e = b2gd_batch_solve( s_batch, n );
+	e |= b2gd_batch_sync( s_batch );
+
+	double t1 = b2g_now_ms();
+	for ( int k = 0; k < n; ++k )
+	{
+		gWorld* w = s_worlds[k];
+		if ( e != 0 && w->status == 0 )
+			w->status = e;
+		if ( items[k].solve && w->status == 0 )
+		{
+			w->io.counters[1] = b2gd_batch_counters( s_batch, k )[1];
+			gstep_finish( w );
+		}
+		w->dev.stream = s_streams[k];
+		w->dev.launches = 0;
+		w->dev.fusedUsed = 0;
+		w->mirrorStale = true;
+		w->shapeMirrorStale = true;
+		w->jointMirrorStale = true;
+		w->locked = false;
+		w->profile.step = (float)( t1 - t0 ) / (float)n;
+		if ( w->status )
+			gworld_fail( b2gd_last_error() );
+	}
+}
+
+b2BatchStats b2World_GetBatchStats( void )
+{
+	b2BatchStats s;
+	memset( &s, 0, sizeof( s ) );
+	if ( s_batch != NULL )
+		b2gd_batch_stats( s_batch, &s.collide, &s.solve, &s.solveThreads, &s.launches );
+	return s;
+}

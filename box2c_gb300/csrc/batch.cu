@@ -1,0 +1,553 @@
+/*
+ * batch.cu -- device side of b2World_StepBatch: many independent worlds per launch.
+ *
+ * Narrowphase: two grid-stride kernels over the concatenated contact records and
+ * contact ids of all worlds (a flat index finds its world by binary search over the
+ * prefix sums).  Solver: one persistent kernel; each CTA takes the next world from a
+ * queue (largest first) and runs that world's whole solver stage and finalisation with
+ * __syncthreads between the dependent phases: body states in shared memory, constraint
+ * rows in the world's own row arrays (they stay in L2 while the CTA works on them).
+ * The per-item work is b2g_stages.h's, the same functions the single-world kernels use,
+ * so every world gets the bits it would get from b2World_Step alone.
+ *
+ * Each device segment (uploads, kernels, counter download) is captured once as a CUDA
+ * graph and replayed every step; the kernels read their counts from device memory, so
+ * the graphs do not change while the number of worlds and the shared-memory size stay
+ * the same.  The solver's CTA size is chosen by timing the candidates on the first
+ * steps (any choice gives the same results).
+ */
+#include "b2g_stages.h"
+
+#include <cuda_runtime.h>
+
+#include <stdlib.h>
+#include <string.h>
+
+#define BATCH_GRID_THREADS 256
+#define TUNE_CANDIDATES 3
+#define TUNE_SAMPLES 2
+
+static const int s_tuneThreads[TUNE_CANDIDATES] = { 64, 128, 256 };
+
+struct b2gBatch
+{
+	cudaStream_t stream;
+	int capacity;
+	b2gBatchItem* hItems;
+	b2gBatchItem* dItems;
+	int* hPrefix; /* scatter prefix [n+1], then narrowphase prefix [n+1] */
+	int* dPrefix;
+	int* hOrder; /* [0] = worlds to solve, then their item indices, largest first */
+	int* dOrder;
+	int* hCounters; /* 4 per item */
+	int* dCounters;
+	int* dQueue;
+	int sms;
+	cudaEvent_t ev[4];
+
+	cudaGraphExec_t collideExec;
+	int collideN;
+	cudaGraphExec_t solveExec[TUNE_CANDIDATES];
+	int solveN[TUNE_CANDIDATES];
+	int solveSmem[TUNE_CANDIDATES];
+
+	int tuned, choice, tuneStep;
+	float tuneMs[TUNE_CANDIDATES];
+	float collideMs, solveMs;
+	int launches;
+	int collideTimed, solveTimed;
+};
+
+/* largest w with prefix[w] <= t, given prefix[0] <= t < prefix[n] */
+__device__ __forceinline__ int find_world( const int* prefix, int n, int t )
+{
+	int lo = 0, hi = n;
+	while ( hi - lo > 1 )
+	{
+		int mid = ( lo + hi ) >> 1;
+		if ( prefix[mid] <= t )
+			lo = mid;
+		else
+			hi = mid;
+	}
+	return lo;
+}
+
+__global__ void __launch_bounds__( BATCH_GRID_THREADS ) k_batch_scatter( const b2gBatchItem* items, const int* prefix, int n )
+{
+	int total = prefix[n];
+	for ( int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x )
+	{
+		int w = find_world( prefix, n, t );
+		const b2gDevWorld& W = items[w].W;
+		scatter_contact( W, W.newContacts, t - prefix[w] );
+	}
+}
+
+__global__ void __launch_bounds__( BATCH_GRID_THREADS ) k_batch_collide( const b2gBatchItem* items, const int* prefix, int n )
+{
+	int total = prefix[n];
+	for ( int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x )
+	{
+		int w = find_world( prefix, n, t );
+		collide_contact( items[w].W, t - prefix[w] );
+	}
+}
+
+/* One stage over all colours of one world (overflow first, serially), the CTA's
+ * threads sharing each colour, a CTA barrier after each. */
+template <int T>
+__device__ void world_stage( const b2gBatchItem& it, const SharedBodies& B, int phase, const b2gStepConst& sc )
+{
+	const b2gDevWorld& W = it.W;
+	const int* cs = it.colorStart;
+	const int* js = it.jointStart;
+	int ovRows = cs[B2G_COLORS] - cs[B2G_OVERFLOW];
+	int ovJointsAll = js[B2G_COLORS] - js[B2G_OVERFLOW];
+	bool overflow = phase == 3 ? ovRows > 0 : ovRows + ovJointsAll > 0;
+	if ( overflow )
+	{
+		if ( threadIdx.x == 0 )
+		{
+			if ( phase != 3 )
+				for ( int i = 0; i < ovJointsAll; ++i )
+					joint_work( W, B, W.jointList[js[B2G_OVERFLOW] + i], phase, sc );
+			for ( int i = 0; i < ovRows; ++i )
+				row_work( W, B, cs[B2G_OVERFLOW] + i, phase, true, sc );
+		}
+		__syncthreads();
+	}
+	if ( phase == 0 && sc.enableWarmStarting == 0 )
+		return;
+	for ( int a = 0; a < it.activeCount; ++a )
+	{
+		int c = it.active[a];
+		int nr = cs[c + 1] - cs[c];
+		int nj = phase == 3 ? 0 : js[c + 1] - js[c];
+		if ( phase == 3 && nr == 0 )
+			continue;
+		for ( int t = threadIdx.x; t < nj + nr; t += T )
+		{
+			if ( t < nj )
+				joint_work( W, B, W.jointList[js[c] + t], phase, sc );
+			else
+				row_work( W, B, cs[c] + t - nj, phase, false, sc );
+		}
+		__syncthreads();
+	}
+}
+
+/* The solver stage and finalisation of one world by one CTA (reference src/solver.c
+ * stage order: prepare, substeps of integrate velocities / warm start / solve /
+ * integrate positions / relax, restitution, store impulses, finalize bodies). */
+template <int T>
+__device__ void solve_world( const b2gBatchItem& it, const b2gStepConst& sc, float4* sm )
+{
+	const b2gDevWorld& W = it.W;
+	const int tid = threadIdx.x;
+	const int N = it.bodyIdCount;
+	float4* st0 = sm;
+	float4* st1 = sm + N;
+	float4* term = sm + 2 * N;
+	float* ad = (float*)( sm + 3 * N );
+	SharedBodies B{ st0, st1 };
+	float4* gst = (float4*)W.state;
+	const float4* mass = (const float4*)W.mass;
+
+	if ( tid == 0 )
+		W.counters[1] = 0;
+	for ( int b = tid; b < N; b += T )
+	{
+		st0[b] = gst[2 * b];
+		st1[b] = gst[2 * b + 1];
+	}
+	const int awake = it.awakeCount;
+	for ( int i = tid; i < awake; i += T )
+	{
+		int b = W.awake[i];
+		VelocityTerms v = velocity_terms( mass[b], ( (const float4*)W.force )[b], ( (const float4*)W.extent )[b], sc );
+		term[b] = make_float4( v.lvd.x, v.lvd.y, v.avd, v.ld );
+		ad[b] = v.ad;
+	}
+	const int rows = it.colorStart[B2G_COLORS];
+	for ( int k = tid; k < rows; k += T )
+		prepare_contact_row( W, k, sc );
+	const int joints = it.jointStart[B2G_COLORS];
+	for ( int t = tid; t < joints; t += T )
+		prepare_joint( W, t, sc );
+	__syncthreads();
+
+	for ( int sub = 0; sub < sc.subSteps; ++sub )
+	{
+		for ( int i = tid; i < awake; i += T )
+		{
+			int b = W.awake[i];
+			DevState x = state_of( st0[b], st1[b] );
+			float4 t4 = term[b];
+			VelocityTerms v;
+			v.lvd = gv( t4.x, t4.y );
+			v.avd = t4.z;
+			v.ld = t4.w;
+			v.ad = ad[b];
+			integrate_velocity( x, v, sc );
+			st0[b] = velocity_word( x );
+		}
+		__syncthreads();
+		world_stage<T>( it, B, 0, sc );
+		world_stage<T>( it, B, 1, sc );
+		for ( int i = tid; i < awake; i += T )
+		{
+			int b = W.awake[i];
+			DevState x = state_of( st0[b], st1[b] );
+			integrate_position( x, sc.h );
+			st1[b] = make_float4( x.dp.x, x.dp.y, x.dq.c, x.dq.s );
+		}
+		__syncthreads();
+		world_stage<T>( it, B, 2, sc );
+	}
+	world_stage<T>( it, B, 3, sc );
+
+	for ( int k = tid; k < rows; k += T )
+		store_row( W, k, it.colorStart[B2G_OVERFLOW] );
+	for ( int i = tid; i < awake; i += T )
+	{
+		int b = W.awake[i];
+		gst[2 * b] = st0[b];
+		gst[2 * b + 1] = st1[b];
+	}
+	__syncthreads();
+	for ( int i = tid; i < awake; i += T )
+		finalize_body( W, i, sc );
+}
+
+template <int T>
+__global__ void __launch_bounds__( T ) k_batch_solve( const b2gBatchItem* items, const int* order, int* queue )
+{
+	extern __shared__ float4 sm[];
+	__shared__ int s_next;
+	__shared__ b2gStepConst s_sc;
+	const int m = order[0];
+	for ( ;; )
+	{
+		if ( threadIdx.x == 0 )
+			s_next = atomicAdd( queue, 1 );
+		__syncthreads();
+		int q = s_next;
+		if ( q >= m )
+			break;
+		const b2gBatchItem& it = items[order[1 + q]];
+		if ( threadIdx.x < (int)( sizeof( b2gStepConst ) / 4 ) )
+			( (int*)&s_sc )[threadIdx.x] = ( (const int*)&it.sc )[threadIdx.x];
+		__syncthreads();
+		solve_world<T>( it, s_sc, sm );
+		__syncthreads();
+	}
+}
+
+static_assert( sizeof( b2gStepConst ) / 4 <= 64, "step constants are copied by the first 64 threads" );
+
+/* ------------------------------------------------------------------ host side */
+template <int T>
+static int solve_occupancy( size_t smem )
+{
+	int blocks = 0;
+	cudaFuncSetAttribute( k_batch_solve<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem );
+	if ( cudaOccupancyMaxActiveBlocksPerMultiprocessor( &blocks, k_batch_solve<T>, T, smem ) != cudaSuccess )
+		return 0;
+	return blocks;
+}
+
+template <int T>
+static void launch_solve( b2gBatch* b, size_t smem, int grid )
+{
+	k_batch_solve<T><<<grid, T, smem, b->stream>>>( b->dItems, b->dOrder, b->dQueue );
+}
+
+extern "C" b2gBatch* b2gd_batch_create( void )
+{
+	b2gBatch* b = (b2gBatch*)calloc( 1, sizeof( b2gBatch ) );
+	if ( b == nullptr )
+		return nullptr;
+	if ( cudaStreamCreateWithFlags( &b->stream, cudaStreamNonBlocking ) != cudaSuccess )
+	{
+		free( b );
+		return nullptr;
+	}
+	int dev = 0;
+	cudaGetDevice( &dev );
+	cudaDeviceGetAttribute( &b->sms, cudaDevAttrMultiProcessorCount, dev );
+	for ( int i = 0; i < 4; ++i )
+		cudaEventCreate( &b->ev[i] );
+	cudaMalloc( &b->dQueue, sizeof( int ) );
+	return b;
+}
+
+static void release_graphs( b2gBatch* b )
+{
+	if ( b->collideExec )
+		cudaGraphExecDestroy( b->collideExec );
+	b->collideExec = nullptr;
+	for ( int i = 0; i < TUNE_CANDIDATES; ++i )
+	{
+		if ( b->solveExec[i] )
+			cudaGraphExecDestroy( b->solveExec[i] );
+		b->solveExec[i] = nullptr;
+	}
+}
+
+static void release_buffers( b2gBatch* b )
+{
+	cudaFreeHost( b->hItems );
+	cudaFreeHost( b->hPrefix );
+	cudaFreeHost( b->hOrder );
+	cudaFreeHost( b->hCounters );
+	cudaFree( b->dItems );
+	cudaFree( b->dPrefix );
+	cudaFree( b->dOrder );
+	cudaFree( b->dCounters );
+	b->hItems = b->dItems = nullptr;
+	b->hPrefix = b->dPrefix = b->hOrder = b->dOrder = b->hCounters = b->dCounters = nullptr;
+	b->capacity = 0;
+}
+
+extern "C" void b2gd_batch_destroy( b2gBatch* b )
+{
+	if ( b == nullptr )
+		return;
+	cudaStreamSynchronize( b->stream );
+	release_graphs( b );
+	release_buffers( b );
+	cudaFree( b->dQueue );
+	for ( int i = 0; i < 4; ++i )
+		cudaEventDestroy( b->ev[i] );
+	cudaStreamDestroy( b->stream );
+	free( b );
+}
+
+extern "C" b2gBatchItem* b2gd_batch_items( b2gBatch* b, int count )
+{
+	if ( count <= b->capacity )
+		return b->hItems;
+	cudaStreamSynchronize( b->stream );
+	release_graphs( b );
+	release_buffers( b );
+	int cap = count < 64 ? 64 : count;
+	size_t ints = (size_t)cap + 1;
+	bool ok = cudaMallocHost( &b->hItems, sizeof( b2gBatchItem ) * cap ) == cudaSuccess &&
+			  cudaMallocHost( &b->hPrefix, sizeof( int ) * 2 * ints ) == cudaSuccess &&
+			  cudaMallocHost( &b->hOrder, sizeof( int ) * ints ) == cudaSuccess &&
+			  cudaMallocHost( &b->hCounters, sizeof( int ) * 4 * cap ) == cudaSuccess &&
+			  cudaMalloc( &b->dItems, sizeof( b2gBatchItem ) * cap ) == cudaSuccess &&
+			  cudaMalloc( &b->dPrefix, sizeof( int ) * 2 * ints ) == cudaSuccess &&
+			  cudaMalloc( &b->dOrder, sizeof( int ) * ints ) == cudaSuccess &&
+			  cudaMalloc( &b->dCounters, sizeof( int ) * 4 * cap ) == cudaSuccess;
+	if ( ok == false )
+	{
+		release_buffers( b );
+		return nullptr;
+	}
+	memset( b->hCounters, 0, sizeof( int ) * 4 * cap );
+	b->capacity = cap;
+	return b->hItems;
+}
+
+extern "C" void* b2gd_batch_stream( b2gBatch* b ) { return (void*)b->stream; }
+
+extern "C" const int* b2gd_batch_counters( b2gBatch* b, int i ) { return b->hCounters + 4 * i; }
+
+extern "C" int b2gd_stage_contacts( b2gDevWorld* w, b2gHostIO* io, int count )
+{
+	if ( count <= 0 )
+		return 0;
+	return (int)cudaMemcpyAsync( w->newContacts, io->newContacts, sizeof( b2gContactInit ) * (size_t)count,
+								 cudaMemcpyHostToDevice, (cudaStream_t)w->stream );
+}
+
+static void point_counters( b2gBatch* b, int n )
+{
+	for ( int i = 0; i < n; ++i )
+		b->hItems[i].W.counters = b->dCounters + 4 * i;
+}
+
+extern "C" int b2gd_batch_collide( b2gBatch* b, int n )
+{
+	if ( n <= 0 )
+		return 0;
+	point_counters( b, n );
+	int* ps = b->hPrefix;
+	int* pc = b->hPrefix + n + 1;
+	ps[0] = 0;
+	pc[0] = 0;
+	for ( int i = 0; i < n; ++i )
+	{
+		ps[i + 1] = ps[i] + b->hItems[i].staged;
+		pc[i + 1] = pc[i] + b->hItems[i].idCount;
+	}
+	if ( b->collideExec == nullptr || b->collideN != n )
+	{
+		if ( b->collideExec )
+			cudaGraphExecDestroy( b->collideExec );
+		b->collideExec = nullptr;
+		int grid = b->sms * 8;
+		cudaGraph_t g = nullptr;
+		cudaStreamBeginCapture( b->stream, cudaStreamCaptureModeThreadLocal );
+		cudaMemcpyAsync( b->dItems, b->hItems, sizeof( b2gBatchItem ) * n, cudaMemcpyHostToDevice, b->stream );
+		cudaMemcpyAsync( b->dPrefix, b->hPrefix, sizeof( int ) * 2 * ( n + 1 ), cudaMemcpyHostToDevice, b->stream );
+		cudaMemsetAsync( b->dCounters, 0, sizeof( int ) * 4 * n, b->stream );
+		k_batch_scatter<<<grid, BATCH_GRID_THREADS, 0, b->stream>>>( b->dItems, b->dPrefix, n );
+		k_batch_collide<<<grid, BATCH_GRID_THREADS, 0, b->stream>>>( b->dItems, b->dPrefix + n + 1, n );
+		cudaMemcpyAsync( b->hCounters, b->dCounters, sizeof( int ) * 4 * n, cudaMemcpyDeviceToHost, b->stream );
+		cudaError_t e = cudaStreamEndCapture( b->stream, &g );
+		if ( e != cudaSuccess )
+			return (int)e;
+		e = cudaGraphInstantiate( &b->collideExec, g, 0 );
+		cudaGraphDestroy( g );
+		if ( e != cudaSuccess )
+			return (int)e;
+		b->collideN = n;
+	}
+	cudaEventRecord( b->ev[0], b->stream );
+	cudaError_t e = cudaGraphLaunch( b->collideExec, b->stream );
+	cudaEventRecord( b->ev[1], b->stream );
+	b->collideTimed = 1;
+	b->launches = 2;
+	return (int)e;
+}
+
+static int order_by_size( b2gBatch* b, int n, int* maxBodies )
+{
+	/* worlds to solve, largest first (a counting sort on body count) */
+	int m = 0, top = 0;
+	for ( int i = 0; i < n; ++i )
+	{
+		if ( b->hItems[i].solve == 0 )
+			continue;
+		int nb = b->hItems[i].bodyIdCount;
+		top = nb > top ? nb : top;
+		m += 1;
+	}
+	*maxBodies = top;
+	int* order = b->hOrder + 1;
+	b->hOrder[0] = m;
+	if ( m == 0 )
+		return 0;
+	const int buckets = 64;
+	int count[buckets + 1];
+	memset( count, 0, sizeof( count ) );
+	for ( int i = 0; i < n; ++i )
+		if ( b->hItems[i].solve )
+			count[buckets - 1 - (int)( (long long)b->hItems[i].bodyIdCount * ( buckets - 1 ) / ( top > 0 ? top : 1 ) )] += 1;
+	for ( int k = 0, s = 0; k <= buckets; ++k )
+	{
+		int c = count[k];
+		count[k] = s;
+		s += c;
+	}
+	for ( int i = 0; i < n; ++i )
+		if ( b->hItems[i].solve )
+			order[count[buckets - 1 - (int)( (long long)b->hItems[i].bodyIdCount * ( buckets - 1 ) / ( top > 0 ? top : 1 ) )]++] = i;
+	return m;
+}
+
+extern "C" int b2gd_batch_solve( b2gBatch* b, int n )
+{
+	if ( n <= 0 )
+		return 0;
+	point_counters( b, n );
+	int maxBodies = 0;
+	order_by_size( b, n, &maxBodies );
+	/* shared memory: state (2 float4), velocity terms (float4 + float) per body id,
+	 * rounded up to 256 body ids so that growing worlds rarely recapture the graph */
+	int slots = ( ( maxBodies > 0 ? maxBodies : 1 ) + 255 ) / 256 * 256;
+	size_t smem = (size_t)slots * ( 3 * 16 + 4 );
+	if ( smem > 226 * 1024 )
+		return (int)cudaErrorInvalidValue;
+
+	int choice = b->tuned ? b->choice : ( b->tuneStep / TUNE_SAMPLES ) % TUNE_CANDIDATES;
+	if ( b->solveExec[choice] == nullptr || b->solveN[choice] != n || b->solveSmem[choice] != (int)smem )
+	{
+		if ( b->solveExec[choice] )
+			cudaGraphExecDestroy( b->solveExec[choice] );
+		b->solveExec[choice] = nullptr;
+		int T = s_tuneThreads[choice];
+		int occ = T == 64 ? solve_occupancy<64>( smem ) : T == 128 ? solve_occupancy<128>( smem ) : solve_occupancy<256>( smem );
+		if ( occ <= 0 )
+			return (int)cudaErrorInvalidConfiguration;
+		int grid = b->sms * occ;
+		cudaGraph_t g = nullptr;
+		cudaStreamBeginCapture( b->stream, cudaStreamCaptureModeThreadLocal );
+		cudaMemcpyAsync( b->dItems, b->hItems, sizeof( b2gBatchItem ) * n, cudaMemcpyHostToDevice, b->stream );
+		cudaMemcpyAsync( b->dOrder, b->hOrder, sizeof( int ) * ( n + 1 ), cudaMemcpyHostToDevice, b->stream );
+		cudaMemsetAsync( b->dQueue, 0, sizeof( int ), b->stream );
+		if ( T == 64 )
+			launch_solve<64>( b, smem, grid );
+		else if ( T == 128 )
+			launch_solve<128>( b, smem, grid );
+		else
+			launch_solve<256>( b, smem, grid );
+		cudaMemcpyAsync( b->hCounters, b->dCounters, sizeof( int ) * 4 * n, cudaMemcpyDeviceToHost, b->stream );
+		cudaError_t e = cudaStreamEndCapture( b->stream, &g );
+		if ( e != cudaSuccess )
+			return (int)e;
+		e = cudaGraphInstantiate( &b->solveExec[choice], g, 0 );
+		cudaGraphDestroy( g );
+		if ( e != cudaSuccess )
+			return (int)e;
+		b->solveN[choice] = n;
+		b->solveSmem[choice] = (int)smem;
+	}
+	cudaEventRecord( b->ev[2], b->stream );
+	cudaError_t e = cudaGraphLaunch( b->solveExec[choice], b->stream );
+	cudaEventRecord( b->ev[3], b->stream );
+	b->choice = choice;
+	b->solveTimed = 1;
+	b->launches += 1;
+	return (int)e;
+}
+
+extern "C" int b2gd_batch_sync( b2gBatch* b )
+{
+	cudaError_t e = cudaStreamSynchronize( b->stream );
+	if ( e != cudaSuccess )
+		return (int)e;
+	if ( b->collideTimed )
+		cudaEventElapsedTime( &b->collideMs, b->ev[0], b->ev[1] );
+	if ( b->solveTimed )
+	{
+		cudaEventElapsedTime( &b->solveMs, b->ev[2], b->ev[3] );
+		if ( b->tuned == 0 )
+		{
+			/* the later sample of each candidate counts */
+			if ( b->tuneStep % TUNE_SAMPLES == TUNE_SAMPLES - 1 )
+				b->tuneMs[b->choice] = b->solveMs;
+			b->tuneStep += 1;
+			if ( b->tuneStep == TUNE_SAMPLES * TUNE_CANDIDATES )
+			{
+				int best = 0;
+				for ( int i = 1; i < TUNE_CANDIDATES; ++i )
+					best = b->tuneMs[i] < b->tuneMs[best] ? i : best;
+				b->choice = best;
+				b->tuned = 1;
+				for ( int i = 0; i < TUNE_CANDIDATES; ++i )
+				{
+					if ( i != best && b->solveExec[i] )
+					{
+						cudaGraphExecDestroy( b->solveExec[i] );
+						b->solveExec[i] = nullptr;
+					}
+				}
+			}
+		}
+	}
+	b->collideTimed = 0;
+	b->solveTimed = 0;
+	return (int)cudaGetLastError();
+}
+
+extern "C" void b2gd_batch_stats( b2gBatch* b, float* collideMs, float* solveMs, int* threads, int* launches )
+{
+	*collideMs = b->collideMs;
+	*solveMs = b->solveMs;
+	*threads = b->tuned ? s_tuneThreads[b->choice] : 0;
+	*launches = b->launches;
+}

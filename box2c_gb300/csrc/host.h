@@ -277,6 +277,8 @@ typedef struct gWorld
 	int status; /* last CUDA error or 0 */
 	int unsupportedToi;
 	int lastEventCount, lastRecordCount;
+	double stepStart; /* host clock at the start of the current step phase */
+	int stepIdCount;  /* contact ids of the current step's narrowphase */
 
 	b2gDevWorld dev;
 	b2gHostIO io;
@@ -292,6 +294,15 @@ void gworld_reserve_mirrors( gWorld* w );
 void gworld_flush( gWorld* w );
 
 void gstep_run( gWorld* w, float dt, int subSteps );
+
+/* Phases of one step, driven by gstep_run for one world and by b2World_StepBatch for
+ * many: begin (pairs, staging) -> narrowphase on the device (trees rebuilt meanwhile)
+ * -> after_collide (events, constants, solve lists) -> solver on the device -> finish
+ * (records). */
+int gstep_begin( gWorld* w );
+void gstep_rebuild_trees( gWorld* w );
+int gstep_after_collide( gWorld* w, float dt, int subSteps, b2gStepConst* sc, b2gSolvePlan* plan );
+void gstep_finish( gWorld* w );
 void gcontact_create( gWorld* w, gShape* a, gShape* b );
 void gcontact_destroy( gWorld* w, gContact* c );
 int gassign_joint_color( gWorld* w, int bodyIdA, int bodyIdB, bool staticA, bool staticB );

@@ -650,88 +650,127 @@ static void build_solve_lists( gWorld* w, b2gSolvePlan* plan )
 	w->solveUploaded = false;
 }
 
-void gstep_run( gWorld* w, float dt, int subSteps )
+/* Host work before the narrowphase: pair update, device capacity, contact staging.
+ * Returns the number of staged contact records, or -1 after a device failure. */
+int gstep_begin( gWorld* w )
 {
 	double t0 = b2g_now_ms();
 	update_pairs( w );
 	double t1 = b2g_now_ms();
 	w->profile.pairs = (float)( t1 - t0 );
+	w->stepStart = t1;
 
 	int idCount = w->contactIds.next;
 	int e = b2gd_reserve( &w->dev, &w->io, w->bodyIds.next, w->shapeIds.next, idCount, w->jointIds.next, idCount, w->shapeIds.next );
 	if ( e )
 	{
 		w->status = e;
-		return;
+		return -1;
 	}
 	int staged = compact_pending( w );
 	if ( staged > 0 )
 		memcpy( w->io.newContacts, w->pending, sizeof( b2gContactInit ) * (size_t)staged );
 	w->pendingCount = 0;
-	e = b2gd_collide( &w->dev, &w->io, staged, idCount );
-	/* the tree rebuild overlaps the device narrowphase (reference src/world.c:420) */
+	w->stepIdCount = idCount;
+	return staged;
+}
+
+/* Runs while the device narrowphase is in flight (reference src/world.c:420). */
+void gstep_rebuild_trees( gWorld* w )
+{
 	gtree_rebuild( w->trees + b2_dynamicBody );
 	gtree_rebuild( w->trees + b2_kinematicBody );
-	e |= b2gd_sync( &w->dev );
-	if ( e )
-	{
-		w->status = e;
-		return;
-	}
+}
+
+/* Host work between the narrowphase and the solver: events in contact-id order, step
+ * constants, solve lists.  Returns 1 when the solver stage has to run. */
+int gstep_after_collide( gWorld* w, float dt, int subSteps, b2gStepConst* sc, b2gSolvePlan* plan )
+{
 	int eventCount = w->io.counters[0];
 	w->lastEventCount = eventCount;
 	process_events( w, eventCount < w->dev.eventCap ? eventCount : w->dev.eventCap );
 	double t2 = b2g_now_ms();
-	w->profile.collide = (float)( t2 - t1 );
+	w->profile.collide = (float)( t2 - w->stepStart );
+	w->stepStart = t2;
 
 	if ( dt <= 0.0f )
-		return;
+		return 0;
 
-	b2gStepConst sc;
-	memset( &sc, 0, sizeof( sc ) );
-	sc.subSteps = subSteps < 1 ? 1 : subSteps;
-	sc.dt = dt;
-	sc.inv_dt = 1.0f / dt;
-	sc.h = dt / (float)sc.subSteps;
-	sc.inv_h = (float)sc.subSteps * sc.inv_dt;
-	w->inv_h = sc.inv_h;
-	float contactHertz = gmin( w->contactHertz, 0.25f * sc.inv_h );
-	float jointHertz = gmin( w->jointHertz, 0.125f * sc.inv_h );
-	make_soft( contactHertz, w->contactDamping, sc.h, sc.contactSoft );
-	make_soft( 2.0f * contactHertz, w->contactDamping, sc.h, sc.staticSoft );
-	make_soft( jointHertz, w->jointDamping, sc.h, sc.jointSoft );
-	sc.restitutionThreshold = w->restitutionThreshold;
-	sc.pushout = w->pushout;
-	sc.gravity = w->gravity;
-	sc.enableWarmStarting = w->enableWarmStarting;
-	sc.enableContinuous = w->enableContinuous;
-	sc.enableSleep = w->enableSleep;
+	memset( sc, 0, sizeof( *sc ) );
+	sc->subSteps = subSteps < 1 ? 1 : subSteps;
+	sc->dt = dt;
+	sc->inv_dt = 1.0f / dt;
+	sc->h = dt / (float)sc->subSteps;
+	sc->inv_h = (float)sc->subSteps * sc->inv_dt;
+	w->inv_h = sc->inv_h;
+	float contactHertz = gmin( w->contactHertz, 0.25f * sc->inv_h );
+	float jointHertz = gmin( w->jointHertz, 0.125f * sc->inv_h );
+	make_soft( contactHertz, w->contactDamping, sc->h, sc->contactSoft );
+	make_soft( 2.0f * contactHertz, w->contactDamping, sc->h, sc->staticSoft );
+	make_soft( jointHertz, w->jointDamping, sc->h, sc->jointSoft );
+	sc->restitutionThreshold = w->restitutionThreshold;
+	sc->pushout = w->pushout;
+	sc->gravity = w->gravity;
+	sc->enableWarmStarting = w->enableWarmStarting;
+	sc->enableContinuous = w->enableContinuous;
+	sc->enableSleep = w->enableSleep;
 
 	if ( w->awake.count == 0 )
-		return;
+		return 0;
 
-	b2gSolvePlan plan;
-	build_solve_lists( w, &plan );
-	plan.awakeCount = w->awake.count;
-	plan.bodyIdCount = w->bodyIds.next;
+	build_solve_lists( w, plan );
+	plan->awakeCount = w->awake.count;
+	plan->bodyIdCount = w->bodyIds.next;
 	if ( w->solveUploaded == false )
 	{
-		e = b2gd_upload_solve_lists( &w->dev, w->solveList.data, w->solveList.count, w->jointList.data, w->jointList.count );
+		int e = b2gd_upload_solve_lists( &w->dev, w->solveList.data, w->solveList.count, w->jointList.data, w->jointList.count );
+		if ( e )
+		{
+			w->status = e;
+			return 0;
+		}
 		w->solveUploaded = true;
 	}
-	e |= b2gd_solve( &w->dev, &w->io, &plan, &sc );
+	return 1;
+}
+
+/* Host work after the solver stage: finalisation records in the reference's awake order
+ * (proxy enlargement, move buffer). */
+void gstep_finish( gWorld* w )
+{
+	double t3 = b2g_now_ms();
+	w->profile.solve = (float)( t3 - w->stepStart );
+	int recordCount = w->io.counters[1];
+	w->lastRecordCount = recordCount;
+	process_records( w, recordCount < w->dev.recordCap ? recordCount : w->dev.recordCap );
+	w->profile.broadphase = (float)( b2g_now_ms() - t3 );
+}
+
+void gstep_run( gWorld* w, float dt, int subSteps )
+{
+	int staged = gstep_begin( w );
+	if ( staged < 0 )
+		return;
+	int e = b2gd_collide( &w->dev, &w->io, staged, w->stepIdCount );
+	gstep_rebuild_trees( w );
 	e |= b2gd_sync( &w->dev );
 	if ( e )
 	{
 		w->status = e;
 		return;
 	}
-	double t3 = b2g_now_ms();
-	w->profile.solve = (float)( t3 - t2 );
-	int recordCount = w->io.counters[1];
-	w->lastRecordCount = recordCount;
-	process_records( w, recordCount < w->dev.recordCap ? recordCount : w->dev.recordCap );
-	w->profile.broadphase = (float)( b2g_now_ms() - t3 );
+	b2gStepConst sc;
+	b2gSolvePlan plan;
+	if ( gstep_after_collide( w, dt, subSteps, &sc, &plan ) == 0 )
+		return;
+	e = b2gd_solve( &w->dev, &w->io, &plan, &sc );
+	e |= b2gd_sync( &w->dev );
+	if ( e )
+	{
+		w->status = e;
+		return;
+	}
+	gstep_finish( w );
 }
 
 void b2World_Step( b2WorldId worldId, float timeStep, int subStepCount )

@@ -46,6 +46,27 @@ B2_API b2DeviceTimes b2World_GetDeviceTimes( b2WorldId worldId );
  * bit-identical results. */
 B2_API void b2World_EnableFusedSolver( b2WorldId worldId, bool flag );
 
+/* Steps `count` independent worlds by one b2World_Step each.  The device work of all of
+ * them runs together: one replayed CUDA graph for contact creation and the narrowphase
+ * of every world, one for the solver stage and finalisation (a persistent kernel in
+ * which each CTA solves whole worlds, largest first).  Every world gets exactly the
+ * results b2World_Step would give it alone.  Invalid, failed or repeated ids are
+ * skipped.  Not thread-safe: one batch at a time per process. */
+B2_API void b2World_StepBatch( const b2WorldId* worldIds, int count, float timeStep, int subStepCount );
+
+/* Device milliseconds of the last batched step's narrowphase and solver segments, the
+ * solver CTA size picked by the autotuner (0 while it is still timing candidates) and
+ * the kernel launches of the last batched step. */
+typedef struct b2BatchStats
+{
+	float collide;
+	float solve;
+	int solveThreads;
+	int launches;
+} b2BatchStats;
+
+B2_API b2BatchStats b2World_GetBatchStats( void );
+
 /* Copies p.x p.y q.c q.s v.x v.y w (7 floats) of every body id into out (7 * capacity
  * floats).  One device-to-host copy per call.  Returns the number of body ids. */
 B2_API int b2World_GetBodyStates( b2WorldId worldId, float* out, int capacity );

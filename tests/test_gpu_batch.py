@@ -1,0 +1,89 @@
+"""b2World_StepBatch (include/box2d/gpu.h): many worlds stepped together must give each
+world exactly the bits the oracle gives it stepped alone (reference b2World_Step)."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from box2c_gb300.capi import bind_batch_api, contact_table, world_array
+
+pytestmark = pytest.mark.gpu
+
+
+def _scenes(backend, bases):
+    worlds = [backend.pyramid(int(b), 0.01, 100 + i) for i, b in enumerate(bases)]
+    worlds.append(backend.tumbler(300, 7, 0))
+    worlds.append(backend.hello_world()[0])
+    return worlds
+
+
+def _compare(gpu, oracle, wg, wo):
+    for i, (a, b) in enumerate(zip(wg, wo)):
+        ta, tb = contact_table(gpu.contacts(a)), contact_table(oracle.contacts(b))
+        if ta.shape != tb.shape or not np.array_equal(ta, tb):
+            return f"world {i}: contacts/colours differ"
+        ba, bb = gpu.bodies(a), oracle.bodies(b)
+        if not np.array_equal(ba.view(np.uint32), bb.view(np.uint32)):
+            return f"world {i}: body state differs"
+    return None
+
+
+def test_batch_matches_oracle_worlds(gpu, oracle):
+    bind_batch_api(gpu.lib)
+    rng = np.random.default_rng(5)
+    bases = rng.integers(4, 41, size=14)
+    wg, wo = _scenes(gpu, bases), _scenes(oracle, bases)
+    ids = world_array(wg)
+    try:
+        for s in range(1, 61):
+            gpu.lib.b2World_StepBatch(ids, len(wg), 1.0 / 60.0, 4)
+            for w in wo:
+                oracle.step(w)
+            if s in (1, 2, 5, 10, 30, 60):
+                err = _compare(gpu, oracle, wg, wo)
+                assert err is None, f"step {s}: {err}"
+        stats = gpu.lib.b2World_GetBatchStats()
+        assert stats.solveThreads in (64, 128, 256)  # the autotuner has chosen
+        assert stats.launches == 3
+    finally:
+        for w in wg:
+            gpu.destroy(w)
+        for w in wo:
+            oracle.destroy(w)
+
+
+def test_batch_skips_invalid_and_repeated_ids(gpu, oracle):
+    bind_batch_api(gpu.lib)
+    a, b = gpu.pyramid(6), oracle.pyramid(6)
+    bad = type(a)(index1=4000, revision=1)
+    ids = world_array([a, bad, a])
+    try:
+        for _ in range(20):
+            gpu.lib.b2World_StepBatch(ids, 3, 1.0 / 60.0, 4)
+            oracle.step(b)
+        assert _compare(gpu, oracle, [a], [b]) is None
+    finally:
+        gpu.destroy(a)
+        oracle.destroy(b)
+
+
+def test_batch_then_single_steps_continue_bit_exact(gpu, oracle):
+    """Batched and single steps can be mixed on the same world."""
+    bind_batch_api(gpu.lib)
+    wg, wo = [gpu.pyramid(12), gpu.pyramid(7)], [oracle.pyramid(12), oracle.pyramid(7)]
+    ids = world_array(wg)
+    try:
+        for s in range(40):
+            if s % 3 == 0:
+                for w in wg:
+                    gpu.step(w)
+            else:
+                gpu.lib.b2World_StepBatch(ids, 2, 1.0 / 60.0, 4)
+            for w in wo:
+                oracle.step(w)
+        assert _compare(gpu, oracle, wg, wo) is None
+    finally:
+        for w in wg + wo[:0]:
+            gpu.destroy(w)
+        for w in wo:
+            oracle.destroy(w)
