@@ -168,6 +168,9 @@ extern "C" int b2gd_reserve( b2gDevWorld* w, b2gHostIO* io, int bodyCap, int sha
 {
 	cudaStream_t s = (cudaStream_t)w->stream;
 	int e = 0;
+	if ( bodyCap <= w->bodyCap && shapeCap <= w->shapeCap && contactCap <= w->contactCap && solveCap <= w->solveCap &&
+		 jointCap <= w->jointCap )
+		return 0;
 	if ( bodyCap > w->bodyCap )
 	{
 		int nc = next_cap( w->bodyCap, bodyCap );
@@ -240,6 +243,7 @@ extern "C" int b2gd_reserve( b2gDevWorld* w, b2gHostIO* io, int bodyCap, int sha
 		w->jointCap = nc;
 	}
 	(void)listCap;
+	/* new arrays are cleared and filled on the stream: finish before the host uses them */
 	if ( e == 0 )
 		e = ok( cudaStreamSynchronize( s ) );
 	return e;

@@ -43,6 +43,108 @@ static void fill_item( b2gBatchItem* it, gWorld* w )
 	it->bodyIdCount = w->bodyIds.next;
 }
 
+typedef struct BatchCtx
+{
+	b2gBatchItem* items;
+	void* stream;
+	float timeStep;
+	int subStepCount;
+	int error;
+} BatchCtx;
+
+static void begin_worlds( int begin, int end, void* arg )
+{
+	BatchCtx* c = (BatchCtx*)arg;
+	for ( int k = begin; k < end; ++k )
+	{
+		gWorld* w = s_worlds[k];
+		b2gBatchItem* it = c->items + k;
+		memset( it, 0, sizeof( *it ) );
+		w->beginCount = 0;
+		w->endCount = 0;
+		memset( &w->profile, 0, sizeof( w->profile ) );
+		s_streams[k] = w->dev.stream;
+		w->dev.stream = c->stream;
+		gworld_flush( w );
+		int staged = gstep_begin( w );
+		if ( staged < 0 )
+			continue;
+		if ( b2gd_stage_contacts( &w->dev, &w->io, staged ) != 0 )
+		{
+			w->status = -1;
+			continue;
+		}
+		fill_item( it, w );
+		it->idCount = w->stepIdCount;
+		it->staged = staged;
+	}
+}
+
+static void rebuild_worlds( int begin, int end, void* arg )
+{
+	(void)arg;
+	for ( int k = begin; k < end; ++k )
+		if ( s_worlds[k]->status == 0 )
+			gstep_rebuild_trees( s_worlds[k] );
+}
+
+static void middle_worlds( int begin, int end, void* arg )
+{
+	BatchCtx* c = (BatchCtx*)arg;
+	for ( int k = begin; k < end; ++k )
+	{
+		gWorld* w = s_worlds[k];
+		b2gBatchItem* it = c->items + k;
+		if ( c->error != 0 )
+			w->status = c->error;
+		if ( w->status != 0 )
+		{
+			it->solve = 0;
+			continue;
+		}
+		w->io.counters[0] = b2gd_batch_counters( s_batch, k )[0];
+		b2gStepConst sc;
+		b2gSolvePlan plan;
+		int run = gstep_after_collide( w, c->timeStep, c->subStepCount, &sc, &plan );
+		/* uploads above may have grown the arena: copy the descriptor again */
+		fill_item( it, w );
+		it->solve = run && w->status == 0;
+		if ( it->solve == 0 )
+			continue;
+		it->sc = sc;
+		memcpy( it->colorStart, plan.colorStart, sizeof( it->colorStart ) );
+		memcpy( it->jointStart, plan.jointStart, sizeof( it->jointStart ) );
+		memcpy( it->active, plan.active, sizeof( it->active ) );
+		it->activeCount = plan.activeCount;
+		it->awakeCount = plan.awakeCount;
+		it->bodyIdCount = plan.bodyIdCount;
+	}
+}
+
+static void finish_worlds( int begin, int end, void* arg )
+{
+	BatchCtx* c = (BatchCtx*)arg;
+	for ( int k = begin; k < end; ++k )
+	{
+		gWorld* w = s_worlds[k];
+		if ( c->error != 0 && w->status == 0 )
+			w->status = c->error;
+		if ( c->items[k].solve && w->status == 0 )
+		{
+			w->io.counters[1] = b2gd_batch_counters( s_batch, k )[1];
+			gstep_finish( w );
+		}
+		w->dev.stream = s_streams[k];
+		w->dev.launches = 0;
+		w->dev.fusedUsed = 0;
+		w->mirrorStale = true;
+		w->shapeMirrorStale = true;
+		w->jointMirrorStale = true;
+	}
+}
+
+static float s_hostMs[5];
+
 void b2World_StepBatch( const b2WorldId* worldIds, int count, float timeStep, int subStepCount )
 {
 	if ( worldIds == NULL || count <= 0 || timeStep == 0.0f )
@@ -70,97 +172,46 @@ void b2World_StepBatch( const b2WorldId* worldIds, int count, float timeStep, in
 	}
 	if ( n == 0 )
 		return;
-	b2gBatchItem* items = b2gd_batch_items( s_batch, n );
-	void* stream = b2gd_batch_stream( s_batch );
-	if ( items == NULL )
+	BatchCtx c;
+	c.items = b2gd_batch_items( s_batch, n );
+	c.stream = b2gd_batch_stream( s_batch );
+	c.timeStep = timeStep;
+	c.subStepCount = subStepCount;
+	c.error = 0;
+	if ( c.items == NULL )
 	{
 		for ( int k = 0; k < n; ++k )
 			s_worlds[k]->locked = false;
 		return;
 	}
+	const int grain = 16;
 
 	double t0 = b2g_now_ms();
-	for ( int k = 0; k < n; ++k )
-	{
-		gWorld* w = s_worlds[k];
-		b2gBatchItem* it = items + k;
-		memset( it, 0, sizeof( *it ) );
-		w->beginCount = 0;
-		w->endCount = 0;
-		memset( &w->profile, 0, sizeof( w->profile ) );
-		s_streams[k] = w->dev.stream;
-		w->dev.stream = stream;
-		gworld_flush( w );
-		int staged = gstep_begin( w );
-		if ( staged < 0 )
-			continue;
-		if ( b2gd_stage_contacts( &w->dev, &w->io, staged ) != 0 )
-		{
-			w->status = -1;
-			continue;
-		}
-		fill_item( it, w );
-		it->idCount = w->stepIdCount;
-		it->staged = staged;
-	}
-
+	gpool_for( n, grain, begin_worlds, &c );
+	double t1 = b2g_now_ms();
 	int e = b2gd_batch_collide( s_batch, n );
-	for ( int k = 0; k < n; ++k )
-		if ( s_worlds[k]->status == 0 )
-			gstep_rebuild_trees( s_worlds[k] );
+	gpool_for( n, grain, rebuild_worlds, &c );
 	e |= b2gd_batch_sync( s_batch );
-
-	for ( int k = 0; k < n; ++k )
-	{
-		gWorld* w = s_worlds[k];
-		b2gBatchItem* it = items + k;
-		if ( e != 0 )
-			w->status = e;
-		if ( w->status != 0 )
-		{
-			it->solve = 0;
-			continue;
-		}
-		w->io.counters[0] = b2gd_batch_counters( s_batch, k )[0];
-		b2gStepConst sc;
-		b2gSolvePlan plan;
-		int run = gstep_after_collide( w, timeStep, subStepCount, &sc, &plan );
-		/* uploads above may have grown the arena: copy the descriptor again */
-		fill_item( it, w );
-		it->solve = run && w->status == 0;
-		if ( it->solve == 0 )
-			continue;
-		it->sc = sc;
-		memcpy( it->colorStart, plan.colorStart, sizeof( it->colorStart ) );
-		memcpy( it->jointStart, plan.jointStart, sizeof( it->jointStart ) );
-		memcpy( it->active, plan.active, sizeof( it->active ) );
-		it->activeCount = plan.activeCount;
-		it->awakeCount = plan.awakeCount;
-		it->bodyIdCount = plan.bodyIdCount;
-	}
-
+	double t2 = b2g_now_ms();
+	c.error = e;
+	gpool_for( n, grain, middle_worlds, &c );
+	double t3 = b2g_now_ms();
 	e = b2gd_batch_solve( s_batch, n );
 	e |= b2gd_batch_sync( s_batch );
-
-	double t1 = b2g_now_ms();
+	double t4 = b2g_now_ms();
+	c.error = e;
+	gpool_for( n, grain, finish_worlds, &c );
+	double t5 = b2g_now_ms();
+	s_hostMs[0] = (float)( t1 - t0 );
+	s_hostMs[1] = (float)( t2 - t1 );
+	s_hostMs[2] = (float)( t3 - t2 );
+	s_hostMs[3] = (float)( t4 - t3 );
+	s_hostMs[4] = (float)( t5 - t4 );
 	for ( int k = 0; k < n; ++k )
 	{
 		gWorld* w = s_worlds[k];
-		if ( e != 0 && w->status == 0 )
-			w->status = e;
-		if ( items[k].solve && w->status == 0 )
-		{
-			w->io.counters[1] = b2gd_batch_counters( s_batch, k )[1];
-			gstep_finish( w );
-		}
-		w->dev.stream = s_streams[k];
-		w->dev.launches = 0;
-		w->dev.fusedUsed = 0;
-		w->mirrorStale = true;
-		w->shapeMirrorStale = true;
-		w->jointMirrorStale = true;
 		w->locked = false;
-		w->profile.step = (float)( t1 - t0 ) / (float)n;
+		w->profile.step = (float)( t5 - t0 ) / (float)n;
 		if ( w->status )
 			gworld_fail( b2gd_last_error() );
 	}
@@ -172,5 +223,11 @@ b2BatchStats b2World_GetBatchStats( void )
 	memset( &s, 0, sizeof( s ) );
 	if ( s_batch != NULL )
 		b2gd_batch_stats( s_batch, &s.collide, &s.solve, &s.solveThreads, &s.launches );
+	s.hostBegin = s_hostMs[0];
+	s.hostCollide = s_hostMs[1];
+	s.hostMiddle = s_hostMs[2];
+	s.hostSolve = s_hostMs[3];
+	s.hostFinish = s_hostMs[4];
+	s.hostThreads = gpool_threads();
 	return s;
 }

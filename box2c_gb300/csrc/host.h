@@ -300,6 +300,11 @@ void gstep_run( gWorld* w, float dt, int subSteps );
  * -> after_collide (events, constants, solve lists) -> solver on the device -> finish
  * (records). */
 int gstep_begin( gWorld* w );
+
+/* Fork-join pool for per-world host work (pool.c). */
+typedef void gTaskFn( int begin, int end, void* ctx );
+void gpool_for( int count, int grain, gTaskFn* fn, void* ctx );
+int gpool_threads( void );
 void gstep_rebuild_trees( gWorld* w );
 int gstep_after_collide( gWorld* w, float dt, int subSteps, b2gStepConst* sc, b2gSolvePlan* plan );
 void gstep_finish( gWorld* w );
