@@ -149,6 +149,131 @@ def cpu_baseline(steps_sample=20):
     return ms, steps_sample
 
 
+BATCH_WORLDS = 4096
+BATCH_SEED = 1237
+
+
+def batch_bases():
+    """Pyramid bases U{4..40} for the batched workload (4096 worlds)."""
+    rng = np.random.default_rng(BATCH_SEED)
+    return rng.integers(4, 41, size=BATCH_WORLDS)
+
+
+def run_batch(g, steps, warmup):
+    """Batched worlds: 4096 pyramids with bases U{4..40} (config-0 material, dt, substeps)
+    stepped together with b2World_StepBatch; also times a loop of single-world
+    b2World_Step calls over a sample of the same worlds."""
+    from box2c_gb300.capi import bind_batch_api, world_array
+    import torch
+    L = g.lib
+    bind_batch_api(L)
+    bases = batch_bases()
+    worlds = [g.pyramid(int(b), 0.0, 0) for b in bases]
+    ids = world_array(worlds)
+    n = len(worlds)
+    for _ in range(max(3, warmup)):
+        L.b2World_StepBatch(ids, n, DT, SUBSTEPS)
+    torch.cuda.synchronize()
+    host, dev_c, dev_s = [], [], []
+    prof = []
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        t = time.perf_counter()
+        L.b2World_StepBatch(ids, n, DT, SUBSTEPS)
+        host.append(time.perf_counter() - t)
+        st = L.b2World_GetBatchStats()
+        dev_c.append(st.collide)
+        dev_s.append(st.solve)
+        prof.append((st.hostBegin, st.hostCollide, st.hostMiddle, st.hostSolve, st.hostFinish))
+    total = time.perf_counter() - t0
+    st = L.b2World_GetBatchStats()
+    # loop of single-world steps over a sample (the per-world path)
+    sample = worlds[:256]
+    t = time.perf_counter()
+    for w in sample:
+        L.b2World_Step(w, DT, SUBSTEPS)
+    loop = len(sample) / (time.perf_counter() - t)
+    bodies = int(sum(int(b) * (int(b) + 1) // 2 for b in bases))
+    failed = sum(1 for w in worlds if L.b2World_GetStatus(w) != 0)
+    for w in worlds:
+        g.destroy(w)
+    value = n * steps / total
+    return {
+        "metric": "batched world-steps/s", "value": round(value, 1), "unit": "world-steps/s",
+        "worlds": n, "bodies": bodies, "steps": steps, "warmup": max(3, warmup),
+        "ms_per_batched_step": round(total * 1e3 / steps, 4),
+        "device_ms": {"collide": round(float(np.mean(dev_c)), 4), "solve": round(float(np.mean(dev_s)), 4)},
+        "host_ms": dict(zip(("prepare", "narrowphase_wait", "events_lists", "solve_wait", "records"),
+                            [round(float(x), 4) for x in np.mean(np.array(prof), 0)])),
+        "host_threads": st.hostThreads, "solve_cta_threads": st.solveThreads, "gpu_launches_per_step": st.launches,
+        "loop_world_steps_per_s": round(loop, 1), "speedup_vs_loop": round(value / loop, 1),
+        "failed_worlds": failed,
+    }
+
+
+def run_adjoint(g, reps=3):
+    """Differentiable stepping: 256 worlds x 8 boxes (half-extent 0.5) dropped from
+    U(1,5) m with N(0,1) velocities and per-world friction U(0.2,0.9), 120 steps x 4
+    substeps; loss = sum of squared final positions; gradient w.r.t. initial velocities
+    and friction by b2World_StepBackwardBatch.  Times the stepped forward (plain and
+    recording) and the backward pass."""
+    import torch
+    from box2c_gb300.autograd import DropBoxes
+    rng = np.random.default_rng(1238)
+    n = 256
+    heights = rng.uniform(1, 5, size=(n, 8)).astype(np.float32)
+    v0 = rng.normal(0, 1, size=(n, 8, 2)).astype(np.float32)
+    mu = rng.uniform(0.2, 0.9, size=n).astype(np.float32)
+    sim = DropBoxes(g, heights, steps=120, substeps=SUBSTEPS, dt=DT)
+    plain, taped, back = [], [], []
+    for r in range(reps + 1):
+        sim.create(v0, mu, record=False)
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        sim.step_all()
+        p0 = sim.positions()
+        plain.append(time.perf_counter() - t)
+        sim.create(v0, mu, record=True)
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        sim.step_all()
+        p = sim.positions()
+        taped.append(time.perf_counter() - t)
+        t = time.perf_counter()
+        gv, gm = sim.backward(2.0 * p)
+        back.append(time.perf_counter() - t)
+    sim.destroy()
+    f0, f1, bw = (1e3 * float(np.median(x[1:])) for x in (plain, taped, back))
+    return {
+        "metric": "fwd+bwd vs fwd ms", "workload": "256 worlds x 8 boxes, 120 steps x 4 substeps",
+        "fwd_ms": round(f0, 3), "fwd_recording_ms": round(f1, 3), "bwd_ms": round(bw, 3),
+        "fwd_plus_bwd_ms": round(f1 + bw, 3), "ratio_vs_fwd": round((f1 + bw) / f0, 3),
+        "same_final_state": bool(np.array_equal(p0, p)), "grad_norm": float(np.linalg.norm(gv)),
+        "status": sim.last_status,
+    }
+
+
+def batch_cpu_baseline(sample=1024, steps=5):
+    """The plain-C CPU restatement stepping a sample of the batched worlds, one world per
+    task on all host cores (worlds are independent)."""
+    from concurrent.futures import ThreadPoolExecutor
+    subprocess.run(["make", "-s", "-j8", "-f", "oracle/Makefile"], cwd=REPO, check=True, capture_output=True)
+    from box2c_gb300.capi import Backend
+    ob = os.path.join(REPO, "oracle", "_build")
+    o = Backend(os.path.join(ob, "liboracle.so"), os.path.join(ob, "liboracle_scenes.so"), "oracle")
+    worlds = [o.pyramid(int(b), 0.0, 0) for b in batch_bases()[:sample]]
+    cores = os.cpu_count() or 1
+    with ThreadPoolExecutor(max_workers=cores) as ex:
+        list(ex.map(lambda w: o.step(w, DT, SUBSTEPS, count=2), worlds))
+        t0 = time.perf_counter()
+        list(ex.map(lambda w: o.step(w, DT, SUBSTEPS, count=steps), worlds))
+        dt = time.perf_counter() - t0
+    for w in worlds:
+        o.destroy(w)
+    return {"value": round(len(worlds) * steps / dt, 1), "unit": "world-steps/s", "cores": cores, "kind": "port",
+            "sample": f"{len(worlds)} of the 4096 worlds x {steps} steps after 2 warm-up steps, one world per task"}
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -243,9 +368,14 @@ def run_gpu(args):
     toi = L.b2World_GetUnsupportedToiCount(w)
     g.destroy(w)
 
+    batch = run_batch(g, args.batch_steps, 5) if args.batch_steps > 0 else None
+    adjoint = run_adjoint(g) if not args.no_adjoint else None
+
     if rank != 0:
         return
     cpu_ms, cpu_n = cpu_baseline() if not args.no_cpu else (None, 0)
+    if batch is not None and not args.no_cpu:
+        batch["cpu_baseline"] = batch_cpu_baseline()
     clocks = sampler.summary()
     line = {
         "metric": METRIC, "value": round(ms, 4), "unit": "ms/step", "n_gpus": world_size, "steps": args.steps,
@@ -272,6 +402,8 @@ def run_gpu(args):
                           "sample": f"{cpu_n} steps of the same 100-row pyramid after 2 warm-up steps"}
                          if cpu_ms is not None else None),
         "clocks": clocks, "status": status, "unsupported_toi": toi,
+        "batched": batch,
+        "differentiable": adjoint,
     }
     print(json.dumps(line))
 
@@ -283,6 +415,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--batch-steps", type=int, default=30, help="batched-worlds steps to time (0: skip)")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the differentiable-stepping measurement")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

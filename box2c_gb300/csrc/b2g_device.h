@@ -115,6 +115,63 @@ void b2gd_batch_stats( b2gBatch* b, float* collideMs, float* solveMs, int* threa
 /* Copies a world's staged contact records to the device on the world's stream. */
 int b2gd_stage_contacts( b2gDevWorld* w, b2gHostIO* io, int count );
 
+/* ---------------------------------------------------------------- step adjoint */
+/* One solver row as recorded for the adjoint: the contact, its bodies (-1 static) and
+ * shapes, mixed material and the manifold the solver stage starts from. */
+typedef struct b2gTapeRow
+{
+	int32_t cid, ia, ib, shapeA, shapeB, pad;
+	float friction, restitution;
+	b2gManifold m;
+	float pad2[1];
+} b2gTapeRow;
+
+/* One recorded step: where its body and row records are in the world's tape, the
+ * solve plan and the step constants. */
+typedef struct b2gTapeStep
+{
+	int64_t bodyOff, rowOff; /* float4 offsets of the body records, b2gTapeRow offsets */
+	int32_t bodies, rows, solve, pad;
+	int32_t colorStart[B2G_COLORS + 1];
+	int32_t jointStart[B2G_COLORS + 1];
+	int32_t active[B2G_COLORS];
+	int32_t activeCount, awakeCount;
+	b2gStepConst sc;
+} b2gTapeStep;
+
+/* Body record: 4 float4 per body id: v.x v.y w tag | p.x p.y q.c q.s |
+ * c.x c.y lc.x lc.y | awake 0 0 0. */
+#define B2G_TAPE_BODY_FLOAT4 4
+
+/* Records one step's solver inputs into the tape (world stream). */
+int b2gd_tape_record( b2gDevWorld* w, void* bodyDst, int bodies, void* rowDst, int rows );
+
+/* One world of a backward pass. */
+typedef struct b2gAdjointItem
+{
+	b2gDevWorld W;			   /* geometry, mass, forces, damping of the world */
+	const float* tapeBodies;   /* tape base (4 floats per float4 unit) */
+	const b2gTapeRow* tapeRows; /* tape rows base */
+	const b2gTapeStep* steps;  /* device copy of the step headers */
+	int stepCount;
+	int bodies;				   /* body ids (constant over the tape) */
+	int shapes;
+	int maxRows;
+	int contactCap;
+	int pad;
+	const float* shapeFriction; /* per shape id */
+	const float* gradFinal;		/* 6 per body id: p.x p.y angle v.x v.y w */
+	float* gradInitial;			/* 6 per body id */
+	float* gradFriction;		/* per shape id */
+	float* scratch;
+	int* status; /* [0] unsupported rows, [1] manifold replay mismatches */
+} b2gAdjointItem;
+
+/* Scratch floats one world needs for a backward pass. */
+size_t b2gd_adjoint_scratch( int bodies, int maxRows, int contactCap, int subSteps );
+/* Runs the backward pass of `count` worlds (device item array, one CTA each). */
+int b2gd_adjoint_launch( const b2gAdjointItem* dItems, int count, void* stream );
+
 /* Device time of the last step's stages in milliseconds (CUDA events recorded when
  * w->timing is set). */
 void b2gd_enable_timing( b2gDevWorld* w, int flag );

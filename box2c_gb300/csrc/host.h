@@ -279,6 +279,7 @@ typedef struct gWorld
 	int lastEventCount, lastRecordCount;
 	double stepStart; /* host clock at the start of the current step phase */
 	int stepIdCount;  /* contact ids of the current step's narrowphase */
+	struct gTape* tape; /* recording for b2World_StepBackward, or null */
 
 	b2gDevWorld dev;
 	b2gHostIO io;
@@ -308,6 +309,11 @@ int gpool_threads( void );
 void gstep_rebuild_trees( gWorld* w );
 int gstep_after_collide( gWorld* w, float dt, int subSteps, b2gStepConst* sc, b2gSolvePlan* plan );
 void gstep_finish( gWorld* w );
+
+/* Adjoint tape (adjoint.c): records the solver inputs of the current step when the
+ * world is recording; frees a world's tape. */
+void gtape_record( gWorld* w, const b2gSolvePlan* plan, const b2gStepConst* sc, int solve );
+void gtape_free( gWorld* w );
 void gcontact_create( gWorld* w, gShape* a, gShape* b );
 void gcontact_destroy( gWorld* w, gContact* c );
 int gassign_joint_color( gWorld* w, int bodyIdA, int bodyIdB, bool staticA, bool staticB );

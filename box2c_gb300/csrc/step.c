@@ -716,7 +716,11 @@ int gstep_after_collide( gWorld* w, float dt, int subSteps, b2gStepConst* sc, b2
 	sc->enableSleep = w->enableSleep;
 
 	if ( w->awake.count == 0 )
+	{
+		if ( w->tape )
+			gtape_record( w, NULL, sc, 0 );
 		return 0;
+	}
 
 	build_solve_lists( w, plan );
 	plan->awakeCount = w->awake.count;
@@ -731,6 +735,8 @@ int gstep_after_collide( gWorld* w, float dt, int subSteps, b2gStepConst* sc, b2
 		}
 		w->solveUploaded = true;
 	}
+	if ( w->tape )
+		gtape_record( w, plan, sc, 1 );
 	return 1;
 }
 

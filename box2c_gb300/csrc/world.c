@@ -350,6 +350,7 @@ b2WorldId b2CreateWorld( const b2WorldDef* def )
 void b2DestroyWorld( b2WorldId worldId )
 {
 	gWorld* w = gworld_get( worldId );
+	gtape_free( w );
 	b2gd_free( &w->dev, &w->io );
 	for ( int i = 0; i < 3; ++i )
 		gtree_free( w->trees + i );

@@ -71,6 +71,39 @@ typedef struct b2BatchStats
 
 B2_API b2BatchStats b2World_GetBatchStats( void );
 
+/* Differentiable stepping.  b2World_BeginTape starts recording the world's next
+ * maxSteps steps (0 stops and frees the recording); each recorded step keeps the
+ * solver inputs of that step on the device.  b2World_StepBackward then returns the
+ * gradient of a scalar loss L through all recorded steps, by a hand-written adjoint of
+ * the substepped soft-step solver (reverse colour order, each step recomputed from its
+ * record).  States are 6 floats per body id: p.x p.y angle v.x v.y w.
+ *   gradFinal     dL/d(state after the last recorded step)      (6 x bodies)
+ *   gradInitial   dL/d(state before the first recorded step)    (6 x bodies, out)
+ *   gradFriction  dL/d(shape friction) per shape id             (shapes, out, may be null)
+ * The discrete choices of each step (pairs, colours, contact features, active clamps)
+ * are those of the recorded steps.  Supported: polygon, capsule and segment shapes
+ * without joints or overflow-colour constraints; otherwise B2_ADJOINT_UNSUPPORTED.
+ * B2_ADJOINT_REPLAY_MISMATCH reports that the recomputed contact geometry differed from
+ * the recorded one (the world changed after recording).  No counterpart in the
+ * reference API. */
+#define B2_ADJOINT_UNSUPPORTED ( -3 )
+#define B2_ADJOINT_REPLAY_MISMATCH ( -4 )
+
+B2_API void b2World_BeginTape( b2WorldId worldId, int maxSteps );
+B2_API int b2World_GetTapeSteps( b2WorldId worldId );
+B2_API int b2World_StepBackward( b2WorldId worldId, const float* gradFinal, float* gradInitial, float* gradFriction );
+
+/* The backward pass of `count` recorded worlds in one launch (one warp per world).
+ * Arrays are per world with fixed strides: gradFinal / gradInitial 6 * bodyStride
+ * floats per world, gradFriction shapeStride floats per world. */
+B2_API int b2World_StepBackwardBatch( const b2WorldId* worldIds, int count, int bodyStride, int shapeStride, const float* gradFinal,
+									  float* gradInitial, float* gradFriction );
+
+/* Self-check of the last backward call: recorded manifolds the backward pass did not
+ * reproduce, and replayed steps that did not end bit for bit where the next recorded
+ * step starts (both 0 when the adjoint differentiated exactly the recorded steps). */
+B2_API void b2World_GetBackwardCheck( int* manifoldMismatches, int* replayMismatches );
+
 /* Copies p.x p.y q.c q.s v.x v.y w (7 floats) of every body id into out (7 * capacity
  * floats).  One device-to-host copy per call.  Returns the number of body ids. */
 B2_API int b2World_GetBodyStates( b2WorldId worldId, float* out, int capacity );

@@ -1,0 +1,156 @@
+"""Differentiable stepping (b2World_BeginTape / b2World_StepBackwardBatch) on the
+drop-boxes workload: boxes of half-extent 0.5 dropped from U(1,5) m with N(0,1) initial
+velocities and a per-world friction U(0.2,0.9); loss = sum of squared final positions.
+
+The reference for the gradient is the FP64 CPU restatement of the same step (oracle
+built with -DB2O_F64) under central finite differences.  The soft-step dynamics are
+piecewise smooth (contact clamps, speculative vs soft bias, reference-face choice), so a
+finite difference is a valid reference only where it is stable across step sizes; the
+tests compare wherever it is (eps 1e-5 vs 1e-6 within 1e-4 relative) with tolerance
+1e-3 relative, and require at least half of the worlds to qualify at 30 steps.  Worlds
+whose boxes collide and tip have loss landscapes that are not smooth at the 1e-5 scale;
+there no finite difference (and no gradient) is a meaningful reference.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from box2c_gb300.capi import WorldId
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-3
+STABLE = 1e-4
+
+
+@pytest.fixture(scope="module")
+def fd64(oracle64):
+    L = oracle64.lib
+    L.b2o_GetBodyStateF64.argtypes = [WorldId, C.c_void_p, C.c_int]
+    L.b2o_SetBodyVelocityF64.argtypes = [WorldId, C.c_int, C.c_double, C.c_double, C.c_double]
+    L.b2o_SetShapeFrictionF64.argtypes = [WorldId, C.c_int, C.c_double]
+
+    def loss(h, v0, mu, steps):
+        w = oracle64.drop_boxes(h, v0[:, 0].astype(np.float32), v0[:, 1].astype(np.float32), float(mu))
+        for k in range(len(h)):
+            L.b2o_SetBodyVelocityF64(w, k + 1, float(v0[k, 0]), float(v0[k, 1]), 0.0)
+        for s in range(len(h) + 1):
+            L.b2o_SetShapeFrictionF64(w, s, float(mu))
+        oracle64.step(w, count=steps)
+        st = np.zeros(7 * (len(h) + 1))
+        L.b2o_GetBodyStateF64(w, st.ctypes.data, len(h) + 1)
+        oracle64.destroy(w)
+        p = st.reshape(-1, 7)[1:, :2]
+        return float((p ** 2).sum())
+
+    def grad(h, v0, mu, steps, eps):
+        v = v0.astype(np.float64)
+        g = np.zeros(v.size + 1)
+        for i in range(v.size):
+            vp, vm = v.copy(), v.copy()
+            vp.flat[i] += eps
+            vm.flat[i] -= eps
+            g[i] = (loss(h, vp, mu, steps) - loss(h, vm, mu, steps)) / (2 * eps)
+        g[-1] = (loss(h, v, float(mu) + eps, steps) - loss(h, v, float(mu) - eps, steps)) / (2 * eps)
+        return g
+
+    return grad
+
+
+def _scene(n, boxes=8, seed=1238):
+    rng = np.random.default_rng(seed)
+    heights = rng.uniform(1, 5, size=(n, boxes)).astype(np.float32)
+    v0 = rng.normal(0, 1, size=(n, boxes, 2)).astype(np.float32)
+    mu = rng.uniform(0.2, 0.9, size=n).astype(np.float32)
+    return heights, v0, mu
+
+
+def _adjoint(gpu, heights, v0, mu, steps):
+    from box2c_gb300.autograd import DropBoxes
+    sim = DropBoxes(gpu, heights, steps=steps)
+    p = sim.run(v0, mu)
+    gv, gm = sim.backward(2.0 * p)
+    manifold, replay = C.c_int(), C.c_int()
+    gpu.lib.b2World_GetBackwardCheck(C.byref(manifold), C.byref(replay))
+    sim.destroy()
+    assert manifold.value == 0 and replay.value == 0, "the backward pass did not replay the recorded steps exactly"
+    return np.concatenate([gv.reshape(len(mu), -1), gm[:, None]], axis=1)
+
+
+def _compare(gpu, fd64, n, steps, seed=1238):
+    heights, v0, mu = _scene(n, seed=seed)
+    ga = _adjoint(gpu, heights, v0, mu, steps)
+    stable, errs = 0, []
+    for w in range(n):
+        f6 = fd64(heights[w], v0[w], mu[w], steps, 1e-6)
+        f5 = fd64(heights[w], v0[w], mu[w], steps, 1e-5)
+        if np.linalg.norm(f5 - f6) > STABLE * np.linalg.norm(f6):
+            continue
+        stable += 1
+        errs.append(np.linalg.norm(ga[w] - f6) / np.linalg.norm(f6))
+    return stable, errs
+
+
+def test_free_flight_gradient_is_exact(gpu, fd64):
+    heights, v0, mu = _scene(2, seed=7)
+    heights[:] = 4.5  # no contact within 10 steps
+    ga = _adjoint(gpu, heights, v0, mu, 10)
+    for w in range(2):
+        f = fd64(heights[w], v0[w], mu[w], 10, 1e-6)
+        assert np.linalg.norm(ga[w] - f) <= 1e-5 * np.linalg.norm(f)
+
+
+def test_gradient_matches_fp64_derivative_30_steps(gpu, fd64):
+    stable, errs = _compare(gpu, fd64, 6, 30)
+    assert stable >= 3, f"only {stable} of 6 worlds have a stable finite difference"
+    assert max(errs) <= TOL, f"relative gradient errors {errs}"
+
+
+def test_gradient_matches_fp64_derivative_120_steps(gpu, fd64):
+    stable, errs = _compare(gpu, fd64, 16, 120)
+    assert stable >= 1, "no world with a stable finite difference at 120 steps"
+    assert max(errs) <= TOL, f"relative gradient errors {errs}"
+
+
+def test_autograd_function_matches_direct_call(gpu):
+    torch = pytest.importorskip("torch")
+    from box2c_gb300.autograd import DropBoxes, drop_boxes_loss
+    heights, v0, mu = _scene(3, seed=11)
+    sim = DropBoxes(gpu, heights, steps=40)
+    tv = torch.tensor(v0, requires_grad=True)
+    tm = torch.tensor(mu, requires_grad=True)
+    loss = drop_boxes_loss(sim, tv, tm)
+    loss.backward()
+    sim.destroy()
+    direct = _adjoint(gpu, heights, v0, mu, 40)
+    assert np.allclose(tv.grad.numpy().reshape(3, -1), direct[:, :-1], rtol=0, atol=0)
+    assert np.allclose(tm.grad.numpy(), direct[:, -1], rtol=0, atol=0)
+
+
+def test_joints_are_reported_unsupported(gpu):
+    from box2c_gb300.autograd import bind_adjoint_api
+    from box2c_gb300.capi import bind_gpu_api
+    bind_gpu_api(gpu.lib)
+    bind_adjoint_api(gpu.lib)
+    w = gpu.tumbler(40, 3, 0)
+    gpu.lib.b2World_BeginTape(w, 5)
+    gpu.step(w, count=5)
+    n = gpu.lib.b2World_GetBodyStates(w, None, 0)
+    gf = np.zeros(6 * n, np.float32)
+    gi = np.zeros_like(gf)
+    rc = gpu.lib.b2World_StepBackward(w, gf.ctypes.data, gi.ctypes.data, None)
+    gpu.destroy(w)
+    assert rc == -3  # B2_ADJOINT_UNSUPPORTED
+
+
+def test_backward_without_tape_is_rejected(gpu):
+    from box2c_gb300.autograd import bind_adjoint_api
+    bind_adjoint_api(gpu.lib)
+    w = gpu.pyramid(4)
+    gpu.step(w, count=2)
+    gf = np.zeros(6 * 16, np.float32)
+    gi = np.zeros_like(gf)
+    rc = gpu.lib.b2World_StepBackward(w, gf.ctypes.data, gi.ctypes.data, None)
+    gpu.destroy(w)
+    assert rc == -1
