@@ -134,11 +134,21 @@ void gtape_record( gWorld* w, const b2gSolvePlan* plan, const b2gStepConst* sc, 
 		h->activeCount = plan->activeCount;
 		h->awakeCount = plan->awakeCount;
 	}
-	int e = b2gd_tape_record( &w->dev, t->dev + bodyByte, bodies, t->dev + rowByte, rows );
-	if ( e )
+	if ( w->batching )
 	{
-		w->status = e;
-		return;
+		/* recorded by the batch's solver graph */
+		w->tapeBodyDst = t->dev + bodyByte;
+		w->tapeRowDst = t->dev + rowByte;
+		w->tapeRowCount = rows;
+	}
+	else
+	{
+		int e = b2gd_tape_record( &w->dev, t->dev + bodyByte, bodies, t->dev + rowByte, rows );
+		if ( e )
+		{
+			w->status = e;
+			return;
+		}
 	}
 	t->used = end;
 	t->maxRows = rows > t->maxRows ? rows : t->maxRows;

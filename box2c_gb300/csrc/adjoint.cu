@@ -36,34 +36,7 @@
 /* ------------------------------------------------------------------ recording */
 __global__ void k_tape_record( b2gDevWorld W, float4* bodies, int bodyCount, b2gTapeRow* rows, int rowCount )
 {
-	int t = blockIdx.x * blockDim.x + threadIdx.x;
-	if ( t < bodyCount )
-	{
-		const float4* st = (const float4*)W.state;
-		float4 f = ( (const float4*)W.force )[t];
-		float awake = ( W.bodyInfo[t] & B2G_B_AWAKE ) ? 1.0f : 0.0f;
-		float4* o = bodies + B2G_TAPE_BODY_FLOAT4 * t;
-		o[0] = st[2 * t];
-		o[1] = ( (const float4*)W.xf )[t];
-		o[2] = ( (const float4*)W.centers )[t];
-		o[3] = make_float4( awake, f.x, f.y, f.z );
-	}
-	if ( t < rowCount )
-	{
-		int cid = W.solveList[t];
-		b2gTapeRow r;
-		r.cid = cid;
-		r.ia = W.cBodies[2 * cid];
-		r.ib = W.cBodies[2 * cid + 1];
-		r.shapeA = W.cShapes[2 * cid];
-		r.shapeB = W.cShapes[2 * cid + 1];
-		r.pad = 0;
-		r.friction = W.cMix[2 * cid];
-		r.restitution = W.cMix[2 * cid + 1];
-		r.m = W.manifold[cid];
-		r.pad2[0] = 0.0f;
-		rows[t] = r;
-	}
+	tape_record_one( W, bodies, bodyCount, rows, rowCount, blockIdx.x * blockDim.x + threadIdx.x );
 }
 
 extern "C" int b2gd_tape_record( b2gDevWorld* w, void* bodyDst, int bodies, void* rowDst, int rows )

@@ -91,6 +91,9 @@ typedef struct b2gBatchItem
 	int idCount; /* contact ids run through the narrowphase */
 	int staged;	 /* staged contact records */
 	int solve;	 /* 1 when the solver stage runs */
+	int tapeRows;	  /* rows recorded for the adjoint this step */
+	void* tapeBodies; /* adjoint tape destinations, or null when not recording */
+	void* tapeRowDst;
 } b2gBatchItem;
 
 /* Device context of batched steps: pinned staging of items and counters, device copies,

@@ -573,3 +573,37 @@ static __device__ void finalize_body( const b2gDevWorld& W, int i, const b2gStep
 	}
 }
 
+/* Adjoint tape record of one step (item t of max(bodies, rows)): body state, transform,
+ * centre, awake flag and applied force per body id; the solver rows with their input
+ * manifolds. */
+static __device__ __forceinline__ void tape_record_one( const b2gDevWorld& W, float4* bodies, int bodyCount, b2gTapeRow* rows, int rowCount,
+														int t )
+{
+	if ( t < bodyCount )
+	{
+		const float4* st = (const float4*)W.state;
+		float4 f = ( (const float4*)W.force )[t];
+		float awake = ( W.bodyInfo[t] & B2G_B_AWAKE ) ? 1.0f : 0.0f;
+		float4* o = bodies + B2G_TAPE_BODY_FLOAT4 * t;
+		o[0] = st[2 * t];
+		o[1] = ( (const float4*)W.xf )[t];
+		o[2] = ( (const float4*)W.centers )[t];
+		o[3] = make_float4( awake, f.x, f.y, f.z );
+	}
+	if ( t < rowCount )
+	{
+		int cid = W.solveList[t];
+		b2gTapeRow r;
+		r.cid = cid;
+		r.ia = W.cBodies[2 * cid];
+		r.ib = W.cBodies[2 * cid + 1];
+		r.shapeA = W.cShapes[2 * cid];
+		r.shapeB = W.cShapes[2 * cid + 1];
+		r.pad = 0;
+		r.friction = W.cMix[2 * cid];
+		r.restitution = W.cMix[2 * cid + 1];
+		r.m = W.manifold[cid];
+		r.pad2[0] = 0.0f;
+		rows[t] = r;
+	}
+}

@@ -65,6 +65,8 @@ static void begin_worlds( int begin, int end, void* arg )
 		memset( &w->profile, 0, sizeof( w->profile ) );
 		s_streams[k] = w->dev.stream;
 		w->dev.stream = c->stream;
+		w->batching = true;
+		w->tapeBodyDst = NULL;
 		gworld_flush( w );
 		int staged = gstep_begin( w );
 		if ( staged < 0 )
@@ -118,6 +120,13 @@ static void middle_worlds( int begin, int end, void* arg )
 		it->activeCount = plan.activeCount;
 		it->awakeCount = plan.awakeCount;
 		it->bodyIdCount = plan.bodyIdCount;
+		if ( w->tapeBodyDst )
+		{
+			it->tapeBodies = w->tapeBodyDst;
+			it->tapeRowDst = w->tapeRowDst;
+			it->tapeRows = w->tapeRowCount;
+			w->tapeBodyDst = NULL;
+		}
 	}
 }
 
@@ -135,6 +144,7 @@ static void finish_worlds( int begin, int end, void* arg )
 			gstep_finish( w );
 		}
 		w->dev.stream = s_streams[k];
+		w->batching = false;
 		w->dev.launches = 0;
 		w->dev.fusedUsed = 0;
 		w->mirrorStale = true;

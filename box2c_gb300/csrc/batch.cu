@@ -94,6 +94,20 @@ __global__ void __launch_bounds__( BATCH_GRID_THREADS ) k_batch_collide( const b
 	}
 }
 
+/* Adjoint tape records of the worlds that are recording (one CTA per world in turn). */
+__global__ void __launch_bounds__( BATCH_GRID_THREADS ) k_batch_tape( const b2gBatchItem* items, int n )
+{
+	for ( int w = blockIdx.x; w < n; w += gridDim.x )
+	{
+		const b2gBatchItem& it = items[w];
+		if ( it.tapeBodies == nullptr || it.solve == 0 )
+			continue;
+		int count = it.bodyIdCount > it.tapeRows ? it.bodyIdCount : it.tapeRows;
+		for ( int t = threadIdx.x; t < count; t += blockDim.x )
+			tape_record_one( it.W, (float4*)it.tapeBodies, it.bodyIdCount, (b2gTapeRow*)it.tapeRowDst, it.tapeRows, t );
+	}
+}
+
 /* One stage over all colours of one world (overflow first, serially), the CTA's
  * threads sharing each colour, a CTA barrier after each. */
 template <int T>
@@ -479,6 +493,7 @@ extern "C" int b2gd_batch_solve( b2gBatch* b, int n )
 		cudaMemcpyAsync( b->dItems, b->hItems, sizeof( b2gBatchItem ) * n, cudaMemcpyHostToDevice, b->stream );
 		cudaMemcpyAsync( b->dOrder, b->hOrder, sizeof( int ) * ( n + 1 ), cudaMemcpyHostToDevice, b->stream );
 		cudaMemsetAsync( b->dQueue, 0, sizeof( int ), b->stream );
+		k_batch_tape<<<b->sms * 4, BATCH_GRID_THREADS, 0, b->stream>>>( b->dItems, n );
 		if ( T == 64 )
 			launch_solve<64>( b, smem, grid );
 		else if ( T == 128 )
@@ -501,7 +516,7 @@ extern "C" int b2gd_batch_solve( b2gBatch* b, int n )
 	cudaEventRecord( b->ev[3], b->stream );
 	b->choice = choice;
 	b->solveTimed = 1;
-	b->launches += 1;
+	b->launches += 2; /* tape records, solver */
 	return (int)e;
 }
 

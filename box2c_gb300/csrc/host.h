@@ -280,6 +280,10 @@ typedef struct gWorld
 	double stepStart; /* host clock at the start of the current step phase */
 	int stepIdCount;  /* contact ids of the current step's narrowphase */
 	struct gTape* tape; /* recording for b2World_StepBackward, or null */
+	bool batching;		/* inside b2World_StepBatch: tape records go into the batch's graph */
+	void* tapeBodyDst;	/* this step's tape destinations while batching */
+	void* tapeRowDst;
+	int tapeRowCount;
 
 	b2gDevWorld dev;
 	b2gHostIO io;
