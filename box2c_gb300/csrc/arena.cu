@@ -33,13 +33,15 @@ extern "C" int b2gd_device_ok( void )
 	return n > 0;
 }
 
-/* Reallocates a device array from oldBytes to newBytes keeping the prefix. */
+/* Reallocates a device array from oldBytes to newBytes keeping the prefix.  Stream
+ * ordered (the device's default memory pool): no host synchronisation, so growing the
+ * arenas of many worlds in one batched step does not serialise on the host. */
 static int grow( void** ptr, size_t oldBytes, size_t newBytes, cudaStream_t s )
 {
 	if ( newBytes <= oldBytes && *ptr != nullptr )
 		return 0;
 	void* p = nullptr;
-	int e = ok( cudaMalloc( &p, newBytes ) );
+	int e = ok( cudaMallocAsync( &p, newBytes, s ) );
 	if ( e )
 		return e;
 	cudaMemsetAsync( p, 0, newBytes, s );
@@ -47,8 +49,7 @@ static int grow( void** ptr, size_t oldBytes, size_t newBytes, cudaStream_t s )
 	{
 		if ( oldBytes > 0 )
 			cudaMemcpyAsync( p, *ptr, oldBytes, cudaMemcpyDeviceToDevice, s );
-		cudaStreamSynchronize( s );
-		cudaFree( *ptr );
+		cudaFreeAsync( *ptr, s );
 	}
 	*ptr = p;
 	return 0;
@@ -77,21 +78,25 @@ extern "C" int b2gd_init( b2gDevWorld* w, b2gHostIO* io )
 		return e;
 	w->stream = (void*)s;
 	w->fused = 1;
-	e = ok( cudaMalloc( (void**)&w->counters, 4 * sizeof( int ) ) );
+	e = ok( cudaMallocAsync( (void**)&w->counters, 4 * sizeof( int ), s ) );
 	if ( e )
 		return e;
 	e = ok( cudaHostAlloc( (void**)&io->counters, 4 * sizeof( int ), cudaHostAllocDefault ) );
 	if ( e )
 		return e;
 	memset( io->counters, 0, 4 * sizeof( int ) );
-	return ok( cudaMemsetAsync( w->counters, 0, 4 * sizeof( int ), s ) );
+	e = ok( cudaMemsetAsync( w->counters, 0, 4 * sizeof( int ), s ) );
+	if ( e )
+		return e;
+	/* room for small worlds from the start, so that their first steps allocate nothing */
+	return b2gd_reserve( w, io, 32, 32, 128, 4, 128, 32 );
 }
 
 #define FREE_DEV( p )                                                                                                            \
 	do                                                                                                                           \
 	{                                                                                                                            \
 		if ( p )                                                                                                                 \
-			cudaFree( (void*)( p ) );                                                                                            \
+			cudaFreeAsync( (void*)( p ), (cudaStream_t)w->stream );                                                              \
 		p = nullptr;                                                                                                             \
 	}                                                                                                                            \
 	while ( 0 )
@@ -243,9 +248,8 @@ extern "C" int b2gd_reserve( b2gDevWorld* w, b2gHostIO* io, int bodyCap, int sha
 		w->jointCap = nc;
 	}
 	(void)listCap;
-	/* new arrays are cleared and filled on the stream: finish before the host uses them */
-	if ( e == 0 )
-		e = ok( cudaStreamSynchronize( s ) );
+	/* new arrays are cleared and filled in stream order; the host reads device arrays
+	 * only through copies on the same stream */
 	return e;
 }
 
