@@ -94,6 +94,8 @@ typedef struct b2gBatchItem
 	int tapeRows;	  /* rows recorded for the adjoint this step */
 	void* tapeBodies; /* adjoint tape destinations, or null when not recording */
 	void* tapeRowDst;
+	int rowsOnChip; /* 1 when the solver keeps this world's rows in shared memory (set at launch) */
+	int pad;
 } b2gBatchItem;
 
 /* Device context of batched steps: pinned staging of items and counters, device copies,

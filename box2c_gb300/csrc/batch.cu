@@ -5,17 +5,21 @@
  * contact ids of all worlds (a flat index finds its world by binary search over the
  * prefix sums).  Solver: one persistent kernel; each CTA takes the next world from a
  * queue (largest first) and runs that world's whole solver stage and finalisation with
- * __syncthreads between the dependent phases: body states in shared memory, constraint
- * rows in the world's own row arrays (they stay in L2 while the CTA works on them).
- * The per-item work is b2g_stages.h's, the same functions the single-world kernels use,
- * so every world gets the bits it would get from b2World_Step alone.
+ * __syncthreads between the dependent phases.  Body states always live in shared
+ * memory; a world whose constraint rows fit beside them keeps the rows there too, a
+ * larger one in its own row arrays (they stay in L2 while the CTA works on them).  The
+ * per-row work is b2g_stages.h's and b2g_cluster.h's, the same functions the
+ * single-world kernels use, so every world gets the bits it would get from
+ * b2World_Step alone.
  *
  * Each device segment (uploads, kernels, counter download) is captured once as a CUDA
  * graph and replayed every step; the kernels read their counts from device memory, so
  * the graphs do not change while the number of worlds and the shared-memory size stay
- * the same.  The solver's CTA size is chosen by timing the candidates on the first
- * steps (any choice gives the same results).
+ * the same.  The solver's launch shape (threads per CTA, CTAs per SM and so shared
+ * memory per world) is chosen by timing the candidates on the first steps (any choice
+ * gives the same results).
  */
+#include "b2g_cluster.h"
 #include "b2g_stages.h"
 
 #include <cuda_runtime.h>
@@ -24,10 +28,10 @@
 #include <string.h>
 
 #define BATCH_GRID_THREADS 256
-#define TUNE_CANDIDATES 3
+#define TUNE_CANDIDATES 6
 #define TUNE_SAMPLES 2
-
-static const int s_tuneThreads[TUNE_CANDIDATES] = { 64, 128, 256 };
+#define SM_SHARED_BYTES ( 228u * 1024u ) /* shared memory of one SM */
+#define CTA_SHARED_MAX ( 226u * 1024u )	 /* dynamic shared memory one CTA may take here */
 
 struct b2gBatch
 {
@@ -108,44 +112,94 @@ __global__ void __launch_bounds__( BATCH_GRID_THREADS ) k_batch_tape( const b2gB
 	}
 }
 
+/* Shared-memory image of one world on its solver CTA: body states (two float4) by
+ * body id; after them, for a world that fits, its constraint rows by solve-list
+ * position (nine float4 each).  Velocity terms are recomputed every substep from the
+ * body's mass, force and extent rather than held, which keeps the image small. */
+__host__ __device__ inline int body_float4s( int bodies ) { return 2 * bodies; }
+__host__ __device__ inline size_t world_smem_bytes( int bodies, int rows )
+{
+	return 16u * (size_t)body_float4s( bodies ) + 144u * (size_t)rows;
+}
+
+struct WorldImage
+{
+	SharedBodies B;
+	SmemRows m;
+};
+
+/* Asks L2 for rows [first, first + n) of the world's row arrays: one bulk prefetch per
+ * array, nothing to wait for. */
+__device__ __forceinline__ void prefetch_rows( const b2gDevWorld& W, int first, int n )
+{
+	const void* arrays[10] = { W.kIdx, W.kNF, W.kSoft, W.kMass, W.kAnchor[0], W.kAnchor[1], W.kCoef[0], W.kCoef[1], W.kImp[0], W.kImp[1] };
+	unsigned bytes = 16u * (unsigned)n;
+	for ( int i = 0; i < 10; ++i )
+	{
+		const char* p = (const char*)arrays[i] + 16u * (size_t)first;
+		asm volatile( "cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"( p ), "r"( bytes ) : "memory" );
+	}
+}
+
+/* One row phase: the row in shared memory (ONCHIP) or in the world's row arrays. */
+template <bool ONCHIP>
+__device__ __forceinline__ void world_row( const b2gDevWorld& W, const WorldImage& s, int k, int phase, bool scalar,
+										   const b2gStepConst& sc )
+{
+	if constexpr ( ONCHIP )
+		row_step( s.m, s.B, k, phase, scalar, sc );
+	else
+		row_work( W, s.B, k, phase, scalar, sc );
+}
+
 /* One stage over all colours of one world (overflow first, serially), the CTA's
  * threads sharing each colour, a CTA barrier after each. */
-template <int T>
-__device__ void world_stage( const b2gBatchItem& it, const SharedBodies& B, int phase, const b2gStepConst& sc )
+template <int T, bool ONCHIP>
+__device__ void world_stage( const b2gBatchItem& it, const WorldImage& s, int phase, const b2gStepConst& sc )
 {
 	const b2gDevWorld& W = it.W;
 	const int* cs = it.colorStart;
 	const int* js = it.jointStart;
 	int ovRows = cs[B2G_COLORS] - cs[B2G_OVERFLOW];
 	int ovJointsAll = js[B2G_COLORS] - js[B2G_OVERFLOW];
-	bool overflow = phase == 3 ? ovRows > 0 : ovRows + ovJointsAll > 0;
+	bool overflow = phase == F_RESTITUTION ? ovRows > 0 : ovRows + ovJointsAll > 0;
 	if ( overflow )
 	{
 		if ( threadIdx.x == 0 )
 		{
-			if ( phase != 3 )
+			if ( phase != F_RESTITUTION )
 				for ( int i = 0; i < ovJointsAll; ++i )
-					joint_work( W, B, W.jointList[js[B2G_OVERFLOW] + i], phase, sc );
+					joint_work( W, s.B, W.jointList[js[B2G_OVERFLOW] + i], phase, sc );
 			for ( int i = 0; i < ovRows; ++i )
-				row_work( W, B, cs[B2G_OVERFLOW] + i, phase, true, sc );
+				world_row<ONCHIP>( W, s, cs[B2G_OVERFLOW] + i, phase, true, sc );
 		}
 		__syncthreads();
 	}
-	if ( phase == 0 && sc.enableWarmStarting == 0 )
+	if ( phase == F_WARM && sc.enableWarmStarting == 0 )
 		return;
 	for ( int a = 0; a < it.activeCount; ++a )
 	{
 		int c = it.active[a];
 		int nr = cs[c + 1] - cs[c];
-		int nj = phase == 3 ? 0 : js[c + 1] - js[c];
-		if ( phase == 3 && nr == 0 )
+		int nj = phase == F_RESTITUTION ? 0 : js[c + 1] - js[c];
+		if ( phase == F_RESTITUTION && nr == 0 )
 			continue;
+		if constexpr ( ONCHIP == false )
+		{
+			/* the colour after this one (the next stage starts again at the first) */
+			if ( threadIdx.x == T - 1 )
+			{
+				int cn = it.active[a + 1 < it.activeCount ? a + 1 : 0];
+				if ( cs[cn + 1] > cs[cn] )
+					prefetch_rows( W, cs[cn], cs[cn + 1] - cs[cn] );
+			}
+		}
 		for ( int t = threadIdx.x; t < nj + nr; t += T )
 		{
 			if ( t < nj )
-				joint_work( W, B, W.jointList[js[c] + t], phase, sc );
+				joint_work( W, s.B, W.jointList[js[c] + t], phase, sc );
 			else
-				row_work( W, B, cs[c] + t - nj, phase, false, sc );
+				world_row<ONCHIP>( W, s, cs[c] + t - nj, phase, false, sc );
 		}
 		__syncthreads();
 	}
@@ -153,18 +207,30 @@ __device__ void world_stage( const b2gBatchItem& it, const SharedBodies& B, int 
 
 /* The solver stage and finalisation of one world by one CTA (reference src/solver.c
  * stage order: prepare, substeps of integrate velocities / warm start / solve /
- * integrate positions / relax, restitution, store impulses, finalize bodies). */
-template <int T>
+ * integrate positions / relax, restitution, store impulses, finalize bodies).  With
+ * ONCHIP the rows are prepared straight into shared memory (reference
+ * src/contact_solver.c:597-808) and only their impulses go back to the manifolds. */
+template <int T, bool ONCHIP>
 __device__ void solve_world( const b2gBatchItem& it, const b2gStepConst& sc, float4* sm )
 {
 	const b2gDevWorld& W = it.W;
 	const int tid = threadIdx.x;
 	const int N = it.bodyIdCount;
-	float4* st0 = sm;
-	float4* st1 = sm + N;
-	float4* term = sm + 2 * N;
-	float* ad = (float*)( sm + 3 * N );
-	SharedBodies B{ st0, st1 };
+	const int rows = it.colorStart[B2G_COLORS];
+	WorldImage s;
+	s.B = SharedBodies{ sm, sm + N };
+	float4* rb = sm + body_float4s( N );
+	s.m.idx = (int4*)rb;
+	s.m.nf = rb + rows;
+	s.m.ms = rb + 2 * rows;
+	s.m.anc0 = rb + 3 * rows;
+	s.m.anc1 = rb + 4 * rows;
+	s.m.coef0 = rb + 5 * rows;
+	s.m.coef1 = rb + 6 * rows;
+	s.m.imp0 = rb + 7 * rows;
+	s.m.imp1 = rb + 8 * rows;
+	float4* st0 = s.B.st0;
+	float4* st1 = s.B.st1;
 	float4* gst = (float4*)W.state;
 	const float4* mass = (const float4*)W.mass;
 
@@ -176,16 +242,28 @@ __device__ void solve_world( const b2gBatchItem& it, const b2gStepConst& sc, flo
 		st1[b] = gst[2 * b + 1];
 	}
 	const int awake = it.awakeCount;
-	for ( int i = tid; i < awake; i += T )
+	if constexpr ( ONCHIP )
 	{
-		int b = W.awake[i];
-		VelocityTerms v = velocity_terms( mass[b], ( (const float4*)W.force )[b], ( (const float4*)W.extent )[b], sc );
-		term[b] = make_float4( v.lvd.x, v.lvd.y, v.avd, v.ld );
-		ad[b] = v.ad;
+		const float4 zero = make_float4( 0.0f, 0.0f, 0.0f, 0.0f );
+		const float warm = sc.enableWarmStarting ? 1.0f : 0.0f;
+		for ( int k = tid; k < rows; k += T )
+		{
+			int cid = W.solveList[k];
+			int ia = W.cBodies[2 * cid];
+			int ib = W.cBodies[2 * cid + 1];
+			DevState sA = ia >= 0 ? state_of( gst[2 * ia], gst[2 * ia + 1] ) : identity_state();
+			DevState sB = ib >= 0 ? state_of( gst[2 * ib], gst[2 * ib + 1] ) : identity_state();
+			Row r;
+			prepare_row( r, W.manifold + cid, ia, ib, ia >= 0 ? mass[ia] : zero, ib >= 0 ? mass[ib] : zero, sA, sB, W.cMix[2 * cid],
+						 W.cMix[2 * cid + 1], ( ia < 0 || ib < 0 ) ? sc.staticSoft : sc.contactSoft, warm );
+			store_row_smem( s.m, k, cid, r );
+		}
 	}
-	const int rows = it.colorStart[B2G_COLORS];
-	for ( int k = tid; k < rows; k += T )
-		prepare_contact_row( W, k, sc );
+	else
+	{
+		for ( int k = tid; k < rows; k += T )
+			prepare_contact_row( W, k, sc );
+	}
 	const int joints = it.jointStart[B2G_COLORS];
 	for ( int t = tid; t < joints; t += T )
 		prepare_joint( W, t, sc );
@@ -197,18 +275,13 @@ __device__ void solve_world( const b2gBatchItem& it, const b2gStepConst& sc, flo
 		{
 			int b = W.awake[i];
 			DevState x = state_of( st0[b], st1[b] );
-			float4 t4 = term[b];
-			VelocityTerms v;
-			v.lvd = gv( t4.x, t4.y );
-			v.avd = t4.z;
-			v.ld = t4.w;
-			v.ad = ad[b];
+			VelocityTerms v = velocity_terms( mass[b], ( (const float4*)W.force )[b], ( (const float4*)W.extent )[b], sc );
 			integrate_velocity( x, v, sc );
 			st0[b] = velocity_word( x );
 		}
 		__syncthreads();
-		world_stage<T>( it, B, 0, sc );
-		world_stage<T>( it, B, 1, sc );
+		world_stage<T, ONCHIP>( it, s, F_WARM, sc );
+		world_stage<T, ONCHIP>( it, s, F_SOLVE, sc );
 		for ( int i = tid; i < awake; i += T )
 		{
 			int b = W.awake[i];
@@ -217,12 +290,35 @@ __device__ void solve_world( const b2gBatchItem& it, const b2gStepConst& sc, flo
 			st1[b] = make_float4( x.dp.x, x.dp.y, x.dq.c, x.dq.s );
 		}
 		__syncthreads();
-		world_stage<T>( it, B, 2, sc );
+		world_stage<T, ONCHIP>( it, s, F_RELAX, sc );
 	}
-	world_stage<T>( it, B, 3, sc );
+	world_stage<T, ONCHIP>( it, s, F_RESTITUTION, sc );
 
-	for ( int k = tid; k < rows; k += T )
-		store_row( W, k, it.colorStart[B2G_OVERFLOW] );
+	if constexpr ( ONCHIP )
+	{
+		/* colour rows store both point slots, overflow rows their points (as store_row) */
+		const int ov = it.colorStart[B2G_OVERFLOW];
+		for ( int k = tid; k < rows; k += T )
+		{
+			int4 idx = s.m.idx[k];
+			b2gManifold* mf = W.manifold + idx.z;
+			int n = k < ov ? 2 : idx.w;
+			float4 imp[2] = { s.m.imp0[k], s.m.imp1[k] };
+			float4 coef[2] = { s.m.coef0[k], s.m.coef1[k] };
+			for ( int j = 0; j < n; ++j )
+			{
+				mf->pts[j].normalImpulse = imp[j].x;
+				mf->pts[j].tangentImpulse = imp[j].y;
+				mf->pts[j].maxNormalImpulse = imp[j].z;
+				mf->pts[j].normalVelocity = coef[j].w;
+			}
+		}
+	}
+	else
+	{
+		for ( int k = tid; k < rows; k += T )
+			store_row( W, k, it.colorStart[B2G_OVERFLOW] );
+	}
 	for ( int i = tid; i < awake; i += T )
 	{
 		int b = W.awake[i];
@@ -234,8 +330,10 @@ __device__ void solve_world( const b2gBatchItem& it, const b2gStepConst& sc, flo
 		finalize_body( W, i, sc );
 }
 
-template <int T>
-__global__ void __launch_bounds__( T ) k_batch_solve( const b2gBatchItem* items, const int* order, int* queue )
+/* Persistent: each CTA takes the next world from the queue (order[0] worlds, then their
+ * item indices). */
+template <int T, int MINB>
+__global__ void __launch_bounds__( T, MINB ) k_batch_solve( const b2gBatchItem* items, const int* order, int* queue )
 {
 	extern __shared__ float4 sm[];
 	__shared__ int s_next;
@@ -253,7 +351,10 @@ __global__ void __launch_bounds__( T ) k_batch_solve( const b2gBatchItem* items,
 		if ( threadIdx.x < (int)( sizeof( b2gStepConst ) / 4 ) )
 			( (int*)&s_sc )[threadIdx.x] = ( (const int*)&it.sc )[threadIdx.x];
 		__syncthreads();
-		solve_world<T>( it, s_sc, sm );
+		if ( it.rowsOnChip )
+			solve_world<T, true>( it, s_sc, sm );
+		else
+			solve_world<T, false>( it, s_sc, sm );
 		__syncthreads();
 	}
 }
@@ -261,21 +362,34 @@ __global__ void __launch_bounds__( T ) k_batch_solve( const b2gBatchItem* items,
 static_assert( sizeof( b2gStepConst ) / 4 <= 64, "step constants are copied by the first 64 threads" );
 
 /* ------------------------------------------------------------------ host side */
-template <int T>
+template <int T, int MINB>
 static int solve_occupancy( size_t smem )
 {
 	int blocks = 0;
-	cudaFuncSetAttribute( k_batch_solve<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem );
-	if ( cudaOccupancyMaxActiveBlocksPerMultiprocessor( &blocks, k_batch_solve<T>, T, smem ) != cudaSuccess )
+	cudaFuncSetAttribute( k_batch_solve<T, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem );
+	if ( cudaOccupancyMaxActiveBlocksPerMultiprocessor( &blocks, k_batch_solve<T, MINB>, T, smem ) != cudaSuccess )
 		return 0;
 	return blocks;
 }
 
-template <int T>
-static void launch_solve( b2gBatch* b, size_t smem, int grid )
+template <int T, int MINB>
+static void launch_solve( b2gBatch* b, int grid, size_t smem )
 {
-	k_batch_solve<T><<<grid, T, smem, b->stream>>>( b->dItems, b->dOrder, b->dQueue );
+	k_batch_solve<T, MINB><<<grid, T, smem, b->stream>>>( b->dItems, b->dOrder, b->dQueue );
 }
+
+/* Solver launch shapes tried on the first steps: threads per CTA and CTAs per SM (which
+ * also caps the registers per thread and sets the shared memory per world). */
+struct TuneCandidate
+{
+	int threads, perSM;
+	int ( *occupancy )( size_t smem );
+	void ( *launch )( b2gBatch* b, int grid, size_t smem );
+};
+#define TUNE_SHAPE( T, B ) { T, B, solve_occupancy<T, B>, launch_solve<T, B> }
+static const TuneCandidate s_tune[TUNE_CANDIDATES] = { TUNE_SHAPE( 128, 8 ), TUNE_SHAPE( 256, 4 ), TUNE_SHAPE( 64, 16 ),
+													   TUNE_SHAPE( 128, 6 ), TUNE_SHAPE( 256, 3 ), TUNE_SHAPE( 128, 4 ) };
+#undef TUNE_SHAPE
 
 extern "C" b2gBatch* b2gd_batch_create( void )
 {
@@ -292,7 +406,7 @@ extern "C" b2gBatch* b2gd_batch_create( void )
 	cudaDeviceGetAttribute( &b->sms, cudaDevAttrMultiProcessorCount, dev );
 	for ( int i = 0; i < 4; ++i )
 		cudaEventCreate( &b->ev[i] );
-	cudaMalloc( &b->dQueue, sizeof( int ) );
+	cudaMalloc( &b->dQueue, sizeof( int ) * 8 );
 	return b;
 }
 
@@ -349,7 +463,7 @@ extern "C" b2gBatchItem* b2gd_batch_items( b2gBatch* b, int count )
 	size_t ints = (size_t)cap + 1;
 	bool ok = cudaMallocHost( &b->hItems, sizeof( b2gBatchItem ) * cap ) == cudaSuccess &&
 			  cudaMallocHost( &b->hPrefix, sizeof( int ) * 2 * ints ) == cudaSuccess &&
-			  cudaMallocHost( &b->hOrder, sizeof( int ) * ints ) == cudaSuccess &&
+			  cudaMallocHost( &b->hOrder, sizeof( int ) * 2u * ints ) == cudaSuccess && /* order + scratch */
 			  cudaMallocHost( &b->hCounters, sizeof( int ) * 4 * cap ) == cudaSuccess &&
 			  cudaMalloc( &b->dItems, sizeof( b2gBatchItem ) * cap ) == cudaSuccess &&
 			  cudaMalloc( &b->dPrefix, sizeof( int ) * 2 * ints ) == cudaSuccess &&
@@ -428,19 +542,27 @@ extern "C" int b2gd_batch_collide( b2gBatch* b, int n )
 	return (int)e;
 }
 
-static int order_by_size( b2gBatch* b, int n, int* maxBodies )
+/* Worlds to solve, largest first (a counting sort on body count), then alternating
+ * from both ends of that order so that the largest start early and the resident worlds
+ * mix sizes.  Marks the worlds whose rows fit beside their bodies in smem bytes of
+ * shared memory and returns the largest body count among the others. */
+static int order_worlds( b2gBatch* b, int n, size_t smem, int* rowBodies )
 {
-	/* worlds to solve, largest first (a counting sort on body count) */
-	int m = 0, top = 0;
+	int m = 0, top = 0, rowTop = 0;
 	for ( int i = 0; i < n; ++i )
 	{
-		if ( b->hItems[i].solve == 0 )
+		b2gBatchItem& it = b->hItems[i];
+		it.rowsOnChip = 0;
+		if ( it.solve == 0 )
 			continue;
-		int nb = b->hItems[i].bodyIdCount;
+		int nb = it.bodyIdCount;
+		it.rowsOnChip = world_smem_bytes( nb, it.colorStart[B2G_COLORS] ) <= smem ? 1 : 0;
+		if ( it.rowsOnChip == 0 )
+			rowTop = nb > rowTop ? nb : rowTop;
 		top = nb > top ? nb : top;
 		m += 1;
 	}
-	*maxBodies = top;
+	*rowBodies = rowTop;
 	int* order = b->hOrder + 1;
 	b->hOrder[0] = m;
 	if ( m == 0 )
@@ -448,18 +570,22 @@ static int order_by_size( b2gBatch* b, int n, int* maxBodies )
 	const int buckets = 64;
 	int count[buckets + 1];
 	memset( count, 0, sizeof( count ) );
+	int scale = top > 0 ? top : 1;
 	for ( int i = 0; i < n; ++i )
 		if ( b->hItems[i].solve )
-			count[buckets - 1 - (int)( (long long)b->hItems[i].bodyIdCount * ( buckets - 1 ) / ( top > 0 ? top : 1 ) )] += 1;
+			count[buckets - 1 - (int)( (long long)b->hItems[i].bodyIdCount * ( buckets - 1 ) / scale )] += 1;
 	for ( int k = 0, s = 0; k <= buckets; ++k )
 	{
 		int c = count[k];
 		count[k] = s;
 		s += c;
 	}
+	int* tmp = b->hOrder + 1 + m;
 	for ( int i = 0; i < n; ++i )
 		if ( b->hItems[i].solve )
-			order[count[buckets - 1 - (int)( (long long)b->hItems[i].bodyIdCount * ( buckets - 1 ) / ( top > 0 ? top : 1 ) )]++] = i;
+			tmp[count[buckets - 1 - (int)( (long long)b->hItems[i].bodyIdCount * ( buckets - 1 ) / scale )]++] = i;
+	for ( int i = 0, lo = 0, hi = m - 1; lo <= hi; ++i )
+		order[i] = ( i & 1 ) == 0 ? tmp[lo++] : tmp[hi--];
 	return m;
 }
 
@@ -468,38 +594,37 @@ extern "C" int b2gd_batch_solve( b2gBatch* b, int n )
 	if ( n <= 0 )
 		return 0;
 	point_counters( b, n );
-	int maxBodies = 0;
-	order_by_size( b, n, &maxBodies );
-	/* shared memory: state (2 float4), velocity terms (float4 + float) per body id,
-	 * rounded up to 256 body ids so that growing worlds rarely recapture the graph */
-	int slots = ( ( maxBodies > 0 ? maxBodies : 1 ) + 255 ) / 256 * 256;
-	size_t smem = (size_t)slots * ( 3 * 16 + 4 );
-	if ( smem > 226 * 1024 )
+	int choice = b->tuned ? b->choice : ( b->tuneStep / TUNE_SAMPLES ) % TUNE_CANDIDATES;
+	const TuneCandidate tc = s_tune[choice];
+	/* shared memory per CTA: the candidate's share of the SM (less the per-CTA
+	 * reservation), or more when a world that keeps its rows in global memory needs it
+	 * for its bodies (rounded up to 256 body ids so that growing worlds rarely recapture) */
+	size_t target = ( SM_SHARED_BYTES / (size_t)tc.perSM - 2048u ) / 256u * 256u;
+	int rowBodies = 0;
+	order_worlds( b, n, target, &rowBodies );
+	size_t smem = 16u * (size_t)body_float4s( ( rowBodies + 255 ) / 256 * 256 );
+	smem = smem > target ? smem : target;
+	if ( smem > CTA_SHARED_MAX )
 		return (int)cudaErrorInvalidValue;
 
-	int choice = b->tuned ? b->choice : ( b->tuneStep / TUNE_SAMPLES ) % TUNE_CANDIDATES;
 	if ( b->solveExec[choice] == nullptr || b->solveN[choice] != n || b->solveSmem[choice] != (int)smem )
 	{
 		if ( b->solveExec[choice] )
 			cudaGraphExecDestroy( b->solveExec[choice] );
 		b->solveExec[choice] = nullptr;
-		int T = s_tuneThreads[choice];
-		int occ = T == 64 ? solve_occupancy<64>( smem ) : T == 128 ? solve_occupancy<128>( smem ) : solve_occupancy<256>( smem );
+		int occ = tc.occupancy( smem );
 		if ( occ <= 0 )
 			return (int)cudaErrorInvalidConfiguration;
+		occ = occ < tc.perSM ? occ : tc.perSM;
 		int grid = b->sms * occ;
+		cudaGetLastError();
 		cudaGraph_t g = nullptr;
 		cudaStreamBeginCapture( b->stream, cudaStreamCaptureModeThreadLocal );
 		cudaMemcpyAsync( b->dItems, b->hItems, sizeof( b2gBatchItem ) * n, cudaMemcpyHostToDevice, b->stream );
 		cudaMemcpyAsync( b->dOrder, b->hOrder, sizeof( int ) * ( n + 1 ), cudaMemcpyHostToDevice, b->stream );
 		cudaMemsetAsync( b->dQueue, 0, sizeof( int ), b->stream );
 		k_batch_tape<<<b->sms * 4, BATCH_GRID_THREADS, 0, b->stream>>>( b->dItems, n );
-		if ( T == 64 )
-			launch_solve<64>( b, smem, grid );
-		else if ( T == 128 )
-			launch_solve<128>( b, smem, grid );
-		else
-			launch_solve<256>( b, smem, grid );
+		tc.launch( b, grid, smem );
 		cudaMemcpyAsync( b->hCounters, b->dCounters, sizeof( int ) * 4 * n, cudaMemcpyDeviceToHost, b->stream );
 		cudaError_t e = cudaStreamEndCapture( b->stream, &g );
 		if ( e != cudaSuccess )
@@ -563,6 +688,6 @@ extern "C" void b2gd_batch_stats( b2gBatch* b, float* collideMs, float* solveMs,
 {
 	*collideMs = b->collideMs;
 	*solveMs = b->solveMs;
-	*threads = b->tuned ? s_tuneThreads[b->choice] : 0;
+	*threads = b->tuned ? s_tune[b->choice].threads : 0;
 	*launches = b->launches;
 }
