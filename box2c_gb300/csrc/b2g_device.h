@@ -94,8 +94,8 @@ typedef struct b2gBatchItem
 	int tapeRows;	  /* rows recorded for the adjoint this step */
 	void* tapeBodies; /* adjoint tape destinations, or null when not recording */
 	void* tapeRowDst;
+	int widest;		/* most rows + joints of any colour but the overflow colour */
 	int rowsOnChip; /* 1 when the solver keeps this world's rows in shared memory (set at launch) */
-	int pad;
 } b2gBatchItem;
 
 /* Device context of batched steps: pinned staging of items and counters, device copies,
@@ -111,7 +111,8 @@ void* b2gd_batch_stream( b2gBatch* b );
 const int* b2gd_batch_counters( b2gBatch* b, int i );
 /* Narrowphase of all items (contact records staged by b2gd_stage_contacts). */
 int b2gd_batch_collide( b2gBatch* b, int count );
-/* Solver stage and finalisation of all items with solve != 0, one world per CTA. */
+/* Solver stage and finalisation of all items with solve != 0: packs of similar-sized
+ * worlds, each world on one warp, a group of warps or a whole CTA. */
 int b2gd_batch_solve( b2gBatch* b, int count );
 int b2gd_batch_sync( b2gBatch* b );
 /* Device milliseconds of the last batched narrowphase and solve, the solver's CTA size

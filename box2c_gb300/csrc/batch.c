@@ -120,6 +120,13 @@ static void middle_worlds( int begin, int end, void* arg )
 		it->activeCount = plan.activeCount;
 		it->awakeCount = plan.awakeCount;
 		it->bodyIdCount = plan.bodyIdCount;
+		it->widest = 0;
+		for ( int a = 0; a < plan.activeCount; ++a )
+		{
+			int col = plan.active[a];
+			int nr = plan.colorStart[col + 1] - plan.colorStart[col] + plan.jointStart[col + 1] - plan.jointStart[col];
+			it->widest = nr > it->widest ? nr : it->widest;
+		}
 		if ( w->tapeBodyDst )
 		{
 			it->tapeBodies = w->tapeBodyDst;

@@ -41,8 +41,9 @@ struct b2gBatch
 	b2gBatchItem* dItems;
 	int* hPrefix; /* scatter prefix [n+1], then narrowphase prefix [n+1] */
 	int* dPrefix;
-	int* hOrder; /* [0] = worlds to solve, then their item indices, largest first */
+	int* hOrder; /* [0] = packs to solve, then PACK_INTS ints per pack; then scratch */
 	int* dOrder;
+	int* hScratch; /* 5 ints per item */
 	int* hCounters; /* 4 per item */
 	int* dCounters;
 	int* dQueue;
@@ -152,10 +153,30 @@ __device__ __forceinline__ void world_row( const b2gDevWorld& W, const WorldImag
 		row_work( W, s.B, k, phase, scalar, sc );
 }
 
-/* One stage over all colours of one world (overflow first, serially), the CTA's
- * threads sharing each colour, a CTA barrier after each. */
+/* The threads that solve one world: g consecutive threads of the CTA (a warp, a named-
+ * barrier group of 64 or 128, or the whole CTA), group number gi, own index t. */
+struct Group
+{
+	int g, gi, t;
+};
+
+/* Barrier of one group: every thread of the group reaches each of these at the same
+ * point of its world's (group-uniform) control flow. */
+template <int T>
+__device__ __forceinline__ void group_sync( const Group& G )
+{
+	if ( G.g == 32 )
+		__syncwarp();
+	else if ( G.g == T )
+		__syncthreads();
+	else
+		asm volatile( "bar.sync %0, %1;" ::"r"( G.gi + 1 ), "r"( G.g ) : "memory" );
+}
+
+/* One stage over all colours of one world (overflow first, serially), the group's
+ * threads sharing each colour, a group barrier after each. */
 template <int T, bool ONCHIP>
-__device__ void world_stage( const b2gBatchItem& it, const WorldImage& s, int phase, const b2gStepConst& sc )
+__device__ void world_stage( const b2gBatchItem& it, const WorldImage& s, const Group& G, int phase, const b2gStepConst& sc )
 {
 	const b2gDevWorld& W = it.W;
 	const int* cs = it.colorStart;
@@ -165,7 +186,7 @@ __device__ void world_stage( const b2gBatchItem& it, const WorldImage& s, int ph
 	bool overflow = phase == F_RESTITUTION ? ovRows > 0 : ovRows + ovJointsAll > 0;
 	if ( overflow )
 	{
-		if ( threadIdx.x == 0 )
+		if ( G.t == 0 )
 		{
 			if ( phase != F_RESTITUTION )
 				for ( int i = 0; i < ovJointsAll; ++i )
@@ -173,7 +194,7 @@ __device__ void world_stage( const b2gBatchItem& it, const WorldImage& s, int ph
 			for ( int i = 0; i < ovRows; ++i )
 				world_row<ONCHIP>( W, s, cs[B2G_OVERFLOW] + i, phase, true, sc );
 		}
-		__syncthreads();
+		group_sync<T>( G );
 	}
 	if ( phase == F_WARM && sc.enableWarmStarting == 0 )
 		return;
@@ -187,34 +208,35 @@ __device__ void world_stage( const b2gBatchItem& it, const WorldImage& s, int ph
 		if constexpr ( ONCHIP == false )
 		{
 			/* the colour after this one (the next stage starts again at the first) */
-			if ( threadIdx.x == T - 1 )
+			if ( G.t == G.g - 1 )
 			{
 				int cn = it.active[a + 1 < it.activeCount ? a + 1 : 0];
 				if ( cs[cn + 1] > cs[cn] )
 					prefetch_rows( W, cs[cn], cs[cn + 1] - cs[cn] );
 			}
 		}
-		for ( int t = threadIdx.x; t < nj + nr; t += T )
+		for ( int t = G.t; t < nj + nr; t += G.g )
 		{
 			if ( t < nj )
 				joint_work( W, s.B, W.jointList[js[c] + t], phase, sc );
 			else
 				world_row<ONCHIP>( W, s, cs[c] + t - nj, phase, false, sc );
 		}
-		__syncthreads();
+		group_sync<T>( G );
 	}
 }
 
-/* The solver stage and finalisation of one world by one CTA (reference src/solver.c
+/* The solver stage and finalisation of one world by one group (reference src/solver.c
  * stage order: prepare, substeps of integrate velocities / warm start / solve /
  * integrate positions / relax, restitution, store impulses, finalize bodies).  With
  * ONCHIP the rows are prepared straight into shared memory (reference
  * src/contact_solver.c:597-808) and only their impulses go back to the manifolds. */
 template <int T, bool ONCHIP>
-__device__ void solve_world( const b2gBatchItem& it, const b2gStepConst& sc, float4* sm )
+__device__ void solve_world( const b2gBatchItem& it, const b2gStepConst& sc, float4* sm, const Group& G )
 {
 	const b2gDevWorld& W = it.W;
-	const int tid = threadIdx.x;
+	const int tid = G.t;
+	const int step = G.g;
 	const int N = it.bodyIdCount;
 	const int rows = it.colorStart[B2G_COLORS];
 	WorldImage s;
@@ -236,7 +258,7 @@ __device__ void solve_world( const b2gBatchItem& it, const b2gStepConst& sc, flo
 
 	if ( tid == 0 )
 		W.counters[1] = 0;
-	for ( int b = tid; b < N; b += T )
+	for ( int b = tid; b < N; b += step )
 	{
 		st0[b] = gst[2 * b];
 		st1[b] = gst[2 * b + 1];
@@ -246,7 +268,7 @@ __device__ void solve_world( const b2gBatchItem& it, const b2gStepConst& sc, flo
 	{
 		const float4 zero = make_float4( 0.0f, 0.0f, 0.0f, 0.0f );
 		const float warm = sc.enableWarmStarting ? 1.0f : 0.0f;
-		for ( int k = tid; k < rows; k += T )
+		for ( int k = tid; k < rows; k += step )
 		{
 			int cid = W.solveList[k];
 			int ia = W.cBodies[2 * cid];
@@ -261,17 +283,17 @@ __device__ void solve_world( const b2gBatchItem& it, const b2gStepConst& sc, flo
 	}
 	else
 	{
-		for ( int k = tid; k < rows; k += T )
+		for ( int k = tid; k < rows; k += step )
 			prepare_contact_row( W, k, sc );
 	}
 	const int joints = it.jointStart[B2G_COLORS];
-	for ( int t = tid; t < joints; t += T )
+	for ( int t = tid; t < joints; t += step )
 		prepare_joint( W, t, sc );
-	__syncthreads();
+	group_sync<T>( G );
 
 	for ( int sub = 0; sub < sc.subSteps; ++sub )
 	{
-		for ( int i = tid; i < awake; i += T )
+		for ( int i = tid; i < awake; i += step )
 		{
 			int b = W.awake[i];
 			DevState x = state_of( st0[b], st1[b] );
@@ -279,26 +301,26 @@ __device__ void solve_world( const b2gBatchItem& it, const b2gStepConst& sc, flo
 			integrate_velocity( x, v, sc );
 			st0[b] = velocity_word( x );
 		}
-		__syncthreads();
-		world_stage<T, ONCHIP>( it, s, F_WARM, sc );
-		world_stage<T, ONCHIP>( it, s, F_SOLVE, sc );
-		for ( int i = tid; i < awake; i += T )
+		group_sync<T>( G );
+		world_stage<T, ONCHIP>( it, s, G, F_WARM, sc );
+		world_stage<T, ONCHIP>( it, s, G, F_SOLVE, sc );
+		for ( int i = tid; i < awake; i += step )
 		{
 			int b = W.awake[i];
 			DevState x = state_of( st0[b], st1[b] );
 			integrate_position( x, sc.h );
 			st1[b] = make_float4( x.dp.x, x.dp.y, x.dq.c, x.dq.s );
 		}
-		__syncthreads();
-		world_stage<T, ONCHIP>( it, s, F_RELAX, sc );
+		group_sync<T>( G );
+		world_stage<T, ONCHIP>( it, s, G, F_RELAX, sc );
 	}
-	world_stage<T, ONCHIP>( it, s, F_RESTITUTION, sc );
+	world_stage<T, ONCHIP>( it, s, G, F_RESTITUTION, sc );
 
 	if constexpr ( ONCHIP )
 	{
 		/* colour rows store both point slots, overflow rows their points (as store_row) */
 		const int ov = it.colorStart[B2G_OVERFLOW];
-		for ( int k = tid; k < rows; k += T )
+		for ( int k = tid; k < rows; k += step )
 		{
 			int4 idx = s.m.idx[k];
 			b2gManifold* mf = W.manifold + idx.z;
@@ -316,29 +338,34 @@ __device__ void solve_world( const b2gBatchItem& it, const b2gStepConst& sc, flo
 	}
 	else
 	{
-		for ( int k = tid; k < rows; k += T )
+		for ( int k = tid; k < rows; k += step )
 			store_row( W, k, it.colorStart[B2G_OVERFLOW] );
 	}
-	for ( int i = tid; i < awake; i += T )
+	for ( int i = tid; i < awake; i += step )
 	{
 		int b = W.awake[i];
 		gst[2 * b] = st0[b];
 		gst[2 * b + 1] = st1[b];
 	}
-	__syncthreads();
-	for ( int i = tid; i < awake; i += T )
+	group_sync<T>( G );
+	for ( int i = tid; i < awake; i += step )
 		finalize_body( W, i, sc );
 }
 
-/* Persistent: each CTA takes the next world from the queue (order[0] worlds, then their
- * item indices). */
+/* A pack: worlds of similar size solved side by side by one CTA, each by a group of
+ * `group` threads with 1 / (T / group) of the CTA's shared memory. */
+#define PACK_WORLDS 8
+#define PACK_INTS ( 1 + PACK_WORLDS )
+
+/* Persistent: each CTA takes the next pack from the queue (packs[0] packs, then
+ * PACK_INTS ints each: group size, item indices or -1). */
 template <int T, int MINB>
-__global__ void __launch_bounds__( T, MINB ) k_batch_solve( const b2gBatchItem* items, const int* order, int* queue )
+__global__ void __launch_bounds__( T, MINB ) k_batch_solve( const b2gBatchItem* items, const int* packs, int* queue, int smemFloat4 )
 {
 	extern __shared__ float4 sm[];
 	__shared__ int s_next;
-	__shared__ b2gStepConst s_sc;
-	const int m = order[0];
+	__shared__ b2gStepConst s_sc[T / 32];
+	const int m = packs[0];
 	for ( ;; )
 	{
 		if ( threadIdx.x == 0 )
@@ -347,19 +374,30 @@ __global__ void __launch_bounds__( T, MINB ) k_batch_solve( const b2gBatchItem* 
 		int q = s_next;
 		if ( q >= m )
 			break;
-		const b2gBatchItem& it = items[order[1 + q]];
-		if ( threadIdx.x < (int)( sizeof( b2gStepConst ) / 4 ) )
-			( (int*)&s_sc )[threadIdx.x] = ( (const int*)&it.sc )[threadIdx.x];
-		__syncthreads();
-		if ( it.rowsOnChip )
-			solve_world<T, true>( it, s_sc, sm );
-		else
-			solve_world<T, false>( it, s_sc, sm );
+		const int* p = packs + 1 + PACK_INTS * q;
+		Group G;
+		G.g = p[0];
+		G.gi = threadIdx.x / G.g;
+		G.t = threadIdx.x - G.gi * G.g;
+		int w = G.gi < PACK_WORLDS ? p[1 + G.gi] : -1;
+		if ( w >= 0 )
+		{
+			const b2gBatchItem& it = items[w];
+			b2gStepConst* sc = s_sc + G.gi;
+			for ( int i = G.t; i < (int)( sizeof( b2gStepConst ) / 4 ); i += G.g )
+				( (int*)sc )[i] = ( (const int*)&it.sc )[i];
+			group_sync<T>( G );
+			float4* region = sm + ( smemFloat4 / ( T / G.g ) ) * G.gi;
+			if ( it.rowsOnChip )
+				solve_world<T, true>( it, *sc, region, G );
+			else
+				solve_world<T, false>( it, *sc, region, G );
+		}
 		__syncthreads();
 	}
 }
 
-static_assert( sizeof( b2gStepConst ) / 4 <= 64, "step constants are copied by the first 64 threads" );
+static_assert( PACK_WORLDS * 32 >= 256, "a pack holds a world for every warp of the largest CTA" );
 
 /* ------------------------------------------------------------------ host side */
 template <int T, int MINB>
@@ -375,7 +413,7 @@ static int solve_occupancy( size_t smem )
 template <int T, int MINB>
 static void launch_solve( b2gBatch* b, int grid, size_t smem )
 {
-	k_batch_solve<T, MINB><<<grid, T, smem, b->stream>>>( b->dItems, b->dOrder, b->dQueue );
+	k_batch_solve<T, MINB><<<grid, T, smem, b->stream>>>( b->dItems, b->dOrder, b->dQueue, (int)( smem / 16u ) );
 }
 
 /* Solver launch shapes tried on the first steps: threads per CTA and CTAs per SM (which
@@ -428,13 +466,14 @@ static void release_buffers( b2gBatch* b )
 	cudaFreeHost( b->hItems );
 	cudaFreeHost( b->hPrefix );
 	cudaFreeHost( b->hOrder );
+	cudaFreeHost( b->hScratch );
 	cudaFreeHost( b->hCounters );
 	cudaFree( b->dItems );
 	cudaFree( b->dPrefix );
 	cudaFree( b->dOrder );
 	cudaFree( b->dCounters );
 	b->hItems = b->dItems = nullptr;
-	b->hPrefix = b->dPrefix = b->hOrder = b->dOrder = b->hCounters = b->dCounters = nullptr;
+	b->hPrefix = b->dPrefix = b->hOrder = b->dOrder = b->hScratch = b->hCounters = b->dCounters = nullptr;
 	b->capacity = 0;
 }
 
@@ -463,11 +502,12 @@ extern "C" b2gBatchItem* b2gd_batch_items( b2gBatch* b, int count )
 	size_t ints = (size_t)cap + 1;
 	bool ok = cudaMallocHost( &b->hItems, sizeof( b2gBatchItem ) * cap ) == cudaSuccess &&
 			  cudaMallocHost( &b->hPrefix, sizeof( int ) * 2 * ints ) == cudaSuccess &&
-			  cudaMallocHost( &b->hOrder, sizeof( int ) * 2u * ints ) == cudaSuccess && /* order + scratch */
+			  cudaMallocHost( &b->hOrder, sizeof( int ) * ( 1u + 2u * PACK_INTS * ints ) ) == cudaSuccess && /* packs + scratch */
+			  cudaMallocHost( &b->hScratch, sizeof( int ) * 5u * ints ) == cudaSuccess &&
 			  cudaMallocHost( &b->hCounters, sizeof( int ) * 4 * cap ) == cudaSuccess &&
 			  cudaMalloc( &b->dItems, sizeof( b2gBatchItem ) * cap ) == cudaSuccess &&
 			  cudaMalloc( &b->dPrefix, sizeof( int ) * 2 * ints ) == cudaSuccess &&
-			  cudaMalloc( &b->dOrder, sizeof( int ) * ints ) == cudaSuccess &&
+			  cudaMalloc( &b->dOrder, sizeof( int ) * ( 1u + PACK_INTS * ints ) ) == cudaSuccess &&
 			  cudaMalloc( &b->dCounters, sizeof( int ) * 4 * cap ) == cudaSuccess;
 	if ( ok == false )
 	{
@@ -542,51 +582,100 @@ extern "C" int b2gd_batch_collide( b2gBatch* b, int n )
 	return (int)e;
 }
 
-/* Worlds to solve, largest first (a counting sort on body count), then alternating
- * from both ends of that order so that the largest start early and the resident worlds
- * mix sizes.  Marks the worlds whose rows fit beside their bodies in smem bytes of
- * shared memory and returns the largest body count among the others. */
-static int order_worlds( b2gBatch* b, int n, size_t smem, int* rowBodies )
+/* Builds the packs of this step into hOrder for CTAs of T threads with smem bytes of
+ * shared memory: each world gets the smallest group (32, 64, 128 or T threads) that
+ * covers its widest colour in two passes and holds its bodies in the group's share of
+ * shared memory, and keeps its rows on chip when they fit there too.  Worlds of one
+ * group size are packed largest first; packs go into the queue by their longest world
+ * (colours x passes), then alternating from both ends.  Returns the number of packs. */
+static int build_packs( b2gBatch* b, int n, int T, size_t smem )
 {
-	int m = 0, top = 0, rowTop = 0;
+	int* groupOf = b->hScratch;			 /* per item: group size, 0 when not solved */
+	int* byGroup = b->hScratch + n;		 /* items by group size, largest first */
+	int* packCost = b->hScratch + 2 * n; /* per pack */
+	int* sizeKey = b->hScratch + 3 * n;	 /* per item: body count */
+	int* cost = b->hScratch + 4 * n;	 /* per item: colours x passes */
+	int* packs = b->hOrder + 1;
+	int* tmp = b->hOrder + 1 + PACK_INTS * n;
+	int top = 1;
 	for ( int i = 0; i < n; ++i )
 	{
 		b2gBatchItem& it = b->hItems[i];
 		it.rowsOnChip = 0;
+		groupOf[i] = 0;
 		if ( it.solve == 0 )
 			continue;
-		int nb = it.bodyIdCount;
-		it.rowsOnChip = world_smem_bytes( nb, it.colorStart[B2G_COLORS] ) <= smem ? 1 : 0;
-		if ( it.rowsOnChip == 0 )
-			rowTop = nb > rowTop ? nb : rowTop;
-		top = nb > top ? nb : top;
-		m += 1;
+		int g = 32;
+		while ( g < T && ( 2 * g < it.widest || 32u * (size_t)it.bodyIdCount > smem / (size_t)( T / g ) ) )
+			g *= 2;
+		groupOf[i] = g;
+		it.rowsOnChip = world_smem_bytes( it.bodyIdCount, it.colorStart[B2G_COLORS] ) <= ( smem / (size_t)( T / g ) ) / 16u * 16u;
+		sizeKey[i] = it.bodyIdCount;
+		cost[i] = ( it.activeCount + 1 ) * ( ( it.widest + g - 1 ) / g + 1 );
+		top = it.bodyIdCount > top ? it.bodyIdCount : top;
 	}
-	*rowBodies = rowTop;
-	int* order = b->hOrder + 1;
-	b->hOrder[0] = m;
-	if ( m == 0 )
-		return 0;
+	/* counting sort on (group size, body count): 4 group sizes x 64 size buckets */
 	const int buckets = 64;
-	int count[buckets + 1];
+	int count[4 * buckets + 1];
 	memset( count, 0, sizeof( count ) );
-	int scale = top > 0 ? top : 1;
+	auto key = [&]( int i ) {
+		int g = groupOf[i];
+		int gk = g == 32 ? 0 : g == 64 ? 1 : g == 128 ? 2 : 3;
+		return gk * buckets + buckets - 1 - (int)( (long long)sizeKey[i] * ( buckets - 1 ) / top );
+	};
 	for ( int i = 0; i < n; ++i )
-		if ( b->hItems[i].solve )
-			count[buckets - 1 - (int)( (long long)b->hItems[i].bodyIdCount * ( buckets - 1 ) / scale )] += 1;
-	for ( int k = 0, s = 0; k <= buckets; ++k )
+		if ( groupOf[i] )
+			count[key( i )] += 1;
+	for ( int k = 0, s = 0; k <= 4 * buckets; ++k )
 	{
 		int c = count[k];
 		count[k] = s;
 		s += c;
 	}
-	int* tmp = b->hOrder + 1 + m;
+	int m = count[4 * buckets];
 	for ( int i = 0; i < n; ++i )
-		if ( b->hItems[i].solve )
-			tmp[count[buckets - 1 - (int)( (long long)b->hItems[i].bodyIdCount * ( buckets - 1 ) / scale )]++] = i;
-	for ( int i = 0, lo = 0, hi = m - 1; lo <= hi; ++i )
-		order[i] = ( i & 1 ) == 0 ? tmp[lo++] : tmp[hi--];
-	return m;
+		if ( groupOf[i] )
+			byGroup[count[key( i )]++] = i;
+	/* packs of T / g consecutive worlds of one group size */
+	int P = 0, costTop = 1;
+	for ( int k = 0; k < m; )
+	{
+		int g = groupOf[byGroup[k]];
+		int* p = tmp + PACK_INTS * P;
+		p[0] = g;
+		int most = 0;
+		for ( int j = 0; j < PACK_WORLDS; ++j )
+		{
+			bool take = j < T / g && k < m && groupOf[byGroup[k]] == g;
+			p[1 + j] = take ? byGroup[k++] : -1;
+			if ( take )
+				most = cost[p[1 + j]] > most ? cost[p[1 + j]] : most;
+		}
+		packCost[P++] = most;
+		costTop = most > costTop ? most : costTop;
+	}
+	/* queue order: costliest first (counting sort), then alternating from both ends */
+	int ccount[buckets + 1];
+	memset( ccount, 0, sizeof( ccount ) );
+	auto ckey = [&]( int q ) { return buckets - 1 - (int)( (long long)packCost[q] * ( buckets - 1 ) / costTop ); };
+	for ( int q = 0; q < P; ++q )
+		ccount[ckey( q )] += 1;
+	for ( int k = 0, s = 0; k <= buckets; ++k )
+	{
+		int c = ccount[k];
+		ccount[k] = s;
+		s += c;
+	}
+	int* sorted = byGroup; /* reused: pack indices by cost */
+	for ( int q = 0; q < P; ++q )
+		sorted[ccount[ckey( q )]++] = q;
+	for ( int i = 0, lo = 0, hi = P - 1; lo <= hi; ++i )
+	{
+		int q = ( i & 1 ) == 0 ? sorted[lo++] : sorted[hi--];
+		memcpy( packs + PACK_INTS * i, tmp + PACK_INTS * q, sizeof( int ) * PACK_INTS );
+	}
+	b->hOrder[0] = P;
+	return P;
 }
 
 extern "C" int b2gd_batch_solve( b2gBatch* b, int n )
@@ -597,15 +686,18 @@ extern "C" int b2gd_batch_solve( b2gBatch* b, int n )
 	int choice = b->tuned ? b->choice : ( b->tuneStep / TUNE_SAMPLES ) % TUNE_CANDIDATES;
 	const TuneCandidate tc = s_tune[choice];
 	/* shared memory per CTA: the candidate's share of the SM (less the per-CTA
-	 * reservation), or more when a world that keeps its rows in global memory needs it
-	 * for its bodies (rounded up to 256 body ids so that growing worlds rarely recapture) */
+	 * reservation), or more when the largest world needs it for its bodies (rounded up
+	 * to 256 body ids so that growing worlds rarely recapture) */
 	size_t target = ( SM_SHARED_BYTES / (size_t)tc.perSM - 2048u ) / 256u * 256u;
-	int rowBodies = 0;
-	order_worlds( b, n, target, &rowBodies );
-	size_t smem = 16u * (size_t)body_float4s( ( rowBodies + 255 ) / 256 * 256 );
+	int top = 0;
+	for ( int i = 0; i < n; ++i )
+		if ( b->hItems[i].solve )
+			top = b->hItems[i].bodyIdCount > top ? b->hItems[i].bodyIdCount : top;
+	size_t smem = 16u * (size_t)body_float4s( ( top + 255 ) / 256 * 256 );
 	smem = smem > target ? smem : target;
 	if ( smem > CTA_SHARED_MAX )
 		return (int)cudaErrorInvalidValue;
+	build_packs( b, n, tc.threads, smem );
 
 	if ( b->solveExec[choice] == nullptr || b->solveN[choice] != n || b->solveSmem[choice] != (int)smem )
 	{
@@ -621,7 +713,7 @@ extern "C" int b2gd_batch_solve( b2gBatch* b, int n )
 		cudaGraph_t g = nullptr;
 		cudaStreamBeginCapture( b->stream, cudaStreamCaptureModeThreadLocal );
 		cudaMemcpyAsync( b->dItems, b->hItems, sizeof( b2gBatchItem ) * n, cudaMemcpyHostToDevice, b->stream );
-		cudaMemcpyAsync( b->dOrder, b->hOrder, sizeof( int ) * ( n + 1 ), cudaMemcpyHostToDevice, b->stream );
+		cudaMemcpyAsync( b->dOrder, b->hOrder, sizeof( int ) * ( 1 + PACK_INTS * (size_t)n ), cudaMemcpyHostToDevice, b->stream );
 		cudaMemsetAsync( b->dQueue, 0, sizeof( int ), b->stream );
 		k_batch_tape<<<b->sms * 4, BATCH_GRID_THREADS, 0, b->stream>>>( b->dItems, n );
 		tc.launch( b, grid, smem );
