@@ -150,16 +150,19 @@ def cpu_baseline(steps_sample=20):
 
 
 BATCH_WORLDS = 4096
+# DRAM bytes of the solver stage of one large-pyramid step (k_fused_stage 2.35 MB +
+# k_solve_fused 2.76 MB), from the committed ncu capture of the same workload
+SOLVER_DRAM_BYTES = 5.11e6
 BATCH_SEED = 1237
 
 
-def batch_bases():
+def batch_bases(n=BATCH_WORLDS):
     """Pyramid bases U{4..40} for the batched workload (4096 worlds)."""
     rng = np.random.default_rng(BATCH_SEED)
-    return rng.integers(4, 41, size=BATCH_WORLDS)
+    return rng.integers(4, 41, size=n)
 
 
-def run_batch(g, steps, warmup):
+def run_batch(g, steps, warmup, n_worlds=BATCH_WORLDS):
     """Batched worlds: 4096 pyramids with bases U{4..40} (config-0 material, dt, substeps)
     stepped together with b2World_StepBatch; also times a loop of single-world
     b2World_Step calls over a sample of the same worlds."""
@@ -167,12 +170,15 @@ def run_batch(g, steps, warmup):
     import torch
     L = g.lib
     bind_batch_api(L)
-    bases = batch_bases()
+    bases = batch_bases(n_worlds)
     worlds = [g.pyramid(int(b), 0.0, 0) for b in bases]
     ids = world_array(worlds)
     n = len(worlds)
-    for _ in range(max(3, warmup)):
+    # warm up past the solver autotuner (it times each launch shape on the first steps)
+    warm = 0
+    while warm < max(3, warmup) or (L.b2World_GetBatchStats().solveThreads == 0 and warm < 100):
         L.b2World_StepBatch(ids, n, DT, SUBSTEPS)
+        warm += 1
     torch.cuda.synchronize()
     host, dev_c, dev_s = [], [], []
     prof = []
@@ -200,12 +206,13 @@ def run_batch(g, steps, warmup):
     value = n * steps / total
     return {
         "metric": "batched world-steps/s", "value": round(value, 1), "unit": "world-steps/s",
-        "worlds": n, "bodies": bodies, "steps": steps, "warmup": max(3, warmup),
+        "worlds": n, "bodies": bodies, "steps": steps, "warmup": warm,
         "ms_per_batched_step": round(total * 1e3 / steps, 4),
         "device_ms": {"collide": round(float(np.mean(dev_c)), 4), "solve": round(float(np.mean(dev_s)), 4)},
         "host_ms": dict(zip(("prepare", "narrowphase_wait", "events_lists", "solve_wait", "records"),
                             [round(float(x), 4) for x in np.mean(np.array(prof), 0)])),
-        "host_threads": st.hostThreads, "solve_cta_threads": st.solveThreads, "gpu_launches_per_step": st.launches,
+        "host_threads": st.hostThreads, "solve_cta_threads": st.solveThreads, "solve_ctas_per_sm": st.solveCtasPerSm,
+        "gpu_launches_per_step": st.launches,
         "loop_world_steps_per_s": round(loop, 1), "speedup_vs_loop": round(value / loop, 1),
         "failed_worlds": failed,
     }
@@ -368,7 +375,7 @@ def run_gpu(args):
     toi = L.b2World_GetUnsupportedToiCount(w)
     g.destroy(w)
 
-    batch = run_batch(g, args.batch_steps, 5) if args.batch_steps > 0 else None
+    batch = run_batch(g, args.batch_steps, 5, args.batch_worlds) if args.batch_steps > 0 else None
     adjoint = run_adjoint(g) if not args.no_adjoint else None
 
     if rank != 0:
@@ -391,7 +398,10 @@ def run_gpu(args):
         "host_ms": dict(zip(("step", "pairs", "collide_and_events", "solve_and_sync", "records"),
                             [round(float(x), 4) for x in np.mean(np.array(host_prof), 0)])),
         "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
-                     "frac": round(achieved / peak, 4), "traffic": None, "kernel": "solver stage (prepare..store)",
+                     "frac": round(achieved / peak, 4), "traffic": SOLVER_DRAM_BYTES,
+                     "traffic_source": "ncu dram__bytes_read+write of k_fused_stage + k_solve_fused, one step "
+                                       "(profiles/solver_fused_large_pyramid.txt)",
+                     "kernel": "solver stage (prepare..store)",
                      "algorithmic_bytes_per_step": solver_bytes, "peak_kind": peak_kind},
         "step_roofline": {"algorithmic_bytes_per_step": total_bytes,
                           "achieved_gbs": round(total_bytes / (ms * 1e-3) / 1e9, 2)},
@@ -417,7 +427,14 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--batch-steps", type=int, default=30, help="batched-worlds steps to time (0: skip)")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the differentiable-stepping measurement")
+    ap.add_argument("--part", default="all", choices=["all", "batch"],
+                    help="batch: only the batched-worlds measurement (for profiling), printed as its own line")
+    ap.add_argument("--batch-worlds", type=int, default=BATCH_WORLDS, help="worlds of the batched workload")
     args = ap.parse_args()
+    if args.part == "batch":
+        import box2c_gb300
+        print(json.dumps(run_batch(box2c_gb300.load(), args.batch_steps, args.warmup, args.batch_worlds)))
+        return
     if args.impl == "reference":
         run_reference(args)
     else:

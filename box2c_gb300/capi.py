@@ -278,7 +278,8 @@ class BatchStats(C.Structure):
     """include/box2d/gpu.h b2BatchStats."""
     _fields_ = [("collide", C.c_float), ("solve", C.c_float), ("solveThreads", C.c_int), ("launches", C.c_int),
                 ("hostBegin", C.c_float), ("hostCollide", C.c_float), ("hostMiddle", C.c_float),
-                ("hostSolve", C.c_float), ("hostFinish", C.c_float), ("hostThreads", C.c_int)]
+                ("hostSolve", C.c_float), ("hostFinish", C.c_float), ("hostThreads", C.c_int),
+                ("solveCtasPerSm", C.c_int)]
 
 
 def bind_batch_api(lib: C.CDLL) -> None:

@@ -342,32 +342,34 @@ B2G_HD bool gvertex_manifold( b2gManifold* m, b2gVec vA, b2gVec vB, float dist2,
 	return true;
 }
 
-/* Polygon (or capsule / segment cast as a polygon) against polygon. */
-B2G_HD void gcollide_polygons( b2gManifold* m, const b2gPoly* polyA, b2gXf xfA, const b2gPoly* polyB, b2gXf xfB )
+/* Polygon (or capsule / segment cast as a polygon) against polygon, on the vertex and
+ * normal arrays of either a b2gPoly or a polygon shape (no copy of the shapes). */
+B2G_HD void gcollide_polygons_raw( b2gManifold* m, const b2gVec* vA, const b2gVec* nA, int countA, float radiusA, b2gXf xfA,
+								   const b2gVec* vB, const b2gVec* nB, int countB, float radiusB, b2gXf xfB )
 {
 	gmanifold_clear( m );
-	b2gVec origin = polyA->v[0];
+	b2gVec origin = vA[0];
 	b2gXf sfA;
 	sfA.p = gadd( xfA.p, grotate( xfA.q, origin ) );
 	sfA.q = xfA.q;
 	b2gXf xf = ginvmulxf( sfA, xfB );
 
 	b2gPoly A, B;
-	A.count = polyA->count;
-	A.radius = polyA->radius;
+	A.count = countA;
+	A.radius = radiusA;
 	A.v[0] = gv( 0.0f, 0.0f );
-	A.n[0] = polyA->n[0];
+	A.n[0] = nA[0];
 	for ( int i = 1; i < A.count; ++i )
 	{
-		A.v[i] = gsub( polyA->v[i], origin );
-		A.n[i] = polyA->n[i];
+		A.v[i] = gsub( vA[i], origin );
+		A.n[i] = nA[i];
 	}
-	B.count = polyB->count;
-	B.radius = polyB->radius;
+	B.count = countB;
+	B.radius = radiusB;
 	for ( int i = 0; i < B.count; ++i )
 	{
-		B.v[i] = gxfpoint( xf, polyB->v[i] );
-		B.n[i] = grotate( xf.q, polyB->n[i] );
+		B.v[i] = gxfpoint( xf, vB[i] );
+		B.n[i] = grotate( xf.q, nB[i] );
 	}
 
 	int edgeA = 0;
@@ -463,6 +465,12 @@ B2G_HD void gcollide_polygons( b2gManifold* m, const b2gPoly* polyA, b2gXf xfA, 
 	}
 }
 
+B2G_HD void gcollide_polygons( b2gManifold* m, const b2gPoly* polyA, b2gXf xfA, const b2gPoly* polyB, b2gXf xfB )
+{
+	gcollide_polygons_raw( m, polyA->v, polyA->n, polyA->count, polyA->radius, xfA, polyB->v, polyB->n, polyB->count, polyB->radius,
+						   xfB );
+}
+
 /* Shape as a polygon for the polygon path: capsules and segments become 2-gons. */
 B2G_HD void gshape_poly( b2gPoly* p, const b2gShapeGeo* g )
 {
@@ -502,6 +510,11 @@ B2G_HD void gcollide_shapes( b2gManifold* m, const b2gShapeGeo* a, b2gXf xfA, co
 			gshape_poly( &pa, a );
 			gcollide_polygon_circle( m, &pa, xfA, b->v[0], b->radius, xfB );
 		}
+		return;
+	}
+	if ( a->type == 3 && b->type == 3 )
+	{
+		gcollide_polygons_raw( m, a->v, a->n, a->count, a->radius, xfA, b->v, b->n, b->count, b->radius, xfB );
 		return;
 	}
 	b2gPoly pa, pb;

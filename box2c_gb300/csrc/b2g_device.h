@@ -116,8 +116,8 @@ int b2gd_batch_collide( b2gBatch* b, int count );
 int b2gd_batch_solve( b2gBatch* b, int count );
 int b2gd_batch_sync( b2gBatch* b );
 /* Device milliseconds of the last batched narrowphase and solve, the solver's CTA size
- * and the number of graph launches. */
-void b2gd_batch_stats( b2gBatch* b, float* collideMs, float* solveMs, int* threads, int* launches );
+ * and resident CTAs per SM, and the number of kernel launches. */
+void b2gd_batch_stats( b2gBatch* b, float* collideMs, float* solveMs, int* threads, int* ctasPerSm, int* launches );
 /* Copies a world's staged contact records to the device on the world's stream. */
 int b2gd_stage_contacts( b2gDevWorld* w, b2gHostIO* io, int count );
 

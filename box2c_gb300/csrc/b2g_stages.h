@@ -128,12 +128,28 @@ static __device__ __forceinline__ void scatter_contact( const b2gDevWorld& W, co
  * boxes on sm_103a (nvcc 13.0.88, -O3 --fmad=false) while the same source called from a
  * one-thread kernel, or on the host, was correct; the non-inlined form is correct in
  * both kernels and bit-identical to the reference. */
+static __device__ __noinline__ void narrowphase_polygons( b2gManifold* m, const b2gShapeGeo* gA, b2gXf xfA, const b2gShapeGeo* gB,
+														  b2gXf xfB )
+{
+	gcollide_polygons_raw( m, gA->v, gA->n, gA->count, gA->radius, xfA, gB->v, gB->n, gB->count, gB->radius, xfB );
+}
+
+static __device__ __noinline__ void narrowphase_shapes( b2gManifold* m, const b2gShapeGeo* gA, b2gXf xfA, const b2gShapeGeo* gB,
+														b2gXf xfB )
+{
+	gcollide_shapes( m, gA, xfA, gB, xfB );
+}
+
+/* Polygon pairs (the common case) take their own call, whose frame holds only the two
+ * polygons in the contact frame; the other pairs' polygon copies stay out of it. */
 static __device__ __noinline__ void narrowphase( b2gManifold* m, const b2gShapeGeo* gA, b2gXf xfA, const b2gShapeGeo* gB, b2gXf xfB )
 {
 	if ( gA->isSensor || gB->isSensor )
 		gmanifold_clear( m );
+	else if ( gA->type == 3 && gB->type == 3 )
+		narrowphase_polygons( m, gA, xfA, gB, xfB );
 	else
-		gcollide_shapes( m, gA, xfA, gB, xfB );
+		narrowphase_shapes( m, gA, xfA, gB, xfB );
 }
 
 static __device__ __forceinline__ void emit_event( const b2gDevWorld& W, int id, int code )
@@ -179,7 +195,12 @@ static __device__ void collide_contact( const b2gDevWorld& W, int id )
 	b2gVec offA = grotate( xfA.q, gv( ca.z, ca.w ) );
 	b2gVec offB = grotate( xfB.q, gv( cb.z, cb.w ) );
 
-	b2gManifold old = W.manifold[id];
+	/* the previous manifold's feature ids and impulses, for warm starting */
+	const b2gManifold* prev = W.manifold + id;
+	const int oldCount = prev->count;
+	const uint16_t oldId0 = prev->pts[0].id, oldId1 = prev->pts[1].id;
+	const float oldN0 = prev->pts[0].normalImpulse, oldT0 = prev->pts[0].tangentImpulse;
+	const float oldN1 = prev->pts[1].normalImpulse, oldT1 = prev->pts[1].tangentImpulse;
 	b2gManifold m;
 	narrowphase( &m, gA, xfA, gB, xfB );
 
@@ -195,15 +216,18 @@ static __device__ void collide_contact( const b2gDevWorld& W, int id )
 		mp2->maxNormalImpulse = 0.0f;
 		mp2->normalVelocity = 0.0f;
 		mp2->persisted = 0;
-		for ( int j = 0; j < old.count; ++j )
+		/* first old point with the same id (reference src/contact.c:539-570) */
+		if ( oldCount > 0 && oldId0 == mp2->id )
 		{
-			if ( old.pts[j].id == mp2->id )
-			{
-				mp2->normalImpulse = old.pts[j].normalImpulse;
-				mp2->tangentImpulse = old.pts[j].tangentImpulse;
-				mp2->persisted = 1;
-				break;
-			}
+			mp2->normalImpulse = oldN0;
+			mp2->tangentImpulse = oldT0;
+			mp2->persisted = 1;
+		}
+		else if ( oldCount > 1 && oldId1 == mp2->id )
+		{
+			mp2->normalImpulse = oldN1;
+			mp2->tangentImpulse = oldT1;
+			mp2->persisted = 1;
 		}
 	}
 	W.manifold[id] = m;

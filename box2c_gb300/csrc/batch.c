@@ -239,7 +239,7 @@ b2BatchStats b2World_GetBatchStats( void )
 	b2BatchStats s;
 	memset( &s, 0, sizeof( s ) );
 	if ( s_batch != NULL )
-		b2gd_batch_stats( s_batch, &s.collide, &s.solve, &s.solveThreads, &s.launches );
+		b2gd_batch_stats( s_batch, &s.collide, &s.solve, &s.solveThreads, &s.solveCtasPerSm, &s.launches );
 	s.hostBegin = s_hostMs[0];
 	s.hostCollide = s_hostMs[1];
 	s.hostMiddle = s_hostMs[2];

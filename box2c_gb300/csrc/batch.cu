@@ -55,6 +55,7 @@ struct b2gBatch
 	cudaGraphExec_t solveExec[TUNE_CANDIDATES];
 	int solveN[TUNE_CANDIDATES];
 	int solveSmem[TUNE_CANDIDATES];
+	int solvePerSm[TUNE_CANDIDATES]; /* resident CTAs per SM of each captured launch */
 
 	int tuned, choice, tuneStep;
 	float tuneMs[TUNE_CANDIDATES];
@@ -404,6 +405,9 @@ template <int T, int MINB>
 static int solve_occupancy( size_t smem )
 {
 	int blocks = 0;
+	/* the default carve-out: the L1 left beside shared memory caches the row arrays of
+	 * the worlds whose rows stay in global memory (a maximal shared carve-out measured
+	 * 20% slower) */
 	cudaFuncSetAttribute( k_batch_solve<T, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem );
 	if ( cudaOccupancyMaxActiveBlocksPerMultiprocessor( &blocks, k_batch_solve<T, MINB>, T, smem ) != cudaSuccess )
 		return 0;
@@ -708,6 +712,7 @@ extern "C" int b2gd_batch_solve( b2gBatch* b, int n )
 		if ( occ <= 0 )
 			return (int)cudaErrorInvalidConfiguration;
 		occ = occ < tc.perSM ? occ : tc.perSM;
+		b->solvePerSm[choice] = occ;
 		int grid = b->sms * occ;
 		cudaGetLastError();
 		cudaGraph_t g = nullptr;
@@ -776,10 +781,11 @@ extern "C" int b2gd_batch_sync( b2gBatch* b )
 	return (int)cudaGetLastError();
 }
 
-extern "C" void b2gd_batch_stats( b2gBatch* b, float* collideMs, float* solveMs, int* threads, int* launches )
+extern "C" void b2gd_batch_stats( b2gBatch* b, float* collideMs, float* solveMs, int* threads, int* ctasPerSm, int* launches )
 {
 	*collideMs = b->collideMs;
 	*solveMs = b->solveMs;
 	*threads = b->tuned ? s_tune[b->choice].threads : 0;
+	*ctasPerSm = b->tuned ? b->solvePerSm[b->choice] : 0;
 	*launches = b->launches;
 }

@@ -55,10 +55,11 @@ B2_API void b2World_EnableFusedSolver( b2WorldId worldId, bool flag );
 B2_API void b2World_StepBatch( const b2WorldId* worldIds, int count, float timeStep, int subStepCount );
 
 /* Device milliseconds of the last batched step's narrowphase and solver segments, the
- * solver CTA size picked by the autotuner (0 while it is still timing candidates), the
- * kernel launches of the last batched step, and its host milliseconds per phase: world
- * preparation, narrowphase (host tree rebuilds and the wait), events and solve lists,
- * solver wait, finalisation records; per-world host work runs on hostThreads threads. */
+ * solver CTA size and resident CTAs per SM picked by the autotuner (0 while it is still
+ * timing candidates), the kernel launches of the last batched step, and its host
+ * milliseconds per phase: world preparation, narrowphase (host tree rebuilds and the
+ * wait), events and solve lists, solver wait, finalisation records; per-world host work
+ * runs on hostThreads threads. */
 typedef struct b2BatchStats
 {
 	float collide;
@@ -67,6 +68,7 @@ typedef struct b2BatchStats
 	int launches;
 	float hostBegin, hostCollide, hostMiddle, hostSolve, hostFinish;
 	int hostThreads;
+	int solveCtasPerSm;
 } b2BatchStats;
 
 B2_API b2BatchStats b2World_GetBatchStats( void );
