@@ -75,6 +75,24 @@ int b2gd_collide( b2gDevWorld* w, b2gHostIO* io, int newContactCount, int contac
 int b2gd_solve( b2gDevWorld* w, b2gHostIO* io, const b2gSolvePlan* plan, const b2gStepConst* sc );
 int b2gd_sync( b2gDevWorld* w );
 
+/* ---------------------------------------------------------------- broadphase query */
+/* Device pair query of one step's moved proxies (reference src/broad_phase.c:278-331
+ * b2FindPairsTask): for each moved proxy key (proxyId << 2 | tree type, or B2G_NULL), the
+ * leaves of the kinematic, static (dynamic proxies only) and dynamic trees whose fat
+ * boxes overlap its fat box, in the order of the host tree query (depth first, child1
+ * pushed before child2).  Candidates of proxy i are cand[2 * (B2G_QUERY_SLOTS * i + k)]
+ * (leaf proxy key) and cand[... + 1] (shape id) for k < counts[i]; counts[i] is -1 when
+ * the proxy needed more than B2G_QUERY_SLOTS slots or a deeper stack, and the host
+ * queries that proxy itself.  Synchronises the world's stream; the result arrays are
+ * host memory owned by the query and valid until the next call. */
+#define B2G_QUERY_SLOTS 32
+
+typedef struct b2gPairQuery b2gPairQuery;
+
+int b2gd_pair_query( b2gDevWorld* w, b2gPairQuery** query, const b2gTreeNode* const nodes[3], const int capacity[3], const int root[3],
+					 const int* keys, int count, const int** cand, const int** counts );
+void b2gd_pair_query_free( b2gPairQuery* query );
+
 /* ---------------------------------------------------------------- batched worlds */
 /* One world of a batched step (device copy of its descriptor plus the step's counts).
  * W.counters points into the batch's counter array, 4 ints per world. */

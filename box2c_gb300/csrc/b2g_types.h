@@ -22,6 +22,20 @@
 extern "C" {
 #endif
 
+/* Dynamic-tree node (reference include/box2d/collision.h:600-635 b2TreeNode fields the
+ * path uses): fat box, category bits, links, shape id of a leaf, height (0 for leaves).
+ * The host trees use this layout, so a tree is copied to the device as it is. */
+typedef struct b2gTreeNode
+{
+	b2gBox box;
+	uint32_t category;
+	int32_t parent;
+	int32_t child1, child2;
+	int32_t userData;
+	int16_t height;
+	bool enlarged;
+} b2gTreeNode;
+
 /* Shape geometry record (160 bytes).  Polygons use v/n/centroid/count/radius; circles
  * v[0] and radius; capsules v[0], v[1] and radius; segments v[0], v[1]. */
 typedef struct b2gShapeGeo

@@ -66,16 +66,7 @@ void gbits_clear( gBits* b, int i );
 void gbits_free( gBits* b );
 
 /* ---------------------------------------------------------------- tree */
-typedef struct gNode
-{
-	b2gBox box;
-	uint32_t category;
-	int parent;
-	int child1, child2;
-	int userData;
-	int16_t height;
-	bool enlarged;
-} gNode;
+typedef b2gTreeNode gNode;
 
 typedef struct gTree
 {
@@ -258,6 +249,7 @@ typedef struct gWorld
 	gIntArray jointList;
 	b2gSolvePlan solvePlan; /* plan of the current solve lists */
 	bool solveUploaded;		/* solve lists on the device match the host's */
+	b2gPairQuery* pairQuery; /* device pair query buffers, made on first use */
 
 	b2gVec gravity;
 	float restitutionThreshold, pushout, hitThreshold, contactHertz, contactDamping, jointHertz, jointDamping;

@@ -368,13 +368,36 @@ static bool pair_query( int proxyId, int shapeId, void* context )
 	return true;
 }
 
+/* Moved proxies from which the tree query runs on the device: below this a host query
+ * costs less than the device round trip (upload, launch, synchronise). */
+#define DEVICE_QUERY_MIN_MOVES 256
+
 /* All moved proxies are queried before any contact is created; each proxy's pairs are
- * then created in reverse discovery order (the reference prepends to a list). */
-static void update_pairs( gWorld* w )
+ * then created in reverse discovery order (the reference prepends to a list).  With many
+ * moved proxies the tree walks run on the device (pairs.cu) and their candidate leaves
+ * pass through pair_query here in the same order as the host walk would report them.
+ * Returns 0 or a CUDA error. */
+static int update_pairs( gWorld* w )
 {
 	int moveCount = w->moveArray.count;
 	if ( moveCount == 0 )
-		return;
+		return 0;
+	const int* cand = NULL;
+	const int* counts = NULL;
+	if ( moveCount >= DEVICE_QUERY_MIN_MOVES )
+	{
+		const b2gTreeNode* nodes[3];
+		int capacity[3], root[3];
+		for ( int t = 0; t < 3; ++t )
+		{
+			nodes[t] = w->trees[t].nodes;
+			capacity[t] = w->trees[t].capacity;
+			root[t] = w->trees[t].root;
+		}
+		int e = b2gd_pair_query( &w->dev, &w->pairQuery, nodes, capacity, root, w->moveArray.data, moveCount, &cand, &counts );
+		if ( e )
+			return e;
+	}
 	gPairList* lists = (gPairList*)calloc( (size_t)moveCount, sizeof( gPairList ) );
 	for ( int i = 0; i < moveCount; ++i )
 	{
@@ -390,6 +413,16 @@ static void update_pairs( gWorld* w )
 		q.list = lists + i;
 		q.queryProxyKey = proxyKey;
 		q.queryShapeIndex = base->nodes[proxyId].userData;
+		if ( counts != NULL && counts[i] >= 0 )
+		{
+			const int* c = cand + 2 * B2G_QUERY_SLOTS * i;
+			for ( int k = 0; k < counts[i]; ++k )
+			{
+				q.queryTreeType = c[2 * k] & 3;
+				pair_query( c[2 * k] >> 2, c[2 * k + 1], &q );
+			}
+			continue;
+		}
 		if ( proxyType == b2_dynamicBody )
 		{
 			q.queryTreeType = b2_kinematicBody;
@@ -411,6 +444,7 @@ static void update_pairs( gWorld* w )
 	free( lists );
 	w->moveArray.count = 0;
 	gset_clear( &w->moveSet );
+	return 0;
 }
 
 /* ------------------------------------------------------------ narrowphase events */
@@ -655,7 +689,12 @@ static void build_solve_lists( gWorld* w, b2gSolvePlan* plan )
 int gstep_begin( gWorld* w )
 {
 	double t0 = b2g_now_ms();
-	update_pairs( w );
+	int pe = update_pairs( w );
+	if ( pe )
+	{
+		w->status = pe;
+		return -1;
+	}
 	double t1 = b2g_now_ms();
 	w->profile.pairs = (float)( t1 - t0 );
 	w->stepStart = t1;

@@ -351,6 +351,8 @@ void b2DestroyWorld( b2WorldId worldId )
 {
 	gWorld* w = gworld_get( worldId );
 	gtape_free( w );
+	b2gd_pair_query_free( w->pairQuery );
+	w->pairQuery = NULL;
 	b2gd_free( &w->dev, &w->io );
 	for ( int i = 0; i < 3; ++i )
 		gtree_free( w->trees + i );
