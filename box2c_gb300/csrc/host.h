@@ -301,6 +301,7 @@ int gstep_begin( gWorld* w );
 /* Fork-join pool for per-world host work (pool.c). */
 typedef void gTaskFn( int begin, int end, void* ctx );
 void gpool_for( int count, int grain, gTaskFn* fn, void* ctx );
+bool gpool_try_for( int count, int grain, gTaskFn* fn, void* ctx );
 int gpool_threads( void );
 void gstep_rebuild_trees( gWorld* w );
 int gstep_after_collide( gWorld* w, float dt, int subSteps, b2gStepConst* sc, b2gSolvePlan* plan );

@@ -6,7 +6,9 @@
  *
  * gpool_for( count, grain, fn, ctx ) calls fn( begin, end, ctx ) over [0, count) in
  * chunks of `grain`, on the calling thread and the pool's workers, and returns when all
- * chunks are done.  Calls must not nest and come from one thread at a time.
+ * chunks are done.  One job runs at a time: gpool_for waits for the pool, gpool_try_for
+ * returns false at once when the pool is busy (another thread's job, or a call from
+ * inside a job) and the caller runs the range itself.  gpool_for must not nest.
  */
 #include "host.h"
 
@@ -34,6 +36,7 @@ typedef struct gPool
 
 static gPool s_pool;
 static pthread_once_t s_once = PTHREAD_ONCE_INIT;
+static pthread_mutex_t s_job = PTHREAD_MUTEX_INITIALIZER; /* held while a job runs */
 
 static void run_chunks( gPool* p )
 {
@@ -91,18 +94,9 @@ int gpool_threads( void )
 	return s_pool.workers + 1;
 }
 
-void gpool_for( int count, int grain, gTaskFn* fn, void* ctx )
+static void run_job( int count, int grain, gTaskFn* fn, void* ctx )
 {
-	if ( count <= 0 )
-		return;
-	grain = grain < 1 ? 1 : grain;
-	pthread_once( &s_once, pool_start );
 	gPool* p = &s_pool;
-	if ( p->workers == 0 || count <= grain )
-	{
-		fn( 0, count, ctx );
-		return;
-	}
 	pthread_mutex_lock( &p->lock );
 	p->fn = fn;
 	p->ctx = ctx;
@@ -118,4 +112,35 @@ void gpool_for( int count, int grain, gTaskFn* fn, void* ctx )
 	while ( p->active > 0 )
 		pthread_cond_wait( &p->done, &p->lock );
 	pthread_mutex_unlock( &p->lock );
+}
+
+void gpool_for( int count, int grain, gTaskFn* fn, void* ctx )
+{
+	if ( count <= 0 )
+		return;
+	grain = grain < 1 ? 1 : grain;
+	pthread_once( &s_once, pool_start );
+	if ( s_pool.workers == 0 || count <= grain )
+	{
+		fn( 0, count, ctx );
+		return;
+	}
+	pthread_mutex_lock( &s_job );
+	run_job( count, grain, fn, ctx );
+	pthread_mutex_unlock( &s_job );
+}
+
+bool gpool_try_for( int count, int grain, gTaskFn* fn, void* ctx )
+{
+	if ( count <= 0 )
+		return true;
+	grain = grain < 1 ? 1 : grain;
+	pthread_once( &s_once, pool_start );
+	if ( s_pool.workers == 0 || count <= grain )
+		return false;
+	if ( pthread_mutex_trylock( &s_job ) != 0 )
+		return false;
+	run_job( count, grain, fn, ctx );
+	pthread_mutex_unlock( &s_job );
+	return true;
 }

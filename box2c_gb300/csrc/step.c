@@ -371,35 +371,25 @@ static bool pair_query( int proxyId, int shapeId, void* context )
 /* Moved proxies from which the tree query runs on the device: below this a host query
  * costs less than the device round trip (upload, launch, synchronise). */
 #define DEVICE_QUERY_MIN_MOVES 256
+/* Moved proxies per chunk when the pair rules run on the host pool. */
+#define PAIR_GRAIN 64
 
-/* All moved proxies are queried before any contact is created; each proxy's pairs are
- * then created in reverse discovery order (the reference prepends to a list).  With many
- * moved proxies the tree walks run on the device (pairs.cu) and their candidate leaves
- * pass through pair_query here in the same order as the host walk would report them.
- * Returns 0 or a CUDA error. */
-static int update_pairs( gWorld* w )
+typedef struct gPairCtx
 {
-	int moveCount = w->moveArray.count;
-	if ( moveCount == 0 )
-		return 0;
-	const int* cand = NULL;
-	const int* counts = NULL;
-	if ( moveCount >= DEVICE_QUERY_MIN_MOVES )
-	{
-		const b2gTreeNode* nodes[3];
-		int capacity[3], root[3];
-		for ( int t = 0; t < 3; ++t )
-		{
-			nodes[t] = w->trees[t].nodes;
-			capacity[t] = w->trees[t].capacity;
-			root[t] = w->trees[t].root;
-		}
-		int e = b2gd_pair_query( &w->dev, &w->pairQuery, nodes, capacity, root, w->moveArray.data, moveCount, &cand, &counts );
-		if ( e )
-			return e;
-	}
-	gPairList* lists = (gPairList*)calloc( (size_t)moveCount, sizeof( gPairList ) );
-	for ( int i = 0; i < moveCount; ++i )
+	gWorld* w;
+	gPairList* lists;
+	const int* cand;
+	const int* counts;
+} gPairCtx;
+
+/* Pairs of moved proxies [begin, end): the device's candidates, or a host tree walk,
+ * through pair_query.  Reads the trees, move and pair sets, shapes, bodies and joints,
+ * writes only the proxies' own lists, so ranges run in parallel. */
+static void query_moved( int begin, int end, void* arg )
+{
+	gPairCtx* c = (gPairCtx*)arg;
+	gWorld* w = c->w;
+	for ( int i = begin; i < end; ++i )
 	{
 		int proxyKey = w->moveArray.data[i];
 		if ( proxyKey == B2G_NULL )
@@ -410,16 +400,16 @@ static int update_pairs( gWorld* w )
 		b2gBox fat = base->nodes[proxyId].box;
 		gQueryCtx q;
 		q.w = w;
-		q.list = lists + i;
+		q.list = c->lists + i;
 		q.queryProxyKey = proxyKey;
 		q.queryShapeIndex = base->nodes[proxyId].userData;
-		if ( counts != NULL && counts[i] >= 0 )
+		if ( c->counts != NULL && c->counts[i] >= 0 )
 		{
-			const int* c = cand + 2 * B2G_QUERY_SLOTS * i;
-			for ( int k = 0; k < counts[i]; ++k )
+			const int* cand = c->cand + 2 * B2G_QUERY_SLOTS * i;
+			for ( int k = 0; k < c->counts[i]; ++k )
 			{
-				q.queryTreeType = c[2 * k] & 3;
-				pair_query( c[2 * k] >> 2, c[2 * k + 1], &q );
+				q.queryTreeType = cand[2 * k] & 3;
+				pair_query( cand[2 * k] >> 2, cand[2 * k + 1], &q );
 			}
 			continue;
 		}
@@ -433,15 +423,50 @@ static int update_pairs( gWorld* w )
 		q.queryTreeType = b2_dynamicBody;
 		gtree_query( w->trees + b2_dynamicBody, fat, 0xFFFFFFFFu, pair_query, &q );
 	}
+}
+
+/* All moved proxies are queried before any contact is created (reference
+ * src/broad_phase.c:333-436, the queries as parallel tasks); each proxy's pairs are then
+ * created in move order, in reverse discovery order (the reference prepends to a list).
+ * With many moved proxies the tree walks run on the device (pairs.cu) and their
+ * candidate leaves pass through pair_query in the order the host walk would report
+ * them; the pair rules run on the host pool when it is free.  Returns 0 or a CUDA
+ * error. */
+static int update_pairs( gWorld* w )
+{
+	int moveCount = w->moveArray.count;
+	if ( moveCount == 0 )
+		return 0;
+	gPairCtx c;
+	c.w = w;
+	c.cand = NULL;
+	c.counts = NULL;
+	if ( moveCount >= DEVICE_QUERY_MIN_MOVES )
+	{
+		const b2gTreeNode* nodes[3];
+		int capacity[3], root[3];
+		for ( int t = 0; t < 3; ++t )
+		{
+			nodes[t] = w->trees[t].nodes;
+			capacity[t] = w->trees[t].capacity;
+			root[t] = w->trees[t].root;
+		}
+		int e = b2gd_pair_query( &w->dev, &w->pairQuery, nodes, capacity, root, w->moveArray.data, moveCount, &c.cand, &c.counts );
+		if ( e )
+			return e;
+	}
+	c.lists = (gPairList*)calloc( (size_t)moveCount, sizeof( gPairList ) );
+	if ( gpool_try_for( moveCount, PAIR_GRAIN, query_moved, &c ) == false )
+		query_moved( 0, moveCount, &c );
 	for ( int i = 0; i < moveCount; ++i )
 	{
-		gPairList* l = lists + i;
+		gPairList* l = c.lists + i;
 		for ( int k = l->count - 1; k >= 0; --k )
 			gcontact_create( w, w->shapes + l->a[k], w->shapes + l->b[k] );
 		free( l->a );
 		free( l->b );
 	}
-	free( lists );
+	free( c.lists );
 	w->moveArray.count = 0;
 	gset_clear( &w->moveSet );
 	return 0;
