@@ -164,17 +164,26 @@ __device__ __forceinline__ void row_step( const SmemRows& m, const Bodies& B, in
 	}
 }
 
+/* One joint phase with its bodies at B-indices ia and ib (-1 for a static body). */
 template <class Bodies>
-__device__ __forceinline__ void joint_step( const b2gDevWorld& W, const Bodies& B, int jid, int phase, const b2gStepConst& sc )
+__device__ __forceinline__ void joint_step_at( const b2gDevWorld& W, const Bodies& B, int jid, int ia, int ib, int phase,
+											   const b2gStepConst& sc )
 {
 	b2gJointDev* j = W.joints + jid;
-	DevState a = B.load( j->indexA );
-	DevState b = B.load( j->indexB );
+	DevState a = B.load( ia );
+	DevState b = B.load( ib );
 	if ( phase == F_WARM )
 		joint_warm_state( j, a, b );
 	else
 		joint_solve_state( j, a, b, phase == F_SOLVE, sc );
-	B.store( j->indexA, a );
-	B.store( j->indexB, b );
+	B.store( ia, a );
+	B.store( ib, b );
+}
+
+template <class Bodies>
+__device__ __forceinline__ void joint_step( const b2gDevWorld& W, const Bodies& B, int jid, int phase, const b2gStepConst& sc )
+{
+	const b2gJointDev* j = W.joints + jid;
+	joint_step_at( W, B, jid, j->indexA, j->indexB, phase, sc );
 }
 

@@ -492,3 +492,24 @@ __device__ __forceinline__ void integrate_position( DevState& s, float h )
 	s.dq = gintrot( s.dq, h * s.w );
 	s.dp = gmuladd( s.dp, h, s.v );
 }
+
+/* Body states in one CTA's shared memory, by index (a body id or a slot); -1 is a static
+ * body.  Stores write the velocity word only: no row or joint phase changes dp or dq. */
+struct SharedBodies
+{
+	float4* st0;
+	float4* st1;
+	__device__ __forceinline__ DevState load( int b ) const
+	{
+		return b < 0 ? identity_state() : state_of( st0[b], st1[b] );
+	}
+	__device__ __forceinline__ DevState load_velocity( int b ) const
+	{
+		return b < 0 ? identity_state() : state_of( st0[b], make_float4( 0.0f, 0.0f, 1.0f, 0.0f ) );
+	}
+	__device__ __forceinline__ void store( int b, const DevState& x ) const
+	{
+		if ( b >= 0 )
+			st0[b] = velocity_word( x );
+	}
+};

@@ -319,25 +319,6 @@ struct GlobalBodies
 	__device__ __forceinline__ void store( int b, const DevState& x ) const { store_velocity( *W, b, x ); }
 };
 
-struct SharedBodies
-{
-	float4* st0;
-	float4* st1;
-	__device__ __forceinline__ DevState load( int b ) const
-	{
-		return b < 0 ? identity_state() : state_of( st0[b], st1[b] );
-	}
-	__device__ __forceinline__ DevState load_velocity( int b ) const
-	{
-		return b < 0 ? identity_state() : state_of( st0[b], make_float4( 0.0f, 0.0f, 1.0f, 0.0f ) );
-	}
-	__device__ __forceinline__ void store( int b, const DevState& x ) const
-	{
-		if ( b >= 0 )
-			st0[b] = velocity_word( x );
-	}
-};
-
 /* One row phase (0 warm start, 1 solve, 2 relax, 3 restitution): row from the world's
  * row arrays, bodies through B. */
 template <class Bodies>

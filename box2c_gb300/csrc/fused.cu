@@ -53,6 +53,10 @@ struct FusedPlan
 	 * ctaBase[B2G_OVERFLOW][0] */
 	int split[B2G_OVERFLOW][B2G_FUSED_CTAS + 1];
 	int ctaBase[B2G_COLORS][B2G_FUSED_CTAS];
+	/* overflow set solved on local copies of its bodies in CTA 0 (1) or in place (0);
+	 * the copies and their index tables start at float4 offset ovOffset */
+	int ovCached;
+	int ovOffset;
 };
 
 /* Shared-memory carve-up; every CTA uses the same offsets, so a local address maps to
@@ -78,6 +82,42 @@ static __host__ __device__ int image_float4( int bodySlots, int rowCap )
 static size_t fused_smem_bytes( int bodySlots, int rowCap )
 {
 	return 16 * (size_t)image_float4( bodySlots, rowCap ) + 4 * (size_t)bodySlots + 16;
+}
+
+/* Overflow cache of CTA 0: for R overflow rows and J overflow joints with E = 2 (R + J)
+ * body ends, the rows' indices with body slots (int4 x R), slot states (2 x float4 x E),
+ * slot bodies, first occurrences and slots per end (3 x int x E), joint slots (int2 x J). */
+#define FUSED_OVERFLOW_MAX 512
+
+struct OverflowCache
+{
+	int4* idx;
+	float4* st0;
+	float4* st1;
+	int* body;
+	int* first;
+	int* slot;
+	int2* jslot;
+};
+
+static __host__ __device__ size_t overflow_bytes( int R, int J )
+{
+	size_t E = 2u * (size_t)( R + J );
+	return 16u * ( (size_t)R + 2u * E ) + 4u * ( 3u * E + 2u * (size_t)J );
+}
+
+__device__ __forceinline__ OverflowCache carve_overflow( float4* base, int R, int J )
+{
+	int E = 2 * ( R + J );
+	OverflowCache o;
+	o.idx = (int4*)base;
+	o.st0 = base + R;
+	o.st1 = o.st0 + E;
+	o.body = (int*)( o.st1 + E );
+	o.first = o.body + E;
+	o.slot = o.first + E;
+	o.jslot = (int2*)( o.slot + E );
+	return o;
 }
 
 __device__ __forceinline__ FusedSmem carve( float4* base, int BS, int RC )
@@ -107,7 +147,7 @@ __device__ __forceinline__ int local_count( int n, int rank, int CL ) { return n
  * each active colour with a cluster barrier after it. */
 template <int CL>
 __device__ void run_stage( const b2gDevWorld& W, const FusedPlan& P, const FusedSmem& m, const ClusterBodies& B, int rank,
-						   int phase, const b2gStepConst& sc )
+						   int phase, const b2gStepConst& sc, const OverflowCache& ov, int ovSlots )
 {
 	const int* cs = P.colorStart;
 	const int* js = P.jointStart;
@@ -119,11 +159,44 @@ __device__ void run_stage( const b2gDevWorld& W, const FusedPlan& P, const Fused
 	bool overflow = phase == F_RESTITUTION ? ovRows > 0 : ovRows + ovJointsAll > 0;
 	if ( overflow )
 	{
-		if ( rank == 0 && threadIdx.x == 0 )
+		int base = P.ctaBase[B2G_OVERFLOW][0];
+		if ( rank == 0 && P.ovCached )
+		{
+			/* the set's bodies to local slots, the serial pass on them, velocities back:
+			 * nothing else touches a body while the set runs */
+			for ( int s = threadIdx.x; s < ovSlots; s += FUSED_THREADS )
+			{
+				int b = ov.body[s];
+				ov.st0[s] = *B.word( B.st0, b );
+				ov.st1[s] = *B.word( B.st1, b );
+			}
+			__syncthreads();
+			if ( threadIdx.x == 0 )
+			{
+				SharedBodies OB{ ov.st0, ov.st1 };
+				for ( int i = 0; i < ovJoints; ++i )
+					joint_step_at( W, OB, W.jointList[js[B2G_OVERFLOW] + i], ov.jslot[i].x, ov.jslot[i].y, phase, sc );
+				SmemRows mo;
+				mo.idx = ov.idx;
+				mo.nf = m.nf + base;
+				mo.ms = m.ms + base;
+				mo.anc0 = m.anc0 + base;
+				mo.anc1 = m.anc1 + base;
+				mo.coef0 = m.coef0 + base;
+				mo.coef1 = m.coef1 + base;
+				mo.imp0 = m.imp0 + base;
+				mo.imp1 = m.imp1 + base;
+				for ( int i = 0; i < ovRows; ++i )
+					row_step( mo, OB, i, phase, true, sc );
+			}
+			__syncthreads();
+			for ( int s = threadIdx.x; s < ovSlots; s += FUSED_THREADS )
+				*B.word( B.st0, ov.body[s] ) = ov.st0[s];
+		}
+		else if ( rank == 0 && threadIdx.x == 0 )
 		{
 			for ( int i = 0; i < ovJoints; ++i )
 				joint_step( W, B, W.jointList[js[B2G_OVERFLOW] + i], phase, sc );
-			int base = P.ctaBase[B2G_OVERFLOW][0];
 			for ( int i = 0; i < ovRows; ++i )
 				row_step( m, B, base + i, phase, true, sc );
 		}
@@ -231,6 +304,83 @@ __global__ void __launch_bounds__( FUSED_THREADS ) k_solve_fused( b2gDevWorld W,
 		if ( m.flags[s] )
 			m.awake[atomicAdd( &awakeLocal, 1 )] = s;
 	}
+	/* overflow cache: distinct bodies of the set's ends get slots in end order */
+	const int ovR = cs[B2G_COLORS] - cs[B2G_OVERFLOW];
+	const int ovJ = P.jointStart[B2G_COLORS] - P.jointStart[B2G_OVERFLOW];
+	const int ovBase = P.ctaBase[B2G_OVERFLOW][0];
+	OverflowCache ov = carve_overflow( smem + P.ovOffset, ovR, ovJ );
+	__shared__ int ovSlots;
+	if ( rank == 0 && P.ovCached )
+	{
+		const int E = 2 * ( ovR + ovJ );
+		auto end_body = [&]( int e ) {
+			if ( e < 2 * ovJ )
+			{
+				const b2gJointDev* j = W.joints + W.jointList[P.jointStart[B2G_OVERFLOW] + ( e >> 1 )];
+				return ( e & 1 ) ? j->indexB : j->indexA;
+			}
+			int4 ix = m.idx[ovBase + ( ( e - 2 * ovJ ) >> 1 )];
+			return ( e & 1 ) ? ix.y : ix.x;
+		};
+		for ( int e = tid; e < E; e += FUSED_THREADS )
+		{
+			int b = end_body( e );
+			int f = -1;
+			if ( b >= 0 )
+			{
+				f = e;
+				for ( int e2 = 0; e2 < e; ++e2 )
+				{
+					if ( end_body( e2 ) == b )
+					{
+						f = e2;
+						break;
+					}
+				}
+			}
+			ov.first[e] = f;
+		}
+		__syncthreads();
+		if ( tid == 0 )
+		{
+			int K = 0;
+			for ( int e = 0; e < E; ++e )
+			{
+				if ( ov.first[e] == e )
+				{
+					ov.slot[e] = K;
+					ov.body[K++] = end_body( e );
+				}
+			}
+			ovSlots = K;
+		}
+		__syncthreads();
+		for ( int e = tid; e < E; e += FUSED_THREADS )
+		{
+			int f = ov.first[e];
+			int s = f < 0 ? -1 : ov.slot[f];
+			if ( e < 2 * ovJ )
+			{
+				if ( e & 1 )
+					ov.jslot[e >> 1].y = s;
+				else
+					ov.jslot[e >> 1].x = s;
+			}
+			else
+			{
+				int r = ( e - 2 * ovJ ) >> 1;
+				if ( e & 1 )
+					ov.idx[r].y = s;
+				else
+				{
+					int4 ix = m.idx[ovBase + r];
+					ov.idx[r].x = s;
+					ov.idx[r].z = ix.z;
+					ov.idx[r].w = ix.w;
+				}
+			}
+		}
+	}
 	ClusterBodies B{ cl, m.st0, m.st1, BS, rank };
 	cl.sync();
 
@@ -250,8 +400,8 @@ __global__ void __launch_bounds__( FUSED_THREADS ) k_solve_fused( b2gDevWorld W,
 			m.st0[s] = velocity_word( x );
 		}
 		cl.sync();
-		run_stage<CL>( W, P, m, B, rank, F_WARM, sc );
-		run_stage<CL>( W, P, m, B, rank, F_SOLVE, sc );
+		run_stage<CL>( W, P, m, B, rank, F_WARM, sc, ov, ovSlots );
+		run_stage<CL>( W, P, m, B, rank, F_SOLVE, sc, ov, ovSlots );
 		for ( int j = tid; j < awakeLocal; j += FUSED_THREADS )
 		{
 			int s = m.awake[j];
@@ -260,9 +410,9 @@ __global__ void __launch_bounds__( FUSED_THREADS ) k_solve_fused( b2gDevWorld W,
 			m.st1[s] = make_float4( x.dp.x, x.dp.y, x.dq.c, x.dq.s );
 		}
 		cl.sync();
-		run_stage<CL>( W, P, m, B, rank, F_RELAX, sc );
+		run_stage<CL>( W, P, m, B, rank, F_RELAX, sc, ov, ovSlots );
 	}
-	run_stage<CL>( W, P, m, B, rank, F_RESTITUTION, sc );
+	run_stage<CL>( W, P, m, B, rank, F_RESTITUTION, sc, ov, ovSlots );
 
 	/* store impulses (reference src/contact_solver.c:442-471, :1180-1293): colour rows
 	 * write both point slots, overflow rows their points */
@@ -376,6 +526,16 @@ extern "C" int b2gd_solver_fused( b2gDevWorld* w, const b2gSolvePlan* plan, cons
 	size_t bytes = fused_smem_bytes( P.bodySlots, P.rowCap );
 	if ( bytes > FUSED_SMEM_MAX )
 		return 0;
+	int ovR = plan->colorStart[B2G_COLORS] - plan->colorStart[B2G_OVERFLOW];
+	int ovJ = plan->jointStart[B2G_COLORS] - plan->jointStart[B2G_OVERFLOW];
+	size_t ovAt = ( bytes + 15 ) / 16;
+	size_t withCache = 16 * ovAt + overflow_bytes( ovR, ovJ );
+	if ( ovR + ovJ > 0 && ovR + ovJ <= FUSED_OVERFLOW_MAX && withCache <= FUSED_SMEM_MAX )
+	{
+		P.ovCached = 1;
+		P.ovOffset = (int)ovAt;
+		bytes = withCache;
+	}
 
 	auto kernel = k_solve_fused<FUSED_CLUSTER>;
 	if ( ready == 0 )
