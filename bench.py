@@ -149,6 +149,56 @@ def cpu_baseline(steps_sample=20):
     return ms, steps_sample
 
 
+TUMBLER_BODIES = 2000
+OVERFLOW_COLOR = 11  # slot of the overflow colour in b2Counters.colorCounts
+TUMBLER_SEED = 1236
+
+
+def run_tumbler(g, steps=1000, cpu=True):
+    """Tumbler: a 20 m hollow box of four walls on a revolute motor (0.05 pi rad/s) with
+    2000 boxes (half-extent 0.125) and circles (radius 0.125) at seeded random positions,
+    4 substeps, 1000 steps; device and wall ms per b2World_Step, host pair time, and the
+    oracle on a bounded sample of the same scene (one thread)."""
+    from box2c_gb300.capi import bind_gpu_api
+    L = g.lib
+    bind_gpu_api(L)
+    w = g.tumbler(TUMBLER_BODIES, TUMBLER_SEED, 0)
+    L.b2World_EnableDeviceTiming(w, True)
+    wall, dev, solve, pairs = [], [], [], []
+    for _ in range(steps):
+        t = time.perf_counter()
+        L.b2World_Step(w, DT, SUBSTEPS)
+        wall.append(time.perf_counter() - t)
+        d = L.b2World_GetDeviceTimes(w)
+        dev.append(d.step)
+        solve.append(d.solve)
+        pairs.append(L.b2World_GetProfile(w).pairs)
+    status = L.b2World_GetStatus(w)
+    counters = g.counters(w)
+    g.destroy(w)
+    skip = min(50, steps // 2)
+    out = {"workload": "tumbler_2000_bodies_revolute_motor", "steps": steps,
+           "wall_ms_per_step": round(float(np.mean(wall[skip:])) * 1e3, 4),
+           "device_ms_per_step": round(float(np.mean(dev[skip:])), 4),
+           "solve_ms": round(float(np.mean(solve[skip:])), 4),
+           "host_pairs_ms": round(float(np.mean(pairs[skip:])), 4),
+           "overflow_constraints": int(counters.colorCounts[OVERFLOW_COLOR]), "status": status}
+    if cpu:
+        subprocess.run(["make", "-s", "-j8", "-f", "oracle/Makefile"], cwd=REPO, check=True, capture_output=True)
+        from box2c_gb300.capi import Backend
+        ob = os.path.join(REPO, "oracle", "_build")
+        o = Backend(os.path.join(ob, "liboracle.so"), os.path.join(ob, "liboracle_scenes.so"), "oracle")
+        wo = o.tumbler(TUMBLER_BODIES, TUMBLER_SEED, 0)
+        o.step(wo, DT, SUBSTEPS, count=100)
+        n = 20
+        t0 = time.perf_counter()
+        o.step(wo, DT, SUBSTEPS, count=n)
+        out["cpu_baseline"] = {"value": round((time.perf_counter() - t0) * 1e3 / n, 4), "unit": "ms/step", "cores": 1,
+                               "kind": "port", "sample": f"steps 100-{100 + n} of the same tumbler"}
+        o.destroy(wo)
+    return out
+
+
 BATCH_WORLDS = 4096
 # DRAM bytes of the solver stage of one large-pyramid step (k_fused_stage 2.35 MB +
 # k_solve_fused 2.76 MB), from the committed ncu capture of the same workload
@@ -376,6 +426,7 @@ def run_gpu(args):
     g.destroy(w)
 
     batch = run_batch(g, args.batch_steps, 5, args.batch_worlds) if args.batch_steps > 0 else None
+    tumbler = run_tumbler(g, cpu=not args.no_cpu) if not args.no_tumbler else None
     adjoint = run_adjoint(g) if not args.no_adjoint else None
 
     if rank != 0:
@@ -413,6 +464,7 @@ def run_gpu(args):
                          if cpu_ms is not None else None),
         "clocks": clocks, "status": status, "unsupported_toi": toi,
         "batched": batch,
+        "tumbler": tumbler,
         "differentiable": adjoint,
     }
     print(json.dumps(line))
@@ -427,6 +479,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--batch-steps", type=int, default=30, help="batched-worlds steps to time (0: skip)")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the differentiable-stepping measurement")
+    ap.add_argument("--no-tumbler", action="store_true", help="skip the tumbler measurement")
     ap.add_argument("--part", default="all", choices=["all", "batch"],
                     help="batch: only the batched-worlds measurement (for profiling), printed as its own line")
     ap.add_argument("--batch-worlds", type=int, default=BATCH_WORLDS, help="worlds of the batched workload")
