@@ -134,14 +134,14 @@ def algorithmic_bytes(contacts, awake_bodies, shape_vertex_counts, substeps):
     return total, solver
 
 
-def cpu_baseline(steps_sample=20):
+def cpu_baseline(steps_sample=20, warmup=2):
     """Times the plain-C CPU restatement of the step on the same workload (1 thread)."""
     subprocess.run(["make", "-s", "-j8", "-f", "oracle/Makefile"], cwd=REPO, check=True, capture_output=True)
     from box2c_gb300.capi import Backend
     ob = os.path.join(REPO, "oracle", "_build")
     o = Backend(os.path.join(ob, "liboracle.so"), os.path.join(ob, "liboracle_scenes.so"), "oracle")
     w = o.pyramid(BASE, JITTER, SEED)
-    o.step(w, DT, SUBSTEPS, count=2)
+    o.step(w, DT, SUBSTEPS, count=warmup)
     t0 = time.perf_counter()
     o.step(w, DT, SUBSTEPS, count=steps_sample)
     ms = (time.perf_counter() - t0) * 1e3 / steps_sample
@@ -335,13 +335,14 @@ def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    ms, n = cpu_baseline(steps_sample=max(5, min(args.steps, 40)))
+    warm = max(3, args.warmup)
+    ms, n = cpu_baseline(steps_sample=max(5, min(args.steps, 40)), warmup=warm)
     line = {"metric": METRIC, "value": round(ms, 4), "unit": "ms/step", "n_gpus": args.gpus, "steps": n,
-            "warmup": 2, "ms_per_step": round(ms, 4), "higher_is_better": False, "impl": "reference",
+            "warmup": warm, "ms_per_step": round(ms, 4), "higher_is_better": False, "impl": "reference",
             "dtype": "f32", "data": "synthetic", "scaling": "weak", "vs_baseline": None,
             "config": {"workload": "large_pyramid_100_rows_5050_boxes", "dt": DT, "substeps": SUBSTEPS},
             "cpu_baseline": {"value": round(ms, 4), "unit": "ms/step", "cores": 1, "kind": "port",
-                             "sample": f"{n} steps of the 100-row pyramid after 2 warm-up steps"},
+                             "sample": f"{n} steps of the 100-row pyramid after {warm} warm-up steps"},
             "e2e": {"value": round(ms, 4), "unit": "ms/step", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 

@@ -22,7 +22,7 @@ _backend: Backend | None = None
 
 
 def build(verbose: bool = False, force: bool = False) -> str:
-    from .build import build as _build
+    from .compile import build as _build
     return _build(verbose=verbose, force=force)
 
 

@@ -123,7 +123,7 @@ static oMass polygon_mass( const oPolygon* s, b2r density )
 	if ( s->count == 2 )
 		return capsule_mass( s->v[0], s->v[1], s->radius, density );
 
-	oVec vs[8];
+	oVec vs[8] = { { 0 } };
 	int count = s->count;
 	if ( s->radius > R( 0 ) )
 	{
