@@ -31,7 +31,9 @@
 #define TUNE_CANDIDATES 6
 #define TUNE_SAMPLES 2
 #define SM_SHARED_BYTES ( 228u * 1024u ) /* shared memory of one SM */
-#define CTA_SHARED_MAX ( 226u * 1024u )	 /* dynamic shared memory one CTA may take here */
+/* dynamic shared memory one solver CTA may take: the 227 KB opt-in limit covers the
+ * kernel's static shared memory too (up to 1.4 KB), so leave room for it */
+#define CTA_SHARED_MAX ( 222u * 1024u )
 
 struct b2gBatch
 {
@@ -355,7 +357,7 @@ __device__ void solve_world( const b2gBatchItem& it, const b2gStepConst& sc, flo
 
 /* A pack: worlds of similar size solved side by side by one CTA, each by a group of
  * `group` threads with 1 / (T / group) of the CTA's shared memory. */
-#define PACK_WORLDS 8
+#define PACK_WORLDS 16
 #define PACK_INTS ( 1 + PACK_WORLDS )
 
 /* Persistent: each CTA takes the next pack from the queue (packs[0] packs, then
@@ -398,7 +400,7 @@ __global__ void __launch_bounds__( T, MINB ) k_batch_solve( const b2gBatchItem* 
 	}
 }
 
-static_assert( PACK_WORLDS * 32 >= 256, "a pack holds a world for every warp of the largest CTA" );
+static_assert( PACK_WORLDS * 32 >= 512, "a pack holds a world for every warp of the largest CTA" );
 
 /* ------------------------------------------------------------------ host side */
 template <int T, int MINB>
@@ -429,8 +431,8 @@ struct TuneCandidate
 	void ( *launch )( b2gBatch* b, int grid, size_t smem );
 };
 #define TUNE_SHAPE( T, B ) { T, B, solve_occupancy<T, B>, launch_solve<T, B> }
-static const TuneCandidate s_tune[TUNE_CANDIDATES] = { TUNE_SHAPE( 128, 8 ), TUNE_SHAPE( 256, 4 ), TUNE_SHAPE( 64, 16 ),
-													   TUNE_SHAPE( 128, 6 ), TUNE_SHAPE( 256, 3 ), TUNE_SHAPE( 128, 4 ) };
+static const TuneCandidate s_tune[TUNE_CANDIDATES] = { TUNE_SHAPE( 128, 6 ), TUNE_SHAPE( 512, 1 ), TUNE_SHAPE( 128, 8 ),
+													   TUNE_SHAPE( 512, 2 ), TUNE_SHAPE( 256, 3 ), TUNE_SHAPE( 128, 4 ) };
 #undef TUNE_SHAPE
 
 extern "C" b2gBatch* b2gd_batch_create( void )
@@ -568,10 +570,15 @@ extern "C" int b2gd_batch_collide( b2gBatch* b, int n )
 		cudaMemsetAsync( b->dCounters, 0, sizeof( int ) * 4 * n, b->stream );
 		k_batch_scatter<<<grid, BATCH_GRID_THREADS, 0, b->stream>>>( b->dItems, b->dPrefix, n );
 		k_batch_collide<<<grid, BATCH_GRID_THREADS, 0, b->stream>>>( b->dItems, b->dPrefix + n + 1, n );
+		cudaError_t launch = cudaGetLastError();
 		cudaMemcpyAsync( b->hCounters, b->dCounters, sizeof( int ) * 4 * n, cudaMemcpyDeviceToHost, b->stream );
 		cudaError_t e = cudaStreamEndCapture( b->stream, &g );
-		if ( e != cudaSuccess )
-			return (int)e;
+		if ( launch != cudaSuccess || e != cudaSuccess )
+		{
+			if ( g )
+				cudaGraphDestroy( g );
+			return (int)( launch != cudaSuccess ? launch : e );
+		}
 		e = cudaGraphInstantiate( &b->collideExec, g, 0 );
 		cudaGraphDestroy( g );
 		if ( e != cudaSuccess )
@@ -609,34 +616,46 @@ static int build_packs( b2gBatch* b, int n, int T, size_t smem )
 		groupOf[i] = 0;
 		if ( it.solve == 0 )
 			continue;
+		/* rows on chip: two passes per colour; rows in global memory: one, so that fewer
+		 * such worlds are resident at once and their rows stay in L2 */
 		int g = 32;
-		while ( g < T && ( 2 * g < it.widest || 32u * (size_t)it.bodyIdCount > smem / (size_t)( T / g ) ) )
+		bool onChip = false;
+		for ( ;; )
+		{
+			size_t share = ( smem / (size_t)( T / g ) ) / 16u * 16u;
+			onChip = world_smem_bytes( it.bodyIdCount, it.colorStart[B2G_COLORS] ) <= share;
+			bool bodiesFit = 32u * (size_t)it.bodyIdCount <= share;
+			if ( g >= T || ( bodiesFit && ( onChip ? 2 : 1 ) * g >= it.widest ) )
+				break;
 			g *= 2;
+		}
 		groupOf[i] = g;
-		it.rowsOnChip = world_smem_bytes( it.bodyIdCount, it.colorStart[B2G_COLORS] ) <= ( smem / (size_t)( T / g ) ) / 16u * 16u;
+		it.rowsOnChip = onChip ? 1 : 0;
 		sizeKey[i] = it.bodyIdCount;
 		cost[i] = ( it.activeCount + 1 ) * ( ( it.widest + g - 1 ) / g + 1 );
 		top = it.bodyIdCount > top ? it.bodyIdCount : top;
 	}
-	/* counting sort on (group size, body count): 4 group sizes x 64 size buckets */
+	/* counting sort on (group size, body count): 5 group sizes (32 .. 512) x 64 size buckets */
 	const int buckets = 64;
-	int count[4 * buckets + 1];
+	const int groups = 5;
+	int count[groups * buckets + 1];
 	memset( count, 0, sizeof( count ) );
 	auto key = [&]( int i ) {
-		int g = groupOf[i];
-		int gk = g == 32 ? 0 : g == 64 ? 1 : g == 128 ? 2 : 3;
+		int gk = 0;
+		for ( int g = groupOf[i]; g > 32; g >>= 1 )
+			gk += 1;
 		return gk * buckets + buckets - 1 - (int)( (long long)sizeKey[i] * ( buckets - 1 ) / top );
 	};
 	for ( int i = 0; i < n; ++i )
 		if ( groupOf[i] )
 			count[key( i )] += 1;
-	for ( int k = 0, s = 0; k <= 4 * buckets; ++k )
+	for ( int k = 0, s = 0; k <= groups * buckets; ++k )
 	{
 		int c = count[k];
 		count[k] = s;
 		s += c;
 	}
-	int m = count[4 * buckets];
+	int m = count[groups * buckets];
 	for ( int i = 0; i < n; ++i )
 		if ( groupOf[i] )
 			byGroup[count[key( i )]++] = i;
@@ -693,6 +712,7 @@ extern "C" int b2gd_batch_solve( b2gBatch* b, int n )
 	 * reservation), or more when the largest world needs it for its bodies (rounded up
 	 * to 256 body ids so that growing worlds rarely recapture) */
 	size_t target = ( SM_SHARED_BYTES / (size_t)tc.perSM - 2048u ) / 256u * 256u;
+	target = target < CTA_SHARED_MAX ? target : CTA_SHARED_MAX;
 	int top = 0;
 	for ( int i = 0; i < n; ++i )
 		if ( b->hItems[i].solve )
@@ -722,10 +742,15 @@ extern "C" int b2gd_batch_solve( b2gBatch* b, int n )
 		cudaMemsetAsync( b->dQueue, 0, sizeof( int ), b->stream );
 		k_batch_tape<<<b->sms * 4, BATCH_GRID_THREADS, 0, b->stream>>>( b->dItems, n );
 		tc.launch( b, grid, smem );
+		cudaError_t launch = cudaGetLastError();
 		cudaMemcpyAsync( b->hCounters, b->dCounters, sizeof( int ) * 4 * n, cudaMemcpyDeviceToHost, b->stream );
 		cudaError_t e = cudaStreamEndCapture( b->stream, &g );
-		if ( e != cudaSuccess )
-			return (int)e;
+		if ( launch != cudaSuccess || e != cudaSuccess )
+		{
+			if ( g )
+				cudaGraphDestroy( g );
+			return (int)( launch != cudaSuccess ? launch : e );
+		}
 		e = cudaGraphInstantiate( &b->solveExec[choice], g, 0 );
 		cudaGraphDestroy( g );
 		if ( e != cudaSuccess )

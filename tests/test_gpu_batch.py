@@ -43,7 +43,7 @@ def test_batch_matches_oracle_worlds(gpu, oracle):
                 err = _compare(gpu, oracle, wg, wo)
                 assert err is None, f"step {s}: {err}"
         stats = gpu.lib.b2World_GetBatchStats()
-        assert stats.solveThreads in (64, 128, 256)  # the autotuner has chosen
+        assert stats.solveThreads in (64, 128, 256, 512)  # the autotuner has chosen
         assert stats.launches == 4  # scatter, narrowphase, tape records, solver
     finally:
         for w in wg:
