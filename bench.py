@@ -427,7 +427,7 @@ def run_gpu(args):
     g.destroy(w)
 
     batch = run_batch(g, args.batch_steps, 5, args.batch_worlds) if args.batch_steps > 0 else None
-    tumbler = run_tumbler(g, cpu=not args.no_cpu) if not args.no_tumbler else None
+    tumbler = run_tumbler(g, steps=args.tumbler_steps, cpu=not args.no_cpu) if not args.no_tumbler else None
     adjoint = run_adjoint(g) if not args.no_adjoint else None
 
     if rank != 0:
@@ -481,13 +481,21 @@ def main():
     ap.add_argument("--batch-steps", type=int, default=30, help="batched-worlds steps to time (0: skip)")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the differentiable-stepping measurement")
     ap.add_argument("--no-tumbler", action="store_true", help="skip the tumbler measurement")
-    ap.add_argument("--part", default="all", choices=["all", "batch"],
-                    help="batch: only the batched-worlds measurement (for profiling), printed as its own line")
+    ap.add_argument("--part", default="all", choices=["all", "batch", "tumbler", "adjoint"],
+                    help="one workload only (for profiling), printed as its own line")
+    ap.add_argument("--tumbler-steps", type=int, default=1000, help="steps of the tumbler measurement")
     ap.add_argument("--batch-worlds", type=int, default=BATCH_WORLDS, help="worlds of the batched workload")
     args = ap.parse_args()
-    if args.part == "batch":
+    if args.part != "all":
         import box2c_gb300
-        print(json.dumps(run_batch(box2c_gb300.load(), args.batch_steps, args.warmup, args.batch_worlds)))
+        g = box2c_gb300.load()
+        if args.part == "batch":
+            out = run_batch(g, args.batch_steps, args.warmup, args.batch_worlds)
+        elif args.part == "tumbler":
+            out = run_tumbler(g, steps=args.tumbler_steps, cpu=not args.no_cpu)
+        else:
+            out = run_adjoint(g)
+        print(json.dumps(out))
         return
     if args.impl == "reference":
         run_reference(args)
