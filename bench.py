@@ -259,7 +259,8 @@ def run_batch(g, steps, warmup, n_worlds=BATCH_WORLDS):
         "worlds": n, "bodies": bodies, "steps": steps, "warmup": warm,
         "ms_per_batched_step": round(total * 1e3 / steps, 4),
         "device_ms": {"collide": round(float(np.mean(dev_c)), 4), "solve": round(float(np.mean(dev_s)), 4)},
-        "host_ms": dict(zip(("prepare", "narrowphase_wait", "events_lists", "solve_wait", "records"),
+        "host_ms": dict(zip(("prepare_first_half", "launch_prepare_rebuild", "narrowphase_wait_events_lists",
+                             "solver_wait_records", "end_of_step"),
                             [round(float(x), 4) for x in np.mean(np.array(prof), 0)])),
         "host_threads": st.hostThreads, "solve_cta_threads": st.solveThreads, "solve_ctas_per_sm": st.solveCtasPerSm,
         "gpu_launches_per_step": st.launches,

@@ -127,12 +127,19 @@ b2gBatchItem* b2gd_batch_items( b2gBatch* b, int count );
 void* b2gd_batch_stream( b2gBatch* b );
 /* Host copy of world i's 4 counters after the last sync. */
 const int* b2gd_batch_counters( b2gBatch* b, int i );
-/* Narrowphase of all items (contact records staged by b2gd_stage_contacts). */
-int b2gd_batch_collide( b2gBatch* b, int count );
-/* Solver stage and finalisation of all items with solve != 0: packs of similar-sized
- * worlds, each world on one warp, a group of warps or a whole CTA. */
-int b2gd_batch_solve( b2gBatch* b, int count );
-int b2gd_batch_sync( b2gBatch* b );
+/* A step's items run in halves (h = 0, 1: items [first, first + count)), each with its
+ * own graphs, so that the host phases of one half overlap the device work of the other;
+ * everything is ordered on the batch's stream.  begin_step picks the solver's launch
+ * shape for the step; end_step waits for the stream and does the timing and tuning. */
+void b2gd_batch_begin_step( b2gBatch* b );
+/* Narrowphase of a half (contact records staged by b2gd_stage_contacts). */
+int b2gd_batch_collide( b2gBatch* b, int h, int first, int count );
+/* Solver stage and finalisation of a half's items with solve != 0: packs of
+ * similar-sized worlds, each world on one warp, a group of warps or a whole CTA. */
+int b2gd_batch_solve( b2gBatch* b, int h, int first, int count );
+int b2gd_batch_wait_collide( b2gBatch* b, int h );
+int b2gd_batch_wait_solve( b2gBatch* b, int h );
+int b2gd_batch_end_step( b2gBatch* b );
 /* Device milliseconds of the last batched narrowphase and solve, the solver's CTA size
  * and resident CTAs per SM, and the number of kernel launches. */
 void b2gd_batch_stats( b2gBatch* b, float* collideMs, float* solveMs, int* threads, int* ctasPerSm, int* launches );

@@ -15,6 +15,9 @@
 #include <stdlib.h>
 #include <string.h>
 
+/* Below this many worlds per half a step is not split in two. */
+#define BATCH_MIN_HALF 64
+
 static b2gBatch* s_batch;
 static gWorld** s_worlds;
 static void** s_streams;
@@ -43,19 +46,21 @@ static void fill_item( b2gBatchItem* it, gWorld* w )
 	it->bodyIdCount = w->bodyIds.next;
 }
 
+/* One half of the step's worlds: s_worlds[first .. first + count). */
 typedef struct BatchCtx
 {
 	b2gBatchItem* items;
 	void* stream;
 	float timeStep;
 	int subStepCount;
+	int first, count;
 	int error;
 } BatchCtx;
 
 static void begin_worlds( int begin, int end, void* arg )
 {
 	BatchCtx* c = (BatchCtx*)arg;
-	for ( int k = begin; k < end; ++k )
+	for ( int k = c->first + begin; k < c->first + end; ++k )
 	{
 		gWorld* w = s_worlds[k];
 		b2gBatchItem* it = c->items + k;
@@ -84,8 +89,8 @@ static void begin_worlds( int begin, int end, void* arg )
 
 static void rebuild_worlds( int begin, int end, void* arg )
 {
-	(void)arg;
-	for ( int k = begin; k < end; ++k )
+	BatchCtx* c = (BatchCtx*)arg;
+	for ( int k = c->first + begin; k < c->first + end; ++k )
 		if ( s_worlds[k]->status == 0 )
 			gstep_rebuild_trees( s_worlds[k] );
 }
@@ -93,7 +98,7 @@ static void rebuild_worlds( int begin, int end, void* arg )
 static void middle_worlds( int begin, int end, void* arg )
 {
 	BatchCtx* c = (BatchCtx*)arg;
-	for ( int k = begin; k < end; ++k )
+	for ( int k = c->first + begin; k < c->first + end; ++k )
 	{
 		gWorld* w = s_worlds[k];
 		b2gBatchItem* it = c->items + k;
@@ -140,7 +145,7 @@ static void middle_worlds( int begin, int end, void* arg )
 static void finish_worlds( int begin, int end, void* arg )
 {
 	BatchCtx* c = (BatchCtx*)arg;
-	for ( int k = begin; k < end; ++k )
+	for ( int k = c->first + begin; k < c->first + end; ++k )
 	{
 		gWorld* w = s_worlds[k];
 		if ( c->error != 0 && w->status == 0 )
@@ -189,36 +194,61 @@ void b2World_StepBatch( const b2WorldId* worldIds, int count, float timeStep, in
 	}
 	if ( n == 0 )
 		return;
-	BatchCtx c;
-	c.items = b2gd_batch_items( s_batch, n );
-	c.stream = b2gd_batch_stream( s_batch );
-	c.timeStep = timeStep;
-	c.subStepCount = subStepCount;
-	c.error = 0;
-	if ( c.items == NULL )
+	b2gBatchItem* items = b2gd_batch_items( s_batch, n );
+	if ( items == NULL )
 	{
 		for ( int k = 0; k < n; ++k )
 			s_worlds[k]->locked = false;
 		return;
 	}
+	/* two halves (one when there are few worlds): the host phases of one half run while
+	 * the device works on the other */
+	BatchCtx c[2];
+	int split = n >= 2 * BATCH_MIN_HALF ? n / 2 : n;
+	for ( int h = 0; h < 2; ++h )
+	{
+		c[h].items = items;
+		c[h].stream = b2gd_batch_stream( s_batch );
+		c[h].timeStep = timeStep;
+		c[h].subStepCount = subStepCount;
+		c[h].first = h == 0 ? 0 : split;
+		c[h].count = h == 0 ? split : n - split;
+		c[h].error = 0;
+	}
 	const int grain = 16;
+	b2gd_batch_begin_step( s_batch );
 
 	double t0 = b2g_now_ms();
-	gpool_for( n, grain, begin_worlds, &c );
+	gpool_for( c[0].count, grain, begin_worlds, &c[0] );
 	double t1 = b2g_now_ms();
-	int e = b2gd_batch_collide( s_batch, n );
-	gpool_for( n, grain, rebuild_worlds, &c );
-	e |= b2gd_batch_sync( s_batch );
+	c[0].error = b2gd_batch_collide( s_batch, 0, c[0].first, c[0].count );
+	gpool_for( c[1].count, grain, begin_worlds, &c[1] );
+	c[1].error = b2gd_batch_collide( s_batch, 1, c[1].first, c[1].count );
+	gpool_for( c[0].count, grain, rebuild_worlds, &c[0] );
+	gpool_for( c[1].count, grain, rebuild_worlds, &c[1] );
 	double t2 = b2g_now_ms();
-	c.error = e;
-	gpool_for( n, grain, middle_worlds, &c );
+	for ( int h = 0; h < 2; ++h )
+	{
+		c[h].error |= b2gd_batch_wait_collide( s_batch, h );
+		gpool_for( c[h].count, grain, middle_worlds, &c[h] );
+		if ( c[h].error == 0 )
+			c[h].error = b2gd_batch_solve( s_batch, h, c[h].first, c[h].count );
+	}
 	double t3 = b2g_now_ms();
-	e = b2gd_batch_solve( s_batch, n );
-	e |= b2gd_batch_sync( s_batch );
+	for ( int h = 0; h < 2; ++h )
+	{
+		c[h].error |= b2gd_batch_wait_solve( s_batch, h );
+		gpool_for( c[h].count, grain, finish_worlds, &c[h] );
+	}
 	double t4 = b2g_now_ms();
-	c.error = e;
-	gpool_for( n, grain, finish_worlds, &c );
+	int e = b2gd_batch_end_step( s_batch );
 	double t5 = b2g_now_ms();
+	if ( e != 0 )
+	{
+		for ( int k = 0; k < n; ++k )
+			if ( s_worlds[k]->status == 0 )
+				s_worlds[k]->status = e;
+	}
 	s_hostMs[0] = (float)( t1 - t0 );
 	s_hostMs[1] = (float)( t2 - t1 );
 	s_hostMs[2] = (float)( t3 - t2 );

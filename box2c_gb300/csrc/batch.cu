@@ -30,10 +30,33 @@
 #define BATCH_GRID_THREADS 256
 #define TUNE_CANDIDATES 6
 #define TUNE_SAMPLES 2
+#define B2G_BATCH_HALVES 2
 #define SM_SHARED_BYTES ( 228u * 1024u ) /* shared memory of one SM */
 /* dynamic shared memory one solver CTA may take: the 227 KB opt-in limit covers the
  * kernel's static shared memory too (up to 1.4 KB), so leave room for it */
 #define CTA_SHARED_MAX ( 222u * 1024u )
+
+/* One half of a batched step's worlds: its own graphs, prefix sums, packs, queue and
+ * timing events, so that the host phases of one half overlap the other's device work. */
+struct BatchHalf
+{
+	int* hPrefix; /* scatter prefix [n+1], then narrowphase prefix [n+1] */
+	int* dPrefix;
+	int* hOrder; /* [0] = packs to solve, then PACK_INTS ints per pack; then scratch */
+	int* dOrder;
+	int* hScratch; /* 5 ints per item */
+	int* dQueue;
+	cudaEvent_t ev[4]; /* narrowphase start / end, solver start / end */
+
+	cudaGraphExec_t collideExec;
+	int collideFirst, collideN;
+	cudaGraphExec_t solveExec[TUNE_CANDIDATES];
+	int solveFirst[TUNE_CANDIDATES];
+	int solveN[TUNE_CANDIDATES];
+	int solveSmem[TUNE_CANDIDATES];
+	int solvePerSm[TUNE_CANDIDATES]; /* resident CTAs per SM of each captured launch */
+	int collideTimed, solveTimed;
+};
 
 struct b2gBatch
 {
@@ -41,30 +64,17 @@ struct b2gBatch
 	int capacity;
 	b2gBatchItem* hItems;
 	b2gBatchItem* dItems;
-	int* hPrefix; /* scatter prefix [n+1], then narrowphase prefix [n+1] */
-	int* dPrefix;
-	int* hOrder; /* [0] = packs to solve, then PACK_INTS ints per pack; then scratch */
-	int* dOrder;
-	int* hScratch; /* 5 ints per item */
 	int* hCounters; /* 4 per item */
 	int* dCounters;
-	int* dQueue;
 	int sms;
-	cudaEvent_t ev[4];
-
-	cudaGraphExec_t collideExec;
-	int collideN;
-	cudaGraphExec_t solveExec[TUNE_CANDIDATES];
-	int solveN[TUNE_CANDIDATES];
-	int solveSmem[TUNE_CANDIDATES];
-	int solvePerSm[TUNE_CANDIDATES]; /* resident CTAs per SM of each captured launch */
+	BatchHalf half[B2G_BATCH_HALVES];
 
 	int tuned, choice, tuneStep;
 	float tuneMs[TUNE_CANDIDATES];
 	float collideMs, solveMs;
 	int launches;
-	int collideTimed, solveTimed;
 };
+
 
 /* largest w with prefix[w] <= t, given prefix[0] <= t < prefix[n] */
 __device__ __forceinline__ int find_world( const int* prefix, int n, int t )
@@ -92,7 +102,7 @@ __global__ void __launch_bounds__( BATCH_GRID_THREADS ) k_batch_scatter( const b
 	}
 }
 
-__global__ void __launch_bounds__( BATCH_GRID_THREADS ) k_batch_collide( const b2gBatchItem* items, const int* prefix, int n )
+__global__ void __launch_bounds__( BATCH_GRID_THREADS, 4 ) k_batch_collide( const b2gBatchItem* items, const int* prefix, int n )
 {
 	int total = prefix[n];
 	for ( int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x )
@@ -417,9 +427,9 @@ static int solve_occupancy( size_t smem )
 }
 
 template <int T, int MINB>
-static void launch_solve( b2gBatch* b, int grid, size_t smem )
+static void launch_solve( b2gBatch* b, int grid, size_t smem, const int* packs, int* queue )
 {
-	k_batch_solve<T, MINB><<<grid, T, smem, b->stream>>>( b->dItems, b->dOrder, b->dQueue, (int)( smem / 16u ) );
+	k_batch_solve<T, MINB><<<grid, T, smem, b->stream>>>( b->dItems, packs, queue, (int)( smem / 16u ) );
 }
 
 /* Solver launch shapes tried on the first steps: threads per CTA and CTAs per SM (which
@@ -428,7 +438,7 @@ struct TuneCandidate
 {
 	int threads, perSM;
 	int ( *occupancy )( size_t smem );
-	void ( *launch )( b2gBatch* b, int grid, size_t smem );
+	void ( *launch )( b2gBatch* b, int grid, size_t smem, const int* packs, int* queue );
 };
 #define TUNE_SHAPE( T, B ) { T, B, solve_occupancy<T, B>, launch_solve<T, B> }
 static const TuneCandidate s_tune[TUNE_CANDIDATES] = { TUNE_SHAPE( 128, 6 ), TUNE_SHAPE( 512, 1 ), TUNE_SHAPE( 128, 8 ),
@@ -448,38 +458,50 @@ extern "C" b2gBatch* b2gd_batch_create( void )
 	int dev = 0;
 	cudaGetDevice( &dev );
 	cudaDeviceGetAttribute( &b->sms, cudaDevAttrMultiProcessorCount, dev );
-	for ( int i = 0; i < 4; ++i )
-		cudaEventCreate( &b->ev[i] );
-	cudaMalloc( &b->dQueue, sizeof( int ) * 8 );
+	for ( int h = 0; h < B2G_BATCH_HALVES; ++h )
+	{
+		for ( int i = 0; i < 4; ++i )
+			cudaEventCreate( &b->half[h].ev[i] );
+		cudaMalloc( &b->half[h].dQueue, sizeof( int ) );
+	}
 	return b;
 }
 
 static void release_graphs( b2gBatch* b )
 {
-	if ( b->collideExec )
-		cudaGraphExecDestroy( b->collideExec );
-	b->collideExec = nullptr;
-	for ( int i = 0; i < TUNE_CANDIDATES; ++i )
+	for ( int h = 0; h < B2G_BATCH_HALVES; ++h )
 	{
-		if ( b->solveExec[i] )
-			cudaGraphExecDestroy( b->solveExec[i] );
-		b->solveExec[i] = nullptr;
+		BatchHalf& H = b->half[h];
+		if ( H.collideExec )
+			cudaGraphExecDestroy( H.collideExec );
+		H.collideExec = nullptr;
+		for ( int i = 0; i < TUNE_CANDIDATES; ++i )
+		{
+			if ( H.solveExec[i] )
+				cudaGraphExecDestroy( H.solveExec[i] );
+			H.solveExec[i] = nullptr;
+		}
 	}
 }
 
 static void release_buffers( b2gBatch* b )
 {
 	cudaFreeHost( b->hItems );
-	cudaFreeHost( b->hPrefix );
-	cudaFreeHost( b->hOrder );
-	cudaFreeHost( b->hScratch );
 	cudaFreeHost( b->hCounters );
 	cudaFree( b->dItems );
-	cudaFree( b->dPrefix );
-	cudaFree( b->dOrder );
 	cudaFree( b->dCounters );
 	b->hItems = b->dItems = nullptr;
-	b->hPrefix = b->dPrefix = b->hOrder = b->dOrder = b->hScratch = b->hCounters = b->dCounters = nullptr;
+	b->hCounters = b->dCounters = nullptr;
+	for ( int h = 0; h < B2G_BATCH_HALVES; ++h )
+	{
+		BatchHalf& H = b->half[h];
+		cudaFreeHost( H.hPrefix );
+		cudaFreeHost( H.hOrder );
+		cudaFreeHost( H.hScratch );
+		cudaFree( H.dPrefix );
+		cudaFree( H.dOrder );
+		H.hPrefix = H.dPrefix = H.hOrder = H.dOrder = H.hScratch = nullptr;
+	}
 	b->capacity = 0;
 }
 
@@ -490,9 +512,12 @@ extern "C" void b2gd_batch_destroy( b2gBatch* b )
 	cudaStreamSynchronize( b->stream );
 	release_graphs( b );
 	release_buffers( b );
-	cudaFree( b->dQueue );
-	for ( int i = 0; i < 4; ++i )
-		cudaEventDestroy( b->ev[i] );
+	for ( int h = 0; h < B2G_BATCH_HALVES; ++h )
+	{
+		cudaFree( b->half[h].dQueue );
+		for ( int i = 0; i < 4; ++i )
+			cudaEventDestroy( b->half[h].ev[i] );
+	}
 	cudaStreamDestroy( b->stream );
 	free( b );
 }
@@ -507,14 +532,18 @@ extern "C" b2gBatchItem* b2gd_batch_items( b2gBatch* b, int count )
 	int cap = count < 64 ? 64 : count;
 	size_t ints = (size_t)cap + 1;
 	bool ok = cudaMallocHost( &b->hItems, sizeof( b2gBatchItem ) * cap ) == cudaSuccess &&
-			  cudaMallocHost( &b->hPrefix, sizeof( int ) * 2 * ints ) == cudaSuccess &&
-			  cudaMallocHost( &b->hOrder, sizeof( int ) * ( 1u + 2u * PACK_INTS * ints ) ) == cudaSuccess && /* packs + scratch */
-			  cudaMallocHost( &b->hScratch, sizeof( int ) * 5u * ints ) == cudaSuccess &&
 			  cudaMallocHost( &b->hCounters, sizeof( int ) * 4 * cap ) == cudaSuccess &&
 			  cudaMalloc( &b->dItems, sizeof( b2gBatchItem ) * cap ) == cudaSuccess &&
-			  cudaMalloc( &b->dPrefix, sizeof( int ) * 2 * ints ) == cudaSuccess &&
-			  cudaMalloc( &b->dOrder, sizeof( int ) * ( 1u + PACK_INTS * ints ) ) == cudaSuccess &&
 			  cudaMalloc( &b->dCounters, sizeof( int ) * 4 * cap ) == cudaSuccess;
+	for ( int h = 0; h < B2G_BATCH_HALVES && ok; ++h )
+	{
+		BatchHalf& H = b->half[h];
+		ok = cudaMallocHost( &H.hPrefix, sizeof( int ) * 2 * ints ) == cudaSuccess &&
+			 cudaMallocHost( &H.hOrder, sizeof( int ) * ( 1u + 2u * PACK_INTS * ints ) ) == cudaSuccess && /* packs + scratch */
+			 cudaMallocHost( &H.hScratch, sizeof( int ) * 5u * ints ) == cudaSuccess &&
+			 cudaMalloc( &H.dPrefix, sizeof( int ) * 2 * ints ) == cudaSuccess &&
+			 cudaMalloc( &H.dOrder, sizeof( int ) * ( 1u + PACK_INTS * ints ) ) == cudaSuccess;
+	}
 	if ( ok == false )
 	{
 		release_buffers( b );
@@ -537,81 +566,102 @@ extern "C" int b2gd_stage_contacts( b2gDevWorld* w, b2gHostIO* io, int count )
 								 cudaMemcpyHostToDevice, (cudaStream_t)w->stream );
 }
 
-static void point_counters( b2gBatch* b, int n )
+static void point_counters( b2gBatch* b, int first, int count )
 {
-	for ( int i = 0; i < n; ++i )
+	for ( int i = first; i < first + count; ++i )
 		b->hItems[i].W.counters = b->dCounters + 4 * i;
 }
 
-extern "C" int b2gd_batch_collide( b2gBatch* b, int n )
+/* Ends a capture; on a failed launch or capture nothing is instantiated. */
+static cudaError_t finish_capture( cudaStream_t s, cudaError_t launch, cudaGraphExec_t* exec )
+{
+	cudaGraph_t g = nullptr;
+	cudaError_t e = cudaStreamEndCapture( s, &g );
+	if ( launch != cudaSuccess || e != cudaSuccess )
+	{
+		if ( g )
+			cudaGraphDestroy( g );
+		return launch != cudaSuccess ? launch : e;
+	}
+	e = cudaGraphInstantiate( exec, g, 0 );
+	cudaGraphDestroy( g );
+	return e;
+}
+
+extern "C" void b2gd_batch_begin_step( b2gBatch* b )
+{
+	b->choice = b->tuned ? b->choice : ( b->tuneStep / TUNE_SAMPLES ) % TUNE_CANDIDATES;
+	b->launches = 0;
+	for ( int h = 0; h < B2G_BATCH_HALVES; ++h )
+		b->half[h].collideTimed = b->half[h].solveTimed = 0;
+}
+
+extern "C" int b2gd_batch_collide( b2gBatch* b, int h, int first, int n )
 {
 	if ( n <= 0 )
 		return 0;
-	point_counters( b, n );
-	int* ps = b->hPrefix;
-	int* pc = b->hPrefix + n + 1;
+	BatchHalf& H = b->half[h];
+	point_counters( b, first, n );
+	int* ps = H.hPrefix;
+	int* pc = H.hPrefix + n + 1;
 	ps[0] = 0;
 	pc[0] = 0;
 	for ( int i = 0; i < n; ++i )
 	{
-		ps[i + 1] = ps[i] + b->hItems[i].staged;
-		pc[i + 1] = pc[i] + b->hItems[i].idCount;
+		ps[i + 1] = ps[i] + b->hItems[first + i].staged;
+		pc[i + 1] = pc[i] + b->hItems[first + i].idCount;
 	}
-	if ( b->collideExec == nullptr || b->collideN != n )
+	if ( H.collideExec == nullptr || H.collideN != n || H.collideFirst != first )
 	{
-		if ( b->collideExec )
-			cudaGraphExecDestroy( b->collideExec );
-		b->collideExec = nullptr;
+		if ( H.collideExec )
+			cudaGraphExecDestroy( H.collideExec );
+		H.collideExec = nullptr;
 		int grid = b->sms * 8;
-		cudaGraph_t g = nullptr;
+		const b2gBatchItem* items = b->dItems + first;
+		cudaGetLastError();
 		cudaStreamBeginCapture( b->stream, cudaStreamCaptureModeThreadLocal );
-		cudaMemcpyAsync( b->dItems, b->hItems, sizeof( b2gBatchItem ) * n, cudaMemcpyHostToDevice, b->stream );
-		cudaMemcpyAsync( b->dPrefix, b->hPrefix, sizeof( int ) * 2 * ( n + 1 ), cudaMemcpyHostToDevice, b->stream );
-		cudaMemsetAsync( b->dCounters, 0, sizeof( int ) * 4 * n, b->stream );
-		k_batch_scatter<<<grid, BATCH_GRID_THREADS, 0, b->stream>>>( b->dItems, b->dPrefix, n );
-		k_batch_collide<<<grid, BATCH_GRID_THREADS, 0, b->stream>>>( b->dItems, b->dPrefix + n + 1, n );
+		cudaMemcpyAsync( b->dItems + first, b->hItems + first, sizeof( b2gBatchItem ) * n, cudaMemcpyHostToDevice, b->stream );
+		cudaMemcpyAsync( H.dPrefix, H.hPrefix, sizeof( int ) * 2 * ( n + 1 ), cudaMemcpyHostToDevice, b->stream );
+		cudaMemsetAsync( b->dCounters + 4 * first, 0, sizeof( int ) * 4 * n, b->stream );
+		k_batch_scatter<<<grid, BATCH_GRID_THREADS, 0, b->stream>>>( items, H.dPrefix, n );
+		k_batch_collide<<<grid, BATCH_GRID_THREADS, 0, b->stream>>>( items, H.dPrefix + n + 1, n );
 		cudaError_t launch = cudaGetLastError();
-		cudaMemcpyAsync( b->hCounters, b->dCounters, sizeof( int ) * 4 * n, cudaMemcpyDeviceToHost, b->stream );
-		cudaError_t e = cudaStreamEndCapture( b->stream, &g );
-		if ( launch != cudaSuccess || e != cudaSuccess )
-		{
-			if ( g )
-				cudaGraphDestroy( g );
-			return (int)( launch != cudaSuccess ? launch : e );
-		}
-		e = cudaGraphInstantiate( &b->collideExec, g, 0 );
-		cudaGraphDestroy( g );
+		cudaMemcpyAsync( b->hCounters + 4 * first, b->dCounters + 4 * first, sizeof( int ) * 4 * n, cudaMemcpyDeviceToHost, b->stream );
+		cudaError_t e = finish_capture( b->stream, launch, &H.collideExec );
 		if ( e != cudaSuccess )
 			return (int)e;
-		b->collideN = n;
+		H.collideN = n;
+		H.collideFirst = first;
 	}
-	cudaEventRecord( b->ev[0], b->stream );
-	cudaError_t e = cudaGraphLaunch( b->collideExec, b->stream );
-	cudaEventRecord( b->ev[1], b->stream );
-	b->collideTimed = 1;
-	b->launches = 2;
+	cudaEventRecord( H.ev[0], b->stream );
+	cudaError_t e = cudaGraphLaunch( H.collideExec, b->stream );
+	cudaEventRecord( H.ev[1], b->stream );
+	H.collideTimed = 1;
+	b->launches += 2;
 	return (int)e;
 }
 
-/* Builds the packs of this step into hOrder for CTAs of T threads with smem bytes of
- * shared memory: each world gets the smallest group (32, 64, 128 or T threads) that
- * covers its widest colour in two passes and holds its bodies in the group's share of
- * shared memory, and keeps its rows on chip when they fit there too.  Worlds of one
- * group size are packed largest first; packs go into the queue by their longest world
- * (colours x passes), then alternating from both ends.  Returns the number of packs. */
-static int build_packs( b2gBatch* b, int n, int T, size_t smem )
+/* Builds the packs of items [first, first + n) into the half's hOrder for CTAs of T
+ * threads with smem bytes of shared memory.  Each world gets the smallest group (32 ..
+ * T threads, powers of two) that holds its bodies in the group's share of shared
+ * memory and covers its widest colour in two passes when its rows fit in that share too
+ * (they are then kept on chip), in one pass otherwise.  Worlds of one group size are
+ * packed largest first; packs go into the queue by their longest world (colours x
+ * passes), then alternating from both ends.  Returns the number of packs. */
+static int build_packs( b2gBatch* b, BatchHalf& H, int first, int n, int T, size_t smem )
 {
-	int* groupOf = b->hScratch;			 /* per item: group size, 0 when not solved */
-	int* byGroup = b->hScratch + n;		 /* items by group size, largest first */
-	int* packCost = b->hScratch + 2 * n; /* per pack */
-	int* sizeKey = b->hScratch + 3 * n;	 /* per item: body count */
-	int* cost = b->hScratch + 4 * n;	 /* per item: colours x passes */
-	int* packs = b->hOrder + 1;
-	int* tmp = b->hOrder + 1 + PACK_INTS * n;
+	/* per item of the half (local index): */
+	int* groupOf = H.hScratch;			 /* group size, 0 when not solved */
+	int* byGroup = H.hScratch + n;		 /* local indices by group size, largest first */
+	int* packCost = H.hScratch + 2 * n; /* per pack */
+	int* sizeKey = H.hScratch + 3 * n;	 /* body count */
+	int* cost = H.hScratch + 4 * n;	 /* colours x passes */
+	int* packs = H.hOrder + 1;
+	int* tmp = H.hOrder + 1 + PACK_INTS * n;
 	int top = 1;
 	for ( int i = 0; i < n; ++i )
 	{
-		b2gBatchItem& it = b->hItems[i];
+		b2gBatchItem& it = b->hItems[first + i];
 		it.rowsOnChip = 0;
 		groupOf[i] = 0;
 		if ( it.solve == 0 )
@@ -670,9 +720,10 @@ static int build_packs( b2gBatch* b, int n, int T, size_t smem )
 		for ( int j = 0; j < PACK_WORLDS; ++j )
 		{
 			bool take = j < T / g && k < m && groupOf[byGroup[k]] == g;
-			p[1 + j] = take ? byGroup[k++] : -1;
+			int li = take ? byGroup[k++] : -1;
+			p[1 + j] = take ? first + li : -1;
 			if ( take )
-				most = cost[p[1 + j]] > most ? cost[p[1 + j]] : most;
+				most = cost[li] > most ? cost[li] : most;
 		}
 		packCost[P++] = most;
 		costTop = most > costTop ? most : costTop;
@@ -697,16 +748,17 @@ static int build_packs( b2gBatch* b, int n, int T, size_t smem )
 		int q = ( i & 1 ) == 0 ? sorted[lo++] : sorted[hi--];
 		memcpy( packs + PACK_INTS * i, tmp + PACK_INTS * q, sizeof( int ) * PACK_INTS );
 	}
-	b->hOrder[0] = P;
+	H.hOrder[0] = P;
 	return P;
 }
 
-extern "C" int b2gd_batch_solve( b2gBatch* b, int n )
+extern "C" int b2gd_batch_solve( b2gBatch* b, int h, int first, int n )
 {
 	if ( n <= 0 )
 		return 0;
-	point_counters( b, n );
-	int choice = b->tuned ? b->choice : ( b->tuneStep / TUNE_SAMPLES ) % TUNE_CANDIDATES;
+	BatchHalf& H = b->half[h];
+	point_counters( b, first, n );
+	const int choice = b->choice;
 	const TuneCandidate tc = s_tune[choice];
 	/* shared memory per CTA: the candidate's share of the SM (less the per-CTA
 	 * reservation), or more when the largest world needs it for its bodies (rounded up
@@ -714,95 +766,111 @@ extern "C" int b2gd_batch_solve( b2gBatch* b, int n )
 	size_t target = ( SM_SHARED_BYTES / (size_t)tc.perSM - 2048u ) / 256u * 256u;
 	target = target < CTA_SHARED_MAX ? target : CTA_SHARED_MAX;
 	int top = 0;
-	for ( int i = 0; i < n; ++i )
+	for ( int i = first; i < first + n; ++i )
 		if ( b->hItems[i].solve )
 			top = b->hItems[i].bodyIdCount > top ? b->hItems[i].bodyIdCount : top;
 	size_t smem = 16u * (size_t)body_float4s( ( top + 255 ) / 256 * 256 );
 	smem = smem > target ? smem : target;
 	if ( smem > CTA_SHARED_MAX )
 		return (int)cudaErrorInvalidValue;
-	build_packs( b, n, tc.threads, smem );
+	build_packs( b, H, first, n, tc.threads, smem );
 
-	if ( b->solveExec[choice] == nullptr || b->solveN[choice] != n || b->solveSmem[choice] != (int)smem )
+	if ( H.solveExec[choice] == nullptr || H.solveN[choice] != n || H.solveFirst[choice] != first || H.solveSmem[choice] != (int)smem )
 	{
-		if ( b->solveExec[choice] )
-			cudaGraphExecDestroy( b->solveExec[choice] );
-		b->solveExec[choice] = nullptr;
+		if ( H.solveExec[choice] )
+			cudaGraphExecDestroy( H.solveExec[choice] );
+		H.solveExec[choice] = nullptr;
 		int occ = tc.occupancy( smem );
 		if ( occ <= 0 )
 			return (int)cudaErrorInvalidConfiguration;
 		occ = occ < tc.perSM ? occ : tc.perSM;
-		b->solvePerSm[choice] = occ;
+		H.solvePerSm[choice] = occ;
 		int grid = b->sms * occ;
 		cudaGetLastError();
-		cudaGraph_t g = nullptr;
 		cudaStreamBeginCapture( b->stream, cudaStreamCaptureModeThreadLocal );
-		cudaMemcpyAsync( b->dItems, b->hItems, sizeof( b2gBatchItem ) * n, cudaMemcpyHostToDevice, b->stream );
-		cudaMemcpyAsync( b->dOrder, b->hOrder, sizeof( int ) * ( 1 + PACK_INTS * (size_t)n ), cudaMemcpyHostToDevice, b->stream );
-		cudaMemsetAsync( b->dQueue, 0, sizeof( int ), b->stream );
-		k_batch_tape<<<b->sms * 4, BATCH_GRID_THREADS, 0, b->stream>>>( b->dItems, n );
-		tc.launch( b, grid, smem );
+		cudaMemcpyAsync( b->dItems + first, b->hItems + first, sizeof( b2gBatchItem ) * n, cudaMemcpyHostToDevice, b->stream );
+		cudaMemcpyAsync( H.dOrder, H.hOrder, sizeof( int ) * ( 1 + PACK_INTS * (size_t)n ), cudaMemcpyHostToDevice, b->stream );
+		cudaMemsetAsync( H.dQueue, 0, sizeof( int ), b->stream );
+		k_batch_tape<<<b->sms * 4, BATCH_GRID_THREADS, 0, b->stream>>>( b->dItems + first, n );
+		tc.launch( b, grid, smem, H.dOrder, H.dQueue );
 		cudaError_t launch = cudaGetLastError();
-		cudaMemcpyAsync( b->hCounters, b->dCounters, sizeof( int ) * 4 * n, cudaMemcpyDeviceToHost, b->stream );
-		cudaError_t e = cudaStreamEndCapture( b->stream, &g );
-		if ( launch != cudaSuccess || e != cudaSuccess )
-		{
-			if ( g )
-				cudaGraphDestroy( g );
-			return (int)( launch != cudaSuccess ? launch : e );
-		}
-		e = cudaGraphInstantiate( &b->solveExec[choice], g, 0 );
-		cudaGraphDestroy( g );
+		cudaMemcpyAsync( b->hCounters + 4 * first, b->dCounters + 4 * first, sizeof( int ) * 4 * n, cudaMemcpyDeviceToHost, b->stream );
+		cudaError_t e = finish_capture( b->stream, launch, &H.solveExec[choice] );
 		if ( e != cudaSuccess )
 			return (int)e;
-		b->solveN[choice] = n;
-		b->solveSmem[choice] = (int)smem;
+		H.solveN[choice] = n;
+		H.solveFirst[choice] = first;
+		H.solveSmem[choice] = (int)smem;
 	}
-	cudaEventRecord( b->ev[2], b->stream );
-	cudaError_t e = cudaGraphLaunch( b->solveExec[choice], b->stream );
-	cudaEventRecord( b->ev[3], b->stream );
-	b->choice = choice;
-	b->solveTimed = 1;
+	cudaEventRecord( H.ev[2], b->stream );
+	cudaError_t e = cudaGraphLaunch( H.solveExec[choice], b->stream );
+	cudaEventRecord( H.ev[3], b->stream );
+	H.solveTimed = 1;
 	b->launches += 2; /* tape records, solver */
 	return (int)e;
 }
 
-extern "C" int b2gd_batch_sync( b2gBatch* b )
+extern "C" int b2gd_batch_wait_collide( b2gBatch* b, int h )
+{
+	if ( b->half[h].collideTimed == 0 )
+		return 0;
+	return (int)cudaEventSynchronize( b->half[h].ev[1] );
+}
+
+extern "C" int b2gd_batch_wait_solve( b2gBatch* b, int h )
+{
+	if ( b->half[h].solveTimed == 0 )
+		return 0;
+	return (int)cudaEventSynchronize( b->half[h].ev[3] );
+}
+
+extern "C" int b2gd_batch_end_step( b2gBatch* b )
 {
 	cudaError_t e = cudaStreamSynchronize( b->stream );
 	if ( e != cudaSuccess )
 		return (int)e;
-	if ( b->collideTimed )
-		cudaEventElapsedTime( &b->collideMs, b->ev[0], b->ev[1] );
-	if ( b->solveTimed )
+	float collide = 0.0f, solve = 0.0f;
+	int solved = 0;
+	for ( int h = 0; h < B2G_BATCH_HALVES; ++h )
 	{
-		cudaEventElapsedTime( &b->solveMs, b->ev[2], b->ev[3] );
-		if ( b->tuned == 0 )
+		BatchHalf& H = b->half[h];
+		float ms = 0.0f;
+		if ( H.collideTimed && cudaEventElapsedTime( &ms, H.ev[0], H.ev[1] ) == cudaSuccess )
+			collide += ms;
+		if ( H.solveTimed && cudaEventElapsedTime( &ms, H.ev[2], H.ev[3] ) == cudaSuccess )
 		{
-			/* the later sample of each candidate counts */
-			if ( b->tuneStep % TUNE_SAMPLES == TUNE_SAMPLES - 1 )
-				b->tuneMs[b->choice] = b->solveMs;
-			b->tuneStep += 1;
-			if ( b->tuneStep == TUNE_SAMPLES * TUNE_CANDIDATES )
+			solve += ms;
+			solved = 1;
+		}
+	}
+	b->collideMs = collide;
+	b->solveMs = solve;
+	if ( solved && b->tuned == 0 )
+	{
+		/* the later sample of each candidate counts */
+		if ( b->tuneStep % TUNE_SAMPLES == TUNE_SAMPLES - 1 )
+			b->tuneMs[b->choice] = solve;
+		b->tuneStep += 1;
+		if ( b->tuneStep == TUNE_SAMPLES * TUNE_CANDIDATES )
+		{
+			int best = 0;
+			for ( int i = 1; i < TUNE_CANDIDATES; ++i )
+				best = b->tuneMs[i] < b->tuneMs[best] ? i : best;
+			b->choice = best;
+			b->tuned = 1;
+			for ( int h = 0; h < B2G_BATCH_HALVES; ++h )
 			{
-				int best = 0;
-				for ( int i = 1; i < TUNE_CANDIDATES; ++i )
-					best = b->tuneMs[i] < b->tuneMs[best] ? i : best;
-				b->choice = best;
-				b->tuned = 1;
 				for ( int i = 0; i < TUNE_CANDIDATES; ++i )
 				{
-					if ( i != best && b->solveExec[i] )
+					if ( i != best && b->half[h].solveExec[i] )
 					{
-						cudaGraphExecDestroy( b->solveExec[i] );
-						b->solveExec[i] = nullptr;
+						cudaGraphExecDestroy( b->half[h].solveExec[i] );
+						b->half[h].solveExec[i] = nullptr;
 					}
 				}
 			}
 		}
 	}
-	b->collideTimed = 0;
-	b->solveTimed = 0;
 	return (int)cudaGetLastError();
 }
 
@@ -811,6 +879,6 @@ extern "C" void b2gd_batch_stats( b2gBatch* b, float* collideMs, float* solveMs,
 	*collideMs = b->collideMs;
 	*solveMs = b->solveMs;
 	*threads = b->tuned ? s_tune[b->choice].threads : 0;
-	*ctasPerSm = b->tuned ? b->solvePerSm[b->choice] : 0;
+	*ctasPerSm = b->tuned ? b->half[0].solvePerSm[b->choice] : 0;
 	*launches = b->launches;
 }

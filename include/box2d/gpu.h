@@ -54,11 +54,14 @@ B2_API void b2World_EnableFusedSolver( b2WorldId worldId, bool flag );
  * skipped.  Not thread-safe: one batch at a time per process. */
 B2_API void b2World_StepBatch( const b2WorldId* worldIds, int count, float timeStep, int subStepCount );
 
-/* Device milliseconds of the last batched step's narrowphase and solver segments, the
- * solver CTA size and resident CTAs per SM picked by the autotuner (0 while it is still
- * timing candidates), the kernel launches of the last batched step, and its host
- * milliseconds per phase: world preparation, narrowphase (host tree rebuilds and the
- * wait), events and solve lists, solver wait, finalisation records; per-world host work
+/* Device milliseconds of the last batched step's narrowphase and solver segments (both
+ * halves), the solver CTA size and resident CTAs per SM picked by the autotuner (0 while
+ * it is still timing candidates), the kernel launches of the last batched step, and its
+ * host milliseconds per segment.  A step runs its worlds in two halves so that one
+ * half's host work overlaps the other's device work; the segments are: preparation of
+ * the first half; its narrowphase launch, the second half's preparation and launch and
+ * the tree rebuilds; the narrowphase waits, events and solve lists and solver launches;
+ * the solver waits and finalisation records; the end of the step.  Per-world host work
  * runs on hostThreads threads. */
 typedef struct b2BatchStats
 {
