@@ -73,6 +73,10 @@ int b2gd_download_joints( b2gDevWorld* w, b2gJointDev* joints, int count );
  * record count back.  b2gd_sync waits for the stream; returns 0 or a CUDA error. */
 int b2gd_collide( b2gDevWorld* w, b2gHostIO* io, int newContactCount, int contactIdCount );
 int b2gd_solve( b2gDevWorld* w, b2gHostIO* io, const b2gSolvePlan* plan, const b2gStepConst* sc );
+/* The fused solver stage and finalisation launched before the narrowphase's events are
+ * known; they do nothing when there were events.  1 launched, 0 not (the world does not
+ * fit the fused solver), -1 launch error. */
+int b2gd_solve_speculative( b2gDevWorld* w, b2gHostIO* io, const b2gSolvePlan* plan, const b2gStepConst* sc );
 int b2gd_sync( b2gDevWorld* w );
 
 /* ---------------------------------------------------------------- broadphase query */

@@ -219,6 +219,9 @@ typedef struct b2gDevWorld
 	int launches;
 	int fused;	   /* use the fused cluster solver when the world fits on chip */
 	int fusedUsed; /* the last step's solver stage ran fused */
+	/* set for a solver stage launched before the host has seen the narrowphase's events:
+	 * its kernels return at once when the narrowphase reported any (counters[0] != 0) */
+	int guardEvents;
 	void* stage;   /* fused solver: per-CTA shared-memory images */
 	size_t stageBytes;
 } b2gDevWorld;

@@ -225,6 +225,8 @@ __device__ void run_stage( const b2gDevWorld& W, const FusedPlan& P, const Fused
  * src/solver.c:34-93) to global memory, one thread per row and per body id. */
 __global__ void __launch_bounds__( 256 ) k_fused_stage( b2gDevWorld W, FusedPlan P, b2gStepConst sc, float4* image )
 {
+	if ( W.guardEvents && W.counters[0] != 0 )
+		return;
 	int t = blockIdx.x * blockDim.x + threadIdx.x;
 	const int* cs = P.colorStart;
 	const int BS = P.bodySlots, RC = P.rowCap;
@@ -279,6 +281,9 @@ __global__ void __launch_bounds__( 256 ) k_fused_stage( b2gDevWorld W, FusedPlan
 template <int CL>
 __global__ void __launch_bounds__( FUSED_THREADS ) k_solve_fused( b2gDevWorld W, FusedPlan P, b2gStepConst sc, const float4* image )
 {
+	/* every CTA of the cluster takes the same branch: no barrier is left waiting */
+	if ( W.guardEvents && W.counters[0] != 0 )
+		return;
 	extern __shared__ float4 smem[];
 	__shared__ int awakeLocal;
 	cg::cluster_group cl = cg::this_cluster();

@@ -56,6 +56,8 @@ __global__ void __launch_bounds__( BLOCK ) k_prepare( b2gDevWorld W, int total, 
 
 __global__ void k_prepare_joints( b2gDevWorld W, int count, b2gStepConst sc )
 {
+	if ( W.guardEvents && W.counters[0] != 0 )
+		return;
 	int t = blockIdx.x * blockDim.x + threadIdx.x;
 	if ( t < count )
 		prepare_joint( W, t, sc );
@@ -84,6 +86,8 @@ __global__ void __launch_bounds__( BLOCK ) k_store( b2gDevWorld W, int total, in
 
 __global__ void __launch_bounds__( BLOCK ) k_finalize( b2gDevWorld W, int awakeCount, b2gStepConst sc )
 {
+	if ( W.guardEvents && W.counters[0] != 0 )
+		return;
 	int i = blockIdx.x * blockDim.x + threadIdx.x;
 	if ( i < awakeCount )
 		finalize_body( W, i, sc );
@@ -295,6 +299,40 @@ extern "C" int b2gd_solve( b2gDevWorld* w, b2gHostIO* io, const b2gSolvePlan* pl
 		cudaEventRecord( (cudaEvent_t)w->timers[5], s );
 	cudaMemcpyAsync( io->counters, w->counters, 4 * sizeof( int ), cudaMemcpyDeviceToHost, s );
 	return check( cudaGetLastError() );
+}
+
+/* The fused solver stage and finalisation launched right behind the narrowphase, before
+ * the host has read its events: with no event the colouring and solve lists are the
+ * ones the host would use, and the step needs no synchronisation in between; with an
+ * event every kernel returns at once and the host solves again after processing them.
+ * Returns 1 when launched, 0 when the world does not fit the fused solver (nothing
+ * launched), or -1 on a launch error. */
+extern "C" int b2gd_solve_speculative( b2gDevWorld* w, b2gHostIO* io, const b2gSolvePlan* plan, const b2gStepConst* scp )
+{
+	cudaStream_t s = (cudaStream_t)w->stream;
+	int awake = plan->awakeCount;
+	if ( w->fused == 0 || awake <= 0 )
+		return 0;
+	w->guardEvents = 1;
+	if ( w->timing )
+		cudaEventRecord( (cudaEvent_t)w->timers[3], s );
+	cudaMemsetAsync( w->counters + 1, 0, sizeof( int ), s );
+	int fused = b2gd_solver_fused( w, plan, scp );
+	if ( fused <= 0 )
+	{
+		w->guardEvents = 0;
+		return fused < 0 ? -1 : 0;
+	}
+	if ( w->timing )
+		cudaEventRecord( (cudaEvent_t)w->timers[4], s );
+	k_finalize<<<blocks_for( awake ), BLOCK, 0, s>>>( *w, awake, *scp );
+	if ( w->timing )
+		cudaEventRecord( (cudaEvent_t)w->timers[5], s );
+	cudaMemcpyAsync( io->counters, w->counters, 4 * sizeof( int ), cudaMemcpyDeviceToHost, s );
+	w->guardEvents = 0;
+	w->fusedUsed = 1;
+	w->launches += fused + 1;
+	return cudaGetLastError() == cudaSuccess ? 1 : -1;
 }
 
 /* ------------------------------------------------------------------ diagnostics */

@@ -748,18 +748,9 @@ void gstep_rebuild_trees( gWorld* w )
 
 /* Host work between the narrowphase and the solver: events in contact-id order, step
  * constants, solve lists.  Returns 1 when the solver stage has to run. */
-int gstep_after_collide( gWorld* w, float dt, int subSteps, b2gStepConst* sc, b2gSolvePlan* plan )
+/* Step constants (reference src/world.c:715-757). */
+static void step_constants( gWorld* w, float dt, int subSteps, b2gStepConst* sc )
 {
-	int eventCount = w->io.counters[0];
-	w->lastEventCount = eventCount;
-	process_events( w, eventCount < w->dev.eventCap ? eventCount : w->dev.eventCap );
-	double t2 = b2g_now_ms();
-	w->profile.collide = (float)( t2 - w->stepStart );
-	w->stepStart = t2;
-
-	if ( dt <= 0.0f )
-		return 0;
-
 	memset( sc, 0, sizeof( *sc ) );
 	sc->subSteps = subSteps < 1 ? 1 : subSteps;
 	sc->dt = dt;
@@ -778,6 +769,21 @@ int gstep_after_collide( gWorld* w, float dt, int subSteps, b2gStepConst* sc, b2
 	sc->enableWarmStarting = w->enableWarmStarting;
 	sc->enableContinuous = w->enableContinuous;
 	sc->enableSleep = w->enableSleep;
+}
+
+int gstep_after_collide( gWorld* w, float dt, int subSteps, b2gStepConst* sc, b2gSolvePlan* plan )
+{
+	int eventCount = w->io.counters[0];
+	w->lastEventCount = eventCount;
+	process_events( w, eventCount < w->dev.eventCap ? eventCount : w->dev.eventCap );
+	double t2 = b2g_now_ms();
+	w->profile.collide = (float)( t2 - w->stepStart );
+	w->stepStart = t2;
+
+	if ( dt <= 0.0f )
+		return 0;
+
+	step_constants( w, dt, subSteps, sc );
 
 	if ( w->awake.count == 0 )
 	{
@@ -816,21 +822,49 @@ void gstep_finish( gWorld* w )
 	w->profile.broadphase = (float)( b2g_now_ms() - t3 );
 }
 
+/* Whether the solver stage can be launched behind the narrowphase before its events are
+ * known: the solve lists on the device are current (no event can have been processed
+ * yet, so they are what the host would use after a step without events), the world
+ * solves, and nothing records the step. */
+static bool can_speculate( const gWorld* w, float dt )
+{
+	int block = ( w->bodyIds.next + B2G_FUSED_CTAS - 1 ) / B2G_FUSED_CTAS;
+	block = block < 1 ? 1 : block;
+	return dt > 0.0f && w->awake.count > 0 && w->tape == NULL && w->dev.fused && w->solveDirty == false && w->solveUploaded &&
+		   w->solvePlan.bodyBlock == block;
+}
+
 void gstep_run( gWorld* w, float dt, int subSteps )
 {
 	int staged = gstep_begin( w );
 	if ( staged < 0 )
 		return;
 	int e = b2gd_collide( &w->dev, &w->io, staged, w->stepIdCount );
-	gstep_rebuild_trees( w );
-	e |= b2gd_sync( &w->dev );
-	if ( e )
-	{
-		w->status = e;
-		return;
-	}
 	b2gStepConst sc;
 	b2gSolvePlan plan;
+	int speculated = 0;
+	if ( e == 0 && can_speculate( w, dt ) )
+	{
+		step_constants( w, dt, subSteps, &sc );
+		plan = w->solvePlan;
+		plan.awakeCount = w->awake.count;
+		plan.bodyIdCount = w->bodyIds.next;
+		speculated = b2gd_solve_speculative( &w->dev, &w->io, &plan, &sc );
+	}
+	gstep_rebuild_trees( w );
+	e |= b2gd_sync( &w->dev );
+	if ( e || speculated < 0 )
+	{
+		w->status = e ? e : -1;
+		return;
+	}
+	if ( speculated > 0 && w->io.counters[0] == 0 )
+	{
+		/* no events: the solver stage has run on the lists the host would have used */
+		gstep_after_collide( w, dt, subSteps, &sc, &plan );
+		gstep_finish( w );
+		return;
+	}
 	if ( gstep_after_collide( w, dt, subSteps, &sc, &plan ) == 0 )
 		return;
 	e = b2gd_solve( &w->dev, &w->io, &plan, &sc );
