@@ -52,6 +52,17 @@ def dist_env():
     return rank, world, local
 
 
+def replica_max(value, dist=None):
+    """The maximum of a per-rank figure over all ranks (replicas: each rank steps its own
+    world, so the job's time per step is the slowest rank's)."""
+    if dist is None:
+        return float(value)
+    import torch
+    t = torch.tensor([float(value)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 class ClockSampler:
     """Samples SM clocks and throttle reasons with nvidia-smi during the timed region."""
 
@@ -398,21 +409,24 @@ def run_gpu(args):
             host_prof.append((p.step, p.pairs, p.collide, p.solve, p.broadphase))
             fused_steps += t.fusedSolver
     torch.cuda.synchronize()
-    ms = float(np.mean(step_ms))
     if dist:
-        tt = torch.tensor([ms])
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        ms = float(tt.item())
+        dist.barrier()
+    ms = replica_max(float(np.mean(step_ms)), dist)
 
     # end to end through the C API with host buffers
     n_bodies = L.b2World_GetBodyStates(w, None, 0)
     host = np.zeros(7 * n_bodies, np.float32)
     e2e_steps = max(10, args.steps // 2)
+    if dist:
+        dist.barrier()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         L.b2World_Step(w, DT, SUBSTEPS)
         L.b2World_GetBodyStates(w, host.ctypes.data, n_bodies)
     e2e_ms = (time.perf_counter() - t0) * 1e3 / e2e_steps
+    if dist:
+        dist.barrier()
+    e2e_ms = replica_max(e2e_ms, dist)
 
     contacts = g.contacts(w)
     touching = contacts[contacts["colorIndex"] >= 0]
