@@ -128,7 +128,6 @@ extern "C" void b2gd_free( b2gDevWorld* w, b2gHostIO* io )
 	FREE_DEV( w->jointList );
 	FREE_DEV( w->kIdx );
 	FREE_DEV( w->kNF );
-	FREE_DEV( w->kSoft );
 	FREE_DEV( w->kMass );
 	for ( int j = 0; j < 2; ++j )
 	{
@@ -230,7 +229,6 @@ extern "C" int b2gd_reserve( b2gDevWorld* w, b2gHostIO* io, int bodyCap, int sha
 		e |= grow( (void**)&w->solveList, 4u * o, 4u * n, s );
 		e |= grow( &w->kIdx, 16u * o, 16u * n, s );
 		e |= grow( &w->kNF, 16u * o, 16u * n, s );
-		e |= grow( &w->kSoft, 16u * o, 16u * n, s );
 		e |= grow( &w->kMass, 16u * o, 16u * n, s );
 		for ( int j = 0; j < 2; ++j )
 		{

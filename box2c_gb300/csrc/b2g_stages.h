@@ -257,7 +257,6 @@ static __device__ void prepare_contact_row( const b2gDevWorld& W, int k, const b
 				 sc.enableWarmStarting ? 1.0f : 0.0f );
 	( (int4*)W.kIdx )[k] = make_int4( ia, ib, cid, r.count );
 	( (float4*)W.kNF )[k] = make_float4( r.n.x, r.n.y, r.friction, r.restitution );
-	( (float4*)W.kSoft )[k] = make_float4( r.biasRate, r.massScale, r.impulseScale, 0.0f );
 	( (float4*)W.kMass )[k] = make_float4( r.mA, r.iA, r.mB, r.iB );
 	for ( int j = 0; j < 2; ++j )
 	{
@@ -267,11 +266,13 @@ static __device__ void prepare_contact_row( const b2gDevWorld& W, int k, const b
 	}
 }
 
-static __device__ __forceinline__ void load_row( const b2gDevWorld& W, int k, Row& r )
+/* Row k for one phase (0 warm start, 1 solve, 2 relax, 3 restitution): the softness
+ * comes from the step constants (a static body's rows use the static softness, as
+ * prepare chose it), and warm starting, which reads no coefficients, skips them. */
+static __device__ __forceinline__ void load_row( const b2gDevWorld& W, int k, int phase, const b2gStepConst& sc, Row& r )
 {
 	int4 idx = ( (const int4*)W.kIdx )[k];
 	float4 nf = ( (const float4*)W.kNF )[k];
-	float4 so = ( (const float4*)W.kSoft )[k];
 	float4 ms = ( (const float4*)W.kMass )[k];
 	r.ia = idx.x;
 	r.ib = idx.y;
@@ -279,9 +280,10 @@ static __device__ __forceinline__ void load_row( const b2gDevWorld& W, int k, Ro
 	r.n = gv( nf.x, nf.y );
 	r.friction = nf.z;
 	r.restitution = nf.w;
-	r.biasRate = so.x;
-	r.massScale = so.y;
-	r.impulseScale = so.z;
+	const float* soft = ( idx.x < 0 || idx.y < 0 ) ? sc.staticSoft : sc.contactSoft;
+	r.biasRate = soft[0];
+	r.massScale = soft[1];
+	r.impulseScale = soft[2];
 	r.mA = ms.x;
 	r.iA = ms.y;
 	r.mB = ms.z;
@@ -289,7 +291,7 @@ static __device__ __forceinline__ void load_row( const b2gDevWorld& W, int k, Ro
 	for ( int j = 0; j < 2; ++j )
 	{
 		float4 a = ( (const float4*)W.kAnchor[j] )[k];
-		float4 c = ( (const float4*)W.kCoef[j] )[k];
+		float4 c = phase == 0 ? make_float4( 0.0f, 0.0f, 0.0f, 0.0f ) : ( (const float4*)W.kCoef[j] )[k];
 		float4 i = ( (const float4*)W.kImp[j] )[k];
 		r.rA[j] = gv( a.x, a.y );
 		r.rB[j] = gv( a.z, a.w );
@@ -326,7 +328,7 @@ static __device__ __forceinline__ void row_work( const b2gDevWorld& W, const Bod
 												 const b2gStepConst& sc )
 {
 	Row r;
-	load_row( W, k, r );
+	load_row( W, k, phase, sc, r );
 	bool delta = phase == 1 || phase == 2;
 	DevState a = delta ? B.load( r.ia ) : B.load_velocity( r.ia );
 	DevState b = delta ? B.load( r.ib ) : B.load_velocity( r.ib );

@@ -162,6 +162,10 @@ typedef struct b2gStepConst
 } b2gStepConst;
 
 /* Device arena of one world: raw device pointers and capacities. */
+/* float4 arrays of one constraint row: indices, normal/friction/restitution, masses,
+ * two anchor pairs, two coefficient sets, two impulse sets (144 bytes) */
+#define B2G_ROW_FLOAT4 9
+
 typedef struct b2gDevWorld
 {
 	int bodyCap, shapeCap, contactCap, jointCap, solveCap, listCap;
@@ -195,10 +199,10 @@ typedef struct b2gDevWorld
 	int* solveList; /* contact ids */
 	int* jointList; /* joint ids */
 
-	/* constraint rows */
+	/* constraint rows (B2G_ROW_FLOAT4 arrays; the softness follows from whether a body
+	 * is static and is not stored) */
 	void* kIdx;	 /* int4: indexA indexB contactId pointCount */
 	void* kNF;	 /* float4: normal.x normal.y friction restitution */
-	void* kSoft; /* float4: biasRate massScale impulseScale 0 */
 	void* kMass; /* float4: mA iA mB iB */
 	void* kAnchor[2];
 	void* kCoef[2]; /* baseSeparation normalMass tangentMass relativeVelocity */

@@ -146,9 +146,9 @@ struct WorldImage
  * array, nothing to wait for. */
 __device__ __forceinline__ void prefetch_rows( const b2gDevWorld& W, int first, int n )
 {
-	const void* arrays[10] = { W.kIdx, W.kNF, W.kSoft, W.kMass, W.kAnchor[0], W.kAnchor[1], W.kCoef[0], W.kCoef[1], W.kImp[0], W.kImp[1] };
+	const void* arrays[B2G_ROW_FLOAT4] = { W.kIdx, W.kNF, W.kMass, W.kAnchor[0], W.kAnchor[1], W.kCoef[0], W.kCoef[1], W.kImp[0], W.kImp[1] };
 	unsigned bytes = 16u * (unsigned)n;
-	for ( int i = 0; i < 10; ++i )
+	for ( int i = 0; i < B2G_ROW_FLOAT4; ++i )
 	{
 		const char* p = (const char*)arrays[i] + 16u * (size_t)first;
 		asm volatile( "cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"( p ), "r"( bytes ) : "memory" );

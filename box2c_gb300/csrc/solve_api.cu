@@ -94,21 +94,20 @@ extern "C" int b2gd_contact_desc( const b2ContactSolveDesc* d, b2gDevWorld* w, b
 	return 0;
 }
 
-/* Points the ten constraint-row arrays into one block of rows * 160 bytes. */
+/* Points the B2G_ROW_FLOAT4 constraint-row arrays into one block of rows * 144 bytes. */
 extern "C" void b2gd_contact_rows( b2gDevWorld* w, void* base, int rows )
 {
 	char* p = (char*)base;
 	size_t n = 16u * (size_t)rows;
 	w->kIdx = p;
 	w->kNF = p + n;
-	w->kSoft = p + 2 * n;
-	w->kMass = p + 3 * n;
-	w->kAnchor[0] = p + 4 * n;
-	w->kAnchor[1] = p + 5 * n;
-	w->kCoef[0] = p + 6 * n;
-	w->kCoef[1] = p + 7 * n;
-	w->kImp[0] = p + 8 * n;
-	w->kImp[1] = p + 9 * n;
+	w->kMass = p + 2 * n;
+	w->kAnchor[0] = p + 3 * n;
+	w->kAnchor[1] = p + 4 * n;
+	w->kCoef[0] = p + 5 * n;
+	w->kCoef[1] = p + 6 * n;
+	w->kImp[0] = p + 7 * n;
+	w->kImp[1] = p + 8 * n;
 	w->solveCap = rows;
 }
 
@@ -122,7 +121,7 @@ extern "C" int b2SolveContacts( const b2ContactSolveDesc* desc )
 	cudaStream_t s = (cudaStream_t)desc->stream;
 	void* rows = nullptr;
 	int n = desc->contactCount > 0 ? desc->contactCount : 1;
-	cudaError_t e = cudaMallocAsync( &rows, 160u * (size_t)n, s );
+	cudaError_t e = cudaMallocAsync( &rows, 16u * B2G_ROW_FLOAT4 * (size_t)n, s );
 	if ( e != cudaSuccess )
 		return (int)e;
 	b2gd_contact_rows( &w, rows, n );

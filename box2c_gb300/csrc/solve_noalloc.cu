@@ -8,7 +8,7 @@
  * that may block on other work or fail under memory pressure halfway through a run.
  * Both pass their own buffers and want the solver to take no memory of its own.
  *
- * The rows: 10 float4 arrays of `contactCount` entries carved from one block, the same
+ * The rows: B2G_ROW_FLOAT4 float4 arrays of `contactCount` entries carved from one block, the same
  * layout b2SolveContacts uses (b2gd_contact_rows).  k_prepare writes every field of
  * every row before any later kernel reads it, so nothing in the array has to start at
  * zero and nothing is cleared between calls.
@@ -29,8 +29,8 @@ extern "C" int b2gd_contact_solver( b2gDevWorld* w, const b2gSolvePlan* plan, co
 extern "C" int b2gd_contact_desc( const b2ContactSolveDesc* d, b2gDevWorld* w, b2gSolvePlan* plan, b2gStepConst* sc );
 extern "C" void b2gd_contact_rows( b2gDevWorld* w, void* base, int rows );
 
-/* 160 bytes per contact row: 10 float4 */
-static __device__ __align__( 256 ) float4 g_contactRows[10 * B2_SOLVE_NOALLOC_MAX_CONTACTS];
+/* 144 bytes per contact row: B2G_ROW_FLOAT4 float4 */
+static __device__ __align__( 256 ) float4 g_contactRows[B2G_ROW_FLOAT4 * B2_SOLVE_NOALLOC_MAX_CONTACTS];
 
 enum
 {

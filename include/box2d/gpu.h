@@ -149,12 +149,12 @@ typedef struct b2ContactSolveDesc
 } b2ContactSolveDesc;
 
 /* Returns 0, or a CUDA error code / -1 for invalid arguments.  Allocates its per-call
- * constraint rows (160 bytes per contact) with stream-ordered device allocation. */
+ * constraint rows (144 bytes per contact) with stream-ordered device allocation. */
 B2_API int b2SolveContacts( const b2ContactSolveDesc* desc );
 
 /* b2SolveContacts that allocates nothing; no counterpart in the reference API.  Its
  * constraint rows live in one fixed device array per device, compiled into the library:
- * B2_SOLVE_NOALLOC_MAX_CONTACTS rows of 160 bytes (2.5 MiB).  Same descriptor, same
+ * B2_SOLVE_NOALLOC_MAX_CONTACTS rows of 144 bytes (2.25 MiB).  Same descriptor, same
  * results and return codes as b2SolveContacts, plus B2_SOLVE_NOALLOC_TOO_LARGE (nothing
  * launched) when contactCount exceeds the maximum.
  * - The first call on each device (with that device current) looks up the array's
