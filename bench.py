@@ -214,6 +214,9 @@ BATCH_WORLDS = 4096
 # DRAM bytes of the solver stage of one large-pyramid step (k_fused_stage 2.35 MB +
 # k_solve_fused 2.76 MB), from the committed ncu capture of the same workload
 SOLVER_DRAM_BYTES = 5.11e6
+# DRAM bytes of the batched solver over 2048 of the batched worlds (both halves), from the
+# committed ncu capture of that workload
+BATCH_SOLVE_DRAM_BYTES = 4.96e9
 BATCH_SEED = 1237
 
 
@@ -262,9 +265,21 @@ def run_batch(g, steps, warmup, n_worlds=BATCH_WORLDS):
     loop = len(sample) / (time.perf_counter() - t)
     bodies = int(sum(int(b) * (int(b) + 1) // 2 for b in bases))
     failed = sum(1 for w in worlds if L.b2World_GetStatus(w) != 0)
+    # algorithmic bytes of one batched solver launch (solver stage + finalisation of every
+    # world, the per-unit model of algorithmic_bytes) from each world's touching contacts
+    solve_bytes = 0
+    for w, b in zip(worlds, bases):
+        c = g.contacts(w)
+        t = c[c["colorIndex"] >= 0]
+        nb = int(b) * (int(b) + 1) // 2
+        _, solver = algorithmic_bytes({"points": t["pointCount"], "all_points": c["pointCount"]}, nb, [4] * nb, SUBSTEPS)
+        solve_bytes += solver + nb * 128 + nb * (8 * 4 + 32)
     for w in worlds:
         g.destroy(w)
     value = n * steps / total
+    solve_dev = float(np.mean(dev_s))
+    peak, peak_kind = measured_peak()
+    achieved = solve_bytes / (solve_dev * 1e-3) / 1e9 if solve_dev > 0 else 0.0
     return {
         "metric": "batched world-steps/s", "value": round(value, 1), "unit": "world-steps/s",
         "worlds": n, "bodies": bodies, "steps": steps, "warmup": warm,
@@ -275,6 +290,12 @@ def run_batch(g, steps, warmup, n_worlds=BATCH_WORLDS):
                             [round(float(x), 4) for x in np.mean(np.array(prof), 0)])),
         "host_threads": st.hostThreads, "solve_cta_threads": st.solveThreads, "solve_ctas_per_sm": st.solveCtasPerSm,
         "gpu_launches_per_step": st.launches,
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "traffic": BATCH_SOLVE_DRAM_BYTES * n / 2048,
+                     "traffic_source": "ncu dram__bytes_read+write of k_batch_solve, 2048 worlds scaled to the "
+                                       "worlds stepped (profiles/batch_solver_4096_worlds.txt)",
+                     "kernel": "k_batch_solve (solver stage + finalisation, both halves)",
+                     "algorithmic_bytes_per_step": int(solve_bytes), "peak_kind": peak_kind},
         "loop_world_steps_per_s": round(loop, 1), "speedup_vs_loop": round(value / loop, 1),
         "failed_worlds": failed,
     }

@@ -29,7 +29,10 @@
 
 #define BATCH_GRID_THREADS 256
 #define TUNE_CANDIDATES 6
-#define TUNE_SAMPLES 2
+/* The candidates are timed round-robin, one per step, for TUNE_ROUNDS rounds: round 0
+ * warms each one up (graph instantiation, first launch) and is not counted, so every
+ * candidate is measured on a similar spread of the first steps' changing workload. */
+#define TUNE_ROUNDS 3
 #define B2G_BATCH_HALVES 2
 #define SM_SHARED_BYTES ( 228u * 1024u ) /* shared memory of one SM */
 /* dynamic shared memory one solver CTA may take: the 227 KB opt-in limit covers the
@@ -590,7 +593,7 @@ static cudaError_t finish_capture( cudaStream_t s, cudaError_t launch, cudaGraph
 
 extern "C" void b2gd_batch_begin_step( b2gBatch* b )
 {
-	b->choice = b->tuned ? b->choice : ( b->tuneStep / TUNE_SAMPLES ) % TUNE_CANDIDATES;
+	b->choice = b->tuned ? b->choice : b->tuneStep % TUNE_CANDIDATES;
 	b->launches = 0;
 	for ( int h = 0; h < B2G_BATCH_HALVES; ++h )
 		b->half[h].collideTimed = b->half[h].solveTimed = 0;
@@ -847,11 +850,10 @@ extern "C" int b2gd_batch_end_step( b2gBatch* b )
 	b->solveMs = solve;
 	if ( solved && b->tuned == 0 )
 	{
-		/* the later sample of each candidate counts */
-		if ( b->tuneStep % TUNE_SAMPLES == TUNE_SAMPLES - 1 )
-			b->tuneMs[b->choice] = solve;
+		if ( b->tuneStep >= TUNE_CANDIDATES )
+			b->tuneMs[b->choice] += solve;
 		b->tuneStep += 1;
-		if ( b->tuneStep == TUNE_SAMPLES * TUNE_CANDIDATES )
+		if ( b->tuneStep == TUNE_ROUNDS * TUNE_CANDIDATES )
 		{
 			int best = 0;
 			for ( int i = 1; i < TUNE_CANDIDATES; ++i )
