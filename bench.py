@@ -216,7 +216,7 @@ BATCH_WORLDS = 4096
 SOLVER_DRAM_BYTES = 5.11e6
 # DRAM bytes of the batched solver over 2048 of the batched worlds (both halves), from the
 # committed ncu capture of that workload
-BATCH_SOLVE_DRAM_BYTES = 4.96e9
+BATCH_SOLVE_DRAM_BYTES = 3.33e9
 BATCH_SEED = 1237
 
 
