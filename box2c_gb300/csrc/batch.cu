@@ -3,21 +3,22 @@
  *
  * Narrowphase: two grid-stride kernels over the concatenated contact records and
  * contact ids of all worlds (a flat index finds its world by binary search over the
- * prefix sums).  Solver: one persistent kernel; each CTA takes the next world from a
- * queue (largest first) and runs that world's whole solver stage and finalisation with
- * __syncthreads between the dependent phases.  Body states always live in shared
- * memory; a world whose constraint rows fit beside them keeps the rows there too, a
- * larger one in its own row arrays (they stay in L2 while the CTA works on them).  The
- * per-row work is b2g_stages.h's and b2g_cluster.h's, the same functions the
- * single-world kernels use, so every world gets the bits it would get from
- * b2World_Step alone.
+ * prefix sums).  Solver: one persistent kernel; each CTA takes the next pack from a
+ * queue: worlds of similar size side by side, each on a group of threads (one warp, a
+ * named-barrier group or the whole CTA) that runs the world's whole solver stage and
+ * finalisation with the group's barrier between the dependent phases.  Body states
+ * always live in shared memory; a world whose constraint rows fit beside them keeps the
+ * rows there too, a larger one in its own row arrays.  The per-row work is
+ * b2g_stages.h's and b2g_cluster.h's, the same functions the single-world kernels use,
+ * so every world gets the bits it would get from b2World_Step alone.
  *
- * Each device segment (uploads, kernels, counter download) is captured once as a CUDA
- * graph and replayed every step; the kernels read their counts from device memory, so
- * the graphs do not change while the number of worlds and the shared-memory size stay
- * the same.  The solver's launch shape (threads per CTA, CTAs per SM and so shared
- * memory per world) is chosen by timing the candidates on the first steps (any choice
- * gives the same results).
+ * A step's worlds run in two halves, each with its own graphs (uploads, kernels,
+ * counter download), captured once and replayed every step, so that the host work of
+ * one half overlaps the device work of the other; the kernels read their counts from
+ * device memory, so the graphs do not change while the number of worlds and the
+ * shared-memory size stay the same.  The solver's launch shape (threads per CTA, CTAs
+ * per SM and so shared memory per world) is chosen by timing the candidates on the
+ * first steps (any choice gives the same results).
  */
 #include "b2g_cluster.h"
 #include "b2g_stages.h"
