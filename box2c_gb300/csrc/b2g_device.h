@@ -129,6 +129,8 @@ void b2gd_batch_destroy( b2gBatch* b );
 /* Grows the item and counter buffers; returns the pinned item array or null. */
 b2gBatchItem* b2gd_batch_items( b2gBatch* b, int count );
 void* b2gd_batch_stream( b2gBatch* b );
+/* Worlds with more body ids than this are stepped alone (b2World_Step) by the batch. */
+int b2gd_batch_max_bodies( void );
 /* Host copy of world i's 4 counters after the last sync. */
 const int* b2gd_batch_counters( b2gBatch* b, int i );
 /* A step's items run in halves (h = 0, 1: items [first, first + count)), each with its

@@ -21,6 +21,7 @@
 static b2gBatch* s_batch;
 static gWorld** s_worlds;
 static void** s_streams;
+static b2WorldId* s_alone; /* worlds too large for the batched solver, stepped alone */
 static int s_cap;
 
 static bool reserve_worlds( int count )
@@ -36,6 +37,10 @@ static bool reserve_worlds( int count )
 	if ( s == NULL )
 		return false;
 	s_streams = s;
+	b2WorldId* a = (b2WorldId*)realloc( s_alone, sizeof( b2WorldId ) * (size_t)cap );
+	if ( a == NULL )
+		return false;
+	s_alone = a;
 	s_cap = cap;
 	return true;
 }
@@ -180,8 +185,10 @@ void b2World_StepBatch( const b2WorldId* worldIds, int count, float timeStep, in
 	if ( reserve_worlds( count ) == false )
 		return;
 
-	/* valid, healthy, distinct worlds */
-	int n = 0;
+	/* valid, healthy, distinct worlds; the ones whose bodies do not fit the batched
+	 * solver's shared memory are stepped alone after the batch */
+	int n = 0, alone = 0;
+	const int maxBodies = b2gd_batch_max_bodies();
 	for ( int i = 0; i < count; ++i )
 	{
 		if ( b2World_IsValid( worldIds[i] ) == false )
@@ -190,7 +197,15 @@ void b2World_StepBatch( const b2WorldId* worldIds, int count, float timeStep, in
 		if ( w->locked || w->status != 0 )
 			continue;
 		w->locked = true;
-		s_worlds[n++] = w;
+		if ( w->bodyIds.next > maxBodies )
+			s_alone[alone++] = worldIds[i];
+		else
+			s_worlds[n++] = w;
+	}
+	for ( int k = 0; k < alone; ++k )
+	{
+		gworld_get( s_alone[k] )->locked = false;
+		b2World_Step( s_alone[k], timeStep, subStepCount );
 	}
 	if ( n == 0 )
 		return;

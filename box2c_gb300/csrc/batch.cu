@@ -560,6 +560,10 @@ extern "C" b2gBatchItem* b2gd_batch_items( b2gBatch* b, int count )
 
 extern "C" void* b2gd_batch_stream( b2gBatch* b ) { return (void*)b->stream; }
 
+/* Largest body-id count the batched solver holds (bodies in shared memory, 32 bytes each,
+ * rounded up to 256 ids). */
+extern "C" int b2gd_batch_max_bodies( void ) { return (int)( CTA_SHARED_MAX / 32u / 256u * 256u ); }
+
 extern "C" const int* b2gd_batch_counters( b2gBatch* b, int i ) { return b->hCounters + 4 * i; }
 
 extern "C" int b2gd_stage_contacts( b2gDevWorld* w, b2gHostIO* io, int count )

@@ -47,11 +47,14 @@ B2_API b2DeviceTimes b2World_GetDeviceTimes( b2WorldId worldId );
 B2_API void b2World_EnableFusedSolver( b2WorldId worldId, bool flag );
 
 /* Steps `count` independent worlds by one b2World_Step each.  The device work of all of
- * them runs together: one replayed CUDA graph for contact creation and the narrowphase
- * of every world, one for the solver stage and finalisation (a persistent kernel in
- * which each CTA solves whole worlds, largest first).  Every world gets exactly the
- * results b2World_Step would give it alone.  Invalid, failed or repeated ids are
- * skipped.  Not thread-safe: one batch at a time per process. */
+ * them runs together, in two halves whose host work overlaps the other half's device
+ * work: replayed CUDA graphs for contact creation and the narrowphase of every world,
+ * and for the solver stage and finalisation (a persistent kernel over packs of
+ * similar-sized worlds, each world on a warp, a group of warps or a whole CTA).  A world
+ * with more bodies than the batched solver holds (about 6900) is stepped alone in the
+ * same call.  Every world gets exactly the results b2World_Step would give it alone.
+ * Invalid, failed or repeated ids are skipped.  Not thread-safe: one batch at a time
+ * per process. */
 B2_API void b2World_StepBatch( const b2WorldId* worldIds, int count, float timeStep, int subStepCount );
 
 /* Device milliseconds of the last batched step's narrowphase and solver segments (both

@@ -87,3 +87,25 @@ def test_batch_then_single_steps_continue_bit_exact(gpu, oracle):
             gpu.destroy(w)
         for w in wo:
             oracle.destroy(w)
+
+
+def test_batch_steps_worlds_too_large_for_it_alone(gpu):
+    """A world with more bodies than the batched solver holds in shared memory is stepped
+    by the single-world path inside the same call; the others are batched."""
+    bind_batch_api(gpu.lib)
+    make = [lambda: gpu.pyramid(120), lambda: gpu.pyramid(9), lambda: gpu.pyramid(14)]
+    wb = [m() for m in make]
+    ws = [m() for m in make]
+    ids = world_array(wb)
+    try:
+        for _ in range(4):
+            gpu.lib.b2World_StepBatch(ids, len(wb), 1.0 / 60.0, 4)
+            for w in ws:
+                gpu.step(w)
+        for i, (a, b) in enumerate(zip(wb, ws)):
+            assert gpu.lib.b2World_GetStatus(a) == 0
+            ba, bb = gpu.bodies(a), gpu.bodies(b)
+            assert np.array_equal(ba.view(np.uint32), bb.view(np.uint32)), f"world {i}"
+    finally:
+        for w in wb + ws:
+            gpu.destroy(w)
