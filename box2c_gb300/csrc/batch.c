@@ -15,8 +15,10 @@
 #include <stdlib.h>
 #include <string.h>
 
-/* Below this many worlds per half a step is not split in two. */
-#define BATCH_MIN_HALF 64
+/* A step is split in two halves only when its worlds hold at least this many bodies:
+ * below it the device work is too short to hide the host work of the other half behind,
+ * and the second set of launches and waits costs more than the overlap gains. */
+#define BATCH_SPLIT_BODIES 100000
 
 static b2gBatch* s_batch;
 static gWorld** s_worlds;
@@ -219,7 +221,10 @@ void b2World_StepBatch( const b2WorldId* worldIds, int count, float timeStep, in
 	/* two halves (one when there are few worlds): the host phases of one half run while
 	 * the device works on the other */
 	BatchCtx c[2];
-	int split = n >= 2 * BATCH_MIN_HALF ? n / 2 : n;
+	long long bodies = 0;
+	for ( int k = 0; k < n; ++k )
+		bodies += s_worlds[k]->bodyIds.next;
+	int split = n >= 2 && bodies >= BATCH_SPLIT_BODIES ? n / 2 : n;
 	for ( int h = 0; h < 2; ++h )
 	{
 		c[h].items = items;

@@ -825,13 +825,14 @@ void gstep_finish( gWorld* w )
 /* Whether the solver stage can be launched behind the narrowphase before its events are
  * known: the solve lists on the device are current (no event can have been processed
  * yet, so they are what the host would use after a step without events), the world
- * solves, and nothing records the step. */
+ * solves, nothing records the step, and the last step had no events either (a world
+ * whose contacts change every step would waste the launches). */
 static bool can_speculate( const gWorld* w, float dt )
 {
 	int block = ( w->bodyIds.next + B2G_FUSED_CTAS - 1 ) / B2G_FUSED_CTAS;
 	block = block < 1 ? 1 : block;
-	return dt > 0.0f && w->awake.count > 0 && w->tape == NULL && w->dev.fused && w->solveDirty == false && w->solveUploaded &&
-		   w->solvePlan.bodyBlock == block;
+	return dt > 0.0f && w->awake.count > 0 && w->tape == NULL && w->dev.fused && w->lastEventCount == 0 &&
+		   w->solveDirty == false && w->solveUploaded && w->solvePlan.bodyBlock == block;
 }
 
 void gstep_run( gWorld* w, float dt, int subSteps )

@@ -109,3 +109,27 @@ def test_batch_steps_worlds_too_large_for_it_alone(gpu):
     finally:
         for w in wb + ws:
             gpu.destroy(w)
+
+
+def test_batch_in_halves_matches_single_steps(gpu):
+    """Batches with at least 100k bodies run in two halves whose host and device work
+    overlap; each world still gets the bits of its own b2World_Step (which the oracle
+    tests pin)."""
+    bind_batch_api(gpu.lib)
+    rng = np.random.default_rng(9)
+    bases = rng.integers(30, 41, size=180)
+    assert sum(int(b) * (int(b) + 1) // 2 for b in bases) >= 100000
+    wb = [gpu.pyramid(int(b), 0.01, 300 + i) for i, b in enumerate(bases)]
+    ws = [gpu.pyramid(int(b), 0.01, 300 + i) for i, b in enumerate(bases)]
+    ids = world_array(wb)
+    try:
+        for _ in range(6):
+            gpu.lib.b2World_StepBatch(ids, len(wb), 1.0 / 60.0, 4)
+            for w in ws:
+                gpu.step(w)
+        for i, (a, b) in enumerate(zip(wb, ws)):
+            ba, bb = gpu.bodies(a), gpu.bodies(b)
+            assert np.array_equal(ba.view(np.uint32), bb.view(np.uint32)), f"world {i}"
+    finally:
+        for w in wb + ws:
+            gpu.destroy(w)
