@@ -48,10 +48,11 @@ struct ClusterBodies
 	float4* st1;
 	int slots;
 	int rank;
+	unsigned slotsInv; /* ceil(2^32 / slots) for slots > 1: b / slots = umulhi(b, slotsInv) for b, slots < 2^16 */
 
 	__device__ __forceinline__ float4* word( float4* base, int b ) const
 	{
-		int r = b / slots;
+		int r = slots == 1 ? b : (int)__umulhi( (unsigned)b, slotsInv );
 		int s = b - r * slots;
 		return r == rank ? base + s : cl.map_shared_rank( base + s, (unsigned)r );
 	}

@@ -57,6 +57,7 @@ struct FusedPlan
 	 * the copies and their index tables start at float4 offset ovOffset */
 	int ovCached;
 	int ovOffset;
+	unsigned bodySlotsInv; /* ceil(2^32 / bodySlots), for the owner of a body id */
 };
 
 /* Shared-memory carve-up; every CTA uses the same offsets, so a local address maps to
@@ -386,7 +387,7 @@ __global__ void __launch_bounds__( FUSED_THREADS ) k_solve_fused( b2gDevWorld W,
 			}
 		}
 	}
-	ClusterBodies B{ cl, m.st0, m.st1, BS, rank };
+	ClusterBodies B{ cl, m.st0, m.st1, BS, rank, P.bodySlotsInv };
 	cl.sync();
 
 	for ( int sub = 0; sub < sc.subSteps; ++sub )
@@ -480,7 +481,8 @@ extern "C" int b2gd_solver_fused( b2gDevWorld* w, const b2gSolvePlan* plan, cons
 	/* per device: 0 unknown, 1 available, -1 unavailable */
 	static int s_readyByDevice[64];
 	const int CL = FUSED_CLUSTER;
-	if ( plan->bodyIdCount <= 0 || plan->bodyBlock <= 0 )
+	/* body ids and slots below 2^16: the owner division is one multiply-high */
+	if ( plan->bodyIdCount <= 0 || plan->bodyBlock <= 0 || plan->bodyIdCount >= 65536 )
 		return 0;
 	int dev = 0;
 	if ( cudaGetDevice( &dev ) != cudaSuccess || dev < 0 || dev >= 64 )
@@ -499,6 +501,7 @@ extern "C" int b2gd_solver_fused( b2gDevWorld* w, const b2gSolvePlan* plan, cons
 	P.activeCount = plan->activeCount;
 	P.bodyIdCount = plan->bodyIdCount;
 	P.bodySlots = plan->bodyBlock;
+	P.bodySlotsInv = P.bodySlots > 1 ? (unsigned)( ( ( 1ull << 32 ) + (unsigned long long)P.bodySlots - 1 ) / (unsigned long long)P.bodySlots ) : 0u;
 	int perCta[B2G_FUSED_CTAS] = { 0 };
 	for ( int c = 0; c < B2G_OVERFLOW; ++c )
 	{
