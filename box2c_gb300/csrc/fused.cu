@@ -224,7 +224,7 @@ __device__ void run_stage( const b2gDevWorld& W, const FusedPlan& P, const Fused
 /* Staging: writes every CTA's shared-memory image (constraint rows, reference
  * src/contact_solver.c:597-808 and :21-147; body states; per-step velocity terms,
  * src/solver.c:34-93) to global memory, one thread per row and per body id. */
-__global__ void __launch_bounds__( 256 ) k_fused_stage( b2gDevWorld W, FusedPlan P, b2gStepConst sc, float4* image )
+__global__ void __launch_bounds__( 128 ) k_fused_stage( b2gDevWorld W, FusedPlan P, b2gStepConst sc, float4* image )
 {
 	if ( W.guardEvents && W.counters[0] != 0 )
 		return;
@@ -578,7 +578,7 @@ extern "C" int b2gd_solver_fused( b2gDevWorld* w, const b2gSolvePlan* plan, cons
 	int launches = b2gd_prepare_joints( w, plan->jointStart[B2G_COLORS], sc );
 	int rows = plan->colorStart[B2G_COLORS];
 	int threads = rows > plan->bodyIdCount ? rows : plan->bodyIdCount;
-	k_fused_stage<<<( threads + 255 ) / 256, 256, 0, s>>>( *w, P, *sc, (float4*)w->stage );
+	k_fused_stage<<<( threads + 127 ) / 128, 128, 0, s>>>( *w, P, *sc, (float4*)w->stage );
 	cudaLaunchAttribute attr[1];
 	cudaLaunchConfig_t cfg = cluster_config( attr, bytes, s );
 	if ( cudaLaunchKernelEx( &cfg, kernel, *w, P, *sc, (const float4*)w->stage ) != cudaSuccess )

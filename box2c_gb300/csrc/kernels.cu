@@ -30,7 +30,7 @@
 
 #include <stdio.h>
 
-#define BLOCK 256
+#define BLOCK 128
 
 /* ------------------------------------------------------------------ single-world kernels */
 __global__ void k_scatter_contacts( b2gDevWorld W, const b2gContactInit* inits, int n )
