@@ -36,7 +36,7 @@ SCENES = {
     "tumbler2000": (200, (1, 50, 100, 200)),
     "tilted": (100, (1, 50, 100)),
     # default world def has sleep on; the reference island falls asleep at step 88,
-    # which this build leaves out, so the fixture stops at step 87
+    # and the library has no islands or sleep, so the fixture stops at step 87
     "hello": (87, (87,)),
     "pyramid100": (40, (40,)),
 }
