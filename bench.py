@@ -145,19 +145,31 @@ def algorithmic_bytes(contacts, awake_bodies, shape_vertex_counts, substeps):
     return total, solver
 
 
-def cpu_baseline(steps_sample=20, warmup=2):
-    """Times the plain-C CPU restatement of the step on the same workload (1 thread)."""
+def oracle_backend(threads):
+    """The plain-C CPU restatement, its parallel loops (colour rows, bodies, narrowphase
+    contacts) on `threads` host threads; any count gives the same bits."""
     subprocess.run(["make", "-s", "-j8", "-f", "oracle/Makefile"], cwd=REPO, check=True, capture_output=True)
     from box2c_gb300.capi import Backend
     ob = os.path.join(REPO, "oracle", "_build")
     o = Backend(os.path.join(ob, "liboracle.so"), os.path.join(ob, "liboracle_scenes.so"), "oracle")
+    o.lib.b2o_SetThreads.argtypes = [C.c_int]
+    o.lib.b2o_SetThreads.restype = C.c_int
+    o.lib.b2o_SetThreads(threads)
+    return o
+
+
+def cpu_baseline(steps_sample=20, warmup=2):
+    """Times the plain-C CPU restatement of the step on the same workload, on all host
+    cores.  Returns (ms per step, steps, threads)."""
+    cores = os.cpu_count() or 1
+    o = oracle_backend(cores)
     w = o.pyramid(BASE, JITTER, SEED)
     o.step(w, DT, SUBSTEPS, count=warmup)
     t0 = time.perf_counter()
     o.step(w, DT, SUBSTEPS, count=steps_sample)
     ms = (time.perf_counter() - t0) * 1e3 / steps_sample
     o.destroy(w)
-    return ms, steps_sample
+    return ms, steps_sample, cores
 
 
 TUMBLER_BODIES = 2000
@@ -169,7 +181,7 @@ def run_tumbler(g, steps=1000, cpu=True):
     """Tumbler: a 20 m hollow box of four walls on a revolute motor (0.05 pi rad/s) with
     2000 boxes (half-extent 0.125) and circles (radius 0.125) at seeded random positions,
     4 substeps, 1000 steps; device and wall ms per b2World_Step, host pair time, and the
-    oracle on a bounded sample of the same scene (one thread)."""
+    oracle on a bounded sample of the same scene (all host cores)."""
     from box2c_gb300.capi import bind_gpu_api
     L = g.lib
     bind_gpu_api(L)
@@ -195,17 +207,15 @@ def run_tumbler(g, steps=1000, cpu=True):
            "host_pairs_ms": round(float(np.mean(pairs[skip:])), 4),
            "overflow_constraints": int(counters.colorCounts[OVERFLOW_COLOR]), "status": status}
     if cpu:
-        subprocess.run(["make", "-s", "-j8", "-f", "oracle/Makefile"], cwd=REPO, check=True, capture_output=True)
-        from box2c_gb300.capi import Backend
-        ob = os.path.join(REPO, "oracle", "_build")
-        o = Backend(os.path.join(ob, "liboracle.so"), os.path.join(ob, "liboracle_scenes.so"), "oracle")
+        cores = os.cpu_count() or 1
+        o = oracle_backend(cores)
         wo = o.tumbler(TUMBLER_BODIES, TUMBLER_SEED, 0)
         o.step(wo, DT, SUBSTEPS, count=100)
         n = 20
         t0 = time.perf_counter()
         o.step(wo, DT, SUBSTEPS, count=n)
-        out["cpu_baseline"] = {"value": round((time.perf_counter() - t0) * 1e3 / n, 4), "unit": "ms/step", "cores": 1,
-                               "kind": "port", "sample": f"steps 100-{100 + n} of the same tumbler"}
+        out["cpu_baseline"] = {"value": round((time.perf_counter() - t0) * 1e3 / n, 4), "unit": "ms/step",
+                               "cores": cores, "kind": "port", "sample": f"steps 100-{100 + n} of the same tumbler"}
         o.destroy(wo)
     return out
 
@@ -347,10 +357,7 @@ def batch_cpu_baseline(sample=1024, steps=5):
     """The plain-C CPU restatement stepping a sample of the batched worlds, one world per
     task on all host cores (worlds are independent)."""
     from concurrent.futures import ThreadPoolExecutor
-    subprocess.run(["make", "-s", "-j8", "-f", "oracle/Makefile"], cwd=REPO, check=True, capture_output=True)
-    from box2c_gb300.capi import Backend
-    ob = os.path.join(REPO, "oracle", "_build")
-    o = Backend(os.path.join(ob, "liboracle.so"), os.path.join(ob, "liboracle_scenes.so"), "oracle")
+    o = oracle_backend(1)  # the worlds run in parallel, each on one thread
     worlds = [o.pyramid(int(b), 0.0, 0) for b in batch_bases()[:sample]]
     cores = os.cpu_count() or 1
     with ThreadPoolExecutor(max_workers=cores) as ex:
@@ -369,12 +376,12 @@ def run_reference(args):
     if rank != 0:
         return
     warm = max(3, args.warmup)
-    ms, n = cpu_baseline(steps_sample=max(5, min(args.steps, 40)), warmup=warm)
+    ms, n, cores = cpu_baseline(steps_sample=max(5, min(args.steps, 40)), warmup=warm)
     line = {"metric": METRIC, "value": round(ms, 4), "unit": "ms/step", "n_gpus": args.gpus, "steps": n,
             "warmup": warm, "ms_per_step": round(ms, 4), "higher_is_better": False, "impl": "reference",
             "dtype": "f32", "data": "synthetic", "scaling": "weak", "vs_baseline": None,
             "config": {"workload": "large_pyramid_100_rows_5050_boxes", "dt": DT, "substeps": SUBSTEPS},
-            "cpu_baseline": {"value": round(ms, 4), "unit": "ms/step", "cores": 1, "kind": "port",
+            "cpu_baseline": {"value": round(ms, 4), "unit": "ms/step", "cores": cores, "kind": "port",
                              "sample": f"{n} steps of the 100-row pyramid after {warm} warm-up steps"},
             "e2e": {"value": round(ms, 4), "unit": "ms/step", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
@@ -468,7 +475,7 @@ def run_gpu(args):
 
     if rank != 0:
         return
-    cpu_ms, cpu_n = cpu_baseline() if not args.no_cpu else (None, 0)
+    cpu_ms, cpu_n, cpu_cores = cpu_baseline() if not args.no_cpu else (None, 0, 0)
     if batch is not None and not args.no_cpu:
         batch["cpu_baseline"] = batch_cpu_baseline()
     clocks = sampler.summary()
@@ -496,7 +503,7 @@ def run_gpu(args):
         "e2e": {"value": round(e2e_ms, 4), "unit": "ms/step", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": int(n_bodies * 7 * 4 + n_bodies * 64)},
         "gpu_launches": int(sum(launches)),
-        "cpu_baseline": ({"value": round(cpu_ms, 4), "unit": "ms/step", "cores": 1, "kind": "port",
+        "cpu_baseline": ({"value": round(cpu_ms, 4), "unit": "ms/step", "cores": cpu_cores, "kind": "port",
                           "sample": f"{cpu_n} steps of the same 100-row pyramid after 2 warm-up steps"}
                          if cpu_ms is not None else None),
         "clocks": clocks, "status": status, "unsupported_toi": toi,

@@ -56,6 +56,13 @@ int oid_alloc( oIdPool* p );
 void oid_free( oIdPool* p, int id );
 int oid_count( const oIdPool* p );
 
+/* Threads of the oracle's independent loops (the rows of one colour, bodies, contacts of
+ * the narrowphase), set by b2o_SetThreads; 1, the default, runs everything on the
+ * calling thread.  The loops' iterations touch disjoint data, so any count gives the
+ * same bits.  Loops shorter than O_PARALLEL_MIN stay serial. */
+extern int o_threads;
+#define O_PARALLEL_MIN 64
+
 typedef struct oBits
 {
 	uint64_t* words;

@@ -523,6 +523,15 @@ static void solve_revolute( oWorld* w, const oStep* st, oJoint* j, bool useBias 
 }
 
 /* ------------------------------------------------------------ bodies */
+int o_threads = 1;
+
+/* Threads for the oracle's parallel loops (CPU baselines); returns the count in use. */
+int b2o_SetThreads( int count )
+{
+	o_threads = count < 1 ? 1 : count;
+	return o_threads;
+}
+
 static void integrate_velocities( oWorld* w, const oStep* st )
 {
 	oVec g = w->gravity;
@@ -530,7 +539,9 @@ static void integrate_velocities( oWorld* w, const oStep* st )
 	b2r maxLin = O_MAX_TRANSLATION * st->inv_dt;
 	b2r maxAng = O_MAX_ROTATION * st->inv_dt;
 	b2r maxLin2 = maxLin * maxLin, maxAng2 = maxAng * maxAng;
-	for ( int i = 0; i < w->awake.count; ++i )
+	const int n = w->awake.count;
+#pragma omp parallel for if ( o_threads > 1 && n >= O_PARALLEL_MIN ) num_threads( o_threads ) schedule( static )
+	for ( int i = 0; i < n; ++i )
 	{
 		oBody* b = w->bodies + w->awake.data[i];
 		oVec v = b->v;
@@ -560,7 +571,9 @@ static void integrate_velocities( oWorld* w, const oStep* st )
 
 static void integrate_positions( oWorld* w, const oStep* st )
 {
-	for ( int i = 0; i < w->awake.count; ++i )
+	const int n = w->awake.count;
+#pragma omp parallel for if ( o_threads > 1 && n >= O_PARALLEL_MIN ) num_threads( o_threads ) schedule( static )
+	for ( int i = 0; i < n; ++i )
 	{
 		oBody* b = w->bodies + w->awake.data[i];
 		b->dq = ointrot( b->dq, st->h * b->w );
@@ -773,8 +786,12 @@ void o_solve( oWorld* w, b2r dt, int subSteps )
 		{
 			colorStart[i] = n;
 			oIntArray* a = &w->colors[i].contacts;
-			for ( int k = 0; k < a->count; ++k )
-				prepare_contact( w, &st, cons + n++, w->contacts + a->data[k] );
+			const int count = a->count;
+			oConstraint* base = cons + n;
+#pragma omp parallel for if ( o_threads > 1 && count >= O_PARALLEL_MIN ) num_threads( o_threads ) schedule( static )
+			for ( int k = 0; k < count; ++k )
+				prepare_contact( w, &st, base + k, w->contacts + a->data[k] );
+			n += count;
 		}
 		colorStart[O_COLORS] = n;
 	}
@@ -804,7 +821,9 @@ void o_solve( oWorld* w, b2r dt, int subSteps )
 				int c = active[a];
 				for ( int k = 0; k < w->colors[c].joints.count; ++k )
 					warm_start_revolute( w, w->joints + w->colors[c].joints.data[k] );
-				for ( int k = colorStart[c]; k < colorStart[c + 1]; ++k )
+				const int k0 = colorStart[c], k1 = colorStart[c + 1];
+#pragma omp parallel for if ( o_threads > 1 && k1 - k0 >= O_PARALLEL_MIN ) num_threads( o_threads ) schedule( static )
+				for ( int k = k0; k < k1; ++k )
 					warm_start_lane( w, cons + k );
 			}
 		}
@@ -818,7 +837,9 @@ void o_solve( oWorld* w, b2r dt, int subSteps )
 			int c = active[a];
 			for ( int k = 0; k < w->colors[c].joints.count; ++k )
 				solve_revolute( w, &st, w->joints + w->colors[c].joints.data[k], true );
-			for ( int k = colorStart[c]; k < colorStart[c + 1]; ++k )
+			const int k0 = colorStart[c], k1 = colorStart[c + 1];
+#pragma omp parallel for if ( o_threads > 1 && k1 - k0 >= O_PARALLEL_MIN ) num_threads( o_threads ) schedule( static )
+			for ( int k = k0; k < k1; ++k )
 				solve_lane( w, &st, cons + k, true );
 		}
 
@@ -833,7 +854,9 @@ void o_solve( oWorld* w, b2r dt, int subSteps )
 			int c = active[a];
 			for ( int k = 0; k < w->colors[c].joints.count; ++k )
 				solve_revolute( w, &st, w->joints + w->colors[c].joints.data[k], false );
-			for ( int k = colorStart[c]; k < colorStart[c + 1]; ++k )
+			const int k0 = colorStart[c], k1 = colorStart[c + 1];
+#pragma omp parallel for if ( o_threads > 1 && k1 - k0 >= O_PARALLEL_MIN ) num_threads( o_threads ) schedule( static )
+			for ( int k = k0; k < k1; ++k )
 				solve_lane( w, &st, cons + k, false );
 		}
 	}
@@ -843,12 +866,16 @@ void o_solve( oWorld* w, b2r dt, int subSteps )
 	for ( int a = 0; a < activeCount; ++a )
 	{
 		int c = active[a];
-		for ( int k = colorStart[c]; k < colorStart[c + 1]; ++k )
+		const int k0 = colorStart[c], k1 = colorStart[c + 1];
+#pragma omp parallel for if ( o_threads > 1 && k1 - k0 >= O_PARALLEL_MIN ) num_threads( o_threads ) schedule( static )
+		for ( int k = k0; k < k1; ++k )
 			restitution_lane( w, &st, cons + k );
 	}
 
 	/* store impulses: the overflow path writes existing points, the 8-lane path both */
-	for ( int k = 0; k < colorStart[O_COLORS]; ++k )
+	const int stored = colorStart[O_COLORS];
+#pragma omp parallel for if ( o_threads > 1 && stored >= O_PARALLEL_MIN ) num_threads( o_threads ) schedule( static )
+	for ( int k = 0; k < stored; ++k )
 	{
 		oConstraint* c = cons + k;
 		oManifold* m = &w->contacts[c->contactId].manifold;

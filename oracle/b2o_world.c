@@ -1258,7 +1258,9 @@ static bool update_contact( oWorld* w, oContact* c, oShape* sA, oXf xfA, oVec of
 	return touching;
 }
 
-static void collide_one( oWorld* w, oContact* c, oBits* changed )
+/* Narrowphase of one contact; returns whether its state changed (disjoint, started or
+ * stopped touching). */
+static bool collide_one( oWorld* w, oContact* c )
 {
 	oShape* sA = w->shapes + c->shapeIdA;
 	oShape* sB = w->shapes + c->shapeIdB;
@@ -1266,8 +1268,7 @@ static void collide_one( oWorld* w, oContact* c, oBits* changed )
 	{
 		c->simFlags |= OS_DISJOINT;
 		c->simFlags &= ~OS_TOUCHING;
-		obits_set( changed, c->id );
-		return;
+		return true;
 	}
 	bool wasTouching = ( c->simFlags & OS_TOUCHING ) != 0;
 	oBody* bA = w->bodies + sA->bodyId;
@@ -1284,13 +1285,28 @@ static void collide_one( oWorld* w, oContact* c, oBits* changed )
 	if ( touching && !wasTouching )
 	{
 		c->simFlags |= OS_STARTED;
-		obits_set( changed, c->id );
+		return true;
 	}
 	else if ( !touching && wasTouching )
 	{
 		c->simFlags |= OS_STOPPED;
-		obits_set( changed, c->id );
+		return true;
 	}
+	return false;
+}
+
+/* Contacts [0, count) of a list through the narrowphase (in parallel: each touches only
+ * its own contact), then their state changes into the bitset in list order. */
+static void collide_list( oWorld* w, const int* ids, int count, oBits* changed )
+{
+	uint8_t* flag = (uint8_t*)malloc( (size_t)( count > 0 ? count : 1 ) );
+#pragma omp parallel for if ( o_threads > 1 && count >= O_PARALLEL_MIN ) num_threads( o_threads ) schedule( static )
+	for ( int k = 0; k < count; ++k )
+		flag[k] = collide_one( w, w->contacts + ids[k] ) ? 1 : 0;
+	for ( int k = 0; k < count; ++k )
+		if ( flag[k] )
+			obits_set( changed, ids[k] );
+	free( flag );
 }
 
 /* Reference src/world.c:410-674. */
@@ -1302,13 +1318,8 @@ void o_collide( oWorld* w )
 
 	oBits changed = { 0 };
 	for ( int i = 0; i < O_COLORS; ++i )
-	{
-		oIntArray* a = &w->colors[i].contacts;
-		for ( int k = 0; k < a->count; ++k )
-			collide_one( w, w->contacts + a->data[k], &changed );
-	}
-	for ( int k = 0; k < w->nonTouching.count; ++k )
-		collide_one( w, w->contacts + w->nonTouching.data[k], &changed );
+		collide_list( w, w->colors[i].contacts.data, w->colors[i].contacts.count, &changed );
+	collide_list( w, w->nonTouching.data, w->nonTouching.count, &changed );
 
 	for ( int word = 0; word < changed.wordCount; ++word )
 	{

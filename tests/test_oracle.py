@@ -137,3 +137,25 @@ def test_fp64_oracle_tracks_fp32(oracle, oracle64):
     oracle.destroy(w32)
     oracle64.destroy(w64)
     assert np.nanmax(np.abs(a[:, :2] - b[:, :2])) < 1e-3
+
+
+@pytest.mark.parametrize("scene,steps", [("pyramid_jitter", 60), ("tumbler", 60)])
+def test_threaded_oracle_is_bit_identical(oracle, scene, steps):
+    """The oracle's parallel loops (colour rows, bodies, narrowphase contacts; the CPU
+    baselines use them) give the bits of the serial oracle."""
+    make = {"pyramid_jitter": lambda: oracle.pyramid(40, 0.01, 77), "tumbler": lambda: oracle.tumbler(900, 5, 0)}[scene]
+    L = oracle.lib
+    L.b2o_SetThreads.argtypes = [C.c_int]
+    L.b2o_SetThreads.restype = C.c_int
+    states = []
+    try:
+        for threads in (1, 8):
+            L.b2o_SetThreads(threads)
+            w = make()
+            oracle.step(w, count=steps)
+            states.append((oracle.bodies(w).view(np.uint32).copy(), contact_table(oracle.contacts(w))))
+            oracle.destroy(w)
+    finally:
+        L.b2o_SetThreads(1)
+    assert np.array_equal(states[0][0], states[1][0])
+    assert np.array_equal(states[0][1], states[1][1])
