@@ -158,9 +158,10 @@ def oracle_backend(threads):
     return o
 
 
-def cpu_baseline(steps_sample=20, warmup=2):
+def cpu_baseline(steps_sample=40, warmup=100):
     """Times the plain-C CPU restatement of the step on the same workload, on all host
-    cores.  Returns (ms per step, steps, threads)."""
+    cores, over steps the device arm also times (after the pyramid has settled for
+    `warmup` steps).  Returns (ms per step, steps, threads)."""
     cores = os.cpu_count() or 1
     o = oracle_backend(cores)
     w = o.pyramid(BASE, JITTER, SEED)
@@ -375,7 +376,7 @@ def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    warm = max(3, args.warmup)
+    warm = max(100, args.warmup)
     ms, n, cores = cpu_baseline(steps_sample=max(5, min(args.steps, 40)), warmup=warm)
     line = {"metric": METRIC, "value": round(ms, 4), "unit": "ms/step", "n_gpus": args.gpus, "steps": n,
             "warmup": warm, "ms_per_step": round(ms, 4), "higher_is_better": False, "impl": "reference",
@@ -504,7 +505,7 @@ def run_gpu(args):
                 "d2h_bytes_per_step": int(n_bodies * 7 * 4 + n_bodies * 64)},
         "gpu_launches": int(sum(launches)),
         "cpu_baseline": ({"value": round(cpu_ms, 4), "unit": "ms/step", "cores": cpu_cores, "kind": "port",
-                          "sample": f"{cpu_n} steps of the same 100-row pyramid after 2 warm-up steps"}
+                          "sample": f"{cpu_n} steps of the same 100-row pyramid after 100 settling steps"}
                          if cpu_ms is not None else None),
         "clocks": clocks, "status": status, "unsupported_toi": toi,
         "batched": batch,
