@@ -1,0 +1,42 @@
+"""Host modules of the library checked on the CPU with small C harnesses (tests/c/): the
+fork-join pool that runs per-world host phases of batched steps and the pair rules of a
+single step (pool.c), and the dynamic tree whose traversal order fixes contact ids
+(tree.c, against the oracle's tree)."""
+import os
+import subprocess
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_pool_jobs_and_try_lock(tmp_path):
+    exe = str(tmp_path / "pool_check")
+    src = os.path.join(REPO, "box2c_gb300", "csrc")
+    subprocess.run(["gcc", "-std=gnu17", "-O2", "-pthread", "-I", src, "-I", os.path.join(REPO, "include"),
+                    os.path.join(REPO, "tests", "c", "pool_check.c"), os.path.join(src, "pool.c"), "-o", exe],
+                   check=True, capture_output=True)
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert r.stdout.startswith("ok")
+
+
+def test_host_tree_matches_oracle_tree(tmp_path):
+    """The library's host dynamic tree against the oracle's under a seeded sequence of
+    creates, moves, enlargements, destroys and rebuilds (tests/c/tree_check.c)."""
+    exe = str(tmp_path / "tree_check")
+    src = os.path.join(REPO, "box2c_gb300", "csrc")
+    inc = os.path.join(REPO, "include")
+    flags = ["-std=gnu17", "-O2", "-ffp-contract=off", "-I", inc]
+    objs = []
+    for name, extra, files in (
+            ("product", ["-I", src], [os.path.join(REPO, "tests", "c", "tree_product.c"), os.path.join(src, "tree.c")]),
+            ("oracle", ["-I", os.path.join(REPO, "oracle")],
+             [os.path.join(REPO, "tests", "c", "tree_oracle.c"), os.path.join(REPO, "oracle", "b2o_tree.c")])):
+        for f in files:
+            obj = str(tmp_path / (name + "_" + os.path.basename(f) + ".o"))
+            subprocess.run(["gcc", *flags, *extra, "-c", f, "-o", obj], check=True, capture_output=True)
+            objs.append(obj)
+    subprocess.run(["gcc", os.path.join(REPO, "tests", "c", "tree_check.c"), *objs, "-lm", "-o", exe],
+                   check=True, capture_output=True)
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert r.stdout.startswith("ok")
