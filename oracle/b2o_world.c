@@ -1131,6 +1131,10 @@ void o_update_pairs( oWorld* w )
 	if ( moveCount == 0 )
 		return;
 	oPairList* lists = (oPairList*)calloc( (size_t)moveCount, sizeof( oPairList ) );
+	/* the queries only read the world and fill their own lists (reference
+	 * src/broad_phase.c:278-331 and :361-362 runs them as parallel tasks); pairs are created below in
+	 * move order */
+#pragma omp parallel for if ( o_threads > 1 && moveCount >= O_PARALLEL_MIN ) num_threads( o_threads ) schedule( dynamic, 16 )
 	for ( int i = 0; i < moveCount; ++i )
 	{
 		int proxyKey = w->moveArray.data[i];
