@@ -21,6 +21,7 @@
  * first steps (any choice gives the same results).
  */
 #include "b2g_cluster.h"
+#include "b2g_packs.h"
 #include "b2g_stages.h"
 
 #include <cuda_runtime.h>
@@ -128,16 +129,6 @@ __global__ void __launch_bounds__( BATCH_GRID_THREADS ) k_batch_tape( const b2gB
 		for ( int t = threadIdx.x; t < count; t += blockDim.x )
 			tape_record_one( it.W, (float4*)it.tapeBodies, it.bodyIdCount, (b2gTapeRow*)it.tapeRowDst, it.tapeRows, t );
 	}
-}
-
-/* Shared-memory image of one world on its solver CTA: body states (two float4) by
- * body id; after them, for a world that fits, its constraint rows by solve-list
- * position (nine float4 each).  Velocity terms are recomputed every substep from the
- * body's mass, force and extent rather than held, which keeps the image small. */
-__host__ __device__ inline int body_float4s( int bodies ) { return 2 * bodies; }
-__host__ __device__ inline size_t world_smem_bytes( int bodies, int rows )
-{
-	return 16u * (size_t)body_float4s( bodies ) + 144u * (size_t)rows;
 }
 
 struct WorldImage
@@ -369,10 +360,6 @@ __device__ void solve_world( const b2gBatchItem& it, const b2gStepConst& sc, flo
 		finalize_body( W, i, sc );
 }
 
-/* A pack: worlds of similar size solved side by side by one CTA, each by a group of
- * `group` threads with 1 / (T / group) of the CTA's shared memory. */
-#define PACK_WORLDS 16
-#define PACK_INTS ( 1 + PACK_WORLDS )
 
 /* Persistent: each CTA takes the next pack from the queue (packs[0] packs, then
  * PACK_INTS ints each: group size, item indices or -1). */
@@ -649,117 +636,6 @@ extern "C" int b2gd_batch_collide( b2gBatch* b, int h, int first, int n )
 	return (int)e;
 }
 
-/* Builds the packs of items [first, first + n) into the half's hOrder for CTAs of T
- * threads with smem bytes of shared memory.  Each world gets the smallest group (32 ..
- * T threads, powers of two) that holds its bodies in the group's share of shared
- * memory and covers its widest colour in two passes when its rows fit in that share too
- * (they are then kept on chip), in one pass otherwise.  Worlds of one group size are
- * packed largest first; packs go into the queue by their longest world (colours x
- * passes), then alternating from both ends.  Returns the number of packs. */
-static int build_packs( b2gBatch* b, BatchHalf& H, int first, int n, int T, size_t smem )
-{
-	/* per item of the half (local index): */
-	int* groupOf = H.hScratch;			 /* group size, 0 when not solved */
-	int* byGroup = H.hScratch + n;		 /* local indices by group size, largest first */
-	int* packCost = H.hScratch + 2 * n; /* per pack */
-	int* sizeKey = H.hScratch + 3 * n;	 /* body count */
-	int* cost = H.hScratch + 4 * n;	 /* colours x passes */
-	int* packs = H.hOrder + 1;
-	int* tmp = H.hOrder + 1 + PACK_INTS * n;
-	int top = 1;
-	for ( int i = 0; i < n; ++i )
-	{
-		b2gBatchItem& it = b->hItems[first + i];
-		it.rowsOnChip = 0;
-		groupOf[i] = 0;
-		if ( it.solve == 0 )
-			continue;
-		/* rows on chip: two passes per colour; rows in global memory: one, so that fewer
-		 * such worlds are resident at once and their rows stay in L2 */
-		int g = 32;
-		bool onChip = false;
-		for ( ;; )
-		{
-			size_t share = ( smem / (size_t)( T / g ) ) / 16u * 16u;
-			onChip = world_smem_bytes( it.bodyIdCount, it.colorStart[B2G_COLORS] ) <= share;
-			bool bodiesFit = 32u * (size_t)it.bodyIdCount <= share;
-			if ( g >= T || ( bodiesFit && ( onChip ? 2 : 1 ) * g >= it.widest ) )
-				break;
-			g *= 2;
-		}
-		groupOf[i] = g;
-		it.rowsOnChip = onChip ? 1 : 0;
-		sizeKey[i] = it.bodyIdCount;
-		cost[i] = ( it.activeCount + 1 ) * ( ( it.widest + g - 1 ) / g + 1 );
-		top = it.bodyIdCount > top ? it.bodyIdCount : top;
-	}
-	/* counting sort on (group size, body count): 5 group sizes (32 .. 512) x 64 size buckets */
-	const int buckets = 64;
-	const int groups = 5;
-	int count[groups * buckets + 1];
-	memset( count, 0, sizeof( count ) );
-	auto key = [&]( int i ) {
-		int gk = 0;
-		for ( int g = groupOf[i]; g > 32; g >>= 1 )
-			gk += 1;
-		return gk * buckets + buckets - 1 - (int)( (long long)sizeKey[i] * ( buckets - 1 ) / top );
-	};
-	for ( int i = 0; i < n; ++i )
-		if ( groupOf[i] )
-			count[key( i )] += 1;
-	for ( int k = 0, s = 0; k <= groups * buckets; ++k )
-	{
-		int c = count[k];
-		count[k] = s;
-		s += c;
-	}
-	int m = count[groups * buckets];
-	for ( int i = 0; i < n; ++i )
-		if ( groupOf[i] )
-			byGroup[count[key( i )]++] = i;
-	/* packs of T / g consecutive worlds of one group size */
-	int P = 0, costTop = 1;
-	for ( int k = 0; k < m; )
-	{
-		int g = groupOf[byGroup[k]];
-		int* p = tmp + PACK_INTS * P;
-		p[0] = g;
-		int most = 0;
-		for ( int j = 0; j < PACK_WORLDS; ++j )
-		{
-			bool take = j < T / g && k < m && groupOf[byGroup[k]] == g;
-			int li = take ? byGroup[k++] : -1;
-			p[1 + j] = take ? first + li : -1;
-			if ( take )
-				most = cost[li] > most ? cost[li] : most;
-		}
-		packCost[P++] = most;
-		costTop = most > costTop ? most : costTop;
-	}
-	/* queue order: costliest first (counting sort), then alternating from both ends */
-	int ccount[buckets + 1];
-	memset( ccount, 0, sizeof( ccount ) );
-	auto ckey = [&]( int q ) { return buckets - 1 - (int)( (long long)packCost[q] * ( buckets - 1 ) / costTop ); };
-	for ( int q = 0; q < P; ++q )
-		ccount[ckey( q )] += 1;
-	for ( int k = 0, s = 0; k <= buckets; ++k )
-	{
-		int c = ccount[k];
-		ccount[k] = s;
-		s += c;
-	}
-	int* sorted = byGroup; /* reused: pack indices by cost */
-	for ( int q = 0; q < P; ++q )
-		sorted[ccount[ckey( q )]++] = q;
-	for ( int i = 0, lo = 0, hi = P - 1; lo <= hi; ++i )
-	{
-		int q = ( i & 1 ) == 0 ? sorted[lo++] : sorted[hi--];
-		memcpy( packs + PACK_INTS * i, tmp + PACK_INTS * q, sizeof( int ) * PACK_INTS );
-	}
-	H.hOrder[0] = P;
-	return P;
-}
-
 extern "C" int b2gd_batch_solve( b2gBatch* b, int h, int first, int n )
 {
 	if ( n <= 0 )
@@ -781,7 +657,7 @@ extern "C" int b2gd_batch_solve( b2gBatch* b, int h, int first, int n )
 	smem = smem > target ? smem : target;
 	if ( smem > CTA_SHARED_MAX )
 		return (int)cudaErrorInvalidValue;
-	build_packs( b, H, first, n, tc.threads, smem );
+	b2g_build_packs( b->hItems, first, n, tc.threads, smem, H.hScratch, H.hOrder );
 
 	if ( H.solveExec[choice] == nullptr || H.solveN[choice] != n || H.solveFirst[choice] != first || H.solveSmem[choice] != (int)smem )
 	{

@@ -40,3 +40,15 @@ def test_host_tree_matches_oracle_tree(tmp_path):
     r = subprocess.run([exe], capture_output=True, text=True, timeout=120)
     assert r.returncode == 0, r.stdout + r.stderr
     assert r.stdout.startswith("ok")
+
+
+def test_batched_world_packing(tmp_path):
+    """The batched solver's packing of worlds into CTAs (box2c_gb300/csrc/b2g_packs.h) on
+    seeded random batches (tests/c/packs_check.cpp)."""
+    exe = str(tmp_path / "packs_check")
+    src = os.path.join(REPO, "box2c_gb300", "csrc")
+    subprocess.run(["g++", "-std=c++17", "-O2", "-I", src, "-I", os.path.join(REPO, "include"),
+                    os.path.join(REPO, "tests", "c", "packs_check.cpp"), "-o", exe], check=True, capture_output=True)
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert r.stdout.startswith("ok")
