@@ -467,7 +467,7 @@ def run_gpu(args):
     peak, peak_kind = measured_peak()
     achieved = solver_bytes / (solve_dev * 1e-3) / 1e9 if solve_dev > 0 else 0.0
     status = L.b2World_GetStatus(w)
-    toi = L.b2World_GetUnsupportedToiCount(w)
+    toi = L.b2World_GetToiEventCount(w)
     g.destroy(w)
 
     batch = run_batch(g, args.batch_steps, 5, args.batch_worlds) if args.batch_steps > 0 else None
@@ -507,7 +507,7 @@ def run_gpu(args):
         "cpu_baseline": ({"value": round(cpu_ms, 4), "unit": "ms/step", "cores": cpu_cores, "kind": "port",
                           "sample": f"{cpu_n} steps of the same 100-row pyramid after 100 settling steps"}
                          if cpu_ms is not None else None),
-        "clocks": clocks, "status": status, "unsupported_toi": toi,
+        "clocks": clocks, "status": status, "toi_events": toi,
         "batched": batch,
         "tumbler": tumbler,
         "differentiable": adjoint,

@@ -124,6 +124,18 @@ class Backend:
         S.b2s_hello_world.restype = WorldId
         S.b2s_tilted_stacks.argtypes = []
         S.b2s_tilted_stacks.restype = WorldId
+        S.b2s_joint_grid.argtypes = [C.c_int, C.c_float]
+        S.b2s_joint_grid.restype = WorldId
+        S.b2s_many_pyramids.argtypes = [C.c_int, C.c_int, C.c_int]
+        S.b2s_many_pyramids.restype = WorldId
+        S.b2s_shape_pile.argtypes = [C.c_int, C.c_uint64]
+        S.b2s_shape_pile.restype = WorldId
+        S.b2s_joint_hub.argtypes = [C.c_int, C.c_int, C.c_int, C.c_uint64]
+        S.b2s_joint_hub.restype = WorldId
+        S.b2s_joint_chains.argtypes = [C.c_int, C.c_int, C.c_int, C.c_uint64]
+        S.b2s_joint_chains.restype = WorldId
+        S.b2s_fast_shots.argtypes = [C.c_int, C.c_uint64]
+        S.b2s_fast_shots.restype = WorldId
         S.b2s_draw_ints.argtypes = [C.c_int, C.c_uint64, C.c_int, C.c_int, C.c_void_p]
         S.b2s_draw_ints.restype = None
         S.b2s_draw_uniform.argtypes = [C.c_int, C.c_uint64, C.c_float, C.c_float, C.c_void_p]
@@ -154,6 +166,31 @@ class Backend:
 
     def tilted_stacks(self) -> WorldId:
         return self.scenes.b2s_tilted_stacks()
+
+    def joint_grid(self, n: int = 100, gravity_y: float = 0.0) -> WorldId:
+        return self._made(self.scenes.b2s_joint_grid(n, gravity_y))
+
+    def many_pyramids(self, rows: int = 20, columns: int = 20, base: int = 10) -> WorldId:
+        return self._made(self.scenes.b2s_many_pyramids(rows, columns, base))
+
+    def shape_pile(self, count: int = 600, seed: int = 1239) -> WorldId:
+        return self._made(self.scenes.b2s_shape_pile(count, seed))
+
+    def joint_hub(self, spokes: int = 20, chains: int = 6, flags: int = 0, seed: int = 1240) -> WorldId:
+        """flags: 1 joint limits, 2 joint springs, 4 motors."""
+        return self._made(self.scenes.b2s_joint_hub(spokes, chains, flags, seed))
+
+    def joint_chains(self, chains: int = 8, links: int = 8, flags: int = 7, seed: int = 1242) -> WorldId:
+        """flags: 1 joint limits, 2 joint springs, 4 motors."""
+        return self._made(self.scenes.b2s_joint_chains(chains, links, flags, seed))
+
+    def fast_shots(self, count: int = 60, seed: int = 1241) -> WorldId:
+        return self._made(self.scenes.b2s_fast_shots(count, seed))
+
+    def _made(self, w: WorldId) -> WorldId:
+        if w.index1 == 0:
+            raise RuntimeError(f"{self.name}: world creation failed")
+        return w
 
     def draw_ints(self, n, seed, lo, hi):
         out = np.zeros(n, np.int32)
@@ -262,8 +299,8 @@ def bind_gpu_api(lib: C.CDLL) -> None:
     """Binds the additive device entry points of include/box2d/gpu.h."""
     lib.b2World_GetStatus.argtypes = [WorldId]
     lib.b2World_GetStatus.restype = C.c_int
-    lib.b2World_GetUnsupportedToiCount.argtypes = [WorldId]
-    lib.b2World_GetUnsupportedToiCount.restype = C.c_int
+    lib.b2World_GetToiEventCount.argtypes = [WorldId]
+    lib.b2World_GetToiEventCount.restype = C.c_int
     lib.b2World_EnableDeviceTiming.argtypes = [WorldId, C.c_bool]
     lib.b2World_EnableDeviceTiming.restype = None
     lib.b2World_GetDeviceTimes.argtypes = [WorldId]

@@ -70,6 +70,7 @@ void b2World_BeginTape( b2WorldId worldId, int maxSteps )
 	t->used = 0;
 	t->maxRows = 0;
 	t->bodies = w->bodyIds.next;
+	w->tapeToiEvents = 0;
 }
 
 int b2World_GetTapeSteps( b2WorldId worldId )
@@ -309,7 +310,8 @@ int b2World_StepBackwardBatch( const b2WorldId* worldIds, int count, int bodyStr
 					sizeof( float ) * (size_t)w->shapeIds.next );
 		s_lastCheck[0] += status[4 * i + 2];
 		s_lastCheck[1] += status[4 * i + 3];
-		if ( status[4 * i] != 0 )
+		/* a time-of-impact event moved a body outside the recorded solver stage */
+		if ( status[4 * i] != 0 || w->tapeToiEvents != 0 )
 			result = B2_ADJOINT_UNSUPPORTED;
 		else if ( status[4 * i + 1] != 0 && result == 0 )
 			result = B2_ADJOINT_REPLAY_MISMATCH;

@@ -322,6 +322,25 @@ extern "C" int b2gd_upload_fat( b2gDevWorld* w, int shapeId, const float* fat4 )
 	return h2d( (char*)w->fat + 16u * (size_t)shapeId, fat4, 16u, (cudaStream_t)w->stream );
 }
 
+extern "C" int b2gd_upload_pose( b2gDevWorld* w, int bodyId, const float* xf4, const float* center4, const float* prev4 )
+{
+	cudaStream_t s = (cudaStream_t)w->stream;
+	size_t at = 16u * (size_t)bodyId;
+	int e = h2d( (char*)w->xf + at, xf4, 16u, s );
+	e |= h2d( (char*)w->centers + at, center4, 16u, s );
+	e |= h2d( (char*)w->prev + at, prev4, 16u, s );
+	return e;
+}
+
+extern "C" int b2gd_upload_shape_boxes( b2gDevWorld* w, int shapeId, const float* aabb4, const float* fat4 )
+{
+	cudaStream_t s = (cudaStream_t)w->stream;
+	size_t at = 16u * (size_t)shapeId;
+	int e = h2d( (char*)w->aabb + at, aabb4, 16u, s );
+	e |= h2d( (char*)w->fat + at, fat4, 16u, s );
+	return e;
+}
+
 extern "C" int b2gd_upload_body_velocity( b2gDevWorld* w, int bodyId, const float* v3 )
 {
 	return h2d( (char*)w->state + 32u * (size_t)bodyId, v3, 12u, (cudaStream_t)w->stream );

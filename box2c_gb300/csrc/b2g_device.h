@@ -61,6 +61,10 @@ int b2gd_upload_joints( b2gDevWorld* w, const b2gJointDev* joints, int count );
 int b2gd_upload_solve_lists( b2gDevWorld* w, const int* solveList, int solveCount, const int* jointList, int jointCount );
 int b2gd_upload_fat( b2gDevWorld* w, int shapeId, const float* fat4 );
 int b2gd_upload_body_velocity( b2gDevWorld* w, int bodyId, const float* v3 );
+/* Pose of one body after a time-of-impact event: transform, centre (with local centre)
+ * and sweep start; tight and fat boxes of one of its shapes.  Stream-ordered copies. */
+int b2gd_upload_pose( b2gDevWorld* w, int bodyId, const float* xf4, const float* center4, const float* prev4 );
+int b2gd_upload_shape_boxes( b2gDevWorld* w, int shapeId, const float* aabb4, const float* fat4 );
 
 /* Device -> host copies. */
 int b2gd_download_bodies( b2gDevWorld* w, float* state, float* xf, float* centers, int count );

@@ -465,26 +465,22 @@ static __device__ __forceinline__ void store_row( const b2gDevWorld& W, int k, i
 	}
 }
 
+/* Appends a finalisation record; the sweep poses are written for fast shapes only. */
 static __device__ __forceinline__ void emit_record( const b2gDevWorld& W, int awakeIndex, int slot, int shapeId, int flags, b2gBox fat,
-											 b2gBox sweep )
+											 b2gBox sweep, const float4* pose1 = nullptr, const float4* pose2 = nullptr )
 {
 	int r = atomicAdd( W.counters + 1, 1 );
 	if ( r >= W.recordCap )
 		return;
-	b2gRecord rec;
-	rec.awakeIndex = awakeIndex;
-	rec.slot = slot;
-	rec.shapeId = shapeId;
-	rec.flags = flags;
-	rec.fat[0] = fat.lo.x;
-	rec.fat[1] = fat.lo.y;
-	rec.fat[2] = fat.hi.x;
-	rec.fat[3] = fat.hi.y;
-	rec.sweep[0] = sweep.lo.x;
-	rec.sweep[1] = sweep.lo.y;
-	rec.sweep[2] = sweep.hi.x;
-	rec.sweep[3] = sweep.hi.y;
-	W.records[r] = rec;
+	float4* o = (float4*)( W.records + r );
+	o[0] = make_float4( __int_as_float( awakeIndex ), __int_as_float( slot ), __int_as_float( shapeId ), __int_as_float( flags ) );
+	o[1] = make_float4( fat.lo.x, fat.lo.y, fat.hi.x, fat.hi.y );
+	o[2] = make_float4( sweep.lo.x, sweep.lo.y, sweep.hi.x, sweep.hi.y );
+	if ( pose1 != nullptr )
+	{
+		o[3] = *pose1;
+		o[4] = *pose2;
+	}
 }
 
 static __device__ void finalize_body( const b2gDevWorld& W, int i, const b2gStepConst& sc )
@@ -529,8 +525,11 @@ static __device__ void finalize_body( const b2gDevWorld& W, int i, const b2gStep
 		if ( ( info & B2G_B_TYPE_MASK ) == 2 && sc.enableContinuous && maxVelocity * sc.dt > 0.5f * minExtent )
 			isFast = true;
 	}
-	/* with no time-of-impact event the fast body also advances its sweep start */
-	prev[b] = make_float4( center.x, center.y, q.c, q.s );
+	/* with no time-of-impact event the fast body also advances its sweep start; the host
+	 * moves it back along the sweep when continuous collision finds an impact */
+	float4 pose1 = prev[b];
+	float4 pose2 = make_float4( center.x, center.y, q.c, q.s );
+	prev[b] = pose2;
 
 	int start = W.shapeRange[2 * b];
 	int count = W.shapeRange[2 * b + 1];
@@ -557,7 +556,7 @@ static __device__ void finalize_body( const b2gDevWorld& W, int i, const b2gStep
 				fats[sid] = f4_of( fat );
 				flags |= B2G_R_FAST_ENLARGED;
 			}
-			emit_record( W, i, slot, sid, flags, fat, gbox_union( box1, box2 ) );
+			emit_record( W, i, slot, sid, flags, fat, gbox_union( box1, box2 ), &pose1, &pose2 );
 		}
 		else
 		{

@@ -126,6 +126,10 @@ typedef struct b2gRecord
 	int32_t flags;
 	float fat[4];
 	float sweep[4]; /* swept box of a fast shape (union of old and new boxes) */
+	/* fast shapes only: the body's sweep, start (centre0, rotation0) and end (centre,
+	 * rotation) of the step, for continuous collision on the host */
+	float pose1[4];
+	float pose2[4];
 } b2gRecord;
 
 /* Revolute joint configuration (host-owned) and solver state (device-owned),

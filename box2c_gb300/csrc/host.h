@@ -267,7 +267,8 @@ typedef struct gWorld
 
 	b2Profile profile;
 	int status; /* last CUDA error or 0 */
-	int unsupportedToi;
+	int toiEvents;	   /* time-of-impact events since the world was created */
+	int tapeToiEvents; /* time-of-impact events while the tape records */
 	int lastEventCount, lastRecordCount;
 	double stepStart; /* host clock at the start of the current step phase */
 	int stepIdCount;  /* contact ids of the current step's narrowphase */

@@ -8,6 +8,8 @@
  */
 #include "scenes.h"
 
+#include <math.h>
+#include <stdlib.h>
 #include <string.h>
 
 void b2s_seed( b2sRandom* rng, uint64_t seed )
@@ -321,6 +323,478 @@ b2WorldId b2s_tilted_stacks( void )
 			bd.position = ( b2Vec2 ){ x + offset * i, 0.5f + 1.0f * i };
 			b2BodyId bodyId = b2CreateBody( worldId, &bd );
 			b2CreatePolygonShape( bodyId, &sd, &box );
+		}
+	}
+	return worldId;
+}
+
+b2WorldId b2s_joint_grid( int n, float gravityY )
+{
+	b2WorldDef wd = b2s_world_def();
+	wd.gravity = ( b2Vec2 ){ 0.0f, gravityY };
+	b2WorldId worldId = b2CreateWorld( &wd );
+	if ( B2_IS_NULL( worldId ) || n <= 0 )
+		return worldId;
+
+	/* column k holds the bodies k*n .. k*n + n - 1, top to bottom */
+	b2BodyId* grid = (b2BodyId*)malloc( sizeof( b2BodyId ) * (size_t)n * (size_t)n );
+
+	b2ShapeDef sd = b2DefaultShapeDef();
+	sd.density = 1.0f;
+	sd.filter.categoryBits = 2;
+	sd.filter.maskBits = ~2u;
+	b2Circle circle = { { 0.0f, 0.0f }, 0.4f };
+
+	b2RevoluteJointDef jd = b2DefaultRevoluteJointDef();
+	b2BodyDef bd = b2DefaultBodyDef();
+	bd.enableSleep = false;
+
+	int at = 0;
+	for ( int k = 0; k < n; ++k )
+	{
+		for ( int i = 0; i < n; ++i )
+		{
+			bool anchor = i == 0 && k >= n / 2 - 3 && k <= n / 2 + 3;
+			bd.type = anchor ? b2_staticBody : b2_dynamicBody;
+			bd.position = ( b2Vec2 ){ (float)k, -(float)i };
+			b2BodyId body = b2CreateBody( worldId, &bd );
+			b2CreateCircleShape( body, &sd, &circle );
+			if ( i > 0 )
+			{
+				/* link to the body above */
+				jd.bodyIdA = grid[at - 1];
+				jd.bodyIdB = body;
+				jd.localAnchorA = ( b2Vec2 ){ 0.0f, -0.5f };
+				jd.localAnchorB = ( b2Vec2 ){ 0.0f, 0.5f };
+				b2CreateRevoluteJoint( worldId, &jd );
+			}
+			if ( k > 0 )
+			{
+				/* link to the body on the left */
+				jd.bodyIdA = grid[at - n];
+				jd.bodyIdB = body;
+				jd.localAnchorA = ( b2Vec2 ){ 0.5f, 0.0f };
+				jd.localAnchorB = ( b2Vec2 ){ -0.5f, 0.0f };
+				b2CreateRevoluteJoint( worldId, &jd );
+			}
+			grid[at++] = body;
+		}
+	}
+	free( grid );
+	return worldId;
+}
+
+b2WorldId b2s_many_pyramids( int rowCount, int columnCount, int baseCount )
+{
+	b2WorldDef wd = b2s_world_def();
+	b2WorldId worldId = b2CreateWorld( &wd );
+	if ( B2_IS_NULL( worldId ) )
+		return worldId;
+
+	float extent = 0.5f;
+	b2BodyDef gd = b2DefaultBodyDef();
+	b2BodyId groundId = b2CreateBody( worldId, &gd );
+
+	/* one ground segment under each row of pyramids, rows stacked groundDeltaY apart */
+	float groundDeltaY = 2.0f * extent * ( baseCount + 1.0f );
+	float groundWidth = 2.0f * extent * columnCount * ( baseCount + 1.0f );
+	b2ShapeDef gsd = b2DefaultShapeDef();
+	float groundY = 0.0f;
+	for ( int i = 0; i < rowCount; ++i )
+	{
+		b2Segment segment = { { -0.5f * 2.0f * groundWidth, groundY }, { 0.5f * 2.0f * groundWidth, groundY } };
+		b2CreateSegmentShape( groundId, &gsd, &segment );
+		groundY += groundDeltaY;
+	}
+
+	b2BodyDef bd = b2DefaultBodyDef();
+	bd.type = b2_dynamicBody;
+	b2ShapeDef sd = b2DefaultShapeDef();
+	b2Polygon box = b2MakeSquare( extent );
+	float baseWidth = 2.0f * extent * baseCount;
+	float baseY = 0.0f;
+	for ( int r = 0; r < rowCount; ++r )
+	{
+		for ( int c = 0; c < columnCount; ++c )
+		{
+			float centerX = -0.5f * groundWidth + c * ( baseWidth + 2.0f * extent ) + extent;
+			for ( int i = 0; i < baseCount; ++i )
+			{
+				float y = ( 2.0f * i + 1.0f ) * extent + baseY;
+				for ( int j = i; j < baseCount; ++j )
+				{
+					float x = ( i + 1.0f ) * extent + 2.0f * ( j - i ) * extent + centerX - 0.5f;
+					bd.position = ( b2Vec2 ){ x, y };
+					b2BodyId bodyId = b2CreateBody( worldId, &bd );
+					b2CreatePolygonShape( bodyId, &sd, &box );
+				}
+			}
+		}
+		baseY += groundDeltaY;
+	}
+	return worldId;
+}
+
+b2WorldId b2s_shape_pile( int count, uint64_t seed )
+{
+	b2WorldDef wd = b2s_world_def();
+	b2WorldId worldId = b2CreateWorld( &wd );
+	if ( B2_IS_NULL( worldId ) )
+		return worldId;
+
+	/* static funnel: a floor segment, two sloped segments, a static capsule bar and a
+	 * static box ledge */
+	b2BodyDef gd = b2DefaultBodyDef();
+	b2BodyId groundId = b2CreateBody( worldId, &gd );
+	b2ShapeDef gsd = b2DefaultShapeDef();
+	b2Segment floorSeg = { { -12.0f, 0.0f }, { 12.0f, 0.0f } };
+	b2CreateSegmentShape( groundId, &gsd, &floorSeg );
+	b2Segment left = { { -12.0f, 0.0f }, { -16.0f, 12.0f } };
+	b2CreateSegmentShape( groundId, &gsd, &left );
+	b2Segment right = { { 12.0f, 0.0f }, { 16.0f, 12.0f } };
+	b2CreateSegmentShape( groundId, &gsd, &right );
+	b2Capsule bar = { { -4.0f, 3.0f }, { -1.0f, 2.0f }, 0.25f };
+	b2CreateCapsuleShape( groundId, &gsd, &bar );
+	b2Polygon ledge = b2MakeOffsetBox( 1.5f, 0.25f, ( b2Vec2 ){ 4.0f, 2.5f }, 0.0f );
+	b2CreatePolygonShape( groundId, &gsd, &ledge );
+
+	b2BodyDef bd = b2DefaultBodyDef();
+	bd.type = b2_dynamicBody;
+	b2ShapeDef sd = b2DefaultShapeDef();
+	sd.density = 1.0f;
+	sd.friction = 0.6f;
+
+	/* seeded jittered grid of 1 m cells above the funnel: 20 columns, rows upward;
+	 * five shape kinds in turn */
+	b2sRandom rng;
+	b2s_seed( &rng, seed );
+	b2Capsule capsule = { { -0.25f, 0.0f }, { 0.25f, 0.0f }, 0.3f };
+	b2Capsule upright = { { 0.0f, -0.2f }, { 0.0f, 0.2f }, 0.3f };
+	b2Polygon box = b2MakeBox( 0.35f, 0.3f );
+	b2Polygon rounded = b2MakeRoundedBox( 0.25f, 0.2f, 0.1f );
+	b2Circle circle = { { 0.0f, 0.0f }, 0.35f };
+	for ( int k = 0; k < count; ++k )
+	{
+		int col = k % 20;
+		int row = k / 20;
+		float x = -9.5f + 1.0f * col + b2s_uniform( &rng, -0.05f, 0.05f );
+		float y = 4.5f + 1.05f * row + b2s_uniform( &rng, -0.05f, 0.05f );
+		bd.position = ( b2Vec2 ){ x, y };
+		b2BodyId bodyId = b2CreateBody( worldId, &bd );
+		switch ( k % 5 )
+		{
+			case 0:
+				b2CreateCapsuleShape( bodyId, &sd, &capsule );
+				break;
+			case 1:
+				b2CreatePolygonShape( bodyId, &sd, &box );
+				break;
+			case 2:
+				b2CreateCircleShape( bodyId, &sd, &circle );
+				break;
+			case 3:
+				b2CreatePolygonShape( bodyId, &sd, &rounded );
+				break;
+			default:
+				b2CreateCapsuleShape( bodyId, &sd, &upright );
+				break;
+		}
+	}
+	return worldId;
+}
+
+/* Point on the unit circle at parameter t in [-1, 1] (quarter turn per unit), by the
+ * rational parametrisation ((1 - t^2), 2t) / (1 + t^2): float arithmetic only. */
+static b2Vec2 b2s_circle_point( float t )
+{
+	float d = 1.0f + t * t;
+	return ( b2Vec2 ){ ( 1.0f - t * t ) / d, 2.0f * t / d };
+}
+
+b2WorldId b2s_joint_hub( int spokes, int chains, int flags, uint64_t seed )
+{
+	b2WorldDef wd = b2s_world_def();
+	b2WorldId worldId = b2CreateWorld( &wd );
+	if ( B2_IS_NULL( worldId ) )
+		return worldId;
+	b2s_ground( worldId, 0.6f );
+
+	b2BodyDef anchorDef = b2DefaultBodyDef();
+	b2BodyId anchorId = b2CreateBody( worldId, &anchorDef );
+
+	b2BodyDef bd = b2DefaultBodyDef();
+	bd.type = b2_dynamicBody;
+	bd.enableSleep = false;
+	b2ShapeDef sd = b2DefaultShapeDef();
+	sd.density = 1.0f;
+	sd.friction = 0.6f;
+
+	b2RevoluteJointDef jd = b2DefaultRevoluteJointDef();
+	bool limits = ( flags & 1 ) != 0;
+	bool springs = ( flags & 2 ) != 0;
+	bool motor = ( flags & 4 ) != 0;
+
+	/* hub: a circle of radius 1 at (0, 8) pinned to the static anchor */
+	b2Vec2 hubCenter = { 0.0f, 8.0f };
+	bd.position = hubCenter;
+	b2BodyId hubId = b2CreateBody( worldId, &bd );
+	b2Circle hubCircle = { { 0.0f, 0.0f }, 1.0f };
+	b2CreateCircleShape( hubId, &sd, &hubCircle );
+	jd.bodyIdA = anchorId;
+	jd.bodyIdB = hubId;
+	jd.localAnchorA = hubCenter;
+	jd.localAnchorB = ( b2Vec2 ){ 0.0f, 0.0f };
+	jd.enableMotor = motor;
+	jd.motorSpeed = 1.0f;
+	jd.maxMotorTorque = 2000.0f;
+	b2CreateRevoluteJoint( worldId, &jd );
+
+	/* spokes: boxes on a ring of radius 2.5 around the hub, each pinned to the hub at its
+	 * own centre and to the next spoke; the hub's joints beyond the graph's colours go to
+	 * the overflow set */
+	b2Polygon spokeBox = b2MakeBox( 0.3f, 0.3f );
+	b2BodyId first = b2_nullBodyId, prev = b2_nullBodyId;
+	b2Vec2 prevPos = { 0.0f, 0.0f }, firstPos = { 0.0f, 0.0f };
+	for ( int k = 0; k < spokes; ++k )
+	{
+		/* four quarter arcs of spokes / 4 points each */
+		int quarter = ( 4 * k ) / ( spokes > 0 ? spokes : 1 );
+		float t = -1.0f + 2.0f * ( (float)( 4 * k - quarter * spokes ) + 0.5f ) / (float)spokes;
+		b2Vec2 u = b2s_circle_point( t );
+		for ( int q = 0; q < quarter; ++q )
+			u = ( b2Vec2 ){ -u.y, u.x };
+		b2Vec2 offset = { 2.5f * u.x, 2.5f * u.y };
+		b2Vec2 pos = { hubCenter.x + offset.x, hubCenter.y + offset.y };
+		bd.position = pos;
+		b2BodyId spokeId = b2CreateBody( worldId, &bd );
+		b2CreatePolygonShape( spokeId, &sd, &spokeBox );
+
+		jd = b2DefaultRevoluteJointDef();
+		jd.bodyIdA = hubId;
+		jd.bodyIdB = spokeId;
+		jd.localAnchorA = offset;
+		jd.localAnchorB = ( b2Vec2 ){ 0.0f, 0.0f };
+		jd.enableLimit = limits;
+		jd.lowerAngle = -0.2f * b2_pi;
+		jd.upperAngle = 0.1f * b2_pi;
+		jd.enableSpring = springs;
+		jd.hertz = 1.5f;
+		jd.dampingRatio = 0.4f;
+		jd.enableMotor = motor && ( k % 3 ) == 0;
+		jd.motorSpeed = ( k & 1 ) ? 0.5f : -0.5f;
+		jd.maxMotorTorque = 5.0f;
+		b2CreateRevoluteJoint( worldId, &jd );
+
+		if ( k > 0 )
+		{
+			jd = b2DefaultRevoluteJointDef();
+			jd.bodyIdA = prev;
+			jd.bodyIdB = spokeId;
+			b2Vec2 mid = { 0.5f * ( prevPos.x + pos.x ), 0.5f * ( prevPos.y + pos.y ) };
+			jd.localAnchorA = ( b2Vec2 ){ mid.x - prevPos.x, mid.y - prevPos.y };
+			jd.localAnchorB = ( b2Vec2 ){ mid.x - pos.x, mid.y - pos.y };
+			b2CreateRevoluteJoint( worldId, &jd );
+		}
+		else
+		{
+			first = spokeId;
+			firstPos = pos;
+		}
+		prev = spokeId;
+		prevPos = pos;
+	}
+	if ( spokes > 2 )
+	{
+		jd = b2DefaultRevoluteJointDef();
+		jd.bodyIdA = prev;
+		jd.bodyIdB = first;
+		b2Vec2 mid = { 0.5f * ( prevPos.x + firstPos.x ), 0.5f * ( prevPos.y + firstPos.y ) };
+		jd.localAnchorA = ( b2Vec2 ){ mid.x - prevPos.x, mid.y - prevPos.y };
+		jd.localAnchorB = ( b2Vec2 ){ mid.x - firstPos.x, mid.y - firstPos.y };
+		b2CreateRevoluteJoint( worldId, &jd );
+	}
+
+	/* chains: capsule links of length 0.5 hanging from static pins on a line at y = 14,
+	 * laid out along a 45 degree diagonal so they swing down; adjacent links are jointed
+	 * and do not collide */
+	b2sRandom rng;
+	b2s_seed( &rng, seed );
+	b2Capsule link = { { -0.25f, 0.0f }, { 0.25f, 0.0f }, 0.2f };
+	const int links = 6;
+	for ( int c = 0; c < chains; ++c )
+	{
+		b2Vec2 pin = { -12.0f + 4.0f * c, 14.0f };
+		b2BodyId above = anchorId;
+		b2Vec2 aboveAnchor = pin;
+		for ( int i = 0; i < links; ++i )
+		{
+			/* link i spans pin + d * (i, i+1) along d = (0.3536, -0.3536) */
+			float s = 0.35355339f;
+			b2Vec2 center = { pin.x + s * ( i + 0.5f ), pin.y - s * ( i + 0.5f ) };
+			bd.position = center;
+			bd.rotation = ( b2Rot ){ 0.70710678f, -0.70710678f };
+			bd.angularVelocity = b2s_uniform( &rng, -0.5f, 0.5f );
+			b2BodyId linkId = b2CreateBody( worldId, &bd );
+			b2CreateCapsuleShape( linkId, &sd, &link );
+
+			jd = b2DefaultRevoluteJointDef();
+			jd.bodyIdA = above;
+			jd.bodyIdB = linkId;
+			jd.localAnchorA = aboveAnchor;
+			jd.localAnchorB = ( b2Vec2 ){ -0.25f, 0.0f };
+			jd.referenceAngle = i == 0 ? -0.25f * b2_pi : 0.0f;
+			jd.enableLimit = limits;
+			jd.lowerAngle = -0.3f * b2_pi;
+			jd.upperAngle = 0.3f * b2_pi;
+			jd.enableSpring = springs && ( i & 1 ) == 0;
+			jd.hertz = 3.0f;
+			jd.dampingRatio = 0.7f;
+			b2CreateRevoluteJoint( worldId, &jd );
+
+			above = linkId;
+			aboveAnchor = ( b2Vec2 ){ 0.25f, 0.0f };
+		}
+	}
+	bd.rotation = b2Rot_identity;
+	bd.angularVelocity = 0.0f;
+
+	/* a few boxes dropped onto the spokes and the chains */
+	b2Polygon box = b2MakeBox( 0.4f, 0.4f );
+	for ( int k = 0; k < 12; ++k )
+	{
+		bd.position = ( b2Vec2 ){ -6.0f + 1.1f * k + b2s_uniform( &rng, -0.1f, 0.1f ), 12.0f + 0.5f * ( k & 1 ) };
+		b2BodyId bodyId = b2CreateBody( worldId, &bd );
+		b2CreatePolygonShape( bodyId, &sd, &box );
+	}
+	return worldId;
+}
+
+b2WorldId b2s_fast_shots( int count, uint64_t seed )
+{
+	b2WorldDef wd = b2s_world_def();
+	b2WorldId worldId = b2CreateWorld( &wd );
+	if ( B2_IS_NULL( worldId ) )
+		return worldId;
+
+	/* static: a ground segment and a 0.1 m thick wall at x = 20 */
+	b2BodyDef gd = b2DefaultBodyDef();
+	b2BodyId groundId = b2CreateBody( worldId, &gd );
+	b2ShapeDef gsd = b2DefaultShapeDef();
+	b2Segment floorSeg = { { -10.0f, 0.0f }, { 40.0f, 0.0f } };
+	b2CreateSegmentShape( groundId, &gsd, &floorSeg );
+	b2Polygon wall = b2MakeOffsetBox( 0.05f, 10.0f, ( b2Vec2 ){ 20.0f, 10.0f }, 0.0f );
+	b2CreatePolygonShape( groundId, &gsd, &wall );
+
+	b2ShapeDef sd = b2DefaultShapeDef();
+	sd.density = 1.0f;
+	sd.friction = 0.6f;
+	b2BodyDef bd = b2DefaultBodyDef();
+	bd.type = b2_dynamicBody;
+
+	/* a column of boxes standing in front of the wall: bullets sweep against them */
+	b2Polygon block = b2MakeBox( 0.4f, 0.4f );
+	for ( int i = 0; i < 10; ++i )
+	{
+		bd.position = ( b2Vec2 ){ 15.0f, 0.4f + 0.8f * i };
+		b2BodyId bodyId = b2CreateBody( worldId, &bd );
+		b2CreatePolygonShape( bodyId, &sd, &block );
+	}
+
+	/* projectiles fired at the wall at 60 to 120 m/s: circles, boxes and capsules in
+	 * turn; every fourth is a bullet */
+	b2sRandom rng;
+	b2s_seed( &rng, seed );
+	b2Circle circle = { { 0.0f, 0.0f }, 0.1f };
+	b2Polygon box = b2MakeBox( 0.1f, 0.1f );
+	b2Capsule capsule = { { -0.1f, 0.0f }, { 0.1f, 0.0f }, 0.08f };
+	for ( int k = 0; k < count; ++k )
+	{
+		bd.position = ( b2Vec2 ){ b2s_uniform( &rng, 0.0f, 5.0f ), b2s_uniform( &rng, 1.0f, 15.0f ) };
+		bd.linearVelocity = ( b2Vec2 ){ b2s_uniform( &rng, 60.0f, 120.0f ), b2s_uniform( &rng, -5.0f, 5.0f ) };
+		bd.angularVelocity = b2s_uniform( &rng, -10.0f, 10.0f );
+		bd.isBullet = ( k & 3 ) == 3;
+		b2BodyId bodyId = b2CreateBody( worldId, &bd );
+		switch ( k % 3 )
+		{
+			case 0:
+				b2CreateCircleShape( bodyId, &sd, &circle );
+				break;
+			case 1:
+				b2CreatePolygonShape( bodyId, &sd, &box );
+				break;
+			default:
+				b2CreateCapsuleShape( bodyId, &sd, &capsule );
+				break;
+		}
+	}
+	return worldId;
+}
+
+/* Rotation with the direction of (x, y): sqrtf and division only. */
+static b2Rot b2s_unit( float x, float y )
+{
+	float len = sqrtf( x * x + y * y );
+	return ( b2Rot ){ x / len, y / len };
+}
+
+b2WorldId b2s_joint_chains( int chains, int links, int flags, uint64_t seed )
+{
+	b2WorldDef wd = b2s_world_def();
+	b2WorldId worldId = b2CreateWorld( &wd );
+	if ( B2_IS_NULL( worldId ) )
+		return worldId;
+
+	b2BodyDef anchorDef = b2DefaultBodyDef();
+	b2BodyId anchorId = b2CreateBody( worldId, &anchorDef );
+
+	/* links never touch: one category that its own mask excludes */
+	b2ShapeDef sd = b2DefaultShapeDef();
+	sd.density = 1.0f;
+	sd.filter.categoryBits = 4;
+	sd.filter.maskBits = ~4u;
+	b2Capsule link = { { -0.25f, 0.0f }, { 0.25f, 0.0f }, 0.1f };
+
+	b2BodyDef bd = b2DefaultBodyDef();
+	bd.type = b2_dynamicBody;
+	bd.enableSleep = false;
+	bd.angularDamping = 0.1f;
+
+	b2sRandom rng;
+	b2s_seed( &rng, seed );
+	for ( int c = 0; c < chains; ++c )
+	{
+		b2Vec2 pin = { 3.0f * c, 0.0f };
+		/* chains start along a line tilted by a seeded slope below the horizontal */
+		float slope = b2s_uniform( &rng, 0.2f, 1.0f );
+		b2Rot rot = b2s_unit( 1.0f, -slope );
+		b2BodyId above = anchorId;
+		b2Vec2 aboveAnchor = pin;
+		for ( int i = 0; i < links; ++i )
+		{
+			b2Vec2 center = { pin.x + rot.c * 0.5f * ( i + 0.5f ), pin.y + rot.s * 0.5f * ( i + 0.5f ) };
+			bd.position = center;
+			bd.rotation = rot;
+			b2BodyId linkId = b2CreateBody( worldId, &bd );
+			b2CreateCapsuleShape( linkId, &sd, &link );
+
+			b2RevoluteJointDef jd = b2DefaultRevoluteJointDef();
+			jd.bodyIdA = above;
+			jd.bodyIdB = linkId;
+			jd.localAnchorA = aboveAnchor;
+			jd.localAnchorB = ( b2Vec2 ){ -0.25f, 0.0f };
+			jd.enableLimit = ( flags & 1 ) != 0;
+			jd.lowerAngle = -0.3f * b2_pi;
+			jd.upperAngle = 0.15f * b2_pi;
+			jd.enableSpring = ( flags & 2 ) != 0;
+			jd.hertz = 2.0f;
+			jd.dampingRatio = 0.5f;
+			jd.enableMotor = ( flags & 4 ) != 0 && ( i % 3 ) == 1;
+			jd.motorSpeed = ( c & 1 ) ? 0.5f : -0.5f;
+			jd.maxMotorTorque = 2.0f;
+			b2CreateRevoluteJoint( worldId, &jd );
+
+			above = linkId;
+			aboveAnchor = ( b2Vec2 ){ 0.25f, 0.0f };
 		}
 	}
 	return worldId;

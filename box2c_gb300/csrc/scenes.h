@@ -55,6 +55,39 @@ b2WorldId b2s_tumbler( int count, uint64_t seed, int variant );
  * (vx[k], vy[k]), on the pyramid ground; every shape uses `friction`. */
 b2WorldId b2s_drop_boxes( int count, const float* heights, const float* vx, const float* vy, float friction );
 
+/* Reference benchmark/joint_grid.c: an n x n grid of circles (radius 0.4, filtered so
+ * that no two touch) with revolute joints to the neighbours above and to the left; the
+ * seven centre bodies of the top row are static.  The benchmark has n = 100 and no
+ * gravity; a negative gravityY makes the grid hang and swing from its static anchors. */
+b2WorldId b2s_joint_grid( int n, float gravityY );
+
+/* Reference benchmark/many_pyramids.c: rowCount x columnCount pyramids of baseCount
+ * boxes (half-extent 0.5, default material), each row of pyramids standing on its own
+ * static segment; sleep off.  The benchmark has 20 x 20 pyramids of base 10. */
+b2WorldId b2s_many_pyramids( int rowCount, int columnCount, int baseCount );
+
+/* Mixed-shape pile in a static funnel of segments (floor, two slopes) with a static
+ * capsule bar and a static box ledge: `count` bodies dropped from a seeded jittered
+ * grid, in turn a horizontal capsule, a box, a circle, a rounded box and an upright
+ * capsule.  Every registered shape pair of the narrowphase occurs. */
+b2WorldId b2s_shape_pile( int count, uint64_t seed );
+
+/* Revolute joint scene: a hub circle pinned to a static anchor, `spokes` boxes on a ring
+ * pinned to the hub and to each other (the hub's joints beyond the colours go to the
+ * overflow set), `chains` six-link capsule chains swinging from static pins, and twelve
+ * boxes dropped onto them.  flags: 1 joint limits, 2 joint springs, 4 motors. */
+b2WorldId b2s_joint_hub( int spokes, int chains, int flags, uint64_t seed );
+
+/* Contact-free revolute chains: `chains` chains of `links` capsules (filtered so that no
+ * two shapes touch) swinging from static pins, with joint limits (flags & 1), damped
+ * springs (flags & 2) and motors on every third joint (flags & 4). */
+b2WorldId b2s_joint_chains( int chains, int links, int flags, uint64_t seed );
+
+/* Continuous collision scene: `count` small projectiles (circles, boxes, capsules; every
+ * fourth a bullet) fired at 60 to 120 m/s at a 0.1 m thick static wall, past a column of
+ * ten dynamic boxes, above a static ground segment. */
+b2WorldId b2s_fast_shots( int count, uint64_t seed );
+
 /* Draws `n` integers uniform in [lo, hi] from `seed` into out. */
 void b2s_draw_ints( int n, uint64_t seed, int lo, int hi, int* out );
 /* Draws `n` floats uniform in [lo, hi) / standard normal from `seed` into out. */

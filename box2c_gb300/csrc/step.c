@@ -13,6 +13,7 @@
  * Steps 3 and 5 only touch the few contacts and proxies whose state changed.
  */
 #include "host.h"
+#include "b2g_toi.h"
 
 #include <string.h>
 
@@ -525,35 +526,6 @@ static void process_events( gWorld* w, int count )
 }
 
 /* ------------------------------------------------------------ finalisation records */
-typedef struct gSweepCtx
-{
-	gWorld* w;
-	gShape* fast;
-	int hits;
-} gSweepCtx;
-
-/* Candidate filter of the fast-body sweep (reference src/solver.c:800-858).  Time of
- * impact is not computed: a sweep that reaches it is counted in the world status. */
-static bool sweep_query( int proxyId, int shapeId, void* context )
-{
-	(void)proxyId;
-	gSweepCtx* q = (gSweepCtx*)context;
-	gWorld* w = q->w;
-	if ( shapeId == q->fast->id )
-		return true;
-	gShape* s = w->shapes + shapeId;
-	if ( s->bodyId == q->fast->bodyId )
-		return true;
-	if ( should_shapes_collide( q->fast->filter, s->filter ) == false )
-		return true;
-	if ( s->isSensor )
-		return true;
-	if ( w->bodies[s->bodyId].isBullet )
-		return true;
-	q->hits += 1;
-	return true;
-}
-
 static int cmp_record( const void* a, const void* b )
 {
 	const b2gRecord* x = (const b2gRecord*)a;
@@ -569,6 +541,192 @@ static b2gBox box4( const float* f )
 	b.lo = gv( f[0], f[1] );
 	b.hi = gv( f[2], f[3] );
 	return b;
+}
+
+/* Continuous collision of one fast body (reference src/solver.c:787-1105): the static
+ * shapes (and, for a bullet, kinematic and dynamic shapes) its shapes sweep over, in the
+ * host trees' query order, lower the body's time-of-impact fraction. */
+typedef struct gSweepCtx
+{
+	gWorld* w;
+	gShape* fast;
+	gBody* fastBody;
+	b2gSweep sweep;
+	float fraction;
+} gSweepCtx;
+
+/* Sweep of a body from the host mirrors: static bodies never move; the others are read
+ * after the mirrors were refreshed from the device. */
+static b2gSweep mirror_sweep( const gWorld* w, int bodyId )
+{
+	const float* x = w->hXf + 4 * bodyId;
+	const float* c = w->hCenters + 4 * bodyId;
+	const float* p = w->hPrev + 4 * bodyId;
+	b2gSweep s;
+	s.c1 = gv( p[0], p[1] );
+	s.c2 = gv( c[0], c[1] );
+	s.q1 = grot( p[2], p[3] );
+	s.q2 = grot( x[2], x[3] );
+	s.localCenter = gv( c[2], c[3] );
+	return s;
+}
+
+static bool sweep_query( int proxyId, int shapeId, void* context )
+{
+	(void)proxyId;
+	gSweepCtx* q = (gSweepCtx*)context;
+	gWorld* w = q->w;
+	if ( shapeId == q->fast->id )
+		return true;
+	gShape* s = w->shapes + shapeId;
+	if ( s->bodyId == q->fast->bodyId )
+		return true;
+	if ( should_shapes_collide( q->fast->filter, s->filter ) == false )
+		return true;
+	if ( s->isSensor )
+		return true;
+	gBody* body = w->bodies + s->bodyId;
+	if ( body->isBullet )
+		return true;
+	if ( should_bodies_collide( w, q->fastBody, body ) == false )
+		return true;
+
+	b2gProxy pa = gproxy_shape( w->hGeo + shapeId );
+	b2gProxy pb = gproxy_shape( w->hGeo + q->fast->id );
+	b2gSweep sa = mirror_sweep( w, s->bodyId );
+	int state;
+	float t = gtime_of_impact( &pa, &sa, &pb, &q->sweep, q->fraction, &state );
+	if ( 0.0f < t && t < q->fraction )
+		q->fraction = t;
+	else if ( 0.0f == t )
+	{
+		/* fall back to a small circle around the fast shape's centroid */
+		b2gVec centroid = gshape_centroid( w->hGeo + q->fast->id );
+		pb = gproxy_points( &centroid, 1, B2G_SPECULATIVE );
+		t = gtime_of_impact( &pa, &sa, &pb, &q->sweep, q->fraction, &state );
+		if ( 0.0f < t && t < q->fraction )
+			q->fraction = t;
+	}
+	return true;
+}
+
+/* recs: the body's records (one per shape, in shape-list order).  With an impact the
+ * body is moved back along its sweep on the device and the records carry the fat boxes
+ * of the new pose; without one the device's pose and boxes stand. */
+static void solve_continuous( gWorld* w, b2gRecord* recs, int n, bool bullet )
+{
+	int bodyId = w->awake.data[recs[0].awakeIndex];
+	gBody* b = w->bodies + bodyId;
+	gSweepCtx q;
+	q.w = w;
+	q.fastBody = b;
+	q.fraction = 1.0f;
+	q.sweep.c1 = gv( recs[0].pose1[0], recs[0].pose1[1] );
+	q.sweep.q1 = grot( recs[0].pose1[2], recs[0].pose1[3] );
+	q.sweep.c2 = gv( recs[0].pose2[0], recs[0].pose2[1] );
+	q.sweep.q2 = grot( recs[0].pose2[2], recs[0].pose2[3] );
+	q.sweep.localCenter = gv( w->hCenters[4 * bodyId + 2], w->hCenters[4 * bodyId + 3] );
+	for ( int k = 0; k < n; ++k )
+	{
+		gShape* s = w->shapes + recs[k].shapeId;
+		if ( s->isSensor )
+			continue;
+		q.fast = s;
+		b2gBox sweep = box4( recs[k].sweep );
+		gtree_query( w->trees + b2_staticBody, sweep, 0xFFFFFFFFu, sweep_query, &q );
+		if ( bullet )
+		{
+			gtree_query( w->trees + b2_kinematicBody, sweep, 0xFFFFFFFFu, sweep_query, &q );
+			gtree_query( w->trees + b2_dynamicBody, sweep, 0xFFFFFFFFu, sweep_query, &q );
+		}
+	}
+	if ( q.fraction >= 1.0f )
+		return;
+
+	/* time-of-impact event */
+	float f = q.fraction;
+	b2gRot rq = gnormrot( grot( ( 1.0f - f ) * q.sweep.q1.c + f * q.sweep.q2.c, ( 1.0f - f ) * q.sweep.q1.s + f * q.sweep.q2.s ) );
+	b2gVec c = glerp( q.sweep.c1, q.sweep.c2, f );
+	b2gXf xf;
+	xf.q = rq;
+	xf.p = gsub( c, grotate( rq, q.sweep.localCenter ) );
+	float xf4[4] = { xf.p.x, xf.p.y, rq.c, rq.s };
+	float center4[4] = { c.x, c.y, q.sweep.localCenter.x, q.sweep.localCenter.y };
+	float prev4[4] = { c.x, c.y, rq.c, rq.s };
+	int e = b2gd_upload_pose( &w->dev, bodyId, xf4, center4, prev4 );
+	if ( w->mirrorStale == false )
+	{
+		memcpy( w->hXf + 4 * bodyId, xf4, 16 );
+		memcpy( w->hCenters + 4 * bodyId, center4, 16 );
+		memcpy( w->hPrev + 4 * bodyId, prev4, 16 );
+	}
+	for ( int k = 0; k < n; ++k )
+	{
+		b2gRecord* r = recs + k;
+		b2gBox aabb = gshape_geo_aabb( w->hGeo + r->shapeId, xf );
+		aabb.lo.x -= B2G_SPECULATIVE;
+		aabb.lo.y -= B2G_SPECULATIVE;
+		aabb.hi.x += B2G_SPECULATIVE;
+		aabb.hi.y += B2G_SPECULATIVE;
+		b2gBox fat = box4( w->hFat + 4 * r->shapeId );
+		r->flags &= ~B2G_R_FAST_ENLARGED;
+		if ( gbox_contains( fat, aabb ) == false )
+		{
+			fat.lo.x = aabb.lo.x - B2G_AABB_MARGIN;
+			fat.lo.y = aabb.lo.y - B2G_AABB_MARGIN;
+			fat.hi.x = aabb.hi.x + B2G_AABB_MARGIN;
+			fat.hi.y = aabb.hi.y + B2G_AABB_MARGIN;
+			r->flags |= B2G_R_FAST_ENLARGED;
+		}
+		float aabb4[4] = { aabb.lo.x, aabb.lo.y, aabb.hi.x, aabb.hi.y };
+		float fat4[4] = { fat.lo.x, fat.lo.y, fat.hi.x, fat.hi.y };
+		memcpy( r->fat, fat4, 16 );
+		e |= b2gd_upload_shape_boxes( &w->dev, r->shapeId, aabb4, fat4 );
+	}
+	if ( e )
+		w->status = e;
+	w->toiEvents += 1;
+	if ( w->tape )
+		w->tapeToiEvents += 1;
+}
+
+/* Continuous collision of the fast bodies of one class (bullets or not), then their
+ * grown fat boxes into the dynamic tree (reference src/solver.c:1839-1950: fast bodies
+ * first, then bullets, which see the fast bodies' proxies). */
+static void continuous_pass( gWorld* w, b2gRecord* rec, int count, bool bullets )
+{
+	bool mirrored = false;
+	for ( int i = 0; i < count; )
+	{
+		b2gRecord* r = rec + i;
+		int end = i + 1;
+		while ( end < count && rec[end].awakeIndex == r->awakeIndex )
+			++end;
+		if ( ( r->flags & B2G_R_FAST ) && ( ( r->flags & B2G_R_BULLET ) != 0 ) == bullets )
+		{
+			if ( bullets && mirrored == false )
+			{
+				/* a bullet sweeps against moving bodies: their poses after this step */
+				w->mirrorStale = true;
+				gworld_ensure_mirror( w );
+				mirrored = true;
+			}
+			solve_continuous( w, r, end - i, bullets );
+		}
+		i = end;
+	}
+	for ( int i = 0; i < count; ++i )
+	{
+		b2gRecord* r = rec + i;
+		if ( ( r->flags & B2G_R_FAST ) == 0 || ( ( r->flags & B2G_R_BULLET ) != 0 ) != bullets )
+			continue;
+		if ( r->flags & B2G_R_FAST_ENLARGED )
+		{
+			gShape* s = w->shapes + r->shapeId;
+			memcpy( w->hFat + 4 * r->shapeId, r->fat, 16 );
+			gtree_enlarge_proxy( w->trees + b2_dynamicBody, s->proxyKey >> 2, box4( r->fat ) );
+		}
+	}
 }
 
 static void process_records( gWorld* w, int count )
@@ -591,31 +749,8 @@ static void process_records( gWorld* w, int count )
 			gbuffer_move( w, s->proxyKey );
 		}
 	}
-	/* fast shapes: sweep candidates, then enlarge in the dynamic tree (src/solver.c:1807-1954) */
-	for ( int i = 0; i < count; ++i )
-	{
-		b2gRecord* r = rec + i;
-		if ( ( r->flags & B2G_R_FAST ) == 0 )
-			continue;
-		gShape* s = w->shapes + r->shapeId;
-		if ( s->isSensor == false )
-		{
-			gSweepCtx q = { w, s, 0 };
-			b2gBox sweep = box4( r->sweep );
-			gtree_query( w->trees + b2_staticBody, sweep, 0xFFFFFFFFu, sweep_query, &q );
-			if ( r->flags & B2G_R_BULLET )
-			{
-				gtree_query( w->trees + b2_kinematicBody, sweep, 0xFFFFFFFFu, sweep_query, &q );
-				gtree_query( w->trees + b2_dynamicBody, sweep, 0xFFFFFFFFu, sweep_query, &q );
-			}
-			w->unsupportedToi += q.hits;
-		}
-		if ( r->flags & B2G_R_FAST_ENLARGED )
-		{
-			memcpy( w->hFat + 4 * r->shapeId, r->fat, 16 );
-			gtree_enlarge_proxy( w->trees + b2_dynamicBody, s->proxyKey >> 2, box4( r->fat ) );
-		}
-	}
+	continuous_pass( w, rec, count, false );
+	continuous_pass( w, rec, count, true );
 }
 
 /* ------------------------------------------------------------ step */

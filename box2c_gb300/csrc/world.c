@@ -1311,7 +1311,7 @@ int b2World_InspectContacts( b2WorldId worldId, b2InspectContact* out, int capac
 /* ------------------------------------------------------------ box2d/gpu.h */
 int b2World_GetStatus( b2WorldId worldId ) { return gworld_get( worldId )->status; }
 
-int b2World_GetUnsupportedToiCount( b2WorldId worldId ) { return gworld_get( worldId )->unsupportedToi; }
+int b2World_GetToiEventCount( b2WorldId worldId ) { return gworld_get( worldId )->toiEvents; }
 
 void b2World_EnableDeviceTiming( b2WorldId worldId, bool flag )
 {

@@ -18,10 +18,11 @@ extern "C" {
  * failure.  A failed world stops stepping; the process is never aborted. */
 B2_API int b2World_GetStatus( b2WorldId worldId );
 
-/* Number of fast-body sweeps that reached a static candidate.  Time of impact is not
- * computed by this backend; a non-zero count means the step diverged from the reference
- * for those bodies. */
-B2_API int b2World_GetUnsupportedToiCount( b2WorldId worldId );
+/* Number of time-of-impact events since the world was created: fast bodies (and
+ * bullets) that continuous collision moved back along their sweep to the first contact
+ * with a static shape (or, for a bullet, with any non-bullet shape), as the reference's
+ * src/solver.c:787-1105 does. */
+B2_API int b2World_GetToiEventCount( b2WorldId worldId );
 
 /* Device stage timings of the last step (milliseconds, CUDA events on the world's
  * stream): whole step, narrowphase, solver (prepare .. store impulses), finalisation. */
@@ -90,7 +91,8 @@ B2_API b2BatchStats b2World_GetBatchStats( void );
  *   gradFriction  dL/d(shape friction) per shape id             (shapes, out, may be null)
  * The discrete choices of each step (pairs, colours, contact features, active clamps)
  * are those of the recorded steps.  Supported: polygon, capsule and segment shapes
- * without joints or overflow-colour constraints; otherwise B2_ADJOINT_UNSUPPORTED.
+ * without joints or overflow-colour constraints, and steps without time-of-impact
+ * events; otherwise B2_ADJOINT_UNSUPPORTED.
  * B2_ADJOINT_REPLAY_MISMATCH reports that the recomputed contact geometry differed from
  * the recorded one (the world changed after recording).  No counterpart in the
  * reference API. */

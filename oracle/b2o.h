@@ -348,7 +348,7 @@ typedef struct oWorld
 	b2Profile profile;
 	uint64_t stepIndex;
 	b2r inv_h;
-	int unsupportedToi;
+	int toiEvents; /* time-of-impact events (fast bodies moved back along their sweep) */
 } oWorld;
 
 oWorld* o_world( b2WorldId id );
@@ -366,6 +366,35 @@ int o_assign_joint_color( oWorld* w, int bodyIdA, int bodyIdB, bool staticA, boo
 oBox o_shape_aabb( const oShape* s, oXf xf );
 void o_update_body_mass( oWorld* w, oBody* b );
 oSoft o_make_soft( b2r hertz, b2r zeta, b2r h );
+bool o_should_bodies_collide( oWorld* w, oBody* a, oBody* b );
+
+/* ---------------------------------------------------------------- time of impact
+ * (b2o_toi.c; reference src/distance.c, src/shape.c:480-497, :713-735) */
+typedef struct oSweep
+{
+	oVec localCenter, c1, c2;
+	oRot q1, q2;
+} oSweep;
+
+typedef struct oProxy
+{
+	oVec pts[8];
+	int count;
+	b2r radius;
+} oProxy;
+
+typedef struct oDistCache
+{
+	int count;
+	int indexA[3], indexB[3];
+} oDistCache;
+
+oXf o_sweep_xf( const oSweep* s, b2r t );
+oProxy o_make_proxy( const oVec* points, int count, b2r radius );
+oProxy o_shape_proxy( const oShape* s );
+oVec o_shape_centroid( const oShape* s );
+b2r o_distance( oDistCache* cache, const oProxy* A, oXf xfA, const oProxy* B, oXf xfB, oVec* pointA, oVec* pointB );
+b2r o_time_of_impact( const oProxy* A, const oSweep* sA, const oProxy* B, const oSweep* sB, b2r tMax, int* state );
 
 oVec ovf( b2Vec2 v );
 b2Vec2 vfo( oVec v );

@@ -112,7 +112,7 @@ int b2World_InspectContacts( b2WorldId worldId, b2InspectContact* out, int capac
 }
 
 /* Oracle-only queries. */
-int b2o_UnsupportedToiCount( b2WorldId worldId ) { return o_world( worldId )->unsupportedToi; }
+int b2o_ToiEventCount( b2WorldId worldId ) { return o_world( worldId )->toiEvents; }
 
 /* Double-precision state access for the FP64 gradient check (meaningful when the oracle
  * is compiled with -DB2O_F64). out: p.x p.y q.c q.s v.x v.y w per body id. */

@@ -664,16 +664,28 @@ static void buffer_move( oWorld* w, int proxyKey )
 		oia_push( &w->moveArray, proxyKey );
 }
 
-/* Candidate filter of the static-tree sweep (reference src/solver.c:800-858).  Time of
- * impact itself is not restated: a sweep that reaches it is counted and treated as no
- * hit, and the tests assert that the count stays zero on the scenes they compare. */
+/* Continuous collision of a fast body against static shapes (and, for a bullet, against
+ * kinematic and dynamic shapes): reference src/solver.c:787-1105.  The query callback
+ * filters the candidates and lowers the body's time-of-impact fraction. */
 typedef struct oSweepCtx
 {
 	oWorld* w;
 	oShape* fast;
 	oBody* fastBody;
-	int hits;
+	oSweep sweep;
+	b2r fraction;
 } oSweepCtx;
+
+static oSweep body_sweep( const oBody* b )
+{
+	oSweep s;
+	s.c1 = b->center0;
+	s.c2 = b->center;
+	s.q1 = b->rot0;
+	s.q2 = b->xf.q;
+	s.localCenter = b->localCenter;
+	return s;
+}
 
 static bool sweep_query( int proxyId, int shapeId, void* context )
 {
@@ -698,14 +710,38 @@ static bool sweep_query( int proxyId, int shapeId, void* context )
 	oBody* body = w->bodies + s->bodyId;
 	if ( body->isBullet )
 		return true;
-	q->hits += 1;
+	if ( o_should_bodies_collide( w, q->fastBody, body ) == false )
+		return true;
+
+	oProxy pa = o_shape_proxy( s );
+	oProxy pb = o_shape_proxy( q->fast );
+	oSweep sa = body_sweep( body );
+	int state;
+	b2r t = o_time_of_impact( &pa, &sa, &pb, &q->sweep, q->fraction, &state );
+	if ( R( 0 ) < t && t < q->fraction )
+		q->fraction = t;
+	else if ( R( 0 ) == t )
+	{
+		/* fall back to a small circle around the fast shape's centroid */
+		oVec centroid = o_shape_centroid( q->fast );
+		pb = o_make_proxy( &centroid, 1, O_SPECULATIVE );
+		t = o_time_of_impact( &pa, &sa, &pb, &q->sweep, q->fraction, &state );
+		if ( R( 0 ) < t && t < q->fraction )
+			q->fraction = t;
+	}
 	return true;
 }
 
 static void solve_continuous( oWorld* w, oBody* b )
 {
-	oXf xf2 = b->xf;
-	oSweepCtx q = { w, NULL, b, 0 };
+	oSweepCtx q;
+	q.w = w;
+	q.fastBody = b;
+	q.sweep = body_sweep( b );
+	q.fraction = R( 1 );
+	oXf xf2;
+	xf2.q = q.sweep.q2;
+	xf2.p = osub( q.sweep.c2, orotate( q.sweep.q2, q.sweep.localCenter ) );
 	for ( int sid = b->headShape; sid != O_NULL; sid = w->shapes[sid].next )
 	{
 		oShape* s = w->shapes + sid;
@@ -724,7 +760,42 @@ static void solve_continuous( oWorld* w, oBody* b )
 			otree_query( w->trees + b2_dynamicBody, box, 0xFFFFFFFFu, sweep_query, &q );
 		}
 	}
-	w->unsupportedToi += q.hits;
+
+	if ( q.fraction < R( 1 ) )
+	{
+		/* time-of-impact event: move the body back along its sweep */
+		oRot rq = onormrot( orot( ( R( 1 ) - q.fraction ) * q.sweep.q1.c + q.fraction * q.sweep.q2.c,
+								  ( R( 1 ) - q.fraction ) * q.sweep.q1.s + q.fraction * q.sweep.q2.s ) );
+		oVec c = olerp( q.sweep.c1, q.sweep.c2, q.fraction );
+		oVec origin = osub( c, orotate( rq, q.sweep.localCenter ) );
+		b->xf.p = origin;
+		b->xf.q = rq;
+		b->center = c;
+		b->rot0 = rq;
+		b->center0 = c;
+		for ( int sid = b->headShape; sid != O_NULL; sid = w->shapes[sid].next )
+		{
+			oShape* s = w->shapes + sid;
+			oBox aabb = o_shape_aabb( s, b->xf );
+			aabb.lo.x -= O_SPECULATIVE;
+			aabb.lo.y -= O_SPECULATIVE;
+			aabb.hi.x += O_SPECULATIVE;
+			aabb.hi.y += O_SPECULATIVE;
+			s->aabb = aabb;
+			if ( obox_contains( s->fatAABB, aabb ) == false )
+			{
+				s->fatAABB.lo.x = aabb.lo.x - O_AABB_MARGIN;
+				s->fatAABB.lo.y = aabb.lo.y - O_AABB_MARGIN;
+				s->fatAABB.hi.x = aabb.hi.x + O_AABB_MARGIN;
+				s->fatAABB.hi.y = aabb.hi.y + O_AABB_MARGIN;
+				s->enlargedAABB = true;
+				b->enlargeAABB = true;
+			}
+		}
+		w->toiEvents += 1;
+		return;
+	}
+
 	b->rot0 = b->xf.q;
 	b->center0 = b->center;
 	for ( int sid = b->headShape; sid != O_NULL; sid = w->shapes[sid].next )
@@ -738,6 +809,31 @@ static void solve_continuous( oWorld* w, oBody* b )
 			s->fatAABB.hi.y = s->aabb.hi.y + O_AABB_MARGIN;
 			s->enlargedAABB = true;
 			b->enlargeAABB = true;
+		}
+	}
+}
+
+/* Continuous collision of one class of fast bodies, then their grown proxies in the
+ * dynamic tree (reference src/solver.c:1839-1950: fast bodies first, then bullets, which
+ * see the fast bodies' proxies). */
+static void continuous_pass( oWorld* w, const int* fast, int count, bool bullets )
+{
+	for ( int i = 0; i < count; ++i )
+		if ( w->bodies[fast[i]].isBullet == bullets )
+			solve_continuous( w, w->bodies + fast[i] );
+	for ( int i = 0; i < count; ++i )
+	{
+		oBody* b = w->bodies + fast[i];
+		if ( b->isBullet != bullets || b->enlargeAABB == false )
+			continue;
+		b->enlargeAABB = false;
+		for ( int sid = b->headShape; sid != O_NULL; sid = w->shapes[sid].next )
+		{
+			oShape* s = w->shapes + sid;
+			if ( s->enlargedAABB == false )
+				continue;
+			s->enlargedAABB = false;
+			otree_enlarge_proxy( w->trees + b2_dynamicBody, s->proxyKey >> 2, s->fatAABB );
 		}
 	}
 }
@@ -920,23 +1016,8 @@ void o_solve( oWorld* w, b2r dt, int subSteps )
 		}
 	}
 
-	for ( int i = 0; i < f.fastCount; ++i )
-		solve_continuous( w, w->bodies + f.fast[i] );
-	for ( int i = 0; i < f.fastCount; ++i )
-	{
-		oBody* b = w->bodies + f.fast[i];
-		if ( b->enlargeAABB == false )
-			continue;
-		b->enlargeAABB = false;
-		for ( int sid = b->headShape; sid != O_NULL; sid = w->shapes[sid].next )
-		{
-			oShape* s = w->shapes + sid;
-			if ( s->enlargedAABB == false )
-				continue;
-			s->enlargedAABB = false;
-			otree_enlarge_proxy( w->trees + b2_dynamicBody, s->proxyKey >> 2, s->fatAABB );
-		}
-	}
+	continuous_pass( w, f.fast, f.fastCount, false );
+	continuous_pass( w, f.fast, f.fastCount, true );
 	free( f.enlarged );
 	free( f.fast );
 }

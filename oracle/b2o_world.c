@@ -883,7 +883,7 @@ int o_assign_joint_color( oWorld* w, int bodyIdA, int bodyIdB, bool staticA, boo
 }
 
 /* ------------------------------------------------------------ joints */
-static bool should_bodies_collide( oWorld* w, oBody* a, oBody* b )
+bool o_should_bodies_collide( oWorld* w, oBody* a, oBody* b )
 {
 	if ( a->type != b2_dynamicBody && b->type != b2_dynamicBody )
 		return false;
@@ -1108,7 +1108,7 @@ static bool pair_query( int proxyId, int shapeId, void* context )
 		return true;
 	if ( sA->isSensor && sB->isSensor )
 		return true;
-	if ( should_bodies_collide( w, w->bodies + sA->bodyId, w->bodies + sB->bodyId ) == false )
+	if ( o_should_bodies_collide( w, w->bodies + sA->bodyId, w->bodies + sB->bodyId ) == false )
 		return true;
 	oPairList* l = q->list;
 	if ( l->count == l->capacity )

@@ -39,6 +39,21 @@ SCENES = {
     # and the library has no islands or sleep, so the fixture stops at step 87
     "hello": (87, (87,)),
     "pyramid100": (40, (40,)),
+    # reference benchmark/joint_grid.c with gravity, at 30 x 30 and at the benchmark's
+    # 100 x 100 (19800 revolute joints in the graph colours)
+    "joint_grid30": (120, (1, 60, 120)),
+    "joint_grid100": (30, (30,)),
+    # reference benchmark/many_pyramids.c: 5 x 5 and the benchmark's 20 x 20 pyramids on
+    # static segments
+    "many_pyramids5": (120, (1, 60, 120)),
+    "many_pyramids20": (30, (30,)),
+    # capsules, segments, circles, boxes and rounded boxes; time-of-impact events
+    "shape_pile": (300, (1, 100, 200, 300)),
+    # joints in the overflow colour; with limits, springs and motors (flags 7)
+    "joint_hub": (300, (1, 100, 200, 300)),
+    "joint_hub_limits": (300, (1, 100, 200, 300)),
+    # projectiles and bullets against a thin wall: continuous collision
+    "fast_shots": (200, (1, 50, 100, 200)),
 }
 
 
@@ -53,6 +68,22 @@ def make_scene(b: Backend, name: str):
         return b.tilted_stacks()
     if name == "hello":
         return b.hello_world()[0]
+    if name == "joint_grid30":
+        return b.joint_grid(30, -10.0)
+    if name == "joint_grid100":
+        return b.joint_grid(100, -10.0)
+    if name == "many_pyramids5":
+        return b.many_pyramids(5, 5, 10)
+    if name == "many_pyramids20":
+        return b.many_pyramids(20, 20, 10)
+    if name == "shape_pile":
+        return b.shape_pile(600, 1239)
+    if name == "joint_hub":
+        return b.joint_hub(20, 6, 0, 1240)
+    if name == "joint_hub_limits":
+        return b.joint_hub(20, 6, 7, 1240)
+    if name == "fast_shots":
+        return b.fast_shots(60, 1241)
     raise KeyError(name)
 
 

@@ -133,3 +133,68 @@ def test_batch_in_halves_matches_single_steps(gpu):
     finally:
         for w in wb + ws:
             gpu.destroy(w)
+
+
+def test_batch_full_size_workload(gpu, oracle):
+    """The batched workload at full size: 4096 pyramids with bases U{4..40} (the bench's
+    seeded draw), 30 batched steps.  Every world ends bit-identical to the same world
+    stepped alone with b2World_Step (checked in chunks of 512 worlds), and a sample of 128
+    worlds (every 32nd) equals the oracle stepping it."""
+    bind_batch_api(gpu.lib)
+    steps = 30
+    bases = np.random.default_rng(1237).integers(4, 41, size=4096)
+    wb = [gpu.pyramid(int(b), 0.0, 0) for b in bases]
+    ids = world_array(wb)
+    try:
+        for _ in range(steps):
+            gpu.lib.b2World_StepBatch(ids, len(wb), 1.0 / 60.0, 4)
+        assert all(gpu.lib.b2World_GetStatus(w) == 0 for w in wb)
+        batched = [gpu.bodies(w) for w in wb]
+        tables = [contact_table(gpu.contacts(w)) for w in wb]
+    finally:
+        for w in wb:
+            gpu.destroy(w)
+    for start in range(0, len(bases), 512):
+        chunk = bases[start:start + 512]
+        ws = [gpu.pyramid(int(b), 0.0, 0) for b in chunk]
+        try:
+            for w in ws:
+                gpu.step(w, count=steps)
+            for k, w in enumerate(ws):
+                i = start + k
+                assert np.array_equal(gpu.bodies(w).view(np.uint32), batched[i].view(np.uint32)), f"world {i}"
+                assert np.array_equal(contact_table(gpu.contacts(w)), tables[i]), f"world {i} contacts"
+        finally:
+            for w in ws:
+                gpu.destroy(w)
+    for i in range(0, len(bases), 32):
+        wo = oracle.pyramid(int(bases[i]), 0.0, 0)
+        oracle.step(wo, count=steps)
+        same = np.array_equal(oracle.bodies(wo).view(np.uint32), batched[i].view(np.uint32))
+        oracle.destroy(wo)
+        assert same, f"world {i} differs from the oracle"
+
+
+def test_batch_mixed_paths_match_oracle(gpu, oracle):
+    """Batched worlds that take the paths the pyramids do not: capsule and segment
+    manifolds, joints in colours and in the overflow colour, motors, and time-of-impact
+    events of fast bodies and bullets (handled per world after the batched solver)."""
+    bind_batch_api(gpu.lib)
+    makers = [lambda b: b.shape_pile(200, 31), lambda b: b.joint_hub(16, 3, 4, 32), lambda b: b.fast_shots(30, 33),
+              lambda b: b.many_pyramids(2, 2, 8), lambda b: b.joint_grid(12, -10.0), lambda b: b.pyramid(10)]
+    wg = [m(gpu) for m in makers]
+    wo = [m(oracle) for m in makers]
+    ids = world_array(wg)
+    try:
+        for s in range(1, 121):
+            gpu.lib.b2World_StepBatch(ids, len(wg), 1.0 / 60.0, 4)
+            for w in wo:
+                oracle.step(w)
+            if s % 20 == 0:
+                err = _compare(gpu, oracle, wg, wo)
+                assert err is None, f"step {s}: {err}"
+    finally:
+        for w in wg:
+            gpu.destroy(w)
+        for w in wo:
+            oracle.destroy(w)

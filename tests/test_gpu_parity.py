@@ -14,7 +14,9 @@ pytestmark = pytest.mark.gpu
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
 
 
-@pytest.mark.parametrize("name", ["pyramid20", "tilted", "hello", "tumbler2000", "pyramid100"])
+@pytest.mark.parametrize("name", ["pyramid20", "tilted", "hello", "tumbler2000", "pyramid100", "joint_grid30",
+                                  "joint_grid100", "many_pyramids5", "many_pyramids20", "shape_pile", "joint_hub",
+                                  "fast_shots"])
 def test_gpu_matches_reference_golden(gpu, name):
     g = np.load(os.path.join(GOLDEN, "scenes.npz"))
     steps, snaps = SCENES[name]
@@ -52,6 +54,47 @@ def test_gpu_lockstep_oracle(gpu, oracle, scene, steps, sub):
     }[scene]
     step, detail, worst = lockstep(gpu, oracle, make, steps, substeps=sub, check_manifolds=True)
     assert step is None, f"{scene}: {detail} at step {step}"
+
+
+@pytest.mark.parametrize("scene,steps", [("shape_pile", 250), ("joint_hub_motors", 250), ("fast_shots", 150),
+                                         ("many_pyramids", 100), ("joint_grid", 100)])
+def test_gpu_lockstep_oracle_new_paths(gpu, oracle, scene, steps):
+    """Device paths the pyramid and tumbler scenes do not reach, stepped against the oracle
+    with every manifold compared: capsule and segment manifolds (capsule-capsule,
+    polygon-capsule, segment-polygon, segment-capsule, segment-circle) and rounded
+    polygons; revolute joints in the graph colours and in the overflow colour, with
+    motors; time of impact of fast bodies and bullets; segment grounds."""
+    make = {
+        "shape_pile": lambda b: b.shape_pile(300, 91),
+        "joint_hub_motors": lambda b: b.joint_hub(16, 4, 4, 92),
+        "fast_shots": lambda b: b.fast_shots(40, 93),
+        "many_pyramids": lambda b: b.many_pyramids(3, 3, 10),
+        "joint_grid": lambda b: b.joint_grid(20, -10.0),
+    }[scene]
+    step, detail, worst = lockstep(gpu, oracle, make, steps, check_manifolds=True)
+    assert step is None, f"{scene}: {detail} at step {step}"
+
+
+def test_gpu_time_of_impact_events(gpu, oracle):
+    """Continuous collision happens on the device path as often as in the oracle: the
+    projectiles stop at the thin wall instead of tunnelling through it."""
+    import ctypes as C
+    from box2c_gb300.capi import WorldId
+    bind_gpu_api(gpu.lib)
+    oracle.lib.b2o_ToiEventCount.argtypes = [WorldId]
+    oracle.lib.b2o_ToiEventCount.restype = C.c_int
+    wg, wo = gpu.fast_shots(60, 1241), oracle.fast_shots(60, 1241)
+    gpu.step(wg, count=120)
+    oracle.step(wo, count=120)
+    ng, no = gpu.lib.b2World_GetToiEventCount(wg), oracle.lib.b2o_ToiEventCount(wo)
+    bg = gpu.bodies(wg)
+    gpu.destroy(wg)
+    oracle.destroy(wo)
+    assert ng == no and ng > 50
+    # no projectile tunnelled through the wall (x = 20, 0.05 thick); rows are
+    # p.x p.y q.c q.s v.x v.y w type, static bodies included
+    dynamic = bg[:, 7] == 2
+    assert np.all(bg[dynamic, 0] < 20.0)
 
 
 def test_gpu_hello_world(gpu):

@@ -52,3 +52,27 @@ def test_batched_world_packing(tmp_path):
     r = subprocess.run([exe], capture_output=True, text=True, timeout=120)
     assert r.returncode == 0, r.stdout + r.stderr
     assert r.stdout.startswith("ok")
+
+
+def test_time_of_impact_matches_oracle(tmp_path):
+    """The library's time of impact and GJK distance (box2c_gb300/csrc/b2g_toi.h, host
+    build) against the oracle's (oracle/b2o_toi.c) on seeded random proxies and sweeps:
+    same time bits, same outcome, same distance bits (tests/c/toi_check.c)."""
+    exe = str(tmp_path / "toi_check")
+    src = os.path.join(REPO, "box2c_gb300", "csrc")
+    inc = os.path.join(REPO, "include")
+    flags = ["-std=gnu17", "-O2", "-ffp-contract=off", "-I", inc]
+    objs = []
+    for name, extra, files in (
+            ("product", ["-I", src], [os.path.join(REPO, "tests", "c", "toi_product.c")]),
+            ("oracle", ["-I", os.path.join(REPO, "oracle")],
+             [os.path.join(REPO, "tests", "c", "toi_oracle.c"), os.path.join(REPO, "oracle", "b2o_toi.c")])):
+        for f in files:
+            obj = str(tmp_path / (name + "_" + os.path.basename(f) + ".o"))
+            subprocess.run(["gcc", *flags, *extra, "-c", f, "-o", obj], check=True, capture_output=True)
+            objs.append(obj)
+    subprocess.run(["gcc", os.path.join(REPO, "tests", "c", "toi_check.c"), *objs, "-lm", "-o", exe],
+                   check=True, capture_output=True)
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert r.stdout.startswith("ok"), r.stdout
