@@ -12,11 +12,14 @@ Printed JSON line (rank 0):
   roofline    algorithmic bytes of the colour-phase solver stage (per-unit byte model of
               the step path, counted from the live contact and body counts) over its
               device time, against the measured HBM copy bandwidth
-  cpu_baseline  the plain-C CPU restatement of the same step (single thread) on a
-              bounded sample of the same workload
+  cpu_baseline  the plain-C CPU restatement of the same step on all host cores, over a
+              bounded sample of the same step window
+  window      the timed steps (W+1 .. W+K after W warm-up steps) and, beside them, the
+              same number of steps once the pyramid has settled (from step 100 on)
 
 --impl reference times the CPU implementation of the step (the plain-C restatement
-built from oracle/, single thread) on the same workload and prints the same metric.
+built from oracle/, on all host cores) over the same workload, warm-up and step window
+and prints the same metric.
 --gpus N: the path does not shard (colour phases are global Gauss-Seidel sweeps), so N
 ranks step N independent replicas; value is the slowest rank's ms/step.
 """
@@ -158,19 +161,46 @@ def oracle_backend(threads):
     return o
 
 
-def cpu_baseline(steps_sample=40, warmup=100):
-    """Times the plain-C CPU restatement of the step on the same workload, on all host
-    cores, over steps the device arm also times (after the pyramid has settled for
-    `warmup` steps).  Returns (ms per step, steps, threads)."""
+SETTLE_STEPS = 100  # the large pyramid is at rest from about this step on
+CPU_SAMPLE_STEPS = 40  # bounded sample of the CPU baseline leg of the GPU arm
+
+
+def workload_config(world_size=1):
+    """The workload both arms name in `config` (identical dicts)."""
+    return {"workload": "large_pyramid_100_rows_5050_boxes", "rows": BASE, "bodies": BASE * (BASE + 1) // 2,
+            "jitter": JITTER, "seed": SEED, "dt": DT, "substeps": SUBSTEPS, "parallelism": f"replicas{world_size}"}
+
+
+def oracle_windows(warmup, steps, settled=True, sample=None):
+    """The plain-C CPU restatement stepping the large pyramid on all host cores: `warmup`
+    untimed steps, then the timed window of `steps` steps (at most `sample` of them), then
+    (optionally) the same number of steps once the pyramid has settled.
+    Returns (ms/step of the window, steps timed, ms/step settled or None, threads)."""
     cores = os.cpu_count() or 1
     o = oracle_backend(cores)
     w = o.pyramid(BASE, JITTER, SEED)
     o.step(w, DT, SUBSTEPS, count=warmup)
+    n = steps if sample is None else min(steps, sample)
     t0 = time.perf_counter()
-    o.step(w, DT, SUBSTEPS, count=steps_sample)
-    ms = (time.perf_counter() - t0) * 1e3 / steps_sample
+    o.step(w, DT, SUBSTEPS, count=n)
+    ms = (time.perf_counter() - t0) * 1e3 / n
+    settled_ms = None
+    if settled:
+        done = warmup + n
+        o.step(w, DT, SUBSTEPS, count=max(0, SETTLE_STEPS - done))
+        t0 = time.perf_counter()
+        o.step(w, DT, SUBSTEPS, count=n)
+        settled_ms = (time.perf_counter() - t0) * 1e3 / n
     o.destroy(w)
-    return ms, steps_sample, cores
+    return ms, n, settled_ms, cores
+
+
+def cpu_baseline(warmup, steps):
+    """The CPU baseline beside the GPU arm: the oracle over the GPU arm's timed step window
+    (a bounded sample of it), on all host cores."""
+    ms, n, _, cores = oracle_windows(warmup, steps, settled=False, sample=CPU_SAMPLE_STEPS)
+    return {"value": round(ms, 4), "unit": "ms/step", "cores": cores, "kind": "port",
+            "sample": f"steps {warmup + 1}-{warmup + n} of the same 100-row pyramid (the GPU arm's timed window)"}
 
 
 TUMBLER_BODIES = 2000
@@ -373,17 +403,24 @@ def batch_cpu_baseline(sample=1024, steps=5):
 
 
 def run_reference(args):
+    """Reference arm: the CPU implementation of the step on the machine's host cores, over the
+    same workload, warm-up and timed steps as the GPU arm (steps W+1 .. W+K of the large
+    pyramid), with the settled window reported beside it."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    warm = max(100, args.warmup)
-    ms, n, cores = cpu_baseline(steps_sample=max(5, min(args.steps, 40)), warmup=warm)
+    warm = max(3, args.warmup)
+    ms, n, settled_ms, cores = oracle_windows(warm, args.steps)
     line = {"metric": METRIC, "value": round(ms, 4), "unit": "ms/step", "n_gpus": args.gpus, "steps": n,
             "warmup": warm, "ms_per_step": round(ms, 4), "higher_is_better": False, "impl": "reference",
             "dtype": "f32", "data": "synthetic", "scaling": "weak", "vs_baseline": None,
-            "config": {"workload": "large_pyramid_100_rows_5050_boxes", "dt": DT, "substeps": SUBSTEPS},
+            "config": workload_config(args.gpus),
+            "window": {"timed_steps": [warm + 1, warm + n],
+                       "settled_steps": [max(SETTLE_STEPS, warm + n) + 1, max(SETTLE_STEPS, warm + n) + n],
+                       "settled_ms_per_step": round(settled_ms, 4)},
             "cpu_baseline": {"value": round(ms, 4), "unit": "ms/step", "cores": cores, "kind": "port",
-                             "sample": f"{n} steps of the 100-row pyramid after {warm} warm-up steps"},
+                             "sample": f"steps {warm + 1}-{warm + n} of the 100-row pyramid (the GPU arm's window), "
+                                       "the oracle on every host core"},
             "e2e": {"value": round(ms, 4), "unit": "ms/step", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
@@ -406,62 +443,60 @@ def run_gpu(args):
     L = g.lib
     bind_gpu_api(L)
 
+    warm = max(3, args.warmup)
     w = g.pyramid(BASE, JITTER, SEED)
     L.b2World_EnableDeviceTiming(w, True)
-    for _ in range(max(3, args.warmup)):
+    for _ in range(warm):
         g.step(w, DT, SUBSTEPS)
 
     # L2 is flushed between timed steps by writing a buffer larger than the 129 MB L2
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
-    step_ms, solve_ms, collide_ms, finalize_ms, launches = [], [], [], [], []
-    fused_steps = 0
-    host_prof = []
+    def device_window(count):
+        rec = {"step": [], "solve": [], "collide": [], "finalize": [], "launches": [], "fused": 0, "host": []}
+        for _ in range(count):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            g.step(w, DT, SUBSTEPS)
+            t = L.b2World_GetDeviceTimes(w)
+            rec["step"].append(t.step)
+            rec["solve"].append(t.solve)
+            rec["collide"].append(t.collide)
+            rec["finalize"].append(t.finalize)
+            rec["launches"].append(t.launches)
+            rec["fused"] += t.fusedSolver
+            p = L.b2World_GetProfile(w)
+            rec["host"].append((p.step, p.pairs, p.collide, p.solve, p.broadphase))
+        return rec
+
+    # timed window: steps warm+1 .. warm+K of the pyramid (the reference arm times the
+    # same steps of the same scene)
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
     sampler = ClockSampler(0)
     with sampler:
-        for _ in range(args.steps):
-            flush.fill_(1.0)
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            g.step(w, DT, SUBSTEPS)
-            t1 = time.perf_counter()
-            t = L.b2World_GetDeviceTimes(w)
-            step_ms.append(t.step)
-            solve_ms.append(t.solve)
-            collide_ms.append(t.collide)
-            finalize_ms.append(t.finalize)
-            launches.append(t.launches)
-            p = L.b2World_GetProfile(w)
-            host_prof.append((p.step, p.pairs, p.collide, p.solve, p.broadphase))
-            fused_steps += t.fusedSolver
+        rec = device_window(args.steps)
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
-    ms = replica_max(float(np.mean(step_ms)), dist)
+    ms = replica_max(float(np.mean(rec["step"])), dist)
+    solve_ms, collide_ms, finalize_ms = rec["solve"], rec["collide"], rec["finalize"]
 
-    # end to end through the C API with host buffers
-    n_bodies = L.b2World_GetBodyStates(w, None, 0)
-    host = np.zeros(7 * n_bodies, np.float32)
-    e2e_steps = max(10, args.steps // 2)
-    if dist:
-        dist.barrier()
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        L.b2World_Step(w, DT, SUBSTEPS)
-        L.b2World_GetBodyStates(w, host.ctypes.data, n_bodies)
-    e2e_ms = (time.perf_counter() - t0) * 1e3 / e2e_steps
-    if dist:
-        dist.barrier()
-    e2e_ms = replica_max(e2e_ms, dist)
+    # settled window: the same number of steps once the pyramid has come to rest
+    # (from step SETTLE_STEPS on), reported beside the timed window
+    done = warm + args.steps
+    for _ in range(max(0, SETTLE_STEPS - done)):
+        g.step(w, DT, SUBSTEPS)
+    settled = device_window(args.steps)
+    settled_ms = float(np.mean(settled["step"]))
 
     contacts = g.contacts(w)
     touching = contacts[contacts["colorIndex"] >= 0]
     cinfo = {"points": touching["pointCount"], "all_points": contacts["pointCount"]}
     counters = g.counters(w)
     shapes = g.shapes(w)
+    n_bodies = L.b2World_GetBodyStates(w, None, 0)
     total_bytes, solver_bytes = algorithmic_bytes(cinfo, n_bodies - 1, [4] * (len(shapes) - 1), SUBSTEPS)
     solve_dev = float(np.mean(solve_ms))
     peak, peak_kind = measured_peak()
@@ -470,29 +505,55 @@ def run_gpu(args):
     toi = L.b2World_GetToiEventCount(w)
     g.destroy(w)
 
+    # end to end through the C API with host buffers, over the same step window of a
+    # fresh world: b2World_Step, then every body's state copied to a host array; the
+    # library counts the bytes each step moves between host and device
+    w = g.pyramid(BASE, JITTER, SEED)
+    for _ in range(warm):
+        L.b2World_Step(w, DT, SUBSTEPS)
+    host = np.zeros(7 * n_bodies, np.float32)
+    h2d, d2h = [], []
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        L.b2World_Step(w, DT, SUBSTEPS)
+        L.b2World_GetBodyStates(w, host.ctypes.data, n_bodies)
+        t = L.b2World_GetDeviceTimes(w)
+        h2d.append(t.hostToDeviceBytes)
+        d2h.append(t.deviceToHostBytes)
+    e2e_ms = (time.perf_counter() - t0) * 1e3 / args.steps
+    if dist:
+        dist.barrier()
+    e2e_ms = replica_max(e2e_ms, dist)
+    g.destroy(w)
+
     batch = run_batch(g, args.batch_steps, 5, args.batch_worlds) if args.batch_steps > 0 else None
     tumbler = run_tumbler(g, steps=args.tumbler_steps, cpu=not args.no_cpu) if not args.no_tumbler else None
     adjoint = run_adjoint(g) if not args.no_adjoint else None
 
     if rank != 0:
         return
-    cpu_ms, cpu_n, cpu_cores = cpu_baseline() if not args.no_cpu else (None, 0, 0)
+    cpu = cpu_baseline(warm, args.steps) if not args.no_cpu else None
     if batch is not None and not args.no_cpu:
         batch["cpu_baseline"] = batch_cpu_baseline()
     clocks = sampler.summary()
     line = {
         "metric": METRIC, "value": round(ms, 4), "unit": "ms/step", "n_gpus": world_size, "steps": args.steps,
-        "warmup": max(3, args.warmup), "ms_per_step": round(ms, 4), "higher_is_better": False,
+        "warmup": warm, "ms_per_step": round(ms, 4), "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "large_pyramid_100_rows_5050_boxes", "rows": BASE, "bodies": n_bodies - 1,
-                   "contacts": int(len(contacts)), "touching": int(len(touching)), "colors": list(counters.colorCounts),
-                   "dt": DT, "substeps": SUBSTEPS, "l2": "flushed between timed steps (256 MB write)",
-                   "parallelism": f"replicas{world_size}",
-                   "solver": "fused cluster kernel" if fused_steps == args.steps else "per-phase kernels"},
+        "config": workload_config(world_size),
+        "window": {"timed_steps": [warm + 1, warm + args.steps],
+                   "settled_steps": [max(SETTLE_STEPS, done) + 1, max(SETTLE_STEPS, done) + args.steps],
+                   "settled_ms_per_step": round(settled_ms, 4),
+                   "settled_solve_ms": round(float(np.mean(settled["solve"])), 4)},
+        "scene": {"bodies": n_bodies - 1, "contacts": int(len(contacts)), "touching": int(len(touching)),
+                  "colors": list(counters.colorCounts), "l2": "flushed between timed steps (256 MB write)",
+                  "solver": "fused cluster kernel" if rec["fused"] == args.steps else "per-phase kernels"},
         "stages_ms": {"collide": round(float(np.mean(collide_ms)), 4), "solve": round(solve_dev, 4),
                       "finalize": round(float(np.mean(finalize_ms)), 4)},
         "host_ms": dict(zip(("step", "pairs", "collide_and_events", "solve_and_sync", "records"),
-                            [round(float(x), 4) for x in np.mean(np.array(host_prof), 0)])),
+                            [round(float(x), 4) for x in np.mean(np.array(rec["host"]), 0)])),
         "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": SOLVER_DRAM_BYTES,
                      "traffic_source": "ncu dram__bytes_read+write of k_fused_stage + k_solve_fused, one step "
@@ -501,12 +562,13 @@ def run_gpu(args):
                      "algorithmic_bytes_per_step": solver_bytes, "peak_kind": peak_kind},
         "step_roofline": {"algorithmic_bytes_per_step": total_bytes,
                           "achieved_gbs": round(total_bytes / (ms * 1e-3) / 1e9, 2)},
-        "e2e": {"value": round(e2e_ms, 4), "unit": "ms/step", "h2d_bytes_per_step": 0,
-                "d2h_bytes_per_step": int(n_bodies * 7 * 4 + n_bodies * 64)},
-        "gpu_launches": int(sum(launches)),
-        "cpu_baseline": ({"value": round(cpu_ms, 4), "unit": "ms/step", "cores": cpu_cores, "kind": "port",
-                          "sample": f"{cpu_n} steps of the same 100-row pyramid after 100 settling steps"}
-                         if cpu_ms is not None else None),
+        "e2e": {"value": round(e2e_ms, 4), "unit": "ms/step", "h2d_bytes_per_step": int(np.mean(h2d)),
+                "d2h_bytes_per_step": int(np.mean(d2h)),
+                "bytes_source": "counted by the library per step (b2DeviceTimes host/device bytes): staged contacts, "
+                                "solve lists, counters, mapped events and records, and the body-state download of "
+                                "b2World_GetBodyStates"},
+        "gpu_launches": int(sum(rec["launches"])),
+        "cpu_baseline": cpu,
         "clocks": clocks, "status": status, "toi_events": toi,
         "batched": batch,
         "tumbler": tumbler,

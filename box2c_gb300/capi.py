@@ -292,7 +292,8 @@ def bind_solve_api(lib: C.CDLL) -> None:
 class DeviceTimes(C.Structure):
     """include/box2d/gpu.h b2DeviceTimes."""
     _fields_ = [("step", C.c_float), ("collide", C.c_float), ("solve", C.c_float), ("finalize", C.c_float),
-                ("eventCount", C.c_int), ("recordCount", C.c_int), ("launches", C.c_int), ("fusedSolver", C.c_int)]
+                ("eventCount", C.c_int), ("recordCount", C.c_int), ("launches", C.c_int), ("fusedSolver", C.c_int),
+                ("hostToDeviceBytes", C.c_longlong), ("deviceToHostBytes", C.c_longlong)]
 
 
 def bind_gpu_api(lib: C.CDLL) -> None:

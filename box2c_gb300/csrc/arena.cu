@@ -251,17 +251,20 @@ extern "C" int b2gd_reserve( b2gDevWorld* w, b2gHostIO* io, int bodyCap, int sha
 	return e;
 }
 
-static int h2d( void* dst, const void* src, size_t bytes, cudaStream_t s )
+/* Copies between host and device on stream s, counted in the world's transfer totals. */
+static int h2d( b2gDevWorld* w, void* dst, const void* src, size_t bytes, cudaStream_t s )
 {
 	if ( bytes == 0 )
 		return 0;
+	w->h2dBytes += (long long)bytes;
 	return ok( cudaMemcpyAsync( dst, src, bytes, cudaMemcpyHostToDevice, s ) );
 }
 
-static int d2h( void* dst, const void* src, size_t bytes, cudaStream_t s )
+static int d2h( b2gDevWorld* w, void* dst, const void* src, size_t bytes, cudaStream_t s )
 {
 	if ( bytes == 0 )
 		return 0;
+	w->d2hBytes += (long long)bytes;
 	return ok( cudaMemcpyAsync( dst, src, bytes, cudaMemcpyDeviceToHost, s ) );
 }
 
@@ -271,64 +274,64 @@ extern "C" int b2gd_upload_bodies( b2gDevWorld* w, const float* state, const flo
 	cudaStream_t s = (cudaStream_t)w->stream;
 	size_t n4 = 16u * (size_t)count;
 	int e = 0;
-	e |= h2d( w->state, state, 2 * n4, s );
-	e |= h2d( w->xf, xf, n4, s );
-	e |= h2d( w->centers, centers, n4, s );
-	e |= h2d( w->prev, prev, n4, s );
-	e |= h2d( w->mass, mass, n4, s );
-	e |= h2d( w->force, force, n4, s );
-	e |= h2d( w->extent, extent, n4, s );
-	e |= h2d( w->bodyInfo, info, 4u * (size_t)count, s );
+	e |= h2d( w, w->state, state, 2 * n4, s );
+	e |= h2d( w, w->xf, xf, n4, s );
+	e |= h2d( w, w->centers, centers, n4, s );
+	e |= h2d( w, w->prev, prev, n4, s );
+	e |= h2d( w, w->mass, mass, n4, s );
+	e |= h2d( w, w->force, force, n4, s );
+	e |= h2d( w, w->extent, extent, n4, s );
+	e |= h2d( w, w->bodyInfo, info, 4u * (size_t)count, s );
 	return e;
 }
 
 extern "C" int b2gd_upload_awake( b2gDevWorld* w, const int* awake, int count )
 {
-	return h2d( w->awake, awake, 4u * (size_t)count, (cudaStream_t)w->stream );
+	return h2d( w, w->awake, awake, 4u * (size_t)count, (cudaStream_t)w->stream );
 }
 
 extern "C" int b2gd_upload_shapes( b2gDevWorld* w, const b2gShapeGeo* geo, const float* aabb, const float* fat, int count )
 {
 	cudaStream_t s = (cudaStream_t)w->stream;
-	int e = h2d( w->geo, geo, sizeof( b2gShapeGeo ) * (size_t)count, s );
-	e |= h2d( w->aabb, aabb, 16u * (size_t)count, s );
-	e |= h2d( w->fat, fat, 16u * (size_t)count, s );
+	int e = h2d( w, w->geo, geo, sizeof( b2gShapeGeo ) * (size_t)count, s );
+	e |= h2d( w, w->aabb, aabb, 16u * (size_t)count, s );
+	e |= h2d( w, w->fat, fat, 16u * (size_t)count, s );
 	return e;
 }
 
 extern "C" int b2gd_upload_shape_lists( b2gDevWorld* w, const int* range, int bodyCount, const int* list, int listCount )
 {
 	cudaStream_t s = (cudaStream_t)w->stream;
-	int e = h2d( w->shapeRange, range, 8u * (size_t)bodyCount, s );
-	e |= h2d( w->shapeList, list, 4u * (size_t)listCount, s );
+	int e = h2d( w, w->shapeRange, range, 8u * (size_t)bodyCount, s );
+	e |= h2d( w, w->shapeList, list, 4u * (size_t)listCount, s );
 	return e;
 }
 
 extern "C" int b2gd_upload_joints( b2gDevWorld* w, const b2gJointDev* joints, int count )
 {
-	return h2d( w->joints, joints, sizeof( b2gJointDev ) * (size_t)count, (cudaStream_t)w->stream );
+	return h2d( w, w->joints, joints, sizeof( b2gJointDev ) * (size_t)count, (cudaStream_t)w->stream );
 }
 
 extern "C" int b2gd_upload_solve_lists( b2gDevWorld* w, const int* solveList, int solveCount, const int* jointList, int jointCount )
 {
 	cudaStream_t s = (cudaStream_t)w->stream;
-	int e = h2d( w->solveList, solveList, 4u * (size_t)solveCount, s );
-	e |= h2d( w->jointList, jointList, 4u * (size_t)jointCount, s );
+	int e = h2d( w, w->solveList, solveList, 4u * (size_t)solveCount, s );
+	e |= h2d( w, w->jointList, jointList, 4u * (size_t)jointCount, s );
 	return e;
 }
 
 extern "C" int b2gd_upload_fat( b2gDevWorld* w, int shapeId, const float* fat4 )
 {
-	return h2d( (char*)w->fat + 16u * (size_t)shapeId, fat4, 16u, (cudaStream_t)w->stream );
+	return h2d( w, (char*)w->fat + 16u * (size_t)shapeId, fat4, 16u, (cudaStream_t)w->stream );
 }
 
 extern "C" int b2gd_upload_pose( b2gDevWorld* w, int bodyId, const float* xf4, const float* center4, const float* prev4 )
 {
 	cudaStream_t s = (cudaStream_t)w->stream;
 	size_t at = 16u * (size_t)bodyId;
-	int e = h2d( (char*)w->xf + at, xf4, 16u, s );
-	e |= h2d( (char*)w->centers + at, center4, 16u, s );
-	e |= h2d( (char*)w->prev + at, prev4, 16u, s );
+	int e = h2d( w, (char*)w->xf + at, xf4, 16u, s );
+	e |= h2d( w, (char*)w->centers + at, center4, 16u, s );
+	e |= h2d( w, (char*)w->prev + at, prev4, 16u, s );
 	return e;
 }
 
@@ -336,23 +339,23 @@ extern "C" int b2gd_upload_shape_boxes( b2gDevWorld* w, int shapeId, const float
 {
 	cudaStream_t s = (cudaStream_t)w->stream;
 	size_t at = 16u * (size_t)shapeId;
-	int e = h2d( (char*)w->aabb + at, aabb4, 16u, s );
-	e |= h2d( (char*)w->fat + at, fat4, 16u, s );
+	int e = h2d( w, (char*)w->aabb + at, aabb4, 16u, s );
+	e |= h2d( w, (char*)w->fat + at, fat4, 16u, s );
 	return e;
 }
 
 extern "C" int b2gd_upload_body_velocity( b2gDevWorld* w, int bodyId, const float* v3 )
 {
-	return h2d( (char*)w->state + 32u * (size_t)bodyId, v3, 12u, (cudaStream_t)w->stream );
+	return h2d( w, (char*)w->state + 32u * (size_t)bodyId, v3, 12u, (cudaStream_t)w->stream );
 }
 
 extern "C" int b2gd_download_bodies( b2gDevWorld* w, float* state, float* xf, float* centers, int count )
 {
 	cudaStream_t s = (cudaStream_t)w->stream;
 	size_t n4 = 16u * (size_t)count;
-	int e = d2h( state, w->state, 2 * n4, s );
-	e |= d2h( xf, w->xf, n4, s );
-	e |= d2h( centers, w->centers, n4, s );
+	int e = d2h( w, state, w->state, 2 * n4, s );
+	e |= d2h( w, xf, w->xf, n4, s );
+	e |= d2h( w, centers, w->centers, n4, s );
 	e |= ok( cudaStreamSynchronize( s ) );
 	return e;
 }
@@ -360,9 +363,9 @@ extern "C" int b2gd_download_bodies( b2gDevWorld* w, float* state, float* xf, fl
 extern "C" int b2gd_download_manifolds( b2gDevWorld* w, b2gManifold* out, uint32_t* flags, int count )
 {
 	cudaStream_t s = (cudaStream_t)w->stream;
-	int e = d2h( out, w->manifold, sizeof( b2gManifold ) * (size_t)count, s );
+	int e = d2h( w, out, w->manifold, sizeof( b2gManifold ) * (size_t)count, s );
 	if ( flags )
-		e |= d2h( flags, w->cFlags, 4u * (size_t)count, s );
+		e |= d2h( w, flags, w->cFlags, 4u * (size_t)count, s );
 	e |= ok( cudaStreamSynchronize( s ) );
 	return e;
 }
@@ -370,8 +373,8 @@ extern "C" int b2gd_download_manifolds( b2gDevWorld* w, b2gManifold* out, uint32
 extern "C" int b2gd_download_shapes( b2gDevWorld* w, float* aabb, float* fat, int count )
 {
 	cudaStream_t s = (cudaStream_t)w->stream;
-	int e = d2h( aabb, w->aabb, 16u * (size_t)count, s );
-	e |= d2h( fat, w->fat, 16u * (size_t)count, s );
+	int e = d2h( w, aabb, w->aabb, 16u * (size_t)count, s );
+	e |= d2h( w, fat, w->fat, 16u * (size_t)count, s );
 	e |= ok( cudaStreamSynchronize( s ) );
 	return e;
 }
@@ -379,7 +382,7 @@ extern "C" int b2gd_download_shapes( b2gDevWorld* w, float* aabb, float* fat, in
 extern "C" int b2gd_download_joints( b2gDevWorld* w, b2gJointDev* joints, int count )
 {
 	cudaStream_t s = (cudaStream_t)w->stream;
-	int e = d2h( joints, w->joints, sizeof( b2gJointDev ) * (size_t)count, s );
+	int e = d2h( w, joints, w->joints, sizeof( b2gJointDev ) * (size_t)count, s );
 	e |= ok( cudaStreamSynchronize( s ) );
 	return e;
 }

@@ -147,6 +147,56 @@ B2G_HD b2gXf ginvmulxf( b2gXf A, b2gXf B )
 	C.p = ginvrotate( A.q, gsub( B.p, A.p ) );
 	return C;
 }
+/* atan2 of finite arguments, in single precision, evaluated in double with IEEE
+ * operations only (no library call), so host and device compute the same bits.  Method:
+ * reduce to z = min(|x|,|y|) / max(|x|,|y|) in [0, 1]; take the nearest table point
+ * c = k/8 and t = (z - c) / (1 + z c), |t| <= 1/16, so atan z = atan c + atan t by the
+ * arctangent addition formula; atan t by its Taylor series to t^13 (truncation below
+ * 2^-56 relative); then undo the octant reduction.  The table holds atan(k/8) rounded
+ * to double.  The double result is within a few double ulps of the true value, so the
+ * returned float is the correctly rounded atan2 except in rare midpoint cases; it is
+ * within one float ulp of glibc's atan2f. */
+B2G_HD float gatan2( float y, float x )
+{
+	const double atanTable[9] = { 0.0,
+								  0x1.fd5ba9aac2f6ep-4,
+								  0x1.f5b75f92c80ddp-3,
+								  0x1.6f61941e4def1p-2,
+								  0x1.dac670561bb4fp-2,
+								  0x1.1e00babdefeb4p-1,
+								  0x1.4978fa3269ee1p-1,
+								  0x1.700a7c5784634p-1,
+								  0x1.921fb54442d18p-1 };
+	const double pi = 0x1.921fb54442d18p+1, halfPi = 0x1.921fb54442d18p+0;
+	double ax = x < 0.0f ? -(double)x : (double)x;
+	double ay = y < 0.0f ? -(double)y : (double)y;
+	bool negX = signbit( x ) != 0, negY = signbit( y ) != 0;
+	double r;
+	if ( ax == 0.0 && ay == 0.0 )
+		r = negX ? pi : 0.0;
+	else
+	{
+		bool swap = ay > ax;
+		double z = swap ? ax / ay : ay / ax;
+		int k = (int)( z * 8.0 + 0.5 );
+		double c = (double)k * 0.125;
+		double t = ( z - c ) / ( 1.0 + z * c );
+		double t2 = t * t;
+		double p = 0x1.3b13b13b13b14p-4;
+		p = p * t2 - 0x1.745d1745d1746p-4;
+		p = p * t2 + 0x1.c71c71c71c71cp-4;
+		p = p * t2 - 0x1.2492492492492p-3;
+		p = p * t2 + 0x1.999999999999ap-3;
+		p = p * t2 - 0x1.5555555555555p-2;
+		r = atanTable[k] + ( t + t * ( t2 * p ) );
+		if ( swap )
+			r = halfPi - r;
+		if ( negX )
+			r = pi - r;
+	}
+	return (float)( negY ? -r : r );
+}
+
 B2G_HD bool gbox_contains( b2gBox a, b2gBox b )
 {
 	return a.lo.x <= b.lo.x && a.lo.y <= b.lo.y && b.hi.x <= a.hi.x && b.hi.y <= a.hi.y;

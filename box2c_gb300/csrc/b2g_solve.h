@@ -311,11 +311,14 @@ __device__ __forceinline__ bool restitution_scalar( Row& r, DevState& a, DevStat
 }
 
 /* ------------------------------------------------------------------ revolute joint */
+/* Relative angle of two rotations (reference include/box2d/math_functions.h:386-394).
+ * The reference calls the C library's atan2f; the device uses gatan2, which is within one
+ * float ulp of it and gives the same bits on host and device. */
 __device__ __forceinline__ float rel_angle( b2gRot b, b2gRot a )
 {
 	float s = b.s * a.c - b.c * a.s;
 	float c = b.c * a.c + b.s * a.s;
-	return atan2f( s, c );
+	return gatan2( s, c );
 }
 
 __device__ __forceinline__ float unwind( float a )

@@ -225,6 +225,7 @@ typedef struct b2gDevWorld
 	void* timers[8]; /* cudaEvent_t: step start, collide start/end, solve start/end, finalize end, step end */
 	int timing;
 	int launches;
+	long long h2dBytes, d2hBytes; /* host <-> device bytes of the current step */
 	int fused;	   /* use the fused cluster solver when the world fits on chip */
 	int fusedUsed; /* the last step's solver stage ran fused */
 	/* set for a solver stage launched before the host has seen the narrowphase's events:

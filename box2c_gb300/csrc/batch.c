@@ -79,6 +79,8 @@ static void begin_worlds( int begin, int end, void* arg )
 		w->dev.stream = c->stream;
 		w->batching = true;
 		w->tapeBodyDst = NULL;
+		w->dev.h2dBytes = 0;
+		w->dev.d2hBytes = 0;
 		gworld_flush( w );
 		int staged = gstep_begin( w );
 		if ( staged < 0 )

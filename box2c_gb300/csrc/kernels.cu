@@ -159,6 +159,7 @@ extern "C" int b2gd_collide( b2gDevWorld* w, b2gHostIO* io, int newCount, int id
 	if ( newCount > 0 )
 	{
 		cudaMemcpyAsync( w->newContacts, io->newContacts, sizeof( b2gContactInit ) * (size_t)newCount, cudaMemcpyHostToDevice, s );
+		w->h2dBytes += (long long)( sizeof( b2gContactInit ) * (size_t)newCount );
 		k_scatter_contacts<<<blocks_for( newCount ), BLOCK, 0, s>>>( *w, w->newContacts, newCount );
 		w->launches += 1;
 	}
@@ -170,6 +171,7 @@ extern "C" int b2gd_collide( b2gDevWorld* w, b2gHostIO* io, int newCount, int id
 	if ( w->timing )
 		cudaEventRecord( (cudaEvent_t)w->timers[2], s );
 	cudaMemcpyAsync( io->counters, w->counters, 4 * sizeof( int ), cudaMemcpyDeviceToHost, s );
+	w->d2hBytes += 4 * sizeof( int );
 	return check( cudaGetLastError() );
 }
 
@@ -298,6 +300,7 @@ extern "C" int b2gd_solve( b2gDevWorld* w, b2gHostIO* io, const b2gSolvePlan* pl
 	if ( w->timing )
 		cudaEventRecord( (cudaEvent_t)w->timers[5], s );
 	cudaMemcpyAsync( io->counters, w->counters, 4 * sizeof( int ), cudaMemcpyDeviceToHost, s );
+	w->d2hBytes += 4 * sizeof( int );
 	return check( cudaGetLastError() );
 }
 
@@ -329,6 +332,7 @@ extern "C" int b2gd_solve_speculative( b2gDevWorld* w, b2gHostIO* io, const b2gS
 	if ( w->timing )
 		cudaEventRecord( (cudaEvent_t)w->timers[5], s );
 	cudaMemcpyAsync( io->counters, w->counters, 4 * sizeof( int ), cudaMemcpyDeviceToHost, s );
+	w->d2hBytes += 4 * sizeof( int );
 	w->guardEvents = 0;
 	w->fusedUsed = 1;
 	w->launches += fused + 1;

@@ -238,8 +238,12 @@ extern "C" int b2gd_pair_query( b2gDevWorld* w, b2gPairQuery** query, const b2gT
 		}
 		if ( bytes > 0 )
 			cudaMemcpyAsync( q->nodes[t], nodes[t], bytes, cudaMemcpyHostToDevice, s );
+		w->h2dBytes += (long long)bytes;
 	}
 	memcpy( q->hKeys, keys, sizeof( int ) * (size_t)count );
+	/* moved-proxy keys are read by the device and counts and candidates written to the
+	 * host through mapped memory */
+	w->h2dBytes += (long long)( sizeof( int ) * (size_t)count );
 	int3 r = make_int3( root[0], root[1], root[2] );
 	k_pair_query<<<( count + QUERY_WARPS - 1 ) / QUERY_WARPS, 32 * QUERY_WARPS, 0, s>>>(
 		q->nodes[0], q->nodes[1], q->nodes[2], r, q->dKeys, count, (int2*)q->dCand, q->dCount );
@@ -248,6 +252,13 @@ extern "C" int b2gd_pair_query( b2gDevWorld* w, b2gPairQuery** query, const b2gT
 		e = cudaStreamSynchronize( s );
 	*cand = q->hCand;
 	*counts = q->hCount;
+	if ( e == cudaSuccess )
+	{
+		long long n = 0;
+		for ( int i = 0; i < count; ++i )
+			n += q->hCount[i] > 0 ? q->hCount[i] : 0;
+		w->d2hBytes += (long long)sizeof( int ) * ( (long long)count + 2 * n );
+	}
 	return (int)e;
 }
 

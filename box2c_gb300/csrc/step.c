@@ -910,6 +910,8 @@ int gstep_after_collide( gWorld* w, float dt, int subSteps, b2gStepConst* sc, b2
 {
 	int eventCount = w->io.counters[0];
 	w->lastEventCount = eventCount;
+	/* events reach the host through mapped memory */
+	w->dev.d2hBytes += 4 * (long long)( eventCount < w->dev.eventCap ? eventCount : w->dev.eventCap );
 	process_events( w, eventCount < w->dev.eventCap ? eventCount : w->dev.eventCap );
 	double t2 = b2g_now_ms();
 	w->profile.collide = (float)( t2 - w->stepStart );
@@ -953,6 +955,9 @@ void gstep_finish( gWorld* w )
 	w->profile.solve = (float)( t3 - w->stepStart );
 	int recordCount = w->io.counters[1];
 	w->lastRecordCount = recordCount;
+	/* records reach the host through mapped memory: 48 bytes, 80 for fast shapes */
+	for ( int i = 0; i < ( recordCount < w->dev.recordCap ? recordCount : w->dev.recordCap ); ++i )
+		w->dev.d2hBytes += ( w->io.records[i].flags & B2G_R_FAST ) ? 80 : 48;
 	process_records( w, recordCount < w->dev.recordCap ? recordCount : w->dev.recordCap );
 	w->profile.broadphase = (float)( b2g_now_ms() - t3 );
 }
@@ -1025,6 +1030,8 @@ void b2World_Step( b2WorldId worldId, float timeStep, int subStepCount )
 		return;
 	double t0 = b2g_now_ms();
 	w->locked = true;
+	w->dev.h2dBytes = 0;
+	w->dev.d2hBytes = 0;
 	b2gd_mark( &w->dev, 0 );
 	gworld_flush( w );
 	gstep_run( w, timeStep, subStepCount );

@@ -1329,6 +1329,8 @@ b2DeviceTimes b2World_GetDeviceTimes( b2WorldId worldId )
 	t.recordCount = w->lastRecordCount;
 	t.launches = w->dev.launches;
 	t.fusedSolver = w->dev.fusedUsed;
+	t.hostToDeviceBytes = w->dev.h2dBytes;
+	t.deviceToHostBytes = w->dev.d2hBytes;
 	return t;
 }
 

@@ -36,6 +36,11 @@ typedef struct b2DeviceTimes
 	int recordCount; /* finalisation records (grown proxies, fast shapes) */
 	int launches;	 /* kernel launches of the last step */
 	int fusedSolver; /* 1 when the last step's solver stage ran as one fused launch */
+	/* bytes the last step moved between host and device: copies (setup changes, new
+	 * contacts, solve lists, tree nodes, counters, time-of-impact poses) and device
+	 * reads or writes of mapped host memory (events, records, pair candidates) */
+	long long hostToDeviceBytes;
+	long long deviceToHostBytes;
 } b2DeviceTimes;
 
 B2_API void b2World_EnableDeviceTiming( b2WorldId worldId, bool flag );

@@ -21,6 +21,12 @@ typedef double b2r;
 	#define RATAN2( y, x ) atan2( y, x )
 	#define RCOS( x ) cos( x )
 	#define RSIN( x ) sin( x )
+#elif defined( B2O_OWN_ATAN2 )
+typedef float b2r;
+	#define RSQRT( x ) sqrtf( x )
+	#define RATAN2( y, x ) o_atan2( y, x )
+	#define RCOS( x ) cosf( x )
+	#define RSIN( x ) sinf( x )
 #else
 typedef float b2r;
 	#define RSQRT( x ) sqrtf( x )
@@ -30,6 +36,55 @@ typedef float b2r;
 #endif
 
 #define R( x ) ( (b2r)( x ) )
+
+#ifdef B2O_OWN_ATAN2
+/* The float build that checks the library on joint springs and limits replaces the C
+ * library's atan2f (which the reference calls, and which differs from the device's by a
+ * float ulp at times) with the library's own atan2: double evaluation with IEEE
+ * operations only; reduction to [0, 1], the arctangent addition formula around the
+ * nearest k/8 with a table of atan(k/8), and the Taylor series of atan to t^13 for
+ * |t| <= 1/16.  Same operations in the same order as the library's gatan2. */
+static inline float o_atan2( float y, float x )
+{
+	static const double table[9] = { 0.0,
+									 0x1.fd5ba9aac2f6ep-4,
+									 0x1.f5b75f92c80ddp-3,
+									 0x1.6f61941e4def1p-2,
+									 0x1.dac670561bb4fp-2,
+									 0x1.1e00babdefeb4p-1,
+									 0x1.4978fa3269ee1p-1,
+									 0x1.700a7c5784634p-1,
+									 0x1.921fb54442d18p-1 };
+	const double pi = 0x1.921fb54442d18p+1, halfPi = 0x1.921fb54442d18p+0;
+	double ax = x < 0.0f ? -(double)x : (double)x;
+	double ay = y < 0.0f ? -(double)y : (double)y;
+	int negX = signbit( x ) != 0, negY = signbit( y ) != 0;
+	double r;
+	if ( ax == 0.0 && ay == 0.0 )
+		r = negX ? pi : 0.0;
+	else
+	{
+		int swap = ay > ax;
+		double z = swap ? ax / ay : ay / ax;
+		int k = (int)( z * 8.0 + 0.5 );
+		double c = (double)k * 0.125;
+		double t = ( z - c ) / ( 1.0 + z * c );
+		double t2 = t * t;
+		double p = 0x1.3b13b13b13b14p-4;
+		p = p * t2 - 0x1.745d1745d1746p-4;
+		p = p * t2 + 0x1.c71c71c71c71cp-4;
+		p = p * t2 - 0x1.2492492492492p-3;
+		p = p * t2 + 0x1.999999999999ap-3;
+		p = p * t2 - 0x1.5555555555555p-2;
+		r = table[k] + ( t + t * ( t2 * p ) );
+		if ( swap )
+			r = halfPi - r;
+		if ( negX )
+			r = pi - r;
+	}
+	return (float)( negY ? -r : r );
+}
+#endif
 #define O_PI R( 3.14159265359f )
 #define O_EPS R( FLT_EPSILON )
 #define O_MAX R( FLT_MAX )

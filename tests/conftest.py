@@ -38,6 +38,15 @@ def oracle64():
 
 
 @pytest.fixture(scope="session")
+def oracle_atan():
+    """The float oracle with the library's own atan2 in place of the C library's (joint
+    springs and limits are then comparable bit for bit with the device)."""
+    _make(["-f", "oracle/Makefile"])
+    b = os.path.join(ORACLE_DIR, "_build")
+    return Backend(os.path.join(b, "liboracle_atan.so"), os.path.join(b, "liboracle_atan_scenes.so"), "oracle_atan")
+
+
+@pytest.fixture(scope="session")
 def reference():
     if not os.path.isdir(os.path.join(REF_SRC, "src")):
         pytest.skip("reference sources not present on this machine")

@@ -52,6 +52,8 @@ SCENES = {
     # joints in the overflow colour; with limits, springs and motors (flags 7)
     "joint_hub": (300, (1, 100, 200, 300)),
     "joint_hub_limits": (300, (1, 100, 200, 300)),
+    # contact-free revolute chains with limits, springs and motors
+    "joint_chains": (300, (1, 2, 10, 60, 300)),
     # projectiles and bullets against a thin wall: continuous collision
     "fast_shots": (200, (1, 50, 100, 200)),
 }
@@ -82,6 +84,8 @@ def make_scene(b: Backend, name: str):
         return b.joint_hub(20, 6, 0, 1240)
     if name == "joint_hub_limits":
         return b.joint_hub(20, 6, 7, 1240)
+    if name == "joint_chains":
+        return b.joint_chains(8, 8, 7, 1242)
     if name == "fast_shots":
         return b.fast_shots(60, 1241)
     raise KeyError(name)

@@ -159,3 +159,37 @@ def test_gpu_solver_path_selection(gpu, fused):
     gpu.destroy(w)
     assert status == 0
     assert t.fusedSolver == (1 if fused else 0)
+
+
+@pytest.mark.parametrize("scene", ["joint_chains", "joint_hub_limits"])
+def test_gpu_joint_limits_springs_lockstep(gpu, oracle_atan, scene):
+    """Revolute joints with limits, springs and motors, against the oracle build that
+    uses the library's own atan2 for the joint angle: bit-identical every step (in the
+    graph colours and in the overflow colour, with contacts in the hub scene)."""
+    make = {"joint_chains": lambda b: b.joint_chains(8, 8, 7, 1242),
+            "joint_hub_limits": lambda b: b.joint_hub(20, 6, 7, 1240)}[scene]
+    step, detail, worst = lockstep(gpu, oracle_atan, make, 300, check_manifolds=True)
+    assert step is None, f"{scene}: {detail} at step {step}"
+
+
+@pytest.mark.parametrize("name", ["joint_chains", "joint_hub_limits"])
+def test_gpu_joint_limits_against_reference_golden(gpu, name):
+    """The same scenes against the reference's own states: the first step (identical
+    start) within 1e-5 relative; the drift at later snapshots is printed (a one-ulp
+    difference of atan2 grows in these many-body scenes)."""
+    g = np.load(os.path.join(GOLDEN, "scenes.npz"))
+    steps, snaps = SCENES[name]
+    w = make_scene(gpu, name)
+    drift = {}
+    try:
+        for s in range(1, steps + 1):
+            gpu.step(w)
+            if s in snaps:
+                ref = g[f"{name}/bodies_{s}"]
+                b = gpu.bodies(w)
+                drift[s] = float(np.max(np.abs(b - ref) / np.maximum(np.abs(ref), 1.0)))
+    finally:
+        gpu.destroy(w)
+    print(f"{name}: max rel state error vs the reference after N steps {drift}")
+    assert drift[1] <= 1e-5, drift
+    assert all(np.isfinite(v) for v in drift.values())

@@ -76,3 +76,23 @@ def test_time_of_impact_matches_oracle(tmp_path):
     r = subprocess.run([exe], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stdout + r.stderr
     assert r.stdout.startswith("ok"), r.stdout
+
+
+def test_joint_angle_atan2(tmp_path):
+    """The library's atan2 for joint angles (box2c_gb300/csrc/b2g_math.h gatan2) against
+    the oracle's copy (bit for bit) and the C library's atan2f (one ulp at most) on
+    rotation-like, small-angle, general and signed-zero inputs (tests/c/atan_check.c)."""
+    exe = str(tmp_path / "atan_check")
+    src = os.path.join(REPO, "box2c_gb300", "csrc")
+    flags = ["-std=gnu17", "-O2", "-ffp-contract=off", "-I", os.path.join(REPO, "include")]
+    objs = []
+    for f, extra in (("atan_product.c", ["-I", src]), ("atan_oracle.c", ["-I", os.path.join(REPO, "oracle")])):
+        obj = str(tmp_path / (f + ".o"))
+        subprocess.run(["gcc", *flags, *extra, "-c", os.path.join(REPO, "tests", "c", f), "-o", obj],
+                       check=True, capture_output=True)
+        objs.append(obj)
+    subprocess.run(["gcc", *flags, os.path.join(REPO, "tests", "c", "atan_check.c"), *objs, "-lm", "-o", exe],
+                   check=True, capture_output=True)
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert r.stdout.startswith("ok"), r.stdout

@@ -159,3 +159,29 @@ def test_threaded_oracle_is_bit_identical(oracle, scene, steps):
         L.b2o_SetThreads(1)
     assert np.array_equal(states[0][0], states[1][0])
     assert np.array_equal(states[0][1], states[1][1])
+
+
+@pytest.mark.parametrize("scene", ["joint_chains", "joint_hub_limits"])
+def test_own_atan2_per_step_error_and_drift(reference, oracle_atan, scene):
+    """Joint springs and limits take the joint angle through atan2; the library (and the
+    oracle build it is checked against bit for bit) uses its own atan2, within one float
+    ulp of the reference's atan2f.  From identical states the first step's error is the
+    per-step error: within 1e-5 relative (max(|ref|, 1) as the scale).  The drift after
+    N steps is reported; in these many-body scenes a one-ulp difference grows."""
+    make = {"joint_chains": lambda b: b.joint_chains(8, 8, 7, 1242),
+            "joint_hub_limits": lambda b: b.joint_hub(20, 6, 7, 1240)}[scene]
+    wr, wa = make(reference), make(oracle_atan)
+    drift = {}
+    try:
+        for s in range(1, 301):
+            reference.step(wr)
+            oracle_atan.step(wa)
+            if s in (1, 10, 60, 300):
+                a, b = oracle_atan.bodies(wa), reference.bodies(wr)
+                drift[s] = float(np.max(np.abs(a - b) / np.maximum(np.abs(b), 1.0)))
+    finally:
+        reference.destroy(wr)
+        oracle_atan.destroy(wa)
+    print(f"{scene}: max rel state error after N steps {drift}")
+    assert drift[1] <= 1e-5, drift
+    assert all(np.isfinite(v) for v in drift.values())
