@@ -342,7 +342,66 @@ def run_batch(g, steps, warmup, n_worlds=BATCH_WORLDS):
     }
 
 
-def run_adjoint(g, reps=3):
+def fd64_gradient_check(heights, v0, mu, grads, steps=120, sample=16):
+    """The gradient against central finite differences of the FP64 CPU restatement of the
+    same step (the oracle's double build), per world of a fixed sample: relative error
+    |g - fd| / |fd| at eps 1e-3 (the specified step) and at eps 1e-6, and whether the
+    finite difference is stable (eps 1e-5 and 1e-6 within 1e-4 relative).  All worlds of
+    the sample are reported; none is dropped."""
+    subprocess.run(["make", "-s", "-j8", "-f", "oracle/Makefile"], cwd=REPO, check=True, capture_output=True)
+    from box2c_gb300.capi import Backend, WorldId
+    ob = os.path.join(REPO, "oracle", "_build")
+    o = Backend(os.path.join(ob, "liboracle64.so"), os.path.join(ob, "liboracle64_scenes.so"), "oracle64")
+    L = o.lib
+    L.b2o_GetBodyStateF64.argtypes = [WorldId, C.c_void_p, C.c_int]
+    L.b2o_SetBodyVelocityF64.argtypes = [WorldId, C.c_int, C.c_double, C.c_double, C.c_double]
+    L.b2o_SetShapeFrictionF64.argtypes = [WorldId, C.c_int, C.c_double]
+
+    def loss(h, v, m):
+        w = o.drop_boxes(h, v[:, 0].astype(np.float32), v[:, 1].astype(np.float32), float(m))
+        for k in range(len(h)):
+            L.b2o_SetBodyVelocityF64(w, k + 1, float(v[k, 0]), float(v[k, 1]), 0.0)
+        for sh in range(len(h) + 1):
+            L.b2o_SetShapeFrictionF64(w, sh, float(m))
+        o.step(w, DT, SUBSTEPS, count=steps)
+        st = np.zeros(7 * (len(h) + 1))
+        L.b2o_GetBodyStateF64(w, st.ctypes.data, len(h) + 1)
+        o.destroy(w)
+        return float((st.reshape(-1, 7)[1:, :2] ** 2).sum())
+
+    def fd(h, v, m, eps):
+        v = v.astype(np.float64)
+        out = np.zeros(v.size + 1)
+        for i in range(v.size):
+            vp, vm = v.copy(), v.copy()
+            vp.flat[i] += eps
+            vm.flat[i] -= eps
+            out[i] = (loss(h, vp, m) - loss(h, vm, m)) / (2 * eps)
+        out[-1] = (loss(h, v, float(m) + eps) - loss(h, v, float(m) - eps)) / (2 * eps)
+        return out
+
+    rows = []
+    for w in range(sample):
+        g = grads[w]
+        f3, f5, f6 = (fd(heights[w], v0[w], mu[w], e) for e in (1e-3, 1e-5, 1e-6))
+        stable = bool(np.linalg.norm(f5 - f6) <= 1e-4 * np.linalg.norm(f6))
+        rows.append((float(np.linalg.norm(g - f3) / np.linalg.norm(f3)), float(np.linalg.norm(g - f6) / np.linalg.norm(f6)),
+                     stable))
+    e3 = np.array([r[0] for r in rows])
+    e6 = np.array([r[1] for r in rows])
+    st = np.array([r[2] for r in rows])
+
+    def summary(x):
+        return {"median": float(np.median(x)), "max": float(np.max(x)),
+                "within_1e-3": int(np.sum(x <= 1e-3))} if len(x) else None
+
+    return {"sample": f"worlds 0-{sample - 1} of the 256, {steps} steps, loss sum |p|^2, 17 parameters per world",
+            "eps_1e-3": summary(e3), "eps_1e-6": summary(e6), "stable_fraction": float(np.mean(st)),
+            "stable_eps_1e-6": summary(e6[st]), "per_world_eps_1e-3": [round(float(x), 6) for x in e3],
+            "per_world_eps_1e-6": [round(float(x), 6) for x in e6], "per_world_stable": [bool(x) for x in st]}
+
+
+def run_adjoint(g, reps=3, check=True):
     """Differentiable stepping: 256 worlds x 8 boxes (half-extent 0.5) dropped from
     U(1,5) m with N(0,1) velocities and per-world friction U(0.2,0.9), 120 steps x 4
     substeps; loss = sum of squared final positions; gradient w.r.t. initial velocities
@@ -375,12 +434,14 @@ def run_adjoint(g, reps=3):
         back.append(time.perf_counter() - t)
     sim.destroy()
     f0, f1, bw = (1e3 * float(np.median(x[1:])) for x in (plain, taped, back))
+    grads = np.concatenate([gv.reshape(n, -1), gm[:, None]], axis=1)
+    check_out = fd64_gradient_check(heights, v0, mu, grads) if check else None
     return {
         "metric": "fwd+bwd vs fwd ms", "workload": "256 worlds x 8 boxes, 120 steps x 4 substeps",
         "fwd_ms": round(f0, 3), "fwd_recording_ms": round(f1, 3), "bwd_ms": round(bw, 3),
         "fwd_plus_bwd_ms": round(f1 + bw, 3), "ratio_vs_fwd": round((f1 + bw) / f0, 3),
         "same_final_state": bool(np.array_equal(p0, p)), "grad_norm": float(np.linalg.norm(gv)),
-        "status": sim.last_status,
+        "status": sim.last_status, "grad_rel_err": check_out,
     }
 
 
@@ -530,7 +591,7 @@ def run_gpu(args):
 
     batch = run_batch(g, args.batch_steps, 5, args.batch_worlds) if args.batch_steps > 0 else None
     tumbler = run_tumbler(g, steps=args.tumbler_steps, cpu=not args.no_cpu) if not args.no_tumbler else None
-    adjoint = run_adjoint(g) if not args.no_adjoint else None
+    adjoint = run_adjoint(g, check=not args.no_cpu) if not args.no_adjoint else None
 
     if rank != 0:
         return

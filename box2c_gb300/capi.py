@@ -114,6 +114,14 @@ class Backend:
         L.b2Body_GetAngularVelocity.restype = C.c_float
         L.b2Body_SetLinearVelocity.argtypes = [BodyId, Vec2]
         L.b2Body_SetLinearVelocity.restype = None
+        for name, idt in (("b2DestroyBody", BodyId), ("b2DestroyShape", ShapeId), ("b2DestroyJoint", JointId)):
+            getattr(L, name).argtypes = [idt]
+            getattr(L, name).restype = None
+        for name, idt in (("b2Body_IsValid", BodyId), ("b2Shape_IsValid", ShapeId), ("b2Joint_IsValid", JointId)):
+            getattr(L, name).argtypes = [idt]
+            getattr(L, name).restype = C.c_bool
+        L.b2Body_GetShapes.argtypes = [BodyId, C.c_void_p, C.c_int]
+        L.b2Body_GetShapes.restype = C.c_int
         S.b2s_pyramid.argtypes = [C.c_int, C.c_float, C.c_uint64]
         S.b2s_pyramid.restype = WorldId
         S.b2s_tumbler.argtypes = [C.c_int, C.c_uint64, C.c_int]
@@ -134,6 +142,16 @@ class Backend:
         S.b2s_joint_hub.restype = WorldId
         S.b2s_joint_chains.argtypes = [C.c_int, C.c_int, C.c_int, C.c_uint64]
         S.b2s_joint_chains.restype = WorldId
+        S.b2s_empty_world.argtypes = []
+        S.b2s_empty_world.restype = WorldId
+        S.b2s_add_body.argtypes = [WorldId, C.c_int]
+        S.b2s_add_body.restype = BodyId
+        S.b2s_add_square.argtypes = [WorldId, C.c_float]
+        S.b2s_add_square.restype = BodyId
+        S.b2s_destruction.argtypes = []
+        S.b2s_destruction.restype = WorldId
+        S.b2s_destruction_step.argtypes = [WorldId, C.c_int]
+        S.b2s_destruction_step.restype = None
         S.b2s_fast_shots.argtypes = [C.c_int, C.c_uint64]
         S.b2s_fast_shots.restype = WorldId
         S.b2s_draw_ints.argtypes = [C.c_int, C.c_uint64, C.c_int, C.c_int, C.c_void_p]
@@ -183,6 +201,12 @@ class Backend:
     def joint_chains(self, chains: int = 8, links: int = 8, flags: int = 7, seed: int = 1242) -> WorldId:
         """flags: 1 joint limits, 2 joint springs, 4 motors."""
         return self._made(self.scenes.b2s_joint_chains(chains, links, flags, seed))
+
+    def destruction(self) -> WorldId:
+        return self._made(self.scenes.b2s_destruction())
+
+    def destruction_step(self, world: WorldId, step: int) -> None:
+        self.scenes.b2s_destruction_step(world, step)
 
     def fast_shots(self, count: int = 60, seed: int = 1241) -> WorldId:
         return self._made(self.scenes.b2s_fast_shots(count, seed))

@@ -799,3 +799,165 @@ b2WorldId b2s_joint_chains( int chains, int links, int flags, uint64_t seed )
 	}
 	return worldId;
 }
+
+/* ids of the destruction scene, per process (one such scene at a time) */
+static struct
+{
+	b2BodyId pyramid[55];
+	b2BodyId hub;
+	b2BodyId spokes[14];
+	b2JointId spokeJoints[14];
+	b2BodyId pairs[6];
+	b2ShapeId pairShapes[6][2];
+	b2ShapeId ledge;
+} s_destruction;
+
+b2WorldId b2s_destruction( void )
+{
+	b2WorldDef wd = b2s_world_def();
+	b2WorldId worldId = b2CreateWorld( &wd );
+	if ( B2_IS_NULL( worldId ) )
+		return worldId;
+	memset( &s_destruction, 0, sizeof( s_destruction ) );
+
+	b2BodyDef gd = b2DefaultBodyDef();
+	gd.position = ( b2Vec2 ){ 0.0f, -0.5f };
+	b2BodyId groundId = b2CreateBody( worldId, &gd );
+	b2ShapeDef gsd = b2DefaultShapeDef();
+	b2Polygon groundBox = b2MakeBox( 40.0f, 0.5f );
+	b2CreatePolygonShape( groundId, &gsd, &groundBox );
+	b2Polygon ledge = b2MakeOffsetBox( 2.0f, 0.25f, ( b2Vec2 ){ 12.0f, 4.0f }, 0.0f );
+	s_destruction.ledge = b2CreatePolygonShape( groundId, &gsd, &ledge );
+
+	b2BodyDef bd = b2DefaultBodyDef();
+	bd.type = b2_dynamicBody;
+	b2ShapeDef sd = b2DefaultShapeDef();
+	sd.density = 1.0f;
+	sd.friction = 0.6f;
+
+	/* a 10-row pyramid of unit boxes left of the origin */
+	b2Polygon box = b2MakeSquare( 0.5f );
+	int n = 0;
+	for ( int i = 0; i < 10; ++i )
+	{
+		for ( int j = i; j < 10; ++j )
+		{
+			bd.position = ( b2Vec2 ){ -15.0f + ( i + 1.0f ) * 0.5f + ( j - i ) * 1.0f, ( 2.0f * i + 1.0f ) * 0.5f };
+			s_destruction.pyramid[n] = b2CreateBody( worldId, &bd );
+			b2CreatePolygonShape( s_destruction.pyramid[n], &sd, &box );
+			n += 1;
+		}
+	}
+
+	/* a hub pinned to a shapeless static anchor with 14 spokes pinned to it (the joints
+	 * beyond the graph's colours go to the overflow set) */
+	b2BodyDef ad = b2DefaultBodyDef();
+	b2BodyId anchorId = b2CreateBody( worldId, &ad );
+	bd.position = ( b2Vec2 ){ 0.0f, 6.0f };
+	s_destruction.hub = b2CreateBody( worldId, &bd );
+	b2Circle hubCircle = { { 0.0f, 0.0f }, 0.8f };
+	b2CreateCircleShape( s_destruction.hub, &sd, &hubCircle );
+	b2RevoluteJointDef jd = b2DefaultRevoluteJointDef();
+	jd.bodyIdA = anchorId;
+	jd.bodyIdB = s_destruction.hub;
+	jd.localAnchorA = ( b2Vec2 ){ 0.0f, 6.0f };
+	b2CreateRevoluteJoint( worldId, &jd );
+	b2Polygon spokeBox = b2MakeBox( 0.25f, 0.25f );
+	for ( int k = 0; k < 14; ++k )
+	{
+		b2Vec2 u = b2s_circle_point( -1.0f + 2.0f * ( k + 0.5f ) / 14.0f );
+		b2Vec2 offset = { 2.0f * u.x, 2.0f * u.y };
+		bd.position = ( b2Vec2 ){ offset.x, 6.0f + offset.y };
+		s_destruction.spokes[k] = b2CreateBody( worldId, &bd );
+		b2CreatePolygonShape( s_destruction.spokes[k], &sd, &spokeBox );
+		jd = b2DefaultRevoluteJointDef();
+		jd.bodyIdA = s_destruction.hub;
+		jd.bodyIdB = s_destruction.spokes[k];
+		jd.localAnchorA = offset;
+		s_destruction.spokeJoints[k] = b2CreateRevoluteJoint( worldId, &jd );
+	}
+
+	/* bodies of two shapes each (a box and a capsule) dropped onto the ledge */
+	b2Capsule cap = { { -0.3f, 0.0f }, { 0.3f, 0.0f }, 0.2f };
+	b2Polygon small = b2MakeOffsetBox( 0.2f, 0.2f, ( b2Vec2 ){ 0.0f, 0.4f }, 0.0f );
+	for ( int k = 0; k < 6; ++k )
+	{
+		bd.position = ( b2Vec2 ){ 10.5f + 0.6f * k, 5.0f + 1.2f * k };
+		s_destruction.pairs[k] = b2CreateBody( worldId, &bd );
+		s_destruction.pairShapes[k][0] = b2CreateCapsuleShape( s_destruction.pairs[k], &sd, &cap );
+		s_destruction.pairShapes[k][1] = b2CreatePolygonShape( s_destruction.pairs[k], &sd, &small );
+	}
+	return worldId;
+}
+
+void b2s_destruction_step( b2WorldId worldId, int step )
+{
+	if ( step == 20 )
+	{
+		/* bodies inside the pyramid: the awake order changes by swap-removal */
+		int doomed[5] = { 3, 12, 27, 40, 54 };
+		for ( int i = 0; i < 5; ++i )
+			b2DestroyBody( s_destruction.pyramid[doomed[i]] );
+	}
+	else if ( step == 40 )
+	{
+		/* spoke joints, in the graph colours and in the overflow set */
+		int doomed[4] = { 0, 5, 11, 13 };
+		for ( int i = 0; i < 4; ++i )
+			b2DestroyJoint( s_destruction.spokeJoints[doomed[i]] );
+	}
+	else if ( step == 60 )
+	{
+		/* one shape of each two-shape body: contacts go, masses are recomputed */
+		for ( int k = 0; k < 6; ++k )
+			b2DestroyShape( s_destruction.pairShapes[k][k & 1] );
+	}
+	else if ( step == 80 )
+	{
+		/* the hub with its remaining joints and contacts */
+		b2DestroyBody( s_destruction.hub );
+	}
+	else if ( step == 100 )
+	{
+		/* new bodies take the freed ids */
+		b2BodyDef bd = b2DefaultBodyDef();
+		bd.type = b2_dynamicBody;
+		b2ShapeDef sd = b2DefaultShapeDef();
+		b2Polygon box = b2MakeSquare( 0.4f );
+		for ( int k = 0; k < 8; ++k )
+		{
+			bd.position = ( b2Vec2 ){ -4.0f + 1.0f * k, 3.0f };
+			b2BodyId id = b2CreateBody( worldId, &bd );
+			b2CreatePolygonShape( id, &sd, &box );
+		}
+	}
+	else if ( step == 120 )
+	{
+		/* a static shape under resting bodies */
+		b2DestroyShape( s_destruction.ledge );
+	}
+}
+
+b2WorldId b2s_empty_world( void )
+{
+	b2WorldDef wd = b2DefaultWorldDef();
+	return b2CreateWorld( &wd );
+}
+
+b2BodyId b2s_add_body( b2WorldId worldId, int type )
+{
+	b2BodyDef bd = b2DefaultBodyDef();
+	bd.type = (b2BodyType)type;
+	return b2CreateBody( worldId, &bd );
+}
+
+b2BodyId b2s_add_square( b2WorldId worldId, float h )
+{
+	b2BodyDef bd = b2DefaultBodyDef();
+	bd.type = b2_dynamicBody;
+	b2BodyId bodyId = b2CreateBody( worldId, &bd );
+	b2ShapeDef sd = b2DefaultShapeDef();
+	b2Polygon square = b2MakeSquare( h );
+	b2CreatePolygonShape( bodyId, &sd, &square );
+	return bodyId;
+}

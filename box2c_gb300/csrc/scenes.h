@@ -88,6 +88,22 @@ b2WorldId b2s_joint_chains( int chains, int links, int flags, uint64_t seed );
  * ten dynamic boxes, above a static ground segment. */
 b2WorldId b2s_fast_shots( int count, uint64_t seed );
 
+/* Destruction scene: a pyramid, a hub with 14 pinned spokes (some joints in the
+ * overflow set) and bodies of two shapes on a static ledge.  b2s_destruction_step,
+ * called after each step with the step number, destroys pyramid bodies (step 20), spoke
+ * joints (40), one shape of each two-shape body (60), the hub (80), creates bodies that
+ * reuse the freed ids (100) and destroys the static ledge (120).  One such scene at a
+ * time per process. */
+b2WorldId b2s_destruction( void );
+void b2s_destruction_step( b2WorldId worldId, int step );
+
+/* Building blocks of the reference's test/test_world.c checks: a world of the default
+ * definition (gravity, sleep on), a body of the default definition and the given type
+ * at the origin, and a dynamic body at the origin with a square of half-extent h. */
+b2WorldId b2s_empty_world( void );
+b2BodyId b2s_add_body( b2WorldId worldId, int type );
+b2BodyId b2s_add_square( b2WorldId worldId, float h );
+
 /* Draws `n` integers uniform in [lo, hi] from `seed` into out. */
 void b2s_draw_ints( int n, uint64_t seed, int lo, int hi, int* out );
 /* Draws `n` floats uniform in [lo, hi) / standard normal from `seed` into out. */

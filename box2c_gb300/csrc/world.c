@@ -1374,3 +1374,169 @@ int b2World_DebugCollide( b2WorldId worldId, int contactId, float* out64 )
 {
 	return b2gd_debug_collide( &gworld_get( worldId )->dev, contactId, out64 );
 }
+
+/* ------------------------------------------------------------ destruction
+ * Reference src/body.c:161-176, :336-430 (b2DestroyBody), src/shape.c:220-290
+ * (b2DestroyShapeInternal, b2DestroyShape), src/shape.c:704-711 with
+ * src/broad_phase.c:71-116 (proxy destruction and the move-buffer purge),
+ * src/joint.c:657-768 (b2DestroyJointInternal) with src/constraint_graph.c:297-324.
+ * Islands and sleep are not built, so waking the bodies touched is a no-op.  Device
+ * records of destroyed ids stay in place unused: contacts are retired before the next
+ * narrowphase, and the awake list, shape lists and solve lists that the kernels walk
+ * are rebuilt without them. */
+static void unbuffer_move( gWorld* w, int proxyKey )
+{
+	if ( gset_remove( &w->moveSet, (uint64_t)( proxyKey + 1 ) ) == false )
+		return;
+	for ( int i = 0; i < w->moveArray.count; ++i )
+	{
+		if ( w->moveArray.data[i] == proxyKey )
+		{
+			gia_remove_swap( &w->moveArray, i );
+			break;
+		}
+	}
+}
+
+static void destroy_proxy( gWorld* w, gShape* s )
+{
+	if ( s->proxyKey == B2G_NULL )
+		return;
+	unbuffer_move( w, s->proxyKey );
+	gtree_destroy_proxy( w->trees + ( s->proxyKey & 3 ), s->proxyKey >> 2 );
+	s->proxyKey = B2G_NULL;
+}
+
+static void unlink_joint_edge( gWorld* w, gJoint* j, int e )
+{
+	gEdge* edge = j->edges + e;
+	gBody* body = w->bodies + edge->bodyId;
+	if ( edge->prevKey != B2G_NULL )
+		w->joints[edge->prevKey >> 1].edges[edge->prevKey & 1].nextKey = edge->nextKey;
+	if ( edge->nextKey != B2G_NULL )
+		w->joints[edge->nextKey >> 1].edges[edge->nextKey & 1].prevKey = edge->prevKey;
+	int key = ( j->id << 1 ) | e;
+	if ( body->headJointKey == key )
+		body->headJointKey = edge->nextKey;
+	body->jointCount -= 1;
+}
+
+static void destroy_joint( gWorld* w, gJoint* j )
+{
+	unlink_joint_edge( w, j, 0 );
+	unlink_joint_edge( w, j, 1 );
+	if ( j->colorIndex != B2G_NULL )
+	{
+		/* swap-remove from the colour: the overflow colour is solved in array order */
+		gColor* color = w->colors + j->colorIndex;
+		if ( j->colorIndex != B2G_OVERFLOW )
+		{
+			gbits_clear( &color->bodySet, j->edges[0].bodyId );
+			gbits_clear( &color->bodySet, j->edges[1].bodyId );
+		}
+		int moved = gia_remove_swap( &color->joints, j->localIndex );
+		if ( moved != B2G_NULL )
+			w->joints[color->joints.data[j->localIndex]].localIndex = j->localIndex;
+		w->solveDirty = true;
+	}
+	int id = j->id;
+	j->colorIndex = B2G_NULL;
+	j->localIndex = B2G_NULL;
+	j->id = B2G_NULL;
+	gid_free( &w->jointIds, id );
+}
+
+void b2DestroyJoint( b2JointId jointId )
+{
+	if ( b2Joint_IsValid( jointId ) == false )
+		return;
+	gWorld* w = s_worlds[jointId.world0];
+	if ( w->locked )
+		return;
+	destroy_joint( w, get_joint( jointId ) );
+}
+
+void b2DestroyShape( b2ShapeId shapeId )
+{
+	if ( b2Shape_IsValid( shapeId ) == false )
+		return;
+	gWorld* w = s_worlds[shapeId.world0];
+	if ( w->locked )
+		return;
+	gworld_ensure_mirror( w );
+	gworld_ensure_shape_mirror( w );
+	gShape* s = get_shape( shapeId );
+	gBody* b = w->bodies + s->bodyId;
+	int id = s->id;
+	if ( s->prev != B2G_NULL )
+		w->shapes[s->prev].next = s->next;
+	if ( s->next != B2G_NULL )
+		w->shapes[s->next].prev = s->prev;
+	if ( b->headShape == id )
+		b->headShape = s->next;
+	b->shapeCount -= 1;
+	destroy_proxy( w, s );
+	int key = b->headContactKey;
+	while ( key != B2G_NULL )
+	{
+		gContact* c = w->contacts + ( key >> 1 );
+		key = c->edges[key & 1].nextKey;
+		if ( c->shapeIdA == id || c->shapeIdB == id )
+			gcontact_destroy( w, c );
+	}
+	gid_free( &w->shapeIds, id );
+	s->id = B2G_NULL;
+	if ( b->automaticMass )
+		gbody_update_mass( w, b );
+	w->shapeListsDirty = true;
+	w->bodiesDirty = true;
+}
+
+void b2DestroyBody( b2BodyId bodyId )
+{
+	if ( b2Body_IsValid( bodyId ) == false )
+		return;
+	gWorld* w = body_world( bodyId );
+	if ( w->locked )
+		return;
+	gworld_ensure_mirror( w );
+	gBody* b = get_body( bodyId );
+	int key = b->headJointKey;
+	while ( key != B2G_NULL )
+	{
+		gJoint* j = w->joints + ( key >> 1 );
+		key = j->edges[key & 1].nextKey;
+		destroy_joint( w, j );
+	}
+	key = b->headContactKey;
+	while ( key != B2G_NULL )
+	{
+		gContact* c = w->contacts + ( key >> 1 );
+		key = c->edges[key & 1].nextKey;
+		gcontact_destroy( w, c );
+	}
+	for ( int sid = b->headShape; sid != B2G_NULL; )
+	{
+		gShape* s = w->shapes + sid;
+		destroy_proxy( w, s );
+		gid_free( &w->shapeIds, sid );
+		s->id = B2G_NULL;
+		sid = s->next;
+	}
+	/* the awake set drops the body by moving its last body into the slot */
+	if ( b->awakeIndex != B2G_NULL )
+	{
+		int at = b->awakeIndex;
+		int moved = gia_remove_swap( &w->awake, at );
+		if ( moved != B2G_NULL )
+			w->bodies[w->awake.data[at]].awakeIndex = at;
+		w->awakeDirty = true;
+	}
+	w->hInfo[b->id] = 0;
+	gid_free( &w->bodyIds, b->id );
+	b->awakeIndex = B2G_NULL;
+	b->id = B2G_NULL;
+	w->bodiesDirty = true;
+	w->shapeListsDirty = true;
+	w->solveDirty = true;
+}

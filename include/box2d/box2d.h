@@ -37,6 +37,10 @@ B2_API b2Counters b2World_GetCounters( b2WorldId worldId );
 
 /* Body (reference box2d.h:175-405) */
 B2_API b2BodyId b2CreateBody( b2WorldId worldId, const b2BodyDef* def );
+/* Destroys a body with its shapes, contacts and joints (reference box2d.h:179).  The
+ * last awake body takes the destroyed one's place in the awake order, as in the
+ * reference, so the following steps stay bit-identical to it. */
+B2_API void b2DestroyBody( b2BodyId bodyId );
 B2_API bool b2Body_IsValid( b2BodyId id );
 B2_API b2BodyType b2Body_GetType( b2BodyId bodyId );
 B2_API void b2Body_SetUserData( b2BodyId bodyId, void* userData );
@@ -68,6 +72,9 @@ B2_API b2ShapeId b2CreateCircleShape( b2BodyId bodyId, const b2ShapeDef* def, co
 B2_API b2ShapeId b2CreateSegmentShape( b2BodyId bodyId, const b2ShapeDef* def, const b2Segment* segment );
 B2_API b2ShapeId b2CreateCapsuleShape( b2BodyId bodyId, const b2ShapeDef* def, const b2Capsule* capsule );
 B2_API b2ShapeId b2CreatePolygonShape( b2BodyId bodyId, const b2ShapeDef* def, const b2Polygon* polygon );
+/* Destroys a shape and its contacts and updates the body's mass when it is automatic
+ * (reference box2d.h:441). */
+B2_API void b2DestroyShape( b2ShapeId shapeId );
 B2_API bool b2Shape_IsValid( b2ShapeId id );
 B2_API b2ShapeType b2Shape_GetType( b2ShapeId shapeId );
 B2_API b2BodyId b2Shape_GetBody( b2ShapeId shapeId );
@@ -83,6 +90,8 @@ B2_API b2AABB b2Shape_GetAABB( b2ShapeId shapeId );
 
 /* Joint (reference box2d.h:605-946); the revolute joint is the one on the step path. */
 B2_API b2JointId b2CreateRevoluteJoint( b2WorldId worldId, const b2RevoluteJointDef* def );
+/* Destroys a joint (reference box2d.h:605). */
+B2_API void b2DestroyJoint( b2JointId jointId );
 B2_API bool b2Joint_IsValid( b2JointId id );
 B2_API b2JointType b2Joint_GetType( b2JointId jointId );
 B2_API b2BodyId b2Joint_GetBodyA( b2JointId jointId );

@@ -1395,3 +1395,154 @@ void b2World_Step( b2WorldId worldId, float timeStep, int subStepCount )
 	o_step( w, timeStep, subStepCount );
 	w->locked = false;
 }
+
+/* ------------------------------------------------------------ destruction
+ * reference src/body.c:161-176, :336-430 (b2DestroyBody), src/shape.c:220-290
+ * (b2DestroyShapeInternal, b2DestroyShape), src/shape.c:704-711 and
+ * src/broad_phase.c:71-116 (proxy destruction with the move-buffer purge),
+ * src/joint.c:657-768 (b2DestroyJointInternal) and src/constraint_graph.c:297-324.
+ * Islands and sleep are not restated: with every body awake, waking is a no-op. */
+static void unbuffer_move( oWorld* w, int proxyKey )
+{
+	if ( oset_remove( &w->moveSet, (uint64_t)( proxyKey + 1 ) ) == false )
+		return;
+	for ( int i = 0; i < w->moveArray.count; ++i )
+	{
+		if ( w->moveArray.data[i] == proxyKey )
+		{
+			oia_remove_swap( &w->moveArray, i );
+			break;
+		}
+	}
+}
+
+static void destroy_proxy( oWorld* w, oShape* s )
+{
+	if ( s->proxyKey == O_NULL )
+		return;
+	unbuffer_move( w, s->proxyKey );
+	otree_destroy_proxy( w->trees + ( s->proxyKey & 3 ), s->proxyKey >> 2 );
+	s->proxyKey = O_NULL;
+}
+
+static void unlink_joint_edge( oWorld* w, oJoint* j, int e )
+{
+	oEdge* edge = j->edges + e;
+	oBody* body = w->bodies + edge->bodyId;
+	if ( edge->prevKey != O_NULL )
+		w->joints[edge->prevKey >> 1].edges[edge->prevKey & 1].nextKey = edge->nextKey;
+	if ( edge->nextKey != O_NULL )
+		w->joints[edge->nextKey >> 1].edges[edge->nextKey & 1].prevKey = edge->prevKey;
+	int key = ( j->id << 1 ) | e;
+	if ( body->headJointKey == key )
+		body->headJointKey = edge->nextKey;
+	body->jointCount -= 1;
+}
+
+static void destroy_joint( oWorld* w, oJoint* j )
+{
+	unlink_joint_edge( w, j, 0 );
+	unlink_joint_edge( w, j, 1 );
+	if ( j->colorIndex != O_NULL )
+	{
+		oColor* color = w->colors + j->colorIndex;
+		if ( j->colorIndex != O_OVERFLOW )
+		{
+			obits_clear( &color->bodySet, j->edges[0].bodyId );
+			obits_clear( &color->bodySet, j->edges[1].bodyId );
+		}
+		int moved = oia_remove_swap( &color->joints, j->localIndex );
+		if ( moved != O_NULL )
+			w->joints[color->joints.data[j->localIndex]].localIndex = j->localIndex;
+	}
+	int id = j->id;
+	j->colorIndex = O_NULL;
+	j->localIndex = O_NULL;
+	j->id = O_NULL;
+	oid_free( &w->jointIds, id );
+}
+
+void b2DestroyJoint( b2JointId jointId )
+{
+	if ( b2Joint_IsValid( jointId ) == false )
+		return;
+	oWorld* w = s_worlds[jointId.world0];
+	if ( w->locked )
+		return;
+	destroy_joint( w, w->joints + ( jointId.index1 - 1 ) );
+}
+
+void b2DestroyShape( b2ShapeId shapeId )
+{
+	if ( b2Shape_IsValid( shapeId ) == false )
+		return;
+	oWorld* w = s_worlds[shapeId.world0];
+	if ( w->locked )
+		return;
+	oShape* s = get_shape( shapeId );
+	oBody* b = w->bodies + s->bodyId;
+	int id = s->id;
+	if ( s->prev != O_NULL )
+		w->shapes[s->prev].next = s->next;
+	if ( s->next != O_NULL )
+		w->shapes[s->next].prev = s->prev;
+	if ( b->headShape == id )
+		b->headShape = s->next;
+	b->shapeCount -= 1;
+	destroy_proxy( w, s );
+	int key = b->headContactKey;
+	while ( key != O_NULL )
+	{
+		oContact* c = w->contacts + ( key >> 1 );
+		key = c->edges[key & 1].nextKey;
+		if ( c->shapeIdA == id || c->shapeIdB == id )
+			o_destroy_contact( w, c );
+	}
+	oid_free( &w->shapeIds, id );
+	s->id = O_NULL;
+	if ( b->automaticMass )
+		o_update_body_mass( w, b );
+}
+
+void b2DestroyBody( b2BodyId bodyId )
+{
+	if ( b2Body_IsValid( bodyId ) == false )
+		return;
+	oWorld* w = body_world( bodyId );
+	if ( w->locked )
+		return;
+	oBody* b = get_body( bodyId );
+	int key = b->headJointKey;
+	while ( key != O_NULL )
+	{
+		oJoint* j = w->joints + ( key >> 1 );
+		key = j->edges[key & 1].nextKey;
+		destroy_joint( w, j );
+	}
+	key = b->headContactKey;
+	while ( key != O_NULL )
+	{
+		oContact* c = w->contacts + ( key >> 1 );
+		key = c->edges[key & 1].nextKey;
+		o_destroy_contact( w, c );
+	}
+	for ( int sid = b->headShape; sid != O_NULL; )
+	{
+		oShape* s = w->shapes + sid;
+		destroy_proxy( w, s );
+		oid_free( &w->shapeIds, sid );
+		s->id = O_NULL;
+		sid = s->next;
+	}
+	/* the awake set drops the body by moving its last body into the slot */
+	if ( b->awakeIndex != O_NULL )
+	{
+		int at = b->awakeIndex;
+		int moved = oia_remove_swap( &w->awake, at );
+		if ( moved != O_NULL )
+			w->bodies[w->awake.data[at]].awakeIndex = at;
+	}
+	oid_free( &w->bodyIds, b->id );
+	b->awakeIndex = O_NULL;
+	b->id = O_NULL;
+}

@@ -9,8 +9,10 @@ def state_bits(backend, world):
     return b, b.view(np.uint32)
 
 
-def lockstep(a, b, make, steps, dt=1.0 / 60.0, substeps=4, check_manifolds=False):
-    """Steps both backends; returns (first mismatching step or None, detail, worst rel err)."""
+def lockstep(a, b, make, steps, dt=1.0 / 60.0, substeps=4, check_manifolds=False, after_step=None):
+    """Steps both backends; returns (first mismatching step or None, detail, worst rel err).
+    after_step(backend, world, step), when given, runs on both after each step (world
+    edits such as destruction)."""
     wa, wb = make(a), make(b)
     worst = 0.0
     try:
@@ -37,7 +39,46 @@ def lockstep(a, b, make, steps, dt=1.0 / 60.0, substeps=4, check_manifolds=False
             if s < steps:
                 a.step(wa, dt, substeps)
                 b.step(wb, dt, substeps)
+                if after_step is not None:
+                    after_step(a, wa, s + 1)
+                    after_step(b, wb, s + 1)
         return None, "bit-exact", worst
     finally:
         a.destroy(wa)
         b.destroy(wb)
+
+
+def run_world_api_checks(backend):
+    """Reference test/test_world.c:121-204 (DestroyAllBodiesWorld, TestIsValid): bodies
+    created one per step and then destroyed one per step leave no body behind; ids are
+    invalid after destruction and after the world is destroyed."""
+    L = backend.lib
+    w = backend.scenes.b2s_empty_world()
+    assert L.b2World_IsValid(w)
+    ids = []
+    creating = True
+    for _ in range(2 * 10 + 10):
+        if creating:
+            if len(ids) < 10:
+                ids.append(backend.scenes.b2s_add_square(w, 0.5))
+            else:
+                creating = False
+        elif ids:
+            L.b2DestroyBody(ids.pop())
+        L.b2World_Step(w, 1.0 / 60.0, 3)
+    assert backend.counters(w).bodyCount == 0
+    L.b2DestroyWorld(w)
+    assert not L.b2World_IsValid(w)
+
+    w = backend.scenes.b2s_empty_world()
+    b1 = backend.scenes.b2s_add_body(w, 0)
+    assert L.b2Body_IsValid(b1)
+    b2 = backend.scenes.b2s_add_body(w, 0)
+    assert L.b2Body_IsValid(b2)
+    L.b2DestroyBody(b1)
+    assert not L.b2Body_IsValid(b1)
+    L.b2DestroyBody(b2)
+    assert not L.b2Body_IsValid(b2)
+    L.b2DestroyWorld(w)
+    assert not L.b2World_IsValid(w)
+    assert not L.b2Body_IsValid(b2) and not L.b2Body_IsValid(b1)

@@ -193,3 +193,19 @@ def test_gpu_joint_limits_against_reference_golden(gpu, name):
     print(f"{name}: max rel state error vs the reference after N steps {drift}")
     assert drift[1] <= 1e-5, drift
     assert all(np.isfinite(v) for v in drift.values())
+
+
+def test_gpu_destruction_lockstep_oracle(gpu, oracle):
+    """b2DestroyBody / b2DestroyShape / b2DestroyJoint between steps (pyramid bodies,
+    joints in the colours and in the overflow set, one shape of two-shape bodies, a hub
+    with its joints, a static shape, then new bodies on the freed ids): the device stays
+    bit-identical to the oracle, which the CPU tests pin to the reference."""
+    step, detail, _ = lockstep(gpu, oracle, lambda b: b.destruction(), 160, check_manifolds=True,
+                               after_step=lambda b, w, s: b.destruction_step(w, s))
+    assert step is None, f"{detail} at step {step}"
+
+
+def test_gpu_world_destroy_all_bodies_and_validity(gpu):
+    """Reference test/test_world.c:121-204 (DestroyAllBodiesWorld, TestIsValid)."""
+    from tests.helpers import run_world_api_checks
+    run_world_api_checks(gpu)
