@@ -35,8 +35,8 @@ void gtape_free( gWorld* w )
 		return;
 	if ( t->dev )
 		cudaFree( t->dev );
-	free( t->hdr );
-	free( t );
+	b2g_free( t->hdr );
+	b2g_free( t );
 	w->tape = NULL;
 }
 
@@ -53,14 +53,14 @@ void b2World_BeginTape( b2WorldId worldId, int maxSteps )
 	gTape* t = w->tape;
 	if ( t == NULL )
 	{
-		t = (gTape*)calloc( 1, sizeof( gTape ) );
+		t = (gTape*)b2g_calloc( 1, sizeof( gTape ) );
 		if ( t == NULL )
 			return;
 		w->tape = t;
 	}
 	if ( maxSteps > t->maxSteps )
 	{
-		b2gTapeStep* h = (b2gTapeStep*)realloc( t->hdr, sizeof( b2gTapeStep ) * (size_t)maxSteps );
+		b2gTapeStep* h = (b2gTapeStep*)b2g_realloc( t->hdr, sizeof( b2gTapeStep ) * (size_t)maxSteps );
 		if ( h == NULL )
 			return;
 		t->hdr = h;

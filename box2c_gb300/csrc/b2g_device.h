@@ -41,6 +41,10 @@ typedef struct b2gHostIO
 	b2gContactInit* newContacts;
 } b2gHostIO;
 
+/* Host memory of the library through the caller's allocator (util.c). */
+void* b2g_calloc( size_t count, size_t size );
+void b2g_free( void* p );
+
 int b2gd_device_ok( void );
 const char* b2gd_last_error( void );
 

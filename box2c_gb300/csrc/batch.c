@@ -31,15 +31,15 @@ static bool reserve_worlds( int count )
 	if ( count <= s_cap )
 		return true;
 	int cap = count < 64 ? 64 : count;
-	gWorld** w = (gWorld**)realloc( s_worlds, sizeof( gWorld* ) * (size_t)cap );
+	gWorld** w = (gWorld**)b2g_realloc( s_worlds, sizeof( gWorld* ) * (size_t)cap );
 	if ( w == NULL )
 		return false;
 	s_worlds = w;
-	void** s = (void**)realloc( s_streams, sizeof( void* ) * (size_t)cap );
+	void** s = (void**)b2g_realloc( s_streams, sizeof( void* ) * (size_t)cap );
 	if ( s == NULL )
 		return false;
 	s_streams = s;
-	b2WorldId* a = (b2WorldId*)realloc( s_alone, sizeof( b2WorldId ) * (size_t)cap );
+	b2WorldId* a = (b2WorldId*)b2g_realloc( s_alone, sizeof( b2WorldId ) * (size_t)cap );
 	if ( a == NULL )
 		return false;
 	s_alone = a;

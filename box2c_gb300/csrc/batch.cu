@@ -438,12 +438,12 @@ static const TuneCandidate s_tune[TUNE_CANDIDATES] = { TUNE_SHAPE( 128, 6 ), TUN
 
 extern "C" b2gBatch* b2gd_batch_create( void )
 {
-	b2gBatch* b = (b2gBatch*)calloc( 1, sizeof( b2gBatch ) );
+	b2gBatch* b = (b2gBatch*)b2g_calloc( 1, sizeof( b2gBatch ) );
 	if ( b == nullptr )
 		return nullptr;
 	if ( cudaStreamCreateWithFlags( &b->stream, cudaStreamNonBlocking ) != cudaSuccess )
 	{
-		free( b );
+		b2g_free( b );
 		return nullptr;
 	}
 	int dev = 0;
@@ -510,7 +510,7 @@ extern "C" void b2gd_batch_destroy( b2gBatch* b )
 			cudaEventDestroy( b->half[h].ev[i] );
 	}
 	cudaStreamDestroy( b->stream );
-	free( b );
+	b2g_free( b );
 }
 
 extern "C" b2gBatchItem* b2gd_batch_items( b2gBatch* b, int count )

@@ -29,6 +29,14 @@ typedef struct gIntArray
 
 void gia_push( gIntArray* a, int v );
 int gia_remove_swap( gIntArray* a, int index ); /* returns the moved index or -1 */
+bool gia_reserve( gIntArray* a, int count );   /* false when memory ran out */
+
+/* Host memory through the caller's allocator (util.c, reference src/allocate.c):
+ * b2g_realloc keeps the old block when it fails; every failure is counted. */
+void* b2g_alloc( size_t size );
+void* b2g_realloc( void* p, size_t size );
+int b2g_alloc_failures( void );
+void b2g_note_alloc_failure( void );
 void gia_free( gIntArray* a );
 
 typedef struct gSet
@@ -73,7 +81,8 @@ typedef struct gTree
 	gNode* nodes;
 	int root;
 	int nodeCount;
-	int capacity;
+	int capacity; /* nodes in the pool (used or on the free list) */
+	int reserved; /* nodes the allocation holds, at least capacity */
 	int freeList;
 	int proxyCount;
 	int* leafIndices;
@@ -286,9 +295,13 @@ gWorld* gworld_get( b2WorldId id );
 gWorld* gworld_slot( int slot );
 void gworld_fail( const char* what );
 
+/* True (and the world marked failed) when a host allocation failed since
+ * b2g_alloc_failures() returned `before`. */
+bool gworld_out_of_memory( gWorld* w, int before );
+
 void gworld_ensure_mirror( gWorld* w );
 void gworld_ensure_shape_mirror( gWorld* w );
-void gworld_reserve_mirrors( gWorld* w );
+bool gworld_reserve_mirrors( gWorld* w ); /* false when pinned memory ran out */
 void gworld_flush( gWorld* w );
 
 void gstep_run( gWorld* w, float dt, int subSteps );

@@ -201,7 +201,7 @@ extern "C" int b2gd_pair_query( b2gDevWorld* w, b2gPairQuery** query, const b2gT
 	b2gPairQuery* q = *query;
 	if ( q == nullptr )
 	{
-		q = (b2gPairQuery*)calloc( 1, sizeof( b2gPairQuery ) );
+		q = (b2gPairQuery*)b2g_calloc( 1, sizeof( b2gPairQuery ) );
 		if ( q == nullptr )
 			return (int)cudaErrorMemoryAllocation;
 		*query = q;
@@ -270,5 +270,5 @@ extern "C" void b2gd_pair_query_free( b2gPairQuery* q )
 		if ( q->nodes[t] )
 			cudaFree( q->nodes[t] );
 	release_mapped( q );
-	free( q );
+	b2g_free( q );
 }

@@ -37,12 +37,53 @@ enum
 	MAX_DEVICES = 64
 };
 
-static std::mutex s_setupLock;
-static void* s_rows[MAX_DEVICES];
+/* The array's address in each device's current context, with the id of that context:
+ * a context made after cudaDeviceReset loads the library's device code anew, so its
+ * address is looked up again. */
+typedef struct RowsAddress
+{
+	void* rows;
+	unsigned long long context;
+} RowsAddress;
 
-/* Looks up the array's device address once per device, with that device current.  The
- * lookup may load the library's device code on that device, so the first call on each
- * device belongs before any stream capture starts. */
+static std::mutex s_setupLock;
+static RowsAddress s_rows[MAX_DEVICES];
+
+typedef int ( *CtxGetCurrentFn )( void** ctx );
+typedef int ( *CtxGetIdFn )( void* ctx, unsigned long long* id );
+
+/* Id of the current context through the driver's entry points (no link to the driver
+ * library); 0 when the driver does not provide them, and then the address is kept per
+ * device ordinal only. */
+static unsigned long long current_context_id( void )
+{
+	static CtxGetCurrentFn getCurrent;
+	static CtxGetIdFn getId;
+	static bool looked;
+	if ( looked == false )
+	{
+		cudaDriverEntryPointQueryResult q;
+		void* f = nullptr;
+		if ( cudaGetDriverEntryPointByVersion( "cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q ) == cudaSuccess &&
+			 q == cudaDriverEntryPointSuccess )
+			getCurrent = (CtxGetCurrentFn)f;
+		f = nullptr;
+		if ( cudaGetDriverEntryPointByVersion( "cuCtxGetId", &f, 12000, cudaEnableDefault, &q ) == cudaSuccess &&
+			 q == cudaDriverEntryPointSuccess )
+			getId = (CtxGetIdFn)f;
+		looked = true;
+	}
+	void* ctx = nullptr;
+	unsigned long long id = 0;
+	if ( getCurrent == nullptr || getId == nullptr || getCurrent( &ctx ) != 0 || ctx == nullptr || getId( ctx, &id ) != 0 )
+		return 0;
+	return id;
+}
+
+/* Looks up the array's device address once per device (and again after the device's
+ * context was replaced), with that device current.  The lookup may load the library's
+ * device code on that device, so the first call on each device belongs before any
+ * stream capture starts. */
 static int rows_on_current_device( void** out )
 {
 	int dev = -1;
@@ -50,17 +91,20 @@ static int rows_on_current_device( void** out )
 	if ( e != cudaSuccess )
 		return (int)e;
 	if ( dev < 0 || dev >= MAX_DEVICES )
-		return -1;
+		return B2_SOLVE_NOALLOC_DEVICE_LIMIT;
 	std::lock_guard<std::mutex> guard( s_setupLock );
-	if ( s_rows[dev] == nullptr )
+	RowsAddress* a = s_rows + dev;
+	if ( a->rows == nullptr || a->context != current_context_id() )
 	{
 		void* p = nullptr;
 		e = cudaGetSymbolAddress( &p, g_contactRows );
 		if ( e != cudaSuccess )
 			return (int)e;
-		s_rows[dev] = p;
+		a->rows = p;
+		/* the lookup has made the device's context current: its id keys the address */
+		a->context = current_context_id();
 	}
-	*out = s_rows[dev];
+	*out = a->rows;
 	return 0;
 }
 

@@ -14,6 +14,7 @@
  */
 #include "host.h"
 #include "b2g_toi.h"
+#include "box2d/gpu.h"
 
 #include <string.h>
 
@@ -24,8 +25,12 @@ static void push_begin( gWorld* w, int a, int b )
 {
 	if ( w->beginCount == w->beginCap )
 	{
-		w->beginCap = w->beginCap ? 2 * w->beginCap : 16;
-		w->beginEvents = realloc( w->beginEvents, sizeof( b2ContactBeginTouchEvent ) * (size_t)w->beginCap );
+		int cap = w->beginCap ? 2 * w->beginCap : 16;
+		void* p = b2g_realloc( w->beginEvents, sizeof( b2ContactBeginTouchEvent ) * (size_t)cap );
+		if ( p == NULL )
+			return;
+		w->beginEvents = p;
+		w->beginCap = cap;
 	}
 	b2ContactBeginTouchEvent* e = w->beginEvents + w->beginCount++;
 	e->shapeIdA = ( b2ShapeId ){ a + 1, (uint16_t)w->slot, w->shapes[a].revision };
@@ -36,8 +41,12 @@ static void push_end( gWorld* w, int a, int b )
 {
 	if ( w->endCount == w->endCap )
 	{
-		w->endCap = w->endCap ? 2 * w->endCap : 16;
-		w->endEvents = realloc( w->endEvents, sizeof( b2ContactEndTouchEvent ) * (size_t)w->endCap );
+		int cap = w->endCap ? 2 * w->endCap : 16;
+		void* p = b2g_realloc( w->endEvents, sizeof( b2ContactEndTouchEvent ) * (size_t)cap );
+		if ( p == NULL )
+			return;
+		w->endEvents = p;
+		w->endCap = cap;
 	}
 	b2ContactEndTouchEvent* e = w->endEvents + w->endCount++;
 	e->shapeIdA = ( b2ShapeId ){ a + 1, (uint16_t)w->slot, w->shapes[a].revision };
@@ -51,8 +60,17 @@ static b2gContactInit* push_pending( gWorld* w )
 {
 	if ( w->pendingCount == w->pendingCap )
 	{
-		w->pendingCap = w->pendingCap ? 2 * w->pendingCap : 256;
-		w->pending = (b2gContactInit*)realloc( w->pending, sizeof( b2gContactInit ) * (size_t)w->pendingCap );
+		int cap = w->pendingCap ? 2 * w->pendingCap : 256;
+		b2gContactInit* p = (b2gContactInit*)b2g_realloc( w->pending, sizeof( b2gContactInit ) * (size_t)cap );
+		if ( p == NULL )
+		{
+			/* out of memory: the record is written nowhere and the world fails at the
+			 * next check of its API call */
+			static _Thread_local b2gContactInit sink;
+			return &sink;
+		}
+		w->pending = p;
+		w->pendingCap = cap;
 	}
 	return w->pending + w->pendingCount++;
 }
@@ -68,7 +86,10 @@ static int compact_pending( gWorld* w )
 			ids = w->pending[i].id + 1;
 	if ( ids > w->scratchCap )
 	{
-		w->scratch = (int*)realloc( w->scratch, sizeof( int ) * (size_t)ids );
+		int* p = (int*)b2g_realloc( w->scratch, sizeof( int ) * (size_t)ids );
+		if ( p == NULL )
+			return -1;
+		w->scratch = p;
 		w->scratchCap = ids;
 	}
 	for ( int i = 0; i < n; ++i )
@@ -111,7 +132,13 @@ void gcontact_create( gWorld* w, gShape* shapeA, gShape* shapeB )
 		int nc = w->contactCap < 64 ? 64 : w->contactCap;
 		while ( nc < id + 1 )
 			nc *= 2;
-		w->contacts = (gContact*)realloc( w->contacts, sizeof( gContact ) * (size_t)nc );
+		gContact* p = (gContact*)b2g_realloc( w->contacts, sizeof( gContact ) * (size_t)nc );
+		if ( p == NULL )
+		{
+			gid_free( &w->contactIds, id );
+			return;
+		}
+		w->contacts = p;
 		for ( int i = w->contactCap; i < nc; ++i )
 			w->contacts[i].id = B2G_NULL;
 		w->contactCap = nc;
@@ -359,9 +386,15 @@ static bool pair_query( int proxyId, int shapeId, void* context )
 	gPairList* l = q->list;
 	if ( l->count == l->capacity )
 	{
-		l->capacity = l->capacity ? 2 * l->capacity : 16;
-		l->a = (int*)realloc( l->a, sizeof( int ) * (size_t)l->capacity );
-		l->b = (int*)realloc( l->b, sizeof( int ) * (size_t)l->capacity );
+		int cap = l->capacity ? 2 * l->capacity : 16;
+		int* a = (int*)b2g_realloc( l->a, sizeof( int ) * (size_t)cap );
+		if ( a != NULL )
+			l->a = a;
+		int* b = a != NULL ? (int*)b2g_realloc( l->b, sizeof( int ) * (size_t)cap ) : NULL;
+		if ( b == NULL )
+			return false;
+		l->b = b;
+		l->capacity = cap;
 	}
 	l->a[l->count] = idA;
 	l->b[l->count] = idB;
@@ -456,7 +489,9 @@ static int update_pairs( gWorld* w )
 		if ( e )
 			return e;
 	}
-	c.lists = (gPairList*)calloc( (size_t)moveCount, sizeof( gPairList ) );
+	c.lists = (gPairList*)b2g_calloc( (size_t)moveCount, sizeof( gPairList ) );
+	if ( c.lists == NULL )
+		return -1;
 	if ( gpool_try_for( moveCount, PAIR_GRAIN, query_moved, &c ) == false )
 		query_moved( 0, moveCount, &c );
 	for ( int i = 0; i < moveCount; ++i )
@@ -464,10 +499,10 @@ static int update_pairs( gWorld* w )
 		gPairList* l = c.lists + i;
 		for ( int k = l->count - 1; k >= 0; --k )
 			gcontact_create( w, w->shapes + l->a[k], w->shapes + l->b[k] );
-		free( l->a );
-		free( l->b );
+		b2g_free( l->a );
+		b2g_free( l->b );
 	}
-	free( c.lists );
+	b2g_free( c.lists );
 	w->moveArray.count = 0;
 	gset_clear( &w->moveSet );
 	return 0;
@@ -849,6 +884,7 @@ static void build_solve_lists( gWorld* w, b2gSolvePlan* plan )
 int gstep_begin( gWorld* w )
 {
 	double t0 = b2g_now_ms();
+	int failures = b2g_alloc_failures();
 	int pe = update_pairs( w );
 	if ( pe )
 	{
@@ -867,6 +903,13 @@ int gstep_begin( gWorld* w )
 		return -1;
 	}
 	int staged = compact_pending( w );
+	if ( staged < 0 || gworld_out_of_memory( w, failures ) )
+	{
+		/* nothing reaches the device from a step whose host state is incomplete */
+		if ( w->status == 0 )
+			w->status = B2_STATUS_OUT_OF_HOST_MEMORY;
+		return -1;
+	}
 	if ( staged > 0 )
 		memcpy( w->io.newContacts, w->pending, sizeof( b2gContactInit ) * (size_t)staged );
 	w->pendingCount = 0;
@@ -908,6 +951,7 @@ static void step_constants( gWorld* w, float dt, int subSteps, b2gStepConst* sc 
 
 int gstep_after_collide( gWorld* w, float dt, int subSteps, b2gStepConst* sc, b2gSolvePlan* plan )
 {
+	int failures = b2g_alloc_failures();
 	int eventCount = w->io.counters[0];
 	w->lastEventCount = eventCount;
 	/* events reach the host through mapped memory */
@@ -930,6 +974,8 @@ int gstep_after_collide( gWorld* w, float dt, int subSteps, b2gStepConst* sc, b2
 	}
 
 	build_solve_lists( w, plan );
+	if ( gworld_out_of_memory( w, failures ) )
+		return 0;
 	plan->awakeCount = w->awake.count;
 	plan->bodyIdCount = w->bodyIds.next;
 	if ( w->solveUploaded == false )
@@ -1020,27 +1066,32 @@ void gstep_run( gWorld* w, float dt, int subSteps )
 
 void b2World_Step( b2WorldId worldId, float timeStep, int subStepCount )
 {
+	if ( b2World_IsValid( worldId ) == false )
+		return;
 	gWorld* w = gworld_get( worldId );
 	if ( w->locked )
 		return;
 	w->beginCount = 0;
 	w->endCount = 0;
 	memset( &w->profile, 0, sizeof( w->profile ) );
-	if ( timeStep == 0.0f )
+	if ( timeStep == 0.0f || w->status != 0 )
 		return;
 	double t0 = b2g_now_ms();
+	int failures = b2g_alloc_failures();
 	w->locked = true;
 	w->dev.h2dBytes = 0;
 	w->dev.d2hBytes = 0;
 	b2gd_mark( &w->dev, 0 );
 	gworld_flush( w );
-	gstep_run( w, timeStep, subStepCount );
+	if ( w->status == 0 )
+		gstep_run( w, timeStep, subStepCount );
 	b2gd_mark( &w->dev, 6 );
 	w->mirrorStale = true;
 	w->shapeMirrorStale = true;
 	w->jointMirrorStale = true;
 	w->locked = false;
 	w->profile.step = (float)( b2g_now_ms() - t0 );
+	gworld_out_of_memory( w, failures );
 	if ( w->status )
 		gworld_fail( b2gd_last_error() );
 }

@@ -20,8 +20,12 @@ void gtree_init( gTree* t )
 {
 	memset( t, 0, sizeof( *t ) );
 	t->root = B2G_NULL;
+	t->freeList = B2G_NULL;
+	t->nodes = (gNode*)b2g_calloc( 16, sizeof( gNode ) );
+	if ( t->nodes == NULL )
+		return;
 	t->capacity = 16;
-	t->nodes = (gNode*)calloc( (size_t)t->capacity, sizeof( gNode ) );
+	t->reserved = 16;
 	for ( int i = 0; i < t->capacity - 1; ++i )
 	{
 		t->nodes[i].parent = i + 1;
@@ -34,28 +38,53 @@ void gtree_init( gTree* t )
 
 void gtree_free( gTree* t )
 {
-	free( t->nodes );
-	free( t->leafIndices );
-	free( t->leafCenters );
+	b2g_free( t->nodes );
+	b2g_free( t->leafIndices );
+	b2g_free( t->leafCenters );
 	memset( t, 0, sizeof( *t ) );
+}
+
+/* Capacity after the next growth: by half, as the reference grows its pool, so that
+ * node indices follow its allocation order. */
+static int next_capacity( int cap ) { return cap < 16 ? 16 : cap + ( cap >> 1 ); }
+
+/* Makes the allocation hold `count` nodes without changing the pool.  False when
+ * memory ran out. */
+static bool reserve_nodes( gTree* t, int count )
+{
+	if ( count <= t->reserved )
+		return true;
+	gNode* nodes = (gNode*)b2g_realloc( t->nodes, sizeof( gNode ) * (size_t)count );
+	if ( nodes == NULL )
+		return false;
+	t->nodes = nodes;
+	t->reserved = count;
+	return true;
+}
+
+/* Grows the pool when the free list is empty.  False when memory ran out. */
+static bool grow_nodes( gTree* t )
+{
+	if ( t->freeList != B2G_NULL )
+		return true;
+	int cap = next_capacity( t->capacity );
+	if ( reserve_nodes( t, cap ) == false )
+		return false;
+	t->capacity = cap;
+	for ( int i = t->nodeCount; i < t->capacity - 1; ++i )
+	{
+		t->nodes[i].parent = i + 1;
+		t->nodes[i].height = -1;
+	}
+	t->nodes[t->capacity - 1].parent = B2G_NULL;
+	t->nodes[t->capacity - 1].height = -1;
+	t->freeList = t->nodeCount;
+	return true;
 }
 
 static int alloc_node( gTree* t )
 {
-	if ( t->freeList == B2G_NULL )
-	{
-		int old = t->capacity;
-		t->capacity += old >> 1;
-		t->nodes = (gNode*)realloc( t->nodes, sizeof( gNode ) * (size_t)t->capacity );
-		for ( int i = t->nodeCount; i < t->capacity - 1; ++i )
-		{
-			t->nodes[i].parent = i + 1;
-			t->nodes[i].height = -1;
-		}
-		t->nodes[t->capacity - 1].parent = B2G_NULL;
-		t->nodes[t->capacity - 1].height = -1;
-		t->freeList = t->nodeCount;
-	}
+	grow_nodes( t );
 	int id = t->freeList;
 	gNode* n = t->nodes + id;
 	t->freeList = n->parent;
@@ -436,6 +465,11 @@ static void remove_leaf( gTree* t, int leaf )
 
 int gtree_create_proxy( gTree* t, b2gBox box, uint32_t category, int userData )
 {
+	/* a leaf and, on insertion, a new parent: the memory of a pool growth is held before
+	 * the tree changes, so the insertion cannot fail half way */
+	bool twoFree = t->freeList != B2G_NULL && t->nodes[t->freeList].parent != B2G_NULL;
+	if ( twoFree == false && reserve_nodes( t, next_capacity( t->capacity ) ) == false )
+		return B2G_NULL;
 	int id = alloc_node( t );
 	gNode* n = t->nodes + id;
 	n->box = box;
@@ -645,8 +679,19 @@ void gtree_rebuild( gTree* t )
 	if ( proxyCount > t->rebuildCapacity )
 	{
 		int cap = proxyCount + proxyCount / 2;
-		t->leafIndices = (int*)realloc( t->leafIndices, sizeof( int ) * (size_t)cap );
-		t->leafCenters = (b2gVec*)realloc( t->leafCenters, sizeof( b2gVec ) * (size_t)cap );
+		int* li = (int*)b2g_alloc( sizeof( int ) * (size_t)cap );
+		b2gVec* lc = (b2gVec*)b2g_alloc( sizeof( b2gVec ) * (size_t)cap );
+		if ( li == NULL || lc == NULL )
+		{
+			/* no room for the rebuild's scratch: the tree stays as it is, still valid */
+			b2g_free( li );
+			b2g_free( lc );
+			return;
+		}
+		b2g_free( t->leafIndices );
+		b2g_free( t->leafCenters );
+		t->leafIndices = li;
+		t->leafCenters = lc;
 		t->rebuildCapacity = cap;
 	}
 	int leafCount = 0;

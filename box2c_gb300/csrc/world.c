@@ -34,12 +34,15 @@ double b2g_now_ms( void )
 }
 
 void b2SetAssertFcn( b2AssertFcn* fcn ) { s_assertFcn = fcn; }
-void b2SetAllocator( b2AllocFcn* allocFcn, b2FreeFcn* freeFcn )
+
+bool gworld_out_of_memory( gWorld* w, int before )
 {
-	(void)allocFcn;
-	(void)freeFcn;
+	if ( b2g_alloc_failures() == before )
+		return false;
+	if ( w->status == 0 )
+		w->status = B2_STATUS_OUT_OF_HOST_MEMORY;
+	return true;
 }
-int b2GetByteCount( void ) { return 0; }
 b2Version b2GetVersion( void )
 {
 	b2Version v = { 3, 0, 0 };
@@ -127,20 +130,6 @@ b2RevoluteJointDef b2DefaultRevoluteJointDef( void )
 }
 
 /* ------------------------------------------------------------ pinned mirrors */
-static void* pinned_realloc( void* old, size_t oldBytes, size_t newBytes )
-{
-	void* p = NULL;
-	if ( cudaHostAlloc( &p, newBytes, cudaHostAllocDefault ) != cudaSuccess )
-		return NULL;
-	memset( p, 0, newBytes );
-	if ( old )
-	{
-		memcpy( p, old, oldBytes );
-		cudaFreeHost( old );
-	}
-	return p;
-}
-
 static int grow_cap( int have, int need )
 {
 	int c = have < 64 ? 64 : have;
@@ -149,41 +138,73 @@ static int grow_cap( int have, int need )
 	return c;
 }
 
-void gworld_reserve_mirrors( gWorld* w )
+/* Grows a group of pinned mirrors together: every new buffer is allocated before any
+ * old one is released, so a failed request leaves the group as it was. */
+static bool grow_pinned( void** ptrs[], const size_t oldBytes[], const size_t newBytes[], int n )
+{
+	void* fresh[12];
+	for ( int i = 0; i < n; ++i )
+	{
+		fresh[i] = NULL;
+		if ( cudaHostAlloc( &fresh[i], newBytes[i], cudaHostAllocDefault ) != cudaSuccess )
+		{
+			for ( int k = 0; k < i; ++k )
+				cudaFreeHost( fresh[k] );
+			b2g_note_alloc_failure();
+			return false;
+		}
+		memset( fresh[i], 0, newBytes[i] );
+		if ( *ptrs[i] )
+			memcpy( fresh[i], *ptrs[i], oldBytes[i] );
+	}
+	for ( int i = 0; i < n; ++i )
+	{
+		if ( *ptrs[i] )
+			cudaFreeHost( *ptrs[i] );
+		*ptrs[i] = fresh[i];
+	}
+	return true;
+}
+
+bool gworld_reserve_mirrors( gWorld* w )
 {
 	int needB = w->bodyIds.next;
 	if ( needB > w->mirrorCap )
 	{
 		int nc = grow_cap( w->mirrorCap, needB );
 		size_t o4 = 16u * (size_t)w->mirrorCap, n4 = 16u * (size_t)nc;
-		w->hState = (float*)pinned_realloc( w->hState, 2 * o4, 2 * n4 );
-		w->hXf = (float*)pinned_realloc( w->hXf, o4, n4 );
-		w->hCenters = (float*)pinned_realloc( w->hCenters, o4, n4 );
-		w->hPrev = (float*)pinned_realloc( w->hPrev, o4, n4 );
-		w->hMass = (float*)pinned_realloc( w->hMass, o4, n4 );
-		w->hForce = (float*)pinned_realloc( w->hForce, o4, n4 );
-		w->hExtent = (float*)pinned_realloc( w->hExtent, o4, n4 );
-		w->hInfo = (int*)pinned_realloc( w->hInfo, 4u * (size_t)w->mirrorCap, 4u * (size_t)nc );
+		void** ptrs[] = { (void**)&w->hState, (void**)&w->hXf, (void**)&w->hCenters, (void**)&w->hPrev,
+						  (void**)&w->hMass,  (void**)&w->hForce, (void**)&w->hExtent, (void**)&w->hInfo };
+		size_t ob[] = { 2 * o4, o4, o4, o4, o4, o4, o4, 4u * (size_t)w->mirrorCap };
+		size_t nb[] = { 2 * n4, n4, n4, n4, n4, n4, n4, 4u * (size_t)nc };
+		if ( grow_pinned( ptrs, ob, nb, 8 ) == false )
+			return false;
 		w->mirrorCap = nc;
 	}
 	int needS = w->shapeIds.next;
 	if ( needS > w->shapeMirrorCap )
 	{
 		int nc = grow_cap( w->shapeMirrorCap, needS );
-		w->hGeo = (b2gShapeGeo*)pinned_realloc( w->hGeo, sizeof( b2gShapeGeo ) * (size_t)w->shapeMirrorCap,
-												sizeof( b2gShapeGeo ) * (size_t)nc );
-		w->hAabb = (float*)pinned_realloc( w->hAabb, 16u * (size_t)w->shapeMirrorCap, 16u * (size_t)nc );
-		w->hFat = (float*)pinned_realloc( w->hFat, 16u * (size_t)w->shapeMirrorCap, 16u * (size_t)nc );
+		void** ptrs[] = { (void**)&w->hGeo, (void**)&w->hAabb, (void**)&w->hFat };
+		size_t ob[] = { sizeof( b2gShapeGeo ) * (size_t)w->shapeMirrorCap, 16u * (size_t)w->shapeMirrorCap,
+						16u * (size_t)w->shapeMirrorCap };
+		size_t nb[] = { sizeof( b2gShapeGeo ) * (size_t)nc, 16u * (size_t)nc, 16u * (size_t)nc };
+		if ( grow_pinned( ptrs, ob, nb, 3 ) == false )
+			return false;
 		w->shapeMirrorCap = nc;
 	}
 	int needJ = w->jointIds.next;
 	if ( needJ > w->jointMirrorCap )
 	{
 		int nc = grow_cap( w->jointMirrorCap, needJ );
-		w->hJoints = (b2gJointDev*)pinned_realloc( w->hJoints, sizeof( b2gJointDev ) * (size_t)w->jointMirrorCap,
-												   sizeof( b2gJointDev ) * (size_t)nc );
+		void** ptrs[] = { (void**)&w->hJoints };
+		size_t ob[] = { sizeof( b2gJointDev ) * (size_t)w->jointMirrorCap };
+		size_t nb[] = { sizeof( b2gJointDev ) * (size_t)nc };
+		if ( grow_pinned( ptrs, ob, nb, 1 ) == false )
+			return false;
 		w->jointMirrorCap = nc;
 	}
+	return true;
 }
 
 /* Refreshes the host body mirror from the device after a step. */
@@ -256,8 +277,15 @@ void gworld_flush( gWorld* w )
 	}
 	if ( w->shapeListsDirty )
 	{
-		int* range = (int*)malloc( sizeof( int ) * 2 * (size_t)( nb > 0 ? nb : 1 ) );
-		int* list = (int*)malloc( sizeof( int ) * (size_t)( ns > 0 ? ns : 1 ) );
+		int* range = (int*)b2g_alloc( sizeof( int ) * 2 * (size_t)( nb > 0 ? nb : 1 ) );
+		int* list = (int*)b2g_alloc( sizeof( int ) * (size_t)( ns > 0 ? ns : 1 ) );
+		if ( range == NULL || list == NULL )
+		{
+			b2g_free( range );
+			b2g_free( list );
+			w->status = w->status ? w->status : B2_STATUS_OUT_OF_HOST_MEMORY;
+			return;
+		}
 		int n = 0;
 		for ( int i = 0; i < nb; ++i )
 		{
@@ -275,8 +303,8 @@ void gworld_flush( gWorld* w )
 		}
 		e |= b2gd_upload_shape_lists( &w->dev, range, nb, list, n );
 		e |= b2gd_sync( &w->dev );
-		free( range );
-		free( list );
+		b2g_free( range );
+		b2g_free( list );
 		w->shapeListsDirty = false;
 	}
 	if ( w->jointsDirty )
@@ -312,13 +340,19 @@ b2WorldId b2CreateWorld( const b2WorldDef* def )
 		int nc = s_worldCap ? 2 * s_worldCap : 16;
 		if ( nc > G_MAX_WORLDS )
 			nc = G_MAX_WORLDS;
-		s_worlds = (gWorld**)realloc( s_worlds, sizeof( gWorld* ) * (size_t)nc );
+		gWorld** grown = (gWorld**)b2g_realloc( s_worlds, sizeof( gWorld* ) * (size_t)nc );
+		if ( grown == NULL )
+			return b2_nullWorldId;
+		s_worlds = grown;
 		memset( s_worlds + s_worldCap, 0, sizeof( gWorld* ) * (size_t)( nc - s_worldCap ) );
 		slot = s_worldCap;
 		s_worldCap = nc;
 	}
 	if ( s_worlds[slot] == NULL )
-		s_worlds[slot] = (gWorld*)calloc( 1, sizeof( gWorld ) );
+		s_worlds[slot] = (gWorld*)b2g_calloc( 1, sizeof( gWorld ) );
+	if ( s_worlds[slot] == NULL )
+		return b2_nullWorldId;
+	int failures = b2g_alloc_failures();
 	gWorld* w = s_worlds[slot];
 	uint16_t revision = w->revision;
 	memset( w, 0, sizeof( *w ) );
@@ -344,11 +378,18 @@ b2WorldId b2CreateWorld( const b2WorldDef* def )
 	w->enableWarmStarting = true;
 	w->enableContinuous = def->enableContinous;
 	b2WorldId id = { (uint16_t)( slot + 1 ), w->revision };
+	if ( b2g_alloc_failures() != failures )
+	{
+		b2DestroyWorld( id );
+		return b2_nullWorldId;
+	}
 	return id;
 }
 
 void b2DestroyWorld( b2WorldId worldId )
 {
+	if ( b2World_IsValid( worldId ) == false )
+		return;
 	gWorld* w = gworld_get( worldId );
 	gtape_free( w );
 	b2gd_pair_query_free( w->pairQuery );
@@ -373,14 +414,14 @@ void b2DestroyWorld( b2WorldId worldId )
 	gia_free( &w->jointList );
 	gset_free( &w->moveSet );
 	gset_free( &w->pairSet );
-	free( w->bodies );
-	free( w->shapes );
-	free( w->contacts );
-	free( w->joints );
-	free( w->pending );
-	free( w->scratch );
-	free( w->beginEvents );
-	free( w->endEvents );
+	b2g_free( w->bodies );
+	b2g_free( w->shapes );
+	b2g_free( w->contacts );
+	b2g_free( w->joints );
+	b2g_free( w->pending );
+	b2g_free( w->scratch );
+	b2g_free( w->beginEvents );
+	b2g_free( w->endEvents );
 	void* pinned[] = { w->hState, w->hXf, w->hCenters, w->hPrev, w->hMass, w->hForce, w->hExtent, w->hInfo, w->hGeo, w->hAabb, w->hFat, w->hJoints };
 	for ( size_t i = 0; i < sizeof( pinned ) / sizeof( pinned[0] ); ++i )
 		if ( pinned[i] )
@@ -455,7 +496,9 @@ b2Counters b2World_GetCounters( b2WorldId id )
 }
 
 /* ------------------------------------------------------------ bodies */
-#define GROW_RECORDS( ptr, cap, need, T )                                                                                        \
+/* Grows a record array to `need` entries (new entries free); ok becomes false, and
+ * the array stays as it was, when memory ran out. */
+#define GROW_RECORDS( ptr, cap, need, T, ok )                                                                                    \
 	do                                                                                                                           \
 	{                                                                                                                            \
 		if ( ( need ) > ( cap ) )                                                                                                \
@@ -463,11 +506,17 @@ b2Counters b2World_GetCounters( b2WorldId id )
 			int nc = ( cap ) < 16 ? 16 : ( cap );                                                                                \
 			while ( nc < ( need ) )                                                                                              \
 				nc *= 2;                                                                                                         \
-			ptr = (T*)realloc( ptr, sizeof( T ) * (size_t)nc );                                                                  \
-			memset( ptr + ( cap ), 0, sizeof( T ) * (size_t)( nc - ( cap ) ) );                                                  \
-			for ( int _i = ( cap ); _i < nc; ++_i )                                                                              \
-				ptr[_i].id = B2G_NULL;                                                                                           \
-			cap = nc;                                                                                                            \
+			T* _p = (T*)b2g_realloc( ptr, sizeof( T ) * (size_t)nc );                                                            \
+			if ( _p == NULL )                                                                                                    \
+				ok = false;                                                                                                      \
+			else                                                                                                                 \
+			{                                                                                                                    \
+				ptr = _p;                                                                                                        \
+				memset( ptr + ( cap ), 0, sizeof( T ) * (size_t)( nc - ( cap ) ) );                                              \
+				for ( int _i = ( cap ); _i < nc; ++_i )                                                                          \
+					ptr[_i].id = B2G_NULL;                                                                                       \
+				cap = nc;                                                                                                        \
+			}                                                                                                                    \
 		}                                                                                                                        \
 	}                                                                                                                            \
 	while ( 0 )
@@ -477,13 +526,21 @@ static gWorld* body_world( b2BodyId id ) { return s_worlds[id.world0]; }
 
 b2BodyId b2CreateBody( b2WorldId worldId, const b2BodyDef* def )
 {
+	if ( b2World_IsValid( worldId ) == false )
+		return b2_nullBodyId;
 	gWorld* w = gworld_get( worldId );
 	if ( w->locked )
 		return b2_nullBodyId;
 	gworld_ensure_mirror( w );
 	int id = gid_alloc( &w->bodyIds );
-	GROW_RECORDS( w->bodies, w->bodyCap, id + 1, gBody );
-	gworld_reserve_mirrors( w );
+	bool ok = true;
+	GROW_RECORDS( w->bodies, w->bodyCap, id + 1, gBody, ok );
+	if ( ok == false || gworld_reserve_mirrors( w ) == false )
+	{
+		gid_free( &w->bodyIds, id );
+		w->status = w->status ? w->status : B2_STATUS_OUT_OF_HOST_MEMORY;
+		return b2_nullBodyId;
+	}
 	gBody* b = w->bodies + id;
 	uint16_t rev = b->revision;
 	memset( b, 0, sizeof( *b ) );
@@ -668,10 +725,10 @@ int b2Body_GetContactData( b2BodyId id, b2ContactData* out, int capacity )
 	gWorld* w = body_world( id );
 	gBody* b = get_body( id );
 	int nc = w->contactIds.next;
-	b2gManifold* ms = (b2gManifold*)malloc( sizeof( b2gManifold ) * (size_t)( nc > 0 ? nc : 1 ) );
-	if ( nc > 0 && b2gd_download_manifolds( &w->dev, ms, NULL, nc ) != 0 )
+	b2gManifold* ms = (b2gManifold*)b2g_alloc( sizeof( b2gManifold ) * (size_t)( nc > 0 ? nc : 1 ) );
+	if ( ms == NULL || ( nc > 0 && b2gd_download_manifolds( &w->dev, ms, NULL, nc ) != 0 ) )
 	{
-		free( ms );
+		b2g_free( ms );
 		return 0;
 	}
 	int n = 0;
@@ -705,7 +762,7 @@ int b2Body_GetContactData( b2BodyId id, b2ContactData* out, int capacity )
 		}
 		key = c->edges[key & 1].nextKey;
 	}
-	free( ms );
+	b2g_free( ms );
 	return n;
 }
 
@@ -809,14 +866,23 @@ void gbuffer_move( gWorld* w, int proxyKey )
 
 static b2ShapeId create_shape( b2BodyId bodyId, const b2ShapeDef* def, b2ShapeType type, const b2gShapeGeo* geo )
 {
+	/* an invalid body (a null id from a failed creation included) gets no shape */
+	if ( b2Body_IsValid( bodyId ) == false )
+		return b2_nullShapeId;
 	gWorld* w = body_world( bodyId );
 	if ( w->locked )
 		return b2_nullShapeId;
 	gworld_ensure_mirror( w );
 	gworld_ensure_shape_mirror( w );
 	int id = gid_alloc( &w->shapeIds );
-	GROW_RECORDS( w->shapes, w->shapeCap, id + 1, gShape );
-	gworld_reserve_mirrors( w );
+	bool ok = true;
+	GROW_RECORDS( w->shapes, w->shapeCap, id + 1, gShape, ok );
+	if ( ok == false || gworld_reserve_mirrors( w ) == false )
+	{
+		gid_free( &w->shapeIds, id );
+		w->status = w->status ? w->status : B2_STATUS_OUT_OF_HOST_MEMORY;
+		return b2_nullShapeId;
+	}
 	gBody* body = get_body( bodyId );
 	gShape* s = w->shapes + id;
 	uint16_t rev = s->revision;
@@ -1040,6 +1106,8 @@ int gassign_joint_color( gWorld* w, int bodyIdA, int bodyIdB, bool staticA, bool
 
 b2JointId b2CreateRevoluteJoint( b2WorldId worldId, const b2RevoluteJointDef* def )
 {
+	if ( b2World_IsValid( worldId ) == false || b2Body_IsValid( def->bodyIdA ) == false || b2Body_IsValid( def->bodyIdB ) == false )
+		return b2_nullJointId;
 	gWorld* w = gworld_get( worldId );
 	if ( w->locked )
 		return b2_nullJointId;
@@ -1047,8 +1115,14 @@ b2JointId b2CreateRevoluteJoint( b2WorldId worldId, const b2RevoluteJointDef* de
 	gBody* a = get_body( def->bodyIdA );
 	gBody* b = get_body( def->bodyIdB );
 	int id = gid_alloc( &w->jointIds );
-	GROW_RECORDS( w->joints, w->jointCap, id + 1, gJoint );
-	gworld_reserve_mirrors( w );
+	bool ok = true;
+	GROW_RECORDS( w->joints, w->jointCap, id + 1, gJoint, ok );
+	if ( ok == false || gworld_reserve_mirrors( w ) == false )
+	{
+		gid_free( &w->jointIds, id );
+		w->status = w->status ? w->status : B2_STATUS_OUT_OF_HOST_MEMORY;
+		return b2_nullJointId;
+	}
 	gJoint* j = w->joints + id;
 	uint16_t rev = j->revision;
 	memset( j, 0, sizeof( *j ) );
@@ -1262,10 +1336,10 @@ int b2World_InspectContacts( b2WorldId worldId, b2InspectContact* out, int capac
 		{
 			if ( ms == NULL )
 			{
-				ms = (b2gManifold*)malloc( sizeof( b2gManifold ) * (size_t)nc );
-				if ( b2gd_download_manifolds( &w->dev, ms, NULL, nc ) != 0 )
+				ms = (b2gManifold*)b2g_alloc( sizeof( b2gManifold ) * (size_t)nc );
+				if ( ms == NULL || b2gd_download_manifolds( &w->dev, ms, NULL, nc ) != 0 )
 				{
-					free( ms );
+					b2g_free( ms );
 					return 0;
 				}
 			}
@@ -1304,7 +1378,7 @@ int b2World_InspectContacts( b2WorldId worldId, b2InspectContact* out, int capac
 		}
 		n += 1;
 	}
-	free( ms );
+	b2g_free( ms );
 	return n;
 }
 

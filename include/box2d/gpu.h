@@ -14,8 +14,13 @@
 extern "C" {
 #endif
 
-/* Device status of a world: 0 when healthy, otherwise the CUDA error code of the first
- * failure.  A failed world stops stepping; the process is never aborted. */
+/* Status of a world: 0 when healthy, otherwise the first failure: a CUDA error code
+ * (positive), B2_STATUS_OUT_OF_HOST_MEMORY when the host allocator (b2SetAllocator, or
+ * aligned_alloc by default) refused a request during a call on the world, or -1 for a
+ * failed launch.  A failed world stops stepping; the process is never aborted.  Host
+ * memory failures are counted process-wide, so a world worked on while another thread's
+ * request failed is marked failed too. */
+#define B2_STATUS_OUT_OF_HOST_MEMORY ( -2 )
 B2_API int b2World_GetStatus( b2WorldId worldId );
 
 /* Number of time-of-impact events since the world was created: fast bodies (and
@@ -164,16 +169,21 @@ B2_API int b2SolveContacts( const b2ContactSolveDesc* desc );
 
 /* b2SolveContacts that allocates nothing; no counterpart in the reference API.  Its
  * constraint rows live in one fixed device array per device, compiled into the library:
- * B2_SOLVE_NOALLOC_MAX_CONTACTS rows of 144 bytes (2.25 MiB).  Same descriptor, same
- * results and return codes as b2SolveContacts, plus B2_SOLVE_NOALLOC_TOO_LARGE (nothing
- * launched) when contactCount exceeds the maximum.
+ * B2_SOLVE_NOALLOC_MAX_CONTACTS rows of 144 bytes (2.25 MiB).  Same descriptor and
+ * results as b2SolveContacts, and its return codes but for the allocation failures it
+ * cannot have, plus (nothing launched in either case):
+ *   B2_SOLVE_NOALLOC_TOO_LARGE     contactCount exceeds B2_SOLVE_NOALLOC_MAX_CONTACTS;
+ *   B2_SOLVE_NOALLOC_DEVICE_LIMIT  the current device's ordinal is 64 or more (the
+ *                                  address cache holds 64 devices).
  * - The first call on each device (with that device current) looks up the array's
- *   address; make it before any stream capture starts.
+ *   address, and again after the device's context was replaced (cudaDeviceReset); make
+ *   such calls before any stream capture starts.
  * - Nothing in the array has to start at zero: every row is written before it is read.
  * - Calls that overlap on one device share the array and race: order them (one stream,
  *   or events between streams, and one host thread at a time). */
 #define B2_SOLVE_NOALLOC_MAX_CONTACTS 16384
 #define B2_SOLVE_NOALLOC_TOO_LARGE ( -2 )
+#define B2_SOLVE_NOALLOC_DEVICE_LIMIT ( -3 )
 
 B2_API int b2SolveContactsNoAlloc( const b2ContactSolveDesc* desc );
 

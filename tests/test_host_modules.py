@@ -28,7 +28,8 @@ def test_host_tree_matches_oracle_tree(tmp_path):
     flags = ["-std=gnu17", "-O2", "-ffp-contract=off", "-I", inc]
     objs = []
     for name, extra, files in (
-            ("product", ["-I", src], [os.path.join(REPO, "tests", "c", "tree_product.c"), os.path.join(src, "tree.c")]),
+            ("product", ["-I", src, "-I", os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "include")],
+             [os.path.join(REPO, "tests", "c", "tree_product.c"), os.path.join(src, "tree.c"), os.path.join(src, "util.c")]),
             ("oracle", ["-I", os.path.join(REPO, "oracle")],
              [os.path.join(REPO, "tests", "c", "tree_oracle.c"), os.path.join(REPO, "oracle", "b2o_tree.c")])):
         for f in files:

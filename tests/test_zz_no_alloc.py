@@ -77,3 +77,49 @@ def test_no_alloc_rejects_oversized_set(gpu):
     d.subStepCount = SUBSTEPS
     assert gpu.lib.b2SolveContactsNoAlloc(C.byref(d)) == TOO_LARGE
     torch.cuda.synchronize()
+
+
+def _default_pool_used_high(reset):
+    """High-water mark of the current device's default memory pool (the pool that
+    stream-ordered allocations come from), read through the CUDA runtime the process
+    has loaded; reset to the current use first when `reset`."""
+    lib = None
+    with open("/proc/self/maps") as f:
+        for line in f:
+            if "libcudart.so" in line:
+                lib = line.split()[-1]
+                break
+    if lib is None:
+        pytest.skip("no shared CUDA runtime loaded in this process")
+    rt = C.CDLL(lib)
+    pool = C.c_void_p()
+    dev = C.c_int()
+    assert rt.cudaGetDevice(C.byref(dev)) == 0
+    assert rt.cudaDeviceGetDefaultMemPool(C.byref(pool), dev) == 0
+    used_high = 0x8  # cudaMemPoolAttrUsedMemHigh
+    if reset:
+        zero = C.c_uint64(0)
+        assert rt.cudaMemPoolSetAttribute(pool, used_high, C.byref(zero)) == 0
+    value = C.c_uint64()
+    assert rt.cudaMemPoolGetAttribute(pool, used_high, C.byref(value)) == 0
+    return value.value
+
+
+@pytest.mark.gpu
+def test_no_alloc_takes_no_device_memory(gpu, oracle):
+    """The property the entry point exists for: across a b2SolveContactsNoAlloc call the
+    default pool's high-water mark stays at the use it was reset to, while
+    b2SolveContacts on the same inputs raises it (its rows come from that pool)."""
+    torch = pytest.importorskip("torch")
+    _bind(gpu.lib)
+    cap = _capture(oracle, oracle.pyramid(20), 40)
+    _run(torch, gpu.lib.b2SolveContactsNoAlloc, cap)  # first call on the device: set-up
+    d, t = make_desc(torch, cap, "cuda:0")
+    torch.cuda.synchronize()
+    base = _default_pool_used_high(reset=True)  # the pool's use now (live worlds' arenas)
+    assert gpu.lib.b2SolveContactsNoAlloc(C.byref(d)) == 0
+    torch.cuda.synchronize()
+    assert _default_pool_used_high(reset=False) == base
+    assert gpu.lib.b2SolveContacts(C.byref(d)) == 0
+    torch.cuda.synchronize()
+    assert _default_pool_used_high(reset=False) > base
