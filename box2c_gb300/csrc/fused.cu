@@ -10,13 +10,19 @@
  * latency; a barrier inside one resident cluster costs a small fraction of that.
  *
  * Layout (dynamic shared memory of every CTA, rank r of CL):
- *   bodies  body id b lives in CTA b % CL at slot b / CL: two state float4 (v, w, tag |
- *           dp, dq), the per-step velocity terms (float4 + float), and the CTA's list
- *           of awake slots.  Rows reach a body in another CTA through distributed
+ *   bodies  body ids are cut into CL contiguous blocks of bodySlots: body b lives in CTA
+ *           b / bodySlots at slot b % bodySlots (the owner is found by a multiply-high
+ *           with a host-computed reciprocal): two state float4 (v, w, tag | dp, dq), the
+ *           per-step velocity terms (float4 + float), an awake flag, and the CTA's list
+ *           of awake slots.  Rows reach a body of another CTA through distributed
  *           shared memory.
- *   rows    row i of colour c lives in CTA i % CL at local index base[c] + i / CL, as
- *           nine float4 arrays (structure of arrays, conflict-free).  The overflow
- *           colour's rows all live in CTA 0 and thread 0 of CTA 0 solves them serially.
+ *   rows    the host groups each colour's rows by the CTA owning their first
+ *           non-static body (rows of one colour share no body, so the order within a
+ *           colour changes no result); CTA o holds rows [split[c][o], split[c][o+1]) of
+ *           colour c from local index ctaBase[c][o], as nine float4 arrays (structure of
+ *           arrays, conflict-free).  Most body accesses of a row are then local.  The
+ *           overflow colour's rows all live in CTA 0; thread 0 of CTA 0 solves them
+ *           serially on CTA-local copies of their bodies.
  *   joints  stay in global memory; joint i of colour c is always handled by the same
  *           thread (CTA i % CL), so only that thread reads and writes it.
  *

@@ -60,6 +60,8 @@ typedef struct gIdPool
 
 int gid_alloc( gIdPool* p );
 void gid_free( gIdPool* p, int id );
+/* Returns an id a failed creation took: the pool is as before the gid_alloc. */
+void gid_unalloc( gIdPool* p, int id );
 int gid_count( const gIdPool* p );
 
 typedef struct gBits

@@ -135,7 +135,7 @@ void gcontact_create( gWorld* w, gShape* shapeA, gShape* shapeB )
 		gContact* p = (gContact*)b2g_realloc( w->contacts, sizeof( gContact ) * (size_t)nc );
 		if ( p == NULL )
 		{
-			gid_free( &w->contactIds, id );
+			gid_unalloc( &w->contactIds, id );
 			return;
 		}
 		w->contacts = p;
@@ -833,6 +833,14 @@ static void build_solve_lists( gWorld* w, b2gSolvePlan* plan )
 		return;
 	}
 	memset( plan, 0, sizeof( *plan ) );
+	int rows = 0, joints = 0;
+	for ( int c = 0; c < B2G_COLORS; ++c )
+	{
+		rows += w->colors[c].contacts.count;
+		joints += w->colors[c].joints.count;
+	}
+	if ( gia_reserve( &w->solveList, rows ) == false || gia_reserve( &w->jointList, joints ) == false )
+		return; /* out of memory: counted, and the caller fails the world before the plan is used */
 	plan->bodyBlock = block;
 	w->solveList.count = 0;
 	w->jointList.count = 0;

@@ -113,6 +113,9 @@ void gia_push( gIntArray* a, int v )
 
 int gia_remove_swap( gIntArray* a, int index )
 {
+	/* an index an out-of-memory push never stored is ignored */
+	if ( index < 0 || index >= a->count )
+		return -1;
 	int last = a->count - 1;
 	if ( index == last )
 	{
@@ -237,6 +240,14 @@ int gid_alloc( gIdPool* p )
 		return p->freeIds.data[p->freeIds.count];
 	}
 	return p->next++;
+}
+
+void gid_unalloc( gIdPool* p, int id )
+{
+	if ( id == p->next - 1 )
+		p->next -= 1;
+	else
+		gia_push( &p->freeIds, id );
 }
 
 void gid_free( gIdPool* p, int id )

@@ -537,7 +537,7 @@ b2BodyId b2CreateBody( b2WorldId worldId, const b2BodyDef* def )
 	GROW_RECORDS( w->bodies, w->bodyCap, id + 1, gBody, ok );
 	if ( ok == false || gworld_reserve_mirrors( w ) == false )
 	{
-		gid_free( &w->bodyIds, id );
+		gid_unalloc( &w->bodyIds, id );
 		w->status = w->status ? w->status : B2_STATUS_OUT_OF_HOST_MEMORY;
 		return b2_nullBodyId;
 	}
@@ -879,7 +879,7 @@ static b2ShapeId create_shape( b2BodyId bodyId, const b2ShapeDef* def, b2ShapeTy
 	GROW_RECORDS( w->shapes, w->shapeCap, id + 1, gShape, ok );
 	if ( ok == false || gworld_reserve_mirrors( w ) == false )
 	{
-		gid_free( &w->shapeIds, id );
+		gid_unalloc( &w->shapeIds, id );
 		w->status = w->status ? w->status : B2_STATUS_OUT_OF_HOST_MEMORY;
 		return b2_nullShapeId;
 	}
@@ -936,6 +936,14 @@ static b2ShapeId create_shape( b2BodyId bodyId, const b2ShapeDef* def, b2ShapeTy
 	f4[3] = fat.hi.y;
 	int proxyType = (int)body->type;
 	int proxyId = gtree_create_proxy( w->trees + proxyType, fat, s->filter.categoryBits, id );
+	if ( proxyId == B2G_NULL )
+	{
+		/* the tree had no memory for the proxy: nothing links the shape yet */
+		s->id = B2G_NULL;
+		gid_unalloc( &w->shapeIds, id );
+		w->status = w->status ? w->status : B2_STATUS_OUT_OF_HOST_MEMORY;
+		return b2_nullShapeId;
+	}
 	s->proxyKey = ( proxyId << 2 ) | proxyType;
 	if ( proxyType != b2_staticBody || def->forceContactCreation )
 		gbuffer_move( w, s->proxyKey );
@@ -1119,7 +1127,7 @@ b2JointId b2CreateRevoluteJoint( b2WorldId worldId, const b2RevoluteJointDef* de
 	GROW_RECORDS( w->joints, w->jointCap, id + 1, gJoint, ok );
 	if ( ok == false || gworld_reserve_mirrors( w ) == false )
 	{
-		gid_free( &w->jointIds, id );
+		gid_unalloc( &w->jointIds, id );
 		w->status = w->status ? w->status : B2_STATUS_OUT_OF_HOST_MEMORY;
 		return b2_nullJointId;
 	}

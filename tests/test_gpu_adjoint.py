@@ -79,6 +79,8 @@ def _adjoint(gpu, heights, v0, mu, steps):
 
 
 def _compare(gpu, fd64, n, steps, seed=1238):
+    """Adjoint vs FP64 central differences on the worlds whose finite difference is
+    stable: eps 1e-5, 1e-6 and 1e-7 agree within STABLE relative."""
     heights, v0, mu = _scene(n, seed=seed)
     ga = _adjoint(gpu, heights, v0, mu, steps)
     stable, errs = 0, []
@@ -86,6 +88,9 @@ def _compare(gpu, fd64, n, steps, seed=1238):
         f6 = fd64(heights[w], v0[w], mu[w], steps, 1e-6)
         f5 = fd64(heights[w], v0[w], mu[w], steps, 1e-5)
         if np.linalg.norm(f5 - f6) > STABLE * np.linalg.norm(f6):
+            continue
+        f7 = fd64(heights[w], v0[w], mu[w], steps, 1e-7)
+        if np.linalg.norm(f7 - f6) > STABLE * np.linalg.norm(f6):
             continue
         stable += 1
         errs.append(np.linalg.norm(ga[w] - f6) / np.linalg.norm(f6))
@@ -102,9 +107,34 @@ def test_free_flight_gradient_is_exact(gpu, fd64):
 
 
 def test_gradient_matches_fp64_derivative_30_steps(gpu, fd64):
-    stable, errs = _compare(gpu, fd64, 6, 30)
-    assert stable >= 3, f"only {stable} of 6 worlds have a stable finite difference"
+    stable, errs = _compare(gpu, fd64, 8, 30)
+    assert stable >= 6, f"only {stable} of 8 worlds have a stable finite difference"
     assert max(errs) <= TOL, f"relative gradient errors {errs}"
+
+
+def test_gradient_error_distribution_at_specified_eps(gpu, fd64):
+    """The measurement the workload specifies, reported for all of 16 worlds (none
+    dropped): relative error against FP64 central differences at eps 1e-3 after 120
+    steps, and at eps 1e-6 with the stability of the finite difference.  Contacts make
+    the loss piecewise smooth with kinks denser than 1e-3 once boxes collide and tip, so
+    eps 1e-3 differences are secants across kinks; the assertion is on the worlds whose
+    finite difference is stable, where the adjoint is the derivative."""
+    heights, v0, mu = _scene(16)
+    ga = _adjoint(gpu, heights, v0, mu, 120)
+    rows = []
+    for w in range(16):
+        f3, f5, f6, f7 = (fd64(heights[w], v0[w], mu[w], 120, e) for e in (1e-3, 1e-5, 1e-6, 1e-7))
+        n6 = np.linalg.norm(f6)
+        stable = np.linalg.norm(f5 - f6) <= STABLE * n6 and np.linalg.norm(f7 - f6) <= STABLE * n6
+        rows.append((np.linalg.norm(ga[w] - f3) / np.linalg.norm(f3), np.linalg.norm(ga[w] - f6) / n6, stable))
+    e3 = np.array([r[0] for r in rows])
+    e6 = np.array([r[1] for r in rows])
+    st = np.array([r[2] for r in rows])
+    print(f"eps 1e-3: median {np.median(e3):.3g} max {e3.max():.3g}; eps 1e-6: median {np.median(e6):.3g}; "
+          f"stable {st.sum()}/16, stable errors {np.round(e6[st], 6)}; per world eps 1e-3 {np.round(e3, 4)}")
+    assert np.all(np.isfinite(e3)) and np.all(np.isfinite(e6))
+    if st.any():
+        assert e6[st].max() <= TOL, e6[st]
 
 
 def test_gradient_matches_fp64_derivative_120_steps(gpu, fd64):
