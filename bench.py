@@ -162,6 +162,8 @@ def oracle_backend(threads):
 
 
 SETTLE_STEPS = 100  # the large pyramid is at rest from about this step on
+HOST_PHASES = ("hostPairQuery", "hostPairRules", "hostContactCreate", "hostEvents", "hostSolveLists", "hostTreeRebuild",
+               "hostRecords", "hostContinuous")
 CPU_SAMPLE_STEPS = 40  # bounded sample of the CPU baseline leg of the GPU arm
 
 
@@ -527,7 +529,8 @@ def run_gpu(args):
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
     def device_window(count):
-        rec = {"step": [], "solve": [], "collide": [], "finalize": [], "launches": [], "fused": 0, "host": []}
+        rec = {"step": [], "solve": [], "collide": [], "finalize": [], "launches": [], "fused": 0, "host": [],
+               "phases": []}
         for _ in range(count):
             flush.fill_(1.0)
             torch.cuda.synchronize()
@@ -539,6 +542,7 @@ def run_gpu(args):
             rec["finalize"].append(t.finalize)
             rec["launches"].append(t.launches)
             rec["fused"] += t.fusedSolver
+            rec["phases"].append([getattr(t, f) for f in HOST_PHASES])
             p = L.b2World_GetProfile(w)
             rec["host"].append((p.step, p.pairs, p.collide, p.solve, p.broadphase))
         return rec
@@ -628,6 +632,9 @@ def run_gpu(args):
                       "finalize": round(float(np.mean(finalize_ms)), 4)},
         "host_ms": dict(zip(("step", "pairs", "collide_and_events", "solve_and_sync", "records"),
                             [round(float(x), 4) for x in np.mean(np.array(rec["host"]), 0)])),
+        "host_phase_ms": {"timed": dict(zip(HOST_PHASES, [round(float(x), 4) for x in np.mean(np.array(rec["phases"]), 0)])),
+                          "settled": dict(zip(HOST_PHASES,
+                                              [round(float(x), 4) for x in np.mean(np.array(settled["phases"]), 0)]))},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": SOLVER_DRAM_BYTES,
                      "traffic_source": "ncu dram__bytes_read+write of k_fused_stage + k_solve_fused, one step "

@@ -317,7 +317,10 @@ class DeviceTimes(C.Structure):
     """include/box2d/gpu.h b2DeviceTimes."""
     _fields_ = [("step", C.c_float), ("collide", C.c_float), ("solve", C.c_float), ("finalize", C.c_float),
                 ("eventCount", C.c_int), ("recordCount", C.c_int), ("launches", C.c_int), ("fusedSolver", C.c_int),
-                ("hostToDeviceBytes", C.c_longlong), ("deviceToHostBytes", C.c_longlong)]
+                ("hostToDeviceBytes", C.c_longlong), ("deviceToHostBytes", C.c_longlong),
+                ("hostPairQuery", C.c_float), ("hostPairRules", C.c_float), ("hostContactCreate", C.c_float),
+                ("hostEvents", C.c_float), ("hostSolveLists", C.c_float), ("hostTreeRebuild", C.c_float),
+                ("hostRecords", C.c_float), ("hostContinuous", C.c_float)]
 
 
 def bind_gpu_api(lib: C.CDLL) -> None:

@@ -256,6 +256,10 @@ typedef struct gWorld
 	int pendingCount, pendingCap;
 	int* scratch;
 	int scratchCap;
+	b2gRecord* recordSort; /* finalisation records in awake order */
+	int recordSortCap;
+	int* recordBucket; /* per awake index: first sorted record */
+	int recordBucketCap;
 	gIntArray solveList;
 	gIntArray jointList;
 	b2gSolvePlan solvePlan; /* plan of the current solve lists */
@@ -277,6 +281,9 @@ typedef struct gWorld
 	int endCount, endCap;
 
 	b2Profile profile;
+	/* host phases of the last step in ms (b2DeviceTimes order): pair query, pair rules,
+	 * contact creation, events, solve lists, tree rebuild, records, continuous */
+	float hostMs[8];
 	int status; /* last CUDA error or 0 */
 	int toiEvents;	   /* time-of-impact events since the world was created */
 	int tapeToiEvents; /* time-of-impact events while the tape records */

@@ -475,6 +475,7 @@ static int update_pairs( gWorld* w )
 	c.w = w;
 	c.cand = NULL;
 	c.counts = NULL;
+	double t0 = b2g_now_ms();
 	if ( moveCount >= DEVICE_QUERY_MIN_MOVES )
 	{
 		const b2gTreeNode* nodes[3];
@@ -489,11 +490,13 @@ static int update_pairs( gWorld* w )
 		if ( e )
 			return e;
 	}
+	double t1 = b2g_now_ms();
 	c.lists = (gPairList*)b2g_calloc( (size_t)moveCount, sizeof( gPairList ) );
 	if ( c.lists == NULL )
 		return -1;
 	if ( gpool_try_for( moveCount, PAIR_GRAIN, query_moved, &c ) == false )
 		query_moved( 0, moveCount, &c );
+	double t2 = b2g_now_ms();
 	for ( int i = 0; i < moveCount; ++i )
 	{
 		gPairList* l = c.lists + i;
@@ -505,6 +508,10 @@ static int update_pairs( gWorld* w )
 	b2g_free( c.lists );
 	w->moveArray.count = 0;
 	gset_clear( &w->moveSet );
+	double t3 = b2g_now_ms();
+	w->hostMs[0] = (float)( t1 - t0 );
+	w->hostMs[1] = (float)( t2 - t1 );
+	w->hostMs[2] = (float)( t3 - t2 );
 	return 0;
 }
 
@@ -764,10 +771,51 @@ static void continuous_pass( gWorld* w, b2gRecord* rec, int count, bool bullets 
 	}
 }
 
-static void process_records( gWorld* w, int count )
+/* Records sorted by awake index with a counting sort.  A body's records come from one
+ * device thread in slot order, so the sort, which is stable, leaves them in slot order.
+ * Falls back to a comparison sort in place when memory for the buckets runs out. */
+static b2gRecord* sort_records( gWorld* w, int count )
 {
 	b2gRecord* rec = w->io.records;
-	qsort( rec, (size_t)count, sizeof( b2gRecord ), cmp_record );
+	int n = w->awake.count + 1;
+	if ( count > w->recordSortCap )
+	{
+		b2gRecord* p = (b2gRecord*)b2g_realloc( w->recordSort, sizeof( b2gRecord ) * (size_t)count );
+		if ( p != NULL )
+		{
+			w->recordSort = p;
+			w->recordSortCap = count;
+		}
+	}
+	if ( n > w->recordBucketCap )
+	{
+		int* p = (int*)b2g_realloc( w->recordBucket, sizeof( int ) * (size_t)n );
+		if ( p != NULL )
+		{
+			w->recordBucket = p;
+			w->recordBucketCap = n;
+		}
+	}
+	if ( count > w->recordSortCap || n > w->recordBucketCap )
+	{
+		qsort( rec, (size_t)count, sizeof( b2gRecord ), cmp_record );
+		return rec;
+	}
+	int* first = w->recordBucket;
+	memset( first, 0, sizeof( int ) * (size_t)n );
+	for ( int i = 0; i < count; ++i )
+		first[rec[i].awakeIndex + 1] += 1;
+	for ( int k = 1; k < n; ++k )
+		first[k] += first[k - 1];
+	b2gRecord* out = w->recordSort;
+	for ( int i = 0; i < count; ++i )
+		out[first[rec[i].awakeIndex]++] = rec[i];
+	return out;
+}
+
+static void process_records( gWorld* w, int count )
+{
+	b2gRecord* rec = sort_records( w, count );
 	/* proxy enlargement and move buffer in awake order (reference src/solver.c:1741-1797) */
 	for ( int i = 0; i < count; ++i )
 	{
@@ -784,8 +832,10 @@ static void process_records( gWorld* w, int count )
 			gbuffer_move( w, s->proxyKey );
 		}
 	}
+	double t0 = b2g_now_ms();
 	continuous_pass( w, rec, count, false );
 	continuous_pass( w, rec, count, true );
+	w->hostMs[7] = (float)( b2g_now_ms() - t0 );
 }
 
 /* ------------------------------------------------------------ step */
@@ -928,8 +978,10 @@ int gstep_begin( gWorld* w )
 /* Runs while the device narrowphase is in flight (reference src/world.c:420). */
 void gstep_rebuild_trees( gWorld* w )
 {
+	double t0 = b2g_now_ms();
 	gtree_rebuild( w->trees + b2_dynamicBody );
 	gtree_rebuild( w->trees + b2_kinematicBody );
+	w->hostMs[5] = (float)( b2g_now_ms() - t0 );
 }
 
 /* Host work between the narrowphase and the solver: events in contact-id order, step
@@ -964,8 +1016,10 @@ int gstep_after_collide( gWorld* w, float dt, int subSteps, b2gStepConst* sc, b2
 	w->lastEventCount = eventCount;
 	/* events reach the host through mapped memory */
 	w->dev.d2hBytes += 4 * (long long)( eventCount < w->dev.eventCap ? eventCount : w->dev.eventCap );
+	double te = b2g_now_ms();
 	process_events( w, eventCount < w->dev.eventCap ? eventCount : w->dev.eventCap );
 	double t2 = b2g_now_ms();
+	w->hostMs[3] = (float)( t2 - te );
 	w->profile.collide = (float)( t2 - w->stepStart );
 	w->stepStart = t2;
 
@@ -981,6 +1035,7 @@ int gstep_after_collide( gWorld* w, float dt, int subSteps, b2gStepConst* sc, b2
 		return 0;
 	}
 
+	double tl = b2g_now_ms();
 	build_solve_lists( w, plan );
 	if ( gworld_out_of_memory( w, failures ) )
 		return 0;
@@ -996,6 +1051,7 @@ int gstep_after_collide( gWorld* w, float dt, int subSteps, b2gStepConst* sc, b2
 		}
 		w->solveUploaded = true;
 	}
+	w->hostMs[4] = (float)( b2g_now_ms() - tl );
 	if ( w->tape )
 		gtape_record( w, plan, sc, 1 );
 	return 1;
@@ -1009,11 +1065,14 @@ void gstep_finish( gWorld* w )
 	w->profile.solve = (float)( t3 - w->stepStart );
 	int recordCount = w->io.counters[1];
 	w->lastRecordCount = recordCount;
+	double tr = b2g_now_ms();
 	/* records reach the host through mapped memory: 48 bytes, 80 for fast shapes */
 	for ( int i = 0; i < ( recordCount < w->dev.recordCap ? recordCount : w->dev.recordCap ); ++i )
 		w->dev.d2hBytes += ( w->io.records[i].flags & B2G_R_FAST ) ? 80 : 48;
 	process_records( w, recordCount < w->dev.recordCap ? recordCount : w->dev.recordCap );
 	w->profile.broadphase = (float)( b2g_now_ms() - t3 );
+	w->profile.continuous = w->hostMs[7];
+	w->hostMs[6] = (float)( b2g_now_ms() - tr ) - w->hostMs[7];
 }
 
 /* Whether the solver stage can be launched behind the narrowphase before its events are
@@ -1046,7 +1105,17 @@ void gstep_run( gWorld* w, float dt, int subSteps )
 		plan.bodyIdCount = w->bodyIds.next;
 		speculated = b2gd_solve_speculative( &w->dev, &w->io, &plan, &sc );
 	}
-	gstep_rebuild_trees( w );
+	/* The partial rebuild of the trees (reference src/world.c:420, finished before the
+	 * proxies are enlarged, src/solver.c:1725) runs on the host while the device works:
+	 * beside the whole launch sequence when the solver went out speculatively, else
+	 * beside the solver stage, which takes longer than the narrowphase.  Nothing in
+	 * between reads the trees. */
+	bool rebuilt = false;
+	if ( speculated > 0 )
+	{
+		gstep_rebuild_trees( w );
+		rebuilt = true;
+	}
 	e |= b2gd_sync( &w->dev );
 	if ( e || speculated < 0 )
 	{
@@ -1061,8 +1130,14 @@ void gstep_run( gWorld* w, float dt, int subSteps )
 		return;
 	}
 	if ( gstep_after_collide( w, dt, subSteps, &sc, &plan ) == 0 )
+	{
+		if ( rebuilt == false )
+			gstep_rebuild_trees( w );
 		return;
+	}
 	e = b2gd_solve( &w->dev, &w->io, &plan, &sc );
+	if ( rebuilt == false )
+		gstep_rebuild_trees( w );
 	e |= b2gd_sync( &w->dev );
 	if ( e )
 	{
@@ -1089,6 +1164,7 @@ void b2World_Step( b2WorldId worldId, float timeStep, int subStepCount )
 	w->locked = true;
 	w->dev.h2dBytes = 0;
 	w->dev.d2hBytes = 0;
+	memset( w->hostMs, 0, sizeof( w->hostMs ) );
 	b2gd_mark( &w->dev, 0 );
 	gworld_flush( w );
 	if ( w->status == 0 )

@@ -420,6 +420,8 @@ void b2DestroyWorld( b2WorldId worldId )
 	b2g_free( w->joints );
 	b2g_free( w->pending );
 	b2g_free( w->scratch );
+	b2g_free( w->recordSort );
+	b2g_free( w->recordBucket );
 	b2g_free( w->beginEvents );
 	b2g_free( w->endEvents );
 	void* pinned[] = { w->hState, w->hXf, w->hCenters, w->hPrev, w->hMass, w->hForce, w->hExtent, w->hInfo, w->hGeo, w->hAabb, w->hFat, w->hJoints };
@@ -1413,6 +1415,14 @@ b2DeviceTimes b2World_GetDeviceTimes( b2WorldId worldId )
 	t.fusedSolver = w->dev.fusedUsed;
 	t.hostToDeviceBytes = w->dev.h2dBytes;
 	t.deviceToHostBytes = w->dev.d2hBytes;
+	t.hostPairQuery = w->hostMs[0];
+	t.hostPairRules = w->hostMs[1];
+	t.hostContactCreate = w->hostMs[2];
+	t.hostEvents = w->hostMs[3];
+	t.hostSolveLists = w->hostMs[4];
+	t.hostTreeRebuild = w->hostMs[5];
+	t.hostRecords = w->hostMs[6];
+	t.hostContinuous = w->hostMs[7];
 	return t;
 }
 

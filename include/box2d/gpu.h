@@ -46,6 +46,18 @@ typedef struct b2DeviceTimes
 	 * reads or writes of mapped host memory (events, records, pair candidates) */
 	long long hostToDeviceBytes;
 	long long deviceToHostBytes;
+	/* host phases of the last step (milliseconds): tree walks of the moved proxies on the
+	 * device with their round trip, pair rules, contact creation, narrowphase events
+	 * (colouring), solve lists (build and upload), partial tree rebuild, finalisation
+	 * records (proxy enlargement, move buffer) and continuous collision */
+	float hostPairQuery;
+	float hostPairRules;
+	float hostContactCreate;
+	float hostEvents;
+	float hostSolveLists;
+	float hostTreeRebuild;
+	float hostRecords;
+	float hostContinuous;
 } b2DeviceTimes;
 
 B2_API void b2World_EnableDeviceTiming( b2WorldId worldId, bool flag );
