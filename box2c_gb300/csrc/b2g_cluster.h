@@ -134,13 +134,13 @@ __device__ __forceinline__ void store_row_smem( const SmemRows& m, int k, int ci
 	m.imp1[k] = make_float4( r.ni[1], r.ti[1], r.maxNi[1], 0.0f );
 }
 
-/* One row phase on row k, whose data r has been loaded from shared memory already;
- * Bodies is ClusterBodies (states spread over the cluster) or SharedBodies (states of
- * one CTA, by body id). */
+/* One row phase on a row in shared memory; Bodies is ClusterBodies (states spread over
+ * the cluster) or SharedBodies (states of one CTA, by body id). */
 template <class Bodies>
-__device__ __forceinline__ void row_step_loaded( const SmemRows& m, const Bodies& B, int k, Row& r, int phase, bool scalar,
-												 const b2gStepConst& sc )
+__device__ __forceinline__ void row_step( const SmemRows& m, const Bodies& B, int k, int phase, bool scalar, const b2gStepConst& sc )
 {
+	Row r;
+	load_row_smem( m, k, sc, r );
 	bool delta = phase == F_SOLVE || phase == F_RELAX;
 	DevState a = delta ? B.load( r.ia ) : B.load_velocity( r.ia );
 	DevState b = delta ? B.load( r.ib ) : B.load_velocity( r.ib );
@@ -163,15 +163,6 @@ __device__ __forceinline__ void row_step_loaded( const SmemRows& m, const Bodies
 		m.imp0[k] = make_float4( r.ni[0], r.ti[0], r.maxNi[0], 0.0f );
 		m.imp1[k] = make_float4( r.ni[1], r.ti[1], r.maxNi[1], 0.0f );
 	}
-}
-
-/* One row phase on row k of shared memory. */
-template <class Bodies>
-__device__ __forceinline__ void row_step( const SmemRows& m, const Bodies& B, int k, int phase, bool scalar, const b2gStepConst& sc )
-{
-	Row r;
-	load_row_smem( m, k, sc, r );
-	row_step_loaded( m, B, k, r, phase, scalar, sc );
 }
 
 /* One joint phase with its bodies at B-indices ia and ib (-1 for a static body). */

@@ -150,13 +150,6 @@ __device__ __forceinline__ FusedSmem carve( float4* base, int BS, int RC )
 
 __device__ __forceinline__ int local_count( int n, int rank, int CL ) { return n > rank ? ( n - rank + CL - 1 ) / CL : 0; }
 
-/* The cluster barrier in its two halves, every thread of every CTA taking part in both
- * (.aligned: all threads of a warp execute it together).  Arriving releases this
- * thread's shared-memory writes to the cluster; waiting acquires the others'.  Work that
- * reads only this thread's own data can sit between the halves. */
-__device__ __forceinline__ void cluster_arrive() { asm volatile( "barrier.cluster.arrive.release.aligned;" ::: "memory" ); }
-__device__ __forceinline__ void cluster_wait() { asm volatile( "barrier.cluster.wait.acquire.aligned;" ::: "memory" ); }
-
 /* One stage over all colours: the overflow set first (serially, CTA 0 thread 0), then
  * each active colour with a cluster barrier after it. */
 template <int CL>
@@ -218,12 +211,6 @@ __device__ void run_stage( const b2gDevWorld& W, const FusedPlan& P, const Fused
 	}
 	if ( phase == F_WARM && sc.enableWarmStarting == 0 )
 		return;
-	/* A colour's rows are each handled by the same thread in every phase, so a thread
-	 * may load its first row of the next colour (row data only: indices, masses,
-	 * anchors, coefficients, its own impulses) between arriving at the colour's barrier
-	 * and waiting on it; body states are read after the wait. */
-	Row next;
-	bool haveNext = false;
 	for ( int a = 0; a < P.activeCount; ++a )
 	{
 		int c = P.active[a];
@@ -232,33 +219,11 @@ __device__ void run_stage( const b2gDevWorld& W, const FusedPlan& P, const Fused
 		int base = P.ctaBase[c][rank];
 		int nr = P.split[c][rank + 1] - P.split[c][rank];
 		int nj = phase == F_RESTITUTION ? 0 : local_count( js[c + 1] - js[c], rank, CL );
-		int j = threadIdx.x;
-		if ( haveNext )
-		{
-			row_step_loaded( m, B, base + j, next, phase, false, sc );
-			j += FUSED_THREADS;
-		}
-		for ( ; j < nr; j += FUSED_THREADS )
+		for ( int j = threadIdx.x; j < nr; j += FUSED_THREADS )
 			row_step( m, B, base + j, phase, false, sc );
-		for ( int k = threadIdx.x; k < nj; k += FUSED_THREADS )
-			joint_step( W, B, W.jointList[js[c] + rank + k * CL], phase, sc );
-		cluster_arrive();
-		/* the next colour this stage solves, and this thread's first row of it */
-		haveNext = false;
-		for ( int a2 = a + 1; a2 < P.activeCount; ++a2 )
-		{
-			int c2 = P.active[a2];
-			if ( phase == F_RESTITUTION && cs[c2 + 1] == cs[c2] )
-				continue;
-			int nr2 = P.split[c2][rank + 1] - P.split[c2][rank];
-			if ( (int)threadIdx.x < nr2 )
-			{
-				load_row_smem( m, P.ctaBase[c2][rank] + threadIdx.x, sc, next );
-				haveNext = true;
-			}
-			break;
-		}
-		cluster_wait();
+		for ( int j = threadIdx.x; j < nj; j += FUSED_THREADS )
+			joint_step( W, B, W.jointList[js[c] + rank + j * CL], phase, sc );
+		B.cl.sync();
 	}
 }
 
