@@ -95,14 +95,18 @@ int b2gd_sync( b2gDevWorld* w );
  * pushed before child2).  Candidates of proxy i are cand[2 * (B2G_QUERY_SLOTS * i + k)]
  * (leaf proxy key) and cand[... + 1] (shape id) for k < counts[i]; counts[i] is -1 when
  * the proxy needed more than B2G_QUERY_SLOTS slots or a deeper stack, and the host
- * queries that proxy itself.  Synchronises the world's stream; the result arrays are
- * host memory owned by the query and valid until the next call. */
+ * queries that proxy itself.  Candidates the pair rules reject for the proxy itself, the
+ * moved-pair rule or an existing pair (pairTable: the host pair set's table of pairCap
+ * slots, copied when pairVersion changes) are left out.  Synchronises the world's
+ * stream; the result arrays are host memory owned by the query and valid until the next
+ * call. */
 #define B2G_QUERY_SLOTS 32
 
 typedef struct b2gPairQuery b2gPairQuery;
 
 int b2gd_pair_query( b2gDevWorld* w, b2gPairQuery** query, const b2gTreeNode* const nodes[3], const int capacity[3], const int root[3],
-					 const int* keys, int count, const int** cand, const int** counts );
+					 const int* keys, int count, const unsigned long long* pairTable, int pairCap, unsigned pairVersion,
+					 const int** cand, const int** counts );
 void b2gd_pair_query_free( b2gPairQuery* query );
 
 /* ---------------------------------------------------------------- batched worlds */

@@ -250,6 +250,7 @@ typedef struct gWorld
 	gIntArray moveArray;
 	gSet moveSet;
 	gSet pairSet;
+	unsigned pairSetVersion; /* changes with every pair added or removed */
 
 	/* step staging */
 	b2gContactInit* pending;

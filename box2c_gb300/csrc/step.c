@@ -178,6 +178,7 @@ void gcontact_create( gWorld* w, gShape* shapeA, gShape* shapeB )
 	bodyB->contactCount += 1;
 
 	gset_add( &w->pairSet, PAIR_KEY( (uint64_t)shapeA->id, (uint64_t)shapeB->id ) );
+	w->pairSetVersion += 1;
 	gia_push( &w->nonTouching, id );
 
 	b2gContactInit* init = push_pending( w );
@@ -229,6 +230,7 @@ static void unlink_edge( gWorld* w, gContact* c, int e )
 void gcontact_destroy( gWorld* w, gContact* c )
 {
 	gset_remove( &w->pairSet, PAIR_KEY( (uint64_t)c->shapeIdA, (uint64_t)c->shapeIdB ) );
+	w->pairSetVersion += 1;
 	unlink_edge( w, c, 0 );
 	unlink_edge( w, c, 1 );
 	if ( c->colorIndex != B2G_NULL )
@@ -486,7 +488,9 @@ static int update_pairs( gWorld* w )
 			capacity[t] = w->trees[t].capacity;
 			root[t] = w->trees[t].root;
 		}
-		int e = b2gd_pair_query( &w->dev, &w->pairQuery, nodes, capacity, root, w->moveArray.data, moveCount, &c.cand, &c.counts );
+		int e = b2gd_pair_query( &w->dev, &w->pairQuery, nodes, capacity, root, w->moveArray.data, moveCount,
+								 (const unsigned long long*)w->pairSet.keys, w->pairSet.capacity, w->pairSetVersion, &c.cand,
+								 &c.counts );
 		if ( e )
 			return e;
 	}
