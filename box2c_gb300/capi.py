@@ -38,6 +38,26 @@ ShapeId = BodyId
 JointId = BodyId
 
 
+class ShapePairEvent(C.Structure):
+    """b2ContactBeginTouchEvent / b2ContactEndTouchEvent / b2Sensor*TouchEvent layout."""
+    _fields_ = [("shapeIdA", BodyId), ("shapeIdB", BodyId)]
+
+
+class ContactHitEvent(C.Structure):
+    _fields_ = [("shapeIdA", BodyId), ("shapeIdB", BodyId), ("point", Vec2), ("normal", Vec2), ("approachSpeed", C.c_float)]
+
+
+class ContactEvents(C.Structure):
+    _fields_ = [("beginEvents", C.POINTER(ShapePairEvent)), ("endEvents", C.POINTER(ShapePairEvent)),
+                ("hitEvents", C.POINTER(ContactHitEvent)), ("beginCount", C.c_int32), ("endCount", C.c_int32),
+                ("hitCount", C.c_int32)]
+
+
+class SensorEvents(C.Structure):
+    _fields_ = [("beginEvents", C.POINTER(ShapePairEvent)), ("endEvents", C.POINTER(ShapePairEvent)),
+                ("beginCount", C.c_int32), ("endCount", C.c_int32)]
+
+
 class Counters(C.Structure):
     _fields_ = [(n, C.c_int32) for n in (
         "staticBodyCount", "bodyCount", "shapeCount", "contactCount", "jointCount",
@@ -120,6 +140,10 @@ class Backend:
         for name, idt in (("b2Body_IsValid", BodyId), ("b2Shape_IsValid", ShapeId), ("b2Joint_IsValid", JointId)):
             getattr(L, name).argtypes = [idt]
             getattr(L, name).restype = C.c_bool
+        L.b2World_GetContactEvents.argtypes = [WorldId]
+        L.b2World_GetContactEvents.restype = ContactEvents
+        L.b2World_GetSensorEvents.argtypes = [WorldId]
+        L.b2World_GetSensorEvents.restype = SensorEvents
         L.b2Body_GetShapes.argtypes = [BodyId, C.c_void_p, C.c_int]
         L.b2Body_GetShapes.restype = C.c_int
         S.b2s_pyramid.argtypes = [C.c_int, C.c_float, C.c_uint64]
@@ -142,6 +166,8 @@ class Backend:
         S.b2s_joint_hub.restype = WorldId
         S.b2s_joint_chains.argtypes = [C.c_int, C.c_int, C.c_int, C.c_uint64]
         S.b2s_joint_chains.restype = WorldId
+        S.b2s_event_scene.argtypes = [C.c_int, C.c_uint64]
+        S.b2s_event_scene.restype = WorldId
         S.b2s_empty_world.argtypes = []
         S.b2s_empty_world.restype = WorldId
         S.b2s_add_body.argtypes = [WorldId, C.c_int]
@@ -201,6 +227,25 @@ class Backend:
     def joint_chains(self, chains: int = 8, links: int = 8, flags: int = 7, seed: int = 1242) -> WorldId:
         """flags: 1 joint limits, 2 joint springs, 4 motors."""
         return self._made(self.scenes.b2s_joint_chains(chains, links, flags, seed))
+
+    def event_scene(self, count: int = 40, seed: int = 1243) -> WorldId:
+        return self._made(self.scenes.b2s_event_scene(count, seed))
+
+    def events(self, world: WorldId):
+        """The last step's events as plain tuples: (begin, end, hit, sensorBegin, sensorEnd);
+        shape ids as (index1, revision), hit events with point, normal and speed bits."""
+        L = self.lib
+        ce = L.b2World_GetContactEvents(world)
+        se = L.b2World_GetSensorEvents(world)
+        sid = lambda s: (s.index1, s.revision)
+        begin = [(sid(ce.beginEvents[i].shapeIdA), sid(ce.beginEvents[i].shapeIdB)) for i in range(ce.beginCount)]
+        end = [(sid(ce.endEvents[i].shapeIdA), sid(ce.endEvents[i].shapeIdB)) for i in range(ce.endCount)]
+        f = lambda x: np.float32(x).view(np.uint32).item()
+        hit = [(sid(h.shapeIdA), sid(h.shapeIdB), f(h.point.x), f(h.point.y), f(h.normal.x), f(h.normal.y), f(h.approachSpeed))
+               for h in (ce.hitEvents[i] for i in range(ce.hitCount))]
+        sb = [(sid(se.beginEvents[i].shapeIdA), sid(se.beginEvents[i].shapeIdB)) for i in range(se.beginCount)]
+        sn = [(sid(se.endEvents[i].shapeIdA), sid(se.endEvents[i].shapeIdB)) for i in range(se.endCount)]
+        return begin, end, hit, sb, sn
 
     def destruction(self) -> WorldId:
         return self._made(self.scenes.b2s_destruction())

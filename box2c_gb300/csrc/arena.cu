@@ -122,6 +122,7 @@ extern "C" void b2gd_free( b2gDevWorld* w, b2gHostIO* io )
 	FREE_DEV( w->cShapes );
 	FREE_DEV( w->cMix );
 	FREE_DEV( w->cFlags );
+	FREE_DEV( w->cCache );
 	FREE_DEV( w->cBodies );
 	FREE_DEV( w->manifold );
 	FREE_DEV( w->solveList );
@@ -149,6 +150,10 @@ extern "C" void b2gd_free( b2gDevWorld* w, b2gHostIO* io )
 		cudaFreeHost( io->counters );
 	if ( io->newContacts )
 		cudaFreeHost( io->newContacts );
+	if ( io->hitIds )
+		cudaFreeHost( io->hitIds );
+	if ( io->hitOut )
+		cudaFreeHost( io->hitOut );
 	if ( w->stage )
 		cudaFree( w->stage );
 	if ( w->stream )
@@ -210,6 +215,7 @@ extern "C" int b2gd_reserve( b2gDevWorld* w, b2gHostIO* io, int bodyCap, int sha
 		e |= grow( (void**)&w->cShapes, 8u * o, 8u * n, s );
 		e |= grow( (void**)&w->cMix, 8u * o, 8u * n, s );
 		e |= grow( (void**)&w->cFlags, 4u * o, 4u * n, s );
+		e |= grow( (void**)&w->cCache, 4u * o, 4u * n, s );
 		e |= grow( (void**)&w->cBodies, 8u * o, 8u * n, s );
 		e |= grow( (void**)&w->manifold, sizeof( b2gManifold ) * o, sizeof( b2gManifold ) * n, s );
 		e |= grow_host_mapped( (void**)&io->events, (void**)&w->events, 4u * n );
@@ -356,6 +362,71 @@ extern "C" int b2gd_download_bodies( b2gDevWorld* w, float* state, float* xf, fl
 	int e = d2h( w, state, w->state, 2 * n4, s );
 	e |= d2h( w, xf, w->xf, n4, s );
 	e |= d2h( w, centers, w->centers, n4, s );
+	e |= ok( cudaStreamSynchronize( s ) );
+	return e;
+}
+
+/* Hit test of one contact (reference src/solver.c:1688-1712): the point with the largest
+ * approach speed above the threshold among the points that carry a normal impulse. */
+__global__ void k_hit_events( const b2gManifold* manifolds, const int* ids, int n, float threshold, float4* out )
+{
+	int k = blockIdx.x * blockDim.x + threadIdx.x;
+	if ( k >= n )
+		return;
+	const b2gManifold* m = manifolds + ids[k];
+	float approach = threshold;
+	float hit = 0.0f;
+	b2gVec point = gv( 0.0f, 0.0f );
+	for ( int j = 0; j < m->count; ++j )
+	{
+		const b2gPoint* mp = m->pts + j;
+		float s = -mp->normalVelocity;
+		if ( s > approach && mp->normalImpulse > 0.0f )
+		{
+			approach = s;
+			point = mp->point;
+			hit = 1.0f;
+		}
+	}
+	out[2 * k] = make_float4( hit, approach, point.x, point.y );
+	out[2 * k + 1] = make_float4( m->normal.x, m->normal.y, 0.0f, 0.0f );
+}
+
+extern "C" int b2gd_reserve_hits( b2gHostIO* io, int n )
+{
+	if ( n <= io->hitCap )
+		return 0;
+	int cap = n < 256 ? 256 : n + n / 2;
+	if ( io->hitIds )
+		cudaFreeHost( io->hitIds );
+	if ( io->hitOut )
+		cudaFreeHost( io->hitOut );
+	io->hitIds = nullptr;
+	io->hitOut = nullptr;
+	io->hitCap = 0;
+	int e = ok( cudaHostAlloc( (void**)&io->hitIds, sizeof( int ) * (size_t)cap, cudaHostAllocMapped ) );
+	e |= ok( cudaHostAlloc( (void**)&io->hitOut, sizeof( float ) * 8u * (size_t)cap, cudaHostAllocMapped ) );
+	if ( e == 0 )
+		io->hitCap = cap;
+	return e;
+}
+
+extern "C" int b2gd_hit_events( b2gDevWorld* w, b2gHostIO* io, int n, float threshold )
+{
+	if ( n <= 0 )
+		return 0;
+	cudaStream_t s = (cudaStream_t)w->stream;
+	int* dIds = nullptr;
+	float4* dOut = nullptr;
+	int e = ok( cudaHostGetDevicePointer( (void**)&dIds, io->hitIds, 0 ) );
+	e |= ok( cudaHostGetDevicePointer( (void**)&dOut, io->hitOut, 0 ) );
+	if ( e )
+		return e;
+	k_hit_events<<<( n + 127 ) / 128, 128, 0, s>>>( w->manifold, dIds, n, threshold, dOut );
+	w->launches += 1;
+	w->h2dBytes += 4 * (long long)n;
+	w->d2hBytes += 32 * (long long)n;
+	e = ok( cudaGetLastError() );
 	e |= ok( cudaStreamSynchronize( s ) );
 	return e;
 }

@@ -39,6 +39,9 @@ typedef struct b2gHostIO
 	int* events;		/* mapped: narrowphase events */
 	b2gRecord* records; /* mapped: finalisation records */
 	b2gContactInit* newContacts;
+	int* hitIds;	/* mapped: contacts to test for hit events */
+	float* hitOut; /* mapped: 8 per contact: hit, approach speed, point, normal, 0, 0 */
+	int hitCap;
 } b2gHostIO;
 
 /* Host memory of the library through the caller's allocator (util.c). */
@@ -73,6 +76,12 @@ int b2gd_upload_shape_boxes( b2gDevWorld* w, int shapeId, const float* aabb4, co
 /* Device -> host copies. */
 int b2gd_download_bodies( b2gDevWorld* w, float* state, float* xf, float* centers, int count );
 int b2gd_download_manifolds( b2gDevWorld* w, b2gManifold* out, uint32_t* flags, int count );
+/* Hit test of the contacts ids[0..n) after the solver stage (reference
+ * src/solver.c:1670-1723): out[8 k ..] = hit flag, approach speed and point of the
+ * fastest approaching point above `threshold` with a positive impulse, then the normal.
+ * Synchronises the world's stream; ids and results are io->hitIds / io->hitOut. */
+int b2gd_hit_events( b2gDevWorld* w, b2gHostIO* io, int n, float threshold );
+int b2gd_reserve_hits( b2gHostIO* io, int n );
 int b2gd_download_shapes( b2gDevWorld* w, float* aabb, float* fat, int count );
 int b2gd_download_joints( b2gDevWorld* w, b2gJointDev* joints, int count );
 

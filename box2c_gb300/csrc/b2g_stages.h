@@ -22,6 +22,7 @@
 #include "b2g_collide.h"
 #include "b2g_device.h"
 #include "b2g_solve.h"
+#include "b2g_toi.h"
 
 #include <cuda_runtime.h>
 
@@ -115,6 +116,7 @@ static __device__ __forceinline__ void scatter_contact( const b2gDevWorld& W, co
 	W.cMix[2 * id] = c.friction;
 	W.cMix[2 * id + 1] = c.restitution;
 	W.cFlags[id] = B2G_C_LIVE;
+	W.cCache[id] = 0u;
 	W.cBodies[2 * id] = -1;
 	W.cBodies[2 * id + 1] = -1;
 	b2gManifold m;
@@ -150,6 +152,38 @@ static __device__ __noinline__ void narrowphase( b2gManifold* m, const b2gShapeG
 		narrowphase_polygons( m, gA, xfA, gB, xfB );
 	else
 		narrowphase_shapes( m, gA, xfA, gB, xfB );
+}
+
+/* Sensor contacts: whether the shapes overlap, by their GJK distance with radii,
+ * warm-started from the contact's closest-feature cache and updating it (reference
+ * src/contact.c:476-503).  The cache packs its count in bits 0-1 and the six vertex
+ * indices in 3 bits each from bit 2. */
+static __device__ __noinline__ bool sensor_overlap( const b2gDevWorld& W, int id, const b2gShapeGeo* gA, b2gXf xfA,
+													const b2gShapeGeo* gB, b2gXf xfB )
+{
+	uint32_t packed = W.cCache[id];
+	b2gDistCache cache;
+	cache.count = (int)( packed & 3u );
+	for ( int i = 0; i < 3; ++i )
+	{
+		cache.indexA[i] = (int)( ( packed >> ( 2 + 3 * i ) ) & 7u );
+		cache.indexB[i] = (int)( ( packed >> ( 11 + 3 * i ) ) & 7u );
+	}
+	b2gProxy pa = gproxy_shape( gA );
+	b2gProxy pb = gproxy_shape( gB );
+	float d = gdistance( &cache, &pa, xfA, &pb, xfB );
+	packed = (uint32_t)cache.count;
+	for ( int i = 0; i < cache.count; ++i )
+	{
+		packed |= (uint32_t)cache.indexA[i] << ( 2 + 3 * i );
+		packed |= (uint32_t)cache.indexB[i] << ( 11 + 3 * i );
+	}
+	W.cCache[id] = packed;
+	if ( d < FLT_EPSILON )
+		d = 0.0f;
+	else
+		d = gmax( 0.0f, d - pa.radius - pb.radius );
+	return d < 10.0f * FLT_EPSILON;
 }
 
 static __device__ __forceinline__ void emit_event( const b2gDevWorld& W, int id, int code )
@@ -194,6 +228,18 @@ static __device__ void collide_contact( const b2gDevWorld& W, int id )
 	float4 ca = centers[bA], cb = centers[bB];
 	b2gVec offA = grotate( xfA.q, gv( ca.z, ca.w ) );
 	b2gVec offB = grotate( xfB.q, gv( cb.z, cb.w ) );
+
+	if ( gA->isSensor || gB->isSensor )
+	{
+		/* sensors generate no manifold and no hit events */
+		bool overlap = sensor_overlap( W, id, gA, xfA, gB, xfB );
+		W.cFlags[id] = B2G_C_LIVE | ( overlap ? B2G_C_TOUCHING : 0u );
+		if ( overlap && !wasTouching )
+			emit_event( W, id, B2G_EV_STARTED );
+		else if ( !overlap && wasTouching )
+			emit_event( W, id, B2G_EV_STOPPED );
+		return;
+	}
 
 	/* the previous manifold's feature ids and impulses, for warm starting */
 	const b2gManifold* prev = W.manifold + id;

@@ -196,6 +196,7 @@ typedef struct b2gDevWorld
 	int* cShapes;	/* 2 per contact */
 	float* cMix;	/* friction, restitution */
 	uint32_t* cFlags;
+	uint32_t* cCache; /* sensor contacts: the GJK closest-feature cache, packed */
 	int* cBodies; /* 2 per contact: awake body id or -1 */
 	b2gManifold* manifold;
 

@@ -178,6 +178,7 @@ enum
 	G_SENSOR = 4,
 	G_ENABLE_SENSOR_EVENTS = 0x10,
 	G_ENABLE_CONTACT_EVENTS = 0x20,
+	G_SENSOR_TOUCHING = 0x40,
 };
 
 typedef struct gContact
@@ -280,6 +281,13 @@ typedef struct gWorld
 	int beginCount, beginCap;
 	b2ContactEndTouchEvent* endEvents;
 	int endCount, endCap;
+	b2ContactHitEvent* hitEvents;
+	int hitCount, hitCap;
+	b2SensorBeginTouchEvent* sensorBeginEvents;
+	int sensorBeginCount, sensorBeginCap;
+	b2SensorEndTouchEvent* sensorEndEvents;
+	int sensorEndCount, sensorEndCap;
+	int hitShapes; /* live shapes with hit events enabled */
 
 	b2Profile profile;
 	/* host phases of the last step in ms (b2DeviceTimes order): pair query, pair rules,

@@ -961,3 +961,57 @@ b2BodyId b2s_add_square( b2WorldId worldId, float h )
 	b2CreatePolygonShape( bodyId, &sd, &square );
 	return bodyId;
 }
+
+b2WorldId b2s_event_scene( int count, uint64_t seed )
+{
+	b2WorldDef wd = b2s_world_def();
+	b2WorldId worldId = b2CreateWorld( &wd );
+	if ( B2_IS_NULL( worldId ) )
+		return worldId;
+
+	/* ground with hit events; a static sensor band the bodies fall through */
+	b2BodyDef gd = b2DefaultBodyDef();
+	gd.position = ( b2Vec2 ){ 0.0f, -0.5f };
+	b2BodyId groundId = b2CreateBody( worldId, &gd );
+	b2ShapeDef gsd = b2DefaultShapeDef();
+	gsd.enableHitEvents = true;
+	b2Polygon groundBox = b2MakeBox( 30.0f, 0.5f );
+	b2CreatePolygonShape( groundId, &gsd, &groundBox );
+	b2ShapeDef sensorDef = b2DefaultShapeDef();
+	sensorDef.isSensor = true;
+	b2Polygon band = b2MakeOffsetBox( 12.0f, 0.75f, ( b2Vec2 ){ 0.0f, 4.5f }, 0.0f );
+	b2CreatePolygonShape( groundId, &sensorDef, &band );
+
+	b2sRandom rng;
+	b2s_seed( &rng, seed );
+	b2BodyDef bd = b2DefaultBodyDef();
+	bd.type = b2_dynamicBody;
+	b2Polygon box = b2MakeBox( 0.3f, 0.3f );
+	b2Circle circle = { { 0.0f, 0.0f }, 0.3f };
+	b2Circle ring = { { 0.0f, 0.0f }, 0.8f };
+	for ( int k = 0; k < count; ++k )
+	{
+		bd.position = ( b2Vec2 ){ -10.0f + 20.0f * ( k + 0.5f ) / count + b2s_uniform( &rng, -0.1f, 0.1f ),
+								  6.0f + 2.5f * ( k % 3 ) + b2s_uniform( &rng, 0.0f, 1.0f ) };
+		b2BodyId bodyId = b2CreateBody( worldId, &bd );
+		b2ShapeDef sd = b2DefaultShapeDef();
+		sd.density = 1.0f;
+		sd.friction = 0.5f;
+		sd.restitution = ( k % 4 ) == 0 ? 0.6f : 0.1f;
+		sd.enableHitEvents = ( k & 1 ) == 0;
+		sd.enableContactEvents = ( k % 5 ) != 4;
+		if ( k % 2 == 0 )
+			b2CreatePolygonShape( bodyId, &sd, &box );
+		else
+			b2CreateCircleShape( bodyId, &sd, &circle );
+		if ( k % 7 == 3 )
+		{
+			/* a sensor ring carried by the body */
+			b2ShapeDef ringDef = b2DefaultShapeDef();
+			ringDef.isSensor = true;
+			ringDef.density = 0.0f;
+			b2CreateCircleShape( bodyId, &ringDef, &ring );
+		}
+	}
+	return worldId;
+}

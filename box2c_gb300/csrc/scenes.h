@@ -104,6 +104,12 @@ b2WorldId b2s_empty_world( void );
 b2BodyId b2s_add_body( b2WorldId worldId, int type );
 b2BodyId b2s_add_square( b2WorldId worldId, float h );
 
+/* Event scene: `count` boxes and circles dropped through a static sensor band onto a
+ * ground whose shape reports hit events; some bodies bounce (restitution 0.6), every
+ * other one enables hit events, every fifth disables contact events, every seventh
+ * carries a sensor ring of radius 0.8. */
+b2WorldId b2s_event_scene( int count, uint64_t seed );
+
 /* Draws `n` integers uniform in [lo, hi] from `seed` into out. */
 void b2s_draw_ints( int n, uint64_t seed, int lo, int hi, int* out );
 /* Draws `n` floats uniform in [lo, hi) / standard normal from `seed` into out. */

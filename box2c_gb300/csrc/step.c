@@ -53,6 +53,109 @@ static void push_end( gWorld* w, int a, int b )
 	e->shapeIdB = ( b2ShapeId ){ b + 1, (uint16_t)w->slot, w->shapes[b].revision };
 }
 
+static b2ShapeId shape_id( gWorld* w, int s ) { return ( b2ShapeId ){ s + 1, (uint16_t)w->slot, w->shapes[s].revision }; }
+
+/* Sensor overlap events (reference src/world.c:563-580, :606-624): one per sensor shape
+ * of the pair, the sensor first. */
+static void push_sensor( gWorld* w, bool begin, int sensor, int visitor )
+{
+	if ( begin )
+	{
+		if ( w->sensorBeginCount == w->sensorBeginCap )
+		{
+			int cap = w->sensorBeginCap ? 2 * w->sensorBeginCap : 16;
+			void* p = b2g_realloc( w->sensorBeginEvents, sizeof( b2SensorBeginTouchEvent ) * (size_t)cap );
+			if ( p == NULL )
+				return;
+			w->sensorBeginEvents = p;
+			w->sensorBeginCap = cap;
+		}
+		b2SensorBeginTouchEvent* e = w->sensorBeginEvents + w->sensorBeginCount++;
+		e->sensorShapeId = shape_id( w, sensor );
+		e->visitorShapeId = shape_id( w, visitor );
+	}
+	else
+	{
+		if ( w->sensorEndCount == w->sensorEndCap )
+		{
+			int cap = w->sensorEndCap ? 2 * w->sensorEndCap : 16;
+			void* p = b2g_realloc( w->sensorEndEvents, sizeof( b2SensorEndTouchEvent ) * (size_t)cap );
+			if ( p == NULL )
+				return;
+			w->sensorEndEvents = p;
+			w->sensorEndCap = cap;
+		}
+		b2SensorEndTouchEvent* e = w->sensorEndEvents + w->sensorEndCount++;
+		e->sensorShapeId = shape_id( w, sensor );
+		e->visitorShapeId = shape_id( w, visitor );
+	}
+}
+
+static void sensor_events( gWorld* w, gContact* c, bool begin )
+{
+	if ( ( c->flags & G_ENABLE_SENSOR_EVENTS ) == 0 )
+		return;
+	if ( w->shapes[c->shapeIdA].isSensor )
+		push_sensor( w, begin, c->shapeIdA, c->shapeIdB );
+	if ( w->shapes[c->shapeIdB].isSensor )
+		push_sensor( w, begin, c->shapeIdB, c->shapeIdA );
+}
+
+/* Hit events of the step (reference src/solver.c:1670-1723): the contacts of the graph
+ * colours in colour and array order whose shapes enable hit events, tested on the
+ * device against their solved manifolds. */
+static void report_hits( gWorld* w )
+{
+	if ( w->hitShapes == 0 )
+		return;
+	int n = 0;
+	for ( int i = 0; i < B2G_COLORS; ++i )
+		n += w->colors[i].contacts.count;
+	if ( n == 0 || b2gd_reserve_hits( &w->io, n ) != 0 )
+		return;
+	n = 0;
+	for ( int i = 0; i < B2G_COLORS; ++i )
+	{
+		gIntArray* a = &w->colors[i].contacts;
+		for ( int j = 0; j < a->count; ++j )
+		{
+			gContact* c = w->contacts + a->data[j];
+			if ( w->shapes[c->shapeIdA].enableHitEvents || w->shapes[c->shapeIdB].enableHitEvents )
+				w->io.hitIds[n++] = c->id;
+		}
+	}
+	if ( n == 0 )
+		return;
+	int e = b2gd_hit_events( &w->dev, &w->io, n, w->hitThreshold );
+	if ( e )
+	{
+		w->status = e;
+		return;
+	}
+	for ( int k = 0; k < n; ++k )
+	{
+		const float* r = w->io.hitOut + 8 * k;
+		if ( r[0] == 0.0f )
+			continue;
+		if ( w->hitCount == w->hitCap )
+		{
+			int cap = w->hitCap ? 2 * w->hitCap : 16;
+			void* p = b2g_realloc( w->hitEvents, sizeof( b2ContactHitEvent ) * (size_t)cap );
+			if ( p == NULL )
+				return;
+			w->hitEvents = p;
+			w->hitCap = cap;
+		}
+		gContact* c = w->contacts + w->io.hitIds[k];
+		b2ContactHitEvent* h = w->hitEvents + w->hitCount++;
+		h->shapeIdA = shape_id( w, c->shapeIdA );
+		h->shapeIdB = shape_id( w, c->shapeIdB );
+		h->point = ( b2Vec2 ){ r[2], r[3] };
+		h->normal = ( b2Vec2 ){ r[4], r[5] };
+		h->approachSpeed = r[1];
+	}
+}
+
 /* ------------------------------------------------------------ contacts */
 /* Contact records staged for the device, applied in order before the next narrowphase
  * (creation, or retirement of a contact destroyed outside the narrowphase). */
@@ -546,7 +649,11 @@ static void process_events( gWorld* w, int count )
 		else if ( code == B2G_EV_STARTED )
 		{
 			if ( flags & G_SENSOR )
+			{
+				sensor_events( w, c, true );
+				c->flags |= G_SENSOR_TOUCHING;
 				continue;
+			}
 			if ( flags & G_ENABLE_CONTACT_EVENTS )
 				push_begin( w, c->shapeIdA, c->shapeIdB );
 			c->flags |= G_TOUCHING;
@@ -557,7 +664,11 @@ static void process_events( gWorld* w, int count )
 		else if ( code == B2G_EV_STOPPED )
 		{
 			if ( flags & G_SENSOR )
+			{
+				c->flags &= ~G_SENSOR_TOUCHING;
+				sensor_events( w, c, false );
 				continue;
+			}
 			c->flags &= ~G_TOUCHING;
 			if ( c->flags & G_ENABLE_CONTACT_EVENTS )
 				push_end( w, c->shapeIdA, c->shapeIdB );
@@ -1069,6 +1180,7 @@ void gstep_finish( gWorld* w )
 	w->profile.solve = (float)( t3 - w->stepStart );
 	int recordCount = w->io.counters[1];
 	w->lastRecordCount = recordCount;
+	report_hits( w );
 	double tr = b2g_now_ms();
 	/* records reach the host through mapped memory: 48 bytes, 80 for fast shapes */
 	for ( int i = 0; i < ( recordCount < w->dev.recordCap ? recordCount : w->dev.recordCap ); ++i )
@@ -1160,6 +1272,9 @@ void b2World_Step( b2WorldId worldId, float timeStep, int subStepCount )
 		return;
 	w->beginCount = 0;
 	w->endCount = 0;
+	w->hitCount = 0;
+	w->sensorBeginCount = 0;
+	w->sensorEndCount = 0;
 	memset( &w->profile, 0, sizeof( w->profile ) );
 	if ( timeStep == 0.0f || w->status != 0 )
 		return;

@@ -424,6 +424,9 @@ void b2DestroyWorld( b2WorldId worldId )
 	b2g_free( w->recordBucket );
 	b2g_free( w->beginEvents );
 	b2g_free( w->endEvents );
+	b2g_free( w->hitEvents );
+	b2g_free( w->sensorBeginEvents );
+	b2g_free( w->sensorEndEvents );
 	void* pinned[] = { w->hState, w->hXf, w->hCenters, w->hPrev, w->hMass, w->hForce, w->hExtent, w->hInfo, w->hGeo, w->hAabb, w->hFat, w->hJoints };
 	for ( size_t i = 0; i < sizeof( pinned ) / sizeof( pinned[0] ); ++i )
 		if ( pinned[i] )
@@ -471,6 +474,15 @@ b2ContactEvents b2World_GetContactEvents( b2WorldId id )
 	e.beginCount = w->beginCount;
 	e.endEvents = w->endEvents;
 	e.endCount = w->endCount;
+	e.hitEvents = w->hitEvents;
+	e.hitCount = w->hitCount;
+	return e;
+}
+
+b2SensorEvents b2World_GetSensorEvents( b2WorldId id )
+{
+	gWorld* w = gworld_get( id );
+	b2SensorEvents e = { w->sensorBeginEvents, w->sensorEndEvents, w->sensorBeginCount, w->sensorEndCount };
 	return e;
 }
 
@@ -902,6 +914,8 @@ static b2ShapeId create_shape( b2BodyId bodyId, const b2ShapeDef* def, b2ShapeTy
 	s->enableSensorEvents = def->enableSensorEvents;
 	s->enableContactEvents = def->enableContactEvents;
 	s->enableHitEvents = def->enableHitEvents;
+	if ( def->enableHitEvents )
+		w->hitShapes += 1;
 	s->enablePreSolveEvents = def->enablePreSolveEvents;
 	b2gShapeGeo* g = w->hGeo + id;
 	*g = *geo;
@@ -1578,6 +1592,8 @@ void b2DestroyShape( b2ShapeId shapeId )
 	}
 	gid_free( &w->shapeIds, id );
 	s->id = B2G_NULL;
+	if ( s->enableHitEvents )
+		w->hitShapes -= 1;
 	if ( b->automaticMass )
 		gbody_update_mass( w, b );
 	w->shapeListsDirty = true;
@@ -1613,6 +1629,8 @@ void b2DestroyBody( b2BodyId bodyId )
 		destroy_proxy( w, s );
 		gid_free( &w->shapeIds, sid );
 		s->id = B2G_NULL;
+		if ( s->enableHitEvents )
+			w->hitShapes -= 1;
 		sid = s->next;
 	}
 	/* the awake set drops the body by moving its last body into the slot */

@@ -23,6 +23,9 @@ B2_API b2WorldId b2CreateWorld( const b2WorldDef* def );
 B2_API void b2DestroyWorld( b2WorldId worldId );
 B2_API bool b2World_IsValid( b2WorldId id );
 B2_API void b2World_Step( b2WorldId worldId, float timeStep, int subStepCount );
+/* Events of the last step (reference box2d.h:48, :51): contact begin/end touch and hit
+ * events, sensor begin/end overlap events; valid until the next step. */
+B2_API b2SensorEvents b2World_GetSensorEvents( b2WorldId worldId );
 B2_API b2ContactEvents b2World_GetContactEvents( b2WorldId worldId );
 B2_API void b2World_EnableSleeping( b2WorldId worldId, bool flag );
 B2_API void b2World_EnableContinuous( b2WorldId worldId, bool flag );

@@ -209,6 +209,28 @@ typedef struct b2RevoluteJointDef
 
 B2_API b2RevoluteJointDef b2DefaultRevoluteJointDef( void );
 
+/* Sensor overlap events (reference types.h:877-912): the sensor shape and the shape that
+ * began or stopped overlapping it. */
+typedef struct b2SensorBeginTouchEvent
+{
+	b2ShapeId sensorShapeId;
+	b2ShapeId visitorShapeId;
+} b2SensorBeginTouchEvent;
+
+typedef struct b2SensorEndTouchEvent
+{
+	b2ShapeId sensorShapeId;
+	b2ShapeId visitorShapeId;
+} b2SensorEndTouchEvent;
+
+typedef struct b2SensorEvents
+{
+	b2SensorBeginTouchEvent* beginEvents;
+	b2SensorEndTouchEvent* endEvents;
+	int32_t beginCount;
+	int32_t endCount;
+} b2SensorEvents;
+
 typedef struct b2ContactBeginTouchEvent
 {
 	b2ShapeId shapeIdA;

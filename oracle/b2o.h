@@ -165,6 +165,14 @@ typedef struct oSegDist
 } oSegDist;
 oSegDist o_segment_distance( oVec p1, oVec q1, oVec p2, oVec q2 );
 
+/* Closest-feature cache of the GJK distance (reference include/box2d/collision.h
+ * b2DistanceCache); kept per contact for the sensor overlap test. */
+typedef struct oDistCache
+{
+	int count;
+	int indexA[3], indexB[3];
+} oDistCache;
+
 /* ---------------------------------------------------------------- world records */
 typedef struct oShape
 {
@@ -223,6 +231,7 @@ enum
 	OC_SENSOR = 4,
 	OC_ENABLE_SENSOR_EVENTS = 0x10,
 	OC_ENABLE_CONTACT_EVENTS = 0x20,
+	OC_SENSOR_TOUCHING = 0x40,
 
 	OS_TOUCHING = 0x10000,
 	OS_DISJOINT = 0x20000,
@@ -250,6 +259,7 @@ typedef struct oContact
 	oManifold manifold;
 	b2r friction, restitution;
 	uint32_t simFlags;
+	oDistCache cache; /* sensor overlap test (reference src/contact.h:136) */
 } oContact;
 
 typedef struct oRevolute
@@ -344,6 +354,12 @@ typedef struct oWorld
 	int beginCount, beginCap;
 	b2ContactEndTouchEvent* endEvents;
 	int endCount, endCap;
+	b2ContactHitEvent* hitEvents;
+	int hitCount, hitCap;
+	b2SensorBeginTouchEvent* sensorBeginEvents;
+	int sensorBeginCount, sensorBeginCap;
+	b2SensorEndTouchEvent* sensorEndEvents;
+	int sensorEndCount, sensorEndCap;
 
 	b2Profile profile;
 	uint64_t stepIndex;
@@ -367,6 +383,7 @@ oBox o_shape_aabb( const oShape* s, oXf xf );
 void o_update_body_mass( oWorld* w, oBody* b );
 oSoft o_make_soft( b2r hertz, b2r zeta, b2r h );
 bool o_should_bodies_collide( oWorld* w, oBody* a, oBody* b );
+void o_report_hits( oWorld* w );
 
 /* ---------------------------------------------------------------- time of impact
  * (b2o_toi.c; reference src/distance.c, src/shape.c:480-497, :713-735) */
@@ -382,12 +399,6 @@ typedef struct oProxy
 	int count;
 	b2r radius;
 } oProxy;
-
-typedef struct oDistCache
-{
-	int count;
-	int indexA[3], indexB[3];
-} oDistCache;
 
 oXf o_sweep_xf( const oSweep* s, b2r t );
 oProxy o_make_proxy( const oVec* points, int count, b2r radius );

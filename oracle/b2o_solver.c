@@ -987,6 +987,7 @@ void o_solve( oWorld* w, b2r dt, int subSteps )
 	}
 	free( cons );
 	o_capture_outputs( w );
+	o_report_hits( w );
 
 	oFinalize f;
 	f.enlarged = (uint8_t*)calloc( (size_t)awakeCount, 1 );

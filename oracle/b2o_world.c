@@ -175,6 +175,78 @@ static void add_event_end( oWorld* w, int a, int b )
 	e->shapeIdB = ( b2ShapeId ){ b + 1, (uint16_t)w->slot, w->shapes[b].revision };
 }
 
+static b2ShapeId shape_id( oWorld* w, int s ) { return ( b2ShapeId ){ s + 1, (uint16_t)w->slot, w->shapes[s].revision }; }
+
+static void add_sensor_event( oWorld* w, bool begin, int sensor, int visitor )
+{
+	if ( begin )
+	{
+		if ( w->sensorBeginCount == w->sensorBeginCap )
+		{
+			w->sensorBeginCap = w->sensorBeginCap ? 2 * w->sensorBeginCap : 16;
+			w->sensorBeginEvents = realloc( w->sensorBeginEvents, sizeof( b2SensorBeginTouchEvent ) * (size_t)w->sensorBeginCap );
+		}
+		b2SensorBeginTouchEvent* e = w->sensorBeginEvents + w->sensorBeginCount++;
+		e->sensorShapeId = shape_id( w, sensor );
+		e->visitorShapeId = shape_id( w, visitor );
+	}
+	else
+	{
+		if ( w->sensorEndCount == w->sensorEndCap )
+		{
+			w->sensorEndCap = w->sensorEndCap ? 2 * w->sensorEndCap : 16;
+			w->sensorEndEvents = realloc( w->sensorEndEvents, sizeof( b2SensorEndTouchEvent ) * (size_t)w->sensorEndCap );
+		}
+		b2SensorEndTouchEvent* e = w->sensorEndEvents + w->sensorEndCount++;
+		e->sensorShapeId = shape_id( w, sensor );
+		e->visitorShapeId = shape_id( w, visitor );
+	}
+}
+
+/* Hit events of the step (reference src/solver.c:1670-1723): contacts of the colours in
+ * colour and array order whose touching shapes enable hit events; the point of the
+ * fastest approach above the world's threshold among points that carry an impulse. */
+void o_report_hits( oWorld* w )
+{
+	for ( int i = 0; i < O_COLORS; ++i )
+	{
+		oIntArray* a = &w->colors[i].contacts;
+		for ( int j = 0; j < a->count; ++j )
+		{
+			oContact* c = w->contacts + a->data[j];
+			if ( ( c->simFlags & OS_HIT ) == 0 )
+				continue;
+			b2ContactHitEvent e;
+			memset( &e, 0, sizeof( e ) );
+			b2r approach = R( w->hitThreshold );
+			bool hit = false;
+			for ( int k = 0; k < c->manifold.count; ++k )
+			{
+				oMPoint* mp = c->manifold.pts + k;
+				b2r s = -mp->normalVelocity;
+				if ( s > approach && mp->normalImpulse > R( 0 ) )
+				{
+					approach = s;
+					e.point = ( b2Vec2 ){ (float)mp->point.x, (float)mp->point.y };
+					hit = true;
+				}
+			}
+			if ( hit == false )
+				continue;
+			e.approachSpeed = (float)approach;
+			e.normal = ( b2Vec2 ){ (float)c->manifold.normal.x, (float)c->manifold.normal.y };
+			e.shapeIdA = shape_id( w, c->shapeIdA );
+			e.shapeIdB = shape_id( w, c->shapeIdB );
+			if ( w->hitCount == w->hitCap )
+			{
+				w->hitCap = w->hitCap ? 2 * w->hitCap : 16;
+				w->hitEvents = realloc( w->hitEvents, sizeof( b2ContactHitEvent ) * (size_t)w->hitCap );
+			}
+			w->hitEvents[w->hitCount++] = e;
+		}
+	}
+}
+
 /* ------------------------------------------------------------ world */
 b2WorldId b2CreateWorld( const b2WorldDef* def )
 {
@@ -251,6 +323,9 @@ void b2DestroyWorld( b2WorldId worldId )
 	free( w->joints );
 	free( w->beginEvents );
 	free( w->endEvents );
+	free( w->hitEvents );
+	free( w->sensorBeginEvents );
+	free( w->sensorEndEvents );
 	uint16_t revision = w->revision;
 	memset( w, 0, sizeof( *w ) );
 	w->revision = (uint16_t)( revision + 1 );
@@ -289,6 +364,15 @@ b2ContactEvents b2World_GetContactEvents( b2WorldId id )
 	e.beginCount = w->beginCount;
 	e.endEvents = w->endEvents;
 	e.endCount = w->endCount;
+	e.hitEvents = w->hitEvents;
+	e.hitCount = w->hitCount;
+	return e;
+}
+
+b2SensorEvents b2World_GetSensorEvents( b2WorldId id )
+{
+	oWorld* w = o_world( id );
+	b2SensorEvents e = { w->sensorBeginEvents, w->sensorEndEvents, w->sensorBeginCount, w->sensorEndCount };
 	return e;
 }
 
@@ -1175,6 +1259,22 @@ void o_update_pairs( oWorld* w )
 /* ------------------------------------------------------------ narrowphase */
 static bool update_contact( oWorld* w, oContact* c, oShape* sA, oXf xfA, oVec offA, oShape* sB, oXf xfB, oVec offB )
 {
+	if ( sA->isSensor || sB->isSensor )
+	{
+		/* sensors: overlap of the shapes, no manifold (reference src/contact.c:476-503) */
+		oProxy pa = o_shape_proxy( sA ), pb = o_shape_proxy( sB );
+		b2r d = o_distance( &c->cache, &pa, xfA, &pb, xfB, NULL, NULL );
+		if ( d < O_EPS )
+			d = R( 0 );
+		else
+			d = omax( R( 0 ), d - pa.radius - pb.radius );
+		bool overlap = d < R( 10.0f ) * O_EPS;
+		if ( overlap )
+			c->simFlags |= OS_TOUCHING;
+		else
+			c->simFlags &= ~OS_TOUCHING;
+		return overlap;
+	}
 	oManifold old = c->manifold;
 	oManifold m;
 	switch ( sA->type )
@@ -1347,7 +1447,15 @@ void o_collide( oWorld* w )
 			{
 				if ( flags & OC_SENSOR )
 				{
+					if ( flags & OC_ENABLE_SENSOR_EVENTS )
+					{
+						if ( w->shapes[c->shapeIdA].isSensor )
+							add_sensor_event( w, true, c->shapeIdA, c->shapeIdB );
+						if ( w->shapes[c->shapeIdB].isSensor )
+							add_sensor_event( w, true, c->shapeIdB, c->shapeIdA );
+					}
 					c->simFlags &= ~OS_STARTED;
+					c->flags |= OC_SENSOR_TOUCHING;
 				}
 				else
 				{
@@ -1363,7 +1471,18 @@ void o_collide( oWorld* w )
 			else if ( simFlags & OS_STOPPED )
 			{
 				c->simFlags &= ~OS_STOPPED;
-				if ( ( flags & OC_SENSOR ) == 0 )
+				if ( flags & OC_SENSOR )
+				{
+					c->flags &= ~OC_SENSOR_TOUCHING;
+					if ( flags & OC_ENABLE_SENSOR_EVENTS )
+					{
+						if ( w->shapes[c->shapeIdA].isSensor )
+							add_sensor_event( w, false, c->shapeIdA, c->shapeIdB );
+						if ( w->shapes[c->shapeIdB].isSensor )
+							add_sensor_event( w, false, c->shapeIdB, c->shapeIdA );
+					}
+				}
+				else
 				{
 					c->flags &= ~OC_TOUCHING;
 					if ( c->flags & OC_ENABLE_CONTACT_EVENTS )
@@ -1388,6 +1507,9 @@ void b2World_Step( b2WorldId worldId, float timeStep, int subStepCount )
 		return;
 	w->beginCount = 0;
 	w->endCount = 0;
+	w->hitCount = 0;
+	w->sensorBeginCount = 0;
+	w->sensorEndCount = 0;
 	memset( &w->profile, 0, sizeof( w->profile ) );
 	if ( timeStep == 0.0f )
 		return;

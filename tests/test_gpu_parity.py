@@ -209,3 +209,25 @@ def test_gpu_world_destroy_all_bodies_and_validity(gpu):
     """Reference test/test_world.c:121-204 (DestroyAllBodiesWorld, TestIsValid)."""
     from tests.helpers import run_world_api_checks
     run_world_api_checks(gpu)
+
+
+def test_gpu_events_match_oracle(gpu, oracle):
+    """Contact begin/end, hit and sensor events of every step equal the oracle's (which
+    the CPU tests pin to the reference): sensors tested by GJK overlap on the device with
+    each contact's closest-feature cache, hit events from the solved manifolds."""
+    from box2c_gb300.capi import bind_gpu_api
+    bind_gpu_api(gpu.lib)
+    wg, wo = gpu.event_scene(40, 1243), oracle.event_scene(40, 1243)
+    totals = [0] * 5
+    try:
+        for s in range(1, 301):
+            gpu.step(wg)
+            oracle.step(wo)
+            eg, eo = gpu.events(wg), oracle.events(wo)
+            assert eg == eo, f"events differ at step {s}"
+            totals = [t + len(e) for t, e in zip(totals, eo)]
+        assert np.array_equal(gpu.bodies(wg).view(np.uint32), oracle.bodies(wo).view(np.uint32))
+    finally:
+        gpu.destroy(wg)
+        oracle.destroy(wo)
+    assert all(t > 0 for t in totals), totals

@@ -202,3 +202,24 @@ def test_world_destroy_all_bodies_and_validity(request, backend):
     """Reference test/test_world.c:121-204 (DestroyAllBodiesWorld, TestIsValid) restated
     over the C API."""
     run_world_api_checks(request.getfixturevalue(backend))
+
+
+def test_events_match_reference(reference, oracle):
+    """Contact begin/end touch events, hit events and sensor begin/end overlap events of
+    every step, in order, equal the reference's (reference src/world.c:540-662,
+    src/solver.c:1670-1723, src/contact.c:476-503); the state stays bit-identical."""
+    wo, wr = oracle.event_scene(40, 1243), reference.event_scene(40, 1243)
+    totals = [0] * 5
+    try:
+        for s in range(1, 301):
+            oracle.step(wo)
+            reference.step(wr)
+            eo, er = oracle.events(wo), reference.events(wr)
+            assert eo == er, f"events differ at step {s}"
+            totals = [t + len(e) for t, e in zip(totals, er)]
+    finally:
+        oracle.destroy(wo)
+        reference.destroy(wr)
+    assert all(t > 0 for t in totals), totals
+    step, detail, _ = lockstep(oracle, reference, lambda b: b.event_scene(40, 1243), 300, check_manifolds=True)
+    assert step is None, f"{detail} at step {step}"
