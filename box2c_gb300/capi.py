@@ -166,6 +166,8 @@ class Backend:
         S.b2s_joint_hub.restype = WorldId
         S.b2s_joint_chains.argtypes = [C.c_int, C.c_int, C.c_int, C.c_uint64]
         S.b2s_joint_chains.restype = WorldId
+        S.b2s_joint_zoo.argtypes = [C.c_int, C.c_int, C.c_uint64]
+        S.b2s_joint_zoo.restype = WorldId
         S.b2s_event_scene.argtypes = [C.c_int, C.c_uint64]
         S.b2s_event_scene.restype = WorldId
         S.b2s_empty_world.argtypes = []
@@ -227,6 +229,10 @@ class Backend:
     def joint_chains(self, chains: int = 8, links: int = 8, flags: int = 7, seed: int = 1242) -> WorldId:
         """flags: 1 joint limits, 2 joint springs, 4 motors."""
         return self._made(self.scenes.b2s_joint_chains(chains, links, flags, seed))
+
+    def joint_zoo(self, copies: int = 2, flags: int = 0, seed: int = 1250) -> WorldId:
+        """Every joint type: ropes, pendulum, elevators, car, welds, motor and mouse joints, an overflowing spider."""
+        return self._made(self.scenes.b2s_joint_zoo(copies, flags, seed))
 
     def event_scene(self, count: int = 40, seed: int = 1243) -> WorldId:
         return self._made(self.scenes.b2s_event_scene(count, seed))

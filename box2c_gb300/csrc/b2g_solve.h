@@ -3,13 +3,13 @@
  * (kernels.cu) and the fused cluster solver (fused.cu).
  *
  * Every routine works on values already loaded into registers: one constraint row
- * (Row) or revolute joint (b2gJointDev), and the two body states it couples (DevState).
+ * (Row) or joint (b2gJointDev), and the two body states it couples (DevState).
  * Loading and storing is the caller's business, so the same arithmetic serves body
  * states in global memory and in distributed shared memory.  Operand order follows the
  * reference expression by expression (compiled with --fmad=false):
  *   8-lane contact path   src/contact_solver.c:810-1178
  *   scalar overflow path  src/contact_solver.c:149-440
- *   revolute joint        src/revolute_joint.c:272-470
+ *   joints                b2g_joints.h (every joint type)
  */
 #pragma once
 
@@ -310,144 +310,8 @@ __device__ __forceinline__ bool restitution_scalar( Row& r, DevState& a, DevStat
 	return true;
 }
 
-/* ------------------------------------------------------------------ revolute joint */
-/* Relative angle of two rotations (reference include/box2d/math_functions.h:386-394).
- * The reference calls the C library's atan2f; the device uses gatan2, which is within one
- * float ulp of it and gives the same bits on host and device. */
-__device__ __forceinline__ float rel_angle( b2gRot b, b2gRot a )
-{
-	float s = b.s * a.c - b.c * a.s;
-	float c = b.c * a.c + b.s * a.s;
-	return gatan2( s, c );
-}
-
-__device__ __forceinline__ float unwind( float a )
-{
-	if ( a < -B2G_PI )
-		return a + 2.0f * B2G_PI;
-	if ( a > B2G_PI )
-		return a - 2.0f * B2G_PI;
-	return a;
-}
-
-__device__ __forceinline__ void joint_warm_state( const b2gJointDev* j, DevState& a, DevState& b )
-{
-	b2gVec rA = grotate( a.dq, j->anchorA );
-	b2gVec rB = grotate( b.dq, j->anchorB );
-	float axial = j->springImpulse + j->motorImpulse + j->lowerImpulse - j->upperImpulse;
-	a.v = gmulsub( a.v, j->invMassA, j->linearImpulse );
-	a.w -= j->invIA * ( gcross( rA, j->linearImpulse ) + axial );
-	b.v = gmuladd( b.v, j->invMassB, j->linearImpulse );
-	b.w += j->invIB * ( gcross( rB, j->linearImpulse ) + axial );
-}
-
-__device__ __forceinline__ void joint_solve_state( b2gJointDev* j, DevState& a, DevState& b, bool useBias,
-												   const b2gStepConst& sc )
-{
-	float mA = j->invMassA, mB = j->invMassB, iA = j->invIA, iB = j->invIB;
-	b2gVec vA = a.v, vB = b.v;
-	float wA = a.w, wB = b.w;
-	bool fixedRotation = ( iA + iB == 0.0f );
-	if ( j->enableSpring && fixedRotation == false )
-	{
-		float C = rel_angle( b.dq, a.dq ) + j->deltaAngle;
-		float bias = j->springBias * C;
-		float Cdot = wB - wA;
-		float impulse = -j->springMass * j->axialMass * ( Cdot + bias ) - j->springImpulseScale * j->springImpulse;
-		j->springImpulse += impulse;
-		wA -= iA * impulse;
-		wB += iB * impulse;
-	}
-	if ( j->enableMotor && fixedRotation == false )
-	{
-		float Cdot = wB - wA - j->motorSpeed;
-		float impulse = -j->axialMass * Cdot;
-		float old = j->motorImpulse;
-		float maxImpulse = sc.h * j->maxMotorTorque;
-		j->motorImpulse = gclamp( j->motorImpulse + impulse, -maxImpulse, maxImpulse );
-		impulse = j->motorImpulse - old;
-		wA -= iA * impulse;
-		wB += iB * impulse;
-	}
-	if ( j->enableLimit && fixedRotation == false )
-	{
-		float angle = unwind( rel_angle( b.dq, a.dq ) + j->deltaAngle );
-		{
-			float C = angle - j->lowerAngle;
-			float bias = 0.0f, massScale = 1.0f, impulseScale = 0.0f;
-			if ( C > 0.0f )
-				bias = C * sc.inv_h;
-			else if ( useBias )
-			{
-				bias = sc.jointSoft[0] * C;
-				massScale = sc.jointSoft[1];
-				impulseScale = sc.jointSoft[2];
-			}
-			float Cdot = wB - wA;
-			float impulse = -massScale * j->axialMass * ( Cdot + bias ) - impulseScale * j->lowerImpulse;
-			float old = j->lowerImpulse;
-			j->lowerImpulse = gmax( j->lowerImpulse + impulse, 0.0f );
-			impulse = j->lowerImpulse - old;
-			wA -= iA * impulse;
-			wB += iB * impulse;
-		}
-		{
-			float C = j->upperAngle - angle;
-			float bias = 0.0f, massScale = 1.0f, impulseScale = 0.0f;
-			if ( C > 0.0f )
-				bias = C * sc.inv_h;
-			else if ( useBias )
-			{
-				bias = sc.jointSoft[0] * C;
-				massScale = sc.jointSoft[1];
-				impulseScale = sc.jointSoft[2];
-			}
-			float Cdot = wA - wB;
-			/* upper limit scaled by lowerImpulse, as in the reference (revolute_joint.c:409) */
-			float impulse = -massScale * j->axialMass * ( Cdot + bias ) - impulseScale * j->lowerImpulse;
-			float old = j->upperImpulse;
-			j->upperImpulse = gmax( j->upperImpulse + impulse, 0.0f );
-			impulse = j->upperImpulse - old;
-			wA += iA * impulse;
-			wB -= iB * impulse;
-		}
-	}
-	{
-		b2gVec rA = grotate( a.dq, j->anchorA );
-		b2gVec rB = grotate( b.dq, j->anchorB );
-		b2gVec Cdot = gsub( gadd( vB, gcross_sv( wB, rB ) ), gadd( vA, gcross_sv( wA, rA ) ) );
-		b2gVec bias = gv( 0.0f, 0.0f );
-		float massScale = 1.0f, impulseScale = 0.0f;
-		if ( useBias )
-		{
-			b2gVec sep = gadd( gadd( gsub( b.dp, a.dp ), gsub( rB, rA ) ), j->deltaCenter );
-			bias = gmulsv( sc.jointSoft[0], sep );
-			massScale = sc.jointSoft[1];
-			impulseScale = sc.jointSoft[2];
-		}
-		float k11 = mA + mB + rA.y * rA.y * iA + rB.y * rB.y * iB;
-		float k12 = -rA.y * rA.x * iA - rB.y * rB.x * iB;
-		float k22 = mA + mB + rA.x * rA.x * iA + rB.x * rB.x * iB;
-		b2gVec rhs = gadd( Cdot, bias );
-		float det = k11 * k22 - k12 * k12;
-		if ( det != 0.0f )
-			det = 1.0f / det;
-		b2gVec x = gv( det * ( k22 * rhs.x - k12 * rhs.y ), det * ( k11 * rhs.y - k12 * rhs.x ) );
-		b2gVec impulse;
-		impulse.x = -massScale * x.x - impulseScale * j->linearImpulse.x;
-		impulse.y = -massScale * x.y - impulseScale * j->linearImpulse.y;
-		j->linearImpulse.x += impulse.x;
-		j->linearImpulse.y += impulse.y;
-		vA = gmulsub( vA, mA, impulse );
-		wA -= iA * gcross( rA, impulse );
-		vB = gmuladd( vB, mB, impulse );
-		wB += iB * gcross( rB, impulse );
-	}
-	a.v = vA;
-	a.w = wA;
-	b.v = vB;
-	b.w = wB;
-}
+/* ------------------------------------------------------------------ joints */
+#include "b2g_joints.h"
 
 /* ------------------------------------------------------------------ body integration */
 /* Per-step velocity increments of one body (reference src/solver.c:34-93): the same

@@ -11,7 +11,7 @@
  * contact creation     src/contact.c:185-332 (sim part)
  * narrowphase          src/world.c:290-365, src/contact.c:493-582
  * prepare contacts     src/contact_solver.c:21-147, :597-808
- * prepare joints       src/revolute_joint.c:201-270
+ * prepare joints       src/joint.c:983-1018 (per type: b2g_joints.h)
  * integrate velocities src/solver.c:34-93
  * integrate positions  src/solver.c:146-163
  * store impulses       src/contact_solver.c:442-471, :1180-1293
@@ -400,25 +400,9 @@ static __device__ void row_phase( const b2gDevWorld& W, int k, int phase, bool s
 	row_work( W, GlobalBodies{ &W }, k, phase, scalar, sc );
 }
 
-/* ------------------------------------------------------------------ revolute joint */
-static __device__ void make_soft( float hertz, float zeta, float h, float* out )
-{
-	if ( hertz == 0.0f )
-	{
-		out[0] = 0.0f;
-		out[1] = 1.0f;
-		out[2] = 0.0f;
-		return;
-	}
-	float omega = 2.0f * B2G_PI * hertz;
-	float a1 = 2.0f * zeta + h * omega;
-	float a2 = h * omega * a1;
-	float a3 = 1.0f / ( 1.0f + a2 );
-	out[0] = omega / a1;
-	out[1] = a2 * a3;
-	out[2] = a3;
-}
-
+/* ------------------------------------------------------------------ joints */
+/* Joint preparation (reference src/joint.c:983-1018 and the per-type prepare functions):
+ * gathers the two bodies' mass and pose, then the type's own preparation. */
 static __device__ void prepare_joint( const b2gDevWorld& W, int t, const b2gStepConst& sc )
 {
 	b2gJointDev* j = W.joints + W.jointList[t];
@@ -427,35 +411,22 @@ static __device__ void prepare_joint( const b2gDevWorld& W, int t, const b2gStep
 	const float4* centers = (const float4*)W.centers;
 	int a = j->bodyIdA, b = j->bodyIdB;
 	float4 ma = mass[a], mb = mass[b];
-	j->invMassA = ma.y;
-	j->invMassB = mb.y;
-	j->invIA = ma.w;
-	j->invIB = mb.w;
-	j->indexA = ( W.bodyInfo[a] & B2G_B_AWAKE ) ? a : -1;
-	j->indexB = ( W.bodyInfo[b] & B2G_B_AWAKE ) ? b : -1;
 	float4 xa = xf[a], xb = xf[b];
 	float4 ca = centers[a], cb = centers[b];
-	b2gRot qA = grot( xa.z, xa.w ), qB = grot( xb.z, xb.w );
-	j->anchorA = grotate( qA, gsub( j->localAnchorA, gv( ca.z, ca.w ) ) );
-	j->anchorB = grotate( qB, gsub( j->localAnchorB, gv( cb.z, cb.w ) ) );
-	j->deltaCenter = gsub( gv( cb.x, cb.y ), gv( ca.x, ca.y ) );
-	j->deltaAngle = rel_angle( qB, qA ) - j->referenceAngle;
-	j->deltaAngle = unwind( j->deltaAngle );
-	float k = j->invIA + j->invIB;
-	j->axialMass = k > 0.0f ? 1.0f / k : 0.0f;
-	float s[3];
-	make_soft( j->hertz, j->dampingRatio, sc.h, s );
-	j->springBias = s[0];
-	j->springMass = s[1];
-	j->springImpulseScale = s[2];
-	if ( sc.enableWarmStarting == 0 )
-	{
-		j->linearImpulse = gv( 0.0f, 0.0f );
-		j->springImpulse = 0.0f;
-		j->motorImpulse = 0.0f;
-		j->lowerImpulse = 0.0f;
-		j->upperImpulse = 0.0f;
-	}
+	j->indexA = ( W.bodyInfo[a] & B2G_B_AWAKE ) ? a : -1;
+	j->indexB = ( W.bodyInfo[b] & B2G_B_AWAKE ) ? b : -1;
+	JointBodies jb;
+	jb.mA = ma.y;
+	jb.iA = ma.w;
+	jb.mB = mb.y;
+	jb.iB = mb.w;
+	jb.qA = grot( xa.z, xa.w );
+	jb.qB = grot( xb.z, xb.w );
+	jb.cA = gv( ca.x, ca.y );
+	jb.cB = gv( cb.x, cb.y );
+	jb.lcA = gv( ca.z, ca.w );
+	jb.lcB = gv( cb.z, cb.w );
+	joint_prepare( j, jb, sc );
 }
 
 template <class Bodies>

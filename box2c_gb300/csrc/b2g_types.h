@@ -132,23 +132,55 @@ typedef struct b2gRecord
 	float pose2[4];
 } b2gRecord;
 
-/* Revolute joint configuration (host-owned) and solver state (device-owned),
- * reference src/joint.h:161-190 and src/revolute_joint.c:201-470. */
+/* Joint types, numbered as the reference's b2JointType (include/box2d/types.h:446-455). */
+enum
+{
+	B2G_J_DISTANCE = 0,
+	B2G_J_MOTOR = 1,
+	B2G_J_MOUSE = 2,
+	B2G_J_PRISMATIC = 3,
+	B2G_J_REVOLUTE = 4,
+	B2G_J_WELD = 5,
+	B2G_J_WHEEL = 6,
+};
+
+/* One joint of any type: configuration (host-owned) and solver state (device-owned).
+ * The reference keeps a union of per-type structs (src/joint.h:56-263); this record is
+ * their union by meaning, one field per quantity, so every type is one 256-byte record
+ * and one code path loads it.  Fields a type does not use stay zero. */
 typedef struct b2gJointDev
 {
 	int32_t bodyIdA, bodyIdB;
-	int32_t indexA, indexB;
-	b2gVec localAnchorA, localAnchorB;
-	float hertz, dampingRatio, maxMotorTorque, motorSpeed, referenceAngle, lowerAngle, upperAngle;
+	int32_t indexA, indexB; /* awake body ids, -1 for a body that is not awake */
+	int32_t type;			/* b2JointType */
 	int32_t enableSpring, enableMotor, enableLimit;
+	b2gVec localAnchorA, localAnchorB;
+	b2gVec localAxisA; /* prismatic, wheel: unit axis in body A's frame */
+	b2gVec target;	   /* mouse: target point (targetA); motor: linear offset */
+	float hertz, dampingRatio; /* spring (revolute, prismatic, wheel, distance); linear softness (weld, mouse) */
+	float angularHertz, angularDampingRatio; /* weld */
+	float maxMotor;		  /* revolute, wheel: max motor torque; prismatic, distance: max motor force; motor, mouse: max force */
+	float maxTorque;	  /* motor joint */
+	float motorSpeed;
+	float referenceAngle; /* revolute, prismatic, weld; motor joint: angular offset */
+	float lower, upper;	  /* limits: angles (revolute), translations (prismatic, wheel), lengths (distance) */
+	float length;		  /* distance */
+	float correctionFactor; /* motor joint */
 
 	/* solver state */
 	float invMassA, invMassB, invIA, invIB;
-	b2gVec linearImpulse;
+	b2gVec linearImpulse; /* point constraint (revolute, weld, motor, mouse); prismatic: (perpendicular, angular) */
+	float impulse;		  /* distance: spring or rigid impulse */
+	float perpImpulse;	  /* wheel: point-to-line impulse */
+	float angularImpulse; /* weld, motor, mouse */
 	float springImpulse, motorImpulse, lowerImpulse, upperImpulse;
-	b2gVec anchorA, anchorB, deltaCenter;
-	float deltaAngle, axialMass;
-	float springBias, springMass, springImpulseScale;
+	b2gVec anchorA, anchorB, deltaCenter, axisA;
+	float deltaAngle;
+	float axialMass; /* motor joint: its angular mass */
+	float perpMass, motorMass; /* wheel */
+	float linearMass[4]; /* motor, mouse: inverse of K as cx.x cx.y cy.x cy.y */
+	float springSoft[3]; /* biasRate massScale impulseScale: spring; weld and mouse: linear softness */
+	float angularSoft[3]; /* weld, mouse */
 	int32_t pad;
 } b2gJointDev;
 

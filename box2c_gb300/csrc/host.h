@@ -346,6 +346,12 @@ void gtape_free( gWorld* w );
 void gcontact_create( gWorld* w, gShape* a, gShape* b );
 void gcontact_destroy( gWorld* w, gContact* c );
 int gassign_joint_color( gWorld* w, int bodyIdA, int bodyIdB, bool staticA, bool staticB );
+
+/* Joints (world.c: the record shared by every type; joint.c: the per-type API). */
+b2gJointDev* gjoint_create( b2WorldId worldId, b2BodyId bodyIdA, b2BodyId bodyIdB, b2JointType type, bool collideConnected,
+							void* userData, b2JointId* out );
+void gjoint_disconnect_bodies( gWorld* w, int bodyIdA, int bodyIdB );
+void gworld_ensure_joint_mirror( gWorld* w );
 void gbuffer_move( gWorld* w, int proxyKey );
 
 b2gBox gshape_geo_aabb( const b2gShapeGeo* g, b2gXf xf );

@@ -6,12 +6,12 @@
  * contact creation     src/contact.c:185-332 (sim part)           k_scatter_contacts
  * narrowphase          src/world.c:290-365, src/contact.c:493-582 k_collide
  * prepare contacts     src/contact_solver.c:21-147, :597-808       k_prepare
- * prepare joints       src/revolute_joint.c:201-270                k_prepare_joints
+ * prepare joints       src/joint.c:983-1018 (b2g_joints.h)        k_prepare_joints
  * integrate velocities src/solver.c:34-93                          k_integrate_velocities
  * warm start / solve / relax / restitution
  *                      src/contact_solver.c:149-440 (overflow)     k_overflow (serial)
  *                      src/contact_solver.c:810-1178 (8-lane)      k_color (one colour)
- *                      src/revolute_joint.c:272-470                (joints inside both)
+ *                      src/joint.c:1028-1108 (b2g_joints.h)       (joints inside both)
  * integrate positions  src/solver.c:146-163                        k_integrate_positions
  * store impulses       src/contact_solver.c:442-471, :1180-1293    k_store
  * finalize bodies      src/solver.c:165-351 (+ fast-body sweep

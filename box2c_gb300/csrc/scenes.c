@@ -1015,3 +1015,637 @@ b2WorldId b2s_event_scene( int count, uint64_t seed )
 	}
 	return worldId;
 }
+
+/* One copy of the joint scene at x offset x0 on the shared static ground. */
+static void b2s_zoo_copy( b2WorldId worldId, b2BodyId groundId, float x0, int flags, b2sRandom* rng )
+{
+	bool collide = ( flags & 1 ) != 0;
+	b2ShapeDef sd = b2DefaultShapeDef();
+	b2BodyDef bd = b2DefaultBodyDef();
+	bd.type = b2_dynamicBody;
+	b2BodyDef sb = b2DefaultBodyDef();
+
+	/* distance rope: six circles from a static pin, alternating soft-with-limits, rigid,
+	 * and motorised links */
+	{
+		sb.position = ( b2Vec2 ){ x0 - 15.0f, 12.0f };
+		b2BodyId pin = b2CreateBody( worldId, &sb );
+		b2Circle ball = { { 0.0f, 0.0f }, 0.25f };
+		b2BodyId prev = pin;
+		for ( int i = 0; i < 6; ++i )
+		{
+			bd.position = ( b2Vec2 ){ x0 - 15.0f + 1.0f * ( i + 1 ), 12.0f - 0.2f * ( i + 1 ) };
+			b2BodyId link = b2CreateBody( worldId, &bd );
+			b2CreateCircleShape( link, &sd, &ball );
+			b2DistanceJointDef dj = b2DefaultDistanceJointDef();
+			dj.bodyIdA = prev;
+			dj.bodyIdB = link;
+			dj.length = 1.0f;
+			dj.collideConnected = collide;
+			if ( i % 3 == 0 )
+			{
+				dj.enableSpring = true;
+				dj.hertz = 3.0f;
+				dj.dampingRatio = 0.4f;
+				dj.enableLimit = true;
+				dj.minLength = 0.8f;
+				dj.maxLength = 1.25f;
+			}
+			else if ( i % 3 == 2 )
+			{
+				dj.enableSpring = true;
+				dj.hertz = 2.0f;
+				dj.dampingRatio = 0.2f;
+				dj.enableMotor = true;
+				dj.maxMotorForce = 20.0f;
+				dj.motorSpeed = 0.5f;
+			}
+			b2CreateDistanceJoint( worldId, &dj );
+			prev = link;
+		}
+	}
+
+	/* revolute pendulum with spring, limits and motor */
+	{
+		sb.position = ( b2Vec2 ){ x0 - 3.0f, 8.0f };
+		b2BodyId pin = b2CreateBody( worldId, &sb );
+		bd.position = ( b2Vec2 ){ x0 - 1.5f, 8.0f };
+		b2BodyId bob = b2CreateBody( worldId, &bd );
+		b2Polygon box = b2MakeBox( 1.5f, 0.2f );
+		b2CreatePolygonShape( bob, &sd, &box );
+		b2RevoluteJointDef rj = b2DefaultRevoluteJointDef();
+		rj.bodyIdA = pin;
+		rj.bodyIdB = bob;
+		rj.localAnchorB = ( b2Vec2 ){ -1.5f, 0.0f };
+		rj.enableSpring = true;
+		rj.hertz = 1.0f;
+		rj.dampingRatio = 0.3f;
+		rj.enableLimit = true;
+		rj.lowerAngle = -0.4f * b2_pi;
+		rj.upperAngle = 0.25f * b2_pi;
+		rj.enableMotor = true;
+		rj.maxMotorTorque = 10.0f;
+		rj.motorSpeed = 0.3f;
+		b2CreateRevoluteJoint( worldId, &rj );
+	}
+
+	/* prismatic elevators: a motorised platform with limits, a spring platform on a tilted
+	 * axis, each with a box on top */
+	for ( int k = 0; k < 2; ++k )
+	{
+		float x = x0 + 1.0f + 3.0f * k;
+		bd.position = ( b2Vec2 ){ x, 1.0f };
+		b2BodyId plat = b2CreateBody( worldId, &bd );
+		b2Polygon slab = b2MakeBox( 1.0f, 0.15f );
+		b2CreatePolygonShape( plat, &sd, &slab );
+		b2PrismaticJointDef pj = b2DefaultPrismaticJointDef();
+		pj.bodyIdA = groundId;
+		pj.bodyIdB = plat;
+		pj.localAnchorA = ( b2Vec2 ){ x, 1.0f };
+		pj.localAxisA = k == 0 ? ( b2Vec2 ){ 0.0f, 1.0f } : ( b2Vec2 ){ 0.3f, 1.0f };
+		pj.collideConnected = collide;
+		if ( k == 0 )
+		{
+			pj.enableLimit = true;
+			pj.lowerTranslation = -0.5f;
+			pj.upperTranslation = 3.0f;
+			pj.enableMotor = true;
+			pj.maxMotorForce = 300.0f;
+			pj.motorSpeed = 1.0f;
+		}
+		else
+		{
+			pj.enableSpring = true;
+			pj.hertz = 2.0f;
+			pj.dampingRatio = 0.5f;
+			pj.enableLimit = true;
+			pj.lowerTranslation = -0.75f;
+			pj.upperTranslation = 2.0f;
+		}
+		b2CreatePrismaticJoint( worldId, &pj );
+		bd.position = ( b2Vec2 ){ x + 0.2f, 1.6f };
+		b2BodyId cargo = b2CreateBody( worldId, &bd );
+		b2Polygon cbox = b2MakeBox( 0.4f, 0.4f );
+		b2CreatePolygonShape( cargo, &sd, &cbox );
+	}
+
+	/* wheel car: chassis, two wheels on sprung axles with travel limits, rear motor */
+	{
+		float cx = x0 + 8.0f;
+		bd.position = ( b2Vec2 ){ cx, 1.2f };
+		b2BodyId chassis = b2CreateBody( worldId, &bd );
+		b2Polygon body = b2MakeBox( 1.2f, 0.25f );
+		b2CreatePolygonShape( chassis, &sd, &body );
+		b2Circle tire = { { 0.0f, 0.0f }, 0.4f };
+		b2ShapeDef wsd = b2DefaultShapeDef();
+		wsd.friction = 1.5f;
+		for ( int k = 0; k < 2; ++k )
+		{
+			float wx = cx + ( k == 0 ? -0.9f : 0.9f );
+			bd.position = ( b2Vec2 ){ wx, 0.5f };
+			b2BodyId wheel = b2CreateBody( worldId, &bd );
+			b2CreateCircleShape( wheel, &wsd, &tire );
+			b2WheelJointDef wj = b2DefaultWheelJointDef();
+			wj.bodyIdA = chassis;
+			wj.bodyIdB = wheel;
+			wj.localAnchorA = ( b2Vec2 ){ k == 0 ? -0.9f : 0.9f, -0.7f };
+			wj.hertz = 5.0f;
+			wj.dampingRatio = 0.7f;
+			wj.enableLimit = true;
+			wj.lowerTranslation = -0.25f;
+			wj.upperTranslation = 0.25f;
+			wj.enableMotor = k == 0;
+			wj.maxMotorTorque = 15.0f;
+			wj.motorSpeed = -3.0f;
+			b2CreateWheelJoint( worldId, &wj );
+		}
+	}
+
+	/* weld cantilever: five planks from a static wall, rigid and soft welds in turn */
+	{
+		sb.position = ( b2Vec2 ){ x0 + 12.0f, 6.0f };
+		b2BodyId wall = b2CreateBody( worldId, &sb );
+		b2Polygon post = b2MakeBox( 0.25f, 0.5f );
+		b2CreatePolygonShape( wall, &sd, &post );
+		b2Polygon plank = b2MakeBox( 0.5f, 0.125f );
+		b2BodyId prev = wall;
+		float prevHalf = 0.25f;
+		for ( int i = 0; i < 5; ++i )
+		{
+			bd.position = ( b2Vec2 ){ x0 + 12.0f + 0.25f + 0.5f + 1.0f * i, 6.0f };
+			b2BodyId p = b2CreateBody( worldId, &bd );
+			b2CreatePolygonShape( p, &sd, &plank );
+			b2WeldJointDef wj = b2DefaultWeldJointDef();
+			wj.bodyIdA = prev;
+			wj.bodyIdB = p;
+			wj.localAnchorA = ( b2Vec2 ){ prevHalf, 0.0f };
+			wj.localAnchorB = ( b2Vec2 ){ -0.5f, 0.0f };
+			wj.referenceAngle = i == 2 ? 0.05f : 0.0f;
+			if ( i & 1 )
+			{
+				wj.linearHertz = 6.0f;
+				wj.linearDampingRatio = 0.7f;
+				wj.angularHertz = 3.0f;
+				wj.angularDampingRatio = 0.5f;
+			}
+			b2CreateWeldJoint( worldId, &wj );
+			prev = p;
+			prevHalf = 0.5f;
+		}
+	}
+
+	/* motor joint: a box held at a moving offset from the ground with limited force */
+	{
+		bd.position = ( b2Vec2 ){ x0 + 19.0f, 2.0f };
+		b2BodyId b = b2CreateBody( worldId, &bd );
+		b2Polygon box = b2MakeBox( 0.5f, 0.5f );
+		b2CreatePolygonShape( b, &sd, &box );
+		b2MotorJointDef mj = b2DefaultMotorJointDef();
+		mj.bodyIdA = groundId;
+		mj.bodyIdB = b;
+		mj.linearOffset = ( b2Vec2 ){ x0 + 19.0f, 3.0f };
+		mj.angularOffset = 0.5f;
+		mj.maxForce = 200.0f;
+		mj.maxTorque = 40.0f;
+		mj.correctionFactor = 0.3f;
+		mj.collideConnected = true;
+		b2CreateMotorJoint( worldId, &mj );
+	}
+
+	/* mouse joint: a circle pulled toward a target above and to the side */
+	{
+		bd.position = ( b2Vec2 ){ x0 - 8.0f, 0.6f };
+		b2BodyId b = b2CreateBody( worldId, &bd );
+		b2Circle c = { { 0.0f, 0.0f }, 0.5f };
+		b2CreateCircleShape( b, &sd, &c );
+		b2MouseJointDef mj = b2DefaultMouseJointDef();
+		mj.bodyIdA = groundId;
+		mj.bodyIdB = b;
+		mj.target = ( b2Vec2 ){ x0 - 6.0f, 5.0f };
+		mj.hertz = 3.0f;
+		mj.dampingRatio = 0.7f;
+		mj.maxForce = 60.0f;
+		b2CreateMouseJoint( worldId, &mj );
+	}
+
+	/* spider: a hub box with fourteen legs of every joint type, so that the hub's
+	 * constraints overflow the eleven graph colours */
+	{
+		float hx = x0 - 11.0f;
+		bd.position = ( b2Vec2 ){ hx, 4.0f };
+		b2BodyId hub = b2CreateBody( worldId, &bd );
+		b2Polygon hubBox = b2MakeBox( 0.6f, 0.6f );
+		b2CreatePolygonShape( hub, &sd, &hubBox );
+		b2Polygon leg = b2MakeBox( 0.2f, 0.1f );
+		for ( int k = 0; k < 14; ++k )
+		{
+			b2Vec2 u = b2s_circle_point( -1.0f + 2.0f * ( k + 0.5f ) / 14.0f );
+			b2Vec2 at = { hx + 1.6f * u.x, 4.0f + 1.6f * u.y };
+			bd.position = at;
+			b2BodyId l = b2CreateBody( worldId, &bd );
+			b2CreatePolygonShape( l, &sd, &leg );
+			b2Vec2 anchor = { 0.6f * u.x, 0.6f * u.y };
+			switch ( k % 7 )
+			{
+				case 0:
+				{
+					b2DistanceJointDef j = b2DefaultDistanceJointDef();
+					j.bodyIdA = hub;
+					j.bodyIdB = l;
+					j.localAnchorA = anchor;
+					j.length = 1.0f;
+					j.enableSpring = true;
+					j.hertz = 4.0f;
+					j.dampingRatio = 0.5f;
+					b2CreateDistanceJoint( worldId, &j );
+					break;
+				}
+				case 1:
+				{
+					b2RevoluteJointDef j = b2DefaultRevoluteJointDef();
+					j.bodyIdA = hub;
+					j.bodyIdB = l;
+					j.localAnchorA = anchor;
+					j.localAnchorB = ( b2Vec2 ){ -1.0f * u.x, -1.0f * u.y };
+					j.enableLimit = true;
+					j.lowerAngle = -0.25f;
+					j.upperAngle = 0.25f;
+					b2CreateRevoluteJoint( worldId, &j );
+					break;
+				}
+				case 2:
+				{
+					b2PrismaticJointDef j = b2DefaultPrismaticJointDef();
+					j.bodyIdA = hub;
+					j.bodyIdB = l;
+					j.localAnchorA = anchor;
+					j.localAnchorB = ( b2Vec2 ){ -1.0f * u.x, -1.0f * u.y };
+					j.localAxisA = u;
+					j.enableSpring = true;
+					j.hertz = 3.0f;
+					j.dampingRatio = 0.6f;
+					j.enableLimit = true;
+					j.lowerTranslation = -0.3f;
+					j.upperTranslation = 0.3f;
+					b2CreatePrismaticJoint( worldId, &j );
+					break;
+				}
+				case 3:
+				{
+					b2WheelJointDef j = b2DefaultWheelJointDef();
+					j.bodyIdA = hub;
+					j.bodyIdB = l;
+					j.localAnchorA = anchor;
+					j.localAnchorB = ( b2Vec2 ){ -1.0f * u.x, -1.0f * u.y };
+					j.localAxisA = u;
+					j.enableMotor = true;
+					j.maxMotorTorque = 2.0f;
+					j.motorSpeed = 1.0f;
+					b2CreateWheelJoint( worldId, &j );
+					break;
+				}
+				case 4:
+				{
+					b2WeldJointDef j = b2DefaultWeldJointDef();
+					j.bodyIdA = hub;
+					j.bodyIdB = l;
+					j.localAnchorA = anchor;
+					j.localAnchorB = ( b2Vec2 ){ -1.0f * u.x, -1.0f * u.y };
+					j.linearHertz = 8.0f;
+					j.linearDampingRatio = 1.0f;
+					j.angularHertz = 4.0f;
+					j.angularDampingRatio = 1.0f;
+					b2CreateWeldJoint( worldId, &j );
+					break;
+				}
+				case 5:
+				{
+					b2MotorJointDef j = b2DefaultMotorJointDef();
+					j.bodyIdA = hub;
+					j.bodyIdB = l;
+					j.linearOffset = ( b2Vec2 ){ 1.6f * u.x, 1.6f * u.y };
+					j.maxForce = 50.0f;
+					j.maxTorque = 5.0f;
+					b2CreateMotorJoint( worldId, &j );
+					break;
+				}
+				default:
+				{
+					b2MouseJointDef j = b2DefaultMouseJointDef();
+					j.bodyIdA = hub;
+					j.bodyIdB = l;
+					j.target = ( b2Vec2 ){ at.x + 0.5f * u.x, at.y + 0.5f * u.y };
+					j.hertz = 5.0f;
+					j.dampingRatio = 0.8f;
+					j.maxForce = 30.0f;
+					b2CreateMouseJoint( worldId, &j );
+					break;
+				}
+			}
+		}
+	}
+
+	/* debris: seeded boxes and circles dropped over the mechanisms */
+	for ( int k = 0; k < 12; ++k )
+	{
+		bd.position = ( b2Vec2 ){ x0 + b2s_uniform( rng, -16.0f, 20.0f ), b2s_uniform( rng, 8.0f, 14.0f ) };
+		b2BodyId d = b2CreateBody( worldId, &bd );
+		if ( k & 1 )
+		{
+			b2Circle c = { { 0.0f, 0.0f }, b2s_uniform( rng, 0.15f, 0.35f ) };
+			b2CreateCircleShape( d, &sd, &c );
+		}
+		else
+		{
+			b2Polygon p = b2MakeBox( b2s_uniform( rng, 0.15f, 0.4f ), b2s_uniform( rng, 0.15f, 0.4f ) );
+			b2CreatePolygonShape( d, &sd, &p );
+		}
+	}
+}
+
+b2WorldId b2s_joint_zoo( int copies, int flags, uint64_t seed )
+{
+	b2WorldDef wd = b2s_world_def();
+	b2WorldId worldId = b2CreateWorld( &wd );
+	if ( B2_IS_NULL( worldId ) )
+		return worldId;
+	b2BodyDef gd = b2DefaultBodyDef();
+	b2BodyId groundId = b2CreateBody( worldId, &gd );
+	b2ShapeDef gsd = b2DefaultShapeDef();
+	float half = 20.0f * copies + 10.0f;
+	b2Polygon groundBox = b2MakeOffsetBox( half, 0.5f, ( b2Vec2 ){ 40.0f * 0.5f * ( copies - 1 ), -0.5f }, 0.0f );
+	b2CreatePolygonShape( groundId, &gsd, &groundBox );
+
+	b2sRandom rng;
+	b2s_seed( &rng, seed );
+	for ( int i = 0; i < copies; ++i )
+		b2s_zoo_copy( worldId, groundId, 40.0f * i, flags, &rng );
+	return worldId;
+}
+
+/* Records a float into the script's output. */
+static void b2s_put( float* out, int capacity, int* n, float v )
+{
+	if ( *n < capacity )
+		out[*n] = v;
+	*n += 1;
+}
+
+static void b2s_put_vec( float* out, int capacity, int* n, b2Vec2 v )
+{
+	b2s_put( out, capacity, n, v.x );
+	b2s_put( out, capacity, n, v.y );
+}
+
+/* Reads back every joint's configuration, its reaction force and torque, and the
+ * type-specific queries. */
+static void b2s_joint_readout( b2JointId* j, float* out, int capacity, int* n )
+{
+	for ( int k = 0; k < 7; ++k )
+	{
+		b2s_put( out, capacity, n, (float)b2Joint_GetType( j[k] ) );
+		b2s_put_vec( out, capacity, n, b2Joint_GetLocalAnchorA( j[k] ) );
+		b2s_put_vec( out, capacity, n, b2Joint_GetLocalAnchorB( j[k] ) );
+		b2s_put( out, capacity, n, b2Joint_GetCollideConnected( j[k] ) ? 1.0f : 0.0f );
+		b2s_put_vec( out, capacity, n, b2Joint_GetConstraintForce( j[k] ) );
+		b2s_put( out, capacity, n, b2Joint_GetConstraintTorque( j[k] ) );
+	}
+	b2JointId d = j[0];
+	b2s_put( out, capacity, n, b2DistanceJoint_GetLength( d ) );
+	b2s_put( out, capacity, n, b2DistanceJoint_IsSpringEnabled( d ) );
+	b2s_put( out, capacity, n, b2DistanceJoint_GetHertz( d ) );
+	b2s_put( out, capacity, n, b2DistanceJoint_GetDampingRatio( d ) );
+	b2s_put( out, capacity, n, b2DistanceJoint_IsLimitEnabled( d ) );
+	b2s_put( out, capacity, n, b2DistanceJoint_GetMinLength( d ) );
+	b2s_put( out, capacity, n, b2DistanceJoint_GetMaxLength( d ) );
+	b2s_put( out, capacity, n, b2DistanceJoint_GetCurrentLength( d ) );
+	b2s_put( out, capacity, n, b2DistanceJoint_IsMotorEnabled( d ) );
+	b2s_put( out, capacity, n, b2DistanceJoint_GetMotorSpeed( d ) );
+	b2s_put( out, capacity, n, b2DistanceJoint_GetMaxMotorForce( d ) );
+	b2s_put( out, capacity, n, b2DistanceJoint_GetMotorForce( d ) );
+	b2JointId m = j[1];
+	b2s_put_vec( out, capacity, n, b2MotorJoint_GetLinearOffset( m ) );
+	b2s_put( out, capacity, n, b2MotorJoint_GetAngularOffset( m ) );
+	b2s_put( out, capacity, n, b2MotorJoint_GetMaxForce( m ) );
+	b2s_put( out, capacity, n, b2MotorJoint_GetMaxTorque( m ) );
+	b2s_put( out, capacity, n, b2MotorJoint_GetCorrectionFactor( m ) );
+	b2JointId o = j[2];
+	b2s_put_vec( out, capacity, n, b2MouseJoint_GetTarget( o ) );
+	b2s_put( out, capacity, n, b2MouseJoint_GetSpringHertz( o ) );
+	b2s_put( out, capacity, n, b2MouseJoint_GetSpringDampingRatio( o ) );
+	b2s_put( out, capacity, n, b2MouseJoint_GetMaxForce( o ) );
+	b2JointId p = j[3];
+	b2s_put( out, capacity, n, b2PrismaticJoint_IsSpringEnabled( p ) );
+	b2s_put( out, capacity, n, b2PrismaticJoint_GetSpringHertz( p ) );
+	b2s_put( out, capacity, n, b2PrismaticJoint_GetSpringDampingRatio( p ) );
+	b2s_put( out, capacity, n, b2PrismaticJoint_IsLimitEnabled( p ) );
+	b2s_put( out, capacity, n, b2PrismaticJoint_GetLowerLimit( p ) );
+	b2s_put( out, capacity, n, b2PrismaticJoint_GetUpperLimit( p ) );
+	b2s_put( out, capacity, n, b2PrismaticJoint_IsMotorEnabled( p ) );
+	b2s_put( out, capacity, n, b2PrismaticJoint_GetMotorSpeed( p ) );
+	b2s_put( out, capacity, n, b2PrismaticJoint_GetMaxMotorForce( p ) );
+	b2s_put( out, capacity, n, b2PrismaticJoint_GetMotorForce( p ) );
+	b2JointId r = j[4];
+	b2s_put( out, capacity, n, b2RevoluteJoint_GetSpringHertz( r ) );
+	b2s_put( out, capacity, n, b2RevoluteJoint_GetSpringDampingRatio( r ) );
+	b2s_put( out, capacity, n, b2RevoluteJoint_GetAngle( r ) );
+	b2s_put( out, capacity, n, b2RevoluteJoint_IsLimitEnabled( r ) );
+	b2s_put( out, capacity, n, b2RevoluteJoint_GetLowerLimit( r ) );
+	b2s_put( out, capacity, n, b2RevoluteJoint_GetUpperLimit( r ) );
+	b2s_put( out, capacity, n, b2RevoluteJoint_IsMotorEnabled( r ) );
+	b2s_put( out, capacity, n, b2RevoluteJoint_GetMotorSpeed( r ) );
+	b2s_put( out, capacity, n, b2RevoluteJoint_GetMotorTorque( r ) );
+	b2s_put( out, capacity, n, b2RevoluteJoint_GetMaxMotorTorque( r ) );
+	b2JointId w = j[5];
+	b2s_put( out, capacity, n, b2WeldJoint_GetLinearHertz( w ) );
+	b2s_put( out, capacity, n, b2WeldJoint_GetLinearDampingRatio( w ) );
+	b2s_put( out, capacity, n, b2WeldJoint_GetAngularHertz( w ) );
+	b2s_put( out, capacity, n, b2WeldJoint_GetAngularDampingRatio( w ) );
+	b2JointId h = j[6];
+	b2s_put( out, capacity, n, b2WheelJoint_IsSpringEnabled( h ) );
+	b2s_put( out, capacity, n, b2WheelJoint_GetSpringHertz( h ) );
+	b2s_put( out, capacity, n, b2WheelJoint_GetSpringDampingRatio( h ) );
+	b2s_put( out, capacity, n, b2WheelJoint_IsLimitEnabled( h ) );
+	b2s_put( out, capacity, n, b2WheelJoint_GetLowerLimit( h ) );
+	b2s_put( out, capacity, n, b2WheelJoint_GetUpperLimit( h ) );
+	b2s_put( out, capacity, n, b2WheelJoint_IsMotorEnabled( h ) );
+	b2s_put( out, capacity, n, b2WheelJoint_GetMotorSpeed( h ) );
+	b2s_put( out, capacity, n, b2WheelJoint_GetMaxMotorTorque( h ) );
+	b2s_put( out, capacity, n, b2WheelJoint_GetMotorTorque( h ) );
+}
+
+int b2s_joint_api_script( float* out, int capacity )
+{
+	int n = 0;
+	b2WorldDef wd = b2s_world_def();
+	b2WorldId worldId = b2CreateWorld( &wd );
+	if ( B2_IS_NULL( worldId ) )
+		return -1;
+	b2BodyDef gd = b2DefaultBodyDef();
+	b2BodyId ground = b2CreateBody( worldId, &gd );
+	b2ShapeDef sd = b2DefaultShapeDef();
+	b2Polygon floor = b2MakeOffsetBox( 30.0f, 0.5f, ( b2Vec2 ){ 0.0f, -0.5f }, 0.0f );
+	b2CreatePolygonShape( ground, &sd, &floor );
+
+	/* seven bodies in a row, each on its own joint to the ground or to its neighbour */
+	b2BodyId body[8];
+	b2BodyDef bd = b2DefaultBodyDef();
+	bd.type = b2_dynamicBody;
+	b2Polygon box = b2MakeBox( 0.4f, 0.3f );
+	for ( int k = 0; k < 8; ++k )
+	{
+		bd.position = ( b2Vec2 ){ -10.0f + 3.0f * k, 1.0f + 0.5f * ( k & 1 ) };
+		body[k] = b2CreateBody( worldId, &bd );
+		b2CreatePolygonShape( body[k], &sd, &box );
+	}
+	b2JointId j[7];
+	b2DistanceJointDef dj = b2DefaultDistanceJointDef();
+	dj.bodyIdA = ground;
+	dj.bodyIdB = body[0];
+	dj.localAnchorA = ( b2Vec2 ){ -10.0f, 4.0f };
+	dj.localAnchorB = ( b2Vec2 ){ 0.2f, 0.1f };
+	dj.length = 2.5f;
+	dj.enableSpring = true;
+	dj.hertz = 2.0f;
+	dj.dampingRatio = 0.3f;
+	dj.enableLimit = true;
+	dj.minLength = 2.0f;
+	dj.maxLength = 3.0f;
+	j[0] = b2CreateDistanceJoint( worldId, &dj );
+	b2MotorJointDef mj = b2DefaultMotorJointDef();
+	mj.bodyIdA = body[0];
+	mj.bodyIdB = body[1];
+	mj.linearOffset = ( b2Vec2 ){ 3.0f, 0.5f };
+	mj.angularOffset = 0.3f;
+	mj.maxForce = 100.0f;
+	mj.maxTorque = 20.0f;
+	mj.correctionFactor = 1.5f;
+	j[1] = b2CreateMotorJoint( worldId, &mj );
+	b2MouseJointDef oj = b2DefaultMouseJointDef();
+	oj.bodyIdA = ground;
+	oj.bodyIdB = body[2];
+	oj.target = ( b2Vec2 ){ -3.5f, 3.0f };
+	oj.maxForce = 50.0f;
+	j[2] = b2CreateMouseJoint( worldId, &oj );
+	b2PrismaticJointDef pj = b2DefaultPrismaticJointDef();
+	pj.bodyIdA = ground;
+	pj.bodyIdB = body[3];
+	pj.localAnchorA = ( b2Vec2 ){ -1.0f, 1.5f };
+	pj.localAxisA = ( b2Vec2 ){ 1.0f, 2.0f };
+	pj.enableLimit = true;
+	pj.lowerTranslation = 1.0f;
+	pj.upperTranslation = -0.5f;
+	pj.enableMotor = true;
+	pj.maxMotorForce = 80.0f;
+	pj.motorSpeed = 0.7f;
+	j[3] = b2CreatePrismaticJoint( worldId, &pj );
+	b2RevoluteJointDef rj = b2DefaultRevoluteJointDef();
+	rj.bodyIdA = body[3];
+	rj.bodyIdB = body[4];
+	rj.localAnchorA = ( b2Vec2 ){ 1.5f, 0.25f };
+	rj.localAnchorB = ( b2Vec2 ){ -1.5f, 0.0f };
+	rj.referenceAngle = 4.0f;
+	rj.enableLimit = true;
+	rj.lowerAngle = 0.5f;
+	rj.upperAngle = -0.5f;
+	rj.enableSpring = true;
+	rj.hertz = 1.5f;
+	rj.dampingRatio = 0.2f;
+	j[4] = b2CreateRevoluteJoint( worldId, &rj );
+	b2WeldJointDef wj = b2DefaultWeldJointDef();
+	wj.bodyIdA = body[4];
+	wj.bodyIdB = body[5];
+	wj.localAnchorA = ( b2Vec2 ){ 1.5f, -0.25f };
+	wj.localAnchorB = ( b2Vec2 ){ -1.5f, 0.0f };
+	wj.angularHertz = 2.0f;
+	wj.angularDampingRatio = 0.1f;
+	j[5] = b2CreateWeldJoint( worldId, &wj );
+	b2WheelJointDef hj = b2DefaultWheelJointDef();
+	hj.bodyIdA = body[6];
+	hj.bodyIdB = body[7];
+	hj.localAnchorA = ( b2Vec2 ){ 1.5f, -0.25f };
+	hj.localAnchorB = ( b2Vec2 ){ -1.5f, 0.0f };
+	hj.localAxisA = ( b2Vec2 ){ 0.0f, 3.0f };
+	hj.enableMotor = true;
+	hj.maxMotorTorque = 5.0f;
+	hj.motorSpeed = 2.0f;
+	hj.collideConnected = true;
+	j[6] = b2CreateWheelJoint( worldId, &hj );
+
+	b2s_joint_readout( j, out, capacity, &n );
+	for ( int s = 0; s < 30; ++s )
+		b2World_Step( worldId, 1.0f / 60.0f, 4 );
+	b2s_joint_readout( j, out, capacity, &n );
+
+	/* setters, including those that reset accumulated impulses */
+	b2DistanceJoint_SetLength( j[0], 0.001f );
+	b2DistanceJoint_SetLengthRange( j[0], 3.5f, 1.5f );
+	b2DistanceJoint_EnableMotor( j[0], true );
+	b2DistanceJoint_SetMotorSpeed( j[0], -0.4f );
+	b2DistanceJoint_SetMaxMotorForce( j[0], 30.0f );
+	b2DistanceJoint_SetSpringHertz( j[0], 3.0f );
+	b2DistanceJoint_SetSpringDampingRatio( j[0], 0.6f );
+	b2MotorJoint_SetLinearOffset( j[1], ( b2Vec2 ){ 2.5f, 1.0f } );
+	b2MotorJoint_SetAngularOffset( j[1], 5.0f );
+	b2MotorJoint_SetMaxForce( j[1], -3.0f );
+	b2MotorJoint_SetMaxForce( j[1], 150.0f );
+	b2MotorJoint_SetMaxTorque( j[1], 25.0f );
+	b2MotorJoint_SetCorrectionFactor( j[1], 0.6f );
+	b2MouseJoint_SetTarget( j[2], ( b2Vec2 ){ -2.0f, 4.0f } );
+	b2MouseJoint_SetSpringHertz( j[2], 6.0f );
+	b2MouseJoint_SetSpringDampingRatio( j[2], 0.9f );
+	b2MouseJoint_SetMaxForce( j[2], 70.0f );
+	b2PrismaticJoint_EnableSpring( j[3], true );
+	b2PrismaticJoint_SetSpringHertz( j[3], 2.5f );
+	b2PrismaticJoint_SetSpringDampingRatio( j[3], 0.4f );
+	b2PrismaticJoint_SetLimits( j[3], 2.0f, -1.0f );
+	b2PrismaticJoint_EnableMotor( j[3], false );
+	b2PrismaticJoint_SetMotorSpeed( j[3], -1.0f );
+	b2PrismaticJoint_SetMaxMotorForce( j[3], 60.0f );
+	b2RevoluteJoint_EnableSpring( j[4], false );
+	b2RevoluteJoint_SetSpringHertz( j[4], 2.0f );
+	b2RevoluteJoint_SetSpringDampingRatio( j[4], 0.5f );
+	b2RevoluteJoint_SetLimits( j[4], -4.0f, 4.0f );
+	b2RevoluteJoint_EnableMotor( j[4], true );
+	b2RevoluteJoint_SetMotorSpeed( j[4], 1.0f );
+	b2RevoluteJoint_SetMaxMotorTorque( j[4], 12.0f );
+	b2WeldJoint_SetLinearHertz( j[5], 4.0f );
+	b2WeldJoint_SetLinearDampingRatio( j[5], 0.7f );
+	b2WeldJoint_SetAngularHertz( j[5], 0.0f );
+	b2WeldJoint_SetAngularDampingRatio( j[5], 0.3f );
+	b2WheelJoint_EnableSpring( j[6], false );
+	b2WheelJoint_SetSpringHertz( j[6], 3.0f );
+	b2WheelJoint_SetSpringDampingRatio( j[6], 0.2f );
+	b2WheelJoint_EnableLimit( j[6], true );
+	b2WheelJoint_SetLimits( j[6], 0.3f, -0.3f );
+	b2WheelJoint_SetMotorSpeed( j[6], -2.0f );
+	b2WheelJoint_SetMaxMotorTorque( j[6], 8.0f );
+	b2Joint_SetCollideConnected( j[6], false );
+	b2Joint_SetCollideConnected( j[1], true );
+	b2s_joint_readout( j, out, capacity, &n );
+	for ( int s = 0; s < 30; ++s )
+		b2World_Step( worldId, 1.0f / 60.0f, 4 );
+	b2s_joint_readout( j, out, capacity, &n );
+
+	/* disabling and re-enabling, and destroying a joint mid-run */
+	b2DistanceJoint_EnableLimit( j[0], false );
+	b2DistanceJoint_EnableSpring( j[0], false );
+	b2PrismaticJoint_EnableLimit( j[3], false );
+	b2RevoluteJoint_EnableLimit( j[4], false );
+	b2WheelJoint_EnableMotor( j[6], false );
+	b2Joint_SetCollideConnected( j[1], false );
+	b2DestroyJoint( j[5] );
+	for ( int s = 0; s < 30; ++s )
+		b2World_Step( worldId, 1.0f / 60.0f, 4 );
+	for ( int k = 0; k < 8; ++k )
+	{
+		b2s_put_vec( out, capacity, &n, b2Body_GetPosition( body[k] ) );
+		b2Rot q = b2Body_GetRotation( body[k] );
+		b2s_put( out, capacity, &n, q.c );
+		b2s_put( out, capacity, &n, q.s );
+	}
+	b2s_put( out, capacity, &n, b2Joint_IsValid( j[5] ) ? 1.0f : 0.0f );
+	b2s_put( out, capacity, &n, (float)b2Body_GetJointCount( body[4] ) );
+	b2DestroyWorld( worldId );
+	return n;
+}

@@ -110,6 +110,24 @@ b2BodyId b2s_add_square( b2WorldId worldId, float h );
  * carries a sensor ring of radius 0.8. */
 b2WorldId b2s_event_scene( int count, uint64_t seed );
 
+/* Joint scene with every joint type: `copies` copies 40 m apart on one static ground,
+ * each with a distance-joint rope (soft with length limits, rigid, motorised), a
+ * revolute pendulum (spring, limits, motor), two prismatic elevators (motor and limits;
+ * spring on a tilted axis), a car on two sprung wheel joints with a rear motor, a weld
+ * cantilever (rigid and soft welds), a motor joint and a mouse joint to the ground, a
+ * fourteen-legged spider whose hub joints of every type overflow the graph colours,
+ * and twelve seeded boxes and circles dropped over them.  flags & 1: the rope and
+ * elevator joints let their bodies collide. */
+b2WorldId b2s_joint_zoo( int copies, int flags, uint64_t seed );
+
+/* Joint API script: one joint of each type between a ground and eight boxes; reads
+ * every joint query (configuration, reaction force and torque, type-specific values)
+ * before and after 30 steps, calls every setter (clamping ones with out-of-range values,
+ * impulse-resetting ones, collide-connected toggles), steps and reads again, then
+ * disables features, destroys a joint, steps and reads the bodies.  Writes up to
+ * `capacity` floats to out; returns the number written (-1 without a world). */
+int b2s_joint_api_script( float* out, int capacity );
+
 /* Draws `n` integers uniform in [lo, hi] from `seed` into out. */
 void b2s_draw_ints( int n, uint64_t seed, int lo, int hi, int* out );
 /* Draws `n` floats uniform in [lo, hi) / standard normal from `seed` into out. */

@@ -120,15 +120,6 @@ b2ShapeDef b2DefaultShapeDef( void )
 	return d;
 }
 
-b2RevoluteJointDef b2DefaultRevoluteJointDef( void )
-{
-	b2RevoluteJointDef d;
-	memset( &d, 0, sizeof( d ) );
-	d.drawSize = 0.25f;
-	d.internalValue = 1152023;
-	return d;
-}
-
 /* ------------------------------------------------------------ pinned mirrors */
 static int grow_cap( int have, int need )
 {
@@ -1128,16 +1119,22 @@ int gassign_joint_color( gWorld* w, int bodyIdA, int bodyIdB, bool staticA, bool
 	return B2G_OVERFLOW;
 }
 
-b2JointId b2CreateRevoluteJoint( b2WorldId worldId, const b2RevoluteJointDef* def )
+/* Joint record shared by every joint type (reference src/joint.c:140-288): allocates the
+ * id, links the joint into both bodies' joint lists and puts it in the constraint graph.
+ * Returns the joint's zeroed device record with its type and bodies set, or NULL when the
+ * world or a body is invalid, the world is locked, or host memory ran out. */
+b2gJointDev* gjoint_create( b2WorldId worldId, b2BodyId bodyIdA, b2BodyId bodyIdB, b2JointType type, bool collideConnected,
+							void* userData, b2JointId* out )
 {
-	if ( b2World_IsValid( worldId ) == false || b2Body_IsValid( def->bodyIdA ) == false || b2Body_IsValid( def->bodyIdB ) == false )
-		return b2_nullJointId;
+	*out = b2_nullJointId;
+	if ( b2World_IsValid( worldId ) == false || b2Body_IsValid( bodyIdA ) == false || b2Body_IsValid( bodyIdB ) == false )
+		return NULL;
 	gWorld* w = gworld_get( worldId );
 	if ( w->locked )
-		return b2_nullJointId;
+		return NULL;
 	ensure_joint_mirror( w );
-	gBody* a = get_body( def->bodyIdA );
-	gBody* b = get_body( def->bodyIdB );
+	gBody* a = get_body( bodyIdA );
+	gBody* b = get_body( bodyIdB );
 	int id = gid_alloc( &w->jointIds );
 	bool ok = true;
 	GROW_RECORDS( w->joints, w->jointCap, id + 1, gJoint, ok );
@@ -1145,18 +1142,18 @@ b2JointId b2CreateRevoluteJoint( b2WorldId worldId, const b2RevoluteJointDef* de
 	{
 		gid_unalloc( &w->jointIds, id );
 		w->status = w->status ? w->status : B2_STATUS_OUT_OF_HOST_MEMORY;
-		return b2_nullJointId;
+		return NULL;
 	}
 	gJoint* j = w->joints + id;
 	uint16_t rev = j->revision;
 	memset( j, 0, sizeof( *j ) );
 	j->id = id;
 	j->revision = (uint16_t)( rev + 1 );
-	j->type = b2_revoluteJoint;
+	j->type = type;
 	j->bodyIdA = a->id;
 	j->bodyIdB = b->id;
-	j->userData = def->userData;
-	j->collideConnected = def->collideConnected;
+	j->userData = userData;
+	j->collideConnected = collideConnected;
 
 	j->edges[0].bodyId = a->id;
 	j->edges[0].prevKey = B2G_NULL;
@@ -1194,58 +1191,47 @@ b2JointId b2CreateRevoluteJoint( b2WorldId worldId, const b2RevoluteJointDef* de
 
 	b2gJointDev* d = w->hJoints + id;
 	memset( d, 0, sizeof( *d ) );
+	d->type = (int32_t)type;
 	d->bodyIdA = a->id;
 	d->bodyIdB = b->id;
-	d->localAnchorA = gv( def->localAnchorA.x, def->localAnchorA.y );
-	d->localAnchorB = gv( def->localAnchorB.x, def->localAnchorB.y );
-	d->referenceAngle = gclamp( def->referenceAngle, -B2G_PI, B2G_PI );
-	d->hertz = def->hertz;
-	d->dampingRatio = def->dampingRatio;
-	d->lowerAngle = gmin( def->lowerAngle, def->upperAngle );
-	d->upperAngle = gmax( def->lowerAngle, def->upperAngle );
-	d->lowerAngle = gclamp( d->lowerAngle, -B2G_PI, B2G_PI );
-	d->upperAngle = gclamp( d->upperAngle, -B2G_PI, B2G_PI );
-	d->maxMotorTorque = def->maxMotorTorque;
-	d->motorSpeed = def->motorSpeed;
-	d->enableSpring = def->enableSpring;
-	d->enableLimit = def->enableLimit;
-	d->enableMotor = def->enableMotor;
+	d->indexA = B2G_NULL;
+	d->indexB = B2G_NULL;
 	w->jointsDirty = true;
-
-	if ( def->collideConnected == false )
-	{
-		int key, other;
-		if ( a->contactCount < b->contactCount )
-		{
-			key = a->headContactKey;
-			other = b->id;
-		}
-		else
-		{
-			key = b->headContactKey;
-			other = a->id;
-		}
-		while ( key != B2G_NULL )
-		{
-			gContact* c = w->contacts + ( key >> 1 );
-			int e = key & 1;
-			key = c->edges[e].nextKey;
-			if ( c->edges[e ^ 1].bodyId == other )
-				gcontact_destroy( w, c );
-		}
-	}
 	b2JointId jid = { id + 1, (uint16_t)w->slot, j->revision };
-	return jid;
+	*out = jid;
+	return d;
 }
+
+/* Destroys the contacts between a joint's two bodies (reference src/joint.c:290-322),
+ * walking the shorter contact list. */
+void gjoint_disconnect_bodies( gWorld* w, int bodyIdA, int bodyIdB )
+{
+	gBody* a = w->bodies + bodyIdA;
+	gBody* b = w->bodies + bodyIdB;
+	int key, other;
+	if ( a->contactCount < b->contactCount )
+	{
+		key = a->headContactKey;
+		other = b->id;
+	}
+	else
+	{
+		key = b->headContactKey;
+		other = a->id;
+	}
+	while ( key != B2G_NULL )
+	{
+		gContact* c = w->contacts + ( key >> 1 );
+		int e = key & 1;
+		key = c->edges[e].nextKey;
+		if ( c->edges[e ^ 1].bodyId == other )
+			gcontact_destroy( w, c );
+	}
+}
+
+void gworld_ensure_joint_mirror( gWorld* w ) { ensure_joint_mirror( w ); }
 
 static gJoint* get_joint( b2JointId id ) { return s_worlds[id.world0]->joints + ( id.index1 - 1 ); }
-static b2gJointDev* joint_config( b2JointId id )
-{
-	gWorld* w = s_worlds[id.world0];
-	ensure_joint_mirror( w );
-	w->jointsDirty = true;
-	return w->hJoints + ( id.index1 - 1 );
-}
 
 bool b2Joint_IsValid( b2JointId id )
 {
@@ -1256,41 +1242,6 @@ bool b2Joint_IsValid( b2JointId id )
 		return false;
 	return w->joints[id.index1 - 1].id == id.index1 - 1 && w->joints[id.index1 - 1].revision == id.revision;
 }
-b2JointType b2Joint_GetType( b2JointId id ) { return get_joint( id )->type; }
-b2BodyId b2Joint_GetBodyA( b2JointId id )
-{
-	gWorld* w = s_worlds[id.world0];
-	gJoint* j = get_joint( id );
-	b2BodyId b = { j->bodyIdA + 1, id.world0, w->bodies[j->bodyIdA].revision };
-	return b;
-}
-b2BodyId b2Joint_GetBodyB( b2JointId id )
-{
-	gWorld* w = s_worlds[id.world0];
-	gJoint* j = get_joint( id );
-	b2BodyId b = { j->bodyIdB + 1, id.world0, w->bodies[j->bodyIdB].revision };
-	return b;
-}
-void b2RevoluteJoint_EnableMotor( b2JointId id, bool f ) { joint_config( id )->enableMotor = f; }
-bool b2RevoluteJoint_IsMotorEnabled( b2JointId id ) { return s_worlds[id.world0]->hJoints[id.index1 - 1].enableMotor != 0; }
-void b2RevoluteJoint_SetMotorSpeed( b2JointId id, float s ) { joint_config( id )->motorSpeed = s; }
-float b2RevoluteJoint_GetMotorSpeed( b2JointId id ) { return s_worlds[id.world0]->hJoints[id.index1 - 1].motorSpeed; }
-void b2RevoluteJoint_SetMaxMotorTorque( b2JointId id, float t ) { joint_config( id )->maxMotorTorque = t; }
-float b2RevoluteJoint_GetMaxMotorTorque( b2JointId id ) { return s_worlds[id.world0]->hJoints[id.index1 - 1].maxMotorTorque; }
-float b2RevoluteJoint_GetMotorTorque( b2JointId id )
-{
-	gWorld* w = s_worlds[id.world0];
-	ensure_joint_mirror( w );
-	return w->inv_h * w->hJoints[id.index1 - 1].motorImpulse;
-}
-void b2RevoluteJoint_EnableLimit( b2JointId id, bool f ) { joint_config( id )->enableLimit = f; }
-void b2RevoluteJoint_SetLimits( b2JointId id, float lower, float upper )
-{
-	b2gJointDev* d = joint_config( id );
-	d->lowerAngle = gclamp( gmin( lower, upper ), -B2G_PI, B2G_PI );
-	d->upperAngle = gclamp( gmax( lower, upper ), -B2G_PI, B2G_PI );
-}
-void b2RevoluteJoint_EnableSpring( b2JointId id, bool f ) { joint_config( id )->enableSpring = f; }
 
 /* ------------------------------------------------------------ introspection */
 int b2World_InspectBodies( b2WorldId worldId, float* out, int capacity )

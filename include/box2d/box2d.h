@@ -91,21 +91,141 @@ B2_API b2Polygon b2Shape_GetPolygon( b2ShapeId shapeId );
 B2_API b2Circle b2Shape_GetCircle( b2ShapeId shapeId );
 B2_API b2AABB b2Shape_GetAABB( b2ShapeId shapeId );
 
-/* Joint (reference box2d.h:605-946); the revolute joint is the one on the step path. */
-B2_API b2JointId b2CreateRevoluteJoint( b2WorldId worldId, const b2RevoluteJointDef* def );
-/* Destroys a joint (reference box2d.h:605). */
+/* Joints: generic (reference box2d.h:605-646). */
 B2_API void b2DestroyJoint( b2JointId jointId );
 B2_API bool b2Joint_IsValid( b2JointId id );
 B2_API b2JointType b2Joint_GetType( b2JointId jointId );
 B2_API b2BodyId b2Joint_GetBodyA( b2JointId jointId );
 B2_API b2BodyId b2Joint_GetBodyB( b2JointId jointId );
+B2_API b2Vec2 b2Joint_GetLocalAnchorA( b2JointId jointId );
+B2_API b2Vec2 b2Joint_GetLocalAnchorB( b2JointId jointId );
+B2_API void b2Joint_SetCollideConnected( b2JointId jointId, bool shouldCollide );
+B2_API bool b2Joint_GetCollideConnected( b2JointId jointId );
+B2_API void b2Joint_SetUserData( b2JointId jointId, void* userData );
+B2_API void* b2Joint_GetUserData( b2JointId jointId );
+B2_API void b2Joint_WakeBodies( b2JointId jointId );
+B2_API b2Vec2 b2Joint_GetConstraintForce( b2JointId jointId );
+B2_API float b2Joint_GetConstraintTorque( b2JointId jointId );
+
+/* Distance joint (reference box2d.h:654-720). */
+B2_API b2JointId b2CreateDistanceJoint( b2WorldId worldId, const b2DistanceJointDef* def );
+B2_API void b2DistanceJoint_SetLength( b2JointId jointId, float length );
+B2_API float b2DistanceJoint_GetLength( b2JointId jointId );
+B2_API void b2DistanceJoint_EnableSpring( b2JointId jointId, bool enableSpring );
+B2_API bool b2DistanceJoint_IsSpringEnabled( b2JointId jointId );
+B2_API void b2DistanceJoint_SetSpringHertz( b2JointId jointId, float hertz );
+B2_API void b2DistanceJoint_SetSpringDampingRatio( b2JointId jointId, float dampingRatio );
+B2_API float b2DistanceJoint_GetHertz( b2JointId jointId );
+B2_API float b2DistanceJoint_GetDampingRatio( b2JointId jointId );
+B2_API void b2DistanceJoint_EnableLimit( b2JointId jointId, bool enableLimit );
+B2_API bool b2DistanceJoint_IsLimitEnabled( b2JointId jointId );
+B2_API void b2DistanceJoint_SetLengthRange( b2JointId jointId, float minLength, float maxLength );
+B2_API float b2DistanceJoint_GetMinLength( b2JointId jointId );
+B2_API float b2DistanceJoint_GetMaxLength( b2JointId jointId );
+B2_API float b2DistanceJoint_GetCurrentLength( b2JointId jointId );
+B2_API void b2DistanceJoint_EnableMotor( b2JointId jointId, bool enableMotor );
+B2_API bool b2DistanceJoint_IsMotorEnabled( b2JointId jointId );
+B2_API void b2DistanceJoint_SetMotorSpeed( b2JointId jointId, float motorSpeed );
+B2_API float b2DistanceJoint_GetMotorSpeed( b2JointId jointId );
+B2_API void b2DistanceJoint_SetMaxMotorForce( b2JointId jointId, float force );
+B2_API float b2DistanceJoint_GetMaxMotorForce( b2JointId jointId );
+B2_API float b2DistanceJoint_GetMotorForce( b2JointId jointId );
+
+/* Motor joint (reference box2d.h:736-766). */
+B2_API b2JointId b2CreateMotorJoint( b2WorldId worldId, const b2MotorJointDef* def );
+B2_API void b2MotorJoint_SetLinearOffset( b2JointId jointId, b2Vec2 linearOffset );
+B2_API b2Vec2 b2MotorJoint_GetLinearOffset( b2JointId jointId );
+B2_API void b2MotorJoint_SetAngularOffset( b2JointId jointId, float angularOffset );
+B2_API float b2MotorJoint_GetAngularOffset( b2JointId jointId );
+B2_API void b2MotorJoint_SetMaxForce( b2JointId jointId, float maxForce );
+B2_API float b2MotorJoint_GetMaxForce( b2JointId jointId );
+B2_API void b2MotorJoint_SetMaxTorque( b2JointId jointId, float maxTorque );
+B2_API float b2MotorJoint_GetMaxTorque( b2JointId jointId );
+B2_API void b2MotorJoint_SetCorrectionFactor( b2JointId jointId, float correctionFactor );
+B2_API float b2MotorJoint_GetCorrectionFactor( b2JointId jointId );
+
+/* Mouse joint (reference box2d.h:781-805). */
+B2_API b2JointId b2CreateMouseJoint( b2WorldId worldId, const b2MouseJointDef* def );
+B2_API void b2MouseJoint_SetTarget( b2JointId jointId, b2Vec2 target );
+B2_API b2Vec2 b2MouseJoint_GetTarget( b2JointId jointId );
+B2_API void b2MouseJoint_SetSpringHertz( b2JointId jointId, float hertz );
+B2_API float b2MouseJoint_GetSpringHertz( b2JointId jointId );
+B2_API void b2MouseJoint_SetSpringDampingRatio( b2JointId jointId, float dampingRatio );
+B2_API float b2MouseJoint_GetSpringDampingRatio( b2JointId jointId );
+B2_API void b2MouseJoint_SetMaxForce( b2JointId jointId, float maxForce );
+B2_API float b2MouseJoint_GetMaxForce( b2JointId jointId );
+
+/* Prismatic joint (reference box2d.h:820-876). */
+B2_API b2JointId b2CreatePrismaticJoint( b2WorldId worldId, const b2PrismaticJointDef* def );
+B2_API void b2PrismaticJoint_EnableSpring( b2JointId jointId, bool enableSpring );
+B2_API bool b2PrismaticJoint_IsSpringEnabled( b2JointId jointId );
+B2_API void b2PrismaticJoint_SetSpringHertz( b2JointId jointId, float hertz );
+B2_API float b2PrismaticJoint_GetSpringHertz( b2JointId jointId );
+B2_API void b2PrismaticJoint_SetSpringDampingRatio( b2JointId jointId, float dampingRatio );
+B2_API float b2PrismaticJoint_GetSpringDampingRatio( b2JointId jointId );
+B2_API void b2PrismaticJoint_EnableLimit( b2JointId jointId, bool enableLimit );
+B2_API bool b2PrismaticJoint_IsLimitEnabled( b2JointId jointId );
+B2_API float b2PrismaticJoint_GetLowerLimit( b2JointId jointId );
+B2_API float b2PrismaticJoint_GetUpperLimit( b2JointId jointId );
+B2_API void b2PrismaticJoint_SetLimits( b2JointId jointId, float lower, float upper );
+B2_API void b2PrismaticJoint_EnableMotor( b2JointId jointId, bool enableMotor );
+B2_API bool b2PrismaticJoint_IsMotorEnabled( b2JointId jointId );
+B2_API void b2PrismaticJoint_SetMotorSpeed( b2JointId jointId, float motorSpeed );
+B2_API float b2PrismaticJoint_GetMotorSpeed( b2JointId jointId );
+B2_API void b2PrismaticJoint_SetMaxMotorForce( b2JointId jointId, float force );
+B2_API float b2PrismaticJoint_GetMaxMotorForce( b2JointId jointId );
+B2_API float b2PrismaticJoint_GetMotorForce( b2JointId jointId );
+
+/* Revolute joint (reference box2d.h:891-946). */
+B2_API b2JointId b2CreateRevoluteJoint( b2WorldId worldId, const b2RevoluteJointDef* def );
+B2_API void b2RevoluteJoint_EnableSpring( b2JointId jointId, bool enableSpring );
+B2_API bool b2RevoluteJoint_IsSpringEnabled( b2JointId jointId );
+B2_API void b2RevoluteJoint_SetSpringHertz( b2JointId jointId, float hertz );
+B2_API float b2RevoluteJoint_GetSpringHertz( b2JointId jointId );
+B2_API void b2RevoluteJoint_SetSpringDampingRatio( b2JointId jointId, float dampingRatio );
+B2_API float b2RevoluteJoint_GetSpringDampingRatio( b2JointId jointId );
+B2_API float b2RevoluteJoint_GetAngle( b2JointId jointId );
+B2_API void b2RevoluteJoint_EnableLimit( b2JointId jointId, bool enableLimit );
+B2_API bool b2RevoluteJoint_IsLimitEnabled( b2JointId jointId );
+B2_API float b2RevoluteJoint_GetLowerLimit( b2JointId jointId );
+B2_API float b2RevoluteJoint_GetUpperLimit( b2JointId jointId );
+B2_API void b2RevoluteJoint_SetLimits( b2JointId jointId, float lower, float upper );
 B2_API void b2RevoluteJoint_EnableMotor( b2JointId jointId, bool enableMotor );
 B2_API bool b2RevoluteJoint_IsMotorEnabled( b2JointId jointId );
 B2_API void b2RevoluteJoint_SetMotorSpeed( b2JointId jointId, float motorSpeed );
 B2_API float b2RevoluteJoint_GetMotorSpeed( b2JointId jointId );
+B2_API float b2RevoluteJoint_GetMotorTorque( b2JointId jointId );
 B2_API void b2RevoluteJoint_SetMaxMotorTorque( b2JointId jointId, float torque );
 B2_API float b2RevoluteJoint_GetMaxMotorTorque( b2JointId jointId );
-B2_API float b2RevoluteJoint_GetMotorTorque( b2JointId jointId );
-B2_API void b2RevoluteJoint_EnableLimit( b2JointId jointId, bool enableLimit );
-B2_API void b2RevoluteJoint_SetLimits( b2JointId jointId, float lower, float upper );
-B2_API void b2RevoluteJoint_EnableSpring( b2JointId jointId, bool enableSpring );
+
+/* Weld joint (reference box2d.h:963-987). */
+B2_API b2JointId b2CreateWeldJoint( b2WorldId worldId, const b2WeldJointDef* def );
+B2_API void b2WeldJoint_SetLinearHertz( b2JointId jointId, float hertz );
+B2_API float b2WeldJoint_GetLinearHertz( b2JointId jointId );
+B2_API void b2WeldJoint_SetLinearDampingRatio( b2JointId jointId, float dampingRatio );
+B2_API float b2WeldJoint_GetLinearDampingRatio( b2JointId jointId );
+B2_API void b2WeldJoint_SetAngularHertz( b2JointId jointId, float hertz );
+B2_API float b2WeldJoint_GetAngularHertz( b2JointId jointId );
+B2_API void b2WeldJoint_SetAngularDampingRatio( b2JointId jointId, float dampingRatio );
+B2_API float b2WeldJoint_GetAngularDampingRatio( b2JointId jointId );
+
+/* Wheel joint (reference box2d.h:1003-1057). */
+B2_API b2JointId b2CreateWheelJoint( b2WorldId worldId, const b2WheelJointDef* def );
+B2_API void b2WheelJoint_EnableSpring( b2JointId jointId, bool enableSpring );
+B2_API bool b2WheelJoint_IsSpringEnabled( b2JointId jointId );
+B2_API void b2WheelJoint_SetSpringHertz( b2JointId jointId, float hertz );
+B2_API float b2WheelJoint_GetSpringHertz( b2JointId jointId );
+B2_API void b2WheelJoint_SetSpringDampingRatio( b2JointId jointId, float dampingRatio );
+B2_API float b2WheelJoint_GetSpringDampingRatio( b2JointId jointId );
+B2_API void b2WheelJoint_EnableLimit( b2JointId jointId, bool enableLimit );
+B2_API bool b2WheelJoint_IsLimitEnabled( b2JointId jointId );
+B2_API float b2WheelJoint_GetLowerLimit( b2JointId jointId );
+B2_API float b2WheelJoint_GetUpperLimit( b2JointId jointId );
+B2_API void b2WheelJoint_SetLimits( b2JointId jointId, float lower, float upper );
+B2_API void b2WheelJoint_EnableMotor( b2JointId jointId, bool enableMotor );
+B2_API bool b2WheelJoint_IsMotorEnabled( b2JointId jointId );
+B2_API void b2WheelJoint_SetMotorSpeed( b2JointId jointId, float motorSpeed );
+B2_API float b2WheelJoint_GetMotorSpeed( b2JointId jointId );
+B2_API void b2WheelJoint_SetMaxMotorTorque( b2JointId jointId, float torque );
+B2_API float b2WheelJoint_GetMaxMotorTorque( b2JointId jointId );
+B2_API float b2WheelJoint_GetMotorTorque( b2JointId jointId );

@@ -3,7 +3,7 @@
  *
  * Every struct here keeps the field order and types of the reference
  * `include/box2d/types.h` (b2WorldDef :64-113, b2BodyDef :130-190, b2ShapeDef :256-300,
- * b2Profile :397-421, b2Counters :424-438, b2RevoluteJointDef :620-680, events :900-1010)
+ * b2Profile :397-421, b2Counters :424-438, joint defs :464-853, events :900-1010)
  * so that a caller compiled against the reference headers passes them to this library
  * unchanged.  Defaults come from b2Default*Def (reference src/types.c:8-63).
  */
@@ -208,6 +208,131 @@ typedef struct b2RevoluteJointDef
 } b2RevoluteJointDef;
 
 B2_API b2RevoluteJointDef b2DefaultRevoluteJointDef( void );
+
+/* Distance joint definition (reference types.h:464-517). */
+typedef struct b2DistanceJointDef
+{
+	b2BodyId bodyIdA;
+	b2BodyId bodyIdB;
+	b2Vec2 localAnchorA;
+	b2Vec2 localAnchorB;
+	float length;
+	bool enableSpring;
+	float hertz;
+	float dampingRatio;
+	bool enableLimit;
+	float minLength;
+	float maxLength;
+	bool enableMotor;
+	float maxMotorForce;
+	float motorSpeed;
+	bool collideConnected;
+	void* userData;
+	int32_t internalValue;
+} b2DistanceJointDef;
+
+B2_API b2DistanceJointDef b2DefaultDistanceJointDef( void );
+
+/* Motor joint definition (reference types.h:527-558). */
+typedef struct b2MotorJointDef
+{
+	b2BodyId bodyIdA;
+	b2BodyId bodyIdB;
+	b2Vec2 linearOffset;
+	float angularOffset;
+	float maxForce;
+	float maxTorque;
+	float correctionFactor;
+	bool collideConnected;
+	void* userData;
+	int32_t internalValue;
+} b2MotorJointDef;
+
+B2_API b2MotorJointDef b2DefaultMotorJointDef( void );
+
+/* Mouse joint definition (reference types.h:569-597). */
+typedef struct b2MouseJointDef
+{
+	b2BodyId bodyIdA;
+	b2BodyId bodyIdB;
+	b2Vec2 target;
+	float hertz;
+	float dampingRatio;
+	float maxForce;
+	bool collideConnected;
+	void* userData;
+	int32_t internalValue;
+} b2MouseJointDef;
+
+B2_API b2MouseJointDef b2DefaultMouseJointDef( void );
+
+/* Prismatic joint definition (reference types.h:610-665). */
+typedef struct b2PrismaticJointDef
+{
+	b2BodyId bodyIdA;
+	b2BodyId bodyIdB;
+	b2Vec2 localAnchorA;
+	b2Vec2 localAnchorB;
+	b2Vec2 localAxisA;
+	float referenceAngle;
+	bool enableSpring;
+	float hertz;
+	float dampingRatio;
+	bool enableLimit;
+	float lowerTranslation;
+	float upperTranslation;
+	bool enableMotor;
+	float maxMotorForce;
+	float motorSpeed;
+	bool collideConnected;
+	void* userData;
+	int32_t internalValue;
+} b2PrismaticJointDef;
+
+B2_API b2PrismaticJointDef b2DefaultPrismaticJointDef( void );
+
+/* Weld joint definition (reference types.h:751-788). */
+typedef struct b2WeldJointDef
+{
+	b2BodyId bodyIdA;
+	b2BodyId bodyIdB;
+	b2Vec2 localAnchorA;
+	b2Vec2 localAnchorB;
+	float referenceAngle;
+	float linearHertz;
+	float angularHertz;
+	float linearDampingRatio;
+	float angularDampingRatio;
+	bool collideConnected;
+	void* userData;
+	int32_t internalValue;
+} b2WeldJointDef;
+
+B2_API b2WeldJointDef b2DefaultWeldJointDef( void );
+
+/* Wheel joint definition (reference types.h:801-853). */
+typedef struct b2WheelJointDef
+{
+	b2BodyId bodyIdA;
+	b2BodyId bodyIdB;
+	b2Vec2 localAnchorA;
+	b2Vec2 localAnchorB;
+	b2Vec2 localAxisA;
+	bool enableSpring;
+	float hertz;
+	float dampingRatio;
+	bool enableLimit;
+	float lowerTranslation;
+	float upperTranslation;
+	bool enableMotor;
+	float maxMotorTorque;
+	float motorSpeed;
+	bool collideConnected;
+	void* userData;
+	int32_t internalValue;
+} b2WheelJointDef;
+
+B2_API b2WheelJointDef b2DefaultWheelJointDef( void );
 
 /* Sensor overlap events (reference types.h:877-912): the sensor shape and the shape that
  * began or stopped overlapping it. */

@@ -262,17 +262,92 @@ typedef struct oContact
 	oDistCache cache; /* sensor overlap test (reference src/contact.h:136) */
 } oContact;
 
-typedef struct oRevolute
+typedef struct oSoft
+{
+	b2r biasRate, massScale, impulseScale;
+} oSoft;
+
+typedef struct oMat22
+{
+	oVec cx, cy;
+} oMat22;
+
+/* Per-type joint records (reference src/joint.h:56-234). */
+typedef struct oDistanceJoint
+{
+	b2r length, hertz, dampingRatio, minLength, maxLength, maxMotorForce, motorSpeed;
+	b2r impulse, lowerImpulse, upperImpulse, motorImpulse;
+	oVec anchorA, anchorB, deltaCenter;
+	oSoft distanceSoftness;
+	b2r axialMass;
+	bool enableSpring, enableLimit, enableMotor;
+} oDistanceJoint;
+
+typedef struct oMotorJoint
+{
+	oVec linearOffset;
+	b2r angularOffset;
+	oVec linearImpulse;
+	b2r angularImpulse, maxForce, maxTorque, correctionFactor;
+	oVec anchorA, anchorB, deltaCenter;
+	b2r deltaAngle;
+	oMat22 linearMass;
+	b2r angularMass;
+} oMotorJoint;
+
+typedef struct oMouseJoint
+{
+	oVec targetA;
+	b2r hertz, dampingRatio, maxForce;
+	oVec linearImpulse;
+	b2r angularImpulse;
+	oSoft linearSoftness, angularSoftness;
+	oVec anchorB, deltaCenter;
+	oMat22 linearMass;
+} oMouseJoint;
+
+typedef struct oPrismaticJoint
+{
+	oVec localAxisA, impulse;
+	b2r springImpulse, motorImpulse, lowerImpulse, upperImpulse;
+	b2r hertz, dampingRatio, maxMotorForce, motorSpeed, referenceAngle, lowerTranslation, upperTranslation;
+	oVec anchorA, anchorB, axisA, deltaCenter;
+	b2r deltaAngle, axialMass;
+	oSoft springSoftness;
+	bool enableSpring, enableLimit, enableMotor;
+} oPrismaticJoint;
+
+typedef struct oRevoluteJoint
 {
 	oVec linearImpulse;
 	b2r springImpulse, motorImpulse, lowerImpulse, upperImpulse;
 	b2r hertz, dampingRatio, maxMotorTorque, motorSpeed, referenceAngle, lowerAngle, upperAngle;
-	int indexA, indexB;
 	oVec anchorA, anchorB, deltaCenter;
 	b2r deltaAngle, axialMass;
-	b2r springBias, springMass, springImpulseScale;
+	oSoft springSoftness;
 	bool enableSpring, enableMotor, enableLimit;
-} oRevolute;
+} oRevoluteJoint;
+
+typedef struct oWeldJoint
+{
+	b2r referenceAngle, linearHertz, linearDampingRatio, angularHertz, angularDampingRatio;
+	oSoft linearSoftness, angularSoftness;
+	oVec linearImpulse;
+	b2r angularImpulse;
+	oVec anchorA, anchorB, deltaCenter;
+	b2r deltaAngle, axialMass;
+} oWeldJoint;
+
+typedef struct oWheelJoint
+{
+	oVec localAxisA;
+	b2r perpImpulse, motorImpulse, springImpulse, lowerImpulse, upperImpulse;
+	b2r maxMotorTorque, motorSpeed, lowerTranslation, upperTranslation, hertz, dampingRatio;
+	oVec anchorA, anchorB, axisA, deltaCenter;
+	b2r perpMass, motorMass, axialMass;
+	oSoft springSoftness;
+	bool enableSpring, enableMotor, enableLimit;
+} oWheelJoint;
 
 typedef struct oJoint
 {
@@ -281,18 +356,23 @@ typedef struct oJoint
 	int bodyIdA, bodyIdB;
 	oEdge edges[2];
 	int colorIndex, localIndex;
-	oVec localAnchorA, localAnchorB;
+	oVec localAnchorA, localAnchorB; /* reference localOriginAnchorA/B */
 	b2r invMassA, invMassB, invIA, invIB;
-	oRevolute rev;
+	int indexA, indexB; /* awake body ids, -1 for a body that is not awake */
+	union
+	{
+		oDistanceJoint distance;
+		oMotorJoint motor;
+		oMouseJoint mouse;
+		oPrismaticJoint prismatic;
+		oRevoluteJoint revolute;
+		oWeldJoint weld;
+		oWheelJoint wheel;
+	};
 	bool collideConnected;
 	uint16_t revision;
 	void* userData;
 } oJoint;
-
-typedef struct oSoft
-{
-	b2r biasRate, massScale, impulseScale;
-} oSoft;
 
 typedef struct oColor
 {
@@ -384,6 +464,36 @@ void o_update_body_mass( oWorld* w, oBody* b );
 oSoft o_make_soft( b2r hertz, b2r zeta, b2r h );
 bool o_should_bodies_collide( oWorld* w, oBody* a, oBody* b );
 void o_report_hits( oWorld* w );
+
+/* Step constants (reference b2StepContext, src/solver.h:76-140). */
+typedef struct oStep
+{
+	b2r dt, inv_dt, h, inv_h;
+	int subSteps;
+	oSoft contactSoft, staticSoft, jointSoft;
+	b2r restitutionThreshold, pushout;
+	bool enableWarmStarting;
+} oStep;
+
+/* Solver view of one body (reference b2BodyState, src/body.h:76-91); the identity state
+ * stands in for a static body. */
+typedef struct oState
+{
+	oVec v;
+	b2r w;
+	oVec dp;
+	oRot dq;
+} oState;
+
+/* Joints of every type (b2o_joint.c; reference src/joint.c:983-1108 and the per-type
+ * prepare, warm start and solve functions). */
+void o_prepare_joint( oWorld* w, const oStep* st, oJoint* j );
+oJoint* o_create_joint( b2WorldId worldId, b2BodyId bodyIdA, b2BodyId bodyIdB, b2JointType type, bool collideConnected,
+						void* userData, b2JointId* out );
+void o_destroy_contacts_between( oWorld* w, int bodyIdA, int bodyIdB );
+void o_buffer_move( oWorld* w, int proxyKey );
+void o_warm_start_joint( oJoint* j, oState* a, oState* b );
+void o_solve_joint( oJoint* j, const oStep* st, oState* a, oState* b, bool useBias );
 
 /* ---------------------------------------------------------------- time of impact
  * (b2o_toi.c; reference src/distance.c, src/shape.c:480-497, :713-735) */

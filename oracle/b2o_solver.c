@@ -1,5 +1,5 @@
 /*
- * b2o_solver.c -- soft-step solver, revolute joint, body finalisation, proxy enlargement
+ * b2o_solver.c -- soft-step solver, body finalisation, proxy enlargement
  * and the fast-body path of the plain-C oracle (TEST INFRASTRUCTURE).
  *
  * Restates the reference: step context and softness (src/world.c:717-745,
@@ -9,8 +9,8 @@
  * :1807-1954).  Contact constraints follow src/contact_solver.c: the overflow colour
  * uses the scalar path (:21-471) and graph colours the 8-lane path (:597-1293), whose
  * arithmetic differs; both are restated lane by lane, including the dummy second point
- * the 8-lane path evaluates for one-point manifolds.  The revolute joint follows
- * src/revolute_joint.c:201-470.
+ * the 8-lane path evaluates for one-point manifolds.  Joints of every type are in
+ * b2o_joint.c.
  */
 #include "b2o.h"
 
@@ -18,15 +18,6 @@
 
 void o_capture_inputs( oWorld* w );
 void o_capture_outputs( oWorld* w );
-
-typedef struct oStep
-{
-	b2r dt, inv_dt, h, inv_h;
-	int subSteps;
-	oSoft contactSoft, staticSoft, jointSoft;
-	b2r restitutionThreshold, pushout;
-	bool enableWarmStarting;
-} oStep;
 
 oSoft o_make_soft( b2r hertz, b2r zeta, b2r h )
 {
@@ -49,14 +40,6 @@ oSoft o_make_soft( b2r hertz, b2r zeta, b2r h )
 }
 
 /* Body solver state with a detached dummy for static bodies. */
-typedef struct oState
-{
-	oVec v;
-	b2r w;
-	oVec dp;
-	oRot dq;
-} oState;
-
 static oState load_state( oWorld* w, int index )
 {
 	oState s;
@@ -363,163 +346,23 @@ static void restitution_lane( oWorld* w, const oStep* st, oConstraint* k )
 	store_velocity( w, k->indexB, sB.v, sB.w );
 }
 
-/* ------------------------------------------------------------ revolute joint */
-static void prepare_revolute( oWorld* w, const oStep* st, oJoint* j )
+/* ------------------------------------------------------------ joints */
+static void warm_start_joint( oWorld* w, oJoint* j )
 {
-	oBody* a = w->bodies + j->bodyIdA;
-	oBody* b = w->bodies + j->bodyIdB;
-	j->invMassA = a->invMass;
-	j->invMassB = b->invMass;
-	j->invIA = a->invI;
-	j->invIB = b->invI;
-	oRevolute* r = &j->rev;
-	r->indexA = a->awakeIndex != O_NULL ? a->id : O_NULL;
-	r->indexB = b->awakeIndex != O_NULL ? b->id : O_NULL;
-	r->anchorA = orotate( a->xf.q, osub( j->localAnchorA, a->localCenter ) );
-	r->anchorB = orotate( b->xf.q, osub( j->localAnchorB, b->localCenter ) );
-	r->deltaCenter = osub( b->center, a->center );
-	r->deltaAngle = orelangle( b->xf.q, a->xf.q ) - r->referenceAngle;
-	r->deltaAngle = ounwind( r->deltaAngle );
-	b2r k = j->invIA + j->invIB;
-	r->axialMass = k > R( 0 ) ? R( 1 ) / k : R( 0 );
-	oSoft s = o_make_soft( r->hertz, r->dampingRatio, st->h );
-	r->springBias = s.biasRate;
-	r->springMass = s.massScale;
-	r->springImpulseScale = s.impulseScale;
-	if ( st->enableWarmStarting == false )
-	{
-		r->linearImpulse = ov( 0, 0 );
-		r->springImpulse = 0;
-		r->motorImpulse = 0;
-		r->lowerImpulse = 0;
-		r->upperImpulse = 0;
-	}
+	oState sA = load_state( w, j->indexA );
+	oState sB = load_state( w, j->indexB );
+	o_warm_start_joint( j, &sA, &sB );
+	store_velocity( w, j->indexA, sA.v, sA.w );
+	store_velocity( w, j->indexB, sB.v, sB.w );
 }
 
-static void warm_start_revolute( oWorld* w, oJoint* j )
+static void solve_joint( oWorld* w, const oStep* st, oJoint* j, bool useBias )
 {
-	oRevolute* r = &j->rev;
-	oState sA = load_state( w, r->indexA );
-	oState sB = load_state( w, r->indexB );
-	oVec rA = orotate( sA.dq, r->anchorA );
-	oVec rB = orotate( sB.dq, r->anchorB );
-	b2r axial = r->springImpulse + r->motorImpulse + r->lowerImpulse - r->upperImpulse;
-	sA.v = omulsub( sA.v, j->invMassA, r->linearImpulse );
-	sA.w -= j->invIA * ( ocross( rA, r->linearImpulse ) + axial );
-	sB.v = omuladd( sB.v, j->invMassB, r->linearImpulse );
-	sB.w += j->invIB * ( ocross( rB, r->linearImpulse ) + axial );
-	store_velocity( w, r->indexA, sA.v, sA.w );
-	store_velocity( w, r->indexB, sB.v, sB.w );
-}
-
-static void solve_revolute( oWorld* w, const oStep* st, oJoint* j, bool useBias )
-{
-	oRevolute* r = &j->rev;
-	b2r mA = j->invMassA, mB = j->invMassB, iA = j->invIA, iB = j->invIB;
-	oState sA = load_state( w, r->indexA );
-	oState sB = load_state( w, r->indexB );
-	oVec vA = sA.v, vB = sB.v;
-	b2r wA = sA.w, wB = sB.w;
-	bool fixedRotation = ( iA + iB == R( 0 ) );
-
-	if ( r->enableSpring && fixedRotation == false )
-	{
-		b2r C = orelangle( sB.dq, sA.dq ) + r->deltaAngle;
-		b2r bias = r->springBias * C;
-		b2r Cdot = wB - wA;
-		b2r impulse = -r->springMass * r->axialMass * ( Cdot + bias ) - r->springImpulseScale * r->springImpulse;
-		r->springImpulse += impulse;
-		wA -= iA * impulse;
-		wB += iB * impulse;
-	}
-	if ( r->enableMotor && fixedRotation == false )
-	{
-		b2r Cdot = wB - wA - r->motorSpeed;
-		b2r impulse = -r->axialMass * Cdot;
-		b2r old = r->motorImpulse;
-		b2r maxImpulse = st->h * r->maxMotorTorque;
-		r->motorImpulse = oclamp( r->motorImpulse + impulse, -maxImpulse, maxImpulse );
-		impulse = r->motorImpulse - old;
-		wA -= iA * impulse;
-		wB += iB * impulse;
-	}
-	if ( r->enableLimit && fixedRotation == false )
-	{
-		b2r angle = orelangle( sB.dq, sA.dq ) + r->deltaAngle;
-		angle = ounwind( angle );
-		{
-			b2r C = angle - r->lowerAngle;
-			b2r bias = 0, massScale = 1, impulseScale = 0;
-			if ( C > R( 0 ) )
-				bias = C * st->inv_h;
-			else if ( useBias )
-			{
-				bias = st->jointSoft.biasRate * C;
-				massScale = st->jointSoft.massScale;
-				impulseScale = st->jointSoft.impulseScale;
-			}
-			b2r Cdot = wB - wA;
-			b2r impulse = -massScale * r->axialMass * ( Cdot + bias ) - impulseScale * r->lowerImpulse;
-			b2r old = r->lowerImpulse;
-			r->lowerImpulse = omax( r->lowerImpulse + impulse, R( 0 ) );
-			impulse = r->lowerImpulse - old;
-			wA -= iA * impulse;
-			wB += iB * impulse;
-		}
-		{
-			b2r C = r->upperAngle - angle;
-			b2r bias = 0, massScale = 1, impulseScale = 0;
-			if ( C > R( 0 ) )
-				bias = C * st->inv_h;
-			else if ( useBias )
-			{
-				bias = st->jointSoft.biasRate * C;
-				massScale = st->jointSoft.massScale;
-				impulseScale = st->jointSoft.impulseScale;
-			}
-			b2r Cdot = wA - wB;
-			/* the reference scales the upper-limit term by lowerImpulse (revolute_joint.c:409) */
-			b2r impulse = -massScale * r->axialMass * ( Cdot + bias ) - impulseScale * r->lowerImpulse;
-			b2r old = r->upperImpulse;
-			r->upperImpulse = omax( r->upperImpulse + impulse, R( 0 ) );
-			impulse = r->upperImpulse - old;
-			wA += iA * impulse;
-			wB -= iB * impulse;
-		}
-	}
-	{
-		oVec rA = orotate( sA.dq, r->anchorA );
-		oVec rB = orotate( sB.dq, r->anchorB );
-		oVec Cdot = osub( oadd( vB, ocross_sv( wB, rB ) ), oadd( vA, ocross_sv( wA, rA ) ) );
-		oVec bias = ov( 0, 0 );
-		b2r massScale = 1, impulseScale = 0;
-		if ( useBias )
-		{
-			oVec sep = oadd( oadd( osub( sB.dp, sA.dp ), osub( rB, rA ) ), r->deltaCenter );
-			bias = omulsv( st->jointSoft.biasRate, sep );
-			massScale = st->jointSoft.massScale;
-			impulseScale = st->jointSoft.impulseScale;
-		}
-		b2r k11 = mA + mB + rA.y * rA.y * iA + rB.y * rB.y * iB;
-		b2r k12 = -rA.y * rA.x * iA - rB.y * rB.x * iB;
-		b2r k22 = mA + mB + rA.x * rA.x * iA + rB.x * rB.x * iB;
-		oVec rhs = oadd( Cdot, bias );
-		b2r det = k11 * k22 - k12 * k12;
-		if ( det != R( 0 ) )
-			det = R( 1 ) / det;
-		oVec bb = ov( det * ( k22 * rhs.x - k12 * rhs.y ), det * ( k11 * rhs.y - k12 * rhs.x ) );
-		oVec impulse;
-		impulse.x = -massScale * bb.x - impulseScale * r->linearImpulse.x;
-		impulse.y = -massScale * bb.y - impulseScale * r->linearImpulse.y;
-		r->linearImpulse.x += impulse.x;
-		r->linearImpulse.y += impulse.y;
-		vA = omulsub( vA, mA, impulse );
-		wA -= iA * ocross( rA, impulse );
-		vB = omuladd( vB, mB, impulse );
-		wB += iB * ocross( rB, impulse );
-	}
-	store_velocity( w, r->indexA, vA, wA );
-	store_velocity( w, r->indexB, vB, wB );
+	oState sA = load_state( w, j->indexA );
+	oState sB = load_state( w, j->indexB );
+	o_solve_joint( j, st, &sA, &sB, useBias );
+	store_velocity( w, j->indexA, sA.v, sA.w );
+	store_velocity( w, j->indexB, sB.v, sB.w );
 }
 
 /* ------------------------------------------------------------ bodies */
@@ -895,7 +738,7 @@ void o_solve( oWorld* w, b2r dt, int subSteps )
 	{
 		oIntArray* j = &w->colors[c].joints;
 		for ( int k = 0; k < j->count; ++k )
-			prepare_revolute( w, &st, w->joints + j->data[k] );
+			o_prepare_joint( w, &st, w->joints + j->data[k] );
 	}
 
 	oColor* overflow = w->colors + O_OVERFLOW;
@@ -907,7 +750,7 @@ void o_solve( oWorld* w, b2r dt, int subSteps )
 		integrate_velocities( w, &st );
 
 		for ( int k = 0; k < overflow->joints.count; ++k )
-			warm_start_revolute( w, w->joints + overflow->joints.data[k] );
+			warm_start_joint( w, w->joints + overflow->joints.data[k] );
 		for ( int k = 0; k < ocount; ++k )
 			warm_start_overflow( w, ocons + k );
 		if ( st.enableWarmStarting )
@@ -916,7 +759,7 @@ void o_solve( oWorld* w, b2r dt, int subSteps )
 			{
 				int c = active[a];
 				for ( int k = 0; k < w->colors[c].joints.count; ++k )
-					warm_start_revolute( w, w->joints + w->colors[c].joints.data[k] );
+					warm_start_joint( w, w->joints + w->colors[c].joints.data[k] );
 				const int k0 = colorStart[c], k1 = colorStart[c + 1];
 #pragma omp parallel for if ( o_threads > 1 && k1 - k0 >= O_PARALLEL_MIN ) num_threads( o_threads ) schedule( static )
 				for ( int k = k0; k < k1; ++k )
@@ -925,14 +768,14 @@ void o_solve( oWorld* w, b2r dt, int subSteps )
 		}
 
 		for ( int k = 0; k < overflow->joints.count; ++k )
-			solve_revolute( w, &st, w->joints + overflow->joints.data[k], true );
+			solve_joint( w, &st, w->joints + overflow->joints.data[k], true );
 		for ( int k = 0; k < ocount; ++k )
 			solve_overflow( w, &st, ocons + k, true );
 		for ( int a = 0; a < activeCount; ++a )
 		{
 			int c = active[a];
 			for ( int k = 0; k < w->colors[c].joints.count; ++k )
-				solve_revolute( w, &st, w->joints + w->colors[c].joints.data[k], true );
+				solve_joint( w, &st, w->joints + w->colors[c].joints.data[k], true );
 			const int k0 = colorStart[c], k1 = colorStart[c + 1];
 #pragma omp parallel for if ( o_threads > 1 && k1 - k0 >= O_PARALLEL_MIN ) num_threads( o_threads ) schedule( static )
 			for ( int k = k0; k < k1; ++k )
@@ -942,14 +785,14 @@ void o_solve( oWorld* w, b2r dt, int subSteps )
 		integrate_positions( w, &st );
 
 		for ( int k = 0; k < overflow->joints.count; ++k )
-			solve_revolute( w, &st, w->joints + overflow->joints.data[k], false );
+			solve_joint( w, &st, w->joints + overflow->joints.data[k], false );
 		for ( int k = 0; k < ocount; ++k )
 			solve_overflow( w, &st, ocons + k, false );
 		for ( int a = 0; a < activeCount; ++a )
 		{
 			int c = active[a];
 			for ( int k = 0; k < w->colors[c].joints.count; ++k )
-				solve_revolute( w, &st, w->joints + w->colors[c].joints.data[k], false );
+				solve_joint( w, &st, w->joints + w->colors[c].joints.data[k], false );
 			const int k0 = colorStart[c], k1 = colorStart[c + 1];
 #pragma omp parallel for if ( o_threads > 1 && k1 - k0 >= O_PARALLEL_MIN ) num_threads( o_threads ) schedule( static )
 			for ( int k = k0; k < k1; ++k )

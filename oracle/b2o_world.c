@@ -103,15 +103,6 @@ b2ShapeDef b2DefaultShapeDef( void )
 	return d;
 }
 
-b2RevoluteJointDef b2DefaultRevoluteJointDef( void )
-{
-	b2RevoluteJointDef d;
-	memset( &d, 0, sizeof( d ) );
-	d.drawSize = 0.25f;
-	d.internalValue = 1152023;
-	return d;
-}
-
 /* ------------------------------------------------------------ math API of math_functions.h */
 bool b2IsValid( float a ) { return !isnan( a ) && !isinf( a ); }
 bool b2Vec2_IsValid( b2Vec2 v ) { return b2IsValid( v.x ) && b2IsValid( v.y ); }
@@ -555,6 +546,8 @@ static void buffer_move( oWorld* w, int proxyKey )
 		oia_push( &w->moveArray, proxyKey );
 }
 
+void o_buffer_move( oWorld* w, int proxyKey ) { buffer_move( w, proxyKey ); }
+
 static b2ShapeId create_shape( b2BodyId bodyId, const b2ShapeDef* def, b2ShapeType type, const void* geometry )
 {
 	oWorld* w = body_world( bodyId );
@@ -993,13 +986,17 @@ bool o_should_bodies_collide( oWorld* w, oBody* a, oBody* b )
 	return true;
 }
 
-b2JointId b2CreateRevoluteJoint( b2WorldId worldId, const b2RevoluteJointDef* def )
+/* Joint record shared by every type (reference src/joint.c:140-288): id, body joint
+ * lists, constraint graph colour.  Returns NULL when the world is locked. */
+oJoint* o_create_joint( b2WorldId worldId, b2BodyId bodyIdA, b2BodyId bodyIdB, b2JointType type, bool collideConnected,
+						void* userData, b2JointId* out )
 {
+	*out = b2_nullJointId;
 	oWorld* w = o_world( worldId );
 	if ( w->locked )
-		return b2_nullJointId;
-	oBody* a = get_body( def->bodyIdA );
-	oBody* b = get_body( def->bodyIdB );
+		return NULL;
+	oBody* a = get_body( bodyIdA );
+	oBody* b = get_body( bodyIdB );
 	int id = oid_alloc( &w->jointIds );
 	GROW( w->joints, w->jointCap, id + 1, oJoint );
 	oJoint* j = w->joints + id;
@@ -1007,11 +1004,13 @@ b2JointId b2CreateRevoluteJoint( b2WorldId worldId, const b2RevoluteJointDef* de
 	memset( j, 0, sizeof( *j ) );
 	j->id = id;
 	j->revision = (uint16_t)( rev + 1 );
-	j->type = b2_revoluteJoint;
+	j->type = type;
 	j->bodyIdA = a->id;
 	j->bodyIdB = b->id;
-	j->userData = def->userData;
-	j->collideConnected = def->collideConnected;
+	j->userData = userData;
+	j->collideConnected = collideConnected;
+	j->indexA = O_NULL;
+	j->indexB = O_NULL;
 
 	j->edges[0].bodyId = a->id;
 	j->edges[0].prevKey = O_NULL;
@@ -1045,51 +1044,38 @@ b2JointId b2CreateRevoluteJoint( b2WorldId worldId, const b2RevoluteJointDef* de
 		j->localIndex = w->colors[color].joints.count;
 		oia_push( &w->colors[color].joints, id );
 	}
-
-	j->localAnchorA = ovf( def->localAnchorA );
-	j->localAnchorB = ovf( def->localAnchorB );
-	oRevolute* r = &j->rev;
-	r->referenceAngle = oclamp( def->referenceAngle, -O_PI, O_PI );
-	r->hertz = def->hertz;
-	r->dampingRatio = def->dampingRatio;
-	r->lowerAngle = omin( def->lowerAngle, def->upperAngle );
-	r->upperAngle = omax( def->lowerAngle, def->upperAngle );
-	r->lowerAngle = oclamp( r->lowerAngle, -O_PI, O_PI );
-	r->upperAngle = oclamp( r->upperAngle, -O_PI, O_PI );
-	r->maxMotorTorque = def->maxMotorTorque;
-	r->motorSpeed = def->motorSpeed;
-	r->enableSpring = def->enableSpring;
-	r->enableLimit = def->enableLimit;
-	r->enableMotor = def->enableMotor;
-
-	if ( def->collideConnected == false )
-	{
-		/* destroy contacts between the two bodies (reference src/joint.c:286-322) */
-		int key, other;
-		if ( a->contactCount < b->contactCount )
-		{
-			key = a->headContactKey;
-			other = b->id;
-		}
-		else
-		{
-			key = b->headContactKey;
-			other = a->id;
-		}
-		while ( key != O_NULL )
-		{
-			oContact* c = w->contacts + ( key >> 1 );
-			int e = key & 1;
-			key = c->edges[e].nextKey;
-			if ( c->edges[e ^ 1].bodyId == other )
-				o_destroy_contact( w, c );
-		}
-	}
 	b2JointId jid = { id + 1, worldId.index1 - 1, j->revision };
-	return jid;
+	*out = jid;
+	return j;
 }
 
-static oJoint* get_joint( b2JointId id ) { return s_worlds[id.world0]->joints + ( id.index1 - 1 ); }
+/* Destroys the contacts between two bodies, walking the shorter contact list (reference
+ * src/joint.c:290-322). */
+void o_destroy_contacts_between( oWorld* w, int bodyIdA, int bodyIdB )
+{
+	oBody* a = w->bodies + bodyIdA;
+	oBody* b = w->bodies + bodyIdB;
+	int key, other;
+	if ( a->contactCount < b->contactCount )
+	{
+		key = a->headContactKey;
+		other = b->id;
+	}
+	else
+	{
+		key = b->headContactKey;
+		other = a->id;
+	}
+	while ( key != O_NULL )
+	{
+		oContact* c = w->contacts + ( key >> 1 );
+		int e = key & 1;
+		key = c->edges[e].nextKey;
+		if ( c->edges[e ^ 1].bodyId == other )
+			o_destroy_contact( w, c );
+	}
+}
+
 bool b2Joint_IsValid( b2JointId id )
 {
 	if ( id.world0 >= s_worldCap || s_worlds[id.world0] == NULL || !s_worlds[id.world0]->inUse )
@@ -1099,40 +1085,6 @@ bool b2Joint_IsValid( b2JointId id )
 		return false;
 	return w->joints[id.index1 - 1].id == id.index1 - 1 && w->joints[id.index1 - 1].revision == id.revision;
 }
-b2JointType b2Joint_GetType( b2JointId id ) { return get_joint( id )->type; }
-b2BodyId b2Joint_GetBodyA( b2JointId id )
-{
-	oWorld* w = s_worlds[id.world0];
-	oJoint* j = get_joint( id );
-	b2BodyId b = { j->bodyIdA + 1, id.world0, w->bodies[j->bodyIdA].revision };
-	return b;
-}
-b2BodyId b2Joint_GetBodyB( b2JointId id )
-{
-	oWorld* w = s_worlds[id.world0];
-	oJoint* j = get_joint( id );
-	b2BodyId b = { j->bodyIdB + 1, id.world0, w->bodies[j->bodyIdB].revision };
-	return b;
-}
-void b2RevoluteJoint_EnableMotor( b2JointId id, bool f ) { get_joint( id )->rev.enableMotor = f; }
-bool b2RevoluteJoint_IsMotorEnabled( b2JointId id ) { return get_joint( id )->rev.enableMotor; }
-void b2RevoluteJoint_SetMotorSpeed( b2JointId id, float s ) { get_joint( id )->rev.motorSpeed = s; }
-float b2RevoluteJoint_GetMotorSpeed( b2JointId id ) { return (float)get_joint( id )->rev.motorSpeed; }
-void b2RevoluteJoint_SetMaxMotorTorque( b2JointId id, float t ) { get_joint( id )->rev.maxMotorTorque = t; }
-float b2RevoluteJoint_GetMaxMotorTorque( b2JointId id ) { return (float)get_joint( id )->rev.maxMotorTorque; }
-float b2RevoluteJoint_GetMotorTorque( b2JointId id )
-{
-	oWorld* w = s_worlds[id.world0];
-	return (float)( w->inv_h * get_joint( id )->rev.motorImpulse );
-}
-void b2RevoluteJoint_EnableLimit( b2JointId id, bool f ) { get_joint( id )->rev.enableLimit = f; }
-void b2RevoluteJoint_SetLimits( b2JointId id, float lower, float upper )
-{
-	oRevolute* r = &get_joint( id )->rev;
-	r->lowerAngle = oclamp( omin( lower, upper ), -O_PI, O_PI );
-	r->upperAngle = oclamp( omax( lower, upper ), -O_PI, O_PI );
-}
-void b2RevoluteJoint_EnableSpring( b2JointId id, bool f ) { get_joint( id )->rev.enableSpring = f; }
 
 /* ------------------------------------------------------------ broadphase pairs */
 typedef struct oPairList

@@ -56,6 +56,10 @@ SCENES = {
     "joint_chains": (300, (1, 2, 10, 60, 300)),
     # projectiles and bullets against a thin wall: continuous collision
     "fast_shots": (200, (1, 50, 100, 200)),
+    # every joint type (distance, motor, mouse, prismatic, revolute, weld, wheel), in the
+    # graph colours and in the overflow colour, with contacts
+    "joint_zoo": (300, (1, 2, 10, 60, 300)),
+    "joint_zoo_collide": (200, (1, 2, 10, 100, 200)),
 }
 
 
@@ -88,6 +92,10 @@ def make_scene(b: Backend, name: str):
         return b.joint_chains(8, 8, 7, 1242)
     if name == "fast_shots":
         return b.fast_shots(60, 1241)
+    if name == "joint_zoo":
+        return b.joint_zoo(2, 0, 1250)
+    if name == "joint_zoo_collide":
+        return b.joint_zoo(3, 1, 1251)
     raise KeyError(name)
 
 

@@ -198,3 +198,28 @@ def test_batch_mixed_paths_match_oracle(gpu, oracle):
             gpu.destroy(w)
         for w in wo:
             oracle.destroy(w)
+
+
+def test_batch_joint_types_match_oracle(gpu, oracle_atan):
+    """Batched worlds with every joint type (the joint scene at two sizes and seeds, next
+    to a pyramid): each world bit-identical to the oracle build with the library's own
+    atan2, stepped alone."""
+    bind_batch_api(gpu.lib)
+    makers = [lambda b: b.joint_zoo(1, 0, 61), lambda b: b.joint_zoo(2, 1, 62), lambda b: b.pyramid(12),
+              lambda b: b.joint_zoo(1, 1, 63)]
+    wg = [m(gpu) for m in makers]
+    wo = [m(oracle_atan) for m in makers]
+    ids = world_array(wg)
+    try:
+        for s in range(1, 151):
+            gpu.lib.b2World_StepBatch(ids, len(wg), 1.0 / 60.0, 4)
+            for w in wo:
+                oracle_atan.step(w)
+            if s % 10 == 0:
+                err = _compare(gpu, oracle_atan, wg, wo)
+                assert err is None, f"step {s}: {err}"
+    finally:
+        for w in wg:
+            gpu.destroy(w)
+        for w in wo:
+            oracle_atan.destroy(w)

@@ -172,7 +172,43 @@ def test_gpu_joint_limits_springs_lockstep(gpu, oracle_atan, scene):
     assert step is None, f"{scene}: {detail} at step {step}"
 
 
-@pytest.mark.parametrize("name", ["joint_chains", "joint_hub_limits"])
+@pytest.mark.parametrize("copies,flags,steps,per_phase", [(2, 0, 300, False), (3, 1, 200, False), (2, 0, 150, True)])
+def test_gpu_joint_zoo_lockstep(gpu, oracle_atan, copies, flags, steps, per_phase):
+    """Every joint type (distance, motor, mouse, prismatic, revolute, weld, wheel; springs,
+    limits and motors; a hub whose joints of every type overflow the graph colours), with
+    contacts, against the oracle build that uses the library's own atan2: bit-identical
+    every step, manifolds included, on the fused and on the per-phase solver path."""
+    def make(b):
+        w = b.joint_zoo(copies, flags, 1250 + flags)
+        return _per_phase(b, w) if ( per_phase and b is gpu ) else w
+
+    step, detail, worst = lockstep(gpu, oracle_atan, make, steps, check_manifolds=True)
+    assert step is None, f"joint zoo: {detail} at step {step}"
+
+
+# Positions of b2RevoluteJoint_GetAngle in the joint API script's output (four readouts
+# of 120 values; the angle is value 98 of each): the library answers that query on the
+# host with the C library's atan2f, as the reference does, so it may differ from the
+# own-atan2 oracle build by one float ulp.
+_ANGLE_SLOTS = [98 + 120 * k for k in range(4)]
+
+
+def test_gpu_joint_api_script(gpu, oracle_atan):
+    """Every joint type's creation, queries, reaction forces and torques, impulse-resetting
+    setters, collide-connected toggles and destruction through the library: the bits of
+    the own-atan2 oracle build (the revolute angle query within 2 ulp)."""
+    from tests.test_oracle import joint_api_script
+    a, b = joint_api_script(gpu), joint_api_script(oracle_atan)
+    assert a.shape == b.shape == (514,)
+    mask = np.ones(a.shape, bool)
+    mask[_ANGLE_SLOTS] = False
+    bad = np.nonzero((a.view(np.uint32) != b.view(np.uint32)) & mask)[0]
+    assert bad.size == 0, (bad[:10], a[bad[:10]], b[bad[:10]])
+    ulps = np.abs(a[_ANGLE_SLOTS].view(np.int32).astype(np.int64) - b[_ANGLE_SLOTS].view(np.int32).astype(np.int64))
+    assert ulps.max() <= 2, (a[_ANGLE_SLOTS], b[_ANGLE_SLOTS])
+
+
+@pytest.mark.parametrize("name", ["joint_chains", "joint_hub_limits", "joint_zoo", "joint_zoo_collide"])
 def test_gpu_joint_limits_against_reference_golden(gpu, name):
     """The same scenes against the reference's own states: the first step (identical
     start) within 1e-5 relative; the drift at later snapshots is printed (a one-ulp

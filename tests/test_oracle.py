@@ -223,3 +223,34 @@ def test_events_match_reference(reference, oracle):
     assert all(t > 0 for t in totals), totals
     step, detail, _ = lockstep(oracle, reference, lambda b: b.event_scene(40, 1243), 300, check_manifolds=True)
     assert step is None, f"{detail} at step {step}"
+
+
+def joint_api_script(backend):
+    """Runs the joint API script (every joint type's creation, queries and setters; see
+    b2s_joint_api_script) on a backend; returns its outputs as float32."""
+    f = backend.scenes.b2s_joint_api_script
+    f.argtypes = [C.POINTER(C.c_float), C.c_int]
+    f.restype = C.c_int
+    out = (C.c_float * 4096)()
+    n = f(out, 4096)
+    assert 0 < n <= 4096
+    return np.array(out[:n], np.float32)
+
+
+def test_joint_api_script_matches_reference(reference, oracle):
+    """Every joint type's creation (clamped and reordered limits, normalised axes),
+    queries, reaction forces and torques, setters that reset accumulated impulses,
+    collide-connected toggles and destruction: the oracle gives the reference's bits."""
+    a, b = joint_api_script(oracle), joint_api_script(reference)
+    assert a.shape == b.shape
+    bad = np.nonzero(a.view(np.uint32) != b.view(np.uint32))[0]
+    assert bad.size == 0, (bad[:10], a[bad[:10]], b[bad[:10]])
+
+
+@pytest.mark.parametrize("copies,flags", [(2, 0), (3, 1)])
+def test_joint_zoo_lockstep_reference(reference, oracle, copies, flags):
+    """Every joint type with contacts, in the colours and in the overflow colour: the
+    oracle stays bit-identical to the reference every step, manifolds included."""
+    step, detail, _ = lockstep(reference, oracle, lambda b: b.joint_zoo(copies, flags, 1250 + flags), 200,
+                               check_manifolds=True)
+    assert step is None, f"{detail} at step {step}"
