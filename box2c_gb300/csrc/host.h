@@ -203,6 +203,14 @@ typedef struct gJoint
 	void* userData;
 } gJoint;
 
+/* Pairs found from one moved proxy (kept across steps, only the count is reset). */
+typedef struct gPairList
+{
+	int* a;
+	int* b;
+	int count, capacity;
+} gPairList;
+
 typedef struct gColor
 {
 	gBits bodySet;
@@ -267,6 +275,8 @@ typedef struct gWorld
 	b2gSolvePlan solvePlan; /* plan of the current solve lists */
 	bool solveUploaded;		/* solve lists on the device match the host's */
 	b2gPairQuery* pairQuery; /* device pair query buffers, made on first use */
+	gPairList* pairLists;	 /* per moved proxy, reused every step */
+	int pairListCap;
 
 	b2gVec gravity;
 	float restitutionThreshold, pushout, hitThreshold, contactHertz, contactDamping, jointHertz, jointDamping;

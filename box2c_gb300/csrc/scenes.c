@@ -202,7 +202,11 @@ b2WorldId b2s_tumbler( int count, uint64_t seed, int variant )
 		int cj = cells[k] / gridN;
 		float cx = -9.5f + ( ci + 0.5f ) * cell;
 		float cy = 0.5f + ( cj + 0.5f ) * cell;
-		bd.position = ( b2Vec2 ){ cx + b2s_uniform( &rng, -slack, slack ), cy + b2s_uniform( &rng, -slack, slack ) };
+		/* draws in statements of their own: the order of evaluation inside one
+		 * initialiser list or argument list is unspecified */
+		float jx = b2s_uniform( &rng, -slack, slack );
+		float jy = b2s_uniform( &rng, -slack, slack );
+		bd.position = ( b2Vec2 ){ cx + jx, cy + jy };
 		b2BodyId bodyId = b2CreateBody( worldId, &bd );
 		if ( ( k & 1 ) == 0 )
 			b2CreatePolygonShape( bodyId, &sd, &box );
@@ -709,8 +713,12 @@ b2WorldId b2s_fast_shots( int count, uint64_t seed )
 	b2Capsule capsule = { { -0.1f, 0.0f }, { 0.1f, 0.0f }, 0.08f };
 	for ( int k = 0; k < count; ++k )
 	{
-		bd.position = ( b2Vec2 ){ b2s_uniform( &rng, 0.0f, 5.0f ), b2s_uniform( &rng, 1.0f, 15.0f ) };
-		bd.linearVelocity = ( b2Vec2 ){ b2s_uniform( &rng, 60.0f, 120.0f ), b2s_uniform( &rng, -5.0f, 5.0f ) };
+		float px = b2s_uniform( &rng, 0.0f, 5.0f );
+		float py = b2s_uniform( &rng, 1.0f, 15.0f );
+		float vx = b2s_uniform( &rng, 60.0f, 120.0f );
+		float vy = b2s_uniform( &rng, -5.0f, 5.0f );
+		bd.position = ( b2Vec2 ){ px, py };
+		bd.linearVelocity = ( b2Vec2 ){ vx, vy };
 		bd.angularVelocity = b2s_uniform( &rng, -10.0f, 10.0f );
 		bd.isBullet = ( k & 3 ) == 3;
 		b2BodyId bodyId = b2CreateBody( worldId, &bd );
@@ -991,8 +999,9 @@ b2WorldId b2s_event_scene( int count, uint64_t seed )
 	b2Circle ring = { { 0.0f, 0.0f }, 0.8f };
 	for ( int k = 0; k < count; ++k )
 	{
-		bd.position = ( b2Vec2 ){ -10.0f + 20.0f * ( k + 0.5f ) / count + b2s_uniform( &rng, -0.1f, 0.1f ),
-								  6.0f + 2.5f * ( k % 3 ) + b2s_uniform( &rng, 0.0f, 1.0f ) };
+		float jx = b2s_uniform( &rng, -0.1f, 0.1f );
+		float jy = b2s_uniform( &rng, 0.0f, 1.0f );
+		bd.position = ( b2Vec2 ){ -10.0f + 20.0f * ( k + 0.5f ) / count + jx, 6.0f + 2.5f * ( k % 3 ) + jy };
 		b2BodyId bodyId = b2CreateBody( worldId, &bd );
 		b2ShapeDef sd = b2DefaultShapeDef();
 		sd.density = 1.0f;
@@ -1348,7 +1357,9 @@ static void b2s_zoo_copy( b2WorldId worldId, b2BodyId groundId, float x0, int fl
 	/* debris: seeded boxes and circles dropped over the mechanisms */
 	for ( int k = 0; k < 12; ++k )
 	{
-		bd.position = ( b2Vec2 ){ x0 + b2s_uniform( rng, -16.0f, 20.0f ), b2s_uniform( rng, 8.0f, 14.0f ) };
+		float px = x0 + b2s_uniform( rng, -16.0f, 20.0f );
+		float py = b2s_uniform( rng, 8.0f, 14.0f );
+		bd.position = ( b2Vec2 ){ px, py };
 		b2BodyId d = b2CreateBody( worldId, &bd );
 		if ( k & 1 )
 		{
@@ -1357,7 +1368,9 @@ static void b2s_zoo_copy( b2WorldId worldId, b2BodyId groundId, float x0, int fl
 		}
 		else
 		{
-			b2Polygon p = b2MakeBox( b2s_uniform( rng, 0.15f, 0.4f ), b2s_uniform( rng, 0.15f, 0.4f ) );
+			float hx = b2s_uniform( rng, 0.15f, 0.4f );
+			float hy = b2s_uniform( rng, 0.15f, 0.4f );
+			b2Polygon p = b2MakeBox( hx, hy );
 			b2CreatePolygonShape( d, &sd, &p );
 		}
 	}

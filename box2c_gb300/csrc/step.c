@@ -405,13 +405,6 @@ static void add_to_graph( gWorld* w, gContact* c )
 }
 
 /* ------------------------------------------------------------ broadphase pairs */
-typedef struct gPairList
-{
-	int* a;
-	int* b;
-	int count, capacity;
-} gPairList;
-
 typedef struct gQueryCtx
 {
 	gWorld* w;
@@ -510,8 +503,10 @@ static bool pair_query( int proxyId, int shapeId, void* context )
 /* Moved proxies from which the tree query runs on the device: below this a host query
  * costs less than the device round trip (upload, launch, synchronise). */
 #define DEVICE_QUERY_MIN_MOVES 256
-/* Moved proxies per chunk when the pair rules run on the host pool. */
+/* Moved proxies per chunk when the pair rules run on the host pool, and the host tree
+ * walks below which the rules run on the calling thread. */
 #define PAIR_GRAIN 64
+#define PAIR_POOL_MIN_WALKS 32
 
 typedef struct gPairCtx
 {
@@ -598,10 +593,31 @@ static int update_pairs( gWorld* w )
 			return e;
 	}
 	double t1 = b2g_now_ms();
-	c.lists = (gPairList*)b2g_calloc( (size_t)moveCount, sizeof( gPairList ) );
-	if ( c.lists == NULL )
-		return -1;
-	if ( gpool_try_for( moveCount, PAIR_GRAIN, query_moved, &c ) == false )
+	if ( moveCount > w->pairListCap )
+	{
+		int cap = w->pairListCap < 64 ? 64 : w->pairListCap;
+		while ( cap < moveCount )
+			cap *= 2;
+		gPairList* lists = (gPairList*)b2g_realloc( w->pairLists, sizeof( gPairList ) * (size_t)cap );
+		if ( lists == NULL )
+			return -1;
+		memset( lists + w->pairListCap, 0, sizeof( gPairList ) * (size_t)( cap - w->pairListCap ) );
+		w->pairLists = lists;
+		w->pairListCap = cap;
+	}
+	c.lists = w->pairLists;
+	for ( int i = 0; i < moveCount; ++i )
+		c.lists[i].count = 0;
+	/* After the device walk only candidates that pass its rules remain, and the host work
+	 * per proxy is a few loads: the pool pays only when proxies fall back to host walks. */
+	int hostWalks = moveCount;
+	if ( c.counts != NULL )
+	{
+		hostWalks = 0;
+		for ( int i = 0; i < moveCount; ++i )
+			hostWalks += c.counts[i] < 0;
+	}
+	if ( hostWalks < PAIR_POOL_MIN_WALKS || gpool_try_for( moveCount, PAIR_GRAIN, query_moved, &c ) == false )
 		query_moved( 0, moveCount, &c );
 	double t2 = b2g_now_ms();
 	for ( int i = 0; i < moveCount; ++i )
@@ -609,10 +625,7 @@ static int update_pairs( gWorld* w )
 		gPairList* l = c.lists + i;
 		for ( int k = l->count - 1; k >= 0; --k )
 			gcontact_create( w, w->shapes + l->a[k], w->shapes + l->b[k] );
-		b2g_free( l->a );
-		b2g_free( l->b );
 	}
-	b2g_free( c.lists );
 	w->moveArray.count = 0;
 	gset_clear( &w->moveSet );
 	double t3 = b2g_now_ms();

@@ -385,6 +385,12 @@ void b2DestroyWorld( b2WorldId worldId )
 	gtape_free( w );
 	b2gd_pair_query_free( w->pairQuery );
 	w->pairQuery = NULL;
+	for ( int i = 0; i < w->pairListCap; ++i )
+	{
+		b2g_free( w->pairLists[i].a );
+		b2g_free( w->pairLists[i].b );
+	}
+	b2g_free( w->pairLists );
 	b2gd_free( &w->dev, &w->io );
 	for ( int i = 0; i < 3; ++i )
 		gtree_free( w->trees + i );
