@@ -151,15 +151,16 @@ __device__ __forceinline__ FusedSmem carve( float4* base, int BS, int RC )
 __device__ __forceinline__ int local_count( int n, int rank, int CL ) { return n > rank ? ( n - rank + CL - 1 ) / CL : 0; }
 
 /* One stage over all colours: the overflow set first (serially, CTA 0 thread 0), then
- * each active colour with a cluster barrier after it. */
-template <int CL>
+ * each active colour with a cluster barrier after it.  JOINTS false compiles the joint
+ * calls out, so a world without joints runs the contact sweep alone. */
+template <int CL, bool JOINTS>
 __device__ void run_stage( const b2gDevWorld& W, const FusedPlan& P, const FusedSmem& m, const ClusterBodies& B, int rank,
 						   int phase, const b2gStepConst& sc, const OverflowCache& ov, int ovSlots )
 {
 	const int* cs = P.colorStart;
 	const int* js = P.jointStart;
 	int ovRows = cs[B2G_COLORS] - cs[B2G_OVERFLOW];
-	int ovJointsAll = js[B2G_COLORS] - js[B2G_OVERFLOW];
+	int ovJointsAll = JOINTS ? js[B2G_COLORS] - js[B2G_OVERFLOW] : 0;
 	int ovJoints = phase == F_RESTITUTION ? 0 : ovJointsAll;
 	/* the per-phase path runs the overflow set when it has any constraint, and for
 	 * restitution when it has contacts */
@@ -218,7 +219,7 @@ __device__ void run_stage( const b2gDevWorld& W, const FusedPlan& P, const Fused
 			continue;
 		int base = P.ctaBase[c][rank];
 		int nr = P.split[c][rank + 1] - P.split[c][rank];
-		int nj = phase == F_RESTITUTION ? 0 : local_count( js[c + 1] - js[c], rank, CL );
+		int nj = ( JOINTS == false || phase == F_RESTITUTION ) ? 0 : local_count( js[c + 1] - js[c], rank, CL );
 		for ( int j = threadIdx.x; j < nr; j += FUSED_THREADS )
 			row_step( m, B, base + j, phase, false, sc );
 		for ( int j = threadIdx.x; j < nj; j += FUSED_THREADS )
@@ -285,8 +286,8 @@ __global__ void __launch_bounds__( 128 ) k_fused_stage( b2gDevWorld W, FusedPlan
 	}
 }
 
-template <int CL>
-__global__ void __launch_bounds__( FUSED_THREADS ) k_solve_fused( b2gDevWorld W, FusedPlan P, b2gStepConst sc, const float4* image )
+template <int CL, bool JOINTS>
+__global__ void __launch_bounds__( FUSED_THREADS, 1 ) k_solve_fused( b2gDevWorld W, FusedPlan P, b2gStepConst sc, const float4* image )
 {
 	/* every CTA of the cluster takes the same branch: no barrier is left waiting */
 	if ( W.guardEvents && W.counters[0] != 0 )
@@ -318,7 +319,7 @@ __global__ void __launch_bounds__( FUSED_THREADS ) k_solve_fused( b2gDevWorld W,
 	}
 	/* overflow cache: distinct bodies of the set's ends get slots in end order */
 	const int ovR = cs[B2G_COLORS] - cs[B2G_OVERFLOW];
-	const int ovJ = P.jointStart[B2G_COLORS] - P.jointStart[B2G_OVERFLOW];
+	const int ovJ = JOINTS ? P.jointStart[B2G_COLORS] - P.jointStart[B2G_OVERFLOW] : 0;
 	const int ovBase = P.ctaBase[B2G_OVERFLOW][0];
 	OverflowCache ov = carve_overflow( smem + P.ovOffset, ovR, ovJ );
 	__shared__ int ovSlots;
@@ -412,8 +413,8 @@ __global__ void __launch_bounds__( FUSED_THREADS ) k_solve_fused( b2gDevWorld W,
 			m.st0[s] = velocity_word( x );
 		}
 		cl.sync();
-		run_stage<CL>( W, P, m, B, rank, F_WARM, sc, ov, ovSlots );
-		run_stage<CL>( W, P, m, B, rank, F_SOLVE, sc, ov, ovSlots );
+		run_stage<CL, JOINTS>( W, P, m, B, rank, F_WARM, sc, ov, ovSlots );
+		run_stage<CL, JOINTS>( W, P, m, B, rank, F_SOLVE, sc, ov, ovSlots );
 		for ( int j = tid; j < awakeLocal; j += FUSED_THREADS )
 		{
 			int s = m.awake[j];
@@ -422,9 +423,9 @@ __global__ void __launch_bounds__( FUSED_THREADS ) k_solve_fused( b2gDevWorld W,
 			m.st1[s] = make_float4( x.dp.x, x.dp.y, x.dq.c, x.dq.s );
 		}
 		cl.sync();
-		run_stage<CL>( W, P, m, B, rank, F_RELAX, sc, ov, ovSlots );
+		run_stage<CL, JOINTS>( W, P, m, B, rank, F_RELAX, sc, ov, ovSlots );
 	}
-	run_stage<CL>( W, P, m, B, rank, F_RESTITUTION, sc, ov, ovSlots );
+	run_stage<CL, JOINTS>( W, P, m, B, rank, F_RESTITUTION, sc, ov, ovSlots );
 
 	/* store impulses (reference src/contact_solver.c:442-471, :1180-1293): colour rows
 	 * write both point slots, overflow rows their points */
@@ -551,19 +552,24 @@ extern "C" int b2gd_solver_fused( b2gDevWorld* w, const b2gSolvePlan* plan, cons
 		bytes = withCache;
 	}
 
-	auto kernel = k_solve_fused<FUSED_CLUSTER>;
+	auto plain = k_solve_fused<FUSED_CLUSTER, false>;
+	auto jointed = k_solve_fused<FUSED_CLUSTER, true>;
+	auto kernel = plan->jointStart[B2G_COLORS] > 0 ? jointed : plain;
 	if ( ready == 0 )
 	{
 		ready = -1;
-		if ( cudaFuncSetAttribute( kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1 ) == cudaSuccess &&
-			 cudaFuncSetAttribute( kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, FUSED_SMEM_MAX ) == cudaSuccess )
+		bool ok = true;
+		for ( auto k : { plain, jointed } )
 		{
+			ok = ok && cudaFuncSetAttribute( k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1 ) == cudaSuccess &&
+				 cudaFuncSetAttribute( k, cudaFuncAttributeMaxDynamicSharedMemorySize, FUSED_SMEM_MAX ) == cudaSuccess;
 			cudaLaunchAttribute attr[1];
 			cudaLaunchConfig_t cfg = cluster_config( attr, FUSED_SMEM_MAX, nullptr );
 			int clusters = 0;
-			if ( cudaOccupancyMaxActiveClusters( &clusters, kernel, &cfg ) == cudaSuccess && clusters >= 1 )
-				ready = 1;
+			ok = ok && cudaOccupancyMaxActiveClusters( &clusters, k, &cfg ) == cudaSuccess && clusters >= 1;
 		}
+		if ( ok )
+			ready = 1;
 		cudaGetLastError();
 	}
 	if ( ready != 1 )
