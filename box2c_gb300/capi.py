@@ -168,6 +168,8 @@ class Backend:
         S.b2s_joint_chains.restype = WorldId
         S.b2s_joint_zoo.argtypes = [C.c_int, C.c_int, C.c_uint64]
         S.b2s_joint_zoo.restype = WorldId
+        S.b2s_chain_scene.argtypes = [C.c_int, C.c_uint64]
+        S.b2s_chain_scene.restype = WorldId
         S.b2s_event_scene.argtypes = [C.c_int, C.c_uint64]
         S.b2s_event_scene.restype = WorldId
         S.b2s_empty_world.argtypes = []
@@ -229,6 +231,10 @@ class Backend:
     def joint_chains(self, chains: int = 8, links: int = 8, flags: int = 7, seed: int = 1242) -> WorldId:
         """flags: 1 joint limits, 2 joint springs, 4 motors."""
         return self._made(self.scenes.b2s_joint_chains(chains, links, flags, seed))
+
+    def chain_scene(self, count: int = 200, seed: int = 1260) -> WorldId:
+        """Chains: terrain and a bowl of smooth segments with mixed bodies and bullets."""
+        return self._made(self.scenes.b2s_chain_scene(count, seed))
 
     def joint_zoo(self, copies: int = 2, flags: int = 0, seed: int = 1250) -> WorldId:
         """Every joint type: ropes, pendulum, elevators, car, welds, motor and mouse joints, an overflowing spider."""

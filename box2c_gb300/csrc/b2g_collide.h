@@ -5,12 +5,16 @@
  * Restates the reference src/manifold.c: b2MakeCapsule (:14-30), b2CollideCircles
  * (:36-70), b2CollideCapsuleAndCircle (:73-135), b2CollidePolygonAndCircle (:137-253),
  * b2ClipPolygons (:276-411), b2FindMaxSeparation (:414-450), b2CollidePolygons
- * (:470-700), with b2SegmentDistance from src/distance.c:32-107.  Feature ids
- * (B2_MAKE_ID, manifold.c:12) and operand order are kept so warm starting matches.
+ * (:470-700), the smooth (chain) segment manifolds b2CollideSmoothSegmentAndCircle
+ * (:714-800), b2ClipSegments (:809-874), b2ClassifyNormal (:876-934) and
+ * b2CollideSmoothSegmentAndPolygon (:944-1333), with b2SegmentDistance from
+ * src/distance.c:32-107.  Feature ids (B2_MAKE_ID, manifold.c:12) and operand order are
+ * kept so warm starting matches.
  */
 #pragma once
 
 #include "b2g_math.h"
+#include "b2g_toi.h"
 #include "b2g_types.h"
 
 typedef struct b2gPoly
@@ -491,10 +495,439 @@ B2G_HD void gshape_poly( b2gPoly* p, const b2gShapeGeo* g )
 	}
 }
 
-/* Manifold of a registered shape pair with A the primary type (reference
- * src/contact.c:150-183): circle=0 capsule=1 segment=2 polygon=3. */
-B2G_HD void gcollide_shapes( b2gManifold* m, const b2gShapeGeo* a, b2gXf xfA, const b2gShapeGeo* b, b2gXf xfB )
+/* ------------------------------------------------------------ smooth segments
+ * A smooth segment (a link of a chain) collides on its right side only, and its ghost
+ * vertices (the neighbouring links' far ends) decide which normals it may produce. */
+typedef struct b2gSmooth
 {
+	b2gVec ghost1, p1, p2, ghost2;
+} b2gSmooth;
+
+B2G_HD b2gSmooth gsmooth_of( const b2gShapeGeo* g )
+{
+	b2gSmooth s;
+	s.p1 = g->v[0];
+	s.p2 = g->v[1];
+	s.ghost1 = g->v[2];
+	s.ghost2 = g->v[3];
+	return s;
+}
+
+B2G_HD void gcollide_smooth_circle( b2gManifold* m, const b2gSmooth* sA, b2gXf xfA, b2gVec centerB, float radiusB, b2gXf xfB )
+{
+	gmanifold_clear( m );
+	b2gXf xf = ginvmulxf( xfA, xfB );
+	b2gVec pB = gxfpoint( xf, centerB );
+	b2gVec p1 = sA->p1;
+	b2gVec p2 = sA->p2;
+	b2gVec e = gsub( p2, p1 );
+	float offset = gdot( gright( e ), gsub( pB, p1 ) );
+	if ( offset < 0.0f )
+		return;
+	float u = gdot( e, gsub( p2, pB ) );
+	float v = gdot( e, gsub( pB, p1 ) );
+	b2gVec pA;
+	if ( v <= 0.0f )
+	{
+		b2gVec prevEdge = gsub( p1, sA->ghost1 );
+		float uPrev = gdot( prevEdge, gsub( pB, p1 ) );
+		if ( uPrev <= 0.0f )
+			return;
+		pA = p1;
+	}
+	else if ( u <= 0.0f )
+	{
+		b2gVec nextEdge = gsub( sA->ghost2, p2 );
+		float vNext = gdot( nextEdge, gsub( pB, p2 ) );
+		if ( vNext > 0.0f )
+			return;
+		pA = p2;
+	}
+	else
+	{
+		float ee = gdot( e, e );
+		pA = gv( u * p1.x + v * p2.x, u * p1.y + v * p2.y );
+		pA = ee > 0.0f ? gmulsv( 1.0f / ee, pA ) : p1;
+	}
+	float distance;
+	b2gVec normal = glen_normalize( &distance, gsub( pB, pA ) );
+	float separation = distance - radiusB;
+	if ( separation > B2G_SPECULATIVE )
+		return;
+	b2gVec cA = pA;
+	b2gVec cB = gmuladd( pB, -radiusB, normal );
+	b2gVec contactPointA = glerp( cA, cB, 0.5f );
+	m->normal = grotate( xfA.q, normal );
+	b2gPoint* mp = m->pts + 0;
+	mp->anchorA = grotate( xfA.q, contactPointA );
+	mp->anchorB = gadd( mp->anchorA, gsub( xfA.p, xfB.p ) );
+	mp->point = gadd( xfA.p, mp->anchorA );
+	mp->separation = separation;
+	mp->id = 0;
+	m->count = 1;
+}
+
+/* Two-point manifold of segment a1-a2 (reference side) against b1-b2 (incident, opposite
+ * winding), points at the midpoints accounting for the radii, in frame A. */
+B2G_HD void gclip_segments( b2gManifold* m, b2gVec a1, b2gVec a2, b2gVec b1, b2gVec b2, b2gVec normal, float ra, float rb, uint16_t id1,
+							uint16_t id2 )
+{
+	gmanifold_clear( m );
+	b2gVec tangent = gleft( normal );
+	float lower1 = 0.0f;
+	float upper1 = gdot( gsub( a2, a1 ), tangent );
+	float upper2 = gdot( gsub( b1, a1 ), tangent );
+	float lower2 = gdot( gsub( b2, a1 ), tangent );
+	if ( upper2 < lower1 || upper1 < lower2 )
+		return;
+	b2gVec vLower;
+	if ( lower2 < lower1 && upper2 - lower2 > FLT_EPSILON )
+		vLower = glerp( b2, b1, ( lower1 - lower2 ) / ( upper2 - lower2 ) );
+	else
+		vLower = b2;
+	b2gVec vUpper;
+	if ( upper2 > upper1 && upper2 - lower2 > FLT_EPSILON )
+		vUpper = glerp( b2, b1, ( upper1 - lower2 ) / ( upper2 - lower2 ) );
+	else
+		vUpper = b1;
+	float separationLower = gdot( gsub( vLower, a1 ), normal );
+	float separationUpper = gdot( gsub( vUpper, a1 ), normal );
+	vLower = gmuladd( vLower, 0.5f * ( ra - rb - separationLower ), normal );
+	vUpper = gmuladd( vUpper, 0.5f * ( ra - rb - separationUpper ), normal );
+	float radius = ra + rb;
+	m->normal = normal;
+	m->pts[0].anchorA = vLower;
+	m->pts[0].separation = separationLower - radius;
+	m->pts[0].id = id1;
+	m->pts[1].anchorA = vUpper;
+	m->pts[1].separation = separationUpper - radius;
+	m->pts[1].id = id2;
+	m->count = 2;
+}
+
+enum
+{
+	B2G_NORMAL_SKIP = 0,
+	B2G_NORMAL_ADMIT = 1,
+	B2G_NORMAL_SNAP = 2,
+};
+
+typedef struct b2gSmoothParams
+{
+	b2gVec edge1, normal0, normal2;
+	bool convex1, convex2;
+} b2gSmoothParams;
+
+/* Gauss-map test of a candidate normal against the neighbouring links. */
+B2G_HD int gclassify_normal( const b2gSmoothParams* params, b2gVec normal )
+{
+	const float sinTol = 0.01f;
+	if ( gdot( normal, params->edge1 ) <= 0.0f )
+	{
+		if ( params->convex1 )
+		{
+			if ( gcross( normal, params->normal0 ) > sinTol )
+				return B2G_NORMAL_SKIP;
+			return B2G_NORMAL_ADMIT;
+		}
+		return B2G_NORMAL_SNAP;
+	}
+	if ( params->convex2 )
+	{
+		if ( gcross( params->normal2, normal ) > sinTol )
+			return B2G_NORMAL_SKIP;
+		return B2G_NORMAL_ADMIT;
+	}
+	return B2G_NORMAL_SNAP;
+}
+
+/* The frame-A manifold of a clip to world anchors and points. */
+B2G_HD void gsmooth_finish( b2gManifold* m, b2gXf xfA, b2gXf xfB, b2gVec normalA )
+{
+	m->normal = grotate( xfA.q, normalA );
+	m->pts[0].anchorA = grotate( xfA.q, m->pts[0].anchorA );
+	m->pts[1].anchorA = grotate( xfA.q, m->pts[1].anchorA );
+	b2gVec pAB = gsub( xfA.p, xfB.p );
+	m->pts[0].anchorB = gadd( m->pts[0].anchorA, pAB );
+	m->pts[1].anchorB = gadd( m->pts[1].anchorA, pAB );
+	m->pts[0].point = gadd( xfA.p, m->pts[0].anchorA );
+	m->pts[1].point = gadd( xfA.p, m->pts[1].anchorA );
+}
+
+/* Smooth segment against a polygon (capsules enter as rounded 2-gons); `cache` is the
+ * contact's closest-feature cache, read and updated. */
+B2G_HD void gcollide_smooth_polygon( b2gManifold* m, const b2gSmooth* sA, b2gXf xfA, const b2gVec* vB, const b2gVec* nB, int count,
+									 float radiusB, b2gVec centroidB0, b2gXf xfB, b2gDistCache* cache )
+{
+	gmanifold_clear( m );
+	b2gXf xf = ginvmulxf( xfA, xfB );
+	b2gVec centroidB = gxfpoint( xf, centroidB0 );
+	b2gVec p1 = sA->p1;
+	b2gVec p2 = sA->p2;
+	b2gVec edge1 = gnormalize( gsub( p2, p1 ) );
+
+	b2gSmoothParams sp;
+	sp.edge1 = edge1;
+	const float convexTol = 0.01f;
+	b2gVec edge0 = gnormalize( gsub( p1, sA->ghost1 ) );
+	sp.normal0 = gright( edge0 );
+	sp.convex1 = gcross( edge0, edge1 ) >= convexTol;
+	b2gVec edge2 = gnormalize( gsub( sA->ghost2, p2 ) );
+	sp.normal2 = gright( edge2 );
+	sp.convex2 = gcross( edge1, edge2 ) >= convexTol;
+
+	b2gVec normal1 = gright( edge1 );
+	bool behind1 = gdot( normal1, gsub( centroidB, p1 ) ) < 0.0f;
+	bool behind0 = true;
+	bool behind2 = true;
+	if ( sp.convex1 )
+		behind0 = gdot( sp.normal0, gsub( centroidB, p1 ) ) < 0.0f;
+	if ( sp.convex2 )
+		behind2 = gdot( sp.normal2, gsub( centroidB, p2 ) ) < 0.0f;
+	if ( behind1 && behind0 && behind2 )
+		return;
+
+	b2gVec vertices[8];
+	b2gVec normals[8];
+	for ( int i = 0; i < count; ++i )
+	{
+		vertices[i] = gxfpoint( xf, vB[i] );
+		normals[i] = grotate( xf.q, nB[i] );
+	}
+
+	b2gVec segPts[2] = { p1, p2 };
+	b2gProxy proxyA = gproxy_points( segPts, 2, 0.0f );
+	b2gProxy proxyB = gproxy_points( vertices, count, 0.0f );
+	b2gXf identity;
+	identity.p = gv( 0.0f, 0.0f );
+	identity.q = grot( 1.0f, 0.0f );
+	b2gVec pointA, pointB;
+	float distance = gdistance_points( cache, &proxyA, identity, &proxyB, identity, &pointA, &pointB );
+	if ( distance > radiusB + B2G_SPECULATIVE )
+		return;
+
+	b2gVec n0 = sp.convex1 ? sp.normal0 : normal1;
+	b2gVec n2 = sp.convex2 ? sp.normal2 : normal1;
+	int incidentIndex = -1;
+	int incidentNormal = -1;
+
+	if ( behind1 == false && distance > 0.1f * B2G_LINEAR_SLOP )
+	{
+		if ( cache->count == 1 )
+		{
+			/* vertex-vertex */
+			b2gVec pA = pointA;
+			b2gVec pB = pointB;
+			b2gVec normal = gnormalize( gsub( pB, pA ) );
+			int type = gclassify_normal( &sp, normal );
+			if ( type == B2G_NORMAL_SKIP )
+				return;
+			if ( type == B2G_NORMAL_ADMIT )
+			{
+				m->normal = grotate( xfA.q, normal );
+				b2gPoint* cp = m->pts + 0;
+				cp->anchorA = grotate( xfA.q, pA );
+				cp->anchorB = gadd( cp->anchorA, gsub( xfA.p, xfB.p ) );
+				cp->point = gadd( xfA.p, cp->anchorA );
+				cp->separation = distance - radiusB;
+				cp->id = B2G_MAKE_ID( cache->indexA[0], cache->indexB[0] );
+				m->count = 1;
+				return;
+			}
+			incidentIndex = cache->indexB[0];
+		}
+		else
+		{
+			/* vertex-edge */
+			int ia1 = cache->indexA[0];
+			int ia2 = cache->indexA[1];
+			int ib1 = cache->indexB[0];
+			int ib2 = cache->indexB[1];
+			if ( ia1 == ia2 )
+			{
+				/* one point on A, two on B */
+				b2gVec normalB = gsub( pointA, pointB );
+				float dot1 = gdot( normalB, normals[ib1] );
+				float dot2 = gdot( normalB, normals[ib2] );
+				int ib = dot1 > dot2 ? ib1 : ib2;
+				normalB = normals[ib];
+				int type = gclassify_normal( &sp, gneg( normalB ) );
+				if ( type == B2G_NORMAL_SKIP )
+					return;
+				if ( type == B2G_NORMAL_ADMIT )
+				{
+					ib1 = ib;
+					ib2 = ib < count - 1 ? ib + 1 : 0;
+					b2gVec b1 = vertices[ib1];
+					b2gVec b2 = vertices[ib2];
+					dot1 = gdot( normalB, gsub( p1, b1 ) );
+					dot2 = gdot( normalB, gsub( p2, b1 ) );
+					if ( dot1 < dot2 )
+					{
+						if ( gdot( n0, normalB ) < gdot( normal1, normalB ) )
+							return;
+					}
+					else
+					{
+						if ( gdot( n2, normalB ) < gdot( normal1, normalB ) )
+							return;
+					}
+					gclip_segments( m, b1, b2, p1, p2, normalB, radiusB, 0.0f, B2G_MAKE_ID( ib1, 1 ), B2G_MAKE_ID( ib2, 0 ) );
+					gsmooth_finish( m, xfA, xfB, gneg( normalB ) );
+					return;
+				}
+				incidentNormal = ib;
+			}
+			else
+			{
+				float dot1 = gdot( normal1, gsub( vertices[ib1], p1 ) );
+				float dot2 = gdot( normal1, gsub( vertices[ib2], p2 ) );
+				incidentIndex = dot1 < dot2 ? ib1 : ib2;
+			}
+		}
+	}
+	else
+	{
+		/* SAT: the segment normal */
+		float edgeSeparation = FLT_MAX;
+		for ( int i = 0; i < count; ++i )
+		{
+			float sep = gdot( normal1, gsub( vertices[i], p1 ) );
+			if ( sep < edgeSeparation )
+			{
+				edgeSeparation = sep;
+				incidentIndex = i;
+			}
+		}
+		/* convex neighbours */
+		if ( sp.convex1 )
+		{
+			float s0 = FLT_MAX;
+			for ( int i = 0; i < count; ++i )
+			{
+				float sep = gdot( sp.normal0, gsub( vertices[i], p1 ) );
+				if ( sep < s0 )
+					s0 = sep;
+			}
+			if ( s0 > edgeSeparation )
+			{
+				edgeSeparation = s0;
+				incidentIndex = -1;
+			}
+		}
+		if ( sp.convex2 )
+		{
+			float s2 = FLT_MAX;
+			for ( int i = 0; i < count; ++i )
+			{
+				float sep = gdot( sp.normal2, gsub( vertices[i], p2 ) );
+				if ( sep < s2 )
+					s2 = sep;
+			}
+			if ( s2 > edgeSeparation )
+			{
+				edgeSeparation = s2;
+				incidentIndex = -1;
+			}
+		}
+		/* SAT: the polygon's admitted normals */
+		float polygonSeparation = -FLT_MAX;
+		int referenceIndex = -1;
+		for ( int i = 0; i < count; ++i )
+		{
+			b2gVec n = normals[i];
+			int type = gclassify_normal( &sp, gneg( n ) );
+			if ( type != B2G_NORMAL_ADMIT )
+				continue;
+			b2gVec p = vertices[i];
+			float sep = gmin( gdot( n, gsub( p2, p ) ), gdot( n, gsub( p1, p ) ) );
+			if ( sep > polygonSeparation )
+			{
+				polygonSeparation = sep;
+				referenceIndex = i;
+			}
+		}
+		if ( polygonSeparation > edgeSeparation )
+		{
+			int ia1 = referenceIndex;
+			int ia2 = ia1 < count - 1 ? ia1 + 1 : 0;
+			b2gVec a1 = vertices[ia1];
+			b2gVec a2 = vertices[ia2];
+			b2gVec n = normals[ia1];
+			float dot1 = gdot( n, gsub( p1, a1 ) );
+			float dot2 = gdot( n, gsub( p2, a1 ) );
+			if ( dot1 < dot2 )
+			{
+				if ( gdot( n0, n ) < gdot( normal1, n ) )
+					return;
+			}
+			else
+			{
+				if ( gdot( n2, n ) < gdot( normal1, n ) )
+					return;
+			}
+			gclip_segments( m, a1, a2, p1, p2, normals[ia1], radiusB, 0.0f, B2G_MAKE_ID( ia1, 1 ), B2G_MAKE_ID( ia2, 0 ) );
+			gsmooth_finish( m, xfA, xfB, gneg( normals[ia1] ) );
+			return;
+		}
+		if ( incidentIndex == -1 )
+			return;
+	}
+
+	/* the segment normal is the reference: find the incident polygon edge */
+	b2gVec b1, b2;
+	int ib1, ib2;
+	if ( incidentNormal != -1 )
+	{
+		ib1 = incidentNormal;
+		ib2 = ib1 < count - 1 ? ib1 + 1 : 0;
+		b1 = vertices[ib1];
+		b2 = vertices[ib2];
+	}
+	else
+	{
+		int i2 = incidentIndex;
+		int i1 = i2 > 0 ? i2 - 1 : count - 1;
+		float d1 = gdot( normal1, normals[i1] );
+		float d2 = gdot( normal1, normals[i2] );
+		if ( d1 < d2 )
+		{
+			ib1 = i1;
+			ib2 = i2;
+		}
+		else
+		{
+			ib1 = i2;
+			ib2 = i2 < count - 1 ? i2 + 1 : 0;
+		}
+		b1 = vertices[ib1];
+		b2 = vertices[ib2];
+	}
+	gclip_segments( m, p1, p2, b1, b2, normal1, 0.0f, radiusB, B2G_MAKE_ID( 0, ib2 ), B2G_MAKE_ID( 1, ib1 ) );
+	gsmooth_finish( m, xfA, xfB, m->normal );
+}
+
+/* Manifold of a registered shape pair with A the primary type (reference
+ * src/contact.c:150-183): circle=0 capsule=1 segment=2 polygon=3 smooth segment=4.
+ * `cache` (smooth segments only) is the contact's closest-feature cache. */
+B2G_HD void gcollide_shapes( b2gManifold* m, const b2gShapeGeo* a, b2gXf xfA, const b2gShapeGeo* b, b2gXf xfB,
+							 b2gDistCache* cache )
+{
+	if ( a->type == 4 )
+	{
+		b2gSmooth sa = gsmooth_of( a );
+		if ( b->type == 0 )
+			gcollide_smooth_circle( m, &sa, xfA, b->v[0], b->radius, xfB );
+		else
+		{
+			/* polygon, or a capsule as a rounded 2-gon (reference b2MakeCapsule) */
+			b2gPoly pb;
+			gshape_poly( &pb, b );
+			b2gVec centroid = b->type == 3 ? b->centroid : glerp( b->v[0], b->v[1], 0.5f );
+			gcollide_smooth_polygon( m, &sa, xfA, pb.v, pb.n, pb.count, pb.radius, centroid, xfB, cache );
+		}
+		return;
+	}
 	if ( b->type == 0 )
 	{
 		/* B is a circle */

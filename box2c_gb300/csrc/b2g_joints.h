@@ -106,8 +106,6 @@ __device__ __forceinline__ b2gVec mulmv( const float* m, b2gVec v )
 	return gv( m[0] * v.x + m[2] * v.y, m[1] * v.x + m[3] * v.y );
 }
 
-__device__ __forceinline__ b2gVec gleft( b2gVec v ) { return gv( -v.y, v.x ); }
-
 /* Mass properties and pose of a joint's two bodies at the start of the step. */
 struct JointBodies
 {

@@ -75,6 +75,7 @@ B2G_HD float gdot( b2gVec a, b2gVec b ) { return a.x * b.x + a.y * b.y; }
 B2G_HD float gcross( b2gVec a, b2gVec b ) { return a.x * b.y - a.y * b.x; }
 B2G_HD b2gVec gcross_sv( float s, b2gVec v ) { return gv( -s * v.y, s * v.x ); }
 B2G_HD b2gVec gright( b2gVec v ) { return gv( v.y, -v.x ); }
+B2G_HD b2gVec gleft( b2gVec v ) { return gv( -v.y, v.x ); }
 B2G_HD b2gVec gadd( b2gVec a, b2gVec b ) { return gv( a.x + b.x, a.y + b.y ); }
 B2G_HD b2gVec gsub( b2gVec a, b2gVec b ) { return gv( a.x - b.x, a.y - b.y ); }
 B2G_HD b2gVec gneg( b2gVec a ) { return gv( -a.x, -a.y ); }

@@ -136,22 +136,28 @@ static __device__ __noinline__ void narrowphase_polygons( b2gManifold* m, const 
 	gcollide_polygons_raw( m, gA->v, gA->n, gA->count, gA->radius, xfA, gB->v, gB->n, gB->count, gB->radius, xfB );
 }
 
+/* Other pairs; a smooth segment (chain link) reads and updates the contact's
+ * closest-feature cache (reference src/contact.c:138-148, the cache argument). */
 static __device__ __noinline__ void narrowphase_shapes( b2gManifold* m, const b2gShapeGeo* gA, b2gXf xfA, const b2gShapeGeo* gB,
-														b2gXf xfB )
+														b2gXf xfB, uint32_t* packedCache )
 {
-	gcollide_shapes( m, gA, xfA, gB, xfB );
+	b2gDistCache cache = gcache_unpack( gA->type == 4 ? *packedCache : 0u );
+	gcollide_shapes( m, gA, xfA, gB, xfB, &cache );
+	if ( gA->type == 4 )
+		*packedCache = gcache_pack( &cache );
 }
 
 /* Polygon pairs (the common case) take their own call, whose frame holds only the two
  * polygons in the contact frame; the other pairs' polygon copies stay out of it. */
-static __device__ __noinline__ void narrowphase( b2gManifold* m, const b2gShapeGeo* gA, b2gXf xfA, const b2gShapeGeo* gB, b2gXf xfB )
+static __device__ __noinline__ void narrowphase( b2gManifold* m, const b2gShapeGeo* gA, b2gXf xfA, const b2gShapeGeo* gB, b2gXf xfB,
+												 uint32_t* packedCache )
 {
 	if ( gA->isSensor || gB->isSensor )
 		gmanifold_clear( m );
 	else if ( gA->type == 3 && gB->type == 3 )
 		narrowphase_polygons( m, gA, xfA, gB, xfB );
 	else
-		narrowphase_shapes( m, gA, xfA, gB, xfB );
+		narrowphase_shapes( m, gA, xfA, gB, xfB, packedCache );
 }
 
 /* Sensor contacts: whether the shapes overlap, by their GJK distance with radii,
@@ -161,24 +167,11 @@ static __device__ __noinline__ void narrowphase( b2gManifold* m, const b2gShapeG
 static __device__ __noinline__ bool sensor_overlap( const b2gDevWorld& W, int id, const b2gShapeGeo* gA, b2gXf xfA,
 													const b2gShapeGeo* gB, b2gXf xfB )
 {
-	uint32_t packed = W.cCache[id];
-	b2gDistCache cache;
-	cache.count = (int)( packed & 3u );
-	for ( int i = 0; i < 3; ++i )
-	{
-		cache.indexA[i] = (int)( ( packed >> ( 2 + 3 * i ) ) & 7u );
-		cache.indexB[i] = (int)( ( packed >> ( 11 + 3 * i ) ) & 7u );
-	}
+	b2gDistCache cache = gcache_unpack( W.cCache[id] );
 	b2gProxy pa = gproxy_shape( gA );
 	b2gProxy pb = gproxy_shape( gB );
 	float d = gdistance( &cache, &pa, xfA, &pb, xfB );
-	packed = (uint32_t)cache.count;
-	for ( int i = 0; i < cache.count; ++i )
-	{
-		packed |= (uint32_t)cache.indexA[i] << ( 2 + 3 * i );
-		packed |= (uint32_t)cache.indexB[i] << ( 11 + 3 * i );
-	}
-	W.cCache[id] = packed;
+	W.cCache[id] = gcache_pack( &cache );
 	if ( d < FLT_EPSILON )
 		d = 0.0f;
 	else
@@ -248,7 +241,7 @@ static __device__ void collide_contact( const b2gDevWorld& W, int id )
 	const float oldN0 = prev->pts[0].normalImpulse, oldT0 = prev->pts[0].tangentImpulse;
 	const float oldN1 = prev->pts[1].normalImpulse, oldT1 = prev->pts[1].tangentImpulse;
 	b2gManifold m;
-	narrowphase( &m, gA, xfA, gB, xfB );
+	narrowphase( &m, gA, xfA, gB, xfB, W.cCache + id );
 
 	int pointCount = m.count;
 	bool touching = pointCount > 0;

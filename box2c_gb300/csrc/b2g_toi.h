@@ -33,6 +33,31 @@ typedef struct b2gDistCache
 	int indexA[3], indexB[3];
 } b2gDistCache;
 
+/* A closest-feature cache in one word: the count in bits 0-1, the three vertex indices
+ * of A in 3 bits each from bit 2, those of B from bit 11 (polygons have at most 8). */
+B2G_HD b2gDistCache gcache_unpack( uint32_t packed )
+{
+	b2gDistCache c;
+	c.count = (int)( packed & 3u );
+	for ( int i = 0; i < 3; ++i )
+	{
+		c.indexA[i] = (int)( ( packed >> ( 2 + 3 * i ) ) & 7u );
+		c.indexB[i] = (int)( ( packed >> ( 11 + 3 * i ) ) & 7u );
+	}
+	return c;
+}
+
+B2G_HD uint32_t gcache_pack( const b2gDistCache* c )
+{
+	uint32_t packed = (uint32_t)c->count;
+	for ( int i = 0; i < c->count; ++i )
+	{
+		packed |= (uint32_t)c->indexA[i] << ( 2 + 3 * i );
+		packed |= (uint32_t)c->indexB[i] << ( 11 + 3 * i );
+	}
+	return packed;
+}
+
 /* Time-of-impact outcomes (reference b2TOIState). */
 enum
 {
@@ -216,8 +241,9 @@ B2G_HD void gsimplex3( b2gSimplexVertex* v, int* count )
 }
 
 /* Distance between two proxies (radii not applied), warm-started and updated through
- * `cache`; at most 20 support evaluations. */
-B2G_HD float gdistance( b2gDistCache* cache, const b2gProxy* A, b2gXf xfA, const b2gProxy* B, b2gXf xfB )
+ * `cache`; at most 20 support evaluations.  The closest points go to *pointA and *pointB. */
+B2G_HD float gdistance_points( b2gDistCache* cache, const b2gProxy* A, b2gXf xfA, const b2gProxy* B, b2gXf xfB, b2gVec* pointA,
+							   b2gVec* pointB )
 {
 	b2gSimplexVertex v[3];
 	int count = cache->count;
@@ -303,8 +329,16 @@ B2G_HD float gdistance( b2gDistCache* cache, const b2gProxy* A, b2gXf xfA, const
 		cache->indexA[i] = v[i].indexA;
 		cache->indexB[i] = v[i].indexB;
 	}
+	*pointA = pa;
+	*pointB = pb;
 	float dx = pb.x - pa.x, dy = pb.y - pa.y;
 	return sqrtf( dx * dx + dy * dy );
+}
+
+B2G_HD float gdistance( b2gDistCache* cache, const b2gProxy* A, b2gXf xfA, const b2gProxy* B, b2gXf xfB )
+{
+	b2gVec pa, pb;
+	return gdistance_points( cache, A, xfA, B, xfB, &pa, &pb );
 }
 
 /* ------------------------------------------------------------ time of impact */

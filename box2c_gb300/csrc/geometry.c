@@ -247,6 +247,7 @@ void gshape_extent( const b2gShapeGeo* g, b2gVec lc, float* minExtent, float* ma
 			return;
 		}
 		case b2_segmentShape:
+		case b2_smoothSegmentShape:
 		{
 			b2gVec c1 = gsub( g->v[0], lc ), c2 = gsub( g->v[1], lc );
 			*minExtent = 0.0f;
@@ -282,6 +283,7 @@ b2gBox gshape_geo_aabb( const b2gShapeGeo* g, b2gXf xf )
 			return b;
 		}
 		case b2_segmentShape:
+		case b2_smoothSegmentShape:
 		{
 			b2gVec v1 = gxfpoint( xf, g->v[0] ), v2 = gxfpoint( xf, g->v[1] );
 			b.lo = gminv( v1, v2 );
@@ -405,11 +407,84 @@ static void geo_segment( b2gShapeGeo* g, const b2Segment* s )
 	g->v[1] = gvf( s->point2 );
 }
 
+static void geo_from_polygon( b2gShapeGeo* g, const b2Polygon* p );
+static void geo_capsule( b2gShapeGeo* g, const b2Capsule* c );
+static void geo_circle( b2gShapeGeo* g, const b2Circle* c );
+
 static b2Manifold collide( const b2gShapeGeo* a, b2Transform xfA, const b2gShapeGeo* b, b2Transform xfB )
 {
 	b2gManifold m;
-	gcollide_shapes( &m, a, xf_of( xfA ), b, xf_of( xfB ) );
+	b2gDistCache cache = gcache_unpack( 0u );
+	gcollide_shapes( &m, a, xf_of( xfA ), b, xf_of( xfB ), &cache );
 	return manifold_out( &m );
+}
+
+static void geo_smooth( b2gShapeGeo* g, const b2SmoothSegment* s )
+{
+	memset( g, 0, sizeof( *g ) );
+	g->type = b2_smoothSegmentShape;
+	g->count = 2;
+	g->v[0] = gvf( s->segment.point1 );
+	g->v[1] = gvf( s->segment.point2 );
+	g->v[2] = gvf( s->ghost1 );
+	g->v[3] = gvf( s->ghost2 );
+	g->centroid = glerp( g->v[0], g->v[1], 0.5f );
+}
+
+/* Smooth segment manifolds with the caller's closest-feature cache, read and updated
+ * (reference src/manifold.c:714-807, :944-1333). */
+static b2Manifold collide_cached( const b2gShapeGeo* a, b2Transform xfA, const b2gShapeGeo* b, b2Transform xfB,
+								  b2DistanceCache* cache )
+{
+	b2gDistCache c;
+	memset( &c, 0, sizeof( c ) );
+	if ( cache != NULL )
+	{
+		c.count = cache->count;
+		for ( int i = 0; i < 3; ++i )
+		{
+			c.indexA[i] = cache->indexA[i];
+			c.indexB[i] = cache->indexB[i];
+		}
+	}
+	b2gManifold m;
+	gcollide_shapes( &m, a, xf_of( xfA ), b, xf_of( xfB ), &c );
+	if ( cache != NULL )
+	{
+		cache->count = (uint16_t)c.count;
+		for ( int i = 0; i < 3; ++i )
+		{
+			cache->indexA[i] = (uint8_t)( i < c.count ? c.indexA[i] : 0 );
+			cache->indexB[i] = (uint8_t)( i < c.count ? c.indexB[i] : 0 );
+		}
+	}
+	return manifold_out( &m );
+}
+
+b2Manifold b2CollideSmoothSegmentAndCircle( const b2SmoothSegment* a, b2Transform xfA, const b2Circle* b, b2Transform xfB )
+{
+	b2gShapeGeo ga, gb;
+	geo_smooth( &ga, a );
+	geo_circle( &gb, b );
+	return collide_cached( &ga, xfA, &gb, xfB, NULL );
+}
+
+b2Manifold b2CollideSmoothSegmentAndCapsule( const b2SmoothSegment* a, b2Transform xfA, const b2Capsule* b, b2Transform xfB,
+											 b2DistanceCache* cache )
+{
+	b2gShapeGeo ga, gb;
+	geo_smooth( &ga, a );
+	geo_capsule( &gb, b );
+	return collide_cached( &ga, xfA, &gb, xfB, cache );
+}
+
+b2Manifold b2CollideSmoothSegmentAndPolygon( const b2SmoothSegment* a, b2Transform xfA, const b2Polygon* b, b2Transform xfB,
+											 b2DistanceCache* cache )
+{
+	b2gShapeGeo ga, gb;
+	geo_smooth( &ga, a );
+	geo_from_polygon( &gb, b );
+	return collide_cached( &ga, xfA, &gb, xfB, cache );
 }
 
 b2Manifold b2CollideCircles( const b2Circle* a, b2Transform xfA, const b2Circle* b, b2Transform xfB )

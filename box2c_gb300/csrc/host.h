@@ -147,6 +147,7 @@ typedef struct gBody
 	int headShape, shapeCount;
 	int headContactKey, contactCount;
 	int headJointKey, jointCount;
+	int headChainId;
 	void* userData;
 	uint16_t revision;
 	bool fixedRotation, isBullet, enableSleep, automaticMass;
@@ -163,9 +164,21 @@ typedef struct gShape
 	b2Filter filter;
 	void* userData;
 	int proxyKey;
+	int chainId; /* smooth segments of a chain: the chain, else -1 */
 	uint16_t revision;
 	bool isSensor, enableContactEvents, enableSensorEvents, enableHitEvents, enablePreSolveEvents;
 } gShape;
+
+/* A chain: the smooth segments made from one point list (reference src/shape.h:52-60). */
+typedef struct gChain
+{
+	int id; /* -1 when free */
+	int bodyId;
+	int nextChainId;
+	int* shapeIndices;
+	int count;
+	uint16_t revision;
+} gChain;
 
 typedef struct gEdge
 {
@@ -224,7 +237,7 @@ typedef struct gWorld
 	uint16_t revision;
 	int slot;
 
-	gIdPool bodyIds, shapeIds, contactIds, jointIds;
+	gIdPool bodyIds, shapeIds, contactIds, jointIds, chainIds;
 	gBody* bodies;
 	int bodyCap;
 	gShape* shapes;
@@ -233,6 +246,8 @@ typedef struct gWorld
 	int contactCap;
 	gJoint* joints;
 	int jointCap;
+	gChain* chains;
+	int chainCap;
 
 	/* pinned host mirrors in device layout, indexed by id */
 	float* hState; /* 8 per body */

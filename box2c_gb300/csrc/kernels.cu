@@ -364,7 +364,8 @@ __global__ void k_debug_collide( b2gDevWorld W, int id, float* out )
 	xfB.p = gv( xb.x, xb.y );
 	xfB.q = grot( xb.z, xb.w );
 	b2gManifold m;
-	narrowphase( &m, gA, xfA, gB, xfB );
+	uint32_t cache = W.cCache[id]; /* a copy: the contact's own cache stays as it was */
+	narrowphase( &m, gA, xfA, gB, xfB, &cache );
 	int* oi = (int*)out;
 	oi[0] = sA;
 	oi[1] = sB;

@@ -1662,3 +1662,117 @@ int b2s_joint_api_script( float* out, int capacity )
 	b2DestroyWorld( worldId );
 	return n;
 }
+
+b2WorldId b2s_chain_scene( int count, uint64_t seed )
+{
+	b2WorldDef wd = b2s_world_def();
+	b2WorldId worldId = b2CreateWorld( &wd );
+	if ( B2_IS_NULL( worldId ) )
+		return worldId;
+	b2sRandom rng;
+	b2s_seed( &rng, seed );
+	b2BodyDef gd = b2DefaultBodyDef();
+	b2BodyId groundId = b2CreateBody( worldId, &gd );
+
+	/* terrain: an open chain listed right to left, so its upper side collides */
+	enum
+	{
+		TERRAIN = 81
+	};
+	b2Vec2 terrain[TERRAIN];
+	float y = 0.0f;
+	for ( int i = 0; i < TERRAIN; ++i )
+	{
+		float dy = b2s_uniform( &rng, -0.35f, 0.35f );
+		y = y + dy;
+		y = y < -1.0f ? -1.0f : ( y > 2.0f ? 2.0f : y );
+		terrain[i] = ( b2Vec2 ){ 40.0f - 1.0f * i, y };
+	}
+	/* raised walls at both ends */
+	terrain[0].y = 12.0f;
+	terrain[TERRAIN - 1].y = 12.0f;
+	b2ChainDef cd = b2DefaultChainDef();
+	cd.points = terrain;
+	cd.count = TERRAIN;
+	cd.friction = 0.7f;
+	b2CreateChain( groundId, &cd );
+
+	/* bowl: a clockwise loop (its inside collides), open at the top by an inner lip */
+	enum
+	{
+		HALF = 12
+	};
+	b2Vec2 bowl[2 * HALF];
+	for ( int k = 0; k < HALF; ++k )
+	{
+		b2Vec2 u = b2s_circle_point( -1.0f + 2.0f * k / HALF );
+		bowl[k] = ( b2Vec2 ){ -15.0f + 5.0f * u.x, 14.0f + 4.0f * u.y };
+		bowl[HALF + k] = ( b2Vec2 ){ -15.0f - 5.0f * u.x, 14.0f - 4.0f * u.y };
+	}
+	b2Vec2 bowlCw[2 * HALF];
+	for ( int k = 0; k < 2 * HALF; ++k )
+		bowlCw[k] = bowl[2 * HALF - 1 - k];
+	b2ChainDef bd2 = b2DefaultChainDef();
+	bd2.points = bowlCw;
+	bd2.count = 2 * HALF;
+	bd2.isLoop = true;
+	bd2.restitution = 0.2f;
+	b2CreateChain( groundId, &bd2 );
+
+	/* bodies dropped over the terrain and into the bowl */
+	b2BodyDef bd = b2DefaultBodyDef();
+	bd.type = b2_dynamicBody;
+	b2ShapeDef sd = b2DefaultShapeDef();
+	b2Polygon box = b2MakeBox( 0.3f, 0.2f );
+	b2Polygon rounded = b2MakeRoundedBox( 0.2f, 0.2f, 0.1f );
+	b2Circle circle = { { 0.0f, 0.0f }, 0.25f };
+	b2Capsule capsule = { { -0.3f, 0.0f }, { 0.3f, 0.0f }, 0.15f };
+	for ( int k = 0; k < count; ++k )
+	{
+		float px, py;
+		if ( k % 8 == 7 )
+		{
+			/* inside the bowl */
+			px = -15.0f + b2s_uniform( &rng, -2.5f, 2.5f );
+			py = 13.0f + b2s_uniform( &rng, -1.0f, 2.0f );
+		}
+		else
+		{
+			px = b2s_uniform( &rng, -36.0f, 36.0f );
+			py = b2s_uniform( &rng, 3.0f, 10.0f );
+		}
+		bd.position = ( b2Vec2 ){ px, py };
+		b2BodyId id = b2CreateBody( worldId, &bd );
+		switch ( k & 3 )
+		{
+			case 0:
+				b2CreatePolygonShape( id, &sd, &box );
+				break;
+			case 1:
+				b2CreateCircleShape( id, &sd, &circle );
+				break;
+			case 2:
+				b2CreateCapsuleShape( id, &sd, &capsule );
+				break;
+			default:
+				b2CreatePolygonShape( id, &sd, &rounded );
+				break;
+		}
+	}
+
+	/* fast bodies and bullets shot down at the terrain */
+	b2Polygon pellet = b2MakeBox( 0.1f, 0.1f );
+	b2Circle shot = { { 0.0f, 0.0f }, 0.1f };
+	for ( int k = 0; k < 6; ++k )
+	{
+		bd.position = ( b2Vec2 ){ -25.0f + 10.0f * k, 8.0f };
+		bd.linearVelocity = ( b2Vec2 ){ 10.0f * ( ( k & 1 ) ? 1.0f : -1.0f ), -90.0f };
+		bd.isBullet = ( k % 3 ) == 0;
+		b2BodyId id = b2CreateBody( worldId, &bd );
+		if ( k & 1 )
+			b2CreateCircleShape( id, &sd, &shot );
+		else
+			b2CreatePolygonShape( id, &sd, &pellet );
+	}
+	return worldId;
+}

@@ -120,6 +120,12 @@ b2WorldId b2s_event_scene( int count, uint64_t seed );
  * elevator joints let their bodies collide. */
 b2WorldId b2s_joint_zoo( int copies, int flags, uint64_t seed );
 
+/* Chain scene: a static open chain of 80 links over seeded uneven terrain with raised
+ * ends, a closed clockwise loop (a bowl whose inside collides), `count` boxes, circles,
+ * capsules and rounded boxes dropped over them (every eighth into the bowl), and six
+ * fast bodies (two of them bullets) shot down at the terrain. */
+b2WorldId b2s_chain_scene( int count, uint64_t seed );
+
 /* Joint API script: one joint of each type between a ground and eight boxes; reads
  * every joint query (configuration, reaction force and torque, type-specific values)
  * before and after 30 steps, calls every setter (clamping ones with out-of-range values,

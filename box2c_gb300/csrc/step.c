@@ -722,6 +722,7 @@ typedef struct gSweepCtx
 	gShape* fast;
 	gBody* fastBody;
 	b2gSweep sweep;
+	b2gVec centroid1, centroid2; /* the fast shape's centroid at the sweep's ends */
 	float fraction;
 } gSweepCtx;
 
@@ -760,6 +761,23 @@ static bool sweep_query( int proxyId, int shapeId, void* context )
 		return true;
 	if ( should_bodies_collide( w, q->fastBody, body ) == false )
 		return true;
+	/* a chain link is passed over when the fast shape starts behind it or ends in front
+	 * of it, so bodies do not pause at link junctions (reference src/solver.c:869-885) */
+	if ( s->type == b2_smoothSegmentShape )
+	{
+		const float* x = w->hXf + 4 * s->bodyId;
+		b2gXf t;
+		t.p = gv( x[0], x[1] );
+		t.q = grot( x[2], x[3] );
+		const b2gShapeGeo* g = w->hGeo + shapeId;
+		b2gVec p1 = gxfpoint( t, g->v[0] );
+		b2gVec p2 = gxfpoint( t, g->v[1] );
+		b2gVec e = gsub( p2, p1 );
+		float offset1 = gcross( gsub( q->centroid1, p1 ), e );
+		float offset2 = gcross( gsub( q->centroid2, p1 ), e );
+		if ( offset1 < 0.0f || offset2 > 0.0f )
+			return true;
+	}
 
 	b2gProxy pa = gproxy_shape( w->hGeo + shapeId );
 	b2gProxy pb = gproxy_shape( w->hGeo + q->fast->id );
@@ -796,9 +814,16 @@ static void solve_continuous( gWorld* w, b2gRecord* recs, int n, bool bullet )
 	q.sweep.c2 = gv( recs[0].pose2[0], recs[0].pose2[1] );
 	q.sweep.q2 = grot( recs[0].pose2[2], recs[0].pose2[3] );
 	q.sweep.localCenter = gv( w->hCenters[4 * bodyId + 2], w->hCenters[4 * bodyId + 3] );
+	b2gXf xf1, xf2;
+	xf1.q = q.sweep.q1;
+	xf1.p = gsub( q.sweep.c1, grotate( q.sweep.q1, q.sweep.localCenter ) );
+	xf2.q = q.sweep.q2;
+	xf2.p = gsub( q.sweep.c2, grotate( q.sweep.q2, q.sweep.localCenter ) );
 	for ( int k = 0; k < n; ++k )
 	{
 		gShape* s = w->shapes + recs[k].shapeId;
+		q.centroid1 = gxfpoint( xf1, gshape_centroid( w->hGeo + s->id ) );
+		q.centroid2 = gxfpoint( xf2, gshape_centroid( w->hGeo + s->id ) );
 		if ( s->isSensor )
 			continue;
 		q.fast = s;

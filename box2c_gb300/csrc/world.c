@@ -120,6 +120,16 @@ b2ShapeDef b2DefaultShapeDef( void )
 	return d;
 }
 
+b2ChainDef b2DefaultChainDef( void )
+{
+	b2ChainDef d;
+	memset( &d, 0, sizeof( d ) );
+	d.friction = 0.6f;
+	d.filter = b2DefaultFilter();
+	d.internalValue = 1152023;
+	return d;
+}
+
 /* ------------------------------------------------------------ pinned mirrors */
 static int grow_cap( int have, int need )
 {
@@ -415,6 +425,11 @@ void b2DestroyWorld( b2WorldId worldId )
 	b2g_free( w->shapes );
 	b2g_free( w->contacts );
 	b2g_free( w->joints );
+	for ( int i = 0; i < w->chainCap; ++i )
+		if ( w->chains[i].id != B2G_NULL )
+			b2g_free( w->chains[i].shapeIndices );
+	b2g_free( w->chains );
+	gia_free( &w->chainIds.freeIds );
 	b2g_free( w->pending );
 	b2g_free( w->scratch );
 	b2g_free( w->recordSort );
@@ -562,6 +577,7 @@ b2BodyId b2CreateBody( b2WorldId worldId, const b2BodyDef* def )
 	b->headShape = B2G_NULL;
 	b->headContactKey = B2G_NULL;
 	b->headJointKey = B2G_NULL;
+	b->headChainId = B2G_NULL;
 	b->fixedRotation = def->fixedRotation;
 	b->isBullet = def->isBullet;
 	b->enableSleep = def->enableSleep;
@@ -875,7 +891,10 @@ void gbuffer_move( gWorld* w, int proxyKey )
 		gia_push( &w->moveArray, proxyKey );
 }
 
-static b2ShapeId create_shape( b2BodyId bodyId, const b2ShapeDef* def, b2ShapeType type, const b2gShapeGeo* geo )
+/* Shape creation (reference src/shape.c:62-170); chains skip the mass update as the
+ * reference's b2CreateShapeInternal does. */
+static b2ShapeId create_shape_internal( b2BodyId bodyId, const b2ShapeDef* def, b2ShapeType type, const b2gShapeGeo* geo,
+										bool updateMass )
 {
 	/* an invalid body (a null id from a failed creation included) gets no shape */
 	if ( b2Body_IsValid( bodyId ) == false )
@@ -958,6 +977,7 @@ static b2ShapeId create_shape( b2BodyId bodyId, const b2ShapeDef* def, b2ShapeTy
 		return b2_nullShapeId;
 	}
 	s->proxyKey = ( proxyId << 2 ) | proxyType;
+	s->chainId = B2G_NULL;
 	if ( proxyType != b2_staticBody || def->forceContactCreation )
 		gbuffer_move( w, s->proxyKey );
 
@@ -968,13 +988,18 @@ static b2ShapeId create_shape( b2BodyId bodyId, const b2ShapeDef* def, b2ShapeTy
 	body->headShape = id;
 	body->shapeCount += 1;
 
-	if ( body->automaticMass )
+	if ( updateMass && body->automaticMass )
 		gbody_update_mass( w, body );
 	w->shapesDirty = true;
 	w->shapeListsDirty = true;
 	w->bodiesDirty = true;
 	b2ShapeId sid = { id + 1, bodyId.world0, s->revision };
 	return sid;
+}
+
+static b2ShapeId create_shape( b2BodyId bodyId, const b2ShapeDef* def, b2ShapeType type, const b2gShapeGeo* geo )
+{
+	return create_shape_internal( bodyId, def, type, geo, true );
 }
 
 b2ShapeId b2CreatePolygonShape( b2BodyId bodyId, const b2ShapeDef* def, const b2Polygon* p )
@@ -1076,6 +1101,33 @@ b2Polygon b2Shape_GetPolygon( b2ShapeId id )
 	}
 	return p;
 }
+b2Segment b2Shape_GetSegment( b2ShapeId id )
+{
+	const b2gShapeGeo* g = s_worlds[id.world0]->hGeo + ( id.index1 - 1 );
+	b2Segment r = { { g->v[0].x, g->v[0].y }, { g->v[1].x, g->v[1].y } };
+	return r;
+}
+
+b2SmoothSegment b2Shape_GetSmoothSegment( b2ShapeId id )
+{
+	gWorld* w = s_worlds[id.world0];
+	const b2gShapeGeo* g = w->hGeo + ( id.index1 - 1 );
+	b2SmoothSegment r;
+	r.ghost1 = ( b2Vec2 ){ g->v[2].x, g->v[2].y };
+	r.segment.point1 = ( b2Vec2 ){ g->v[0].x, g->v[0].y };
+	r.segment.point2 = ( b2Vec2 ){ g->v[1].x, g->v[1].y };
+	r.ghost2 = ( b2Vec2 ){ g->v[3].x, g->v[3].y };
+	r.chainId = w->shapes[id.index1 - 1].chainId;
+	return r;
+}
+
+b2Capsule b2Shape_GetCapsule( b2ShapeId id )
+{
+	const b2gShapeGeo* g = s_worlds[id.world0]->hGeo + ( id.index1 - 1 );
+	b2Capsule r = { { g->v[0].x, g->v[0].y }, { g->v[1].x, g->v[1].y }, g->radius };
+	return r;
+}
+
 b2Circle b2Shape_GetCircle( b2ShapeId id )
 {
 	const b2gShapeGeo* g = s_worlds[id.world0]->hGeo + ( id.index1 - 1 );
@@ -1519,17 +1571,10 @@ void b2DestroyJoint( b2JointId jointId )
 	destroy_joint( w, get_joint( jointId ) );
 }
 
-void b2DestroyShape( b2ShapeId shapeId )
+/* Unlinks and frees a shape with its proxy and contacts (reference
+ * src/shape.c:220-269). */
+static void destroy_shape_internal( gWorld* w, gShape* s, gBody* b )
 {
-	if ( b2Shape_IsValid( shapeId ) == false )
-		return;
-	gWorld* w = s_worlds[shapeId.world0];
-	if ( w->locked )
-		return;
-	gworld_ensure_mirror( w );
-	gworld_ensure_shape_mirror( w );
-	gShape* s = get_shape( shapeId );
-	gBody* b = w->bodies + s->bodyId;
 	int id = s->id;
 	if ( s->prev != B2G_NULL )
 		w->shapes[s->prev].next = s->next;
@@ -1551,10 +1596,182 @@ void b2DestroyShape( b2ShapeId shapeId )
 	s->id = B2G_NULL;
 	if ( s->enableHitEvents )
 		w->hitShapes -= 1;
+	w->shapeListsDirty = true;
+}
+
+void b2DestroyShape( b2ShapeId shapeId )
+{
+	if ( b2Shape_IsValid( shapeId ) == false )
+		return;
+	gWorld* w = s_worlds[shapeId.world0];
+	if ( w->locked )
+		return;
+	gworld_ensure_mirror( w );
+	gworld_ensure_shape_mirror( w );
+	gShape* s = get_shape( shapeId );
+	gBody* b = w->bodies + s->bodyId;
+	destroy_shape_internal( w, s, b );
 	if ( b->automaticMass )
 		gbody_update_mass( w, b );
-	w->shapeListsDirty = true;
 	w->bodiesDirty = true;
+}
+
+/* ------------------------------------------------------------ chains */
+/* Chain creation (reference src/shape.c:292-403): one smooth segment per link, each
+ * with the neighbouring points as ghost vertices; a loop closes on its first point. */
+b2ChainId b2CreateChain( b2BodyId bodyId, const b2ChainDef* def )
+{
+	if ( b2Body_IsValid( bodyId ) == false || def->count < 4 || def->points == NULL )
+		return b2_nullChainId;
+	gWorld* w = body_world( bodyId );
+	if ( w->locked )
+		return b2_nullChainId;
+	gworld_ensure_mirror( w );
+	int n = def->count;
+	int links = def->isLoop ? n : n - 3;
+	int* indices = (int*)b2g_alloc( sizeof( int ) * (size_t)n );
+	int chainId = gid_alloc( &w->chainIds );
+	bool ok = indices != NULL;
+	if ( ok )
+		GROW_RECORDS( w->chains, w->chainCap, chainId + 1, gChain, ok );
+	if ( ok == false )
+	{
+		b2g_free( indices );
+		gid_unalloc( &w->chainIds, chainId );
+		w->status = w->status ? w->status : B2_STATUS_OUT_OF_HOST_MEMORY;
+		return b2_nullChainId;
+	}
+	gBody* body = get_body( bodyId );
+	gChain* chain = w->chains + chainId;
+	uint16_t rev = chain->revision;
+	memset( chain, 0, sizeof( *chain ) );
+	chain->revision = (uint16_t)( rev + 1 );
+	chain->id = chainId;
+	chain->bodyId = body->id;
+	chain->nextChainId = body->headChainId;
+	chain->shapeIndices = indices;
+	chain->count = links;
+	body->headChainId = chainId;
+
+	b2ShapeDef sd = b2DefaultShapeDef();
+	sd.userData = def->userData;
+	sd.restitution = def->restitution;
+	sd.friction = def->friction;
+	sd.filter = def->filter;
+	sd.enableContactEvents = false;
+	sd.enableHitEvents = false;
+	sd.enableSensorEvents = false;
+
+	const b2Vec2* pts = def->points;
+	for ( int i = 0; i < links; ++i )
+	{
+		/* ghost1, point1, point2, ghost2 of link i */
+		int i0, i1, i2, i3;
+		if ( def->isLoop )
+		{
+			i1 = i;
+			i2 = ( i + 1 ) % n;
+			i0 = ( i + n - 1 ) % n;
+			i3 = ( i + 2 ) % n;
+		}
+		else
+		{
+			i0 = i;
+			i1 = i + 1;
+			i2 = i + 2;
+			i3 = i + 3;
+		}
+		b2gShapeGeo g;
+		memset( &g, 0, sizeof( g ) );
+		g.count = 2;
+		g.v[0] = gv( pts[i1].x, pts[i1].y );
+		g.v[1] = gv( pts[i2].x, pts[i2].y );
+		g.v[2] = gv( pts[i0].x, pts[i0].y );
+		g.v[3] = gv( pts[i3].x, pts[i3].y );
+		g.centroid = glerp( g.v[0], g.v[1], 0.5f );
+		b2ShapeId sid = create_shape_internal( bodyId, &sd, b2_smoothSegmentShape, &g, false );
+		int shapeId = sid.index1 - 1;
+		indices[i] = shapeId;
+		if ( shapeId >= 0 )
+			w->shapes[shapeId].chainId = chainId;
+	}
+	b2ChainId id = { chainId + 1, (uint16_t)w->slot, chain->revision };
+	return id;
+}
+
+static gChain* get_chain( b2ChainId id ) { return s_worlds[id.world0]->chains + ( id.index1 - 1 ); }
+
+bool b2Chain_IsValid( b2ChainId id )
+{
+	if ( id.world0 >= s_worldCap || s_worlds[id.world0] == NULL || !s_worlds[id.world0]->inUse )
+		return false;
+	gWorld* w = s_worlds[id.world0];
+	if ( id.index1 < 1 || id.index1 > w->chainCap )
+		return false;
+	gChain* c = w->chains + ( id.index1 - 1 );
+	return c->id == id.index1 - 1 && c->revision == id.revision;
+}
+
+/* Chain destruction (reference src/shape.c:405-451). */
+void b2DestroyChain( b2ChainId chainId )
+{
+	if ( b2Chain_IsValid( chainId ) == false )
+		return;
+	gWorld* w = s_worlds[chainId.world0];
+	if ( w->locked )
+		return;
+	gworld_ensure_mirror( w );
+	gworld_ensure_shape_mirror( w );
+	gChain* chain = get_chain( chainId );
+	gBody* body = w->bodies + chain->bodyId;
+	int* link = &body->headChainId;
+	while ( *link != B2G_NULL && *link != chain->id )
+		link = &w->chains[*link].nextChainId;
+	if ( *link == B2G_NULL )
+		return;
+	*link = chain->nextChainId;
+	for ( int i = 0; i < chain->count; ++i )
+	{
+		int sid = chain->shapeIndices[i];
+		if ( sid >= 0 && w->shapes[sid].id == sid )
+			destroy_shape_internal( w, w->shapes + sid, body );
+	}
+	b2g_free( chain->shapeIndices );
+	chain->shapeIndices = NULL;
+	gid_free( &w->chainIds, chain->id );
+	chain->id = B2G_NULL;
+}
+
+void b2Chain_SetFriction( b2ChainId chainId, float friction )
+{
+	gWorld* w = s_worlds[chainId.world0];
+	if ( w->locked )
+		return;
+	gChain* chain = get_chain( chainId );
+	for ( int i = 0; i < chain->count; ++i )
+		w->shapes[chain->shapeIndices[i]].friction = friction;
+}
+
+void b2Chain_SetRestitution( b2ChainId chainId, float restitution )
+{
+	gWorld* w = s_worlds[chainId.world0];
+	if ( w->locked )
+		return;
+	gChain* chain = get_chain( chainId );
+	for ( int i = 0; i < chain->count; ++i )
+		w->shapes[chain->shapeIndices[i]].restitution = restitution;
+}
+
+b2ChainId b2Shape_GetParentChain( b2ShapeId shapeId )
+{
+	gWorld* w = s_worlds[shapeId.world0];
+	gShape* s = get_shape( shapeId );
+	if ( s->type == b2_smoothSegmentShape && s->chainId != B2G_NULL )
+	{
+		b2ChainId id = { s->chainId + 1, shapeId.world0, w->chains[s->chainId].revision };
+		return id;
+	}
+	return b2_nullChainId;
 }
 
 void b2DestroyBody( b2BodyId bodyId )
@@ -1589,6 +1806,16 @@ void b2DestroyBody( b2BodyId bodyId )
 		if ( s->enableHitEvents )
 			w->hitShapes -= 1;
 		sid = s->next;
+	}
+	/* the chains' shapes went with the body's shapes above (reference src/body.c:381-395) */
+	for ( int cid = b->headChainId; cid != B2G_NULL; )
+	{
+		gChain* chain = w->chains + cid;
+		b2g_free( chain->shapeIndices );
+		chain->shapeIndices = NULL;
+		gid_free( &w->chainIds, cid );
+		chain->id = B2G_NULL;
+		cid = chain->nextChainId;
 	}
 	/* the awake set drops the body by moving its last body into the slot */
 	if ( b->awakeIndex != B2G_NULL )

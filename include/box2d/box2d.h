@@ -89,6 +89,17 @@ B2_API float b2Shape_GetRestitution( b2ShapeId shapeId );
 B2_API b2Filter b2Shape_GetFilter( b2ShapeId shapeId );
 B2_API b2Polygon b2Shape_GetPolygon( b2ShapeId shapeId );
 B2_API b2Circle b2Shape_GetCircle( b2ShapeId shapeId );
+B2_API b2Segment b2Shape_GetSegment( b2ShapeId shapeId );
+B2_API b2SmoothSegment b2Shape_GetSmoothSegment( b2ShapeId shapeId );
+B2_API b2Capsule b2Shape_GetCapsule( b2ShapeId shapeId );
+B2_API b2ChainId b2Shape_GetParentChain( b2ShapeId shapeId );
+
+/* Chains of smooth segments (reference box2d.h:576-594). */
+B2_API b2ChainId b2CreateChain( b2BodyId bodyId, const b2ChainDef* def );
+B2_API void b2DestroyChain( b2ChainId chainId );
+B2_API void b2Chain_SetFriction( b2ChainId chainId, float friction );
+B2_API void b2Chain_SetRestitution( b2ChainId chainId, float restitution );
+B2_API bool b2Chain_IsValid( b2ChainId id );
 B2_API b2AABB b2Shape_GetAABB( b2ShapeId shapeId );
 
 /* Joints: generic (reference box2d.h:605-646). */

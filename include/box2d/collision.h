@@ -155,6 +155,14 @@ B2_API b2Manifold b2CollidePolygonAndCapsule( const b2Polygon* polygonA, b2Trans
 B2_API b2Manifold b2CollidePolygons( const b2Polygon* polygonA, b2Transform xfA, const b2Polygon* polygonB, b2Transform xfB );
 B2_API b2Manifold b2CollideSegmentAndPolygon( const b2Segment* segmentA, b2Transform xfA, const b2Polygon* polygonB,
 											  b2Transform xfB );
+/* Chain links (reference collision.h:557-567): one-sided, with ghost vertices; the
+ * capsule and polygon forms warm-start from and update the caller's distance cache. */
+B2_API b2Manifold b2CollideSmoothSegmentAndCircle( const b2SmoothSegment* smoothSegmentA, b2Transform xfA,
+												   const b2Circle* circleB, b2Transform xfB );
+B2_API b2Manifold b2CollideSmoothSegmentAndCapsule( const b2SmoothSegment* smoothSegmentA, b2Transform xfA,
+													const b2Capsule* capsuleB, b2Transform xfB, b2DistanceCache* cache );
+B2_API b2Manifold b2CollideSmoothSegmentAndPolygon( const b2SmoothSegment* smoothSegmentA, b2Transform xfA,
+													const b2Polygon* polygonB, b2Transform xfB, b2DistanceCache* cache );
 
 #define b2_defaultCategoryBits ( 0x00000001 )
 #define b2_defaultMaskBits ( 0xFFFFFFFF )

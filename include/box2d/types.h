@@ -209,6 +209,22 @@ typedef struct b2RevoluteJointDef
 
 B2_API b2RevoluteJointDef b2DefaultRevoluteJointDef( void );
 
+/* Chain definition (reference types.h:364-393): at least four points; a loop connects
+ * the last point to the first. */
+typedef struct b2ChainDef
+{
+	void* userData;
+	const b2Vec2* points;
+	int32_t count;
+	float friction;
+	float restitution;
+	b2Filter filter;
+	bool isLoop;
+	int32_t internalValue;
+} b2ChainDef;
+
+B2_API b2ChainDef b2DefaultChainDef( void );
+
 /* Distance joint definition (reference types.h:464-517). */
 typedef struct b2DistanceJointDef
 {

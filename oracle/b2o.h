@@ -137,6 +137,13 @@ typedef struct oSegment
 	oVec p1, p2;
 } oSegment;
 
+/* Chain link (reference b2SmoothSegment, include/box2d/collision.h:159-172). */
+typedef struct oSmooth
+{
+	oVec ghost1, p1, p2, ghost2;
+	int chainId;
+} oSmooth;
+
 typedef struct oMPoint
 {
 	oVec point, anchorA, anchorB;
@@ -173,6 +180,9 @@ typedef struct oDistCache
 	int indexA[3], indexB[3];
 } oDistCache;
 
+oManifold o_collide_smooth_circle( const oSmooth* a, oXf xfA, const oCircle* b, oXf xfB );
+oManifold o_collide_smooth_polygon( const oSmooth* a, oXf xfA, const oPolygon* b, oXf xfB, oDistCache* cache );
+
 /* ---------------------------------------------------------------- world records */
 typedef struct oShape
 {
@@ -192,6 +202,7 @@ typedef struct oShape
 		oCircle circle;
 		oCapsule capsule;
 		oSegment segment;
+		oSmooth smooth;
 	};
 	uint16_t revision;
 	bool isSensor, enableContactEvents, enableSensorEvents, enableHitEvents, enablePreSolveEvents;
@@ -206,6 +217,7 @@ typedef struct oBody
 	int headShape, shapeCount;
 	int headContactKey, contactCount;
 	int headJointKey, jointCount;
+	int headChainId;
 	void* userData;
 	uint16_t revision;
 	bool fixedRotation, isBullet, enableSleep, isSpeedCapped, automaticMass;
@@ -261,6 +273,17 @@ typedef struct oContact
 	uint32_t simFlags;
 	oDistCache cache; /* sensor overlap test (reference src/contact.h:136) */
 } oContact;
+
+/* A chain of smooth segments (reference src/shape.h:52-60). */
+typedef struct oChain
+{
+	int id; /* -1 when free */
+	int bodyId;
+	int nextChainId;
+	int* shapeIndices;
+	int count;
+	uint16_t revision;
+} oChain;
 
 typedef struct oSoft
 {
@@ -406,7 +429,7 @@ typedef struct oWorld
 	uint16_t revision;
 	int slot;
 
-	oIdPool bodyIds, shapeIds, contactIds, jointIds;
+	oIdPool bodyIds, shapeIds, contactIds, jointIds, chainIds;
 	oBody* bodies;
 	int bodyCap;
 	oShape* shapes;
@@ -415,6 +438,8 @@ typedef struct oWorld
 	int contactCap;
 	oJoint* joints;
 	int jointCap;
+	struct oChain* chains;
+	int chainCap;
 
 	oIntArray awake;		 /* awake body ids in solver order */
 	oIntArray staticBodies;	 /* static body ids */

@@ -253,6 +253,13 @@ oBox o_shape_aabb( const oShape* s, oXf xf )
 			oBox b = { ominv( v1, v2 ), omaxv( v1, v2 ) };
 			return b;
 		}
+		case b2_smoothSegmentShape:
+		{
+			oVec v1 = oxfpoint( xf, s->smooth.p1 );
+			oVec v2 = oxfpoint( xf, s->smooth.p2 );
+			oBox b = { ominv( v1, v2 ), omaxv( v1, v2 ) };
+			return b;
+		}
 		default:
 		{
 			oBox b = { xf.p, xf.p };
@@ -358,6 +365,14 @@ static oExtent shape_extent( const oShape* s, oVec lc )
 			e.minExtent = 0;
 			oVec c1 = osub( s->segment.p1, lc );
 			oVec c2 = osub( s->segment.p2, lc );
+			e.maxExtent = RSQRT( omax( olen2( c1 ), olen2( c2 ) ) );
+			break;
+		}
+		case b2_smoothSegmentShape:
+		{
+			e.minExtent = 0;
+			oVec c1 = osub( s->smooth.p1, lc );
+			oVec c2 = osub( s->smooth.p2, lc );
 			e.maxExtent = RSQRT( omax( olen2( c1 ), olen2( c2 ) ) );
 			break;
 		}
@@ -897,6 +912,368 @@ oManifold o_collide_polygons( const oPolygon* polyA, oXf xfA, const oPolygon* po
 	return m;
 }
 
+/* ------------------------------------------------------------ smooth segments
+ * Chain links collide on their right side only; the ghost vertices decide which normals a
+ * link may produce (reference src/manifold.c:714-1333). */
+static oVec o_leftperp( oVec v ) { return ov( -v.y, v.x ); }
+
+oManifold o_collide_smooth_circle( const oSmooth* a, oXf xfA, const oCircle* b, oXf xfB )
+{
+	oManifold m = empty_manifold();
+	oXf xf = oinvmulxf( xfA, xfB );
+	oVec pB = oxfpoint( xf, b->center );
+	oVec p1 = a->p1;
+	oVec p2 = a->p2;
+	oVec e = osub( p2, p1 );
+	b2r offset = odot( oright( e ), osub( pB, p1 ) );
+	if ( offset < R( 0 ) )
+		return m;
+	b2r u = odot( e, osub( p2, pB ) );
+	b2r v = odot( e, osub( pB, p1 ) );
+	oVec pA;
+	if ( v <= R( 0 ) )
+	{
+		oVec prevEdge = osub( p1, a->ghost1 );
+		b2r uPrev = odot( prevEdge, osub( pB, p1 ) );
+		if ( uPrev <= R( 0 ) )
+			return m;
+		pA = p1;
+	}
+	else if ( u <= R( 0 ) )
+	{
+		oVec nextEdge = osub( a->ghost2, p2 );
+		b2r vNext = odot( nextEdge, osub( pB, p2 ) );
+		if ( vNext > R( 0 ) )
+			return m;
+		pA = p2;
+	}
+	else
+	{
+		b2r ee = odot( e, e );
+		pA = ov( u * p1.x + v * p2.x, u * p1.y + v * p2.y );
+		pA = ee > R( 0 ) ? omulsv( R( 1 ) / ee, pA ) : p1;
+	}
+	b2r distance;
+	oVec normal = olen_normalize( &distance, osub( pB, pA ) );
+	b2r radius = b->radius;
+	b2r separation = distance - radius;
+	if ( separation > O_SPECULATIVE )
+		return m;
+	oVec cA = pA;
+	oVec cB = omuladd( pB, -radius, normal );
+	oVec contactPointA = olerp( cA, cB, R( 0.5f ) );
+	m.normal = orotate( xfA.q, normal );
+	oMPoint* mp = m.pts + 0;
+	mp->anchorA = orotate( xfA.q, contactPointA );
+	mp->anchorB = oadd( mp->anchorA, osub( xfA.p, xfB.p ) );
+	mp->point = oadd( xfA.p, mp->anchorA );
+	mp->separation = separation;
+	mp->id = 0;
+	m.count = 1;
+	return m;
+}
+
+static oManifold o_clip_segments( oVec a1, oVec a2, oVec b1, oVec b2, oVec normal, b2r ra, b2r rb, uint16_t id1, uint16_t id2 )
+{
+	oManifold m = empty_manifold();
+	oVec tangent = o_leftperp( normal );
+	b2r lower1 = 0;
+	b2r upper1 = odot( osub( a2, a1 ), tangent );
+	b2r upper2 = odot( osub( b1, a1 ), tangent );
+	b2r lower2 = odot( osub( b2, a1 ), tangent );
+	if ( upper2 < lower1 || upper1 < lower2 )
+		return m;
+	oVec vLower = ( lower2 < lower1 && upper2 - lower2 > O_EPS ) ? olerp( b2, b1, ( lower1 - lower2 ) / ( upper2 - lower2 ) ) : b2;
+	oVec vUpper = ( upper2 > upper1 && upper2 - lower2 > O_EPS ) ? olerp( b2, b1, ( upper1 - lower2 ) / ( upper2 - lower2 ) ) : b1;
+	b2r separationLower = odot( osub( vLower, a1 ), normal );
+	b2r separationUpper = odot( osub( vUpper, a1 ), normal );
+	vLower = omuladd( vLower, R( 0.5f ) * ( ra - rb - separationLower ), normal );
+	vUpper = omuladd( vUpper, R( 0.5f ) * ( ra - rb - separationUpper ), normal );
+	b2r radius = ra + rb;
+	m.normal = normal;
+	m.pts[0].anchorA = vLower;
+	m.pts[0].separation = separationLower - radius;
+	m.pts[0].id = id1;
+	m.pts[1].anchorA = vUpper;
+	m.pts[1].separation = separationUpper - radius;
+	m.pts[1].id = id2;
+	m.count = 2;
+	return m;
+}
+
+enum
+{
+	O_NORMAL_SKIP,
+	O_NORMAL_ADMIT,
+	O_NORMAL_SNAP
+};
+
+typedef struct oSmoothParams
+{
+	oVec edge1, normal0, normal2;
+	bool convex1, convex2;
+} oSmoothParams;
+
+static int o_classify_normal( const oSmoothParams* p, oVec normal )
+{
+	const b2r sinTol = R( 0.01f );
+	if ( odot( normal, p->edge1 ) <= R( 0 ) )
+	{
+		if ( p->convex1 )
+			return ocross( normal, p->normal0 ) > sinTol ? O_NORMAL_SKIP : O_NORMAL_ADMIT;
+		return O_NORMAL_SNAP;
+	}
+	if ( p->convex2 )
+		return ocross( p->normal2, normal ) > sinTol ? O_NORMAL_SKIP : O_NORMAL_ADMIT;
+	return O_NORMAL_SNAP;
+}
+
+/* frame-A clip result to anchors and points, normal as given (in frame A) */
+static void o_smooth_finish( oManifold* m, oXf xfA, oXf xfB, oVec normalA )
+{
+	m->normal = orotate( xfA.q, normalA );
+	m->pts[0].anchorA = orotate( xfA.q, m->pts[0].anchorA );
+	m->pts[1].anchorA = orotate( xfA.q, m->pts[1].anchorA );
+	oVec pAB = osub( xfA.p, xfB.p );
+	m->pts[0].anchorB = oadd( m->pts[0].anchorA, pAB );
+	m->pts[1].anchorB = oadd( m->pts[1].anchorA, pAB );
+	m->pts[0].point = oadd( xfA.p, m->pts[0].anchorA );
+	m->pts[1].point = oadd( xfA.p, m->pts[1].anchorA );
+}
+
+#define O_MAKE_ID( A, B ) ( (uint16_t)( ( (uint8_t)( A ) << 8 ) | (uint8_t)( B ) ) )
+
+oManifold o_collide_smooth_polygon( const oSmooth* a, oXf xfA, const oPolygon* b, oXf xfB, oDistCache* cache )
+{
+	oManifold m = empty_manifold();
+	oXf xf = oinvmulxf( xfA, xfB );
+	oVec centroidB = oxfpoint( xf, b->centroid );
+	b2r radiusB = b->radius;
+	oVec p1 = a->p1;
+	oVec p2 = a->p2;
+	oVec edge1 = onormalize( osub( p2, p1 ) );
+	oSmoothParams sp;
+	memset( &sp, 0, sizeof( sp ) );
+	sp.edge1 = edge1;
+	const b2r convexTol = R( 0.01f );
+	oVec edge0 = onormalize( osub( p1, a->ghost1 ) );
+	sp.normal0 = oright( edge0 );
+	sp.convex1 = ocross( edge0, edge1 ) >= convexTol;
+	oVec edge2 = onormalize( osub( a->ghost2, p2 ) );
+	sp.normal2 = oright( edge2 );
+	sp.convex2 = ocross( edge1, edge2 ) >= convexTol;
+
+	oVec normal1 = oright( edge1 );
+	bool behind1 = odot( normal1, osub( centroidB, p1 ) ) < R( 0 );
+	bool behind0 = true;
+	bool behind2 = true;
+	if ( sp.convex1 )
+		behind0 = odot( sp.normal0, osub( centroidB, p1 ) ) < R( 0 );
+	if ( sp.convex2 )
+		behind2 = odot( sp.normal2, osub( centroidB, p2 ) ) < R( 0 );
+	if ( behind1 && behind0 && behind2 )
+		return m;
+
+	int count = b->count;
+	oVec vertices[8];
+	oVec normals[8];
+	for ( int i = 0; i < count; ++i )
+	{
+		vertices[i] = oxfpoint( xf, b->v[i] );
+		normals[i] = orotate( xf.q, b->n[i] );
+	}
+	oVec segPts[2] = { p1, p2 };
+	oProxy proxyA = o_make_proxy( segPts, 2, R( 0 ) );
+	oProxy proxyB = o_make_proxy( vertices, count, R( 0 ) );
+	oXf identity;
+	identity.p = ov( 0, 0 );
+	identity.q = orot( 1, 0 );
+	oVec pointA, pointB;
+	b2r distance = o_distance( cache, &proxyA, identity, &proxyB, identity, &pointA, &pointB );
+	if ( distance > radiusB + O_SPECULATIVE )
+		return m;
+
+	oVec n0 = sp.convex1 ? sp.normal0 : normal1;
+	oVec n2 = sp.convex2 ? sp.normal2 : normal1;
+	int incidentIndex = -1;
+	int incidentNormal = -1;
+	if ( behind1 == false && distance > R( 0.1f ) * O_LINEAR_SLOP )
+	{
+		if ( cache->count == 1 )
+		{
+			oVec normal = onormalize( osub( pointB, pointA ) );
+			int type = o_classify_normal( &sp, normal );
+			if ( type == O_NORMAL_SKIP )
+				return m;
+			if ( type == O_NORMAL_ADMIT )
+			{
+				m.normal = orotate( xfA.q, normal );
+				oMPoint* cp = m.pts + 0;
+				cp->anchorA = orotate( xfA.q, pointA );
+				cp->anchorB = oadd( cp->anchorA, osub( xfA.p, xfB.p ) );
+				cp->point = oadd( xfA.p, cp->anchorA );
+				cp->separation = distance - radiusB;
+				cp->id = O_MAKE_ID( cache->indexA[0], cache->indexB[0] );
+				m.count = 1;
+				return m;
+			}
+			incidentIndex = cache->indexB[0];
+		}
+		else
+		{
+			int ia1 = cache->indexA[0], ia2 = cache->indexA[1];
+			int ib1 = cache->indexB[0], ib2 = cache->indexB[1];
+			if ( ia1 == ia2 )
+			{
+				oVec normalB = osub( pointA, pointB );
+				b2r dot1 = odot( normalB, normals[ib1] );
+				b2r dot2 = odot( normalB, normals[ib2] );
+				int ib = dot1 > dot2 ? ib1 : ib2;
+				normalB = normals[ib];
+				int type = o_classify_normal( &sp, oneg( normalB ) );
+				if ( type == O_NORMAL_SKIP )
+					return m;
+				if ( type == O_NORMAL_ADMIT )
+				{
+					ib1 = ib;
+					ib2 = ib < count - 1 ? ib + 1 : 0;
+					oVec b1 = vertices[ib1];
+					oVec b2 = vertices[ib2];
+					dot1 = odot( normalB, osub( p1, b1 ) );
+					dot2 = odot( normalB, osub( p2, b1 ) );
+					if ( dot1 < dot2 )
+					{
+						if ( odot( n0, normalB ) < odot( normal1, normalB ) )
+							return m;
+					}
+					else if ( odot( n2, normalB ) < odot( normal1, normalB ) )
+						return m;
+					m = o_clip_segments( b1, b2, p1, p2, normalB, radiusB, 0, O_MAKE_ID( ib1, 1 ), O_MAKE_ID( ib2, 0 ) );
+					o_smooth_finish( &m, xfA, xfB, oneg( normalB ) );
+					return m;
+				}
+				incidentNormal = ib;
+			}
+			else
+			{
+				b2r dot1 = odot( normal1, osub( vertices[ib1], p1 ) );
+				b2r dot2 = odot( normal1, osub( vertices[ib2], p2 ) );
+				incidentIndex = dot1 < dot2 ? ib1 : ib2;
+			}
+		}
+	}
+	else
+	{
+		b2r edgeSeparation = O_MAX;
+		for ( int i = 0; i < count; ++i )
+		{
+			b2r sep = odot( normal1, osub( vertices[i], p1 ) );
+			if ( sep < edgeSeparation )
+			{
+				edgeSeparation = sep;
+				incidentIndex = i;
+			}
+		}
+		if ( sp.convex1 )
+		{
+			b2r s0 = O_MAX;
+			for ( int i = 0; i < count; ++i )
+			{
+				b2r sep = odot( sp.normal0, osub( vertices[i], p1 ) );
+				if ( sep < s0 )
+					s0 = sep;
+			}
+			if ( s0 > edgeSeparation )
+			{
+				edgeSeparation = s0;
+				incidentIndex = -1;
+			}
+		}
+		if ( sp.convex2 )
+		{
+			b2r s2 = O_MAX;
+			for ( int i = 0; i < count; ++i )
+			{
+				b2r sep = odot( sp.normal2, osub( vertices[i], p2 ) );
+				if ( sep < s2 )
+					s2 = sep;
+			}
+			if ( s2 > edgeSeparation )
+			{
+				edgeSeparation = s2;
+				incidentIndex = -1;
+			}
+		}
+		b2r polygonSeparation = -O_MAX;
+		int referenceIndex = -1;
+		for ( int i = 0; i < count; ++i )
+		{
+			oVec n = normals[i];
+			if ( o_classify_normal( &sp, oneg( n ) ) != O_NORMAL_ADMIT )
+				continue;
+			oVec p = vertices[i];
+			b2r sep = omin( odot( n, osub( p2, p ) ), odot( n, osub( p1, p ) ) );
+			if ( sep > polygonSeparation )
+			{
+				polygonSeparation = sep;
+				referenceIndex = i;
+			}
+		}
+		if ( polygonSeparation > edgeSeparation )
+		{
+			int ia1 = referenceIndex;
+			int ia2 = ia1 < count - 1 ? ia1 + 1 : 0;
+			oVec a1 = vertices[ia1];
+			oVec a2 = vertices[ia2];
+			oVec n = normals[ia1];
+			b2r dot1 = odot( n, osub( p1, a1 ) );
+			b2r dot2 = odot( n, osub( p2, a1 ) );
+			if ( dot1 < dot2 )
+			{
+				if ( odot( n0, n ) < odot( normal1, n ) )
+					return m;
+			}
+			else if ( odot( n2, n ) < odot( normal1, n ) )
+				return m;
+			m = o_clip_segments( a1, a2, p1, p2, normals[ia1], radiusB, 0, O_MAKE_ID( ia1, 1 ), O_MAKE_ID( ia2, 0 ) );
+			o_smooth_finish( &m, xfA, xfB, oneg( normals[ia1] ) );
+			return m;
+		}
+		if ( incidentIndex == -1 )
+			return m;
+	}
+
+	oVec b1, b2;
+	int ib1, ib2;
+	if ( incidentNormal != -1 )
+	{
+		ib1 = incidentNormal;
+		ib2 = ib1 < count - 1 ? ib1 + 1 : 0;
+	}
+	else
+	{
+		int i2 = incidentIndex;
+		int i1 = i2 > 0 ? i2 - 1 : count - 1;
+		b2r d1 = odot( normal1, normals[i1] );
+		b2r d2 = odot( normal1, normals[i2] );
+		if ( d1 < d2 )
+		{
+			ib1 = i1;
+			ib2 = i2;
+		}
+		else
+		{
+			ib1 = i2;
+			ib2 = i2 < count - 1 ? i2 + 1 : 0;
+		}
+	}
+	b1 = vertices[ib1];
+	b2 = vertices[ib2];
+	m = o_clip_segments( p1, p2, b1, b2, normal1, 0, radiusB, O_MAKE_ID( 0, ib2 ), O_MAKE_ID( 1, ib1 ) );
+	o_smooth_finish( &m, xfA, xfB, m.normal );
+	return m;
+}
+
 /* ------------------------------------------------------------ public manifold API */
 static b2Manifold manifold_out( oManifold m )
 {
@@ -986,4 +1363,72 @@ b2Manifold b2CollideSegmentAndPolygon( const b2Segment* a, b2Transform xfA, cons
 	oPolygon pa = o_make_capsule( ovf( a->point1 ), ovf( a->point2 ), 0 );
 	oPolygon pb = poly_from( b );
 	return manifold_out( o_collide_polygons( &pa, xf_from( xfA ), &pb, xf_from( xfB ) ) );
+}
+
+static oSmooth smooth_from( const b2SmoothSegment* a )
+{
+	oSmooth o;
+	o.ghost1 = ovf( a->ghost1 );
+	o.p1 = ovf( a->segment.point1 );
+	o.p2 = ovf( a->segment.point2 );
+	o.ghost2 = ovf( a->ghost2 );
+	o.chainId = a->chainId;
+	return o;
+}
+
+static oDistCache cache_from( const b2DistanceCache* c )
+{
+	oDistCache o;
+	memset( &o, 0, sizeof( o ) );
+	if ( c != NULL )
+	{
+		o.count = c->count;
+		for ( int i = 0; i < 3; ++i )
+		{
+			o.indexA[i] = c->indexA[i];
+			o.indexB[i] = c->indexB[i];
+		}
+	}
+	return o;
+}
+
+static void cache_to( b2DistanceCache* c, const oDistCache* o )
+{
+	if ( c == NULL )
+		return;
+	c->count = (uint16_t)o->count;
+	for ( int i = 0; i < 3; ++i )
+	{
+		c->indexA[i] = (uint8_t)( i < o->count ? o->indexA[i] : 0 );
+		c->indexB[i] = (uint8_t)( i < o->count ? o->indexB[i] : 0 );
+	}
+}
+
+b2Manifold b2CollideSmoothSegmentAndCircle( const b2SmoothSegment* a, b2Transform xfA, const b2Circle* b, b2Transform xfB )
+{
+	oSmooth sa = smooth_from( a );
+	oCircle cb = circle_from( b );
+	return manifold_out( o_collide_smooth_circle( &sa, xf_from( xfA ), &cb, xf_from( xfB ) ) );
+}
+
+b2Manifold b2CollideSmoothSegmentAndCapsule( const b2SmoothSegment* a, b2Transform xfA, const b2Capsule* b, b2Transform xfB,
+											 b2DistanceCache* cache )
+{
+	oSmooth sa = smooth_from( a );
+	oPolygon pb = o_make_capsule( ovf( b->center1 ), ovf( b->center2 ), b->radius );
+	oDistCache c = cache_from( cache );
+	b2Manifold r = manifold_out( o_collide_smooth_polygon( &sa, xf_from( xfA ), &pb, xf_from( xfB ), &c ) );
+	cache_to( cache, &c );
+	return r;
+}
+
+b2Manifold b2CollideSmoothSegmentAndPolygon( const b2SmoothSegment* a, b2Transform xfA, const b2Polygon* b, b2Transform xfB,
+											 b2DistanceCache* cache )
+{
+	oSmooth sa = smooth_from( a );
+	oPolygon pb = poly_from( b );
+	oDistCache c = cache_from( cache );
+	b2Manifold r = manifold_out( o_collide_smooth_polygon( &sa, xf_from( xfA ), &pb, xf_from( xfB ), &c ) );
+	cache_to( cache, &c );
+	return r;
 }

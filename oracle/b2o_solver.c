@@ -516,6 +516,7 @@ typedef struct oSweepCtx
 	oShape* fast;
 	oBody* fastBody;
 	oSweep sweep;
+	oVec centroid1, centroid2; /* the fast shape's centroid at the sweep's ends */
 	b2r fraction;
 } oSweepCtx;
 
@@ -555,6 +556,18 @@ static bool sweep_query( int proxyId, int shapeId, void* context )
 		return true;
 	if ( o_should_bodies_collide( w, q->fastBody, body ) == false )
 		return true;
+	/* chain links: skip when the fast shape starts behind or ends in front (reference
+	 * src/solver.c:869-885) */
+	if ( s->type == b2_smoothSegmentShape )
+	{
+		oVec p1 = oxfpoint( body->xf, s->smooth.p1 );
+		oVec p2 = oxfpoint( body->xf, s->smooth.p2 );
+		oVec e = osub( p2, p1 );
+		b2r offset1 = ocross( osub( q->centroid1, p1 ), e );
+		b2r offset2 = ocross( osub( q->centroid2, p1 ), e );
+		if ( offset1 < R( 0 ) || offset2 > R( 0 ) )
+			return true;
+	}
 
 	oProxy pa = o_shape_proxy( s );
 	oProxy pb = o_shape_proxy( q->fast );
@@ -582,13 +595,17 @@ static void solve_continuous( oWorld* w, oBody* b )
 	q.fastBody = b;
 	q.sweep = body_sweep( b );
 	q.fraction = R( 1 );
-	oXf xf2;
+	oXf xf1, xf2;
+	xf1.q = q.sweep.q1;
+	xf1.p = osub( q.sweep.c1, orotate( q.sweep.q1, q.sweep.localCenter ) );
 	xf2.q = q.sweep.q2;
 	xf2.p = osub( q.sweep.c2, orotate( q.sweep.q2, q.sweep.localCenter ) );
 	for ( int sid = b->headShape; sid != O_NULL; sid = w->shapes[sid].next )
 	{
 		oShape* s = w->shapes + sid;
 		s->isFast = false;
+		q.centroid1 = oxfpoint( xf1, s->localCentroid );
+		q.centroid2 = oxfpoint( xf2, s->localCentroid );
 		oBox box1 = s->aabb;
 		oBox box2 = o_shape_aabb( s, xf2 );
 		oBox box = obox_union( box1, box2 );

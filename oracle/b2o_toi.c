@@ -52,6 +52,11 @@ oProxy o_shape_proxy( const oShape* s )
 			oVec pts[2] = { s->segment.p1, s->segment.p2 };
 			return o_make_proxy( pts, 2, R( 0 ) );
 		}
+		case b2_smoothSegmentShape:
+		{
+			oVec pts[2] = { s->smooth.p1, s->smooth.p2 };
+			return o_make_proxy( pts, 2, R( 0 ) );
+		}
 		default:
 		{
 			oVec zero = { 0, 0 };
@@ -72,6 +77,8 @@ oVec o_shape_centroid( const oShape* s )
 			return s->polygon.centroid;
 		case b2_segmentShape:
 			return olerp( s->segment.p1, s->segment.p2, R( 0.5f ) );
+		case b2_smoothSegmentShape:
+			return olerp( s->smooth.p1, s->smooth.p2, R( 0.5f ) );
 		default:
 			return ov( 0, 0 );
 	}

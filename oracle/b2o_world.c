@@ -312,6 +312,11 @@ void b2DestroyWorld( b2WorldId worldId )
 	free( w->shapes );
 	free( w->contacts );
 	free( w->joints );
+	for ( int i = 0; i < w->chainCap; ++i )
+		if ( w->chains[i].id != O_NULL )
+			free( w->chains[i].shapeIndices );
+	free( w->chains );
+	oia_free( &w->chainIds.freeIds );
 	free( w->beginEvents );
 	free( w->endEvents );
 	free( w->hitEvents );
@@ -407,6 +412,7 @@ b2BodyId b2CreateBody( b2WorldId worldId, const b2BodyDef* def )
 	b->headShape = O_NULL;
 	b->headContactKey = O_NULL;
 	b->headJointKey = O_NULL;
+	b->headChainId = O_NULL;
 	b->fixedRotation = def->fixedRotation;
 	b->isBullet = def->isBullet;
 	b->enableSleep = def->enableSleep;
@@ -548,7 +554,8 @@ static void buffer_move( oWorld* w, int proxyKey )
 
 void o_buffer_move( oWorld* w, int proxyKey ) { buffer_move( w, proxyKey ); }
 
-static b2ShapeId create_shape( b2BodyId bodyId, const b2ShapeDef* def, b2ShapeType type, const void* geometry )
+static b2ShapeId create_shape_internal( b2BodyId bodyId, const b2ShapeDef* def, b2ShapeType type, const void* geometry,
+										bool updateMass )
 {
 	oWorld* w = body_world( bodyId );
 	if ( w->locked )
@@ -616,6 +623,17 @@ static b2ShapeId create_shape( b2BodyId bodyId, const b2ShapeDef* def, b2ShapeTy
 			s->localCentroid = olerp( s->segment.p1, s->segment.p2, R( 0.5f ) );
 			break;
 		}
+		case b2_smoothSegmentShape:
+		{
+			const b2SmoothSegment* g = (const b2SmoothSegment*)geometry;
+			s->smooth.ghost1 = ovf( g->ghost1 );
+			s->smooth.p1 = ovf( g->segment.point1 );
+			s->smooth.p2 = ovf( g->segment.point2 );
+			s->smooth.ghost2 = ovf( g->ghost2 );
+			s->smooth.chainId = g->chainId;
+			s->localCentroid = olerp( s->smooth.p1, s->smooth.p2, R( 0.5f ) );
+			break;
+		}
 		default:
 			break;
 	}
@@ -647,11 +665,16 @@ static b2ShapeId create_shape( b2BodyId bodyId, const b2ShapeDef* def, b2ShapeTy
 	body->headShape = id;
 	body->shapeCount += 1;
 
-	if ( body->automaticMass )
+	if ( updateMass && body->automaticMass )
 		o_update_body_mass( w, body );
 
 	b2ShapeId sid = { id + 1, bodyId.world0, s->revision };
 	return sid;
+}
+
+static b2ShapeId create_shape( b2BodyId bodyId, const b2ShapeDef* def, b2ShapeType type, const void* geometry )
+{
+	return create_shape_internal( bodyId, def, type, geometry, true );
 }
 
 b2ShapeId b2CreatePolygonShape( b2BodyId bodyId, const b2ShapeDef* def, const b2Polygon* polygon )
@@ -1263,6 +1286,19 @@ static bool update_contact( oWorld* w, oContact* c, oShape* sA, oXf xfA, oVec of
 			}
 			break;
 		}
+		case b2_smoothSegmentShape:
+			/* chain links keep the contact's closest-feature cache (reference
+			 * src/contact.c:131-148) */
+			if ( sB->type == b2_circleShape )
+				m = o_collide_smooth_circle( &sA->smooth, xfA, &sB->circle, xfB );
+			else if ( sB->type == b2_capsuleShape )
+			{
+				oPolygon pb = o_make_capsule( sB->capsule.c1, sB->capsule.c2, sB->capsule.radius );
+				m = o_collide_smooth_polygon( &sA->smooth, xfA, &pb, xfB, &c->cache );
+			}
+			else
+				m = o_collide_smooth_polygon( &sA->smooth, xfA, &sB->polygon, xfB, &c->cache );
+			break;
 		case b2_polygonShape:
 			if ( sB->type == b2_circleShape )
 				m = o_collide_polygon_circle( &sA->polygon, xfA, &sB->circle, xfB );
@@ -1546,15 +1582,9 @@ void b2DestroyJoint( b2JointId jointId )
 	destroy_joint( w, w->joints + ( jointId.index1 - 1 ) );
 }
 
-void b2DestroyShape( b2ShapeId shapeId )
+/* Unlinks and frees a shape with its proxy and contacts (reference src/shape.c:220-269). */
+static void destroy_shape_internal( oWorld* w, oShape* s, oBody* b )
 {
-	if ( b2Shape_IsValid( shapeId ) == false )
-		return;
-	oWorld* w = s_worlds[shapeId.world0];
-	if ( w->locked )
-		return;
-	oShape* s = get_shape( shapeId );
-	oBody* b = w->bodies + s->bodyId;
 	int id = s->id;
 	if ( s->prev != O_NULL )
 		w->shapes[s->prev].next = s->next;
@@ -1574,8 +1604,192 @@ void b2DestroyShape( b2ShapeId shapeId )
 	}
 	oid_free( &w->shapeIds, id );
 	s->id = O_NULL;
+}
+
+void b2DestroyShape( b2ShapeId shapeId )
+{
+	if ( b2Shape_IsValid( shapeId ) == false )
+		return;
+	oWorld* w = s_worlds[shapeId.world0];
+	if ( w->locked )
+		return;
+	oShape* s = get_shape( shapeId );
+	oBody* b = w->bodies + s->bodyId;
+	destroy_shape_internal( w, s, b );
 	if ( b->automaticMass )
 		o_update_body_mass( w, b );
+}
+
+/* ------------------------------------------------------------ chains */
+b2ChainDef b2DefaultChainDef( void )
+{
+	b2ChainDef d;
+	memset( &d, 0, sizeof( d ) );
+	d.friction = 0.6f;
+	d.filter = b2DefaultFilter();
+	d.internalValue = 1152023;
+	return d;
+}
+
+/* reference src/shape.c:292-403 */
+b2ChainId b2CreateChain( b2BodyId bodyId, const b2ChainDef* def )
+{
+	oWorld* w = body_world( bodyId );
+	if ( w->locked || def->count < 4 )
+		return b2_nullChainId;
+	oBody* body = get_body( bodyId );
+	int chainId = oid_alloc( &w->chainIds );
+	GROW( w->chains, w->chainCap, chainId + 1, oChain );
+	oChain* chain = w->chains + chainId;
+	uint16_t rev = chain->revision;
+	memset( chain, 0, sizeof( *chain ) );
+	chain->revision = (uint16_t)( rev + 1 );
+	chain->id = chainId;
+	chain->bodyId = body->id;
+	chain->nextChainId = body->headChainId;
+	body->headChainId = chainId;
+
+	b2ShapeDef sd = b2DefaultShapeDef();
+	sd.userData = def->userData;
+	sd.restitution = def->restitution;
+	sd.friction = def->friction;
+	sd.filter = def->filter;
+	sd.enableContactEvents = false;
+	sd.enableHitEvents = false;
+	sd.enableSensorEvents = false;
+
+	int n = def->count;
+	const b2Vec2* points = def->points;
+	chain->shapeIndices = (int*)malloc( sizeof( int ) * (size_t)n );
+	b2SmoothSegment seg;
+	seg.chainId = chainId;
+	if ( def->isLoop )
+	{
+		chain->count = n;
+		int prevIndex = n - 1;
+		for ( int i = 0; i < n - 2; ++i )
+		{
+			seg.ghost1 = points[prevIndex];
+			seg.segment.point1 = points[i];
+			seg.segment.point2 = points[i + 1];
+			seg.ghost2 = points[i + 2];
+			prevIndex = i;
+			chain->shapeIndices[i] = create_shape_internal( bodyId, &sd, b2_smoothSegmentShape, &seg, false ).index1 - 1;
+		}
+		seg.ghost1 = points[n - 3];
+		seg.segment.point1 = points[n - 2];
+		seg.segment.point2 = points[n - 1];
+		seg.ghost2 = points[0];
+		chain->shapeIndices[n - 2] = create_shape_internal( bodyId, &sd, b2_smoothSegmentShape, &seg, false ).index1 - 1;
+		seg.ghost1 = points[n - 2];
+		seg.segment.point1 = points[n - 1];
+		seg.segment.point2 = points[0];
+		seg.ghost2 = points[1];
+		chain->shapeIndices[n - 1] = create_shape_internal( bodyId, &sd, b2_smoothSegmentShape, &seg, false ).index1 - 1;
+	}
+	else
+	{
+		chain->count = n - 3;
+		for ( int i = 0; i < n - 3; ++i )
+		{
+			seg.ghost1 = points[i];
+			seg.segment.point1 = points[i + 1];
+			seg.segment.point2 = points[i + 2];
+			seg.ghost2 = points[i + 3];
+			chain->shapeIndices[i] = create_shape_internal( bodyId, &sd, b2_smoothSegmentShape, &seg, false ).index1 - 1;
+		}
+	}
+	b2ChainId id = { chainId + 1, bodyId.world0, chain->revision };
+	return id;
+}
+
+bool b2Chain_IsValid( b2ChainId id )
+{
+	if ( id.world0 >= s_worldCap || s_worlds[id.world0] == NULL || !s_worlds[id.world0]->inUse )
+		return false;
+	oWorld* w = s_worlds[id.world0];
+	if ( id.index1 < 1 || id.index1 > w->chainCap )
+		return false;
+	oChain* c = w->chains + ( id.index1 - 1 );
+	return c->id == id.index1 - 1 && c->revision == id.revision;
+}
+
+/* reference src/shape.c:405-451 */
+void b2DestroyChain( b2ChainId chainId )
+{
+	if ( b2Chain_IsValid( chainId ) == false )
+		return;
+	oWorld* w = s_worlds[chainId.world0];
+	if ( w->locked )
+		return;
+	oChain* chain = w->chains + ( chainId.index1 - 1 );
+	oBody* body = w->bodies + chain->bodyId;
+	int* link = &body->headChainId;
+	while ( *link != O_NULL && *link != chain->id )
+		link = &w->chains[*link].nextChainId;
+	if ( *link == O_NULL )
+		return;
+	*link = chain->nextChainId;
+	for ( int i = 0; i < chain->count; ++i )
+		destroy_shape_internal( w, w->shapes + chain->shapeIndices[i], body );
+	free( chain->shapeIndices );
+	chain->shapeIndices = NULL;
+	oid_free( &w->chainIds, chain->id );
+	chain->id = O_NULL;
+}
+
+void b2Chain_SetFriction( b2ChainId chainId, float friction )
+{
+	oWorld* w = s_worlds[chainId.world0];
+	oChain* chain = w->chains + ( chainId.index1 - 1 );
+	for ( int i = 0; i < chain->count; ++i )
+		w->shapes[chain->shapeIndices[i]].friction = friction;
+}
+
+void b2Chain_SetRestitution( b2ChainId chainId, float restitution )
+{
+	oWorld* w = s_worlds[chainId.world0];
+	oChain* chain = w->chains + ( chainId.index1 - 1 );
+	for ( int i = 0; i < chain->count; ++i )
+		w->shapes[chain->shapeIndices[i]].restitution = restitution;
+}
+
+b2ChainId b2Shape_GetParentChain( b2ShapeId shapeId )
+{
+	oWorld* w = s_worlds[shapeId.world0];
+	oShape* s = get_shape( shapeId );
+	if ( s->type == b2_smoothSegmentShape && s->smooth.chainId != O_NULL )
+	{
+		b2ChainId id = { s->smooth.chainId + 1, shapeId.world0, w->chains[s->smooth.chainId].revision };
+		return id;
+	}
+	return b2_nullChainId;
+}
+
+b2Segment b2Shape_GetSegment( b2ShapeId id )
+{
+	oShape* s = get_shape( id );
+	b2Segment r = { vfo( s->segment.p1 ), vfo( s->segment.p2 ) };
+	return r;
+}
+
+b2SmoothSegment b2Shape_GetSmoothSegment( b2ShapeId id )
+{
+	oShape* s = get_shape( id );
+	b2SmoothSegment r;
+	r.ghost1 = vfo( s->smooth.ghost1 );
+	r.segment.point1 = vfo( s->smooth.p1 );
+	r.segment.point2 = vfo( s->smooth.p2 );
+	r.ghost2 = vfo( s->smooth.ghost2 );
+	r.chainId = s->smooth.chainId;
+	return r;
+}
+
+b2Capsule b2Shape_GetCapsule( b2ShapeId id )
+{
+	oShape* s = get_shape( id );
+	b2Capsule r = { vfo( s->capsule.c1 ), vfo( s->capsule.c2 ), (float)s->capsule.radius };
+	return r;
 }
 
 void b2DestroyBody( b2BodyId bodyId )
@@ -1607,6 +1821,15 @@ void b2DestroyBody( b2BodyId bodyId )
 		oid_free( &w->shapeIds, sid );
 		s->id = O_NULL;
 		sid = s->next;
+	}
+	for ( int cid = b->headChainId; cid != O_NULL; )
+	{
+		oChain* chain = w->chains + cid;
+		free( chain->shapeIndices );
+		chain->shapeIndices = NULL;
+		oid_free( &w->chainIds, cid );
+		chain->id = O_NULL;
+		cid = chain->nextChainId;
 	}
 	/* the awake set drops the body by moving its last body into the slot */
 	if ( b->awakeIndex != O_NULL )

@@ -9,7 +9,9 @@ Fixtures (all produced by the unmodified reference library, oracle/_ref/libb2ref
                  (contact id, shape pair, colour, touching, point count) plus full body
                  snapshots, for the small pyramid, the tumbler, the tilted stacks and
                  hello-world scenes;
-  manifolds.npz  seeded random shape pairs and the reference manifolds for them.
+  manifolds.npz  seeded random shape pairs and the reference manifolds for them;
+  smooth_manifolds.npz  seeded chain links against every shape type: the reference's
+                 manifolds and closest-feature caches from an empty and a warmed cache.
 The GPU machine has no reference sources; its tests read these files instead.
 """
 from __future__ import annotations
@@ -28,7 +30,7 @@ sys.path.insert(0, REPO)
 
 from box2c_gb300.capi import Backend, contact_table  # noqa: E402
 from tests.golden.shapes import (Manifold, Polygon, Circle, Capsule, Transform,  # noqa: E402
-                                 random_pairs, manifold_array)
+                                 random_pairs, manifold_array, random_smooth_pairs, collide_smooth)
 
 SCENES = {
     # name: (steps, snapshot steps)
@@ -60,6 +62,8 @@ SCENES = {
     # graph colours and in the overflow colour, with contacts
     "joint_zoo": (300, (1, 2, 10, 60, 300)),
     "joint_zoo_collide": (200, (1, 2, 10, 100, 200)),
+    # chains: smooth segments (terrain and a closed bowl) against every shape type, bullets
+    "chain_scene": (300, (1, 10, 60, 150, 300)),
 }
 
 
@@ -96,6 +100,8 @@ def make_scene(b: Backend, name: str):
         return b.joint_zoo(2, 0, 1250)
     if name == "joint_zoo_collide":
         return b.joint_zoo(3, 1, 1251)
+    if name == "chain_scene":
+        return b.chain_scene(200, 1260)
     raise KeyError(name)
 
 
@@ -143,7 +149,9 @@ def main():
         m = fn(C.addressof(a), xa, C.addressof(b), xb)
         results.append(manifold_array(m))
     np.savez_compressed(os.path.join(HERE, "manifolds.npz"), outputs=np.stack(results))
-    print("wrote", os.path.join(HERE, "scenes.npz"), "and manifolds.npz")
+    smooth = [collide_smooth(L, e) for e in random_smooth_pairs(seed=11, count=400)]
+    np.savez_compressed(os.path.join(HERE, "smooth_manifolds.npz"), outputs=np.stack(smooth))
+    print("wrote", os.path.join(HERE, "scenes.npz"), "manifolds.npz and smooth_manifolds.npz")
 
 
 if __name__ == "__main__":

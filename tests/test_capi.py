@@ -79,3 +79,15 @@ def test_manifold_functions_match_reference_golden(lib):
         assert np.array_equal(got.view(np.uint32), golden[k].view(np.uint32)), (k, kind)
         kinds.add(kind)
     assert len(kinds) >= 4
+
+
+def test_smooth_segment_manifolds_match_reference_golden(lib):
+    """The library's chain-link manifold functions (the narrowphase kernel's code, compiled
+    for the host) against the reference on seeded links and shapes: manifolds and the
+    closest-feature cache, from an empty and from a warmed cache, bit for bit."""
+    import numpy as np
+    from tests.golden.shapes import collide_smooth, random_smooth_pairs
+    golden = np.load(os.path.join(REPO, "tests", "golden", "smooth_manifolds.npz"))["outputs"]
+    for k, entry in enumerate(random_smooth_pairs(seed=11, count=len(golden))):
+        got = collide_smooth(lib, entry)
+        assert np.array_equal(got.view(np.uint32), golden[k].view(np.uint32)), (k, entry[0], got, golden[k])

@@ -202,11 +202,11 @@ def test_batch_mixed_paths_match_oracle(gpu, oracle):
 
 def test_batch_joint_types_match_oracle(gpu, oracle_atan):
     """Batched worlds with every joint type (the joint scene at two sizes and seeds, next
-    to a pyramid): each world bit-identical to the oracle build with the library's own
-    atan2, stepped alone."""
+    to a pyramid and a chain scene): each world bit-identical to the oracle build with the
+    library's own atan2, stepped alone."""
     bind_batch_api(gpu.lib)
     makers = [lambda b: b.joint_zoo(1, 0, 61), lambda b: b.joint_zoo(2, 1, 62), lambda b: b.pyramid(12),
-              lambda b: b.joint_zoo(1, 1, 63)]
+              lambda b: b.joint_zoo(1, 1, 63), lambda b: b.chain_scene(120, 64)]
     wg = [m(gpu) for m in makers]
     wo = [m(oracle_atan) for m in makers]
     ids = world_array(wg)

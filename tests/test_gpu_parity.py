@@ -16,7 +16,7 @@ GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
 
 @pytest.mark.parametrize("name", ["pyramid20", "tilted", "hello", "tumbler2000", "pyramid100", "joint_grid30",
                                   "joint_grid100", "many_pyramids5", "many_pyramids20", "shape_pile", "joint_hub",
-                                  "fast_shots"])
+                                  "fast_shots", "chain_scene"])
 def test_gpu_matches_reference_golden(gpu, name):
     g = np.load(os.path.join(GOLDEN, "scenes.npz"))
     steps, snaps = SCENES[name]
@@ -57,14 +57,17 @@ def test_gpu_lockstep_oracle(gpu, oracle, scene, steps, sub):
 
 
 @pytest.mark.parametrize("scene,steps", [("shape_pile", 250), ("joint_hub_motors", 250), ("fast_shots", 150),
-                                         ("many_pyramids", 100), ("joint_grid", 100)])
+                                         ("many_pyramids", 100), ("joint_grid", 100), ("chains", 300)])
 def test_gpu_lockstep_oracle_new_paths(gpu, oracle, scene, steps):
     """Device paths the pyramid and tumbler scenes do not reach, stepped against the oracle
     with every manifold compared: capsule and segment manifolds (capsule-capsule,
     polygon-capsule, segment-polygon, segment-capsule, segment-circle) and rounded
     polygons; revolute joints in the graph colours and in the overflow colour, with
-    motors; time of impact of fast bodies and bullets; segment grounds."""
+    motors; time of impact of fast bodies and bullets; segment grounds; chains of smooth
+    segments (one-sided links with ghost vertices, the contact's closest-feature cache,
+    the continuous-collision rule for links)."""
     make = {
+        "chains": lambda b: b.chain_scene(160, 94),
         "shape_pile": lambda b: b.shape_pile(300, 91),
         "joint_hub_motors": lambda b: b.joint_hub(16, 4, 4, 92),
         "fast_shots": lambda b: b.fast_shots(40, 93),

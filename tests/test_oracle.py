@@ -254,3 +254,20 @@ def test_joint_zoo_lockstep_reference(reference, oracle, copies, flags):
     step, detail, _ = lockstep(reference, oracle, lambda b: b.joint_zoo(copies, flags, 1250 + flags), 200,
                                check_manifolds=True)
     assert step is None, f"{detail} at step {step}"
+
+
+def test_smooth_segment_manifolds_golden(oracle):
+    """The oracle's chain-link manifolds against the reference's golden vectors."""
+    from tests.golden.shapes import collide_smooth, random_smooth_pairs
+    golden = np.load(os.path.join(GOLDEN, "smooth_manifolds.npz"))["outputs"]
+    for k, entry in enumerate(random_smooth_pairs(seed=11, count=len(golden))):
+        got = collide_smooth(oracle.lib, entry)
+        assert np.array_equal(got.view(np.uint32), golden[k].view(np.uint32)), (k, entry[0])
+
+
+def test_chain_scene_lockstep_reference(reference, oracle):
+    """Chains (open terrain and a closed bowl of smooth segments) against circles,
+    capsules, boxes and rounded boxes, with fast bodies and bullets: bit-identical every
+    step, manifolds included."""
+    step, detail, _ = lockstep(reference, oracle, lambda b: b.chain_scene(200, 1260), 300, check_manifolds=True)
+    assert step is None, f"{detail} at step {step}"
