@@ -23,7 +23,7 @@
  * friction (mixed per shape as sqrt(muA * muB), reference src/contact.c:42-45).  The
  * discrete choices of a step (pairs, colours, manifold features, active clamps) are
  * those of the recorded forward step.  Polygon, capsule and segment shapes; joints,
- * overflow-colour rows and circle shapes are reported as unsupported.
+ * overflow-colour rows, circle shapes and chain links are reported as unsupported.
  *
  * Reference arithmetic being differentiated: src/solver.c:34-93, :146-163, :205-223;
  * src/contact_solver.c:597-1293; src/manifold.c:276-700.
@@ -873,8 +873,8 @@ __global__ void __launch_bounds__( ADJ_WARP ) k_adjoint( const b2gAdjointItem* i
 			const b2gTapeRow& tr = recR[k];
 			const b2gShapeGeo& gA = W.geo[tr.shapeA];
 			const b2gShapeGeo& gB = W.geo[tr.shapeB];
-			if ( gB.type == 0 )
-				unsupported += 1;
+			if ( gB.type == 0 || gA.type == 4 )
+				unsupported += 1; /* circles and chain links have no manifold Jacobian here */
 			else if ( manifold_jacobian( gA, gB, L.start + (size_t)gA.bodyId * ADJ_START, L.start + (size_t)gB.bodyId * ADJ_START, tr.ia >= 0,
 										 tr.ib >= 0, tr.m, L.jac + (size_t)k * ADJ_JAC ) == false )
 				mismatches += 1;
