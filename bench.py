@@ -256,7 +256,7 @@ def run_tumbler(g, steps=1000, cpu=True):
 BATCH_WORLDS = 4096
 # DRAM bytes of the solver stage of one large-pyramid step (k_fused_stage 2.35 MB +
 # k_solve_fused 2.76 MB), from the committed ncu capture of the same workload
-SOLVER_DRAM_BYTES = 5.11e6
+SOLVER_DRAM_BYTES = 5.10e6
 # DRAM bytes of the batched solver over 2048 of the batched worlds (both halves), from the
 # committed ncu capture of that workload
 BATCH_SOLVE_DRAM_BYTES = 3.33e9

@@ -86,7 +86,7 @@ __device__ void float_manifold( const b2gShapeGeo& gA, const b2gShapeGeo& gB, co
 	xa.q = grot( sa[2], sa[3] ); xa.p = gsub( gv( sa[0], sa[1] ), grotate( xa.q, gv( sa[4], sa[5] ) ) );
 	xb.q = grot( sb[2], sb[3] ); xb.p = gsub( gv( sb[0], sb[1] ), grotate( xb.q, gv( sb[4], sb[5] ) ) );
 	b2gManifold m;
-	gcollide_shapes( &m, &gA, xa, &gB, xb );
+	gcollide_shapes( &m, &gA, xa, &gB, xb, nullptr );
 	b2gVec offA = grotate( xa.q, gv( sa[4], sa[5] ) ), offB = grotate( xb.q, gv( sb[4], sb[5] ) );
 	for ( int i = 0; i < 12; ++i ) out[i] = 0;
 	out[0] = m.normal.x; out[1] = m.normal.y;
@@ -134,7 +134,7 @@ __global__ void k_jac( unsigned seed, int scene )
 	float a8[8] = { sa[0], sa[1], sa[2], sa[3], sa[4], sa[5], xa.p.x, xa.p.y }, b8[8] = { sb[0], sb[1], sb[2], sb[3], sb[4], sb[5], xb.p.x, xb.p.y };
 	for ( int i = 0; i < 8; ++i ) { stA[i] = a8[i]; stB[i] = b8[i]; }
 	b2gManifold rec;
-	gcollide_shapes( &rec, &gA, xa, &gB, xb );
+	gcollide_shapes( &rec, &gA, xa, &gB, xb, nullptr );
 	b2gVec offA = grotate( xa.q, gv( sa[4], sa[5] ) ), offB = grotate( xb.q, gv( sb[4], sb[5] ) );
 	for ( int j = 0; j < rec.count; ++j ) { rec.pts[j].anchorA = gsub( rec.pts[j].anchorA, offA ); rec.pts[j].anchorB = gsub( rec.pts[j].anchorB, offB ); }
 	float jac[72];
