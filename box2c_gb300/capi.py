@@ -124,6 +124,8 @@ class Backend:
         L.b2World_InspectShapes.restype = C.c_int
         L.b2World_InspectContacts.argtypes = [WorldId, C.c_void_p, C.c_int]
         L.b2World_InspectContacts.restype = C.c_int
+        L.b2World_InspectIslands.argtypes = [WorldId, C.c_void_p, C.c_int]
+        L.b2World_InspectIslands.restype = C.c_int
         L.b2Body_GetPosition.argtypes = [BodyId]
         L.b2Body_GetPosition.restype = Vec2
         L.b2Body_GetRotation.argtypes = [BodyId]
@@ -184,6 +186,10 @@ class Backend:
         S.b2s_destruction_step.restype = None
         S.b2s_fast_shots.argtypes = [C.c_int, C.c_uint64]
         S.b2s_fast_shots.restype = WorldId
+        S.b2s_sleep_scene.argtypes = []
+        S.b2s_sleep_scene.restype = WorldId
+        S.b2s_sleep_step.argtypes = [WorldId, C.c_int]
+        S.b2s_sleep_step.restype = None
         S.b2s_draw_ints.argtypes = [C.c_int, C.c_uint64, C.c_int, C.c_int, C.c_void_p]
         S.b2s_draw_ints.restype = None
         S.b2s_draw_uniform.argtypes = [C.c_int, C.c_uint64, C.c_float, C.c_float, C.c_void_p]
@@ -265,6 +271,13 @@ class Backend:
     def destruction_step(self, world: WorldId, step: int) -> None:
         self.scenes.b2s_destruction_step(world, step)
 
+    def sleep_scene(self) -> WorldId:
+        """Islands and sleep: resting piles, a chain, bodies created asleep, scripted wakes."""
+        return self._made(self.scenes.b2s_sleep_scene())
+
+    def sleep_step(self, world: WorldId, step: int) -> None:
+        self.scenes.b2s_sleep_step(world, step)
+
     def fast_shots(self, count: int = 60, seed: int = 1241) -> WorldId:
         return self._made(self.scenes.b2s_fast_shots(count, seed))
 
@@ -310,6 +323,13 @@ class Backend:
         arr = (InspectShape * max(n, 1))()
         self.lib.b2World_InspectShapes(world, C.addressof(arr), n)
         return np.ctypeslib.as_array(arr)[:n].copy() if n else np.zeros(0, dtype=np.dtype(InspectShape))
+
+    def islands(self, world: WorldId) -> np.ndarray:
+        """(solver set, island id) per body id; -1 for free slots."""
+        n = self.lib.b2World_InspectIslands(world, None, 0)
+        out = np.zeros((n, 2), np.int32)
+        self.lib.b2World_InspectIslands(world, out.ctypes.data, n)
+        return out
 
     def contacts(self, world: WorldId) -> np.ndarray:
         n = self.lib.b2World_InspectContacts(world, None, 0)

@@ -1776,3 +1776,203 @@ b2WorldId b2s_chain_scene( int count, uint64_t seed )
 	}
 	return worldId;
 }
+
+/* ------------------------------------------------------------ sleep scene */
+static struct
+{
+	b2BodyId pileA[15];
+	b2BodyId pileB[10];
+	b2ShapeId pileBCap;
+	b2BodyId links[5];
+	b2JointId linkJoints[5];
+	b2BodyId hover[2];
+	b2BodyId slider;
+	int seedDrops;
+} s_sleep;
+
+static void b2s_sleep_pile( b2WorldId worldId, b2BodyId* out, int rows, float x0 )
+{
+	b2BodyDef bd = b2DefaultBodyDef();
+	bd.type = b2_dynamicBody;
+	b2ShapeDef sd = b2DefaultShapeDef();
+	sd.density = 1.0f;
+	sd.friction = 0.6f;
+	b2Polygon box = b2MakeSquare( 0.5f );
+	int n = 0;
+	for ( int i = 0; i < rows; ++i )
+	{
+		for ( int j = i; j < rows; ++j )
+		{
+			float x = x0 + ( i + 1.0f ) * 0.5f + ( j - i ) * 1.0f;
+			float y = ( 2.0f * i + 1.0f ) * 0.5f;
+			bd.position = ( b2Vec2 ){ x, y };
+			out[n] = b2CreateBody( worldId, &bd );
+			b2CreatePolygonShape( out[n], &sd, &box );
+			n += 1;
+		}
+	}
+}
+
+b2WorldId b2s_sleep_scene( void )
+{
+	b2WorldDef wd = b2DefaultWorldDef();
+	b2WorldId worldId = b2CreateWorld( &wd );
+	if ( B2_IS_NULL( worldId ) )
+		return worldId;
+	memset( &s_sleep, 0, sizeof( s_sleep ) );
+
+	b2BodyDef gd = b2DefaultBodyDef();
+	gd.position = ( b2Vec2 ){ 0.0f, -0.5f };
+	b2BodyId groundId = b2CreateBody( worldId, &gd );
+	b2ShapeDef gsd = b2DefaultShapeDef();
+	b2Polygon groundBox = b2MakeBox( 60.0f, 0.5f );
+	b2CreatePolygonShape( groundId, &gsd, &groundBox );
+
+	/* two resting piles: each settles into one island and falls asleep */
+	b2s_sleep_pile( worldId, s_sleep.pileA, 5, -22.0f );
+	b2s_sleep_pile( worldId, s_sleep.pileB, 4, -8.0f );
+	b2ShapeDef sd = b2DefaultShapeDef();
+	sd.density = 1.0f;
+	b2Circle cap = { { 0.0f, 0.6f }, 0.2f };
+	s_sleep.pileBCap = b2CreateCircleShape( s_sleep.pileB[9], &sd, &cap );
+
+	/* a damped revolute chain hanging from a static pin */
+	b2BodyDef pd = b2DefaultBodyDef();
+	pd.position = ( b2Vec2 ){ 5.0f, 9.0f };
+	b2BodyId pinId = b2CreateBody( worldId, &pd );
+	b2BodyDef bd = b2DefaultBodyDef();
+	bd.type = b2_dynamicBody;
+	bd.linearDamping = 0.6f;
+	bd.angularDamping = 0.6f;
+	b2Capsule link = { { -0.5f, 0.0f }, { 0.5f, 0.0f }, 0.125f };
+	b2BodyId prev = pinId;
+	for ( int k = 0; k < 5; ++k )
+	{
+		bd.position = ( b2Vec2 ){ 5.5f + 1.0f * k, 9.0f };
+		s_sleep.links[k] = b2CreateBody( worldId, &bd );
+		b2CreateCapsuleShape( s_sleep.links[k], &sd, &link );
+		b2RevoluteJointDef jd = b2DefaultRevoluteJointDef();
+		jd.bodyIdA = prev;
+		jd.bodyIdB = s_sleep.links[k];
+		jd.localAnchorA = k == 0 ? ( b2Vec2 ){ 0.0f, 0.0f } : ( b2Vec2 ){ 0.5f, 0.0f };
+		jd.localAnchorB = ( b2Vec2 ){ -0.5f, 0.0f };
+		s_sleep.linkJoints[k] = b2CreateRevoluteJoint( worldId, &jd );
+		prev = s_sleep.links[k];
+	}
+
+	/* two boxes created asleep in mid-air, each in a sleeping set of its own */
+	b2BodyDef hd = b2DefaultBodyDef();
+	hd.type = b2_dynamicBody;
+	hd.isAwake = false;
+	b2Polygon hoverBox = b2MakeBox( 0.75f, 0.25f );
+	for ( int k = 0; k < 2; ++k )
+	{
+		hd.position = ( b2Vec2 ){ 14.0f + 2.5f * k, 4.0f };
+		s_sleep.hover[k] = b2CreateBody( worldId, &hd );
+		b2CreatePolygonShape( s_sleep.hover[k], &sd, &hoverBox );
+	}
+
+	/* a box sliding on a slippery patch */
+	b2BodyDef sdef = b2DefaultBodyDef();
+	sdef.type = b2_dynamicBody;
+	sdef.position = ( b2Vec2 ){ 26.0f, 0.5f };
+	sdef.linearVelocity = ( b2Vec2 ){ -2.0f, 0.0f };
+	s_sleep.slider = b2CreateBody( worldId, &sdef );
+	b2ShapeDef slick = b2DefaultShapeDef();
+	slick.friction = 0.02f;
+	b2Polygon sliderBox = b2MakeSquare( 0.5f );
+	b2CreatePolygonShape( s_sleep.slider, &slick, &sliderBox );
+
+	/* a kinematic platform carrying a box: its island never sleeps */
+	b2BodyDef kd = b2DefaultBodyDef();
+	kd.type = b2_kinematicBody;
+	kd.position = ( b2Vec2 ){ 36.0f, 1.0f };
+	kd.linearVelocity = ( b2Vec2 ){ 0.3f, 0.0f };
+	b2BodyId platform = b2CreateBody( worldId, &kd );
+	b2Polygon plate = b2MakeBox( 2.0f, 0.25f );
+	b2CreatePolygonShape( platform, &sd, &plate );
+	bd = b2DefaultBodyDef();
+	bd.type = b2_dynamicBody;
+	bd.position = ( b2Vec2 ){ 36.0f, 1.75f };
+	b2BodyId rider = b2CreateBody( worldId, &bd );
+	b2CreatePolygonShape( rider, &sd, &sliderBox );
+	return worldId;
+}
+
+void b2s_sleep_step( b2WorldId worldId, int step )
+{
+	b2ShapeDef sd = b2DefaultShapeDef();
+	sd.density = 1.0f;
+	b2BodyDef bd = b2DefaultBodyDef();
+	bd.type = b2_dynamicBody;
+	if ( step == 5 )
+	{
+		/* a joint between two sleeping sets merges them */
+		b2DistanceJointDef dj = b2DefaultDistanceJointDef();
+		dj.bodyIdA = s_sleep.hover[0];
+		dj.bodyIdB = s_sleep.hover[1];
+		dj.localAnchorA = ( b2Vec2 ){ 0.75f, 0.0f };
+		dj.localAnchorB = ( b2Vec2 ){ -0.75f, 0.0f };
+		dj.length = 1.0f;
+		b2CreateDistanceJoint( worldId, &dj );
+	}
+	else if ( step == 60 )
+	{
+		/* put the sliding box's island to sleep mid-slide */
+		b2Body_SetAwake( s_sleep.slider, false );
+	}
+	else if ( step == 120 )
+	{
+		/* destroying a body of the sleeping pile wakes it; its island must split later */
+		b2DestroyBody( s_sleep.pileA[7] );
+	}
+	else if ( step == 130 )
+	{
+		/* removing a joint from the middle of the chain */
+		b2DestroyJoint( s_sleep.linkJoints[2] );
+	}
+	else if ( step == 150 )
+	{
+		/* a box dropped onto the merged sleeping pair wakes both */
+		bd.position = ( b2Vec2 ){ 14.0f, 7.0f };
+		b2BodyId id = b2CreateBody( worldId, &bd );
+		b2Polygon box = b2MakeSquare( 0.4f );
+		b2CreatePolygonShape( id, &sd, &box );
+	}
+	else if ( step == 180 )
+	{
+		b2Body_SetAwake( s_sleep.slider, true );
+	}
+	else if ( step == 200 )
+	{
+		/* a ball rolled into the sleeping second pile */
+		bd.position = ( b2Vec2 ){ -15.0f, 0.5f };
+		bd.linearVelocity = ( b2Vec2 ){ 12.0f, 0.0f };
+		b2BodyId id = b2CreateBody( worldId, &bd );
+		b2Circle ball = { { 0.0f, 0.0f }, 0.5f };
+		b2CreateCircleShape( id, &sd, &ball );
+	}
+	else if ( step == 220 )
+	{
+		b2DestroyShape( s_sleep.pileBCap );
+	}
+	else if ( step == 240 )
+	{
+		/* a velocity set on a sleeping body wakes it first */
+		b2Body_SetLinearVelocity( s_sleep.slider, ( b2Vec2 ){ 1.0f, 0.0f } );
+		b2Joint_WakeBodies( s_sleep.linkJoints[4] );
+	}
+	else if ( step == 260 )
+	{
+		b2Body_EnableSleep( s_sleep.pileA[0], false );
+	}
+	else if ( step == 290 )
+	{
+		b2World_EnableSleeping( worldId, false );
+	}
+	else if ( step == 300 )
+	{
+		b2World_EnableSleeping( worldId, true );
+		b2Body_EnableSleep( s_sleep.pileA[0], true );
+	}
+}

@@ -134,6 +134,19 @@ b2WorldId b2s_chain_scene( int count, uint64_t seed );
  * `capacity` floats to out; returns the number written (-1 without a world). */
 int b2s_joint_api_script( float* out, int capacity );
 
+/* Sleep scene (world and bodies with sleep on): two resting piles of boxes, a damped
+ * revolute chain from a static pin, two boxes created asleep in mid-air, a box sliding
+ * on a slippery patch and a kinematic platform carrying a box.  b2s_sleep_step, called
+ * after each step with the step number, joins the two sleeping boxes (merging their
+ * sets, step 5), puts the slider to sleep (60), destroys a body of the sleeping first
+ * pile (120) and a joint of the chain (130), drops a box onto the sleeping pair (150),
+ * wakes the slider (180), rolls a ball into the second pile (200), destroys a shape of
+ * it (220), sets the sleeping slider's velocity and wakes the chain's end (240),
+ * disables one body's sleep (260) and the world's (290), and enables both again (300).
+ * One such scene at a time per process. */
+b2WorldId b2s_sleep_scene( void );
+void b2s_sleep_step( b2WorldId worldId, int step );
+
 /* Draws `n` integers uniform in [lo, hi] from `seed` into out. */
 void b2s_draw_ints( int n, uint64_t seed, int lo, int hi, int* out );
 /* Draws `n` floats uniform in [lo, hi) / standard normal from `seed` into out. */

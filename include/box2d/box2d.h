@@ -69,6 +69,15 @@ B2_API int b2Body_GetShapes( b2BodyId bodyId, b2ShapeId* shapeArray, int capacit
 B2_API int b2Body_GetJointCount( b2BodyId bodyId );
 B2_API int b2Body_GetContactCapacity( b2BodyId bodyId );
 B2_API int b2Body_GetContactData( b2BodyId bodyId, b2ContactData* contactData, int capacity );
+/* Sleep (reference box2d.h:342-359).  A body sleeps with its whole island: SetAwake(false)
+ * splits the island first when constraints were removed from it, and a body that is not
+ * awake reports zero velocity. */
+B2_API bool b2Body_IsAwake( b2BodyId bodyId );
+B2_API void b2Body_SetAwake( b2BodyId bodyId, bool awake );
+B2_API void b2Body_EnableSleep( b2BodyId bodyId, bool enableSleep );
+B2_API bool b2Body_IsSleepEnabled( b2BodyId bodyId );
+B2_API void b2Body_SetSleepThreshold( b2BodyId bodyId, float sleepVelocity );
+B2_API float b2Body_GetSleepThreshold( b2BodyId bodyId );
 
 /* Shape (reference box2d.h:423-571) */
 B2_API b2ShapeId b2CreateCircleShape( b2BodyId bodyId, const b2ShapeDef* def, const b2Circle* circle );

@@ -67,6 +67,12 @@ int b2World_InspectBodies( b2WorldId worldId, float* out, int capacity );
 int b2World_InspectShapes( b2WorldId worldId, b2InspectShape* out, int capacity );
 int b2World_InspectContacts( b2WorldId worldId, b2InspectContact* out, int capacity );
 
+/* Two ints per body id: the solver set (0 static, 2 awake, 3 and up a sleeping set; the
+ * reference's src/solver_set.h:11-30 numbering) and the island id (-1 for none), both
+ * -1 for a free slot.  Set and island ids come from id pools, so two implementations
+ * that move islands between sets in the same order agree on them exactly. */
+int b2World_InspectIslands( b2WorldId worldId, int* out, int capacity );
+
 #ifdef __cplusplus
 }
 #endif

@@ -222,6 +222,10 @@ typedef struct oBody
 	uint16_t revision;
 	bool fixedRotation, isBullet, enableSleep, isSpeedCapped, automaticMass;
 	b2r sleepThreshold, sleepTime;
+	int setIndex;	/* solver set (O_SET_*); sleeping sets from O_SET_FIRST_SLEEPING */
+	int setLocal;	/* position in a non-awake set's body list */
+	int islandId, islandPrev, islandNext;
+	bool isMarked;
 
 	/* simulation record (reference src/body.h:95-133) */
 	oXf xf;
@@ -260,7 +264,10 @@ typedef struct oEdge
 typedef struct oContact
 {
 	int id; /* -1 when free */
+	int setIndex; /* awake, disabled (non-touching, both bodies asleep) or a sleeping set */
 	int colorIndex, localIndex;
+	int islandId, islandPrev, islandNext;
+	bool isMarked;
 	oEdge edges[2];
 	int shapeIdA, shapeIdB;
 	uint32_t flags;
@@ -378,7 +385,10 @@ typedef struct oJoint
 	b2JointType type;
 	int bodyIdA, bodyIdB;
 	oEdge edges[2];
+	int setIndex;
 	int colorIndex, localIndex;
+	int islandId, islandPrev, islandNext;
+	bool isMarked;
 	oVec localAnchorA, localAnchorB; /* reference localOriginAnchorA/B */
 	b2r invMassA, invMassB, invIA, invIB;
 	int indexA, indexB; /* awake body ids, -1 for a body that is not awake */
@@ -423,6 +433,34 @@ typedef struct oConstraint
 	int pointCount;
 } oConstraint;
 
+/* Solver sets (reference src/solver_set.h): static, disabled, awake, then sleeping sets. */
+enum
+{
+	O_SET_STATIC = 0,
+	O_SET_DISABLED = 1,
+	O_SET_AWAKE = 2,
+	O_SET_FIRST_SLEEPING = 3,
+};
+
+/* A persistent island: bodies, contacts and joints linked through the records
+ * (reference src/island.h:32-56). */
+typedef struct oIsland
+{
+	int setIndex, localIndex, islandId;
+	int headBody, tailBody, bodyCount;
+	int headContact, tailContact, contactCount;
+	int headJoint, tailJoint, jointCount;
+	int parentIsland;
+	int constraintRemoveCount;
+} oIsland;
+
+/* A sleeping set's members in set order (the awake set's are the awake lists). */
+typedef struct oSolverSet
+{
+	int setIndex; /* -1 when free */
+	oIntArray bodies, contacts, joints, islands;
+} oSolverSet;
+
 typedef struct oWorld
 {
 	bool inUse;
@@ -444,6 +482,15 @@ typedef struct oWorld
 	oIntArray awake;		 /* awake body ids in solver order */
 	oIntArray staticBodies;	 /* static body ids */
 	oIntArray nonTouching;	 /* awake non-touching contact ids */
+	oIntArray disabledContacts; /* non-touching contacts whose bodies both sleep */
+	oIntArray awakeIslands;	 /* awake island ids in set order */
+	oIsland* islands;
+	int islandCap;
+	oIdPool islandIds;
+	oSolverSet* sets; /* indexed by set id; entries below O_SET_FIRST_SLEEPING unused */
+	int setCap;
+	oIdPool setIds;
+	int splitIslandId;
 	oColor colors[O_COLORS];
 
 	oTree trees[3];
@@ -479,7 +526,7 @@ void o_update_pairs( oWorld* w );
 void o_collide( oWorld* w );
 void o_solve( oWorld* w, b2r dt, int subSteps );
 void o_create_contact( oWorld* w, oShape* a, oShape* b );
-void o_destroy_contact( oWorld* w, oContact* c );
+void o_destroy_contact( oWorld* w, oContact* c, bool wakeBodies );
 void o_add_contact_to_graph( oWorld* w, oContact* c );
 void o_remove_contact_from_graph( oWorld* w, int bodyIdA, int bodyIdB, int colorIndex, int localIndex );
 int o_assign_joint_color( oWorld* w, int bodyIdA, int bodyIdB, bool staticA, bool staticB );
@@ -513,6 +560,27 @@ typedef struct oState
 /* Joints of every type (b2o_joint.c; reference src/joint.c:983-1108 and the per-type
  * prepare, warm start and solve functions). */
 void o_prepare_joint( oWorld* w, const oStep* st, oJoint* j );
+
+/* Islands and sleep (b2o_island.c; reference src/island.c, src/solver_set.c). */
+void o_islands_init( oWorld* w );
+void o_islands_free( oWorld* w );
+void o_create_island_for_body( oWorld* w, int setIndex, oBody* b );
+void o_remove_body_from_island( oWorld* w, oBody* b );
+void o_remove_body_from_set( oWorld* w, oBody* b );
+void o_link_contact( oWorld* w, oContact* c );
+void o_unlink_contact( oWorld* w, oContact* c );
+void o_link_joint( oWorld* w, oJoint* j );
+void o_unlink_joint( oWorld* w, oJoint* j );
+void o_merge_awake_islands( oWorld* w );
+void o_split_island( oWorld* w, int baseId );
+void o_wake_solver_set( oWorld* w, int setIndex );
+void o_try_sleep_island( oWorld* w, int islandId );
+void o_merge_solver_sets( oWorld* w, int setId1, int setId2 );
+int o_create_sleeping_set( oWorld* w );
+bool o_wake_body( oWorld* w, oBody* b );
+oIntArray* o_set_bodies( oWorld* w, int setIndex );
+oIntArray* o_set_contacts( oWorld* w, int setIndex );
+oIntArray* o_set_joints( oWorld* w, int setIndex );
 oJoint* o_create_joint( b2WorldId worldId, b2BodyId bodyIdA, b2BodyId bodyIdB, b2JointType type, bool collideConnected,
 						void* userData, b2JointId* out );
 void o_destroy_contacts_between( oWorld* w, int bodyIdA, int bodyIdB );

@@ -26,10 +26,25 @@ int b2World_InspectBodies( b2WorldId worldId, float* out, int capacity )
 		o[1] = (float)b->xf.p.y;
 		o[2] = (float)b->xf.q.c;
 		o[3] = (float)b->xf.q.s;
-		o[4] = (float)b->v.x;
-		o[5] = (float)b->v.y;
-		o[6] = (float)b->w;
+		/* velocities live in the awake set only */
+		bool awake = b->setIndex == O_SET_AWAKE;
+		o[4] = awake ? (float)b->v.x : 0.0f;
+		o[5] = awake ? (float)b->v.y : 0.0f;
+		o[6] = awake ? (float)b->w : 0.0f;
 		o[7] = (float)b->type;
+	}
+	return count;
+}
+
+int b2World_InspectIslands( b2WorldId worldId, int* out, int capacity )
+{
+	oWorld* w = o_world( worldId );
+	int count = w->bodyIds.next;
+	for ( int i = 0; i < count && i < capacity; ++i )
+	{
+		oBody* b = w->bodies + i;
+		out[2 * i] = b->id == i ? b->setIndex : -1;
+		out[2 * i + 1] = b->id == i ? b->islandId : -1;
 	}
 	return count;
 }

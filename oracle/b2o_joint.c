@@ -331,7 +331,16 @@ void b2Joint_SetCollideConnected( b2JointId id, bool shouldCollide )
 bool b2Joint_GetCollideConnected( b2JointId id ) { return jget( id )->collideConnected; }
 void b2Joint_SetUserData( b2JointId id, void* userData ) { jget( id )->userData = userData; }
 void* b2Joint_GetUserData( b2JointId id ) { return jget( id )->userData; }
-void b2Joint_WakeBodies( b2JointId id ) { (void)id; }
+/* reference src/joint.c:874-888 */
+void b2Joint_WakeBodies( b2JointId id )
+{
+	oWorld* w = jworld( id );
+	if ( w->locked )
+		return;
+	oJoint* j = jget( id );
+	o_wake_body( w, w->bodies + j->edges[0].bodyId );
+	o_wake_body( w, w->bodies + j->edges[1].bodyId );
+}
 
 b2Vec2 b2Joint_GetConstraintForce( b2JointId id )
 {

@@ -429,7 +429,13 @@ typedef struct oFinalize
 	uint8_t* enlarged; /* by awake index */
 	int* fast;
 	int fastCount;
+	uint8_t* awakeIslands; /* by awake island index: some body keeps the island awake */
+	int splitIslandId;	   /* sleepiest body's island that needs splitting first */
+	b2r splitSleepTime;
 } oFinalize;
+
+/* reference src/core.h b2_timeToSleep */
+#define O_TIME_TO_SLEEP R( 0.5f )
 
 static void finalize_bodies( oWorld* w, const oStep* st, oFinalize* f )
 {
@@ -470,6 +476,18 @@ static void finalize_bodies( oWorld* w, const oStep* st, oFinalize* f )
 			b->center0 = b->center;
 			b->rot0 = b->xf.q;
 			b->sleepTime += st->dt;
+		}
+		/* any single body keeps its island awake (reference src/solver.c:281-298) */
+		oIsland* island = w->islands + b->islandId;
+		if ( b->sleepTime < O_TIME_TO_SLEEP )
+			f->awakeIslands[island->localIndex] = 1;
+		else if ( island->constraintRemoveCount > 0 )
+		{
+			if ( b->sleepTime > f->splitSleepTime )
+			{
+				f->splitIslandId = b->islandId;
+				f->splitSleepTime = b->sleepTime;
+			}
 		}
 		for ( int sid = b->headShape; sid != O_NULL; sid = w->shapes[sid].next )
 		{
@@ -719,6 +737,7 @@ void o_solve( oWorld* w, b2r dt, int subSteps )
 
 	w->stepIndex += 1;
 	w->inv_h = st.inv_h;
+	o_merge_awake_islands( w );
 	int awakeCount = w->awake.count;
 	if ( awakeCount == 0 )
 		return;
@@ -849,10 +868,19 @@ void o_solve( oWorld* w, b2r dt, int subSteps )
 	o_capture_outputs( w );
 	o_report_hits( w );
 
+	/* the previous step's split candidate is split beside the constraint solver, before
+	 * the bodies are finalised (reference src/solver.c:1395-1410, :1614-1620) */
+	if ( w->splitIslandId != O_NULL )
+		o_split_island( w, w->splitIslandId );
+	w->splitIslandId = O_NULL;
+
 	oFinalize f;
 	f.enlarged = (uint8_t*)calloc( (size_t)awakeCount, 1 );
 	f.fast = (int*)malloc( sizeof( int ) * (size_t)awakeCount );
 	f.fastCount = 0;
+	f.awakeIslands = (uint8_t*)calloc( (size_t)( w->awakeIslands.count > 0 ? w->awakeIslands.count : 1 ), 1 );
+	f.splitIslandId = O_NULL;
+	f.splitSleepTime = 0;
 	finalize_bodies( w, &st, &f );
 
 	/* enlarge proxies in awake order (reference src/solver.c:1741-1797) */
@@ -879,6 +907,22 @@ void o_solve( oWorld* w, b2r dt, int subSteps )
 
 	continuous_pass( w, f.fast, f.fastCount, false );
 	continuous_pass( w, f.fast, f.fastCount, true );
+
+	/* island sleep, last because it moves bodies out of the awake set (reference
+	 * src/solver.c:1956-2001): keep the split candidate for the next step, then try the
+	 * islands no body kept awake, in reverse so that removal keeps the rest in place */
+	if ( w->enableSleep )
+	{
+		if ( f.splitIslandId != O_NULL && f.splitSleepTime > R( 0 ) )
+			w->splitIslandId = f.splitIslandId;
+		for ( int i = w->awakeIslands.count - 1; i >= 0; --i )
+		{
+			if ( f.awakeIslands[i] )
+				continue;
+			o_try_sleep_island( w, w->awakeIslands.data[i] );
+		}
+	}
+	free( f.awakeIslands );
 	free( f.enlarged );
 	free( f.fast );
 }

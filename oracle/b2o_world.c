@@ -283,6 +283,7 @@ b2WorldId b2CreateWorld( const b2WorldDef* def )
 	w->enableSleep = def->enableSleep;
 	w->enableWarmStarting = true;
 	w->enableContinuous = def->enableContinous;
+	o_islands_init( w );
 	b2WorldId id = { (uint16_t)( slot + 1 ), w->revision };
 	return id;
 }
@@ -305,6 +306,7 @@ void b2DestroyWorld( b2WorldId worldId )
 	oia_free( &w->awake );
 	oia_free( &w->staticBodies );
 	oia_free( &w->nonTouching );
+	o_islands_free( w );
 	oia_free( &w->moveArray );
 	oset_free( &w->moveSet );
 	oset_free( &w->pairSet );
@@ -335,7 +337,20 @@ bool b2World_IsValid( b2WorldId id )
 	return w && w->inUse && w->revision == id.revision;
 }
 
-void b2World_EnableSleeping( b2WorldId id, bool flag ) { o_world( id )->enableSleep = flag; }
+/* reference src/world.c:1568-1594: turning sleep off wakes every sleeping set */
+void b2World_EnableSleeping( b2WorldId id, bool flag )
+{
+	oWorld* w = o_world( id );
+	if ( w->locked || flag == w->enableSleep )
+		return;
+	w->enableSleep = flag;
+	if ( flag == false )
+	{
+		for ( int i = O_SET_FIRST_SLEEPING; i < w->setCap; ++i )
+			if ( w->sets[i].bodies.count > 0 )
+				o_wake_solver_set( w, i );
+	}
+}
 void b2World_EnableContinuous( b2WorldId id, bool flag ) { o_world( id )->enableContinuous = flag; }
 void b2World_EnableWarmStarting( b2WorldId id, bool flag ) { o_world( id )->enableWarmStarting = flag; }
 void b2World_SetRestitutionThreshold( b2WorldId id, float v ) { o_world( id )->restitutionThreshold = v; }
@@ -428,18 +443,33 @@ b2BodyId b2CreateBody( b2WorldId worldId, const b2BodyDef* def )
 	b->angularDamping = def->angularDamping;
 	b->gravityScale = def->gravityScale;
 	b->dq = orot( 1, 0 );
+	b->islandId = O_NULL;
+	b->islandPrev = O_NULL;
+	b->islandNext = O_NULL;
+	/* solver set (reference src/body.c:196-228): static, awake, or a new sleeping set of
+	 * its own; only an awake body keeps the definition's velocity */
+	bool isAwake = def->isAwake || def->enableSleep == false;
+	int setId;
 	if ( def->type == b2_staticBody )
-	{
-		b->awakeIndex = O_NULL;
-		oia_push( &w->staticBodies, id );
-	}
+		setId = O_SET_STATIC;
+	else if ( isAwake )
+		setId = O_SET_AWAKE;
 	else
+		setId = o_create_sleeping_set( w );
+	b->setIndex = setId;
+	b->awakeIndex = O_NULL;
+	b->setLocal = O_NULL;
+	if ( setId == O_SET_AWAKE )
 	{
 		b->awakeIndex = w->awake.count;
-		oia_push( &w->awake, id );
 		b->v = ovf( def->linearVelocity );
 		b->w = def->angularVelocity;
 	}
+	else
+		b->setLocal = o_set_bodies( w, setId )->count;
+	oia_push( o_set_bodies( w, setId ), id );
+	if ( setId >= O_SET_AWAKE )
+		o_create_island_for_body( w, setId, b );
 	b2BodyId bid = { id + 1, (uint16_t)w->slot, b->revision };
 	return bid;
 }
@@ -474,19 +504,66 @@ b2Transform b2Body_GetTransform( b2BodyId id )
 }
 b2Vec2 b2Body_GetLocalPoint( b2BodyId id, b2Vec2 p ) { return b2InvTransformPoint( b2Body_GetTransform( id ), p ); }
 b2Vec2 b2Body_GetWorldPoint( b2BodyId id, b2Vec2 p ) { return b2TransformPoint( b2Body_GetTransform( id ), p ); }
-b2Vec2 b2Body_GetLinearVelocity( b2BodyId id ) { return vfo( get_body( id )->v ); }
-float b2Body_GetAngularVelocity( b2BodyId id ) { return (float)get_body( id )->w; }
-void b2Body_SetLinearVelocity( b2BodyId id, b2Vec2 v )
+/* Velocities live in the awake set only (reference src/body.c:729-787): a body that is
+ * not awake reports zero, and a non-zero velocity wakes it first. */
+b2Vec2 b2Body_GetLinearVelocity( b2BodyId id )
 {
 	oBody* b = get_body( id );
-	if ( b->type != b2_staticBody )
+	return b->setIndex == O_SET_AWAKE ? vfo( b->v ) : b2Vec2_zero;
+}
+float b2Body_GetAngularVelocity( b2BodyId id )
+{
+	oBody* b = get_body( id );
+	return b->setIndex == O_SET_AWAKE ? (float)b->w : 0.0f;
+}
+void b2Body_SetLinearVelocity( b2BodyId id, b2Vec2 v )
+{
+	oWorld* w = body_world( id );
+	oBody* b = get_body( id );
+	if ( v.x * v.x + v.y * v.y > 0.0f )
+		o_wake_body( w, b );
+	if ( b->setIndex == O_SET_AWAKE )
 		b->v = ovf( v );
 }
 void b2Body_SetAngularVelocity( b2BodyId id, float a )
 {
+	oWorld* w = body_world( id );
 	oBody* b = get_body( id );
-	if ( b->type != b2_staticBody )
+	if ( a != 0.0f )
+		o_wake_body( w, b );
+	if ( b->setIndex == O_SET_AWAKE )
 		b->w = a;
+}
+
+/* reference src/body.c:1358-1433 */
+bool b2Body_IsAwake( b2BodyId id ) { return get_body( id )->setIndex == O_SET_AWAKE; }
+void b2Body_SetAwake( b2BodyId id, bool awake )
+{
+	oWorld* w = body_world( id );
+	if ( w->locked )
+		return;
+	oBody* b = get_body( id );
+	if ( awake && b->setIndex >= O_SET_FIRST_SLEEPING )
+		o_wake_body( w, b );
+	else if ( awake == false && b->setIndex == O_SET_AWAKE )
+	{
+		if ( w->islands[b->islandId].constraintRemoveCount > 0 )
+			o_split_island( w, b->islandId );
+		o_try_sleep_island( w, b->islandId );
+	}
+}
+bool b2Body_IsSleepEnabled( b2BodyId id ) { return get_body( id )->enableSleep; }
+void b2Body_SetSleepThreshold( b2BodyId id, float v ) { get_body( id )->sleepThreshold = v; }
+float b2Body_GetSleepThreshold( b2BodyId id ) { return (float)get_body( id )->sleepThreshold; }
+void b2Body_EnableSleep( b2BodyId id, bool enableSleep )
+{
+	oWorld* w = body_world( id );
+	if ( w->locked )
+		return;
+	oBody* b = get_body( id );
+	b->enableSleep = enableSleep;
+	if ( enableSleep == false )
+		o_wake_body( w, b );
 }
 float b2Body_GetMass( b2BodyId id ) { return (float)get_body( id )->mass; }
 float b2Body_GetInertiaTensor( b2BodyId id ) { return (float)get_body( id )->inertia; }
@@ -802,8 +879,15 @@ void o_create_contact( oWorld* w, oShape* shapeA, oShape* shapeB )
 	oContact* c = w->contacts + id;
 	memset( c, 0, sizeof( *c ) );
 	c->id = id;
+	/* non-touching contacts of two bodies that are not awake live in the disabled set
+	 * (reference src/contact.c:210-222) */
+	int setIndex = bodyA->setIndex == O_SET_AWAKE || bodyB->setIndex == O_SET_AWAKE ? O_SET_AWAKE : O_SET_DISABLED;
+	c->setIndex = setIndex;
 	c->colorIndex = O_NULL;
-	c->localIndex = w->nonTouching.count;
+	c->localIndex = o_set_contacts( w, setIndex )->count;
+	c->islandId = O_NULL;
+	c->islandPrev = O_NULL;
+	c->islandNext = O_NULL;
 	c->shapeIdA = shapeA->id;
 	c->shapeIdB = shapeB->id;
 	if ( shapeA->isSensor || shapeB->isSensor )
@@ -832,7 +916,7 @@ void o_create_contact( oWorld* w, oShape* shapeA, oShape* shapeB )
 	bodyB->contactCount += 1;
 
 	oset_add( &w->pairSet, PAIR_KEY( (uint64_t)shapeA->id, (uint64_t)shapeB->id ) );
-	oia_push( &w->nonTouching, id );
+	oia_push( o_set_contacts( w, setIndex ), id );
 
 	c->simIndexA = O_NULL;
 	c->simIndexB = O_NULL;
@@ -861,20 +945,36 @@ static void unlink_edge( oWorld* w, oContact* c, int e )
 	body->contactCount -= 1;
 }
 
-void o_destroy_contact( oWorld* w, oContact* c )
+/* reference src/contact.c:320-449 */
+void o_destroy_contact( oWorld* w, oContact* c, bool wakeBodies )
 {
 	oset_remove( &w->pairSet, PAIR_KEY( (uint64_t)c->shapeIdA, (uint64_t)c->shapeIdB ) );
+	int bodyIdA = c->edges[0].bodyId;
+	int bodyIdB = c->edges[1].bodyId;
 	unlink_edge( w, c, 0 );
 	unlink_edge( w, c, 1 );
+	if ( c->islandId != O_NULL )
+		o_unlink_contact( w, c );
 	if ( c->colorIndex != O_NULL )
-		o_remove_contact_from_graph( w, c->edges[0].bodyId, c->edges[1].bodyId, c->colorIndex, c->localIndex );
+		o_remove_contact_from_graph( w, bodyIdA, bodyIdB, c->colorIndex, c->localIndex );
 	else
-		remove_non_touching( w, c->localIndex );
+	{
+		oIntArray* list = o_set_contacts( w, c->setIndex );
+		int moved = oia_remove_swap( list, c->localIndex );
+		if ( moved != O_NULL )
+			w->contacts[list->data[c->localIndex]].localIndex = c->localIndex;
+	}
 	int id = c->id;
 	c->id = O_NULL;
+	c->setIndex = O_NULL;
 	c->colorIndex = O_NULL;
 	c->localIndex = O_NULL;
 	oid_free( &w->contactIds, id );
+	if ( wakeBodies )
+	{
+		o_wake_body( w, w->bodies + bodyIdA );
+		o_wake_body( w, w->bodies + bodyIdB );
+	}
 }
 
 /* ------------------------------------------------------------ colouring */
@@ -1053,20 +1153,43 @@ oJoint* o_create_joint( b2WorldId worldId, b2BodyId bodyIdA, b2BodyId bodyIdB, b
 	b->headJointKey = keyB;
 	b->jointCount += 1;
 
-	bool staticA = a->type == b2_staticBody;
-	bool staticB = b->type == b2_staticBody;
-	if ( staticA && staticB )
+	j->islandId = O_NULL;
+	j->islandPrev = O_NULL;
+	j->islandNext = O_NULL;
+	j->colorIndex = O_NULL;
+
+	/* solver set (reference src/joint.c:198-283): between static bodies the static set;
+	 * touching the awake set the constraint graph, waking a sleeping partner first;
+	 * otherwise the sleeping set, merging two sleeping sets */
+	int maxSetIndex = a->setIndex > b->setIndex ? a->setIndex : b->setIndex;
+	if ( a->setIndex == O_SET_STATIC && b->setIndex == O_SET_STATIC )
 	{
-		j->colorIndex = O_NULL;
-		j->localIndex = O_NULL;
+		j->setIndex = O_SET_STATIC;
+		j->localIndex = w->sets[O_SET_STATIC].joints.count;
+		oia_push( &w->sets[O_SET_STATIC].joints, id );
 	}
-	else
+	else if ( a->setIndex == O_SET_AWAKE || b->setIndex == O_SET_AWAKE )
 	{
+		if ( maxSetIndex >= O_SET_FIRST_SLEEPING )
+			o_wake_solver_set( w, maxSetIndex );
+		j->setIndex = O_SET_AWAKE;
+		bool staticA = a->setIndex == O_SET_STATIC;
+		bool staticB = b->setIndex == O_SET_STATIC;
 		int color = o_assign_joint_color( w, a->id, b->id, staticA, staticB );
 		j->colorIndex = color;
 		j->localIndex = w->colors[color].joints.count;
 		oia_push( &w->colors[color].joints, id );
 	}
+	else
+	{
+		j->setIndex = maxSetIndex;
+		j->localIndex = w->sets[maxSetIndex].joints.count;
+		oia_push( &w->sets[maxSetIndex].joints, id );
+		if ( a->setIndex != b->setIndex && a->setIndex >= O_SET_FIRST_SLEEPING && b->setIndex >= O_SET_FIRST_SLEEPING )
+			o_merge_solver_sets( w, a->setIndex, b->setIndex );
+	}
+	if ( j->setIndex > O_SET_DISABLED )
+		o_link_joint( w, j );
 	b2JointId jid = { id + 1, worldId.index1 - 1, j->revision };
 	*out = jid;
 	return j;
@@ -1095,7 +1218,7 @@ void o_destroy_contacts_between( oWorld* w, int bodyIdA, int bodyIdB )
 		int e = key & 1;
 		key = c->edges[e].nextKey;
 		if ( c->edges[e ^ 1].bodyId == other )
-			o_destroy_contact( w, c );
+			o_destroy_contact( w, c, false );
 	}
 }
 
@@ -1429,7 +1552,7 @@ void o_collide( oWorld* w )
 				if ( ( flags & OC_TOUCHING ) && ( flags & OC_ENABLE_CONTACT_EVENTS ) )
 					add_event_end( w, c->shapeIdA, c->shapeIdB );
 				c->flags &= ~OC_TOUCHING;
-				o_destroy_contact( w, c );
+				o_destroy_contact( w, c, false );
 			}
 			else if ( simFlags & OS_STARTED )
 			{
@@ -1449,7 +1572,10 @@ void o_collide( oWorld* w )
 				{
 					if ( flags & OC_ENABLE_CONTACT_EVENTS )
 						add_event_begin( w, c->shapeIdA, c->shapeIdB );
+					/* link first: it may wake a sleeping set, which appends to the awake
+					 * lists and leaves this contact's place unchanged */
 					c->flags |= OC_TOUCHING;
+					o_link_contact( w, c );
 					c->simFlags &= ~OS_STARTED;
 					int localIndex = c->localIndex;
 					o_add_contact_to_graph( w, c );
@@ -1475,8 +1601,10 @@ void o_collide( oWorld* w )
 					c->flags &= ~OC_TOUCHING;
 					if ( c->flags & OC_ENABLE_CONTACT_EVENTS )
 						add_event_end( w, c->shapeIdA, c->shapeIdB );
+					o_unlink_contact( w, c );
 					int a = c->edges[0].bodyId, b = c->edges[1].bodyId;
 					int colorIndex = c->colorIndex, localIndex = c->localIndex;
+					c->setIndex = O_SET_AWAKE;
 					c->colorIndex = O_NULL;
 					c->localIndex = w->nonTouching.count;
 					oia_push( &w->nonTouching, id );
@@ -1511,7 +1639,7 @@ void b2World_Step( b2WorldId worldId, float timeStep, int subStepCount )
  * (b2DestroyShapeInternal, b2DestroyShape), src/shape.c:704-711 and
  * src/broad_phase.c:71-116 (proxy destruction with the move-buffer purge),
  * src/joint.c:657-768 (b2DestroyJointInternal) and src/constraint_graph.c:297-324.
- * Islands and sleep are not restated: with every body awake, waking is a no-op. */
+ * Destruction unlinks islands and wakes the bodies it touches, as the reference does. */
 static void unbuffer_move( oWorld* w, int proxyKey )
 {
 	if ( oset_remove( &w->moveSet, (uint64_t)( proxyKey + 1 ) ) == false )
@@ -1549,11 +1677,22 @@ static void unlink_joint_edge( oWorld* w, oJoint* j, int e )
 	body->jointCount -= 1;
 }
 
-static void destroy_joint( oWorld* w, oJoint* j )
+/* reference src/joint.c:657-752 */
+static void destroy_joint( oWorld* w, oJoint* j, bool wakeBodies )
 {
+	int bodyIdA = j->edges[0].bodyId;
+	int bodyIdB = j->edges[1].bodyId;
 	unlink_joint_edge( w, j, 0 );
 	unlink_joint_edge( w, j, 1 );
-	if ( j->colorIndex != O_NULL )
+	o_unlink_joint( w, j );
+	if ( j->setIndex != O_SET_AWAKE )
+	{
+		oIntArray* list = o_set_joints( w, j->setIndex );
+		int moved = oia_remove_swap( list, j->localIndex );
+		if ( moved != O_NULL )
+			w->joints[list->data[j->localIndex]].localIndex = j->localIndex;
+	}
+	else
 	{
 		oColor* color = w->colors + j->colorIndex;
 		if ( j->colorIndex != O_OVERFLOW )
@@ -1566,10 +1705,16 @@ static void destroy_joint( oWorld* w, oJoint* j )
 			w->joints[color->joints.data[j->localIndex]].localIndex = j->localIndex;
 	}
 	int id = j->id;
+	j->setIndex = O_NULL;
 	j->colorIndex = O_NULL;
 	j->localIndex = O_NULL;
 	j->id = O_NULL;
 	oid_free( &w->jointIds, id );
+	if ( wakeBodies )
+	{
+		o_wake_body( w, w->bodies + bodyIdA );
+		o_wake_body( w, w->bodies + bodyIdB );
+	}
 }
 
 void b2DestroyJoint( b2JointId jointId )
@@ -1579,11 +1724,11 @@ void b2DestroyJoint( b2JointId jointId )
 	oWorld* w = s_worlds[jointId.world0];
 	if ( w->locked )
 		return;
-	destroy_joint( w, w->joints + ( jointId.index1 - 1 ) );
+	destroy_joint( w, w->joints + ( jointId.index1 - 1 ), true );
 }
 
 /* Unlinks and frees a shape with its proxy and contacts (reference src/shape.c:220-269). */
-static void destroy_shape_internal( oWorld* w, oShape* s, oBody* b )
+static void destroy_shape_internal( oWorld* w, oShape* s, oBody* b, bool wakeBodies )
 {
 	int id = s->id;
 	if ( s->prev != O_NULL )
@@ -1600,7 +1745,7 @@ static void destroy_shape_internal( oWorld* w, oShape* s, oBody* b )
 		oContact* c = w->contacts + ( key >> 1 );
 		key = c->edges[key & 1].nextKey;
 		if ( c->shapeIdA == id || c->shapeIdB == id )
-			o_destroy_contact( w, c );
+			o_destroy_contact( w, c, wakeBodies );
 	}
 	oid_free( &w->shapeIds, id );
 	s->id = O_NULL;
@@ -1615,7 +1760,7 @@ void b2DestroyShape( b2ShapeId shapeId )
 		return;
 	oShape* s = get_shape( shapeId );
 	oBody* b = w->bodies + s->bodyId;
-	destroy_shape_internal( w, s, b );
+	destroy_shape_internal( w, s, b, true );
 	if ( b->automaticMass )
 		o_update_body_mass( w, b );
 }
@@ -1731,7 +1876,7 @@ void b2DestroyChain( b2ChainId chainId )
 		return;
 	*link = chain->nextChainId;
 	for ( int i = 0; i < chain->count; ++i )
-		destroy_shape_internal( w, w->shapes + chain->shapeIndices[i], body );
+		destroy_shape_internal( w, w->shapes + chain->shapeIndices[i], body, true );
 	free( chain->shapeIndices );
 	chain->shapeIndices = NULL;
 	oid_free( &w->chainIds, chain->id );
@@ -1805,14 +1950,14 @@ void b2DestroyBody( b2BodyId bodyId )
 	{
 		oJoint* j = w->joints + ( key >> 1 );
 		key = j->edges[key & 1].nextKey;
-		destroy_joint( w, j );
+		destroy_joint( w, j, true );
 	}
 	key = b->headContactKey;
 	while ( key != O_NULL )
 	{
 		oContact* c = w->contacts + ( key >> 1 );
 		key = c->edges[key & 1].nextKey;
-		o_destroy_contact( w, c );
+		o_destroy_contact( w, c, true );
 	}
 	for ( int sid = b->headShape; sid != O_NULL; )
 	{
@@ -1831,15 +1976,12 @@ void b2DestroyBody( b2BodyId bodyId )
 		chain->id = O_NULL;
 		cid = chain->nextChainId;
 	}
-	/* the awake set drops the body by moving its last body into the slot */
-	if ( b->awakeIndex != O_NULL )
-	{
-		int at = b->awakeIndex;
-		int moved = oia_remove_swap( &w->awake, at );
-		if ( moved != O_NULL )
-			w->bodies[w->awake.data[at]].awakeIndex = at;
-	}
+	/* the body's set drops it by moving its last body into the slot */
+	o_remove_body_from_island( w, b );
+	o_remove_body_from_set( w, b );
 	oid_free( &w->bodyIds, b->id );
+	b->setIndex = O_NULL;
 	b->awakeIndex = O_NULL;
+	b->setLocal = O_NULL;
 	b->id = O_NULL;
 }

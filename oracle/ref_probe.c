@@ -49,6 +49,20 @@ int b2World_InspectBodies( b2WorldId worldId, float* out, int capacity )
 	return count;
 }
 
+int b2World_InspectIslands( b2WorldId worldId, int* out, int capacity )
+{
+	b2World* world = b2GetWorldFromId( worldId );
+	int count = b2Array( world->bodyArray ).count;
+	for ( int i = 0; i < count && i < capacity; ++i )
+	{
+		b2Body* body = world->bodyArray + i;
+		bool live = body->id == i && body->setIndex != B2_NULL_INDEX;
+		out[2 * i] = live ? body->setIndex : -1;
+		out[2 * i + 1] = live ? body->islandId : -1;
+	}
+	return count;
+}
+
 int b2World_InspectShapes( b2WorldId worldId, b2InspectShape* out, int capacity )
 {
 	b2World* world = b2GetWorldFromId( worldId );
