@@ -27,7 +27,7 @@ NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = ["kernels.cu", "fused.cu", "batch.cu", "adjoint.cu", "arena.cu", "pairs.cu", "solve_api.cu", "solve_noalloc.cu"]
-C_SOURCES = ["world.c", "joint.c", "step.c", "batch.c", "pool.c", "adjoint.c", "tree.c", "util.c", "geometry.c"]
+C_SOURCES = ["world.c", "joint.c", "island.c", "step.c", "batch.c", "pool.c", "adjoint.c", "tree.c", "util.c", "geometry.c"]
 HEADERS = ["b2g_math.h", "b2g_types.h", "b2g_collide.h", "b2g_device.h", "b2g_solve.h", "b2g_joints.h", "b2g_stages.h", "b2g_dual.h", "b2g_cluster.h", "b2g_packs.h", "host.h"]
 
 LIB = os.path.join(OUT, "libbox2d_gb300.so")

@@ -113,6 +113,8 @@ extern "C" void b2gd_free( b2gDevWorld* w, b2gHostIO* io )
 	FREE_DEV( w->force );
 	FREE_DEV( w->extent );
 	FREE_DEV( w->bodyInfo );
+	FREE_DEV( w->sleepTime );
+	FREE_DEV( w->bodyOps );
 	FREE_DEV( w->awake );
 	FREE_DEV( w->shapeRange );
 	FREE_DEV( w->shapeList );
@@ -146,6 +148,8 @@ extern "C" void b2gd_free( b2gDevWorld* w, b2gHostIO* io )
 		cudaFreeHost( io->events );
 	if ( io->records )
 		cudaFreeHost( io->records );
+	if ( io->sleepy )
+		cudaFreeHost( io->sleepy );
 	if ( io->counters )
 		cudaFreeHost( io->counters );
 	if ( io->newContacts )
@@ -192,7 +196,10 @@ extern "C" int b2gd_reserve( b2gDevWorld* w, b2gHostIO* io, int bodyCap, int sha
 		e |= grow( &w->force, o4, n4, s );
 		e |= grow( &w->extent, o4, n4, s );
 		e |= grow( (void**)&w->bodyInfo, 4u * (size_t)w->bodyCap, 4u * (size_t)nc, s );
+		e |= grow( (void**)&w->sleepTime, 4u * (size_t)w->bodyCap, 4u * (size_t)nc, s );
+		e |= grow( (void**)&w->bodyOps, 4u * (size_t)w->bodyCap, 4u * (size_t)nc, s );
 		e |= grow( (void**)&w->awake, 4u * (size_t)w->bodyCap, 4u * (size_t)nc, s );
+		e |= grow_host_mapped( (void**)&io->sleepy, (void**)&w->sleepy, 8u * (size_t)nc );
 		e |= grow( (void**)&w->shapeRange, 8u * (size_t)w->bodyCap, 8u * (size_t)nc, s );
 		w->bodyCap = nc;
 	}

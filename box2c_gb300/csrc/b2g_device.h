@@ -35,9 +35,10 @@ typedef struct b2gSolvePlan
 /* Pinned host staging owned by the device module (mapped into the device). */
 typedef struct b2gHostIO
 {
-	int* counters;		/* [0] events [1] records [2] status, copied back each sync */
+	int* counters;		/* [0] events [1] records [2] status [3] sleepy bodies, copied back each sync */
 	int* events;		/* mapped: narrowphase events */
 	b2gRecord* records; /* mapped: finalisation records */
+	int* sleepy;		/* mapped: bodies past the sleep time, 2 ints each (awake index, sleep time bits) */
 	b2gContactInit* newContacts;
 	int* hitIds;	/* mapped: contacts to test for hit events */
 	float* hitOut; /* mapped: 8 per contact: hit, approach speed, point, normal, 0, 0 */
@@ -62,6 +63,10 @@ int b2gd_reserve( b2gDevWorld* w, b2gHostIO* io, int bodyCap, int shapeCap, int 
 int b2gd_upload_bodies( b2gDevWorld* w, const float* state, const float* xf, const float* centers, const float* prev,
 						const float* mass, const float* force, const float* extent, const int* info, int count );
 int b2gd_upload_awake( b2gDevWorld* w, const int* awake, int count );
+/* Applies ops[0, count) (one per body, (bodyId << 2) | B2G_BODY_*) on the world's stream
+ * (sleep: stop integrating; wake: identity state, zero sleep timer).  The copy is taken
+ * from pageable memory, so ops may be reused when the call returns. */
+int b2gd_body_ops( b2gDevWorld* w, const int* ops, int count );
 int b2gd_upload_shapes( b2gDevWorld* w, const b2gShapeGeo* geo, const float* aabb, const float* fat, int count );
 int b2gd_upload_shape_lists( b2gDevWorld* w, const int* range, int bodyCount, const int* list, int listCount );
 int b2gd_upload_joints( b2gDevWorld* w, const b2gJointDev* joints, int count );

@@ -101,6 +101,29 @@ static __device__ b2gBox shape_aabb( const b2gShapeGeo& g, b2gXf xf )
 	}
 }
 
+/* ------------------------------------------------------------------ sleep and wake */
+/* A staged body operation (reference src/solver_set.c:50-58, :190-214): a woken body
+ * starts from the identity state (zero velocity, no pending motion) with a zero sleep
+ * timer; a sleeping body stops being integrated.  The sleep threshold in the velocity's
+ * spare lane stays. */
+static __device__ __forceinline__ void apply_body_op( const b2gDevWorld& W, int op )
+{
+	int b = op >> 2;
+	if ( ( op & 3 ) == B2G_BODY_WAKE )
+	{
+		float4* st = (float4*)W.state;
+		float threshold = st[2 * b].w;
+		st[2 * b] = make_float4( 0.0f, 0.0f, 0.0f, threshold );
+		st[2 * b + 1] = make_float4( 0.0f, 0.0f, 1.0f, 0.0f );
+		W.sleepTime[b] = 0.0f;
+		W.bodyInfo[b] |= B2G_B_AWAKE;
+	}
+	else
+	{
+		W.bodyInfo[b] &= ~B2G_B_AWAKE;
+	}
+}
+
 /* ------------------------------------------------------------------ contact creation */
 static __device__ __forceinline__ void scatter_contact( const b2gDevWorld& W, const b2gContactInit* inits, int t )
 {
@@ -111,11 +134,18 @@ static __device__ __forceinline__ void scatter_contact( const b2gDevWorld& W, co
 		W.cFlags[id] = 0;
 		return;
 	}
+	uint32_t asleep = ( c.flags & B2G_INIT_ASLEEP ) ? B2G_C_ASLEEP : 0u;
+	if ( c.flags & B2G_INIT_SET )
+	{
+		/* the contact moved into or out of the awake set: only its set bit changes */
+		W.cFlags[id] = ( W.cFlags[id] & ~(uint32_t)B2G_C_ASLEEP ) | asleep;
+		return;
+	}
 	W.cShapes[2 * id] = c.shapeA;
 	W.cShapes[2 * id + 1] = c.shapeB;
 	W.cMix[2 * id] = c.friction;
 	W.cMix[2 * id + 1] = c.restitution;
-	W.cFlags[id] = B2G_C_LIVE;
+	W.cFlags[id] = B2G_C_LIVE | asleep;
 	W.cCache[id] = 0u;
 	W.cBodies[2 * id] = -1;
 	W.cBodies[2 * id + 1] = -1;
@@ -189,7 +219,8 @@ static __device__ __forceinline__ void emit_event( const b2gDevWorld& W, int id,
 static __device__ void collide_contact( const b2gDevWorld& W, int id )
 {
 	uint32_t flags = W.cFlags[id];
-	if ( ( flags & B2G_C_LIVE ) == 0 )
+	/* only the awake set's contacts are updated (reference src/world.c:436-466) */
+	if ( ( flags & B2G_C_LIVE ) == 0 || ( flags & B2G_C_ASLEEP ) != 0 )
 		return;
 	int sA = W.cShapes[2 * id];
 	int sB = W.cShapes[2 * id + 1];
@@ -206,10 +237,13 @@ static __device__ void collide_contact( const b2gDevWorld& W, int id )
 	const b2gShapeGeo* gB = W.geo + sB;
 	int bA = gA->bodyId;
 	int bB = gB->bodyId;
+	/* solver rows address a body by id unless it is static: a contact joins the graph
+	 * only with awake or static bodies, including a body woken by the contact itself
+	 * after this narrowphase (reference src/constraint_graph.c:141-170) */
 	int infoA = W.bodyInfo[bA];
 	int infoB = W.bodyInfo[bB];
-	W.cBodies[2 * id] = ( infoA & B2G_B_AWAKE ) ? bA : -1;
-	W.cBodies[2 * id + 1] = ( infoB & B2G_B_AWAKE ) ? bB : -1;
+	W.cBodies[2 * id] = ( infoA & B2G_B_TYPE_MASK ) != 0 ? bA : -1;
+	W.cBodies[2 * id + 1] = ( infoB & B2G_B_TYPE_MASK ) != 0 ? bB : -1;
 	const float4* xf = (const float4*)W.xf;
 	const float4* centers = (const float4*)W.centers;
 	float4 xa = xf[bA], xb = xf[bB];
@@ -406,8 +440,9 @@ static __device__ void prepare_joint( const b2gDevWorld& W, int t, const b2gStep
 	float4 ma = mass[a], mb = mass[b];
 	float4 xa = xf[a], xb = xf[b];
 	float4 ca = centers[a], cb = centers[b];
-	j->indexA = ( W.bodyInfo[a] & B2G_B_AWAKE ) ? a : -1;
-	j->indexB = ( W.bodyInfo[b] & B2G_B_AWAKE ) ? b : -1;
+	/* a joint in the graph has awake or static bodies */
+	j->indexA = ( W.bodyInfo[a] & B2G_B_TYPE_MASK ) != 0 ? a : -1;
+	j->indexB = ( W.bodyInfo[b] & B2G_B_TYPE_MASK ) != 0 ? b : -1;
 	JointBodies jb;
 	jb.mA = ma.y;
 	jb.iA = ma.w;
@@ -530,10 +565,28 @@ static __device__ void finalize_body( const b2gDevWorld& W, int i, const b2gStep
 
 	bool isFast = false;
 	float sleepThreshold = s0.w;
+	float sleepTime = W.sleepTime[b];
 	if ( sc.enableSleep == 0 || ( info & B2G_B_SLEEP_OK ) == 0 || sleepVelocity > sleepThreshold )
 	{
+		sleepTime = 0.0f;
 		if ( ( info & B2G_B_TYPE_MASK ) == 2 && sc.enableContinuous && maxVelocity * sc.dt > 0.5f * minExtent )
 			isFast = true;
+	}
+	else
+	{
+		sleepTime += sc.dt;
+	}
+	W.sleepTime[b] = sleepTime;
+	/* a body past the sleep time no longer keeps its island awake: the host learns of
+	 * it and decides the island's sleep (reference src/solver.c:281-298) */
+	if ( sleepTime >= B2G_TIME_TO_SLEEP )
+	{
+		int slot = atomicAdd( W.counters + 3, 1 );
+		if ( slot < W.bodyCap )
+		{
+			W.sleepy[2 * slot] = i;
+			W.sleepy[2 * slot + 1] = __float_as_int( sleepTime );
+		}
 	}
 	/* with no time-of-impact event the fast body also advances its sweep start; the host
 	 * moves it back along the sweep when continuous collision finds an impact */

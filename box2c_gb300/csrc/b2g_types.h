@@ -74,6 +74,7 @@ typedef struct b2gManifold
 enum
 {
 	B2G_C_LIVE = 0x1,
+	B2G_C_ASLEEP = 0x2, /* outside the awake set: skipped by the narrowphase */
 	B2G_C_TOUCHING = 0x10000,
 	B2G_C_HIT = 0x100000,
 };
@@ -95,9 +96,26 @@ enum
 	B2G_B_SLEEP_OK = 0x10,
 };
 
-/* Staged contact record: a contact created by the host broadphase (flags 0), or the
- * retirement of a destroyed contact id (flags B2G_INIT_KILL). */
+/* Staged contact record: a contact created by the host broadphase (flags 0, or
+ * B2G_INIT_ASLEEP when it starts outside the awake set), the retirement of a destroyed
+ * contact id (flags B2G_INIT_KILL), or a move of a live contact into or out of the awake
+ * set (B2G_INIT_SET, with B2G_INIT_ASLEEP when it leaves it). */
 #define B2G_INIT_KILL 0x80000000u
+#define B2G_INIT_SET 0x40000000u
+#define B2G_INIT_ASLEEP 0x20000000u
+
+/* Seconds a body must stay below its sleep velocity before its island may sleep
+ * (reference src/core.h b2_timeToSleep). */
+#define B2G_TIME_TO_SLEEP 0.5f
+
+/* Body operations staged by the host, applied on the device before the next kernel that
+ * reads the body: (bodyId << 2) | code. */
+enum
+{
+	B2G_BODY_SLEEP = 0, /* leaves the awake set */
+	B2G_BODY_WAKE = 1,	/* joins the awake set with zero velocity and a zero sleep timer */
+	B2G_BODY_RESET = 2, /* a new body: zero sleep timer */
+};
 
 typedef struct b2gContactInit
 {
@@ -215,6 +233,8 @@ typedef struct b2gDevWorld
 	void* force;   /* float4: force.x force.y torque gravityScale */
 	void* extent;  /* float4: linearDamping angularDamping minExtent maxExtent */
 	int* bodyInfo;
+	float* sleepTime; /* seconds below the sleep velocity, by body id */
+	int* bodyOps;	  /* staged body operations ((bodyId << 2) | B2G_BODY_*), one per body at most */
 	int* awake;		 /* awake body ids in solver order */
 	int* shapeRange; /* 2 per body: start, count into shapeList */
 	int* shapeList;
@@ -250,9 +270,10 @@ typedef struct b2gDevWorld
 	/* staging and outputs */
 	b2gContactInit* newContacts;
 	int newCap;
-	int* counters;	   /* device: [0] events, [1] records, [2] status */
+	int* counters;	   /* device: [0] events, [1] records, [2] status, [3] sleepy bodies */
 	int* events;	   /* device view of the mapped event buffer */
 	b2gRecord* records; /* device view of the mapped record buffer */
+	int* sleepy;	   /* device view of the mapped sleepy-body buffer: 2 ints per body (awake index, sleep time bits) */
 	int eventCap, recordCap;
 	void* stream; /* cudaStream_t */
 	void* timers[8]; /* cudaEvent_t: step start, collide start/end, solve start/end, finalize end, step end */

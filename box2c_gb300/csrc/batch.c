@@ -162,6 +162,7 @@ static void finish_worlds( int begin, int end, void* arg )
 		if ( c->items[k].solve && w->status == 0 )
 		{
 			w->io.counters[1] = b2gd_batch_counters( s_batch, k )[1];
+			w->io.counters[3] = b2gd_batch_counters( s_batch, k )[3];
 			gstep_finish( w );
 		}
 		w->dev.stream = s_streams[k];

@@ -265,7 +265,10 @@ __device__ void solve_world( const b2gBatchItem& it, const b2gStepConst& sc, flo
 	const float4* mass = (const float4*)W.mass;
 
 	if ( tid == 0 )
+	{
 		W.counters[1] = 0;
+		W.counters[3] = 0;
+	}
 	for ( int b = tid; b < N; b += step )
 	{
 		st0[b] = gst[2 * b];

@@ -152,6 +152,10 @@ typedef struct gBody
 	uint16_t revision;
 	bool fixedRotation, isBullet, enableSleep, automaticMass;
 	float sleepThreshold;
+	int setIndex; /* solver set: G_SET_STATIC, G_SET_AWAKE or a sleeping set */
+	int setLocal; /* position in a sleeping set's body list */
+	int islandId, islandPrev, islandNext;
+	bool isMarked;
 } gBody;
 
 typedef struct gShape
@@ -197,7 +201,10 @@ enum
 typedef struct gContact
 {
 	int id;
+	int setIndex; /* awake, disabled (non-touching between bodies not awake) or sleeping */
 	int colorIndex, localIndex;
+	int islandId, islandPrev, islandNext;
+	bool isMarked;
 	gEdge edges[2];
 	int shapeIdA, shapeIdB;
 	uint32_t flags;
@@ -210,11 +217,45 @@ typedef struct gJoint
 	b2JointType type;
 	int bodyIdA, bodyIdB;
 	gEdge edges[2];
+	int setIndex;
 	int colorIndex, localIndex;
+	int islandId, islandPrev, islandNext;
+	bool isMarked;
 	bool collideConnected;
 	uint16_t revision;
 	void* userData;
 } gJoint;
+
+/* Solver sets (reference src/solver_set.h:11-30): static, disabled, awake, then one per
+ * group of sleeping islands. */
+enum
+{
+	G_SET_STATIC = 0,
+	G_SET_DISABLED = 1,
+	G_SET_AWAKE = 2,
+	G_SET_FIRST_SLEEPING = 3,
+};
+
+/* A persistent island (reference src/island.h:32-56): its bodies, touching contacts and
+ * joints as linked lists through the records, and a union-find parent for islands that
+ * a new constraint joined since the last merge. */
+typedef struct gIsland
+{
+	int setIndex, localIndex, islandId;
+	int headBody, tailBody, bodyCount;
+	int headContact, tailContact, contactCount;
+	int headJoint, tailJoint, jointCount;
+	int parentIsland;
+	int constraintRemoveCount;
+} gIsland;
+
+/* The members of a sleeping set in set order; the awake set's are the awake lists and
+ * the graph colours. */
+typedef struct gSolverSet
+{
+	int setIndex; /* -1 when free */
+	gIntArray bodies, contacts, joints, islands;
+} gSolverSet;
 
 /* Pairs found from one moved proxy (kept across steps, only the count is reset). */
 typedef struct gPairList
@@ -269,6 +310,23 @@ typedef struct gWorld
 	gIntArray awake;
 	gIntArray nonTouching;
 	gColor colors[B2G_COLORS];
+
+	/* islands and solver sets (island.c) */
+	gIntArray disabledContacts; /* non-touching contacts whose bodies are both not awake */
+	gIntArray staticJoints;		/* joints between two static bodies */
+	gIntArray awakeIslands;		/* awake island ids in set order */
+	gIsland* islands;
+	int islandCap;
+	gIdPool islandIds;
+	gSolverSet* sets; /* by set id; entries below G_SET_FIRST_SLEEPING unused */
+	int setCap;
+	gIdPool setIds;
+	int splitIslandId;	  /* island to split at the next solve, or -1 */
+	gIntArray bodyOps;	  /* device body operations staged since the last flush */
+	int* bodyOpSlot;	  /* per body id: its op's position in bodyOps, or -1 */
+	int bodyOpSlotCap;
+	int* islandSleepy;	  /* per awake island: bodies past the sleep time this step */
+	int islandSleepyCap;
 
 	gTree trees[3];
 	gIntArray moveArray;
@@ -369,7 +427,44 @@ void gstep_finish( gWorld* w );
 void gtape_record( gWorld* w, const b2gSolvePlan* plan, const b2gStepConst* sc, int solve );
 void gtape_free( gWorld* w );
 void gcontact_create( gWorld* w, gShape* a, gShape* b );
-void gcontact_destroy( gWorld* w, gContact* c );
+void gcontact_destroy( gWorld* w, gContact* c, bool wakeBodies );
+void gcontact_add_to_graph( gWorld* w, gContact* c );
+void gcontact_remove_from_graph( gWorld* w, int bodyIdA, int bodyIdB, int colorIndex, int localIndex );
+/* Stages the move of a live contact into (asleep false) or out of the awake set for the
+ * device narrowphase. */
+void gcontact_stage_set( gWorld* w, int contactId, bool asleep );
+
+/* Islands, solver sets and sleep (island.c; reference src/island.c, src/solver_set.c,
+ * src/body.c:84-159). */
+void gislands_init( gWorld* w );
+void gislands_free( gWorld* w );
+void gisland_create_for_body( gWorld* w, int setIndex, gBody* b );
+void gisland_remove_body( gWorld* w, gBody* b );
+void gisland_link_contact( gWorld* w, gContact* c );
+void gisland_unlink_contact( gWorld* w, gContact* c );
+void gisland_link_joint( gWorld* w, gJoint* j );
+void gisland_unlink_joint( gWorld* w, gJoint* j );
+void gislands_merge_awake( gWorld* w );
+void gisland_split( gWorld* w, int baseId );
+void gsolver_set_wake( gWorld* w, int setIndex );
+void gisland_try_sleep( gWorld* w, int islandId );
+void gsolver_set_merge( gWorld* w, int setId1, int setId2 );
+int gsolver_set_create( gWorld* w );
+bool gbody_wake( gWorld* w, gBody* b );
+void gbody_remove_from_set( gWorld* w, gBody* b );
+gIntArray* gsolver_set_bodies( gWorld* w, int setIndex );
+gIntArray* gsolver_set_contacts( gWorld* w, int setIndex );
+gIntArray* gsolver_set_joints( gWorld* w, int setIndex );
+/* Stages a device body operation (B2G_BODY_SLEEP or B2G_BODY_WAKE); the last one staged
+ * for a body wins.  The host mirror follows at once. */
+void gbody_stage_op( gWorld* w, int bodyId, int code );
+/* The same for a body being created, whose mirror the caller writes in full. */
+void gbody_stage_new( gWorld* w, int bodyId, int code );
+/* Applies the staged body operations and the awake list on the device. */
+int gbody_flush_ops( gWorld* w );
+/* End of a step: the sleepy bodies the device reported, the split candidate and the
+ * islands that fall asleep (reference src/solver.c:1956-2001). */
+void gislands_sleep_step( gWorld* w );
 int gassign_joint_color( gWorld* w, int bodyIdA, int bodyIdB, bool staticA, bool staticB );
 
 /* Joints (world.c: the record shared by every type; joint.c: the per-type API). */

@@ -358,7 +358,16 @@ void b2Joint_SetUserData( b2JointId id, void* userData ) { joint_rec( id )->user
 void* b2Joint_GetUserData( b2JointId id ) { return joint_rec( id )->userData; }
 
 /* Every body is awake (sleep is not simulated), so waking is a no-op. */
-void b2Joint_WakeBodies( b2JointId id ) { (void)id; }
+/* reference src/joint.c:874-888 */
+void b2Joint_WakeBodies( b2JointId id )
+{
+	gWorld* w = joint_world( id );
+	if ( w->locked )
+		return;
+	gJoint* j = w->joints + ( id.index1 - 1 );
+	gbody_wake( w, w->bodies + j->edges[0].bodyId );
+	gbody_wake( w, w->bodies + j->edges[1].bodyId );
+}
 
 b2Vec2 b2Joint_GetConstraintForce( b2JointId id )
 {

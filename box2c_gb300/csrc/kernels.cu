@@ -40,6 +40,13 @@ __global__ void k_scatter_contacts( b2gDevWorld W, const b2gContactInit* inits, 
 		scatter_contact( W, inits, t );
 }
 
+__global__ void k_body_ops( b2gDevWorld W, const int* ops, int n )
+{
+	int t = blockIdx.x * blockDim.x + threadIdx.x;
+	if ( t < n )
+		apply_body_op( W, ops[t] );
+}
+
 __global__ void __launch_bounds__( BLOCK ) k_collide( b2gDevWorld W, int idCount )
 {
 	int id = blockIdx.x * blockDim.x + threadIdx.x;
@@ -175,6 +182,19 @@ extern "C" int b2gd_collide( b2gDevWorld* w, b2gHostIO* io, int newCount, int id
 	return check( cudaGetLastError() );
 }
 
+/* Applies staged body operations (one per body) on the world's stream, ahead of every
+ * later copy or kernel that reads the bodies. */
+extern "C" int b2gd_body_ops( b2gDevWorld* w, const int* ops, int count )
+{
+	if ( count <= 0 )
+		return 0;
+	cudaStream_t s = (cudaStream_t)w->stream;
+	cudaMemcpyAsync( w->bodyOps, ops, sizeof( int ) * (size_t)count, cudaMemcpyHostToDevice, s );
+	w->h2dBytes += (long long)( sizeof( int ) * (size_t)count );
+	k_body_ops<<<blocks_for( count ), BLOCK, 0, s>>>( *w, w->bodyOps, count );
+	return check( cudaGetLastError() );
+}
+
 /* Prepare .. store impulses on the world's stream (no body finalisation).  Returns the
  * number of kernels launched. */
 extern "C" int b2gd_contact_solver( b2gDevWorld* w, const b2gSolvePlan* plan, const b2gStepConst* scp )
@@ -285,6 +305,7 @@ extern "C" int b2gd_solve( b2gDevWorld* w, b2gHostIO* io, const b2gSolvePlan* pl
 	if ( w->timing )
 		cudaEventRecord( (cudaEvent_t)w->timers[3], s );
 	cudaMemsetAsync( w->counters + 1, 0, sizeof( int ), s );
+	cudaMemsetAsync( w->counters + 3, 0, sizeof( int ), s );
 	int fused = w->fused ? b2gd_solver_fused( w, plan, scp ) : 0;
 	if ( fused < 0 )
 		return check( cudaGetLastError() );
@@ -320,6 +341,7 @@ extern "C" int b2gd_solve_speculative( b2gDevWorld* w, b2gHostIO* io, const b2gS
 	if ( w->timing )
 		cudaEventRecord( (cudaEvent_t)w->timers[3], s );
 	cudaMemsetAsync( w->counters + 1, 0, sizeof( int ), s );
+	cudaMemsetAsync( w->counters + 3, 0, sizeof( int ), s );
 	int fused = b2gd_solver_fused( w, plan, scp );
 	if ( fused <= 0 )
 	{

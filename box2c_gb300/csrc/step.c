@@ -179,7 +179,9 @@ static b2gContactInit* push_pending( gWorld* w )
 }
 
 /* Keeps only the last staged record of each contact id (ids can be freed and reused
- * between two steps), so the device can apply them in parallel. */
+ * between two steps), so the device can apply them in parallel.  A set record (the
+ * contact moved into or out of the awake set) that follows a creation or another set
+ * record of the same contact folds into it. */
 static int compact_pending( gWorld* w )
 {
 	int n = w->pendingCount;
@@ -196,7 +198,20 @@ static int compact_pending( gWorld* w )
 		w->scratchCap = ids;
 	}
 	for ( int i = 0; i < n; ++i )
-		w->scratch[w->pending[i].id] = i;
+		w->scratch[w->pending[i].id] = B2G_NULL;
+	for ( int i = 0; i < n; ++i )
+	{
+		b2gContactInit* r = w->pending + i;
+		int last = w->scratch[r->id];
+		if ( ( r->flags & B2G_INIT_SET ) && last != B2G_NULL && ( w->pending[last].flags & B2G_INIT_KILL ) == 0 )
+		{
+			b2gContactInit* base = w->pending + last;
+			base->flags = ( base->flags & ~B2G_INIT_ASLEEP ) | ( r->flags & B2G_INIT_ASLEEP );
+			r->flags = B2G_INIT_KILL | B2G_INIT_SET; /* folded: dropped below */
+			continue;
+		}
+		w->scratch[r->id] = i;
+	}
 	int m = 0;
 	for ( int i = 0; i < n; ++i )
 		if ( w->scratch[w->pending[i].id] == i )
@@ -249,8 +264,16 @@ void gcontact_create( gWorld* w, gShape* shapeA, gShape* shapeB )
 	gContact* c = w->contacts + id;
 	memset( c, 0, sizeof( *c ) );
 	c->id = id;
+	/* non-touching contacts of two bodies that are not awake live in the disabled set
+	 * (reference src/contact.c:210-222) */
+	int setIndex = bodyA->setIndex == G_SET_AWAKE || bodyB->setIndex == G_SET_AWAKE ? G_SET_AWAKE : G_SET_DISABLED;
+	gIntArray* list = gsolver_set_contacts( w, setIndex );
+	c->setIndex = setIndex;
 	c->colorIndex = B2G_NULL;
-	c->localIndex = w->nonTouching.count;
+	c->localIndex = list->count;
+	c->islandId = B2G_NULL;
+	c->islandPrev = B2G_NULL;
+	c->islandNext = B2G_NULL;
 	c->shapeIdA = shapeA->id;
 	c->shapeIdB = shapeB->id;
 	if ( shapeA->isSensor || shapeB->isSensor )
@@ -282,7 +305,7 @@ void gcontact_create( gWorld* w, gShape* shapeA, gShape* shapeB )
 
 	gset_add( &w->pairSet, PAIR_KEY( (uint64_t)shapeA->id, (uint64_t)shapeB->id ) );
 	w->pairSetVersion += 1;
-	gia_push( &w->nonTouching, id );
+	gia_push( list, id );
 
 	b2gContactInit* init = push_pending( w );
 	init->id = id;
@@ -290,7 +313,15 @@ void gcontact_create( gWorld* w, gShape* shapeA, gShape* shapeB )
 	init->shapeB = shapeB->id;
 	init->friction = c->friction;
 	init->restitution = c->restitution;
-	init->flags = 0;
+	init->flags = setIndex == G_SET_AWAKE ? 0u : B2G_INIT_ASLEEP;
+}
+
+void gcontact_stage_set( gWorld* w, int contactId, bool asleep )
+{
+	b2gContactInit* r = push_pending( w );
+	memset( r, 0, sizeof( *r ) );
+	r->id = contactId;
+	r->flags = B2G_INIT_SET | ( asleep ? B2G_INIT_ASLEEP : 0u );
 }
 
 static void remove_non_touching( gWorld* w, int localIndex )
@@ -300,7 +331,7 @@ static void remove_non_touching( gWorld* w, int localIndex )
 		w->contacts[w->nonTouching.data[localIndex]].localIndex = localIndex;
 }
 
-static void remove_from_graph( gWorld* w, int bodyIdA, int bodyIdB, int colorIndex, int localIndex )
+void gcontact_remove_from_graph( gWorld* w, int bodyIdA, int bodyIdB, int colorIndex, int localIndex )
 {
 	gColor* color = w->colors + colorIndex;
 	if ( colorIndex != B2G_OVERFLOW )
@@ -328,23 +359,38 @@ static void unlink_edge( gWorld* w, gContact* c, int e )
 	body->contactCount -= 1;
 }
 
-/* Reference src/contact.c:342-447.  The device record is retired by the narrowphase
+/* Reference src/contact.c:320-449.  The device record is retired by the narrowphase
  * (disjoint) or ignored once its id is free. */
-void gcontact_destroy( gWorld* w, gContact* c )
+void gcontact_destroy( gWorld* w, gContact* c, bool wakeBodies )
 {
 	gset_remove( &w->pairSet, PAIR_KEY( (uint64_t)c->shapeIdA, (uint64_t)c->shapeIdB ) );
 	w->pairSetVersion += 1;
+	int bodyIdA = c->edges[0].bodyId;
+	int bodyIdB = c->edges[1].bodyId;
 	unlink_edge( w, c, 0 );
 	unlink_edge( w, c, 1 );
+	if ( c->islandId != B2G_NULL )
+		gisland_unlink_contact( w, c );
 	if ( c->colorIndex != B2G_NULL )
-		remove_from_graph( w, c->edges[0].bodyId, c->edges[1].bodyId, c->colorIndex, c->localIndex );
+		gcontact_remove_from_graph( w, bodyIdA, bodyIdB, c->colorIndex, c->localIndex );
 	else
-		remove_non_touching( w, c->localIndex );
+	{
+		gIntArray* list = gsolver_set_contacts( w, c->setIndex );
+		int moved = gia_remove_swap( list, c->localIndex );
+		if ( moved != B2G_NULL )
+			w->contacts[list->data[c->localIndex]].localIndex = c->localIndex;
+	}
 	int id = c->id;
 	c->id = B2G_NULL;
+	c->setIndex = B2G_NULL;
 	c->colorIndex = B2G_NULL;
 	c->localIndex = B2G_NULL;
 	gid_free( &w->contactIds, id );
+	if ( wakeBodies )
+	{
+		gbody_wake( w, w->bodies + bodyIdA );
+		gbody_wake( w, w->bodies + bodyIdB );
+	}
 	/* retire the device record before the next narrowphase */
 	b2gContactInit* kill = push_pending( w );
 	memset( kill, 0, sizeof( *kill ) );
@@ -353,7 +399,7 @@ void gcontact_destroy( gWorld* w, gContact* c )
 }
 
 /* Greedy first-fit colouring keyed by body id (reference src/constraint_graph.c:64-183). */
-static void add_to_graph( gWorld* w, gContact* c )
+void gcontact_add_to_graph( gWorld* w, gContact* c )
 {
 	int colorIndex = B2G_OVERFLOW;
 	int a = c->edges[0].bodyId;
@@ -657,7 +703,7 @@ static void process_events( gWorld* w, int count )
 			if ( ( flags & G_TOUCHING ) && ( flags & G_ENABLE_CONTACT_EVENTS ) )
 				push_end( w, c->shapeIdA, c->shapeIdB );
 			c->flags &= ~G_TOUCHING;
-			gcontact_destroy( w, c );
+			gcontact_destroy( w, c, false );
 		}
 		else if ( code == B2G_EV_STARTED )
 		{
@@ -669,9 +715,12 @@ static void process_events( gWorld* w, int count )
 			}
 			if ( flags & G_ENABLE_CONTACT_EVENTS )
 				push_begin( w, c->shapeIdA, c->shapeIdB );
+			/* link first: it may wake a sleeping set, which appends to the awake lists
+			 * and leaves this contact's place unchanged */
 			c->flags |= G_TOUCHING;
+			gisland_link_contact( w, c );
 			int localIndex = c->localIndex;
-			add_to_graph( w, c );
+			gcontact_add_to_graph( w, c );
 			remove_non_touching( w, localIndex );
 		}
 		else if ( code == B2G_EV_STOPPED )
@@ -685,12 +734,14 @@ static void process_events( gWorld* w, int count )
 			c->flags &= ~G_TOUCHING;
 			if ( c->flags & G_ENABLE_CONTACT_EVENTS )
 				push_end( w, c->shapeIdA, c->shapeIdB );
+			gisland_unlink_contact( w, c );
 			int a = c->edges[0].bodyId, b = c->edges[1].bodyId;
 			int colorIndex = c->colorIndex, localIndex = c->localIndex;
+			c->setIndex = G_SET_AWAKE;
 			c->colorIndex = B2G_NULL;
 			c->localIndex = w->nonTouching.count;
 			gia_push( &w->nonTouching, id );
-			remove_from_graph( w, a, b, colorIndex, localIndex );
+			gcontact_remove_from_graph( w, a, b, colorIndex, localIndex );
 		}
 	}
 }
@@ -1179,6 +1230,24 @@ int gstep_after_collide( gWorld* w, float dt, int subSteps, b2gStepConst* sc, b2
 	if ( dt <= 0.0f )
 		return 0;
 
+	/* islands joined since the last step merge at the start of the solve; the previous
+	 * step's split candidate splits before the bodies are finalised (reference
+	 * src/solver.c:1114, :1395-1410, :1614-1620) */
+	gislands_merge_awake( w );
+	if ( w->awake.count > 0 )
+	{
+		if ( w->splitIslandId != B2G_NULL )
+			gisland_split( w, w->splitIslandId );
+		w->splitIslandId = B2G_NULL;
+	}
+	/* bodies woken by this step's events join the solve */
+	int fe = gbody_flush_ops( w );
+	if ( fe )
+	{
+		w->status = fe;
+		return 0;
+	}
+
 	step_constants( w, dt, subSteps, sc );
 
 	if ( w->awake.count == 0 )
@@ -1224,6 +1293,8 @@ void gstep_finish( gWorld* w )
 	for ( int i = 0; i < ( recordCount < w->dev.recordCap ? recordCount : w->dev.recordCap ); ++i )
 		w->dev.d2hBytes += ( w->io.records[i].flags & B2G_R_FAST ) ? 80 : 48;
 	process_records( w, recordCount < w->dev.recordCap ? recordCount : w->dev.recordCap );
+	/* island sleep comes last: it moves bodies out of the awake set */
+	gislands_sleep_step( w );
 	w->profile.broadphase = (float)( b2g_now_ms() - t3 );
 	w->profile.continuous = w->hostMs[7];
 	w->hostMs[6] = (float)( b2g_now_ms() - tr ) - w->hostMs[7];

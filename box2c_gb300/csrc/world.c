@@ -211,6 +211,14 @@ bool gworld_reserve_mirrors( gWorld* w )
 /* Refreshes the host body mirror from the device after a step. */
 void gworld_ensure_mirror( gWorld* w )
 {
+	/* staged body operations reach the device before anything reads or writes a body
+	 * there */
+	if ( w->bodyOps.count > 0 )
+	{
+		int e = gbody_flush_ops( w );
+		if ( e )
+			w->status = e;
+	}
 	if ( w->mirrorStale == false )
 		return;
 	int n = w->bodyIds.next;
@@ -261,6 +269,9 @@ void gworld_flush( gWorld* w )
 {
 	int nb = w->bodyIds.next, ns = w->shapeIds.next, nj = w->jointIds.next;
 	int e = b2gd_reserve( &w->dev, &w->io, nb, ns, w->contactIds.next, nj, w->contactIds.next, ns );
+	/* body operations first: the full upload below carries a mirror that already
+	 * reflects them */
+	e |= gbody_flush_ops( w );
 	if ( w->bodiesDirty )
 	{
 		e |= b2gd_upload_bodies( &w->dev, w->hState, w->hXf, w->hCenters, w->hPrev, w->hMass, w->hForce, w->hExtent, w->hInfo, nb );
@@ -378,6 +389,7 @@ b2WorldId b2CreateWorld( const b2WorldDef* def )
 	w->enableSleep = def->enableSleep;
 	w->enableWarmStarting = true;
 	w->enableContinuous = def->enableContinous;
+	gislands_init( w );
 	b2WorldId id = { (uint16_t)( slot + 1 ), w->revision };
 	if ( b2g_alloc_failures() != failures )
 	{
@@ -416,6 +428,7 @@ void b2DestroyWorld( b2WorldId worldId )
 	gia_free( &w->jointIds.freeIds );
 	gia_free( &w->awake );
 	gia_free( &w->nonTouching );
+	gislands_free( w );
 	gia_free( &w->moveArray );
 	gia_free( &w->solveList );
 	gia_free( &w->jointList );
@@ -456,7 +469,20 @@ bool b2World_IsValid( b2WorldId id )
 	return w && w->inUse && w->revision == id.revision;
 }
 
-void b2World_EnableSleeping( b2WorldId id, bool flag ) { gworld_get( id )->enableSleep = flag; }
+/* Turning sleep off wakes every sleeping set (reference src/world.c:1568-1594). */
+void b2World_EnableSleeping( b2WorldId id, bool flag )
+{
+	gWorld* w = gworld_get( id );
+	if ( w->locked || flag == w->enableSleep )
+		return;
+	w->enableSleep = flag;
+	if ( flag == false )
+	{
+		for ( int i = G_SET_FIRST_SLEEPING; i < w->setCap; ++i )
+			if ( w->sets[i].setIndex != B2G_NULL && w->sets[i].bodies.count > 0 )
+				gsolver_set_wake( w, i );
+	}
+}
 void b2World_EnableContinuous( b2WorldId id, bool flag ) { gworld_get( id )->enableContinuous = flag; }
 void b2World_EnableWarmStarting( b2WorldId id, bool flag ) { gworld_get( id )->enableWarmStarting = flag; }
 void b2World_SetRestitutionThreshold( b2WorldId id, float v ) { gworld_get( id )->restitutionThreshold = v; }
@@ -512,6 +538,7 @@ b2Counters b2World_GetCounters( b2WorldId id )
 	c.shapeCount = gid_count( &w->shapeIds );
 	c.contactCount = gid_count( &w->contactIds );
 	c.jointCount = gid_count( &w->jointIds );
+	c.islandCount = gid_count( &w->islandIds );
 	c.staticTreeHeight = gtree_height( w->trees + b2_staticBody );
 	int hd = gtree_height( w->trees + b2_dynamicBody );
 	int hk = gtree_height( w->trees + b2_kinematicBody );
@@ -612,13 +639,22 @@ b2BodyId b2CreateBody( b2WorldId worldId, const b2BodyDef* def )
 	ex[1] = def->angularDamping;
 	ex[2] = B2G_HUGE;
 	ex[3] = 0.0f;
+	/* solver set (reference src/body.c:196-228): static, awake, or a sleeping set of its
+	 * own; only an awake body keeps the definition's velocity */
 	int info = (int)def->type;
+	b->awakeIndex = B2G_NULL;
+	b->setLocal = B2G_NULL;
+	b->islandId = B2G_NULL;
+	b->islandPrev = B2G_NULL;
+	b->islandNext = B2G_NULL;
+	bool isAwake = def->isAwake || def->enableSleep == false;
 	if ( def->type == b2_staticBody )
 	{
-		b->awakeIndex = B2G_NULL;
+		b->setIndex = G_SET_STATIC;
 	}
-	else
+	else if ( isAwake )
 	{
+		b->setIndex = G_SET_AWAKE;
 		b->awakeIndex = w->awake.count;
 		gia_push( &w->awake, id );
 		w->awakeDirty = true;
@@ -627,6 +663,22 @@ b2BodyId b2CreateBody( b2WorldId worldId, const b2BodyDef* def )
 		st[1] = def->linearVelocity.y;
 		st[2] = def->angularVelocity;
 	}
+	else
+	{
+		int setId = gsolver_set_create( w );
+		if ( setId == B2G_NULL )
+		{
+			gid_unalloc( &w->bodyIds, id );
+			b->id = B2G_NULL;
+			w->status = w->status ? w->status : B2_STATUS_OUT_OF_HOST_MEMORY;
+			return b2_nullBodyId;
+		}
+		b->setIndex = setId;
+		b->setLocal = w->sets[setId].bodies.count;
+		gia_push( &w->sets[setId].bodies, id );
+	}
+	if ( b->setIndex >= G_SET_AWAKE )
+		gisland_create_for_body( w, b->setIndex, b );
 	/* the spare lane of the velocity float4 carries the sleep threshold */
 	st[3] = def->sleepThreshold;
 	if ( def->isBullet )
@@ -635,6 +687,10 @@ b2BodyId b2CreateBody( b2WorldId worldId, const b2BodyDef* def )
 		info |= B2G_B_SLEEP_OK;
 	w->hInfo[id] = info;
 	w->bodiesDirty = true;
+	/* a new body's sleep timer starts at zero; the upload that follows the operation
+	 * restores the definition's velocity */
+	if ( b->setIndex != G_SET_STATIC )
+		gbody_stage_new( w, id, b->setIndex == G_SET_AWAKE ? B2G_BODY_WAKE : B2G_BODY_SLEEP );
 	b2BodyId bid = { id + 1, (uint16_t)w->slot, b->revision };
 	return bid;
 }
@@ -667,9 +723,13 @@ b2Rot b2Body_GetRotation( b2BodyId id ) { return b2Body_GetTransform( id ).q; }
 b2Vec2 b2Body_GetLocalPoint( b2BodyId id, b2Vec2 p ) { return b2InvTransformPoint( b2Body_GetTransform( id ), p ); }
 b2Vec2 b2Body_GetWorldPoint( b2BodyId id, b2Vec2 p ) { return b2TransformPoint( b2Body_GetTransform( id ), p ); }
 
+/* Velocities live in the awake set only (reference src/body.c:729-787): a body that is
+ * not awake reports zero, and a non-zero velocity wakes it first. */
 b2Vec2 b2Body_GetLinearVelocity( b2BodyId id )
 {
 	gWorld* w = body_world( id );
+	if ( get_body( id )->setIndex != G_SET_AWAKE )
+		return b2Vec2_zero;
 	gworld_ensure_mirror( w );
 	const float* s = w->hState + 8 * ( id.index1 - 1 );
 	b2Vec2 v = { s[0], s[1] };
@@ -679,6 +739,8 @@ b2Vec2 b2Body_GetLinearVelocity( b2BodyId id )
 float b2Body_GetAngularVelocity( b2BodyId id )
 {
 	gWorld* w = body_world( id );
+	if ( get_body( id )->setIndex != G_SET_AWAKE )
+		return 0.0f;
 	gworld_ensure_mirror( w );
 	return w->hState[8 * ( id.index1 - 1 ) + 2];
 }
@@ -687,7 +749,10 @@ static void set_velocity( b2BodyId id, const float* v, int mask )
 {
 	gWorld* w = body_world( id );
 	gBody* b = get_body( id );
-	if ( b->type == b2_staticBody )
+	bool moving = ( mask & 1 ) ? v[0] * v[0] + v[1] * v[1] > 0.0f : v[2] != 0.0f;
+	if ( moving )
+		gbody_wake( w, b );
+	if ( b->setIndex != G_SET_AWAKE )
 		return;
 	gworld_ensure_mirror( w );
 	float* s = w->hState + 8 * b->id;
@@ -713,6 +778,57 @@ void b2Body_SetAngularVelocity( b2BodyId id, float a )
 {
 	float t[3] = { 0.0f, 0.0f, a };
 	set_velocity( id, t, 2 );
+}
+
+/* Sleep (reference src/body.c:1358-1433). */
+bool b2Body_IsAwake( b2BodyId id ) { return get_body( id )->setIndex == G_SET_AWAKE; }
+
+void b2Body_SetAwake( b2BodyId id, bool awake )
+{
+	gWorld* w = body_world( id );
+	if ( w->locked )
+		return;
+	gBody* b = get_body( id );
+	if ( awake && b->setIndex >= G_SET_FIRST_SLEEPING )
+		gbody_wake( w, b );
+	else if ( awake == false && b->setIndex == G_SET_AWAKE )
+	{
+		if ( w->islands[b->islandId].constraintRemoveCount > 0 )
+			gisland_split( w, b->islandId );
+		gisland_try_sleep( w, b->islandId );
+	}
+}
+
+bool b2Body_IsSleepEnabled( b2BodyId id ) { return get_body( id )->enableSleep; }
+
+void b2Body_SetSleepThreshold( b2BodyId id, float sleepVelocity )
+{
+	gWorld* w = body_world( id );
+	gBody* b = get_body( id );
+	b->sleepThreshold = sleepVelocity;
+	/* the threshold rides in the velocity record's spare lane */
+	gworld_ensure_mirror( w );
+	w->hState[8 * b->id + 3] = sleepVelocity;
+	w->bodiesDirty = true;
+}
+
+float b2Body_GetSleepThreshold( b2BodyId id ) { return get_body( id )->sleepThreshold; }
+
+void b2Body_EnableSleep( b2BodyId id, bool enableSleep )
+{
+	gWorld* w = body_world( id );
+	if ( w->locked )
+		return;
+	gBody* b = get_body( id );
+	b->enableSleep = enableSleep;
+	if ( enableSleep )
+		w->hInfo[b->id] |= B2G_B_SLEEP_OK;
+	else
+		w->hInfo[b->id] &= ~B2G_B_SLEEP_OK;
+	gworld_ensure_mirror( w );
+	w->bodiesDirty = true;
+	if ( enableSleep == false )
+		gbody_wake( w, b );
 }
 
 float b2Body_GetMass( b2BodyId id ) { return body_world( id )->hMass[4 * ( id.index1 - 1 )]; }
@@ -1231,21 +1347,44 @@ b2gJointDev* gjoint_create( b2WorldId worldId, b2BodyId bodyIdA, b2BodyId bodyId
 	b->headJointKey = keyB;
 	b->jointCount += 1;
 
-	bool staticA = a->type == b2_staticBody;
-	bool staticB = b->type == b2_staticBody;
-	if ( staticA && staticB )
+	j->islandId = B2G_NULL;
+	j->islandPrev = B2G_NULL;
+	j->islandNext = B2G_NULL;
+	j->colorIndex = B2G_NULL;
+
+	/* solver set (reference src/joint.c:198-283): between static bodies the static set;
+	 * touching the awake set the constraint graph, after waking a sleeping partner;
+	 * otherwise the sleeping set, merging two sleeping sets */
+	int maxSetIndex = a->setIndex > b->setIndex ? a->setIndex : b->setIndex;
+	if ( a->setIndex == G_SET_STATIC && b->setIndex == G_SET_STATIC )
 	{
-		j->colorIndex = B2G_NULL;
-		j->localIndex = B2G_NULL;
+		j->setIndex = G_SET_STATIC;
+		j->localIndex = w->staticJoints.count;
+		gia_push( &w->staticJoints, id );
 	}
-	else
+	else if ( a->setIndex == G_SET_AWAKE || b->setIndex == G_SET_AWAKE )
 	{
+		if ( maxSetIndex >= G_SET_FIRST_SLEEPING )
+			gsolver_set_wake( w, maxSetIndex );
+		j->setIndex = G_SET_AWAKE;
+		bool staticA = a->setIndex == G_SET_STATIC;
+		bool staticB = b->setIndex == G_SET_STATIC;
 		int color = gassign_joint_color( w, a->id, b->id, staticA, staticB );
 		j->colorIndex = color;
 		j->localIndex = w->colors[color].joints.count;
 		gia_push( &w->colors[color].joints, id );
 		w->solveDirty = true;
 	}
+	else
+	{
+		j->setIndex = maxSetIndex;
+		j->localIndex = w->sets[maxSetIndex].joints.count;
+		gia_push( &w->sets[maxSetIndex].joints, id );
+		if ( a->setIndex != b->setIndex && a->setIndex >= G_SET_FIRST_SLEEPING && b->setIndex >= G_SET_FIRST_SLEEPING )
+			gsolver_set_merge( w, a->setIndex, b->setIndex );
+	}
+	if ( j->setIndex > G_SET_DISABLED )
+		gisland_link_joint( w, j );
 
 	b2gJointDev* d = w->hJoints + id;
 	memset( d, 0, sizeof( *d ) );
@@ -1283,7 +1422,7 @@ void gjoint_disconnect_bodies( gWorld* w, int bodyIdA, int bodyIdB )
 		int e = key & 1;
 		key = c->edges[e].nextKey;
 		if ( c->edges[e ^ 1].bodyId == other )
-			gcontact_destroy( w, c );
+			gcontact_destroy( w, c, false );
 	}
 }
 
@@ -1318,7 +1457,8 @@ int b2World_InspectBodies( b2WorldId worldId, float* out, int capacity )
 		}
 		const float* x = w->hXf + 4 * i;
 		const float* s = w->hState + 8 * i;
-		bool moving = w->bodies[i].type != b2_staticBody;
+		/* velocities live in the awake set only */
+		bool moving = w->bodies[i].setIndex == G_SET_AWAKE;
 		o[0] = x[0];
 		o[1] = x[1];
 		o[2] = x[2];
@@ -1327,6 +1467,19 @@ int b2World_InspectBodies( b2WorldId worldId, float* out, int capacity )
 		o[5] = moving ? s[1] : 0.0f;
 		o[6] = moving ? s[2] : 0.0f;
 		o[7] = (float)w->bodies[i].type;
+	}
+	return count;
+}
+
+int b2World_InspectIslands( b2WorldId worldId, int* out, int capacity )
+{
+	gWorld* w = gworld_get( worldId );
+	int count = w->bodyIds.next;
+	for ( int i = 0; i < count && i < capacity; ++i )
+	{
+		const gBody* b = w->bodies + i;
+		out[2 * i] = b->id == i ? b->setIndex : -1;
+		out[2 * i + 1] = b->id == i ? b->islandId : -1;
 	}
 	return count;
 }
@@ -1536,11 +1689,22 @@ static void unlink_joint_edge( gWorld* w, gJoint* j, int e )
 	body->jointCount -= 1;
 }
 
-static void destroy_joint( gWorld* w, gJoint* j )
+/* Reference src/joint.c:657-752. */
+static void destroy_joint( gWorld* w, gJoint* j, bool wakeBodies )
 {
+	int bodyIdA = j->edges[0].bodyId;
+	int bodyIdB = j->edges[1].bodyId;
 	unlink_joint_edge( w, j, 0 );
 	unlink_joint_edge( w, j, 1 );
-	if ( j->colorIndex != B2G_NULL )
+	gisland_unlink_joint( w, j );
+	if ( j->setIndex != G_SET_AWAKE )
+	{
+		gIntArray* list = gsolver_set_joints( w, j->setIndex );
+		int moved = gia_remove_swap( list, j->localIndex );
+		if ( moved != B2G_NULL )
+			w->joints[list->data[j->localIndex]].localIndex = j->localIndex;
+	}
+	else
 	{
 		/* swap-remove from the colour: the overflow colour is solved in array order */
 		gColor* color = w->colors + j->colorIndex;
@@ -1555,10 +1719,16 @@ static void destroy_joint( gWorld* w, gJoint* j )
 		w->solveDirty = true;
 	}
 	int id = j->id;
+	j->setIndex = B2G_NULL;
 	j->colorIndex = B2G_NULL;
 	j->localIndex = B2G_NULL;
 	j->id = B2G_NULL;
 	gid_free( &w->jointIds, id );
+	if ( wakeBodies )
+	{
+		gbody_wake( w, w->bodies + bodyIdA );
+		gbody_wake( w, w->bodies + bodyIdB );
+	}
 }
 
 void b2DestroyJoint( b2JointId jointId )
@@ -1568,12 +1738,12 @@ void b2DestroyJoint( b2JointId jointId )
 	gWorld* w = s_worlds[jointId.world0];
 	if ( w->locked )
 		return;
-	destroy_joint( w, get_joint( jointId ) );
+	destroy_joint( w, get_joint( jointId ), true );
 }
 
 /* Unlinks and frees a shape with its proxy and contacts (reference
  * src/shape.c:220-269). */
-static void destroy_shape_internal( gWorld* w, gShape* s, gBody* b )
+static void destroy_shape_internal( gWorld* w, gShape* s, gBody* b, bool wakeBodies )
 {
 	int id = s->id;
 	if ( s->prev != B2G_NULL )
@@ -1590,7 +1760,7 @@ static void destroy_shape_internal( gWorld* w, gShape* s, gBody* b )
 		gContact* c = w->contacts + ( key >> 1 );
 		key = c->edges[key & 1].nextKey;
 		if ( c->shapeIdA == id || c->shapeIdB == id )
-			gcontact_destroy( w, c );
+			gcontact_destroy( w, c, wakeBodies );
 	}
 	gid_free( &w->shapeIds, id );
 	s->id = B2G_NULL;
@@ -1610,7 +1780,7 @@ void b2DestroyShape( b2ShapeId shapeId )
 	gworld_ensure_shape_mirror( w );
 	gShape* s = get_shape( shapeId );
 	gBody* b = w->bodies + s->bodyId;
-	destroy_shape_internal( w, s, b );
+	destroy_shape_internal( w, s, b, true );
 	if ( b->automaticMass )
 		gbody_update_mass( w, b );
 	w->bodiesDirty = true;
@@ -1734,7 +1904,7 @@ void b2DestroyChain( b2ChainId chainId )
 	{
 		int sid = chain->shapeIndices[i];
 		if ( sid >= 0 && w->shapes[sid].id == sid )
-			destroy_shape_internal( w, w->shapes + sid, body );
+			destroy_shape_internal( w, w->shapes + sid, body, true );
 	}
 	b2g_free( chain->shapeIndices );
 	chain->shapeIndices = NULL;
@@ -1783,19 +1953,20 @@ void b2DestroyBody( b2BodyId bodyId )
 		return;
 	gworld_ensure_mirror( w );
 	gBody* b = get_body( bodyId );
+	/* bodies attached through joints and contacts wake, even when this one is static */
 	int key = b->headJointKey;
 	while ( key != B2G_NULL )
 	{
 		gJoint* j = w->joints + ( key >> 1 );
 		key = j->edges[key & 1].nextKey;
-		destroy_joint( w, j );
+		destroy_joint( w, j, true );
 	}
 	key = b->headContactKey;
 	while ( key != B2G_NULL )
 	{
 		gContact* c = w->contacts + ( key >> 1 );
 		key = c->edges[key & 1].nextKey;
-		gcontact_destroy( w, c );
+		gcontact_destroy( w, c, true );
 	}
 	for ( int sid = b->headShape; sid != B2G_NULL; )
 	{
@@ -1817,17 +1988,12 @@ void b2DestroyBody( b2BodyId bodyId )
 		chain->id = B2G_NULL;
 		cid = chain->nextChainId;
 	}
-	/* the awake set drops the body by moving its last body into the slot */
-	if ( b->awakeIndex != B2G_NULL )
-	{
-		int at = b->awakeIndex;
-		int moved = gia_remove_swap( &w->awake, at );
-		if ( moved != B2G_NULL )
-			w->bodies[w->awake.data[at]].awakeIndex = at;
-		w->awakeDirty = true;
-	}
+	/* the body's set drops it by moving its last body into the slot */
+	gisland_remove_body( w, b );
+	gbody_remove_from_set( w, b );
 	w->hInfo[b->id] = 0;
 	gid_free( &w->bodyIds, b->id );
+	b->setIndex = B2G_NULL;
 	b->awakeIndex = B2G_NULL;
 	b->id = B2G_NULL;
 	w->bodiesDirty = true;

@@ -397,6 +397,7 @@ b2Counters b2World_GetCounters( b2WorldId id )
 	c.shapeCount = oid_count( &w->shapeIds );
 	c.contactCount = oid_count( &w->contactIds );
 	c.jointCount = oid_count( &w->jointIds );
+	c.islandCount = oid_count( &w->islandIds );
 	c.staticTreeHeight = otree_height( w->trees + b2_staticBody );
 	int hd = otree_height( w->trees + b2_dynamicBody );
 	int hk = otree_height( w->trees + b2_kinematicBody );

@@ -5,10 +5,9 @@ Run in a container that has the reference sources (it builds oracle/_ref first):
     python tests/golden/make_golden.py
 
 Fixtures (all produced by the unmodified reference library, oracle/_ref/libb2ref.so):
-  scenes.npz     per-step hashes of body state bits and of the contact table
-                 (contact id, shape pair, colour, touching, point count) plus full body
-                 snapshots, for the small pyramid, the tumbler, the tilted stacks and
-                 hello-world scenes;
+  scenes.npz     per-step hashes of body state bits, of the contact table (contact id,
+                 shape pair, colour, touching, point count) and of every body's solver
+                 set and island id, plus full body snapshots, for the scenes of SCENES;
   manifolds.npz  seeded random shape pairs and the reference manifolds for them;
   smooth_manifolds.npz  seeded chain links against every shape type: the reference's
                  manifolds and closest-feature caches from an empty and a warmed cache.
@@ -37,9 +36,8 @@ SCENES = {
     "pyramid20": (300, (1, 10, 60, 150, 300)),
     "tumbler2000": (200, (1, 50, 100, 200)),
     "tilted": (100, (1, 50, 100)),
-    # default world def has sleep on; the reference island falls asleep at step 88,
-    # and the library has no islands or sleep, so the fixture stops at step 87
-    "hello": (87, (87,)),
+    # default world def has sleep on: the body's island falls asleep at step 88
+    "hello": (200, (87, 88, 200)),
     "pyramid100": (40, (40,)),
     # reference benchmark/joint_grid.c with gravity, at 30 x 30 and at the benchmark's
     # 100 x 100 (19800 revolute joints in the graph colours)
@@ -64,7 +62,13 @@ SCENES = {
     "joint_zoo_collide": (200, (1, 2, 10, 100, 200)),
     # chains: smooth segments (terrain and a closed bowl) against every shape type, bullets
     "chain_scene": (300, (1, 10, 60, 150, 300)),
+    # islands and sleep: piles and a chain fall asleep, sets merge through a joint, and
+    # destruction, contact, velocity and the sleep switches wake them (scripted steps)
+    "sleep_scene": (360, (1, 60, 120, 200, 300, 360)),
 }
+
+# scenes edited between steps: backend method called with (world, step number)
+STEPPERS = {"sleep_scene": "sleep_step"}
 
 
 def make_scene(b: Backend, name: str):
@@ -102,7 +106,16 @@ def make_scene(b: Backend, name: str):
         return b.joint_zoo(3, 1, 1251)
     if name == "chain_scene":
         return b.chain_scene(200, 1260)
+    if name == "sleep_scene":
+        return b.sleep_scene()
     raise KeyError(name)
+
+
+def step_scene(b: Backend, name: str, w, s: int) -> None:
+    """Advances scene `name` from step s-1 to step s (the step, then its scripted edits)."""
+    b.step(w)
+    if name in STEPPERS:
+        getattr(b, STEPPERS[name])(w, s)
 
 
 def digest(arr: np.ndarray) -> np.uint64:
@@ -113,18 +126,19 @@ def digest(arr: np.ndarray) -> np.uint64:
 def record(b: Backend, name: str):
     steps, snaps = SCENES[name]
     w = make_scene(b, name)
-    body_h, contact_h, snap = [], [], {}
+    body_h, contact_h, island_h, snap = [], [], [], {}
     for s in range(steps + 1):
         bodies = b.bodies(w)
         table = contact_table(b.contacts(w))
         body_h.append(digest(bodies.view(np.uint32)))
         contact_h.append(digest(table))
+        island_h.append(digest(b.islands(w)))
         if s in snaps:
             snap[s] = bodies.copy()
         if s < steps:
-            b.step(w)
+            step_scene(b, name, w, s + 1)
     b.destroy(w)
-    return np.array(body_h, np.uint64), np.array(contact_h, np.uint64), snap
+    return np.array(body_h, np.uint64), np.array(contact_h, np.uint64), np.array(island_h, np.uint64), snap
 
 
 def main():
@@ -132,9 +146,10 @@ def main():
     ref = Backend(os.path.join(REPO, "oracle/_ref/libb2ref.so"), os.path.join(REPO, "oracle/_ref/libb2ref_scenes.so"), "ref")
     out = {}
     for name in SCENES:
-        bh, ch, snap = record(ref, name)
+        bh, ch, ih, snap = record(ref, name)
         out[f"{name}/body_hash"] = bh
         out[f"{name}/contact_hash"] = ch
+        out[f"{name}/island_hash"] = ih
         for s, arr in snap.items():
             out[f"{name}/bodies_{s}"] = arr
     np.savez_compressed(os.path.join(HERE, "scenes.npz"), **out)

@@ -9,10 +9,12 @@ def state_bits(backend, world):
     return b, b.view(np.uint32)
 
 
-def lockstep(a, b, make, steps, dt=1.0 / 60.0, substeps=4, check_manifolds=False, after_step=None):
+def lockstep(a, b, make, steps, dt=1.0 / 60.0, substeps=4, check_manifolds=False, after_step=None,
+             check_islands=False):
     """Steps both backends; returns (first mismatching step or None, detail, worst rel err).
     after_step(backend, world, step), when given, runs on both after each step (world
-    edits such as destruction)."""
+    edits such as destruction); check_islands compares every body's solver set and
+    island id."""
     wa, wb = make(a), make(b)
     worst = 0.0
     try:
@@ -22,6 +24,10 @@ def lockstep(a, b, make, steps, dt=1.0 / 60.0, substeps=4, check_manifolds=False
             ta, tb = contact_table(a.contacts(wa)), contact_table(b.contacts(wb))
             if ta.shape != tb.shape or not np.array_equal(ta, tb):
                 return s, "contact set / colours differ", worst
+            if check_islands:
+                ia, ib = a.islands(wa), b.islands(wb)
+                if ia.shape != ib.shape or not np.array_equal(ia, ib):
+                    return s, "solver sets / islands differ", worst
             if not np.array_equal(ua, ub):
                 m = np.isfinite(ba) & np.isfinite(bb)
                 rel = np.abs(ba[m] - bb[m]) / np.maximum(np.abs(bb[m]), 1.0)

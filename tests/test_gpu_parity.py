@@ -7,7 +7,7 @@ import numpy as np
 import pytest
 
 from box2c_gb300.capi import bind_gpu_api, contact_table
-from tests.golden.make_golden import SCENES, make_scene, digest
+from tests.golden.make_golden import SCENES, make_scene, digest, step_scene
 from tests.helpers import lockstep
 
 pytestmark = pytest.mark.gpu
@@ -16,15 +16,16 @@ GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
 
 @pytest.mark.parametrize("name", ["pyramid20", "tilted", "hello", "tumbler2000", "pyramid100", "joint_grid30",
                                   "joint_grid100", "many_pyramids5", "many_pyramids20", "shape_pile", "joint_hub",
-                                  "fast_shots", "chain_scene"])
+                                  "fast_shots", "chain_scene", "sleep_scene"])
 def test_gpu_matches_reference_golden(gpu, name):
     g = np.load(os.path.join(GOLDEN, "scenes.npz"))
     steps, snaps = SCENES[name]
-    bh, ch = g[f"{name}/body_hash"], g[f"{name}/contact_hash"]
+    bh, ch, ih = g[f"{name}/body_hash"], g[f"{name}/contact_hash"], g[f"{name}/island_hash"]
     w = make_scene(gpu, name)
     try:
         for s in range(steps + 1):
             assert digest(contact_table(gpu.contacts(w))) == ch[s], f"{name}: pairs/colours differ at step {s}"
+            assert digest(gpu.islands(w)) == ih[s], f"{name}: solver sets / islands differ at step {s}"
             bodies = gpu.bodies(w)
             if s in snaps:
                 ref = g[f"{name}/bodies_{s}"]
@@ -33,9 +34,20 @@ def test_gpu_matches_reference_golden(gpu, name):
                 assert rel <= 1e-5, f"{name}: step {s} max rel err {rel}"
             assert digest(bodies.view(np.uint32)) == bh[s], f"{name}: body state not bit-exact at step {s}"
             if s < steps:
-                gpu.step(w)
+                step_scene(gpu, name, w, s + 1)
     finally:
         gpu.destroy(w)
+
+
+def test_gpu_sleep_lockstep_oracle(gpu, oracle):
+    """Islands and sleep on the device path: sleeping bodies leave the awake list and the
+    integration, their contacts leave the narrowphase, a woken set rejoins the solve in
+    the step that woke it (contact begin, destruction, velocity, SetAwake, the sleep
+    switches) with the identity state.  Body states, manifolds, contact table, solver
+    sets and island ids equal the oracle's every step."""
+    step, detail, _ = lockstep(gpu, oracle, lambda b: b.sleep_scene(), 360, check_manifolds=True,
+                               after_step=lambda b, w, s: b.sleep_step(w, s), check_islands=True)
+    assert step is None, f"{detail} at step {step}"
 
 
 @pytest.mark.parametrize("scene,steps,sub", [

@@ -10,7 +10,7 @@ import numpy as np
 import pytest
 
 from box2c_gb300.capi import Vec2, Transform, Rot, contact_table
-from tests.golden.make_golden import SCENES, make_scene, digest
+from tests.golden.make_golden import SCENES, make_scene, digest, step_scene
 from tests.golden.shapes import Manifold, random_pairs, manifold_array
 from tests.helpers import lockstep, run_world_api_checks
 
@@ -72,23 +72,23 @@ def test_manifold_golden(oracle):
 
 @pytest.mark.parametrize("name", list(SCENES))
 def test_scene_golden(oracle, name):
-    """Per-step bit-exact body state and contact table against the reference's hashes."""
+    """Per-step bit-exact body state, contact table and solver sets / island ids against
+    the reference's hashes."""
     g = np.load(os.path.join(GOLDEN, "scenes.npz"))
     steps, snaps = SCENES[name]
-    bh, ch = g[f"{name}/body_hash"], g[f"{name}/contact_hash"]
+    bh, ch, ih = g[f"{name}/body_hash"], g[f"{name}/contact_hash"], g[f"{name}/island_hash"]
     w = make_scene(oracle, name)
     try:
         for s in range(steps + 1):
             bodies = oracle.bodies(w)
             assert digest(contact_table(oracle.contacts(w))) == ch[s], f"{name}: contact table differs at step {s}"
+            assert digest(oracle.islands(w)) == ih[s], f"{name}: solver sets / islands differ at step {s}"
             if digest(bodies.view(np.uint32)) != bh[s]:
-                snap = [k for k in snaps if k >= s]
-                msg = f"{name}: body state differs at step {s}"
-                pytest.fail(msg)
+                pytest.fail(f"{name}: body state differs at step {s}")
             if s in snaps:
                 assert np.array_equal(bodies.view(np.uint32), g[f"{name}/bodies_{s}"].view(np.uint32))
             if s < steps:
-                oracle.step(w)
+                step_scene(oracle, name, w, s + 1)
     finally:
         oracle.destroy(w)
 
@@ -195,6 +195,29 @@ def test_destruction_lockstep_reference(reference, oracle):
     step, detail, _ = lockstep(oracle, reference, lambda b: b.destruction(), 160, check_manifolds=True,
                                after_step=lambda b, w, s: b.destruction_step(w, s))
     assert step is None, f"{detail} at step {step}"
+
+
+def test_sleep_lockstep_reference(reference, oracle):
+    """Islands and sleep (reference src/island.c, src/solver_set.c): piles and a damped
+    chain fall asleep island by island, two bodies created asleep share a set through a
+    joint, and a destroyed body and joint, a dropped box, a rolled ball, a velocity set on
+    a sleeping body, SetAwake and the body and world sleep switches wake them.  Every
+    step the body states, the contact table and every body's solver set and island id
+    equal the reference's."""
+    step, detail, _ = lockstep(oracle, reference, lambda b: b.sleep_scene(), 360, check_manifolds=True,
+                               after_step=lambda b, w, s: b.sleep_step(w, s), check_islands=True)
+    assert step is None, f"{detail} at step {step}"
+
+
+def test_hello_world_sleeps_like_reference(reference, oracle):
+    """Reference test/test_world.c:17-97 with sleep on: the box's island falls asleep at
+    step 88 in both, in set 3 of island 0, and stays there."""
+    step, detail, _ = lockstep(oracle, reference, lambda b: b.hello_world()[0], 200, check_islands=True)
+    assert step is None, f"{detail} at step {step}"
+    w = oracle.hello_world()[0]
+    oracle.step(w, count=88)
+    assert oracle.islands(w).tolist() == [[0, -1], [3, 0]]
+    oracle.destroy(w)
 
 
 @pytest.mark.parametrize("backend", ["reference", "oracle"])
