@@ -112,9 +112,9 @@ extern "C" void b2gd_free( b2gDevWorld* w, b2gHostIO* io )
 	FREE_DEV( w->mass );
 	FREE_DEV( w->force );
 	FREE_DEV( w->extent );
-	FREE_DEV( w->bodyInfo );
-	FREE_DEV( w->sleepTime );
-	FREE_DEV( w->bodyOps );
+	FREE_DEV( w->bodyInfo ); /* with the sleep timers and body operations */
+	w->sleepTime = nullptr;
+	w->bodyOps = nullptr;
 	FREE_DEV( w->awake );
 	FREE_DEV( w->shapeRange );
 	FREE_DEV( w->shapeList );
@@ -195,11 +195,28 @@ extern "C" int b2gd_reserve( b2gDevWorld* w, b2gHostIO* io, int bodyCap, int sha
 		e |= grow( &w->mass, o4, n4, s );
 		e |= grow( &w->force, o4, n4, s );
 		e |= grow( &w->extent, o4, n4, s );
-		e |= grow( (void**)&w->bodyInfo, 4u * (size_t)w->bodyCap, 4u * (size_t)nc, s );
-		e |= grow( (void**)&w->sleepTime, 4u * (size_t)w->bodyCap, 4u * (size_t)nc, s );
-		e |= grow( (void**)&w->bodyOps, 4u * (size_t)w->bodyCap, 4u * (size_t)nc, s );
+		/* body info, sleep timers and staged body operations share one allocation (a batch
+		 * of thousands of worlds holds thousands of arenas) */
+		{
+			void* p = nullptr;
+			size_t o = 4u * (size_t)w->bodyCap, n = 4u * (size_t)nc;
+			e |= ok( cudaMallocAsync( &p, 3 * n, s ) );
+			if ( p != nullptr )
+			{
+				cudaMemsetAsync( p, 0, 3 * n, s );
+				if ( w->bodyInfo != nullptr && o > 0 )
+				{
+					cudaMemcpyAsync( p, w->bodyInfo, o, cudaMemcpyDeviceToDevice, s );
+					cudaMemcpyAsync( (char*)p + n, w->sleepTime, o, cudaMemcpyDeviceToDevice, s );
+				}
+				if ( w->bodyInfo != nullptr )
+					cudaFreeAsync( w->bodyInfo, s );
+				w->bodyInfo = (int*)p;
+				w->sleepTime = (float*)( (char*)p + n );
+				w->bodyOps = (int*)( (char*)p + 2 * n );
+			}
+		}
 		e |= grow( (void**)&w->awake, 4u * (size_t)w->bodyCap, 4u * (size_t)nc, s );
-		e |= grow_host_mapped( (void**)&io->sleepy, (void**)&w->sleepy, 8u * (size_t)nc );
 		e |= grow( (void**)&w->shapeRange, 8u * (size_t)w->bodyCap, 8u * (size_t)nc, s );
 		w->bodyCap = nc;
 	}
@@ -295,6 +312,17 @@ extern "C" int b2gd_upload_bodies( b2gDevWorld* w, const float* state, const flo
 	e |= h2d( w, w->force, force, n4, s );
 	e |= h2d( w, w->extent, extent, n4, s );
 	e |= h2d( w, w->bodyInfo, info, 4u * (size_t)count, s );
+	return e;
+}
+
+/* The mapped list of bodies past the sleep time, made on first use: only worlds with
+ * sleep on fill it. */
+extern "C" int b2gd_reserve_sleepy( b2gDevWorld* w, b2gHostIO* io )
+{
+	if ( w->sleepyCap >= w->bodyCap && io->sleepy != nullptr )
+		return 0;
+	int e = grow_host_mapped( (void**)&io->sleepy, (void**)&w->sleepy, 8u * (size_t)w->bodyCap );
+	w->sleepyCap = e == 0 ? w->bodyCap : 0;
 	return e;
 }
 

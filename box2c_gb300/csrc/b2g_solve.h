@@ -221,8 +221,12 @@ __device__ __forceinline__ void restitution_lane( Row& r, DevState& a, DevState&
 __device__ __forceinline__ void warm_scalar( const Row& r, DevState& a, DevState& b )
 {
 	b2gVec t = gright( r.n );
-	for ( int j = 0; j < r.count; ++j )
+	/* constant bounds keep the row's arrays in registers; points past count are skipped */
+#pragma unroll
+	for ( int j = 0; j < 2; ++j )
 	{
+		if ( j >= r.count )
+			break;
 		b2gVec P = gadd( gmulsv( r.ni[j], r.n ), gmulsv( r.ti[j], t ) );
 		a.w -= r.iA * gcross( r.rA[j], P );
 		a.v = gmuladd( a.v, -r.mA, P );
@@ -235,8 +239,12 @@ __device__ __forceinline__ void solve_scalar( Row& r, DevState& a, DevState& b, 
 {
 	b2gVec dp = gsub( b.dp, a.dp );
 	b2gVec n = r.n, t = gright( n );
-	for ( int j = 0; j < r.count; ++j )
+	/* constant bounds keep the row's arrays in registers; points past count are skipped */
+#pragma unroll
+	for ( int j = 0; j < 2; ++j )
 	{
+		if ( j >= r.count )
+			break;
 		b2gVec rA = r.rA[j], rB = r.rB[j];
 		b2gVec ds = gadd( dp, gsub( grotate( b.dq, rB ), grotate( a.dq, rA ) ) );
 		float s = gdot( ds, n ) + r.base[j];
@@ -263,8 +271,12 @@ __device__ __forceinline__ void solve_scalar( Row& r, DevState& a, DevState& b, 
 		b.v = gmuladd( b.v, r.mB, P );
 		b.w += r.iB * gcross( rB, P );
 	}
-	for ( int j = 0; j < r.count; ++j )
+	/* constant bounds keep the row's arrays in registers; points past count are skipped */
+#pragma unroll
+	for ( int j = 0; j < 2; ++j )
 	{
+		if ( j >= r.count )
+			break;
 		b2gVec rA = r.rA[j], rB = r.rB[j];
 		b2gVec vrB = gadd( b.v, gcross_sv( b.w, rB ) );
 		b2gVec vrA = gadd( a.v, gcross_sv( a.w, rA ) );
@@ -288,8 +300,12 @@ __device__ __forceinline__ bool restitution_scalar( Row& r, DevState& a, DevStat
 	if ( r.restitution == 0.0f )
 		return false;
 	b2gVec n = r.n;
-	for ( int j = 0; j < r.count; ++j )
+	/* constant bounds keep the row's arrays in registers; points past count are skipped */
+#pragma unroll
+	for ( int j = 0; j < 2; ++j )
 	{
+		if ( j >= r.count )
+			break;
 		if ( r.relVel[j] > -threshold || r.maxNi[j] == 0.0f )
 			continue;
 		b2gVec rA = r.rA[j], rB = r.rB[j];

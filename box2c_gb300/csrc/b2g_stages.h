@@ -582,7 +582,7 @@ static __device__ void finalize_body( const b2gDevWorld& W, int i, const b2gStep
 	if ( sleepTime >= B2G_TIME_TO_SLEEP )
 	{
 		int slot = atomicAdd( W.counters + 3, 1 );
-		if ( slot < W.bodyCap )
+		if ( slot < W.sleepyCap )
 		{
 			W.sleepy[2 * slot] = i;
 			W.sleepy[2 * slot + 1] = __float_as_int( sleepTime );

@@ -114,7 +114,6 @@ enum
 {
 	B2G_BODY_SLEEP = 0, /* leaves the awake set */
 	B2G_BODY_WAKE = 1,	/* joins the awake set with zero velocity and a zero sleep timer */
-	B2G_BODY_RESET = 2, /* a new body: zero sleep timer */
 };
 
 typedef struct b2gContactInit
@@ -274,7 +273,7 @@ typedef struct b2gDevWorld
 	int* events;	   /* device view of the mapped event buffer */
 	b2gRecord* records; /* device view of the mapped record buffer */
 	int* sleepy;	   /* device view of the mapped sleepy-body buffer: 2 ints per body (awake index, sleep time bits) */
-	int eventCap, recordCap;
+	int eventCap, recordCap, sleepyCap;
 	void* stream; /* cudaStream_t */
 	void* timers[8]; /* cudaEvent_t: step start, collide start/end, solve start/end, finalize end, step end */
 	int timing;

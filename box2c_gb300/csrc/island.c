@@ -858,7 +858,7 @@ void gislands_sleep_step( gWorld* w )
 	/* every body below the sleep time keeps its island awake; among the rest, the first
 	 * body in awake order with the longest sleep time picks the island to split next */
 	int n = w->io.counters[3];
-	n = n < w->dev.bodyCap ? n : w->dev.bodyCap;
+	n = n < w->dev.sleepyCap ? n : w->dev.sleepyCap;
 	w->dev.d2hBytes += 8 * (long long)n;
 	int split = B2G_NULL, splitIndex = 0;
 	float splitTime = 0.0f;

@@ -272,6 +272,8 @@ void gworld_flush( gWorld* w )
 	/* body operations first: the full upload below carries a mirror that already
 	 * reflects them */
 	e |= gbody_flush_ops( w );
+	if ( w->enableSleep )
+		e |= b2gd_reserve_sleepy( &w->dev, &w->io );
 	if ( w->bodiesDirty )
 	{
 		e |= b2gd_upload_bodies( &w->dev, w->hState, w->hXf, w->hCenters, w->hPrev, w->hMass, w->hForce, w->hExtent, w->hInfo, nb );
