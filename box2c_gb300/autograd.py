@@ -37,9 +37,12 @@ def bind_adjoint_api(lib: C.CDLL) -> None:
 class DropBoxes:
     """W drop-boxes worlds stepped together on the GPU library."""
 
-    def __init__(self, backend: Backend, heights: np.ndarray, steps: int = 120, substeps: int = 4, dt: float = 1.0 / 60.0):
+    def __init__(self, backend: Backend, heights: np.ndarray, steps: int = 120, substeps: int = 4, dt: float = 1.0 / 60.0,
+                 kinds: np.ndarray | None = None):
         self.b = backend
         self.heights = np.ascontiguousarray(heights, np.float32)
+        # per world and body: 0 box, 1 circle, 2 capsule (all boxes when None)
+        self.kinds = None if kinds is None else np.ascontiguousarray(kinds, np.int32)
         self.worlds_n, self.boxes = self.heights.shape
         self.steps, self.substeps, self.dt = steps, substeps, dt
         self.bodies = self.boxes + 1  # ground is body 0
@@ -55,7 +58,8 @@ class DropBoxes:
         self.destroy()
         L = self.b.lib
         for w in range(self.worlds_n):
-            world = self.b.drop_boxes(self.heights[w], v0[w, :, 0], v0[w, :, 1], float(mu[w]))
+            world = self.b.drop_boxes(self.heights[w], v0[w, :, 0], v0[w, :, 1], float(mu[w]),
+                                      None if self.kinds is None else self.kinds[w])
             if record:
                 L.b2World_BeginTape(world, self.steps)
             self.worlds.append(world)

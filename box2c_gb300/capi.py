@@ -154,6 +154,8 @@ class Backend:
         S.b2s_tumbler.restype = WorldId
         S.b2s_drop_boxes.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_float]
         S.b2s_drop_boxes.restype = WorldId
+        S.b2s_drop_shapes.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_float, C.c_void_p]
+        S.b2s_drop_shapes.restype = WorldId
         S.b2s_hello_world.argtypes = [C.POINTER(BodyId)]
         S.b2s_hello_world.restype = WorldId
         S.b2s_tilted_stacks.argtypes = []
@@ -207,11 +209,15 @@ class Backend:
     def tumbler(self, count: int = 2000, seed: int = 1236, variant: int = 0) -> WorldId:
         return self.scenes.b2s_tumbler(count, seed, variant)
 
-    def drop_boxes(self, heights, vx, vy, friction: float) -> WorldId:
+    def drop_boxes(self, heights, vx, vy, friction: float, kinds=None) -> WorldId:
+        """Bodies dropped on a ground; kinds[k] picks body k's shape (0 box, 1 circle, 2 capsule)."""
         h = np.ascontiguousarray(heights, np.float32)
         a = np.ascontiguousarray(vx, np.float32)
         b = np.ascontiguousarray(vy, np.float32)
-        return self.scenes.b2s_drop_boxes(len(h), h.ctypes.data, a.ctypes.data, b.ctypes.data, friction)
+        if kinds is None:
+            return self.scenes.b2s_drop_boxes(len(h), h.ctypes.data, a.ctypes.data, b.ctypes.data, friction)
+        k = np.ascontiguousarray(kinds, np.int32)
+        return self.scenes.b2s_drop_shapes(len(h), h.ctypes.data, a.ctypes.data, b.ctypes.data, friction, k.ctypes.data)
 
     def hello_world(self):
         body = BodyId()

@@ -22,8 +22,9 @@
  * Differentiated: body centres, angles, linear and angular velocities, and contact
  * friction (mixed per shape as sqrt(muA * muB), reference src/contact.c:42-45).  The
  * discrete choices of a step (pairs, colours, manifold features, active clamps) are
- * those of the recorded forward step.  Polygon, capsule and segment shapes; joints,
- * overflow-colour rows, circle shapes and chain links are reported as unsupported.
+ * those of the recorded forward step.  Polygon, capsule, segment and circle shapes, and
+ * rows in the graph colours and in the overflow colour; joints and chain links are
+ * reported as unsupported.
  *
  * Reference arithmetic being differentiated: src/solver.c:34-93, :146-163, :205-223;
  * src/contact_solver.c:597-1293; src/manifold.c:276-700.
@@ -201,12 +202,14 @@ __device__ void warm_vjp( const Row& r, const BodyV& aA, const BodyV& aB, RowAdj
 	}
 }
 
-/* Solve / relax (8-lane path).  r holds the impulses before the row ran; a, b the
- * states before it (velocities) and the substep's position deltas.  On entry aA, aB
- * are the adjoints of the velocities after the row; on exit, before it.  dpA.. receive
- * the position-delta adjoints. */
+/* Solve / relax.  r holds the impulses before the row ran; a, b the states before it
+ * (velocities) and the substep's position deltas.  On entry aA, aB are the adjoints of
+ * the velocities after the row; on exit, before it.  dpA.. receive the position-delta
+ * adjoints.  scalar: an overflow row, whose speculative points (s > 0) take the rigid
+ * mass and no impulse scaling where the 8-lane rows keep the soft ones (reference
+ * src/contact_solver.c:266-279 against :905-925). */
 __device__ void solve_vjp( Row r, DevState a, DevState b, bool useBias, const b2gStepConst& sc, BodyV& aA, BodyV& aB, RowAdj& ra,
-						   float* dpA, float* dqA, float* dpB, float* dqB )
+						   float* dpA, float* dqA, float* dpB, float* dqB, bool scalar = false )
 {
 	float biasRate = useBias ? r.biasRate : 0.0f;
 	float massScale = useBias ? r.massScale : 1.0f;
@@ -220,7 +223,7 @@ __device__ void solve_vjp( Row r, DevState a, DevState b, bool useBias, const b2
 	DevState sa[4], sb[4];
 	float ni0[2] = { r.ni[0], r.ni[1] };
 	float ti0[2] = { r.ti[0], r.ti[1] };
-	float s_[2], dbds[2], xN[2];
+	float s_[2], dbds[2], xN[2], ms_[2], is_[2];
 	for ( int j = 0; j < 2; ++j )
 	{
 		sa[j] = a;
@@ -243,9 +246,11 @@ __device__ void solve_vjp( Row r, DevState a, DevState b, bool useBias, const b2
 			dbds[j] = soft > minBias ? biasRate : 0.0f;
 		}
 		s_[j] = s;
+		ms_[j] = scalar && s > 0.0f ? 1.0f : massScale;
+		is_[j] = scalar && s > 0.0f ? 0.0f : impulseScale;
 		b2gVec dv = lane_dv( a, b, aA_, aB_ );
 		float vn = dv.x * n.x + dv.y * n.y;
-		float negImpulse = r.nMass[j] * ( massScale * ( vn + bias ) ) + impulseScale * r.ni[j];
+		float negImpulse = r.nMass[j] * ( ms_[j] * ( vn + bias ) ) + is_[j] * r.ni[j];
 		float x = r.ni[j] - negImpulse;
 		xN[j] = x;
 		float newImpulse = gmax( x, 0.0f );
@@ -333,9 +338,9 @@ __device__ void solve_vjp( Row r, DevState a, DevState b, bool useBias, const b2
 		/* negImpulse = nMass * ( massScale * ( vn + bias ) ) + impulseScale * ni */
 		float s = s_[j];
 		float bias = s > 0.0f ? s * sc.inv_h : gmax( biasRate * s, minBias );
-		ra.nMass[j] += negb * ( massScale * ( vn + bias ) );
-		float vnb = negb * r.nMass[j] * massScale;
-		nib += negb * impulseScale;
+		ra.nMass[j] += negb * ( ms_[j] * ( vn + bias ) );
+		float vnb = negb * r.nMass[j] * ms_[j];
+		nib += negb * is_[j];
 		float sb_ = vnb * dbds[j];
 		ra.n[0] += vnb * dv.x;
 		ra.n[1] += vnb * dv.y;
@@ -595,11 +600,28 @@ __device__ bool manifold_jacobian( const b2gShapeGeo& gA, const b2gShapeGeo& gB,
 		xf[k].q.s = s;
 		q[k] = xf[k].q;
 	}
-	b2gPoly pa, pb;
-	gshape_poly( &pa, &gA );
-	gshape_poly( &pb, &gB );
+	/* the narrowphase's dispatch (b2g_collide.h gcollide_shapes) for A not a chain link */
 	DManifold<6> m;
-	dcollide_polygons( m, pa, xf[0], pb, xf[1] );
+	if ( gB.type == 0 )
+	{
+		if ( gA.type == 0 )
+			dcollide_circles( m, gA.v[0], gA.radius, xf[0], gB.v[0], gB.radius, xf[1] );
+		else if ( gA.type == 1 || gA.type == 2 )
+			dcollide_capsule_circle( m, gA.v[0], gA.v[1], gA.type == 1 ? gA.radius : 0.0f, xf[0], gB.v[0], gB.radius, xf[1] );
+		else
+		{
+			b2gPoly pa;
+			gshape_poly( &pa, &gA );
+			dcollide_polygon_circle( m, pa, xf[0], gB.v[0], gB.radius, xf[1] );
+		}
+	}
+	else
+	{
+		b2gPoly pa, pb;
+		gshape_poly( &pa, &gA );
+		gshape_poly( &pb, &gB );
+		dcollide_polygons( m, pa, xf[0], pb, xf[1] );
+	}
 	DVec<6> offA = drotate( q[0], dvc<6>( gv( startA[4], startA[5] ) ) );
 	DVec<6> offB = drotate( q[1], dvc<6>( gv( startB[4], startB[5] ) ) );
 	bool same = m.count == rec.count && m.normal.x.v == rec.normal.x && m.normal.y.v == rec.normal.y;
@@ -654,9 +676,52 @@ __device__ __forceinline__ void store_row_rec( const AdjLayout& L, int k, const 
 
 /* One forward stage of the replay over the active colours (warm 0, solve 1, relax 2,
  * restitution 3), recording each row's starting velocities and impulses. */
+/* The state a row starts from, kept on the phase tape for its reverse. */
+__device__ __forceinline__ void tape_row_start( float* t, const Row& r, const DevState& A, const DevState& B )
+{
+	t[0] = A.v.x;
+	t[1] = A.v.y;
+	t[2] = A.w;
+	t[3] = B.v.x;
+	t[4] = B.v.y;
+	t[5] = B.w;
+	t[6] = r.ni[0];
+	t[7] = r.ni[1];
+	t[8] = r.ti[0];
+	t[9] = r.ti[1];
+	t[10] = r.maxNi[0];
+	t[11] = r.maxNi[1];
+}
+
 __device__ void replay_stage( const AdjLayout& L, const b2gTapeStep& h, int R, int phase, int tapeIndex, const b2gStepConst& sc )
 {
 	float* tape = L.phase + (size_t)tapeIndex * R * ADJ_PHASE;
+	/* the overflow colour first, one row after another with the scalar arithmetic
+	 * (reference src/contact_solver.c:149-440) */
+	if ( threadIdx.x == 0 )
+	{
+		for ( int k = h.colorStart[B2G_OVERFLOW]; k < h.colorStart[B2G_COLORS]; ++k )
+		{
+			Row r = load_row_rec( L, k );
+			DevState A = replay_state( L, r.ia );
+			DevState B = replay_state( L, r.ib );
+			tape_row_start( tape + (size_t)k * ADJ_PHASE, r, A, B );
+			bool changed = true;
+			if ( phase == 0 )
+				warm_scalar( r, A, B );
+			else if ( phase == 3 )
+				changed = restitution_scalar( r, A, B, sc.restitutionThreshold );
+			else
+				solve_scalar( r, A, B, phase == 1, sc.inv_h, sc.pushout );
+			if ( changed )
+			{
+				replay_store_velocity( L, r.ia, A );
+				replay_store_velocity( L, r.ib, B );
+				store_row_rec( L, k, r );
+			}
+		}
+	}
+	__syncwarp();
 	for ( int a = 0; a < h.activeCount; ++a )
 	{
 		int c = h.active[a];
@@ -665,19 +730,7 @@ __device__ void replay_stage( const AdjLayout& L, const b2gTapeStep& h, int R, i
 			Row r = load_row_rec( L, k );
 			DevState A = replay_state( L, r.ia );
 			DevState B = replay_state( L, r.ib );
-			float* t = tape + (size_t)k * ADJ_PHASE;
-			t[0] = A.v.x;
-			t[1] = A.v.y;
-			t[2] = A.w;
-			t[3] = B.v.x;
-			t[4] = B.v.y;
-			t[5] = B.w;
-			t[6] = r.ni[0];
-			t[7] = r.ni[1];
-			t[8] = r.ti[0];
-			t[9] = r.ti[1];
-			t[10] = r.maxNi[0];
-			t[11] = r.maxNi[1];
+			tape_row_start( tape + (size_t)k * ADJ_PHASE, r, A, B );
 			if ( phase == 0 )
 				warm_lane( r, A, B );
 			else if ( phase == 3 )
@@ -692,8 +745,79 @@ __device__ void replay_stage( const AdjLayout& L, const b2gTapeStep& h, int R, i
 	}
 }
 
-/* Reverse of one stage: colours in reverse order.  snap: body snapshot holding the
- * position deltas the stage used (solve and relax). */
+/* Reverse of one row of a stage (its velocity, impulse and position-delta adjoints).
+ * The scalar overflow rows share the lane rows' derivatives: the arithmetic is the same
+ * up to operand grouping, a point past the manifold's count is a zero point of the lane
+ * layout, and a restitution-free overflow row is skipped as the forward skipped it. */
+__device__ void reverse_row( const AdjLayout& L, const float* tape, int k, int phase, const float* snap, const b2gStepConst& sc,
+							 bool scalar )
+{
+	Row r = load_row_rec( L, k );
+	if ( scalar && phase == 3 && r.restitution == 0.0f )
+		return;
+	const float* t = tape + (size_t)k * ADJ_PHASE;
+	r.ni[0] = t[6];
+	r.ni[1] = t[7];
+	r.ti[0] = t[8];
+	r.ti[1] = t[9];
+	r.maxNi[0] = t[10];
+	r.maxNi[1] = t[11];
+	DevState A = identity_state(), B = identity_state();
+	A.v = gv( t[0], t[1] );
+	A.w = t[2];
+	B.v = gv( t[3], t[4] );
+	B.w = t[5];
+	if ( snap && r.ia >= 0 )
+	{
+		const float* s = snap + (size_t)r.ia * ADJ_SNAP;
+		A.dp = gv( s[4], s[5] );
+		A.dq = grot( s[6], s[7] );
+	}
+	if ( snap && r.ib >= 0 )
+	{
+		const float* s = snap + (size_t)r.ib * ADJ_SNAP;
+		B.dp = gv( s[4], s[5] );
+		B.dq = grot( s[6], s[7] );
+	}
+	float* gA = r.ia >= 0 ? L.bodyAdj + (size_t)r.ia * ADJ_BODY : nullptr;
+	float* gB = r.ib >= 0 ? L.bodyAdj + (size_t)r.ib * ADJ_BODY : nullptr;
+	BodyV aA = { gA ? gA[4] : 0.0f, gA ? gA[5] : 0.0f, gA ? gA[6] : 0.0f };
+	BodyV aB = { gB ? gB[4] : 0.0f, gB ? gB[5] : 0.0f, gB ? gB[6] : 0.0f };
+	RowAdj* ra = (RowAdj*)( L.radj + (size_t)k * ADJ_RADJ );
+	RowAdj g = *ra;
+	float dpA[2] = { 0.0f, 0.0f }, dqA[2] = { 0.0f, 0.0f }, dpB[2] = { 0.0f, 0.0f }, dqB[2] = { 0.0f, 0.0f };
+	if ( phase == 0 )
+		warm_vjp( r, aA, aB, g );
+	else if ( phase == 3 )
+		restitution_vjp( r, A, B, sc, aA, aB, g );
+	else
+		solve_vjp( r, A, B, phase == 1, sc, aA, aB, g, dpA, dqA, dpB, dqB, scalar );
+	*ra = g;
+	if ( gA )
+	{
+		gA[4] = aA.vx;
+		gA[5] = aA.vy;
+		gA[6] = aA.w;
+		gA[7] += dpA[0];
+		gA[8] += dpA[1];
+		gA[9] += dqA[0];
+		gA[10] += dqA[1];
+	}
+	if ( gB )
+	{
+		gB[4] = aB.vx;
+		gB[5] = aB.vy;
+		gB[6] = aB.w;
+		gB[7] += dpB[0];
+		gB[8] += dpB[1];
+		gB[9] += dqB[0];
+		gB[10] += dqB[1];
+	}
+}
+
+/* Reverse of one stage: colours in reverse order, then the overflow rows in reverse
+ * order.  snap: body snapshot holding the position deltas the stage used (solve and
+ * relax). */
 __device__ void reverse_stage( const AdjLayout& L, const b2gTapeStep& h, int R, int phase, int tapeIndex, const float* snap,
 							   const b2gStepConst& sc )
 {
@@ -702,69 +826,15 @@ __device__ void reverse_stage( const AdjLayout& L, const b2gTapeStep& h, int R, 
 	{
 		int c = h.active[a];
 		for ( int k = h.colorStart[c] + (int)threadIdx.x; k < h.colorStart[c + 1]; k += ADJ_WARP )
-		{
-			Row r = load_row_rec( L, k );
-			const float* t = tape + (size_t)k * ADJ_PHASE;
-			r.ni[0] = t[6];
-			r.ni[1] = t[7];
-			r.ti[0] = t[8];
-			r.ti[1] = t[9];
-			r.maxNi[0] = t[10];
-			r.maxNi[1] = t[11];
-			DevState A = identity_state(), B = identity_state();
-			A.v = gv( t[0], t[1] );
-			A.w = t[2];
-			B.v = gv( t[3], t[4] );
-			B.w = t[5];
-			if ( snap && r.ia >= 0 )
-			{
-				const float* s = snap + (size_t)r.ia * ADJ_SNAP;
-				A.dp = gv( s[4], s[5] );
-				A.dq = grot( s[6], s[7] );
-			}
-			if ( snap && r.ib >= 0 )
-			{
-				const float* s = snap + (size_t)r.ib * ADJ_SNAP;
-				B.dp = gv( s[4], s[5] );
-				B.dq = grot( s[6], s[7] );
-			}
-			float* gA = r.ia >= 0 ? L.bodyAdj + (size_t)r.ia * ADJ_BODY : nullptr;
-			float* gB = r.ib >= 0 ? L.bodyAdj + (size_t)r.ib * ADJ_BODY : nullptr;
-			BodyV aA = { gA ? gA[4] : 0.0f, gA ? gA[5] : 0.0f, gA ? gA[6] : 0.0f };
-			BodyV aB = { gB ? gB[4] : 0.0f, gB ? gB[5] : 0.0f, gB ? gB[6] : 0.0f };
-			RowAdj* ra = (RowAdj*)( L.radj + (size_t)k * ADJ_RADJ );
-			RowAdj g = *ra;
-			float dpA[2] = { 0.0f, 0.0f }, dqA[2] = { 0.0f, 0.0f }, dpB[2] = { 0.0f, 0.0f }, dqB[2] = { 0.0f, 0.0f };
-			if ( phase == 0 )
-				warm_vjp( r, aA, aB, g );
-			else if ( phase == 3 )
-				restitution_vjp( r, A, B, sc, aA, aB, g );
-			else
-				solve_vjp( r, A, B, phase == 1, sc, aA, aB, g, dpA, dqA, dpB, dqB );
-			*ra = g;
-			if ( gA )
-			{
-				gA[4] = aA.vx;
-				gA[5] = aA.vy;
-				gA[6] = aA.w;
-				gA[7] += dpA[0];
-				gA[8] += dpA[1];
-				gA[9] += dqA[0];
-				gA[10] += dqA[1];
-			}
-			if ( gB )
-			{
-				gB[4] = aB.vx;
-				gB[5] = aB.vy;
-				gB[6] = aB.w;
-				gB[7] += dpB[0];
-				gB[8] += dpB[1];
-				gB[9] += dqB[0];
-				gB[10] += dqB[1];
-			}
-		}
+			reverse_row( L, tape, k, phase, snap, sc, false );
 		__syncwarp();
 	}
+	if ( threadIdx.x == 0 )
+	{
+		for ( int k = h.colorStart[B2G_COLORS] - 1; k >= h.colorStart[B2G_OVERFLOW]; --k )
+			reverse_row( L, tape, k, phase, snap, sc, true );
+	}
+	__syncwarp();
 }
 
 __device__ void snapshot( const AdjLayout& L, int N, int index )
@@ -809,7 +879,7 @@ __global__ void __launch_bounds__( ADJ_WARP ) k_adjoint( const b2gAdjointItem* i
 			unsupported += h.solve != 0 ? 1 : 0;
 			continue;
 		}
-		if ( h.colorStart[B2G_COLORS] > h.colorStart[B2G_OVERFLOW] || h.jointStart[B2G_COLORS] > 0 )
+		if ( h.jointStart[B2G_COLORS] > 0 )
 			unsupported += 1;
 		const float* recB = it.tapeBodies + 4 * h.bodyOff;
 		const b2gTapeRow* recR = it.tapeRows + h.rowOff;
@@ -873,8 +943,8 @@ __global__ void __launch_bounds__( ADJ_WARP ) k_adjoint( const b2gAdjointItem* i
 			const b2gTapeRow& tr = recR[k];
 			const b2gShapeGeo& gA = W.geo[tr.shapeA];
 			const b2gShapeGeo& gB = W.geo[tr.shapeB];
-			if ( gB.type == 0 || gA.type == 4 )
-				unsupported += 1; /* circles and chain links have no manifold Jacobian here */
+			if ( gA.type == 4 )
+				unsupported += 1; /* chain links have no manifold Jacobian here */
 			else if ( manifold_jacobian( gA, gB, L.start + (size_t)gA.bodyId * ADJ_START, L.start + (size_t)gB.bodyId * ADJ_START, tr.ia >= 0,
 										 tr.ib >= 0, tr.m, L.jac + (size_t)k * ADJ_JAC ) == false )
 				mismatches += 1;
@@ -1034,11 +1104,14 @@ __global__ void __launch_bounds__( ADJ_WARP ) k_adjoint( const b2gAdjointItem* i
 		}
 
 		/* reverse: preparation and the manifold Jacobian, colour by colour so that no
-		 * two lanes update one body */
-		for ( int a = 0; a < h.activeCount; ++a )
+		 * two lanes update one body, then the overflow rows one after another on lane 0 */
+		for ( int a = 0; a <= h.activeCount; ++a )
 		{
-			int c = h.active[a];
-			for ( int k = h.colorStart[c] + lane; k < h.colorStart[c + 1]; k += ADJ_WARP )
+			const bool ov = a == h.activeCount;
+			const int c = ov ? B2G_OVERFLOW : h.active[a];
+			const int first = ov ? ( lane == 0 ? h.colorStart[c] : h.colorStart[c + 1] ) : h.colorStart[c] + lane;
+			const int stride = ov ? 1 : ADJ_WARP;
+			for ( int k = first; k < h.colorStart[c + 1]; k += stride )
 			{
 				const b2gTapeRow& tr = recR[k];
 				Row r = load_row_rec( L, k );

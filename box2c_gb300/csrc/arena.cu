@@ -112,9 +112,9 @@ extern "C" void b2gd_free( b2gDevWorld* w, b2gHostIO* io )
 	FREE_DEV( w->mass );
 	FREE_DEV( w->force );
 	FREE_DEV( w->extent );
-	FREE_DEV( w->bodyInfo ); /* with the sleep timers and body operations */
-	w->sleepTime = nullptr;
-	w->bodyOps = nullptr;
+	FREE_DEV( w->bodyInfo );
+	FREE_DEV( w->sleepTime );
+	FREE_DEV( w->bodyOps );
 	FREE_DEV( w->awake );
 	FREE_DEV( w->shapeRange );
 	FREE_DEV( w->shapeList );
@@ -195,27 +195,10 @@ extern "C" int b2gd_reserve( b2gDevWorld* w, b2gHostIO* io, int bodyCap, int sha
 		e |= grow( &w->mass, o4, n4, s );
 		e |= grow( &w->force, o4, n4, s );
 		e |= grow( &w->extent, o4, n4, s );
-		/* body info, sleep timers and staged body operations share one allocation (a batch
-		 * of thousands of worlds holds thousands of arenas) */
-		{
-			void* p = nullptr;
-			size_t o = 4u * (size_t)w->bodyCap, n = 4u * (size_t)nc;
-			e |= ok( cudaMallocAsync( &p, 3 * n, s ) );
-			if ( p != nullptr )
-			{
-				cudaMemsetAsync( p, 0, 3 * n, s );
-				if ( w->bodyInfo != nullptr && o > 0 )
-				{
-					cudaMemcpyAsync( p, w->bodyInfo, o, cudaMemcpyDeviceToDevice, s );
-					cudaMemcpyAsync( (char*)p + n, w->sleepTime, o, cudaMemcpyDeviceToDevice, s );
-				}
-				if ( w->bodyInfo != nullptr )
-					cudaFreeAsync( w->bodyInfo, s );
-				w->bodyInfo = (int*)p;
-				w->sleepTime = (float*)( (char*)p + n );
-				w->bodyOps = (int*)( (char*)p + 2 * n );
-			}
-		}
+		e |= grow( (void**)&w->bodyInfo, 4u * (size_t)w->bodyCap, 4u * (size_t)nc, s );
+		/* sleep timers only in worlds that have had sleep on (b2gd_reserve_sleep) */
+		if ( w->sleepTime != nullptr )
+			e |= grow( (void**)&w->sleepTime, 4u * (size_t)w->bodyCap, 4u * (size_t)nc, s );
 		e |= grow( (void**)&w->awake, 4u * (size_t)w->bodyCap, 4u * (size_t)nc, s );
 		e |= grow( (void**)&w->shapeRange, 8u * (size_t)w->bodyCap, 8u * (size_t)nc, s );
 		w->bodyCap = nc;
@@ -315,14 +298,32 @@ extern "C" int b2gd_upload_bodies( b2gDevWorld* w, const float* state, const flo
 	return e;
 }
 
-/* The mapped list of bodies past the sleep time, made on first use: only worlds with
- * sleep on fill it. */
-extern "C" int b2gd_reserve_sleepy( b2gDevWorld* w, b2gHostIO* io )
+/* Sleep timers (zero) and the mapped list of bodies past the sleep time, made when a
+ * world first steps with sleep on; a world that never sleeps holds neither and its
+ * finalisation skips the timers. */
+extern "C" int b2gd_reserve_sleep( b2gDevWorld* w, b2gHostIO* io )
 {
-	if ( w->sleepyCap >= w->bodyCap && io->sleepy != nullptr )
+	int e = 0;
+	if ( w->sleepTime == nullptr )
+		e |= grow( (void**)&w->sleepTime, 0, 4u * (size_t)w->bodyCap, (cudaStream_t)w->stream );
+	if ( w->sleepyCap < w->bodyCap || io->sleepy == nullptr )
+	{
+		e |= grow_host_mapped( (void**)&io->sleepy, (void**)&w->sleepy, 8u * (size_t)w->bodyCap );
+		w->sleepyCap = e == 0 ? w->bodyCap : 0;
+	}
+	return e;
+}
+
+/* Device staging of body operations, grown on demand. */
+extern "C" int b2gd_reserve_body_ops( b2gDevWorld* w, int count )
+{
+	if ( count <= w->bodyOpsCap && w->bodyOps != nullptr )
 		return 0;
-	int e = grow_host_mapped( (void**)&io->sleepy, (void**)&w->sleepy, 8u * (size_t)w->bodyCap );
-	w->sleepyCap = e == 0 ? w->bodyCap : 0;
+	int cap = w->bodyOpsCap < 64 ? 64 : w->bodyOpsCap;
+	while ( cap < count )
+		cap *= 2;
+	int e = grow( (void**)&w->bodyOps, 0, 4u * (size_t)cap, (cudaStream_t)w->stream );
+	w->bodyOpsCap = e == 0 ? cap : 0;
 	return e;
 }
 

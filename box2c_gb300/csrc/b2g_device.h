@@ -63,9 +63,10 @@ int b2gd_reserve( b2gDevWorld* w, b2gHostIO* io, int bodyCap, int shapeCap, int 
 int b2gd_upload_bodies( b2gDevWorld* w, const float* state, const float* xf, const float* centers, const float* prev,
 						const float* mass, const float* force, const float* extent, const int* info, int count );
 int b2gd_upload_awake( b2gDevWorld* w, const int* awake, int count );
-/* Makes the mapped list of bodies past the sleep time hold every body (worlds with sleep
- * on; elsewhere it stays unallocated and finalisation never writes it). */
-int b2gd_reserve_sleepy( b2gDevWorld* w, b2gHostIO* io );
+/* Sleep timers and the mapped list of bodies past the sleep time for every body (worlds
+ * that step with sleep on; elsewhere neither exists and finalisation skips the timers). */
+int b2gd_reserve_sleep( b2gDevWorld* w, b2gHostIO* io );
+int b2gd_reserve_body_ops( b2gDevWorld* w, int count );
 /* Applies ops[0, count) (one per body, (bodyId << 2) | B2G_BODY_*) on the world's stream
  * (sleep: stop integrating; wake: identity state, zero sleep timer).  The copy is taken
  * from pageable memory, so ops may be reused when the call returns. */

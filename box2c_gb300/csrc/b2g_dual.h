@@ -548,3 +548,132 @@ __device__ void dcollide_polygons( DManifold<N>& m, const b2gPoly& polyA, const 
 		}
 	}
 }
+
+/* ------------------------------------------------------------------ circle manifolds */
+/* Dual-number twins of the circle manifolds of b2g_collide.h (reference
+ * src/manifold.c:36-250): the same operations in the same order, so the values are the
+ * forward manifold's bits and the derivatives follow the chosen branch. */
+template <int N>
+__device__ __forceinline__ DVec<N> dmulsub_f( const DVec<N>& a, float s, const DVec<N>& b )
+{
+	return dv( a.x - s * b.x, a.y - s * b.y );
+}
+
+template <int N>
+__device__ __forceinline__ DVec<N> dlen_normalize( Dual<N>& length, const DVec<N>& v )
+{
+	length = dsqrt( v.x * v.x + v.y * v.y );
+	if ( length.v < FLT_EPSILON )
+		return dvc<N>( gv( 0.0f, 0.0f ) );
+	Dual<N> inv = dc<N>( 1.0f ) / length;
+	return dv( inv * v.x, inv * v.y );
+}
+
+template <int N>
+__device__ __forceinline__ void done_point( DManifold<N>& m, const DXf<N>& xfA, const DXf<N>& xfB, const DVec<N>& localNormal,
+											const DVec<N>& contactPointA, const Dual<N>& separation )
+{
+	m.normal = drotate( xfA.q, localNormal );
+	DPoint<N>* mp = m.pts;
+	mp->anchorA = drotate( xfA.q, contactPointA );
+	mp->anchorB = dadd( mp->anchorA, dsub( xfA.p, xfB.p ) );
+	mp->separation = separation;
+	mp->id = 0;
+	m.count = 1;
+}
+
+/* the closing part of the circle-circle and capsule-circle manifolds, from the closest
+ * point pA on A and the circle centre pB (A's frame) */
+template <int N>
+__device__ __forceinline__ void dround_pair( DManifold<N>& m, const DVec<N>& pA, const DVec<N>& pB, float rA, float rB, const DXf<N>& xfA,
+											 const DXf<N>& xfB )
+{
+	Dual<N> distance;
+	DVec<N> normal = dlen_normalize( distance, dsub( pB, pA ) );
+	Dual<N> separation = distance - rA - rB;
+	if ( separation.v > B2G_SPECULATIVE )
+		return;
+	DVec<N> cA = dmuladd_f( pA, rA, normal );
+	DVec<N> cB = dmuladd_f( pB, -rB, normal );
+	done_point( m, xfA, xfB, normal, dlerp_f( cA, cB, 0.5f ), separation );
+}
+
+template <int N>
+__device__ void dcollide_circles( DManifold<N>& m, b2gVec centerA, float rA, const DXf<N>& xfA, b2gVec centerB, float rB, const DXf<N>& xfB )
+{
+	m.count = 0;
+	DXf<N> xf = dinvmulxf( xfA, xfB );
+	DVec<N> pB = dxfpoint( xf, dvc<N>( centerB ) );
+	dround_pair( m, dvc<N>( centerA ), pB, rA, rB, xfA, xfB );
+}
+
+template <int N>
+__device__ void dcollide_capsule_circle( DManifold<N>& m, b2gVec p1, b2gVec p2, float rA, const DXf<N>& xfA, b2gVec centerB, float rB,
+										 const DXf<N>& xfB )
+{
+	m.count = 0;
+	DXf<N> xf = dinvmulxf( xfA, xfB );
+	DVec<N> pB = dxfpoint( xf, dvc<N>( centerB ) );
+	b2gVec e = gsub( p2, p1 );
+	DVec<N> E = dvc<N>( e );
+	Dual<N> s1 = ddot( dsub( pB, dvc<N>( p1 ) ), E );
+	Dual<N> s2 = ddot( dsub( dvc<N>( p2 ), pB ), E );
+	DVec<N> pA;
+	if ( s1.v < 0.0f )
+		pA = dvc<N>( p1 );
+	else if ( s2.v < 0.0f )
+		pA = dvc<N>( p2 );
+	else
+	{
+		Dual<N> s = s1 / dc<N>( gdot( e, e ) );
+		pA = dmuladd( dvc<N>( p1 ), s, E );
+	}
+	dround_pair( m, pA, pB, rA, rB, xfA, xfB );
+}
+
+template <int N>
+__device__ void dcollide_polygon_circle( DManifold<N>& m, const b2gPoly& a, const DXf<N>& xfA, b2gVec centerB, float rB, const DXf<N>& xfB )
+{
+	m.count = 0;
+	DXf<N> xf = dinvmulxf( xfA, xfB );
+	DVec<N> c = dxfpoint( xf, dvc<N>( centerB ) );
+	float rA = a.radius;
+	float radius = rA + rB;
+	int normalIndex = 0;
+	Dual<N> separation = dc<N>( -FLT_MAX );
+	for ( int i = 0; i < a.count; ++i )
+	{
+		Dual<N> s = ddot( dvc<N>( a.n[i] ), dsub( c, dvc<N>( a.v[i] ) ) );
+		if ( s.v > separation.v )
+		{
+			separation = s;
+			normalIndex = i;
+		}
+	}
+	if ( separation.v > radius + B2G_SPECULATIVE )
+		return;
+	int i1 = normalIndex;
+	int i2 = i1 + 1 < a.count ? i1 + 1 : 0;
+	b2gVec v1 = a.v[i1], v2 = a.v[i2];
+	Dual<N> u1 = ddot( dsub( c, dvc<N>( v1 ) ), dvc<N>( gsub( v2, v1 ) ) );
+	Dual<N> u2 = ddot( dsub( c, dvc<N>( v2 ) ), dvc<N>( gsub( v1, v2 ) ) );
+	if ( ( u1.v < 0.0f && separation.v > FLT_EPSILON ) || ( u2.v < 0.0f && separation.v > FLT_EPSILON ) )
+	{
+		/* vertex region: the first of the two tests that holds picks the vertex */
+		b2gVec v = u1.v < 0.0f ? v1 : v2;
+		Dual<N> len;
+		DVec<N> d = dsub( c, dvc<N>( v ) );
+		DVec<N> normal = dlen_normalize( len, d );
+		Dual<N> sep = ddot( d, normal );
+		if ( sep.v > radius + B2G_SPECULATIVE )
+			return;
+		DVec<N> cA = dmuladd_f( dvc<N>( v ), rA, normal );
+		DVec<N> cB = dmulsub_f( c, rB, normal );
+		done_point( m, xfA, xfB, normal, dlerp_f( cA, cB, 0.5f ), ddot( dsub( cB, cA ), normal ) );
+		return;
+	}
+	DVec<N> normal = dvc<N>( a.n[normalIndex] );
+	DVec<N> cA = dmuladd( c, dc<N>( rA ) - ddot( dsub( c, dvc<N>( v1 ) ), normal ), normal );
+	DVec<N> cB = dmulsub_f( c, rB, normal );
+	done_point( m, xfA, xfB, normal, dlerp_f( cA, cB, 0.5f ), separation - radius );
+}

@@ -115,7 +115,8 @@ static __device__ __forceinline__ void apply_body_op( const b2gDevWorld& W, int 
 		float threshold = st[2 * b].w;
 		st[2 * b] = make_float4( 0.0f, 0.0f, 0.0f, threshold );
 		st[2 * b + 1] = make_float4( 0.0f, 0.0f, 1.0f, 0.0f );
-		W.sleepTime[b] = 0.0f;
+		if ( W.sleepTime != nullptr )
+			W.sleepTime[b] = 0.0f;
 		W.bodyInfo[b] |= B2G_B_AWAKE;
 	}
 	else
@@ -565,20 +566,21 @@ static __device__ void finalize_body( const b2gDevWorld& W, int i, const b2gStep
 
 	bool isFast = false;
 	float sleepThreshold = s0.w;
-	float sleepTime = W.sleepTime[b];
+	float sleepTime = 0.0f;
 	if ( sc.enableSleep == 0 || ( info & B2G_B_SLEEP_OK ) == 0 || sleepVelocity > sleepThreshold )
 	{
-		sleepTime = 0.0f;
 		if ( ( info & B2G_B_TYPE_MASK ) == 2 && sc.enableContinuous && maxVelocity * sc.dt > 0.5f * minExtent )
 			isFast = true;
 	}
-	else
+	else if ( W.sleepTime != nullptr )
 	{
-		sleepTime += sc.dt;
+		sleepTime = W.sleepTime[b] + sc.dt;
 	}
-	W.sleepTime[b] = sleepTime;
-	/* a body past the sleep time no longer keeps its island awake: the host learns of
-	 * it and decides the island's sleep (reference src/solver.c:281-298) */
+	/* a world that never stepped with sleep on keeps no timers; elsewhere a body past the
+	 * sleep time no longer keeps its island awake: the host learns of it and decides the
+	 * island's sleep (reference src/solver.c:281-298) */
+	if ( W.sleepTime != nullptr )
+		W.sleepTime[b] = sleepTime;
 	if ( sleepTime >= B2G_TIME_TO_SLEEP )
 	{
 		int slot = atomicAdd( W.counters + 3, 1 );

@@ -232,8 +232,9 @@ typedef struct b2gDevWorld
 	void* force;   /* float4: force.x force.y torque gravityScale */
 	void* extent;  /* float4: linearDamping angularDamping minExtent maxExtent */
 	int* bodyInfo;
-	float* sleepTime; /* seconds below the sleep velocity, by body id */
+	float* sleepTime; /* seconds below the sleep velocity, by body id (null until the world steps with sleep on) */
 	int* bodyOps;	  /* staged body operations ((bodyId << 2) | B2G_BODY_*), one per body at most */
+	int bodyOpsCap;
 	int* awake;		 /* awake body ids in solver order */
 	int* shapeRange; /* 2 per body: start, count into shapeList */
 	int* shapeList;

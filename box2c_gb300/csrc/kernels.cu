@@ -189,6 +189,9 @@ extern "C" int b2gd_body_ops( b2gDevWorld* w, const int* ops, int count )
 	if ( count <= 0 )
 		return 0;
 	cudaStream_t s = (cudaStream_t)w->stream;
+	int e = b2gd_reserve_body_ops( w, count );
+	if ( e )
+		return e;
 	cudaMemcpyAsync( w->bodyOps, ops, sizeof( int ) * (size_t)count, cudaMemcpyHostToDevice, s );
 	w->h2dBytes += (long long)( sizeof( int ) * (size_t)count );
 	k_body_ops<<<blocks_for( count ), BLOCK, 0, s>>>( *w, w->bodyOps, count );

@@ -219,6 +219,11 @@ b2WorldId b2s_tumbler( int count, uint64_t seed, int variant )
 
 b2WorldId b2s_drop_boxes( int count, const float* heights, const float* vx, const float* vy, float friction )
 {
+	return b2s_drop_shapes( count, heights, vx, vy, friction, NULL );
+}
+
+b2WorldId b2s_drop_shapes( int count, const float* heights, const float* vx, const float* vy, float friction, const int* kinds )
+{
 	b2WorldDef wd = b2s_world_def();
 	b2WorldId worldId = b2CreateWorld( &wd );
 	if ( B2_IS_NULL( worldId ) )
@@ -232,12 +237,27 @@ b2WorldId b2s_drop_boxes( int count, const float* heights, const float* vx, cons
 	sd.density = 1.0f;
 	sd.friction = friction;
 	b2Polygon box = b2MakeSquare( 0.5f );
+	b2Circle circle = { { 0.0f, 0.0f }, 0.5f };
+	b2Capsule capsule = { { -0.3f, 0.0f }, { 0.3f, 0.0f }, 0.25f };
 	for ( int k = 0; k < count; ++k )
 	{
-		bd.position = ( b2Vec2 ){ 1.5f * k, heights[k] };
+		int kind = kinds != NULL ? kinds[k] : 0;
+		/* a plank spans the whole row, under the bodies that follow it */
+		float x = kind == 3 ? 0.75f * (float)( count - 1 ) : 1.5f * (float)k;
+		bd.position = ( b2Vec2 ){ x, heights[k] };
 		bd.linearVelocity = ( b2Vec2 ){ vx[k], vy[k] };
 		b2BodyId bodyId = b2CreateBody( worldId, &bd );
-		b2CreatePolygonShape( bodyId, &sd, &box );
+		if ( kind == 1 )
+			b2CreateCircleShape( bodyId, &sd, &circle );
+		else if ( kind == 2 )
+			b2CreateCapsuleShape( bodyId, &sd, &capsule );
+		else if ( kind == 3 )
+		{
+			b2Polygon plank = b2MakeBox( 0.75f * (float)count, 0.2f );
+			b2CreatePolygonShape( bodyId, &sd, &plank );
+		}
+		else
+			b2CreatePolygonShape( bodyId, &sd, &box );
 	}
 	return worldId;
 }

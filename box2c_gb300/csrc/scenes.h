@@ -54,6 +54,11 @@ b2WorldId b2s_tumbler( int count, uint64_t seed, int variant );
 /* `count` boxes of half-extent 0.5 at x = 1.5 k, y = heights[k], initial velocity
  * (vx[k], vy[k]), on the pyramid ground; every shape uses `friction`. */
 b2WorldId b2s_drop_boxes( int count, const float* heights, const float* vx, const float* vy, float friction );
+/* The same with body k's shape chosen by kinds[k]: 0 a unit box, 1 a circle of radius
+ * 0.5, 2 a capsule (0.6 long, radius 0.25), 3 a plank 0.4 thick spanning the row of
+ * bodies (centred under it; with more than eleven bodies on it, its contacts overflow
+ * the graph colours); kinds null means boxes. */
+b2WorldId b2s_drop_shapes( int count, const float* heights, const float* vx, const float* vy, float friction, const int* kinds );
 
 /* Reference benchmark/joint_grid.c: an n x n grid of circles (radius 0.4, filtered so
  * that no two touch) with revolute joints to the neighbours above and to the left; the

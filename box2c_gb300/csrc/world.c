@@ -273,7 +273,7 @@ void gworld_flush( gWorld* w )
 	 * reflects them */
 	e |= gbody_flush_ops( w );
 	if ( w->enableSleep )
-		e |= b2gd_reserve_sleepy( &w->dev, &w->io );
+		e |= b2gd_reserve_sleep( &w->dev, &w->io );
 	if ( w->bodiesDirty )
 	{
 		e |= b2gd_upload_bodies( &w->dev, w->hState, w->hXf, w->hCenters, w->hPrev, w->hMass, w->hForce, w->hExtent, w->hInfo, nb );
@@ -689,9 +689,9 @@ b2BodyId b2CreateBody( b2WorldId worldId, const b2BodyDef* def )
 		info |= B2G_B_SLEEP_OK;
 	w->hInfo[id] = info;
 	w->bodiesDirty = true;
-	/* a new body's sleep timer starts at zero; the upload that follows the operation
-	 * restores the definition's velocity */
-	if ( b->setIndex != G_SET_STATIC )
+	/* a new body's sleep timer starts at zero (a world without timers yet gets them
+	 * zeroed); the upload that follows the operation restores the definition's velocity */
+	if ( b->setIndex != G_SET_STATIC && w->dev.sleepTime != NULL )
 		gbody_stage_new( w, id, b->setIndex == G_SET_AWAKE ? B2G_BODY_WAKE : B2G_BODY_SLEEP );
 	b2BodyId bid = { id + 1, (uint16_t)w->slot, b->revision };
 	return bid;
