@@ -38,8 +38,11 @@
 #define B2G_BATCH_HALVES 2
 #define SM_SHARED_BYTES ( 228u * 1024u ) /* shared memory of one SM */
 /* dynamic shared memory one solver CTA may take: the 227 KB opt-in limit covers the
- * kernel's static shared memory too (up to 1.4 KB), so leave room for it */
-#define CTA_SHARED_MAX ( 222u * 1024u )
+ * kernel's static shared memory too (the groups' items, up to 12.3 KB at 512 threads),
+ * so leave room for it */
+#define CTA_SHARED_MAX ( 214u * 1024u )
+/* static shared memory of a solver CTA of T threads, with the 1 KB the system reserves */
+#define SOLVE_STATIC_BYTES( T ) ( (size_t)( ( T ) / 32 ) * sizeof( b2gBatchItem ) + 1024u + 64u )
 
 /* One half of a batched step's worlds: its own graphs, prefix sums, packs, queue and
  * timing events, so that the host phases of one half overlap the other's device work. */
@@ -371,7 +374,9 @@ __global__ void __launch_bounds__( T, MINB ) k_batch_solve( const b2gBatchItem* 
 {
 	extern __shared__ float4 sm[];
 	__shared__ int s_next;
-	__shared__ b2gStepConst s_sc[T / 32];
+	/* each group's item in shared memory: its counts, colour offsets and array pointers
+	 * are read again after every group barrier */
+	__shared__ b2gBatchItem s_it[T / 32];
 	const int m = packs[0];
 	for ( ;; )
 	{
@@ -389,16 +394,15 @@ __global__ void __launch_bounds__( T, MINB ) k_batch_solve( const b2gBatchItem* 
 		int w = G.gi < PACK_WORLDS ? p[1 + G.gi] : -1;
 		if ( w >= 0 )
 		{
-			const b2gBatchItem& it = items[w];
-			b2gStepConst* sc = s_sc + G.gi;
-			for ( int i = G.t; i < (int)( sizeof( b2gStepConst ) / 4 ); i += G.g )
-				( (int*)sc )[i] = ( (const int*)&it.sc )[i];
+			b2gBatchItem& it = s_it[G.gi];
+			for ( int i = G.t; i < (int)( sizeof( b2gBatchItem ) / 4 ); i += G.g )
+				( (int*)&it )[i] = ( (const int*)( items + w ) )[i];
 			group_sync<T>( G );
 			float4* region = sm + ( smemFloat4 / ( T / G.g ) ) * G.gi;
 			if ( it.rowsOnChip )
-				solve_world<T, true>( it, *sc, region, G );
+				solve_world<T, true>( it, it.sc, region, G );
 			else
-				solve_world<T, false>( it, *sc, region, G );
+				solve_world<T, false>( it, it.sc, region, G );
 		}
 		__syncthreads();
 	}
@@ -650,7 +654,7 @@ extern "C" int b2gd_batch_solve( b2gBatch* b, int h, int first, int n )
 	/* shared memory per CTA: the candidate's share of the SM (less the per-CTA
 	 * reservation), or more when the largest world needs it for its bodies (rounded up
 	 * to 256 body ids so that growing worlds rarely recapture) */
-	size_t target = ( SM_SHARED_BYTES / (size_t)tc.perSM - 2048u ) / 256u * 256u;
+	size_t target = ( SM_SHARED_BYTES / (size_t)tc.perSM - SOLVE_STATIC_BYTES( tc.threads ) ) / 256u * 256u;
 	target = target < CTA_SHARED_MAX ? target : CTA_SHARED_MAX;
 	int top = 0;
 	for ( int i = first; i < first + n; ++i )
