@@ -335,8 +335,9 @@ def run_batch(g, steps, warmup, n_worlds=BATCH_WORLDS):
         "gpu_launches_per_step": st.launches,
         "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": BATCH_SOLVE_DRAM_BYTES * n / 2048,
-                     "traffic_source": "ncu dram__bytes_read+write of k_batch_solve, 2048 worlds scaled to the "
-                                       "worlds stepped (profiles/batch_solver_4096_worlds.txt)",
+                     "traffic_source": "ncu dram__bytes_read+write of k_batch_solve, 2048 worlds (a capture "
+                                       "before the per-group descriptor copy) scaled to the worlds stepped "
+                                       "(profiles/batch_solver_4096_worlds.txt)",
                      "kernel": "k_batch_solve (solver stage + finalisation, both halves)",
                      "algorithmic_bytes_per_step": int(solve_bytes), "peak_kind": peak_kind},
         "loop_world_steps_per_s": round(loop, 1), "speedup_vs_loop": round(value / loop, 1),
